@@ -1,0 +1,176 @@
+/*
+ * yastn_gb300 — C ABI of the GB300 (sm_103a) block-sparse backend for YASTN.
+ *
+ * Every entry point takes device pointers, a device-resident plan (packed int64
+ * records built by the host from YASTN's metadata tuples), element/dtype codes and
+ * a cudaStream_t passed as void*. Entry points only enqueue work on that stream;
+ * they allocate nothing (outputs and workspaces are owned by the caller) and return
+ * a status code (YB_OK on success). Plans and record layouts are documented next to
+ * each entry point; the record field indices are the YB_* constants below.
+ *
+ * Reference interfaces replaced (paths within the YASTN source tree):
+ *   transpose_and_merge  yastn/backend/backend_torch.py:588-589 (-> _backend_torch_backwards.py:338-392)
+ *   unmerge              yastn/backend/backend_torch.py:592-593 (-> _backend_torch_backwards.py:395-426)
+ *   dot                  yastn/backend/backend_torch.py:549-550 (-> _backend_torch_backwards.py:98-138)
+ *   transpose_dot_sum    yastn/backend/backend_torch.py:553-554 (-> _backend_torch_backwards.py:141-226)
+ *   svd                  yastn/backend/backend_torch.py:318-319 (-> _backend_torch_backwards.py:26-66,
+ *                        yastn/backend/linalg/torch_svd_gesdd.py:15-21, 296-428)
+ *   eigh                 yastn/backend/backend_torch.py:369-384
+ *   fix_svd_signs        yastn/backend/backend_torch.py:353-366
+ *   apply_mask           yastn/backend/backend_torch.py:576-577 (-> _backend_torch_backwards.py:251-279)
+ *   truncation_mask      yastn/tensor/linalg.py:637-735 (caller-side rule, fused here into one launch)
+ */
+#ifndef YASTN_GB300_H
+#define YASTN_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------- */
+#define YB_OK 0
+#define YB_ERR_INVALID 1      /* bad argument (sizes, null pointers, unsupported dtype) */
+#define YB_ERR_CUDA 2         /* a CUDA launch/runtime call failed; see yb_last_cuda_error */
+#define YB_ERR_NOT_CONVERGED 3 /* an iterative solver hit its sweep cap */
+#define YB_ERR_TOO_LARGE 4    /* problem exceeds a documented size limit of the kernel */
+
+/* ---- dtype codes ------------------------------------------------------------------- */
+#define YB_F64 0
+#define YB_C128 1
+
+/* Version of this ABI (major*100 + minor). */
+int yb_abi_version(void);
+/* Last CUDA error code seen by the library on this thread (0 if none). */
+int yb_last_cuda_error(void);
+
+/* ==== family (a): strided block copies ================================================
+ * One launch moves every block of a merge, unmerge or their adjoints.
+ *
+ * tasks: n_tasks records of YB_COPY_REC int64 each:
+ *   [YB_CP_SRC] src offset (units)  [YB_CP_DST] dst offset (units)
+ *   [YB_CP_NDIM] number of dims (1..YB_CP_MAXD), outermost first
+ *   [YB_CP_COUNT] number of units in the task (< 2^31)
+ *   [YB_CP_VEC] 1 if an FP64 task moves pairs of elements as 16-byte units (offsets,
+ *   strides and extents of the record are then in pairs)
+ *   [YB_CP_SIZE+i] extent, [YB_CP_SSTR+i] src stride, [YB_CP_DSTR+i] dst stride (units),
+ *   [YB_CP_MAGIC+i], [YB_CP_SHIFT+i] fast-division constants of extent i
+ * items: n_items pairs (task index, first unit); each item covers up to
+ *   YB_COPY_ITEM_UNITS units of its task.
+ * unit_bytes: element size, 8 (FP64) or 16 (complex128); src/dst must be 16-byte aligned
+ *   when any task has YB_CP_VEC set.
+ * Replaces the per-block copy loops of transpose_and_merge / unmerge and their adjoints.
+ */
+#define YB_COPY_REC 48
+#define YB_CP_SRC 0
+#define YB_CP_DST 1
+#define YB_CP_NDIM 2
+#define YB_CP_COUNT 3
+#define YB_CP_VEC 4
+#define YB_CP_MAXD 8
+#define YB_CP_SIZE 8
+#define YB_CP_SSTR 16
+#define YB_CP_DSTR 24
+#define YB_CP_MAGIC 32
+#define YB_CP_SHIFT 40
+#define YB_COPY_ITEM_UNITS 8192
+int yb_block_copy(const void* src, void* dst, int unit_bytes,
+                  const int64_t* tasks, int n_tasks,
+                  const int64_t* items, int n_items, void* stream);
+
+/* ==== family (b): grouped sum-of-products GEMM ========================================
+ * For every output block o:  C_o = alpha * sum_{t in terms(o)} op(A_t) op(B_t) + beta * C_o
+ * outs: n_out records of YB_GEMM_OUT_REC int64:
+ *   [0] c offset (elements) [1] m [2] n [3] ldc [4] first term [5] end term
+ * terms: records of YB_GEMM_TERM_REC int64:
+ *   [0] a offset [1] b offset [2] k [3] a row stride [4] a col stride
+ *   [5] b row stride [6] b col stride [7] flags (bit0: conj A, bit1: conj B)
+ *   A_t[i,l] = a[a_off + i*a_rs + l*a_cs], B_t[l,j] = b[b_off + l*b_rs + j*b_cs].
+ * tiles: n_tiles records of 4 int32: (output, tile row, tile col, unused), tile = 64x64,
+ *   ordered by the host (largest K first).
+ * dtype: YB_F64 or YB_C128 (alpha, beta are real).
+ * Replaces dot (one term per output), transpose_dot_sum after the merge of its operands,
+ * and the adjoint products A_b += C_b B^H, B_b += A^H C_b (terms grouped by operand block).
+ */
+#define YB_GEMM_OUT_REC 8
+#define YB_GEMM_TERM_REC 8
+#define YB_GEMM_TILE 64
+int yb_grouped_gemm(const void* a, const void* b, void* c, int dtype,
+                    const int64_t* outs, const int64_t* terms, const int32_t* tiles, int n_tiles,
+                    double alpha, double beta, void* stream);
+
+/* ==== family (c): batched one-sided Jacobi SVD / symmetric eigendecomposition ==========
+ * blocks: n_blocks records of YB_SVD_REC int64:
+ *   [0] a offset [1] m [2] n [3] U offset [4] S offset [5] Vh offset
+ *   [6] workspace X offset [7] workspace W offset [8] first pair item
+ *   [9] k=min(m,n) [10] L=max(m,n) [11] N = k rounded up to even [12] 1 if m > n
+ * pair_items: int32 pairs (block, pair index 0..N/2-1) over all blocks.
+ * Workspace (FP64): X holds k vectors of length L, W the k x k accumulated rotations.
+ * counters: int64[2*n_blocks] (rotations in the last completed sweep | in this sweep).
+ * Sequence: yb_svd_init, then yb_svd_sweep until counters[0:n_blocks] are all zero
+ * (the host reads them between sweeps; its sweep cap maps to YB_ERR_NOT_CONVERGED),
+ * then yb_svd_finalize. shift != NULL (eigh): per-block shifts c_b = ||A_b||_F + 1 are
+ * computed and A_b + c_b I is decomposed (positive definite, so its SVD is its
+ * eigendecomposition); finalize mode 1 writes eigenvalues ascending, mode 2 by
+ * descending magnitude, both with eigenvectors as columns of U; mode 0 is the SVD.
+ * Replaces svd (backend_torch.py:318-319, torch_svd_gesdd.py:15-21) and eigh
+ * (backend_torch.py:369-384, torch_eig_sym.py:14-32) for FP64 blocks.
+ */
+#define YB_SVD_REC 16
+int yb_svd_init(const void* a, void* work, const int64_t* blocks, int n_blocks, int dtype,
+                int64_t* counters, double* shift, void* stream);
+int yb_svd_sweep(void* work, const int64_t* blocks, int n_blocks, const int32_t* pair_items,
+                 int n_pair_items, int max_rounds, int dtype, double tol_scale,
+                 int64_t* counters, void* stream);
+int yb_svd_finalize(const void* work, void* U, double* S, void* Vh, const int64_t* blocks,
+                    int n_blocks, int dtype, int max_k, int mode, const double* shift, void* stream);
+
+/* SVD adjoint core (torch_svd_gesdd.py:296-428): per block record YB_ADJ_REC int64:
+ *   [0] dA offset [1] m [2] n [3] U/gU offset [4] S/gS offset [5] Vh/gVh offset
+ *   [6] offset of the k x k matrices P, Q, K [7] offset of TR [8] k
+ *   [9] kind: 0 square, 1 wide (n > m), 2 tall (m > n)
+ * With P = U^H gU and Q = Vh gVh^H given, writes K and initialises TR; the host
+ * completes dA with grouped GEMMs (see yb_adjoint.cu). gS may be NULL. */
+#define YB_ADJ_REC 16
+int yb_svd_adjoint_core(const void* P, const void* Q, const double* S, const double* gS, void* K,
+                        const void* gU, const void* gVh, void* TR, const int64_t* blocks,
+                        int n_blocks, int dtype, void* stream);
+
+/* ==== masks / gauge ================================================================== */
+/* Gather along one axis: out[sln].reshape(pre, Dn_ax, post)[:, i, :] =
+ *   A[sla].reshape(pre, Da_ax, post)[:, idx[idx_off + i], :]
+ * recs: records of YB_MASK_REC int64: [0] sln start [1] sla start [2] pre [3] Da_ax
+ *   [4] Dn_ax [5] post [6] idx offset [7] unused (offsets in units).
+ * items: n_items pairs (record, first output unit), each covering up to
+ *   YB_COPY_ITEM_UNITS units. scatter != 0 runs the adjoint: A positions are written
+ *   from out (the caller zero-fills the destination first).
+ * Replaces apply_mask (backend_torch.py:576-577) and kernel_apply_mask.backward. */
+#define YB_MASK_REC 8
+int yb_mask_gather(const void* A, void* out, int unit_bytes, const int64_t* recs, const int64_t* items,
+                   int n_items, const int64_t* idx, int scatter, void* stream);
+
+/* fix_svd_signs (backend_np.py:447-458): per block record YB_SVD_REC (uses [1] m, [2] n,
+ * [3] U offset, [4] S offset, [5] Vh offset, [9] k). U[:, c] *= conj(phase_c),
+ * Vh[c, :] *= phase_c, where phase_c = U[r, c]/|U[r, c]| at the first row r maximising
+ * int64(|U[r, c]| * 2^40). Writes Uout/Vout (may alias the inputs).
+ * apply_given = 0: phases are computed and stored in `phases` (dtype, indexed like S;
+ * may be NULL). apply_given = 1: the phases are read from `phases` instead (used by
+ * the real adjoint, where the phases are the constants +-1). max_k: largest k. */
+int yb_fix_signs(const void* Uin, const void* Vin, void* Uout, void* Vout, void* phases,
+                 const int64_t* blocks, int n_blocks, int max_k, int dtype, int apply_given,
+                 void* stream);
+
+/* Fused truncation rule of yastn/tensor/linalg.py:637-735 over a flat spectrum.
+ * S: n values; blk: n_blk records of 4 int64 (start, stop, D_block (or -1 = inf), unused);
+ * tol_block: n_blk doubles; D_total < 0 means inf. Outputs mask (uint8[n]) and
+ * kept (int64[n_blk]). Single-CTA kernel: n <= YB_TRUNC_MAX. */
+#define YB_TRUNC_MAX 16384
+int yb_truncation_mask(const double* S, int64_t n, const int64_t* blk, const double* tol_block,
+                       int n_blk, double tol, int64_t D_total, int truncate_multiplets,
+                       uint8_t* mask, int64_t* kept, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* YASTN_GB300_H */

@@ -1,0 +1,484 @@
+"""Generate golden fixtures from the unmodified reference (YASTN, NumPy backend).
+
+Run in a container that has the reference source tree:
+
+    python tests/golden/make_golden.py [/path/to/yastn/source]
+
+It imports YASTN from that path, wraps the hot-path functions of the NumPy backend
+(``yastn/backend/backend_np.py``) with a recorder, runs scenarios modelled on the
+reference's own tests (``tests/tensor/test_tensordot.py``, ``test_svd.py``,
+``test_fuse_hard.py``) and the benchmark workload, and writes:
+
+* ``<scenario>.json`` — the ordered list of backend calls with their metadata
+  arguments (nested tuples of ints stored as lists) and the names of their array
+  arguments / results;
+* ``<scenario>.npz`` — the arrays (inputs and reference outputs).
+
+Adjoint fixtures come from the reference's torch backend on CPU
+(``yastn/backend/_backend_torch_backwards.py``). Large arrays of the benchmark
+workload are not stored; the workload's data is regenerated from its seed and the
+fixture keeps only checksums, the full singular-value vector and the truncation
+result.
+
+Nothing at run time (tests, bench, smoke) reads the reference tree; only this script does.
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+sys.path.insert(0, REF)
+
+import yastn  # noqa: E402
+import yastn.backend.backend_np as bnp  # noqa: E402
+
+HOT = ['transpose_and_merge', 'unmerge', 'dot', 'transpose_dot_sum', 'svd', 'eigh',
+       'fix_svd_signs', 'apply_mask', 'embed_mask']
+
+
+class Recorder:
+    """Wraps hot-path functions of a backend module and records every call."""
+
+    def __init__(self, module, store_arrays=True, big=None):
+        self.module = module
+        self.calls = []
+        self.arrays = {}
+        self.seen = {}
+        self.store_arrays = store_arrays
+        self.big = big  # arrays with more elements than this are summarised
+        self.orig = {nm: getattr(module, nm) for nm in HOT}
+        for nm in HOT:
+            setattr(module, nm, self._wrap(nm, self.orig[nm]))
+
+    def restore(self):
+        for nm, f in self.orig.items():
+            setattr(self.module, nm, f)
+
+    def _put(self, arr):
+        import hashlib
+        digest = hashlib.sha1(np.ascontiguousarray(arr).tobytes() + str(arr.dtype).encode()).hexdigest()
+        if digest in self.seen:  # identical array already stored: reuse its key
+            return dict(self.seen[digest])
+        key = f"a{len(self.arrays)}"
+        arr = np.array(arr, copy=True)
+        self.seen[digest] = self._put_new(key, arr)
+        return dict(self.seen[digest])
+
+    def _put_new(self, key, arr):
+        if self.big is not None and arr.size > self.big:
+            self.arrays[key] = None
+            return {'__array__': key, 'shape': list(arr.shape), 'dtype': str(arr.dtype),
+                    'checksum': checksum(arr)}
+        self.arrays[key] = arr
+        return {'__array__': key}
+
+    def _enc(self, x):
+        if isinstance(x, np.ndarray):
+            return self._put(x)
+        if isinstance(x, dict):
+            return {'__mask__': [[list(k), self._enc(np.asarray(v))] for k, v in x.items()]}
+        if isinstance(x, (tuple, list)):
+            return [self._enc(y) for y in x]
+        if isinstance(x, (np.integer,)):
+            return int(x)
+        if isinstance(x, (np.floating,)):
+            return float(x)
+        return x
+
+    def _wrap(self, nm, f):
+        def wrapped(*args, **kwargs):
+            enc_args = [self._enc(a) for a in args]
+            out = f(*args, **kwargs)
+            outs = out if isinstance(out, tuple) else (out,)
+            enc_out = [self._enc(o) for o in outs]
+            self.calls.append({'fn': nm, 'args': enc_args, 'kwargs': {k: self._enc(v) for k, v in kwargs.items()},
+                               'out': enc_out})
+            return out
+        return wrapped
+
+
+def checksum(arr):
+    a = np.asarray(arr).ravel()
+    if np.iscomplexobj(a):
+        parts = [a.real, a.imag]
+    else:
+        parts = [a.astype(np.float64)]
+    res = {'n': int(a.size)}
+    for i, p in enumerate(parts):
+        res[f'sum{i}'] = float(np.sum(p))
+        res[f'abs{i}'] = float(np.sum(np.abs(p)))
+        res[f'sq{i}'] = float(np.sum(p * p))
+        res[f'head{i}'] = [float(x) for x in p[:8]]
+        res[f'tail{i}'] = [float(x) for x in p[-8:]]
+    return res
+
+
+def save(name, rec, extra=None):
+    payload = {'scenario': name, 'calls': rec.calls}
+    if extra:
+        payload.update(extra)
+    with open(os.path.join(HERE, name + '.json'), 'w') as f:
+        json.dump(payload, f, separators=(',', ':'))
+    arrays = {k: v for k, v in rec.arrays.items() if v is not None}
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **arrays)
+    print(f"{name}: {len(rec.calls)} calls, {sum(v.size for v in arrays.values())} stored elements")
+
+
+def leg_dims(ts, w, Dtot):
+    """Sector dims proportional to w(t), rounded to sum to Dtot (largest-remainder repair)."""
+    p = np.array([w(t) for t in ts]); p = p / p.sum()
+    D = np.round(p * Dtot).astype(int)
+    while D.sum() > Dtot:
+        D[np.argmax(D - p * Dtot)] -= 1
+    while D.sum() < Dtot:
+        D[np.argmin(D - p * Dtot)] += 1
+    return tuple(int(x) for x in D)
+
+
+# ----------------------------------------------------------------------------- scenarios
+
+def scen_tensordot(policy):
+    cfg = yastn.make_config(sym='U1', backend='np', tensordot_policy=policy)
+    cfgz = yastn.make_config(sym=yastn.sym.sym_Z2xU1, backend='np', tensordot_policy=policy)
+    cfgd = yastn.make_config(sym='none', backend='np', tensordot_policy=policy)
+    bnp.random_seed(11)
+    a = yastn.rand(config=cfg, s=(-1, 1, 1, -1), t=((-1, 1, 2),) * 4,
+                   D=((1, 2, 3), (4, 2, 3), (3, 1, 2), (5, 4, 2)))
+    b = yastn.rand(config=cfg, s=(1, -1, 1), t=((-1, 1, 2), (-1, 1, 2), (-1, 0, 1)),
+                   D=((1, 2, 3), (4, 2, 3), (5, 3, 4)))
+    rec = Recorder(bnp)
+    yastn.tensordot(a, b, axes=((0, 1), (0, 1)))
+    yastn.tensordot(a, b, axes=((1, 3), (1, 2)))
+    yastn.tensordot(a, b, axes=((1, 0), (1, 0)), conj=(1, 1))
+    yastn.tensordot(b, a, axes=((1, 0), (1, 0)))
+    t1 = [(0, -1), (0, 1), (1, -1), (1, 1)]
+    t2 = [(0, 0), (0, 2), (1, 0), (1, 2)]
+    for dtype in ('float64', 'complex128'):
+        az = yastn.rand(config=cfgz, s=(-1, 1, 1, -1), t=(t1, t1, t1, t1),
+                        D=((1, 2, 2, 4), (5, 4, 3, 2), (3, 2, 4, 1), (2, 3, 1, 2)), dtype=dtype)
+        bz = yastn.rand(config=cfgz, s=(1, -1, 1), t=(t1, t1, t2),
+                        D=((1, 2, 2, 4), (5, 4, 3, 2), (3, 2, 4, 1)), dtype=dtype)
+        yastn.tensordot(az, bz, axes=((0, 1), (0, 1)))
+        yastn.tensordot(bz, az, axes=((1, 0), (1, 0)))
+    ad = yastn.rand(config=cfgd, s=(-1, 1, 1, -1), D=(2, 3, 4, 5), dtype='complex128')
+    bd = yastn.rand(config=cfgd, s=(1, -1, 1), D=(2, 3, 5), dtype='complex128')
+    yastn.tensordot(ad, bd, axes=((0, 3), (0, 2)))
+    # hard-fused legs: merges of blocks whose legs carry a fusion history
+    D1, D2 = (1, 3, 2), (3, 3, 4)
+    tt1, tt2 = (-1, 0, 1), (-2, 0, 2)
+    ah = yastn.rand(config=cfg, s=(-1, 1, 1, -1), t=(tt1, tt1, tt2, tt2), D=(D1, D2, D2, D1))
+    bh = yastn.rand(config=cfg, s=(-1, -1, 1, 1), t=(tt1, tt2, tt1, tt2), D=(D2, D1, D1, D1))
+    ahf = ah.fuse_legs(axes=(0, (1, 3), 2), mode='hard')
+    bhf = bh.fuse_legs(axes=((0, 3), 1, 2), mode='hard')
+    yastn.tensordot(ahf, bhf, axes=((1,), (0,)))
+    rec.restore()
+    save(f'tensordot_{policy}', rec)
+
+
+def scen_svd():
+    cfg = yastn.make_config(sym='U1', backend='np')
+    bnp.random_seed(12)
+    legs = [yastn.Leg(cfg, s=-1, t=(-1, 0, 1), D=(2, 3, 2)),
+            yastn.Leg(cfg, s=-1, t=(-2, 0, 2), D=(3, 2, 4)),
+            yastn.Leg(cfg, s=1, t=(-2, -1, 0, 1, 2), D=(3, 2, 4, 3, 2)),
+            yastn.Leg(cfg, s=1, t=(0, 1), D=(2, 3))]
+    rec = Recorder(bnp)
+    for dtype in ('float64', 'complex128'):
+        a = yastn.rand(config=cfg, n=1, legs=legs, dtype=dtype)
+        yastn.linalg.svd(a, axes=((3, 1), (2, 0)), sU=-1)
+        yastn.linalg.svd(a, axes=((3, 1), (2, 0)), sU=1, nU=False, fix_signs=True)
+        yastn.linalg.svd_with_truncation(a, axes=((0, 1), (2, 3)), D_total=20, tol=1e-3)
+    # tall, wide and square blocks in one tensor
+    a = yastn.rand(config=cfg, s=(-1, 1), t=((-1, 0, 1), (-1, 0, 1)), D=((30, 7, 5), (4, 7, 40)))
+    yastn.linalg.svd(a, axes=(0, 1), fix_signs=True)
+    rec.restore()
+    save('svd', rec)
+
+
+def scen_fix_signs():
+    """test_svd.py:159-186: phases of U columns, complex blocks."""
+    cfg = yastn.make_config(sym='U1', backend='np')
+    U = yastn.Tensor(config=cfg, s=(-1, 1), dtype='complex128')
+    S = yastn.Tensor(config=cfg, s=(-1, 1), isdiag=True)
+    V = yastn.Tensor(config=cfg, s=(-1, 1), dtype='complex128')
+    is2 = 0.5 ** 0.5
+    U.set_block(ts=(0, 0), Ds=(3, 2), val=[[-is2, -1 / 2], [is2, -1 / 2], [0, is2 * 1j]])
+    U.set_block(ts=(1, 1), Ds=(2, 2), val=[[0, 1j], [1, 0]])
+    S.set_block(ts=(0, 0), Ds=(2, 2), val=[0.5, 0.2])
+    S.set_block(ts=(1, 1), Ds=(2, 2), val=[0.3, 0.2])
+    V.set_block(ts=(0, 0), Ds=(2, 2), val=[[0, 1], [1, 0]])
+    V.set_block(ts=(1, 1), Ds=(2, 3), val=[[1, 0, 0], [0, 0.8j, 0.6]])
+    USV = U @ S @ V
+    rec = Recorder(bnp)
+    nU, nS, nV = yastn.svd(USV, axis=(0, 1), fix_signs=True)
+    rec.restore()
+    extra = {'Ufixed': {'(0,0)': [[is2, 0, 0, 0.5], [-is2, 0, 0, 0.5], [0, 0, is2, 0]],
+                        '(1,1)': [[0, 0, 1, 0], [1, 0, 0, 0]]}}
+    save('fix_signs', rec, extra)
+
+
+def scen_truncation():
+    """Spectra and options of test_svd.py:189-266 and :344-388 with the reference's masks."""
+    out = []
+    cfg = yastn.make_config(sym='U1', backend='np')
+    bnp.random_seed(0)
+    legs = [yastn.Leg(cfg, s=1, t=(0, 1), D=(5, 6)),
+            yastn.Leg(cfg, s=1, t=(-1, 0), D=(5, 6)),
+            yastn.Leg(cfg, s=-1, t=(-1, 0, 1), D=(2, 3, 4)),
+            yastn.Leg(cfg, s=-1, t=(-1, 0, 1), D=(2, 3, 4))]
+    a = yastn.rand(config=cfg, n=1, legs=legs)
+    U, S, V = yastn.linalg.svd(a, axes=((0, 1), (2, 3)), sU=-1)
+    S.set_block(ts=(-2, -2), Ds=4, val=[2 ** (-ii - 6) for ii in range(4)])
+    S.set_block(ts=(-1, -1), Ds=12, val=[2 ** (-ii - 2) for ii in range(12)])
+    S.set_block(ts=(0, 0), Ds=25, val=[2 ** (-ii - 1) for ii in range(25)])
+    opts_list = [{'tol': 0.01, 'D_block': 100, 'D_total': 12},
+                 {'tol': 0.02, 'D_block': 5, 'D_total': 100},
+                 {'tol': 0, 'tol_block': 0.2, 'D_total': 100},
+                 {'D_block': {(0,): 2, (-1,): 3}, 'tol_block': {(0,): 0.6, (-1,): 0.1}},
+                 {'D_total': 10, 'truncate_multiplets': True},
+                 {'D_total': 0}]
+    for opts in opts_list:
+        m = yastn.linalg.truncation_mask(S, **opts)
+        out.append(_trunc_case(S, m, opts))
+    # multiplets
+    bnp.random_seed(0)
+    legs = [yastn.Leg(cfg, s=1, t=(-1, 0, 1), D=(2, 3, 2)),
+            yastn.Leg(cfg, s=1, t=(-1, 0, 1), D=(3, 4, 3)),
+            yastn.Leg(cfg, s=-1, t=(-1, 0, 1), D=(4, 5, 4)),
+            yastn.Leg(cfg, s=-1, t=(-1, 0, 1), D=(5, 6, 5))]
+    a = yastn.rand(config=cfg, n=0, legs=legs)
+    U, S, V = yastn.linalg.svd(a, axes=((0, 1), (2, 3)))
+    v00 = [1, 1, 0.1001, 0.1000, 0.1000, 0.0999, 0.001001, 0.001000] + [0] * 16
+    S.set_block(ts=(0, 0), Ds=24, val=v00)
+    v11 = [1, 1, 0.1001, 0.1000, 0.0999, 0.001000, 0.000999] + [0] * 10
+    S.set_block(ts=(1, 1), Ds=17, val=v11)
+    S.set_block(ts=(-1, -1), Ds=17, val=v11)
+    v22 = [1, 1, 0.1001, 0.1000, 0.001000, 0]
+    S.set_block(ts=(2, 2), Ds=6, val=v22)
+    S.set_block(ts=(-2, -2), Ds=6, val=v22)
+    for opts in [{'tol': 0.0001, 'D_block': 7, 'D_total': 30},
+                 {'tol': 0.001, 'truncate_multiplets': True},
+                 {'D_total': 17, 'truncate_multiplets': True}]:
+        m = yastn.linalg.truncation_mask(S, **opts)
+        out.append(_trunc_case(S, m, opts))
+    # random spectra with many blocks
+    rng = np.random.default_rng(5)
+    for trial in range(4):
+        nb = 9
+        Ds = rng.integers(1, 30, size=nb)
+        t = [(int(q),) for q in range(-4, 5)]
+        Sx = yastn.Tensor(config=cfg, s=(-1, 1), isdiag=True)
+        for tq, d in zip(t, Ds):
+            vals = np.sort(np.abs(rng.normal(size=d)) * 10 ** rng.uniform(-6, 0))[::-1]
+            Sx.set_block(ts=tq + tq, Ds=int(d), val=vals.tolist())
+        opts = [{'tol': 1e-3, 'D_total': 40}, {'D_block': 6, 'D_total': 35},
+                {'tol_block': 0.05, 'tol': 1e-4}, {'D_total': 25, 'truncate_multiplets': True}][trial]
+        m = yastn.linalg.truncation_mask(Sx, **opts)
+        out.append(_trunc_case(Sx, m, opts))
+    with open(os.path.join(HERE, 'truncation.json'), 'w') as f:
+        json.dump({'scenario': 'truncation', 'cases': out}, f, separators=(',', ':'))
+    print(f"truncation: {len(out)} cases")
+
+
+def _trunc_case(S, mask, opts):
+    def enc(v):
+        if isinstance(v, dict):
+            return {'__dict__': [[list(k), vv] for k, vv in v.items()]}
+        return v
+    return {'S': [float(x) for x in S._data], 'slices': [list(sl.slcs[0]) for sl in S.slices],
+            'charges': [list(t[:1]) for t in S.struct.t],
+            'opts': {k: enc(v) for k, v in opts.items()},
+            'mask': [bool(x) for x in mask._data]}
+
+
+def scen_eigh():
+    cfg = yastn.make_config(sym='U1', backend='np')
+    bnp.random_seed(13)
+    rec = Recorder(bnp)
+    for dtype in ('float64', 'complex128'):
+        a = yastn.rand(config=cfg, s=(1, -1), t=((-1, 0, 1), (-1, 0, 1)), D=((3, 9, 5), (3, 9, 5)), dtype=dtype)
+        a = a + a.transpose(axes=(1, 0)).conj()
+        yastn.linalg.eigh(a, axes=(0, 1))
+    rec.restore()
+    save('eigh', rec)
+
+
+def scen_adjoints():
+    """Reference adjoints from the torch backend on CPU (_backend_torch_backwards.py)."""
+    import torch
+    import yastn.backend.backend_torch as bt
+    from yastn.backend._backend_torch_backwards import (kernel_svd, kernel_dot,
+                                                         kernel_transpose_and_merge, kernel_unmerge,
+                                                         kernel_apply_mask)
+    arrays, calls = {}, []
+
+    def put(x):
+        key = f"a{len(arrays)}"
+        arrays[key] = x.detach().resolve_conj().cpu().numpy().copy() if isinstance(x, torch.Tensor) else np.asarray(x)
+        return key
+
+    g = torch.Generator().manual_seed(7)
+    # SVD adjoint on blocks: square, tall, wide; real and complex
+    for dtype in (torch.float64, torch.complex128):
+        shapes = [(6, 6), (9, 4), (3, 8)]
+        meta, off, offU, offS, offV = [], 0, 0, 0, 0
+        for (m, n) in shapes:
+            k = min(m, n)
+            meta.append(((off, off + m * n), (m, n), (offU, offU + m * k), (m, k), (offS, offS + k),
+                         (offV, offV + k * n), (k, n)))
+            off += m * n; offU += m * k; offS += k; offV += k * n
+        data = torch.randn(off, dtype=dtype, generator=g)
+        U, S, V = kernel_svd.apply(data, tuple(meta), (offU, offS, offV))
+        gU = torch.randn(offU, dtype=dtype, generator=g)
+        gS = torch.randn(offS, dtype=torch.float64, generator=g)
+        gV = torch.randn(offV, dtype=dtype, generator=g)
+        d = data.clone().requires_grad_(True)
+        U2, S2, V2 = kernel_svd.apply(d, tuple(meta), (offU, offS, offV))
+        # the cotangents handed to kernel_svd.backward are exactly (gU, gS, gV)
+        (grad,) = torch.autograd.grad((U2, S2, V2), (d,), grad_outputs=(gU, gS, gV))
+        calls.append({'fn': 'svd_backward', 'meta': meta, 'data': put(data), 'U': put(U), 'S': put(S),
+                      'V': put(V), 'gU': put(gU), 'gS': put(gS), 'gV': put(gV), 'grad': put(grad)})
+    # dot adjoint with shared operand blocks (fuse_contracted style)
+    cfg = yastn.make_config(sym='U1', backend='np', tensordot_policy='fuse_contracted')
+    bnp.random_seed(14)
+    a = yastn.rand(config=cfg, s=(-1, 1, 1), t=((-1, 0, 1),) * 3, D=((2, 3, 2), (4, 5, 4), (3, 3, 2)))
+    b = yastn.rand(config=cfg, s=(-1, 1, 1), t=((-1, 0, 1),) * 3, D=((3, 3, 2), (2, 6, 2), (5, 1, 4)))
+    rec = Recorder(bnp)
+    yastn.tensordot(a, b, axes=((2,), (0,)))
+    rec.restore()
+    dcall = [c for c in rec.calls if c['fn'] == 'dot'][0]
+    A = torch.from_numpy(rec.arrays[dcall['args'][0]['__array__']]).requires_grad_(True)
+    B = torch.from_numpy(rec.arrays[dcall['args'][1]['__array__']]).requires_grad_(True)
+    meta_dot = _tup(dcall['args'][2])
+    C = kernel_dot.apply(A, B, meta_dot, dcall['args'][3])
+    Cb = torch.randn(C.shape, dtype=C.dtype, generator=g)
+    C.backward(Cb)
+    calls.append({'fn': 'dot_backward', 'meta': dcall['args'][2], 'A': put(A), 'B': put(B), 'Cb': put(Cb),
+                  'Ab': put(A.grad), 'Bb': put(B.grad)})
+    # merge / unmerge adjoints with a permutation
+    cfg = yastn.make_config(sym='U1', backend='np', tensordot_policy='fuse_to_matrix')
+    bnp.random_seed(15)
+    a = yastn.rand(config=cfg, s=(-1, 1, 1, -1), t=((-1, 1, 2),) * 4, D=((1, 2, 3), (2, 3, 2), (3, 2, 1), (3, 4, 1)))
+    b = yastn.rand(config=cfg, s=(1, -1, 1), t=((-1, 1, 2), (-1, 1, 2), (-1, 0, 1)), D=((1, 2, 3), (2, 3, 2), (3, 2, 4)))
+    rec = Recorder(bnp)
+    yastn.tensordot(a, b, axes=((1, 3), (1, 2)))
+    rec.restore()
+    mcall = [c for c in rec.calls if c['fn'] == 'transpose_and_merge'][0]
+    data = torch.from_numpy(rec.arrays[mcall['args'][0]['__array__']]).requires_grad_(True)
+    order, mnew, mmrg, Dsize = (_tup(x) for x in mcall['args'][1:])
+    out = kernel_transpose_and_merge.apply(data, order, mnew, mmrg, Dsize)
+    ob = torch.randn(out.shape, dtype=out.dtype, generator=g)
+    out.backward(ob)
+    calls.append({'fn': 'transpose_and_merge_backward', 'order': mcall['args'][1], 'meta_new': mcall['args'][2],
+                  'meta_mrg': mcall['args'][3], 'Dsize': Dsize, 'data': put(data), 'out_b': put(ob),
+                  'grad': put(data.grad)})
+    ucall = [c for c in rec.calls if c['fn'] == 'unmerge'][0]
+    data = torch.from_numpy(rec.arrays[ucall['args'][0]['__array__']]).requires_grad_(True)
+    meta = _tup(ucall['args'][1])
+    out = kernel_unmerge.apply(data, meta)
+    ob = torch.randn(out.shape, dtype=out.dtype, generator=g)
+    out.backward(ob)
+    calls.append({'fn': 'unmerge_backward', 'meta': ucall['args'][1], 'data': put(data), 'out_b': put(ob),
+                  'grad': put(data.grad)})
+    with open(os.path.join(HERE, 'adjoints.json'), 'w') as f:
+        json.dump({'scenario': 'adjoints', 'calls': calls}, f, separators=(',', ':'))
+    np.savez_compressed(os.path.join(HERE, 'adjoints.npz'), **arrays)
+    print(f"adjoints: {len(calls)} calls")
+
+
+def scen_svd_ill():
+    """The ill-conditioned fixture of the reference tests (test_svd.py:335-341), where
+    LAPACK gesdd can fail; records the backend calls of its truncated SVD."""
+    cfg = yastn.make_config(sym='U1', backend='np')
+    fname = os.path.join(REF, 'tests', 'tensor', 'inputs', 'ill_conditioned_svd.npy')
+    tensor_dict = np.load(fname, allow_pickle=True).item()
+    tensor = yastn.from_dict(tensor_dict, cfg)
+    rec = Recorder(bnp)
+    yastn.svd_with_truncation(tensor, axes=((0, 1), (2, 3)), D_total=12)
+    rec.restore()
+    save('svd_ill', rec)
+
+
+def scen_tds_adjoint():
+    """transpose_dot_sum adjoint from the reference torch backend (:170-226)."""
+    import torch
+    from yastn.backend._backend_torch_backwards import kernel_transpose_dot_sum
+    tr_calls = []
+    cfg = yastn.make_config(sym='U1', backend='np', tensordot_policy='no_fusion')
+    bnp.random_seed(16)
+    a = yastn.rand(config=cfg, s=(-1, 1, 1, -1), t=((-1, 1, 2),) * 4, D=((1, 2, 3), (2, 3, 2), (3, 2, 1), (3, 4, 1)))
+    b = yastn.rand(config=cfg, s=(1, -1, 1), t=((-1, 1, 2), (-1, 1, 2), (-1, 0, 1)), D=((1, 2, 3), (2, 3, 2), (3, 2, 4)))
+    rec = Recorder(bnp)
+    yastn.tensordot(a, b, axes=((1, 3), (1, 2)))
+    rec.restore()
+    c = [c for c in rec.calls if c['fn'] == 'transpose_dot_sum'][0]
+    A = torch.from_numpy(rec.arrays[c['args'][0]['__array__']]).requires_grad_(True)
+    B = torch.from_numpy(rec.arrays[c['args'][1]['__array__']]).requires_grad_(True)
+    rest = [_tup(x) for x in c['args'][2:]]
+    C = kernel_transpose_dot_sum.apply(A, B, *rest)
+    g = torch.Generator().manual_seed(8)
+    Cb = torch.randn(C.shape, dtype=C.dtype, generator=g)
+    C.backward(Cb)
+    arrays = {'A': A.detach().numpy(), 'B': B.detach().numpy(), 'Cb': Cb.numpy(), 'Ab': A.grad.numpy(),
+              'Bb': B.grad.numpy()}
+    with open(os.path.join(HERE, 'tds_adjoint.json'), 'w') as f:
+        json.dump({'scenario': 'tds_adjoint', 'args': c['args'][2:]}, f, separators=(',', ':'))
+    np.savez_compressed(os.path.join(HERE, 'tds_adjoint.npz'), **arrays)
+    print("tds_adjoint: 1 call")
+
+
+def _tup(x):
+    if isinstance(x, list):
+        return tuple(_tup(y) for y in x)
+    return x
+
+
+def scen_cfg1():
+    """Benchmark workload: U(1) rank-4 D=64 tensordot (2,3)x(0,1) + SVD, D_total=64.
+
+    Sector dims follow exp(-t^2/4) over t=-3..3 rounded to 64; A then B are drawn
+    with ``rand(distribution='normal')`` after ``random_seed(0)`` (one normal vector
+    of length ``size`` per tensor, in block order).
+    """
+    cfg = yastn.make_config(sym='U1', backend='np', tensordot_policy='fuse_to_matrix')
+    bnp.random_seed(0)
+    ts = tuple(range(-3, 4))
+    Ds = leg_dims(ts, lambda t: np.exp(-t * t / 4), 64)
+    legs = [yastn.Leg(cfg, s=s, t=ts, D=Ds) for s in (1, 1, -1, -1)]
+    A = yastn.rand(cfg, legs=legs, distribution='normal')
+    B = yastn.rand(cfg, legs=legs, distribution='normal')
+    rec = Recorder(bnp, big=5000)
+    C = yastn.tensordot(A, B, axes=((2, 3), (0, 1)))
+    U, S, V = yastn.svd_with_truncation(C, axes=((0, 1), (2, 3)), D_total=64)
+    rec.restore()
+    scall = [c for c in rec.calls if c['fn'] == 'svd'][0]
+    extra = {'leg_t': list(ts), 'leg_D': list(Ds), 'signatures': [1, 1, -1, -1], 'seed': 0,
+             'A_size': int(A.size), 'B_size': int(B.size),
+             'A_struct': {'t': [list(t) for t in A.struct.t], 'D': [list(d) for d in A.struct.D]},
+             'S_kept_t': [list(t) for t in S.struct.t], 'S_kept_D': [list(d) for d in S.struct.D],
+             'S_kept': [float(x) for x in S._data], 'C_checksum': checksum(C._data)}
+    # record the full spectrum from the svd call output
+    srec = scall['out'][1]
+    if rec.arrays.get(srec['__array__']) is not None:
+        extra['S_full'] = [float(x) for x in rec.arrays[srec['__array__']]]
+    save('cfg1', rec, extra)
+
+
+def _arr_from(rec, x):
+    return rec.arrays[x['__array__']]
+
+
+if __name__ == '__main__':
+    for pol in ('fuse_to_matrix', 'fuse_contracted', 'no_fusion'):
+        scen_tensordot(pol)
+    scen_svd()
+    scen_fix_signs()
+    scen_truncation()
+    scen_eigh()
+    scen_adjoints()
+    scen_svd_ill()
+    scen_tds_adjoint()
+    scen_cfg1()

@@ -1,0 +1,106 @@
+"""NumPy interpreter of the packed C-ABI records (test helper).
+
+Executes copy / grouped-GEMM / SVD-adjoint records exactly as the CUDA kernels read
+them (including the 32-bit fast-division constants), so the host plan compiler can be
+checked against the oracle on the CPU.
+"""
+import numpy as np
+
+from yastn_gb300 import _plans as P
+
+
+def fast_div_np(n, magic, shift):
+    n = np.asarray(n, dtype=np.uint64)
+    return ((((n * np.uint64(magic)) >> np.uint64(32)) + n) >> np.uint64(shift)).astype(np.int64)
+
+
+def run_copy(tasks, items, src, dst):
+    """Apply copy tasks from src to dst (1-D numpy arrays of the same dtype)."""
+    covered = {}
+    for ti, first in items:
+        covered.setdefault(int(ti), []).append(int(first))
+    for ti, rec in enumerate(tasks):
+        ndim, count, vec = int(rec[P.CP_NDIM]), int(rec[P.CP_COUNT]), int(rec[P.CP_VEC])
+        firsts = sorted(covered.get(ti, []))
+        assert firsts == list(range(0, count, P.COPY_ITEM_UNITS)), "items do not tile the task"
+        idx = np.arange(count, dtype=np.int64)
+        so = np.full(count, rec[P.CP_SRC], dtype=np.int64)
+        do = np.full(count, rec[P.CP_DST], dtype=np.int64)
+        for d in range(ndim - 1, -1, -1):
+            size = int(rec[P.CP_SIZE + d])
+            q = fast_div_np(idx, int(rec[P.CP_MAGIC + d]), int(rec[P.CP_SHIFT + d]))
+            assert np.array_equal(q, idx // size), "fast division constants are wrong"
+            r = idx - q * size
+            so += r * rec[P.CP_SSTR + d]
+            do += r * rec[P.CP_DSTR + d]
+            idx = q
+        if vec:
+            for j in (0, 1):
+                dst[2 * do + j] = src[2 * so + j]
+        else:
+            dst[do] = src[so]
+    return dst
+
+
+def run_gemm(plan, a, b, c, alpha=1.0, beta=0.0):
+    """Grouped sum-of-products GEMM records applied with numpy."""
+    seen = {}
+    for oi, tr, tc, _ in plan.tiles:
+        seen.setdefault(int(oi), set()).add((int(tr), int(tc)))
+    for oi, o in enumerate(plan.outs):
+        c_off, m, n, ldc, t0, t1 = (int(x) for x in o[:6])
+        if m == 0 or n == 0:
+            continue
+        want = {(i, j) for i in range((m + 63) // 64) for j in range((n + 63) // 64)}
+        assert seen.get(oi, set()) == want, "tiles do not cover the output"
+        acc = np.zeros((m, n), dtype=c.dtype)
+        for t in range(t0, t1):
+            a_off, b_off, k, ars, acs, brs, bcs, fl = (int(x) for x in plan.terms[t])
+            ii, ll = np.meshgrid(np.arange(m), np.arange(k), indexing='ij')
+            At = a[a_off + ii * ars + ll * acs]
+            ll2, jj = np.meshgrid(np.arange(k), np.arange(n), indexing='ij')
+            Bt = b[b_off + ll2 * brs + jj * bcs]
+            if fl & 1:
+                At = At.conj()
+            if fl & 2:
+                Bt = Bt.conj()
+            acc += At @ Bt
+        rows = c_off + np.arange(m)[:, None] * ldc + np.arange(n)[None, :]
+        c[rows] = alpha * acc + (beta * c[rows] if beta != 0 else 0)
+    return c
+
+
+def rinv(x):
+    return x / (x * x + 1e-12)
+
+
+def svd_adjoint_core(plan, Pm, Qm, S, gS, gU, gV, dtype):
+    """The K / TR formulas of csrc/yb_adjoint.cu, restated with numpy."""
+    K = np.zeros(plan.kk, dtype=dtype)
+    TR = np.zeros(max(plan.tr, 1), dtype=dtype)
+    for r in plan.recs:
+        a_off, m, n, uo, so, vo, kko, tro, k, kind = (int(x) for x in r[:10])
+        s = S[so:so + k]
+        Pb = Pm[kko:kko + k * k].reshape(k, k)
+        Qb = Qm[kko:kko + k * k].reshape(k, k)
+        F = rinv(s[None, :] - s[:, None])
+        G = rinv(s[None, :] + s[:, None])
+        np.fill_diagonal(F, 0)
+        np.fill_diagonal(G, 0)
+        Kb = 0.5 * (F + G) * (Pb - Pb.conj().T) + 0.5 * (F - G) * (Qb - Qb.conj().T)
+        d = np.zeros(k, dtype=dtype)
+        if gS is not None:
+            d = d + gS[so:so + k]
+        if np.iscomplexobj(Pb):
+            d = d + 1j * np.diagonal(Pb).imag * rinv(s)
+        Kb[np.arange(k), np.arange(k)] = d
+        if kind == 1:
+            Kb = Kb - rinv(s)[:, None] * Qb.conj().T
+        elif kind == 2:
+            Kb = Kb - Pb * rinv(s)[None, :]
+        K[kko:kko + k * k] = Kb.ravel()
+        if kind == 1:
+            TR[tro:tro + k * n] = (rinv(s)[:, None] * gV[vo:vo + k * n].reshape(k, n)).ravel()
+        elif kind == 2:
+            TR[tro:tro + m * k] = (gU[uo:uo + m * k].reshape(m, k) * rinv(s)[None, :]).ravel()
+    return K, TR

@@ -1,0 +1,165 @@
+"""The oracle (NumPy restatement) against golden vectors recorded from the reference.
+
+Every hot-path backend call recorded from YASTN's NumPy backend is replayed through
+``oracle`` on the recorded inputs; outputs must match (bit-exact for pure data
+movement, 1e-12 relative for arithmetic, gauge-invariant checks for SVD/eigh).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from yastn_gb300.workloads import load_trace, GOLDEN
+
+TRACES = ['tensordot_fuse_to_matrix', 'tensordot_fuse_contracted', 'tensordot_no_fusion', 'svd', 'eigh',
+          'fix_signs']
+MOVES = ('transpose_and_merge', 'unmerge', 'apply_mask', 'embed_mask')
+
+
+def _rel(a, b):
+    den = max(np.abs(b).max(), 1e-300) if b.size else 1.0
+    return float(np.abs(a - b).max() / den) if b.size else 0.0
+
+
+@pytest.mark.parametrize('name', TRACES)
+def test_oracle_replays_reference_calls(name):
+    tr = load_trace(name)
+    n_checked = 0
+    for c in tr['calls']:
+        fn, args, out = c['fn'], c['args'], c['out']
+        if fn in MOVES:
+            res = getattr(oracle, fn)(*args)
+            assert res.dtype == out[0].dtype
+            np.testing.assert_array_equal(res, out[0])
+        elif fn in ('dot', 'transpose_dot_sum'):
+            res = getattr(oracle, fn)(*args)
+            assert res.dtype == out[0].dtype
+            assert _rel(res, out[0]) < 1e-12
+        elif fn == 'svd':
+            data, meta, sizes = args[:3]
+            U, S, V = oracle.svd(data, meta, sizes)
+            assert _rel(S, out[1]) < 1e-12
+            for sl, D, slU, DU, slS, slV, DV in meta:
+                a = data[sl[0]:sl[1]].reshape(D)
+                rec = (U[slU[0]:slU[1]].reshape(DU) * S[slS[0]:slS[1]]) @ V[slV[0]:slV[1]].reshape(DV)
+                assert _rel(rec, a) < 1e-12
+        elif fn == 'fix_svd_signs':
+            Ui, Vi, meta = args
+            Uo, Vo = oracle.fix_svd_signs(Ui, Vi, meta)
+            assert _rel(Uo, out[0]) < 1e-12 and _rel(Vo, out[1]) < 1e-12
+        elif fn == 'eigh':
+            data, meta, sizes = args
+            S, U = oracle.eigh(data, meta, sizes)
+            assert _rel(S, out[0]) < 1e-12
+            for sl, D, slU, DU, slS in meta:
+                a = data[sl[0]:sl[1]].reshape(D)
+                u = U[slU[0]:slU[1]].reshape(DU)
+                s = S[slS[0]:slS[1]]
+                assert _rel((u * s) @ u.conj().T, a) < 1e-12
+        else:
+            continue
+        n_checked += 1
+    assert n_checked > 0
+
+
+def test_oracle_fix_signs_golden_matrix():
+    """test_svd.py:159-186: the gauge-fixed U of the reference test."""
+    tr = load_trace('fix_signs')
+    svd_call = [c for c in tr['calls'] if c['fn'] == 'svd'][0]
+    fix_call = [c for c in tr['calls'] if c['fn'] == 'fix_svd_signs'][0]
+    data, meta, sizes = svd_call['args'][:3]
+    U, S, V = oracle.svd(data, meta, sizes)
+    Uf, Vf = oracle.fix_svd_signs(U, V, meta)
+    assert _rel(Uf, fix_call['out'][0]) < 1e-12
+    # the golden matrix of the reference test, columns (re, im) pairs
+    gold = {k: np.array(v)[:, 0::2] + 1j * np.array(v)[:, 1::2] for k, v in tr['Ufixed'].items()}
+    blocks = [Uf[m[2][0]:m[2][1]].reshape(m[3]) for m in meta]
+    assert any(b.shape == (3, 2) and np.abs(b - gold['(0,0)']).max() < 1e-12 for b in blocks)
+    assert any(b.shape == (2, 2) and np.abs(b - gold['(1,1)']).max() < 1e-12 for b in blocks)
+
+
+def _decode_opts(opts):
+    out = {}
+    for k, v in opts.items():
+        if isinstance(v, dict) and '__dict__' in v:
+            v = {tuple(kk): vv for kk, vv in v['__dict__']}
+        out[k] = v
+    return out
+
+
+def test_oracle_truncation_matches_reference_masks():
+    with open(os.path.join(GOLDEN, 'truncation.json')) as f:
+        cases = json.load(f)['cases']
+    assert len(cases) >= 13
+    for case in cases:
+        S = np.array(case['S'])
+        charges = [tuple(c) for c in case['charges']]
+        mask = oracle.truncation_mask(S, case['slices'], charges, **_decode_opts(case['opts']))
+        np.testing.assert_array_equal(mask, np.array(case['mask'], dtype=bool))
+
+
+def test_oracle_truncation_reference_shapes():
+    """Exact kept counts asserted by the reference tests (test_svd.py:189-266, :344-388)."""
+    with open(os.path.join(GOLDEN, 'truncation.json')) as f:
+        cases = json.load(f)['cases']
+    kept = [int(np.sum(c['mask'])) for c in cases]
+    assert kept[:6] == [12, 11, 9, 4, 12, 0]
+    assert kept[6:9] == [30, 32, 24]
+
+
+def test_oracle_adjoints_match_reference_autograd():
+    tr = load_trace('adjoints')
+    A = tr['_arrays']
+    for c in tr['calls']:
+        if c['fn'] == 'svd_backward':
+            meta = c['meta']
+            U, S, V = A[c['U']], A[c['S']], A[c['V']]
+            # the golden cotangents are stored as d(loss)/d(conj x); pass them as-is
+            grad = oracle.svd_backward(U, S, V, A[c['gU']], A[c['gS']], A[c['gV']], meta,
+                                       A[c['data']].size, A[c['data']].dtype)
+            assert _rel(grad, A[c['grad']]) < 1e-10
+        elif c['fn'] == 'dot_backward':
+            Ab, Bb = oracle.dot_backward(A[c['Cb']], A[c['A']], A[c['B']], c['meta'])
+            assert _rel(Ab, A[c['Ab']]) < 1e-12 and _rel(Bb, A[c['Bb']]) < 1e-12
+        elif c['fn'] == 'transpose_and_merge_backward':
+            g = oracle.transpose_and_merge_backward(A[c['out_b']], c['order'], c['meta_new'], c['meta_mrg'],
+                                                    A[c['data']].size)
+            np.testing.assert_array_equal(g, A[c['grad']])
+        elif c['fn'] == 'unmerge_backward':
+            g = oracle.unmerge_backward(A[c['out_b']], c['meta'], A[c['data']].size)
+            np.testing.assert_array_equal(g, A[c['grad']])
+
+
+def test_cfg1_fixture_consistent_with_regenerated_inputs():
+    """The benchmark inputs regenerate from the seed; the first merge's input checksum matches."""
+    from yastn_gb300.workloads import cfg1_inputs
+    tr = load_trace('cfg1')
+    A, B = cfg1_inputs(tr)
+    first = tr['calls'][0]['args'][0]
+    assert first.shape == A.shape
+    assert abs(first.checksum['sum0'] - float(A.sum())) < 1e-9 * first.checksum['abs0']
+    assert first.checksum['head0'] == [float(x) for x in A[:8]]
+    second = tr['calls'][1]['args'][0]
+    assert second.checksum['head0'] == [float(x) for x in B[:8]]
+
+
+def test_oracle_tds_adjoint_matches_reference_autograd():
+    import numpy as np
+    from yastn_gb300.workloads import GOLDEN
+    with open(os.path.join(GOLDEN, 'tds_adjoint.json')) as f:
+        args = json.load(f)['args']
+    from yastn_gb300.workloads import _decode
+    meta, Ar, Br, Ao, Bo, _ = (_decode(a, None) for a in args)
+    z = np.load(os.path.join(GOLDEN, 'tds_adjoint.npz'))
+    Ab, Bb = oracle.transpose_dot_sum_backward(z['Cb'], z['A'], z['B'], meta, Ar, Br, Ao, Bo)
+    assert _rel(Ab, z['Ab']) < 1e-12 and _rel(Bb, z['Bb']) < 1e-12
+
+
+def test_oracle_ill_conditioned_svd():
+    tr = load_trace('svd_ill')
+    c = [c for c in tr['calls'] if c['fn'] == 'svd'][0]
+    data, meta, sizes = c['args'][:3]
+    U, S, V = oracle.svd(data, meta, sizes)
+    assert _rel(S, c['out'][1]) < 1e-12

@@ -1,0 +1,181 @@
+"""Host plan compiler, checked on the CPU by interpreting the packed records with numpy.
+
+The records are exactly what the CUDA kernels read; interpreting them reproduces the
+oracle on the reference's recorded calls (bit-exact for data movement).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from yastn_gb300 import _plans as P
+from yastn_gb300.workloads import load_trace
+import plan_interp as PI
+
+TRACES = ['tensordot_fuse_to_matrix', 'tensordot_fuse_contracted', 'tensordot_no_fusion', 'svd', 'cfg1']
+
+
+def test_fast_division_constants():
+    rng = np.random.default_rng(0)
+    for d in list(range(1, 70)) + list(rng.integers(1, 2 ** 31 - 1, size=200)):
+        m, s = P.fast_div_consts(int(d))
+        n = np.concatenate([rng.integers(0, 2 ** 31, size=2000), [0, 2 ** 31 - 1, int(d) - 1, int(d)]])
+        np.testing.assert_array_equal(PI.fast_div_np(n, m, s), n // int(d))
+
+
+@pytest.mark.parametrize('name', TRACES)
+@pytest.mark.parametrize('vec', [False, True])
+def test_copy_plans_reproduce_reference(name, vec):
+    tr = load_trace(name)
+    n = 0
+    for c in tr['calls']:
+        if c['fn'] == 'transpose_and_merge':
+            data, order, mn, mm, Dsize = c['args']
+            if not isinstance(data, np.ndarray):
+                continue
+            plan = P.merge_plan(order, mn, mm, Dsize)
+            tasks, items = plan.packed(vec and data.dtype == np.float64)
+            out = PI.run_copy(tasks, items, data, np.zeros(Dsize, dtype=data.dtype))
+            np.testing.assert_array_equal(out, c['out'][0])
+            # adjoint: the swapped plan scatters back exactly onto the source positions
+            inv = plan.swapped(data.size)
+            ti, it = inv.packed(vec and data.dtype == np.float64)
+            back = PI.run_copy(ti, it, out, np.zeros(data.size, dtype=data.dtype))
+            np.testing.assert_array_equal(back, oracle.transpose_and_merge_backward(out, order, mn, mm, data.size))
+            n += 1
+        elif c['fn'] == 'unmerge':
+            data, meta = c['args']
+            if not isinstance(data, np.ndarray):
+                continue
+            plan = P.unmerge_plan(meta, data.size)
+            assert plan.full
+            tasks, items = plan.packed(vec and data.dtype == np.float64)
+            out = PI.run_copy(tasks, items, data, np.zeros(data.size, dtype=data.dtype))
+            np.testing.assert_array_equal(out, c['out'][0])
+            n += 1
+    if name != 'cfg1':
+        assert n > 0
+
+
+def test_cfg1_merge_plan_shape():
+    """The benchmark merge: 231 source blocks into 13 fused sectors, full coverage."""
+    tr = load_trace('cfg1')
+    c = tr['calls'][0]
+    _, order, mn, mm, Dsize = c['args']
+    plan = P.merge_plan(order, mn, mm, Dsize)
+    assert len(plan.tasks_list) == 231 and len(mn) == 13 and plan.full
+    tasks, items = plan.packed(True)
+    assert tasks[:, P.CP_NDIM].max() <= 2  # identity order: rows of the block, one strided dim
+    rng = np.random.default_rng(1)
+    data = rng.normal(size=Dsize)
+    out = PI.run_copy(tasks, items, data, np.zeros(Dsize))
+    np.testing.assert_array_equal(out, oracle.transpose_and_merge(data, order, mn, mm, Dsize))
+
+
+@pytest.mark.parametrize('name', ['tensordot_fuse_to_matrix', 'tensordot_fuse_contracted'])
+def test_dot_plans_reproduce_reference(name):
+    tr = load_trace(name)
+    n = 0
+    for c in tr['calls']:
+        if c['fn'] != 'dot':
+            continue
+        A, B, meta, Dsize = c['args']
+        plan = P.dot_plan(meta)
+        dtype = np.promote_types(A.dtype, B.dtype)
+        out = PI.run_gemm(plan, A.astype(dtype), B.astype(dtype), np.zeros(Dsize, dtype=dtype))
+        ref = c['out'][0]
+        assert np.abs(out - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+        # adjoint plans against the oracle adjoint
+        rng = np.random.default_rng(3)
+        Cb = rng.normal(size=Dsize).astype(dtype)
+        pa, pb = P.dot_backward_plans(meta)
+        Ab = PI.run_gemm(pa, Cb, B.astype(dtype), np.zeros(A.size, dtype=dtype))
+        Bb = PI.run_gemm(pb, A.astype(dtype), Cb, np.zeros(B.size, dtype=dtype))
+        Ab_r, Bb_r = oracle.dot_backward(Cb, A, B, meta)
+        assert np.abs(Ab - Ab_r).max() <= 1e-12 * max(1.0, np.abs(Ab_r).max())
+        assert np.abs(Bb - Bb_r).max() <= 1e-12 * max(1.0, np.abs(Bb_r).max())
+        n += 1
+    assert n > 0
+
+
+def test_tds_plans_reproduce_reference():
+    import yastn_gb300._plans as PP
+    tr = load_trace('tensordot_no_fusion')
+    n = 0
+    for c in tr['calls']:
+        if c['fn'] != 'transpose_dot_sum':
+            continue
+        A, B, meta, Ar, Br, Ao, Bo, Dsize = c['args']
+        dtype = np.promote_types(A.dtype, B.dtype)
+
+        def permute(data, reshape, order):
+            tasks, offs, low = [], [], 0
+            for sl, Di, Dl, Dr in reshape:
+                sst = PP.row_major_strides(Di)
+                Dt = [Di[o] for o in order]
+                tasks.append((sl[0], low, Dt, [sst[o] for o in order], PP.row_major_strides(Dt)))
+                offs.append(low)
+                low += Dl * Dr
+            cp = PP.CopyPlan(tasks, low, low)
+            t, it = cp.packed(False)
+            return PI.run_copy(t, it, data.astype(dtype), np.zeros(low, dtype=dtype)), offs
+        Ap, Aoffs = permute(A, Ar, Ao)
+        Bp, Boffs = permute(B, Br, Bo)
+        plan = PP.tds_plan(meta, Ar, Br, tuple(Aoffs), tuple(Boffs))
+        out = PI.run_gemm(plan, Ap, Bp, np.zeros(Dsize, dtype=dtype))
+        ref = c['out'][0]
+        assert np.abs(out - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+        n += 1
+    assert n > 0
+
+
+@pytest.mark.parametrize('dtype', [np.float64, np.complex128])
+def test_svd_adjoint_decomposition_matches_oracle(dtype):
+    """P/Q GEMMs + K/TR core + finishing GEMMs == torch_svd_gesdd.py:296-428 restated."""
+    rng = np.random.default_rng(4)
+    shapes = [(6, 6), (9, 4), (3, 8), (1, 5), (5, 1)]
+    meta, off, oU, oS, oV = [], 0, 0, 0, 0
+    for m, n in shapes:
+        k = min(m, n)
+        meta.append(((off, off + m * n), (m, n), (oU, oU + m * k), (m, k), (oS, oS + k), (oV, oV + k * n), (k, n)))
+        off += m * n; oU += m * k; oS += k; oV += k * n
+    meta = tuple(meta)
+    data = rng.normal(size=off).astype(dtype)
+    if dtype == np.complex128:
+        data = data + 1j * rng.normal(size=off)
+    U, S, V = oracle.svd(data, meta, (oU, oS, oV))
+    gU = rng.normal(size=oU).astype(dtype)
+    gV = rng.normal(size=oV).astype(dtype)
+    gS = rng.normal(size=oS)
+    if dtype == np.complex128:
+        gU = gU + 1j * rng.normal(size=oU)
+        gV = gV + 1j * rng.normal(size=oV)
+    plan = P.svd_adjoint_plan(meta)
+    Pm = PI.run_gemm(plan.gP, U, gU, np.zeros(plan.kk, dtype=dtype))
+    Qm = PI.run_gemm(plan.gQ, V, gV, np.zeros(plan.kk, dtype=dtype))
+    K, TR = PI.svd_adjoint_core(plan, Pm, Qm, S, gS, gU, gV, dtype)
+    PI.run_gemm(plan.gT, K, V, TR, beta=1.0)
+    PI.run_gemm(plan.gR, U, K, TR, beta=1.0)
+    dA = np.zeros(off, dtype=dtype)
+    PI.run_gemm(plan.gA1, U, TR, dA)
+    PI.run_gemm(plan.gA2, TR, V, dA)
+    ref = oracle.svd_backward(U, S, V, gU, gS, gV, meta, off, dtype)
+    assert np.abs(dA - ref).max() <= 1e-10 * max(1.0, np.abs(ref).max())
+
+
+def test_svd_plan_pairs_cover_all_pairs():
+    """Circle-method ordering: N-1 rounds of disjoint pairs cover every pair once."""
+    for k in (1, 2, 3, 7, 8, 13):
+        N = k + (k % 2)
+        seen = set()
+        for rd in range(N - 1):
+            used = set()
+            for pi in range(N // 2):
+                if pi == 0:
+                    p, q = N - 1, rd
+                else:
+                    p, q = (rd + pi) % (N - 1), (rd - pi + (N - 1)) % (N - 1)
+                assert p not in used and q not in used
+                used |= {p, q}
+                if p < k and q < k:
+                    seen.add((min(p, q), max(p, q)))
+        assert seen == {(i, j) for i in range(k) for j in range(i + 1, k)}

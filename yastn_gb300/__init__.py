@@ -1,0 +1,15 @@
+"""yastn_gb300 — GB300-native (sm_103a) backend for YASTN's block-sparse tensors.
+
+    import yastn, yastn_gb300
+    cfg = yastn.make_config(sym='U1', backend=yastn_gb300.backend, default_device='cuda')
+
+``backend`` is a drop-in for ``yastn.backend.backend_torch``: the hot path
+(merge/unmerge, sector GEMMs, block SVD/eigh, masks, their adjoints) runs on
+hand-written CUDA kernels in ``libyastn_gb300.so``; build it with
+``python yastn_gb300/build.py``. ``truncation_mask`` is a one-launch replacement for
+``yastn.linalg.truncation_mask`` usable as ``mask_f``.
+"""
+from . import backend_gb300 as backend
+from .truncation import truncation_mask
+
+__all__ = ['backend', 'truncation_mask']

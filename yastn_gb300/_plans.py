@@ -1,0 +1,460 @@
+"""Plan compiler: YASTN metadata tuples -> packed int64 device records.
+
+YASTN's metadata layer hands the backend nested tuples (``meta_new``/``meta_mrg`` of
+``transpose_and_merge``, unmerge records, ``meta_dot``, svd records). Each plan below
+turns one such tuple into the flat records of the C ABI (``include/yastn_gb300.h``).
+Plans depend only on the metadata, so they are cached by the identity of the tuple
+(YASTN memoises its metadata with ``lru_cache``, so the same tuple object comes back)
+and, failing that, by value.
+"""
+from collections import OrderedDict
+
+import numpy as np
+
+# record layout constants (must match include/yastn_gb300.h)
+COPY_REC, CP_SRC, CP_DST, CP_NDIM, CP_COUNT, CP_VEC = 48, 0, 1, 2, 3, 4
+CP_MAXD, CP_SIZE, CP_SSTR, CP_DSTR, CP_MAGIC, CP_SHIFT = 8, 8, 16, 24, 32, 40
+COPY_ITEM_UNITS = 8192
+GEMM_OUT_REC, GEMM_TERM_REC, GEMM_TILE = 8, 8, 64
+SVD_REC = 16
+MASK_REC = 8
+
+
+class PlanError(ValueError):
+    """The metadata cannot be expressed as a plan of the C ABI."""
+
+
+# ----------------------------------------------------------------------------- caching
+
+class PlanCache:
+    """LRU cache keyed by metadata identity with a by-value fallback."""
+
+    def __init__(self, maxsize=2048):
+        self.by_id = OrderedDict()
+        self.by_val = OrderedDict()
+        self.maxsize = maxsize
+        self.hits = 0
+        self.misses = 0
+
+    def get(self, key_objs, extra, build):
+        kid = (tuple(id(o) for o in key_objs), extra)
+        ent = self.by_id.get(kid)
+        if ent is not None and all(a is b for a, b in zip(ent[0], key_objs)):
+            self.by_id.move_to_end(kid)
+            self.hits += 1
+            return ent[1]
+        kval = (tuple(key_objs), extra)
+        try:
+            plan = self.by_val.get(kval)
+        except TypeError:  # unhashable metadata (e.g. masks): no by-value cache
+            kval, plan = None, None
+        if plan is None:
+            self.misses += 1
+            plan = build()
+            if kval is not None:
+                self.by_val[kval] = plan
+                if len(self.by_val) > self.maxsize:
+                    self.by_val.popitem(last=False)
+        else:
+            self.hits += 1
+        self.by_id[kid] = (tuple(key_objs), plan)
+        if len(self.by_id) > self.maxsize:
+            self.by_id.popitem(last=False)
+        return plan
+
+
+CACHE = PlanCache()
+
+
+def cache_info():
+    return {'hits': CACHE.hits, 'misses': CACHE.misses, 'size': len(CACHE.by_id)}
+
+
+# ----------------------------------------------------------------------------- helpers
+
+def fast_div_consts(d):
+    """(magic, shift) with n // d == (umulhi(n, magic) + n) >> shift for 0 <= n < 2^31."""
+    if d < 1 or d >= 2 ** 31:
+        raise PlanError(f"extent {d} out of range for 32-bit fast division")
+    shift = 0
+    while (1 << shift) < d:
+        shift += 1
+    magic = ((1 << 32) * ((1 << shift) - d)) // d + 1
+    return magic & 0xFFFFFFFF, shift
+
+
+def row_major_strides(D):
+    st = [1] * len(D)
+    for i in range(len(D) - 2, -1, -1):
+        st[i] = st[i + 1] * D[i + 1]
+    return st
+
+
+def group_dims(dims, targets):
+    """Assign consecutive ``dims`` to groups whose products equal ``targets``.
+
+    Returns a list with the group index of every dim. Dims of extent 1 may sit in
+    any group; they are attached to the current group.
+    """
+    G = len(targets)
+    out = []
+    g, prod = 0, 1
+    for d in dims:
+        while g < G - 1 and prod == targets[g] and d != 1:
+            g, prod = g + 1, 1
+        prod *= d
+        out.append(g)
+    # trailing groups of product 1 are legal
+    prods = [1] * G
+    for d, gi in zip(dims, out):
+        prods[gi] *= d
+    if tuple(prods) != tuple(targets):
+        raise PlanError(f"cannot split dims {dims} into consecutive groups {targets}")
+    return out
+
+
+def _collapse(sizes, ss, ds):
+    """Drop extent-1 dims and merge neighbours contiguous in both source and destination."""
+    dims = [(n, a, b) for n, a, b in zip(sizes, ss, ds) if n != 1]
+    if not dims:
+        return [1], [1], [1]
+    out = [list(dims[0])]
+    for n, a, b in dims[1:]:
+        pn, pa, pb = out[-1]
+        if pa == a * n and pb == b * n:
+            out[-1] = [pn * n, a, b]
+        else:
+            out.append([n, a, b])
+    return [x[0] for x in out], [x[1] for x in out], [x[2] for x in out]
+
+
+class CopyPlan:
+    """Host copy of a family-(a) plan: tasks, items, element coverage."""
+
+    def __init__(self, tasks, covered, size_dst):
+        self.tasks_list = tasks  # list of (src_off, dst_off, sizes, sstr, dstr) in elements
+        self.covered = covered
+        self.size_dst = size_dst
+        self.full = covered == size_dst
+        self._packed = {}
+        self._dev = {}
+
+    def swapped(self, size_src):
+        """The inverse copy (adjoint): source and destination exchanged."""
+        t = [(d, s, sz, dd, sd) for (s, d, sz, sd, dd) in self.tasks_list]
+        return CopyPlan(t, self.covered, size_src)
+
+    def packed(self, vec_ok):
+        """(tasks int64 [n, COPY_REC], items int64 [m, 2]) with 16-byte units where allowed."""
+        if vec_ok in self._packed:
+            return self._packed[vec_ok]
+        recs, items = [], []
+        for ti, (so, do, sizes, ss, ds) in enumerate(self.tasks_list):
+            sizes, ss, ds = _collapse(sizes, ss, ds)
+            if len(sizes) > CP_MAXD:
+                raise PlanError(f"copy task with {len(sizes)} non-collapsible dims (max {CP_MAXD})")
+            vec = 0
+            if vec_ok and ss[-1] == 1 and ds[-1] == 1 and sizes[-1] % 2 == 0 and so % 2 == 0 and do % 2 == 0 \
+                    and all(x % 2 == 0 for x in ss[:-1]) and all(x % 2 == 0 for x in ds[:-1]):
+                vec = 1
+                sizes = sizes[:-1] + [sizes[-1] // 2]
+                ss = [x // 2 for x in ss[:-1]] + [1]
+                ds = [x // 2 for x in ds[:-1]] + [1]
+                so, do = so // 2, do // 2
+            count = int(np.prod(sizes, dtype=np.int64))
+            if count >= 2 ** 31:
+                raise PlanError("copy task larger than 2^31 units")
+            rec = np.zeros(COPY_REC, dtype=np.int64)
+            rec[CP_SRC], rec[CP_DST], rec[CP_NDIM], rec[CP_COUNT], rec[CP_VEC] = so, do, len(sizes), count, vec
+            for i, (n, a, b) in enumerate(zip(sizes, ss, ds)):
+                m, sh = fast_div_consts(n)
+                rec[CP_SIZE + i], rec[CP_SSTR + i], rec[CP_DSTR + i] = n, a, b
+                rec[CP_MAGIC + i], rec[CP_SHIFT + i] = m, sh
+            recs.append(rec)
+            items.extend((ti, f) for f in range(0, count, COPY_ITEM_UNITS))
+        tasks = np.stack(recs) if recs else np.zeros((0, COPY_REC), dtype=np.int64)
+        items = np.array(items, dtype=np.int64).reshape(-1, 2)
+        self._packed[vec_ok] = (tasks, items)
+        return self._packed[vec_ok]
+
+
+# ----------------------------------------------------------------------------- merge / unmerge
+
+def merge_plan(order, meta_new, meta_mrg, Dsize):
+    """Plan of transpose_and_merge (restating yastn/backend/backend_np.py:653-661)."""
+    def build():
+        order_ = tuple(order)
+        tasks, covered = [], 0
+        it = iter(meta_new)
+        cur = None
+        for tn, slo, Do, Dslc, Drsh in meta_mrg:
+            if cur is None or cur[0] != tn:
+                cur = next(it)
+                while cur[0] != tn:
+                    cur = next(it)
+            _, Dn, sln = cur
+            ndim = len(Do)
+            sst = row_major_strides(Do)
+            Dt = [Do[o] for o in order_]
+            tss = [sst[o] for o in order_]
+            groups = group_dims(Dt, Drsh)
+            dn_str = row_major_strides(Dn)
+            dst = [0] * ndim
+            for gi in range(len(Drsh)):
+                members = [i for i in range(ndim) if groups[i] == gi]
+                w = 1
+                for i in reversed(members):
+                    dst[i] = w * dn_str[gi]
+                    w *= Dt[i]
+            doff = sln[0] + sum(s[0] * st for s, st in zip(Dslc, dn_str))
+            n = int(np.prod(Do, dtype=np.int64))
+            if n == 0:
+                continue
+            tasks.append((slo[0], doff, Dt, tss, dst))
+            covered += n
+        return CopyPlan(tasks, covered, Dsize)
+    return CACHE.get((order, meta_new, meta_mrg), ('merge', Dsize), build)
+
+
+def unmerge_plan(meta, size):
+    """Plan of unmerge (restating yastn/backend/backend_np.py:664-669)."""
+    def build():
+        tasks, covered = [], 0
+        for sln, Dn, slo, Do, sub_slc in meta:
+            n = int(np.prod(Dn, dtype=np.int64))
+            if n == 0:
+                continue
+            widths = [b - a for a, b in sub_slc]
+            groups = group_dims(list(Dn), widths)
+            do_str = row_major_strides(Do)
+            ss = [0] * len(Dn)
+            for gi in range(len(widths)):
+                members = [i for i in range(len(Dn)) if groups[i] == gi]
+                w = 1
+                for i in reversed(members):
+                    ss[i] = w * do_str[gi]
+                    w *= Dn[i]
+            soff = slo[0] + sum(a * st for (a, _), st in zip(sub_slc, do_str))
+            tasks.append((soff, sln[0], list(Dn), ss, row_major_strides(Dn)))
+            covered += n
+        return CopyPlan(tasks, covered, size)
+    return CACHE.get((meta,), ('unmerge', size), build)
+
+
+def transpose_plan(axes, meta_transpose, size):
+    """Plan of transpose (yastn/backend/backend_np.py:646-650): blocks permuted in place."""
+    def build():
+        tasks, covered = [], 0
+        for sln, Dn, slo, Do in meta_transpose:
+            n = int(np.prod(Do, dtype=np.int64))
+            if n == 0:
+                continue
+            sst = row_major_strides(Do)
+            tasks.append((slo[0], sln[0], [Do[a] for a in axes], [sst[a] for a in axes], row_major_strides(Dn)))
+            covered += n
+        return CopyPlan(tasks, covered, size)
+    return CACHE.get((axes, meta_transpose), ('transpose', size), build)
+
+
+# ----------------------------------------------------------------------------- grouped GEMM
+
+class GemmPlan:
+    def __init__(self, outs, terms, tiles, flops):
+        self.outs = outs
+        self.terms = terms
+        self.tiles = tiles
+        self.flops = flops  # real multiply-adds x 2 (complex counted by the caller)
+        self._dev = {}
+
+
+def _tiles_for(outs, terms):
+    tiles = []
+    for oi, o in enumerate(outs):
+        m, n = int(o[1]), int(o[2])
+        if m == 0 or n == 0:
+            continue
+        kk = int(sum(terms[t][2] for t in range(o[4], o[5])))
+        for tr in range((m + GEMM_TILE - 1) // GEMM_TILE):
+            for tc in range((n + GEMM_TILE - 1) // GEMM_TILE):
+                tiles.append((kk, oi, tr, tc))
+    tiles.sort(key=lambda x: -x[0])
+    arr = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles], dtype=np.int32).reshape(-1, 4)
+    return arr
+
+
+def _pack_gemm(out_list):
+    """out_list: [(c_off, m, n, ldc, [term tuples])] -> GemmPlan."""
+    outs, terms, flops = [], [], 0
+    for c_off, m, n, ldc, tl in out_list:
+        t0 = len(terms)
+        for t in tl:
+            terms.append(t)
+            flops += 2 * m * n * t[2]
+        outs.append((c_off, m, n, ldc, t0, len(terms), 0, 0))
+    outs = np.array(outs, dtype=np.int64).reshape(-1, GEMM_OUT_REC)
+    terms = np.array(terms, dtype=np.int64).reshape(-1, GEMM_TERM_REC)
+    return GemmPlan(outs, terms, _tiles_for(outs, terms), flops)
+
+
+def dot_plan(meta_dot):
+    """C[slc] = A[sla] @ B[slb] (yastn/backend/backend_np.py:580-587)."""
+    def build():
+        out_list = []
+        for slc, Dc, sla, Da, slb, Db in meta_dot:
+            out_list.append((slc[0], Dc[0], Dc[1], Dc[1], [(sla[0], slb[0], Da[1], Da[1], 1, Db[1], 1, 0)]))
+        return _pack_gemm(out_list)
+    return CACHE.get((meta_dot,), ('dot',), build)
+
+
+def dot_backward_plans(meta_dot):
+    """A_b[sla] += C_b[slc] B[slb]^H and B_b[slb] += A[sla]^H C_b[slc], grouped by operand block
+    (restating yastn/backend/_backend_torch_backwards.py:117-138)."""
+    def build():
+        ga, gb = OrderedDict(), OrderedDict()
+        for slc, Dc, sla, Da, slb, Db in meta_dot:
+            # A_b block: (Da0 x Da1) = (Dc0 x Dc1) @ (Db1 x Db0)^H ; terms use a:=C_b, b:=B
+            ga.setdefault((sla[0], Da[0], Da[1]), []).append((slc[0], slb[0], Dc[1], Dc[1], 1, 1, Db[1], 2))
+            # B_b block: (Db0 x Db1) = (Da1 x Da0) @ (Dc0 x Dc1) ; terms use a:=A, b:=C_b
+            gb.setdefault((slb[0], Db[0], Db[1]), []).append((sla[0], slc[0], Da[0], 1, Da[1], Dc[1], 1, 1))
+        pa = _pack_gemm([(off, m, n, n, tl) for (off, m, n), tl in ga.items()])
+        pb = _pack_gemm([(off, m, n, n, tl) for (off, m, n), tl in gb.items()])
+        return pa, pb
+    return CACHE.get((meta_dot,), ('dot_bwd',), build)
+
+
+def tds_plan(meta_dot, Areshape, Breshape, Aoffs, Boffs):
+    """transpose_dot_sum after the operands were permuted into (Dl, Dr) matrices stored at
+    ``Aoffs``/``Boffs`` (restating yastn/backend/backend_np.py:590-601)."""
+    def build():
+        out_list = []
+        for sl, Dslc, pairs in meta_dot:
+            tl = []
+            for ta, tb in pairs:
+                _, _, Dla, Dra = Areshape[ta]
+                _, _, Dlb, Drb = Breshape[tb]
+                tl.append((Aoffs[ta], Boffs[tb], Dra, Dra, 1, Drb, 1, 0))
+            out_list.append((sl[0], Dslc[0], Dslc[1], Dslc[1], tl))
+        return _pack_gemm(out_list)
+    return CACHE.get((meta_dot, Areshape, Breshape), ('tds',), build)
+
+
+# ----------------------------------------------------------------------------- SVD
+
+class SvdPlan:
+    def __init__(self, blocks, pair_items, max_rounds, work_elems, max_k, nominal_flops):
+        self.blocks = blocks
+        self.pair_items = pair_items
+        self.max_rounds = max_rounds
+        self.work_elems = work_elems
+        self.max_k = max_k
+        self.nominal_flops = nominal_flops
+        self._dev = {}
+
+
+def svd_plan(meta):
+    """Jacobi plan for svd records (sl, D, slU, DU, slS, slV, DV) of yastn/tensor/linalg.py:323-380."""
+    def build():
+        recs, pairs, woff, max_rounds, max_k, fl = [], [], 0, 0, 0, 0
+        for bi, (sl, D, slU, DU, slS, slV, DV) in enumerate(meta):
+            m, n = D
+            k = min(m, n)
+            if k == 0:
+                continue
+            if DU != (m, k) or DV != (k, n) or slS[1] - slS[0] != k:
+                raise PlanError("svd record is not a thin full-rank SVD")
+            L = max(m, n)
+            N = k + (k % 2)
+            rec = np.zeros(SVD_REC, dtype=np.int64)
+            rec[:13] = (sl[0], m, n, slU[0], slS[0], slV[0], woff, woff + k * L, len(pairs), k, L, N, int(m > n))
+            woff += k * L + k * k
+            b = len(recs)
+            recs.append(rec)
+            pairs.extend((b, p) for p in range(N // 2))
+            max_rounds = max(max_rounds, N - 1)
+            max_k = max(max_k, k)
+            fl += 14 * L * k * k + 8 * k ** 3  # nominal Golub-Reinsch count
+        blocks = np.stack(recs) if recs else np.zeros((0, SVD_REC), dtype=np.int64)
+        items = np.array(pairs, dtype=np.int32).reshape(-1, 2)
+        return SvdPlan(blocks, items, max_rounds, woff, max_k, fl)
+    return CACHE.get((meta,), ('svd',), build)
+
+
+class SvdAdjointPlan:
+    def __init__(self, recs, kk, tr, gP, gQ, gT, gR, gA1, gA2):
+        self.recs, self.kk, self.tr = recs, kk, tr
+        self.gP, self.gQ, self.gT, self.gR, self.gA1, self.gA2 = gP, gQ, gT, gR, gA1, gA2
+        self._dev = {}
+
+
+def svd_adjoint_plan(meta):
+    """Grouped-GEMM plans of the SVD adjoint (torch_svd_gesdd.py:296-428), all blocks at once.
+
+    P = U^H gU, Q = Vh gVh^H (k x k); square/wide blocks: TR += K Vh, dA = U TR;
+    tall blocks: TR += U K, dA = TR Vh (see csrc/yb_adjoint.cu for K and TR).
+    """
+    def build():
+        recs, lP, lQ, lT, lR, lA1, lA2 = [], [], [], [], [], [], []
+        kk = tr = 0
+        for sl, D, slU, DU, slS, slV, DV in meta:
+            m, n = D
+            k = min(m, n)
+            if k == 0:
+                continue
+            kind = 0 if m == n else (1 if n > m else 2)
+            rec = np.zeros(16, dtype=np.int64)
+            rec[:10] = (sl[0], m, n, slU[0], slS[0], slV[0], kk, tr, k, kind)
+            recs.append(rec)
+            lP.append((kk, k, k, k, [(slU[0], slU[0], m, 1, k, k, 1, 1)]))
+            lQ.append((kk, k, k, k, [(slV[0], slV[0], n, n, 1, 1, n, 2)]))
+            if kind != 2:
+                lT.append((tr, k, n, n, [(kk, slV[0], k, k, 1, n, 1, 0)]))
+                lA1.append((sl[0], m, n, n, [(slU[0], tr, k, k, 1, n, 1, 0)]))
+                tr += k * n
+            else:
+                lR.append((tr, m, k, k, [(slU[0], kk, k, k, 1, k, 1, 0)]))
+                lA2.append((sl[0], m, n, n, [(tr, slV[0], k, k, 1, n, 1, 0)]))
+                tr += m * k
+            kk += k * k
+        recs = np.stack(recs) if recs else np.zeros((0, 16), dtype=np.int64)
+        return SvdAdjointPlan(recs, kk, tr, *(_pack_gemm(x) for x in (lP, lQ, lT, lR, lA1, lA2)))
+    return CACHE.get((meta,), ('svd_adjoint',), build)
+
+
+def tds_backward_plans(meta_dot, Areshape, Breshape, Aoffs, Boffs):
+    """Adjoint of transpose_dot_sum on the permuted (Dl, Dr) operand matrices:
+    At_b[a] = sum C_b[sl] Bt[b]^H, Bt_b[b] = sum At[a]^H C_b[sl] (grouped by operand)."""
+    def build():
+        ga, gb = OrderedDict(), OrderedDict()
+        for sl, Dslc, pairs in meta_dot:
+            mc, nc = Dslc
+            for ta, tb in pairs:
+                _, _, Dla, Dra = Areshape[ta]
+                _, _, Dlb, Drb = Breshape[tb]
+                ga.setdefault(ta, []).append((sl[0], Boffs[tb], nc, nc, 1, 1, Drb, 2))
+                gb.setdefault(tb, []).append((Aoffs[ta], sl[0], Dla, 1, Dra, nc, 1, 1))
+        pa = _pack_gemm([(Aoffs[ta], Areshape[ta][2], Areshape[ta][3], Areshape[ta][3], tl) for ta, tl in ga.items()])
+        pb = _pack_gemm([(Boffs[tb], Breshape[tb][2], Breshape[tb][3], Breshape[tb][3], tl) for tb, tl in gb.items()])
+        return pa, pb
+    return CACHE.get((meta_dot, Areshape, Breshape), ('tds_bwd',), build)
+
+
+# ----------------------------------------------------------------------------- masks
+
+def mask_plan(meta, axis, lengths):
+    """apply_mask records (yastn/backend/backend_np.py:626-633); ``lengths`` maps a mask charge
+    to (offset in the concatenated index buffer, number of kept indices)."""
+    recs, items, total = [], [], 0
+    for sln, Dn, sla, Da, tm in meta:
+        ioff, cnt = lengths[tm]
+        pre = int(np.prod(Da[:axis], dtype=np.int64))
+        post = int(np.prod(Da[axis + 1:], dtype=np.int64))
+        nout = pre * cnt * post
+        if nout == 0:
+            continue
+        ri = len(recs)
+        recs.append((sln[0], sla[0], pre, Da[axis], cnt, post, ioff, 0))
+        items.extend((ri, f) for f in range(0, nout, COPY_ITEM_UNITS))
+        total += nout
+    recs = np.array(recs, dtype=np.int64).reshape(-1, MASK_REC)
+    items = np.array(items, dtype=np.int64).reshape(-1, 2)
+    return recs, items, total

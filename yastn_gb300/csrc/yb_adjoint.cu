@@ -1,0 +1,134 @@
+// Adjoint of the block SVD (regularised as in yastn/backend/linalg/torch_svd_gesdd.py:296-428).
+//
+// For a block A = U diag(s) Vh (m x n, k = min(m, n)) with cotangents gU, gS, gVh and
+// P = U^H gU, Q = Vh gVh^H (both k x k, computed by the grouped GEMM), this kernel forms
+//
+//   K_ij = (F+G)_ij (P_ij - conj P_ji)/2 + (F-G)_ij (Q_ij - conj Q_ji)/2
+//          + delta_ij (gS_i + i Im(P_ii) sinv_i [complex])
+//          - [n > k] sinv_i conj(Q_ji) - [m > k] P_ij sinv_j
+//
+// with F_ij = r(s_j - s_i), G_ij = r(s_j + s_i) off the diagonal (zero on it),
+// sinv_i = r(s_i) and r(x) = x / (x^2 + 1e-12), and initialises the work matrix TR:
+// wide blocks TR = diag(sinv) gVh, square TR = 0, tall TR = gU diag(sinv). The host
+// then finishes with grouped GEMMs: TR += K Vh, dA = U TR (square/wide) or
+// TR += U K, dA = TR Vh (tall), which equals the reference's u_term + sigma_term +
+// v_term (+ imaginary term).
+#include "yb_common.cuh"
+
+namespace yb {
+namespace {
+
+__device__ __forceinline__ double rinv(double x) { return x / (x * x + 1.0e-12); }
+
+template <bool Cx>
+struct Elt;
+template <>
+struct Elt<false> {
+  using T = double;
+};
+template <>
+struct Elt<true> {
+  using T = double2;
+};
+
+__device__ __forceinline__ double re(double a) { return a; }
+__device__ __forceinline__ double re(double2 a) { return a.x; }
+
+template <bool Cx>
+__global__ void svd_adjoint_core_kernel(const typename Elt<Cx>::T* __restrict__ P,
+                                        const typename Elt<Cx>::T* __restrict__ Q, const double* __restrict__ S,
+                                        const double* __restrict__ gS, typename Elt<Cx>::T* __restrict__ K,
+                                        const typename Elt<Cx>::T* __restrict__ gU,
+                                        const typename Elt<Cx>::T* __restrict__ gVh,
+                                        typename Elt<Cx>::T* __restrict__ TR, const int64_t* __restrict__ blocks) {
+  using T = typename Elt<Cx>::T;
+  const int64_t* r = blocks + (int64_t)blockIdx.y * YB_ADJ_REC;
+  const int64_t m = r[1], n = r[2], k = r[8], kind = r[9];
+  const double* s = S + r[4];
+  const T* Pb = P + r[6];
+  const T* Qb = Q + r[6];
+  T* Kb = K + r[6];
+  const int64_t kk = k * k;
+  const int64_t ntr = (kind == 2) ? m * k : k * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < kk + ntr;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    if (e < kk) {
+      const int64_t i = e / k, j = e - i * k;
+      const double si = s[i], sj = s[j];
+      if constexpr (Cx) {
+        const double2 pij = Pb[i * k + j], pji = Pb[j * k + i];
+        const double2 qij = Qb[i * k + j], qji = Qb[j * k + i];
+        double2 out = make_double2(0.0, 0.0);
+        if (i != j) {
+          const double f = rinv(sj - si), g = rinv(sj + si);
+          const double a = 0.5 * (f + g), b = 0.5 * (f - g);
+          out.x = a * (pij.x - pji.x) + b * (qij.x - qji.x);
+          out.y = a * (pij.y + pji.y) + b * (qij.y + qji.y);
+        } else {
+          out.x = (gS ? gS[r[4] + i] : 0.0);
+          out.y = pij.y * rinv(si);
+        }
+        if (kind == 1) {  // - sinv_i conj(Q_ji)
+          out.x -= rinv(si) * qji.x;
+          out.y += rinv(si) * qji.y;
+        } else if (kind == 2) {  // - P_ij sinv_j
+          out.x -= pij.x * rinv(sj);
+          out.y -= pij.y * rinv(sj);
+        }
+        Kb[i * k + j] = out;
+      } else {
+        const double pij = Pb[i * k + j], pji = Pb[j * k + i];
+        const double qij = Qb[i * k + j], qji = Qb[j * k + i];
+        double out = 0.0;
+        if (i != j) {
+          const double f = rinv(sj - si), g = rinv(sj + si);
+          out = 0.5 * (f + g) * (pij - pji) + 0.5 * (f - g) * (qij - qji);
+        } else {
+          out = gS ? gS[r[4] + i] : 0.0;
+        }
+        if (kind == 1) out -= rinv(si) * qji;
+        else if (kind == 2) out -= pij * rinv(sj);
+        Kb[i * k + j] = out;
+      }
+    } else {
+      const int64_t f = e - kk;
+      T* tr = TR + r[7];
+      if (kind == 0) {
+        if constexpr (Cx) tr[f] = make_double2(0.0, 0.0); else tr[f] = 0.0;
+      } else if (kind == 1) {  // k x n: row i scaled by sinv_i
+        const int64_t i = f / n;
+        const double w = rinv(s[i]);
+        const T g = gVh[r[5] + f];
+        if constexpr (Cx) tr[f] = make_double2(g.x * w, g.y * w); else tr[f] = g * w;
+      } else {  // m x k: column j scaled by sinv_j
+        const int64_t j = f % k;
+        const double w = rinv(s[j]);
+        const T g = gU[r[3] + f];
+        if constexpr (Cx) tr[f] = make_double2(g.x * w, g.y * w); else tr[f] = g * w;
+      }
+    }
+  }
+}
+
+}  // namespace
+}  // namespace yb
+
+extern "C" int yb_svd_adjoint_core(const void* P, const void* Q, const double* S, const double* gS, void* K,
+                                   const void* gU, const void* gVh, void* TR, const int64_t* blocks, int n_blocks,
+                                   int dtype, void* stream) {
+  if (n_blocks == 0) return YB_OK;
+  if (!P || !Q || !S || !K || !gU || !gVh || !TR || !blocks) return YB_ERR_INVALID;
+  dim3 grid(32, (unsigned)n_blocks);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == YB_F64)
+    yb::svd_adjoint_core_kernel<false><<<grid, 256, 0, s>>>((const double*)P, (const double*)Q, S, gS, (double*)K,
+                                                            (const double*)gU, (const double*)gVh, (double*)TR,
+                                                            blocks);
+  else if (dtype == YB_C128)
+    yb::svd_adjoint_core_kernel<true><<<grid, 256, 0, s>>>((const double2*)P, (const double2*)Q, S, gS, (double2*)K,
+                                                           (const double2*)gU, (const double2*)gVh, (double2*)TR,
+                                                           blocks);
+  else
+    return YB_ERR_INVALID;
+  return yb::check_launch();
+}

@@ -1,0 +1,106 @@
+// Family (a): one-launch strided block copies (merge / unmerge / their adjoints).
+//
+// The host compiles YASTN's merge metadata (meta_new/meta_mrg of transpose_and_merge,
+// the unmerge records) into copy tasks: each task is an n-dim strided copy whose
+// extents are the transposed source block and whose source/destination strides map
+// the permutation, the reshape to the fused block and its sub-slice offset. Dims that
+// are contiguous in both source and destination are collapsed on the host, and pairs
+// of FP64 elements are moved as one 16-byte unit when every offset and stride allows.
+//
+// Work is split into items of up to YB_COPY_ITEM_UNITS units of one task; one CTA
+// handles one item. Within an item consecutive threads take consecutive units of the
+// innermost dim (destination-contiguous after collapsing), so stores are coalesced.
+#include "yb_common.cuh"
+
+namespace yb {
+
+static thread_local int g_last_cuda_error = 0;
+void set_cuda_error(int code) { g_last_cuda_error = code; }
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kIlp = 4;
+
+template <typename Unit>
+__device__ __forceinline__ void copy_units(const Unit* __restrict__ src, Unit* __restrict__ dst, const int64_t* rec,
+                                           int64_t first) {
+  const int ndim = (int)rec[YB_CP_NDIM];
+  const int64_t count = rec[YB_CP_COUNT];
+  const int64_t n = min((int64_t)YB_COPY_ITEM_UNITS, count - first);
+  const int64_t sbase = rec[YB_CP_SRC];
+  const int64_t dbase = rec[YB_CP_DST];
+  for (int64_t e0 = threadIdx.x; e0 < n; e0 += (int64_t)kThreads * kIlp) {
+    Unit v[kIlp];
+    int64_t doff[kIlp];
+#pragma unroll
+    for (int j = 0; j < kIlp; ++j) {
+      const int64_t e = e0 + (int64_t)j * kThreads;
+      doff[j] = -1;
+      if (e < n) {
+        uint32_t idx = (uint32_t)(first + e);
+        int64_t so = sbase, dof = dbase;
+#pragma unroll
+        for (int d = YB_CP_MAXD - 1; d >= 0; --d) {
+          if (d < ndim) {
+            const uint32_t size = (uint32_t)rec[YB_CP_SIZE + d];
+            const uint32_t q = fast_div(idx, (uint32_t)rec[YB_CP_MAGIC + d], (uint32_t)rec[YB_CP_SHIFT + d]);
+            const int64_t r = (int64_t)(idx - q * size);
+            so += r * rec[YB_CP_SSTR + d];
+            dof += r * rec[YB_CP_DSTR + d];
+            idx = q;
+          }
+        }
+        v[j] = __ldg(src + so);
+        doff[j] = dof;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kIlp; ++j)
+      if (doff[j] >= 0) dst[doff[j]] = v[j];
+  }
+}
+
+// Elem is the element type of the data (double for FP64, double2 for complex128). FP64
+// tasks flagged YB_CP_VEC move pairs of elements as one 16-byte unit.
+template <typename Elem>
+__global__ void __launch_bounds__(kThreads) block_copy_kernel(const Elem* __restrict__ src, Elem* __restrict__ dst,
+                                                               const int64_t* __restrict__ tasks,
+                                                               const int64_t* __restrict__ items) {
+  __shared__ int64_t rec[YB_COPY_REC];
+  const int64_t* item = items + 2 * (int64_t)blockIdx.x;
+  const int64_t task = item[0];
+  const int64_t first = item[1];
+  if (threadIdx.x < YB_COPY_REC) rec[threadIdx.x] = tasks[task * YB_COPY_REC + threadIdx.x];
+  __syncthreads();
+  if (sizeof(Elem) == 8 && rec[YB_CP_VEC] != 0)
+    copy_units<double2>(reinterpret_cast<const double2*>(src), reinterpret_cast<double2*>(dst), rec, first);
+  else
+    copy_units<Elem>(src, dst, rec, first);
+}
+
+}  // namespace
+}  // namespace yb
+
+extern "C" {
+
+int yb_abi_version(void) { return 100; }
+int yb_last_cuda_error(void) { return yb::g_last_cuda_error; }
+
+int yb_block_copy(const void* src, void* dst, int unit_bytes, const int64_t* tasks, int n_tasks,
+                  const int64_t* items, int n_items, void* stream) {
+  if (n_items == 0) return YB_OK;
+  if (!src || !dst || !tasks || !items || n_tasks <= 0 || n_items < 0) return YB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  dim3 grid((unsigned)n_items);
+  if (unit_bytes == 8) {
+    yb::block_copy_kernel<double><<<grid, yb::kThreads, 0, s>>>((const double*)src, (double*)dst, tasks, items);
+  } else if (unit_bytes == 16) {
+    yb::block_copy_kernel<double2><<<grid, yb::kThreads, 0, s>>>((const double2*)src, (double2*)dst, tasks, items);
+  } else {
+    return YB_ERR_INVALID;
+  }
+  return yb::check_launch();
+}
+
+}  // extern "C"

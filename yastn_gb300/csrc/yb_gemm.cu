@@ -1,0 +1,158 @@
+// Family (b): grouped sum-of-products GEMM over charge sectors, native FP64 / complex128.
+//
+//   C_o = alpha * sum_{t in terms(o)} op(A_t) op(B_t) + beta * C_o
+//
+// One launch covers every 64x64 output tile of every sector; the host orders tiles
+// largest-K first so that the long tiles start early. On GB300 FP64 arithmetic runs at
+// about 1.2 TFLOP/s on the DFMA pipe (the DMMA m8n8k4 tensor path measured slower),
+// so a register-tiled DFMA kernel with shared-memory staging is FP64-bound: each thread
+// owns a 4x4 sub-tile and issues 16 independent FMAs per staged k.
+#include "yb_common.cuh"
+
+namespace yb {
+namespace {
+
+constexpr int kTile = YB_GEMM_TILE;  // 64
+constexpr int kK = 16;
+constexpr int kThreads = 256;
+constexpr int kPad = 2;
+
+struct Real {
+  using T = double;
+  __device__ static T zero() { return 0.0; }
+  __device__ static T conj(T a) { return a; }
+  __device__ static void fma(T& acc, T a, T b) { acc = ::fma(a, b, acc); }
+  __device__ static T scale(T a, double s) { return a * s; }
+  __device__ static T add(T a, T b) { return a + b; }
+};
+
+struct Cplx {
+  using T = double2;
+  __device__ static T zero() { return make_double2(0.0, 0.0); }
+  __device__ static T conj(T a) { return make_double2(a.x, -a.y); }
+  __device__ static void fma(T& acc, T a, T b) {
+    acc.x = ::fma(a.x, b.x, acc.x);
+    acc.x = ::fma(-a.y, b.y, acc.x);
+    acc.y = ::fma(a.x, b.y, acc.y);
+    acc.y = ::fma(a.y, b.x, acc.y);
+  }
+  __device__ static T scale(T a, double s) { return make_double2(a.x * s, a.y * s); }
+  __device__ static T add(T a, T b) { return make_double2(a.x + b.x, a.y + b.y); }
+};
+
+template <class F>
+__global__ void __launch_bounds__(kThreads) grouped_gemm_kernel(const typename F::T* __restrict__ A,
+                                                                 const typename F::T* __restrict__ B,
+                                                                 typename F::T* __restrict__ C,
+                                                                 const int64_t* __restrict__ outs,
+                                                                 const int64_t* __restrict__ terms,
+                                                                 const int32_t* __restrict__ tiles,
+                                                                 double alpha, double beta) {
+  using T = typename F::T;
+  __shared__ T As[kK][kTile + kPad];
+  __shared__ T Bs[kK][kTile + kPad];
+
+  const int4 tl = reinterpret_cast<const int4*>(tiles)[blockIdx.x];
+  const int64_t* orec = outs + (int64_t)tl.x * YB_GEMM_OUT_REC;
+  const int64_t c_off = orec[0], m = orec[1], n = orec[2], ldc = orec[3];
+  const int64_t t0 = orec[4], t1 = orec[5];
+  const int64_t row0 = (int64_t)tl.y * kTile, col0 = (int64_t)tl.z * kTile;
+
+  const int tx = threadIdx.x & 15;  // column group
+  const int ty = threadIdx.x >> 4;  // row group
+  T acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = F::zero();
+
+  for (int64_t t = t0; t < t1; ++t) {
+    const int64_t* trec = terms + t * YB_GEMM_TERM_REC;
+    const int64_t a_off = trec[0], b_off = trec[1], K = trec[2];
+    const int64_t a_rs = trec[3], a_cs = trec[4], b_rs = trec[5], b_cs = trec[6];
+    const int flags = (int)trec[7];
+    const bool conjA = flags & 1, conjB = flags & 2;
+    const bool a_kfast = (a_cs == 1);  // k is the contiguous index of A
+    const bool b_jfast = (b_cs == 1) || (b_rs != 1);
+    for (int64_t k0 = 0; k0 < K; k0 += kK) {
+      // stage A tile: 64 rows x 16 k
+#pragma unroll
+      for (int r = 0; r < (kTile * kK) / kThreads; ++r) {
+        const int e = threadIdx.x + r * kThreads;
+        int i, l;
+        if (a_kfast) { l = e % kK; i = e / kK; } else { i = e % kTile; l = e / kTile; }
+        const int64_t gi = row0 + i, gl = k0 + l;
+        T v = F::zero();
+        if (gi < m && gl < K) {
+          v = A[a_off + gi * a_rs + gl * a_cs];
+          if (conjA) v = F::conj(v);
+        }
+        As[l][i] = v;
+      }
+      // stage B tile: 16 k x 64 cols
+#pragma unroll
+      for (int r = 0; r < (kTile * kK) / kThreads; ++r) {
+        const int e = threadIdx.x + r * kThreads;
+        int j, l;
+        if (b_jfast) { j = e % kTile; l = e / kTile; } else { l = e % kK; j = e / kK; }
+        const int64_t gj = col0 + j, gl = k0 + l;
+        T v = F::zero();
+        if (gj < n && gl < K) {
+          v = B[b_off + gl * b_rs + gj * b_cs];
+          if (conjB) v = F::conj(v);
+        }
+        Bs[l][j] = v;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int l = 0; l < kK; ++l) {
+        T a[4], b[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a[i] = As[l][ty * 4 + i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) b[j] = Bs[l][tx * 4 + j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) F::fma(acc[i][j], a[i], b[j]);
+      }
+      __syncthreads();
+    }
+  }
+  // epilogue
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int64_t gi = row0 + ty * 4 + i;
+    if (gi >= m) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t gj = col0 + tx * 4 + j;
+      if (gj >= n) continue;
+      T* p = C + c_off + gi * ldc + gj;
+      T v = F::scale(acc[i][j], alpha);
+      if (beta != 0.0) v = F::add(v, F::scale(*p, beta));
+      *p = v;
+    }
+  }
+}
+
+}  // namespace
+}  // namespace yb
+
+extern "C" int yb_grouped_gemm(const void* a, const void* b, void* c, int dtype, const int64_t* outs,
+                               const int64_t* terms, const int32_t* tiles, int n_tiles, double alpha,
+                               double beta, void* stream) {
+  if (n_tiles == 0) return YB_OK;
+  if (!a || !b || !c || !outs || !tiles || n_tiles < 0) return YB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == YB_F64) {
+    yb::grouped_gemm_kernel<yb::Real><<<n_tiles, yb::kThreads, 0, s>>>(
+        (const double*)a, (const double*)b, (double*)c, outs, terms, tiles, alpha, beta);
+  } else if (dtype == YB_C128) {
+    yb::grouped_gemm_kernel<yb::Cplx><<<n_tiles, yb::kThreads, 0, s>>>(
+        (const double2*)a, (const double2*)b, (double2*)c, outs, terms, tiles, alpha, beta);
+  } else {
+    return YB_ERR_INVALID;
+  }
+  return yb::check_launch();
+}

@@ -1,0 +1,394 @@
+"""Device operations of the hot path: torch tensors in, C ABI calls, torch tensors out.
+
+Every function here launches the hand-written sm_103a kernels of
+``libyastn_gb300.so`` on torch's current CUDA stream. Inputs must be contiguous 1-D
+CUDA tensors of dtype float64 or complex128; anything else raises (there is no
+fallback path).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native as N
+from . import _plans as P
+
+_SUPPORTED = (torch.float64, torch.complex128)
+MAX_SWEEPS = 64
+
+
+def _vp(x):
+    return ctypes.c_void_p(x)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _dtype_code(dtype):
+    if dtype == torch.float64:
+        return N.YB_F64
+    if dtype == torch.complex128:
+        return N.YB_C128
+    raise NotImplementedError(f"yastn_gb300 kernels support float64 and complex128, got {dtype}")
+
+
+def _check(t, name='data'):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor (yastn_gb300 has no CPU path)")
+    if t.dtype not in _SUPPORTED:
+        raise NotImplementedError(f"yastn_gb300 kernels support float64 and complex128, got {t.dtype}")
+    if t.dim() != 1 or not t.is_contiguous():
+        t = t.reshape(-1).contiguous()
+    return t
+
+
+def _dev(plan, key, arrays, device):
+    """Device copies of a plan's packed arrays, cached on the plan per device."""
+    k = (key, str(device))
+    d = plan._dev.get(k)
+    if d is None:
+        d = tuple(torch.from_numpy(np.ascontiguousarray(a)).to(device) for a in arrays)
+        plan._dev[k] = d
+    return d
+
+
+# ----------------------------------------------------------------------------- family (a)
+
+def run_copy(plan, src, dst):
+    """Run a CopyPlan from ``src`` into ``dst`` (both 1-D, same dtype)."""
+    vec_ok = src.dtype == torch.float64 and src.data_ptr() % 16 == 0 and dst.data_ptr() % 16 == 0
+    tasks, items = plan.packed(vec_ok)
+    if len(items) == 0:
+        return dst
+    dt, di = _dev(plan, ('copy', vec_ok), (tasks, items), src.device)
+    N.call('yb_block_copy', _ptr(src), _ptr(dst), src.element_size(), _ptr(dt), len(tasks), _ptr(di), len(items),
+           _stream())
+    return dst
+
+
+def merge(data, order, meta_new, meta_mrg, Dsize):
+    """transpose_and_merge: fused blocks, zero where no source block lands."""
+    data = _check(data)
+    plan = P.merge_plan(order, meta_new, meta_mrg, Dsize)
+    out = (torch.empty if plan.full else torch.zeros)(Dsize, dtype=data.dtype, device=data.device)
+    return run_copy(plan, data, out)
+
+
+def merge_backward(data_b, order, meta_new, meta_mrg, Dsize, D_source):
+    data_b = _check(data_b)
+    plan = P.merge_plan(order, meta_new, meta_mrg, Dsize)
+    inv = P.CACHE.get((order, meta_new, meta_mrg), ('merge_bwd', Dsize, D_source), lambda: plan.swapped(D_source))
+    out = (torch.empty if inv.full else torch.zeros)(D_source, dtype=data_b.dtype, device=data_b.device)
+    return run_copy(inv, data_b, out)
+
+
+def unmerge(data, meta):
+    data = _check(data)
+    plan = P.unmerge_plan(meta, data.numel())
+    out = (torch.empty if plan.full else torch.zeros)(data.numel(), dtype=data.dtype, device=data.device)
+    return run_copy(plan, data, out)
+
+
+def unmerge_backward(data_b, meta, fwd_size):
+    data_b = _check(data_b)
+    plan = P.unmerge_plan(meta, fwd_size)
+    inv = P.CACHE.get((meta,), ('unmerge_bwd', fwd_size), lambda: plan.swapped(fwd_size))
+    out = (torch.empty if inv.full else torch.zeros)(fwd_size, dtype=data_b.dtype, device=data_b.device)
+    return run_copy(inv, data_b, out)
+
+
+def transpose(data, axes, meta_transpose):
+    data = _check(data)
+    plan = P.transpose_plan(axes, meta_transpose, data.numel())
+    out = (torch.empty if plan.full else torch.zeros)(data.numel(), dtype=data.dtype, device=data.device)
+    return run_copy(plan, data, out)
+
+
+def transpose_backward(data_b, axes, meta_transpose):
+    data_b = _check(data_b)
+    plan = P.transpose_plan(axes, meta_transpose, data_b.numel())
+    inv = P.CACHE.get((axes, meta_transpose), ('transpose_bwd', data_b.numel()), lambda: plan.swapped(data_b.numel()))
+    out = (torch.empty if inv.full else torch.zeros)(data_b.numel(), dtype=data_b.dtype, device=data_b.device)
+    return run_copy(inv, data_b, out)
+
+
+# ----------------------------------------------------------------------------- family (b)
+
+def run_gemm(plan, a, b, c, alpha=1.0, beta=0.0):
+    if len(plan.tiles) == 0:
+        return c
+    do, dtm, dti = _dev(plan, 'gemm', (plan.outs, plan.terms, plan.tiles), a.device)
+    N.call('yb_grouped_gemm', _ptr(a), _ptr(b), _ptr(c), _dtype_code(c.dtype), _ptr(do), _ptr(dtm), _ptr(dti),
+           len(plan.tiles), float(alpha), float(beta), _stream())
+    return c
+
+
+def promote(A, B):
+    dtype = torch.promote_types(A.dtype, B.dtype)
+    return (A if A.dtype == dtype else A.to(dtype)), (B if B.dtype == dtype else B.to(dtype))
+
+
+def dot(A, B, meta_dot, Dsize):
+    A, B = promote(_check(A, 'A'), _check(B, 'B'))
+    plan = P.dot_plan(meta_dot)
+    out = torch.zeros(Dsize, dtype=A.dtype, device=A.device)
+    return run_gemm(plan, A, B, out)
+
+
+def dot_backward(C_b, A, B, meta_dot, need_a=True, need_b=True):
+    A, B = promote(_check(A, 'A'), _check(B, 'B'))
+    C_b = _check(C_b, 'C_b')
+    if C_b.dtype != A.dtype:
+        C_b = C_b.to(A.dtype)
+    pa, pb = P.dot_backward_plans(meta_dot)
+    A_b = B_b = None
+    if need_a:
+        A_b = run_gemm(pa, C_b, B, torch.zeros(A.numel(), dtype=A.dtype, device=A.device))
+    if need_b:
+        B_b = run_gemm(pb, A, C_b, torch.zeros(B.numel(), dtype=A.dtype, device=A.device))
+    return A_b, B_b
+
+
+def permute_blocks(data, reshape, order):
+    """Blocks (sl, Di, Dl, Dr) of ``data`` permuted by ``order`` into consecutive (Dl, Dr)
+    matrices; returns (buffer, offsets, plan)."""
+    def build():
+        tasks, offs, low = [], [], 0
+        for sl, Di, Dl, Dr in reshape:
+            sst = P.row_major_strides(Di)
+            Dt = [Di[o] for o in order]
+            tasks.append((sl[0], low, Dt, [sst[o] for o in order], P.row_major_strides(Dt)))
+            offs.append(low)
+            low += Dl * Dr
+        return P.CopyPlan(tasks, low, low), tuple(offs)
+    plan, offs = P.CACHE.get((reshape, order), ('permute_blocks',), build)
+    buf = torch.empty(plan.size_dst, dtype=data.dtype, device=data.device)
+    return run_copy(plan, data, buf), offs, plan
+
+
+def transpose_dot_sum(A, B, meta_dot, Areshape, Breshape, Aorder, Border, Dsize):
+    A, B = promote(_check(A, 'A'), _check(B, 'B'))
+    Ap, Aoffs, _ = permute_blocks(A, Areshape, Aorder)
+    Bp, Boffs, _ = permute_blocks(B, Breshape, Border)
+    plan = P.tds_plan(meta_dot, Areshape, Breshape, Aoffs, Boffs)
+    out = torch.zeros(Dsize, dtype=A.dtype, device=A.device)
+    return run_gemm(plan, Ap, Bp, out)
+
+
+def transpose_dot_sum_backward(C_b, A, B, meta_dot, Areshape, Breshape, Aorder, Border):
+    A, B = promote(_check(A, 'A'), _check(B, 'B'))
+    C_b = _check(C_b, 'C_b').to(A.dtype)
+    Ap, Aoffs, pa_perm = permute_blocks(A, Areshape, Aorder)
+    Bp, Boffs, pb_perm = permute_blocks(B, Breshape, Border)
+    pa, pb = P.tds_backward_plans(meta_dot, Areshape, Breshape, Aoffs, Boffs)
+    At_b = run_gemm(pa, C_b, Bp, torch.zeros(Ap.numel(), dtype=A.dtype, device=A.device))
+    Bt_b = run_gemm(pb, Ap, C_b, torch.zeros(Bp.numel(), dtype=A.dtype, device=A.device))
+    inv_a = P.CACHE.get((Areshape, Aorder), ('permute_blocks_bwd', A.numel()), lambda: pa_perm.swapped(A.numel()))
+    inv_b = P.CACHE.get((Breshape, Border), ('permute_blocks_bwd', B.numel()), lambda: pb_perm.swapped(B.numel()))
+    A_b = run_copy(inv_a, At_b, (torch.empty if inv_a.full else torch.zeros)(A.numel(), dtype=A.dtype, device=A.device))
+    B_b = run_copy(inv_b, Bt_b, (torch.empty if inv_b.full else torch.zeros)(B.numel(), dtype=A.dtype, device=A.device))
+    return A_b, B_b
+
+
+# ----------------------------------------------------------------------------- family (c)
+
+def _jacobi(data, plan, U, S, V, mode, max_sweeps, tol_scale):
+    """Run the batched Jacobi of ``plan`` on ``data`` and write U, S (and Vh for mode 0)."""
+    nb = len(plan.blocks)
+    dev = data.device
+    code = _dtype_code(data.dtype)
+    dblocks, dpairs = _dev(plan, 'svd', (plan.blocks, plan.pair_items), dev)
+    work = torch.empty(plan.work_elems, dtype=data.dtype, device=dev)
+    counters = torch.empty(2 * nb, dtype=torch.int64, device=dev)
+    shift = torch.empty(nb, dtype=torch.float64, device=dev) if mode != 0 else None
+    st = _stream()
+    N.call('yb_svd_init', _ptr(data), _ptr(work), _ptr(dblocks), nb, code, _ptr(counters),
+           _vp(shift.data_ptr() if shift is not None else 0), st)
+    converged = False
+    for sweep in range(max_sweeps):
+        N.call('yb_svd_sweep', _ptr(work), _ptr(dblocks), nb, _ptr(dpairs), len(plan.pair_items), plan.max_rounds,
+               code, float(tol_scale), _ptr(counters), st)
+        if sweep >= 2 and int(counters[:nb].max().item()) == 0:
+            converged = True
+            break
+    if not converged:
+        raise torch.linalg.LinAlgError(f"yastn_gb300: Jacobi did not converge in {max_sweeps} sweeps")
+    N.call('yb_svd_finalize', _ptr(work), _ptr(U), _ptr(S), _vp(V.data_ptr() if V is not None else 0), _ptr(dblocks),
+           nb, code, plan.max_k, mode, _vp(shift.data_ptr() if shift is not None else 0), st)
+
+
+def svd(data, meta, sizes, max_sweeps=MAX_SWEEPS, tol_scale=1.0):
+    """Thin SVD of every block (one-sided Jacobi); returns (U, S, Vh) flat tensors."""
+    data = _check(data)
+    if _dtype_code(data.dtype) != N.YB_F64:
+        raise NotImplementedError("yastn_gb300 svd: complex128 Jacobi is not implemented yet")
+    dev = data.device
+    U = torch.empty(sizes[0], dtype=data.dtype, device=dev)
+    S = torch.empty(sizes[1], dtype=torch.float64, device=dev)
+    V = torch.empty(sizes[2], dtype=data.dtype, device=dev)
+    plan = P.svd_plan(meta)
+    if len(plan.blocks) == 0:
+        return U, S, V
+    _jacobi(data, plan, U, S, V, 0, max_sweeps, tol_scale)
+    return U, S, V
+
+
+def svd_backward(U, S, V, gU, gS, gV, meta, data_size, dtype):
+    """Regularised SVD adjoint of every block (torch_svd_gesdd.py:296-428) in 7 launches."""
+    plan = P.svd_adjoint_plan(meta)
+    dev = U.device
+    dA = torch.zeros(data_size, dtype=dtype, device=dev)
+    if len(plan.recs) == 0:
+        return dA
+    code = _dtype_code(U.dtype)
+    gU = torch.zeros_like(U) if gU is None else gU.contiguous().to(U.dtype)
+    gV = torch.zeros_like(V) if gV is None else gV.contiguous().to(V.dtype)
+    gS = None if gS is None else gS.contiguous().to(torch.float64)
+    Pm = torch.empty(plan.kk, dtype=U.dtype, device=dev)
+    Qm = torch.empty(plan.kk, dtype=U.dtype, device=dev)
+    Km = torch.empty(plan.kk, dtype=U.dtype, device=dev)
+    TR = torch.empty(max(plan.tr, 1), dtype=U.dtype, device=dev)
+    run_gemm(plan.gP, U, gU, Pm)
+    run_gemm(plan.gQ, V, gV, Qm)
+    (drecs,) = _dev(plan, 'adj', (plan.recs,), dev)
+    N.call('yb_svd_adjoint_core', _ptr(Pm), _ptr(Qm), _ptr(S), _vp(gS.data_ptr() if gS is not None else 0), _ptr(Km),
+           _ptr(gU), _ptr(gV), _ptr(TR), _ptr(drecs), len(plan.recs), code, _stream())
+    run_gemm(plan.gT, Km, V, TR, beta=1.0)
+    run_gemm(plan.gR, U, Km, TR, beta=1.0)
+    run_gemm(plan.gA1, U, TR, dA)
+    run_gemm(plan.gA2, TR, V, dA)
+    if not (dtype.is_complex if hasattr(dtype, 'is_complex') else False) and dA.is_complex():
+        dA = dA.real.contiguous()
+    return dA
+
+
+def eigh(data, meta, sizes, order_by_magnitude=False, max_sweeps=MAX_SWEEPS):
+    """Symmetric eigendecomposition of every block (records (sl, D, slU, DU, slS) of
+    yastn/backend/backend_np.py:461-474): eigenvalues ascending, or by descending
+    magnitude when ``order_by_magnitude`` (yastn/backend/linalg/torch_eig_sym.py:25-32)."""
+    data = _check(data)
+    if _dtype_code(data.dtype) != N.YB_F64:
+        raise NotImplementedError("yastn_gb300 eigh: complex128 (Hermitian) Jacobi is not implemented yet")
+    if data.requires_grad:
+        raise NotImplementedError("yastn_gb300 eigh: the adjoint is not implemented yet")
+    dev = data.device
+    S = torch.zeros(sizes[0], dtype=torch.float64, device=dev)
+    U = torch.zeros(sizes[1], dtype=data.dtype, device=dev)
+    svd_meta = tuple((sl, D, slU, DU, slS, (0, 0), (DU[1], D[1])) for sl, D, slU, DU, slS in meta)
+    plan = P.svd_plan(svd_meta)
+    if len(plan.blocks) == 0:
+        return S, U
+    _jacobi(data, plan, U, S, None, 2 if order_by_magnitude else 1, max_sweeps, 1.0)
+    return S, U
+
+
+def fix_svd_signs(U, V, meta):
+    """Gauge fix of every block; returns (U', Vh', phases)."""
+    U, V = _check(U, 'U'), _check(V, 'V')
+    plan = P.svd_plan(meta)
+    nb = len(plan.blocks)
+    Uo, Vo = torch.empty_like(U), torch.empty_like(V)
+    S_size = max((int(r[4] + r[9]) for r in plan.blocks), default=0)
+    phases = torch.zeros(S_size, dtype=U.dtype, device=U.device)
+    if nb == 0:
+        return U.clone(), V.clone(), phases
+    (dblocks,) = _dev(plan, 'svd_blocks', (plan.blocks,), U.device)
+    N.call('yb_fix_signs', _ptr(U), _ptr(V), _ptr(Uo), _ptr(Vo), _ptr(phases), _ptr(dblocks), nb, plan.max_k,
+           _dtype_code(U.dtype), 0, _stream())
+    return Uo, Vo, phases
+
+
+def fix_svd_signs_backward(gU, gV, phases, meta):
+    """Adjoint of the real gauge fix: cotangents multiplied by the same +-1 phases."""
+    plan = P.svd_plan(meta)
+    nb = len(plan.blocks)
+    gU = torch.zeros(0) if gU is None else gU
+    gV = torch.zeros(0) if gV is None else gV
+    outs = []
+    for g, is_u in ((gU, True), (gV, False)):
+        outs.append(None if g.numel() == 0 else g.contiguous().clone())
+    if nb == 0:
+        return outs[0], outs[1]
+    (dblocks,) = _dev(plan, 'svd_blocks', (plan.blocks,), phases.device)
+    Ui = outs[0] if outs[0] is not None else torch.zeros(int(max((r[3] + r[1] * r[9]) for r in plan.blocks)),
+                                                           dtype=phases.dtype, device=phases.device)
+    Vi = outs[1] if outs[1] is not None else torch.zeros(int(max((r[5] + r[9] * r[2]) for r in plan.blocks)),
+                                                           dtype=phases.dtype, device=phases.device)
+    N.call('yb_fix_signs', _ptr(Ui), _ptr(Vi), _ptr(Ui), _ptr(Vi), _ptr(phases), _ptr(dblocks), nb, plan.max_k,
+           _dtype_code(Ui.dtype), 1, _stream())
+    return (Ui if outs[0] is not None else None), (Vi if outs[1] is not None else None)
+
+
+# ----------------------------------------------------------------------------- masks / truncation
+
+def _idx_buffer(mask, meta, device):
+    order, lengths, off = [], {}, 0
+    for rec in meta:
+        tm = rec[4]
+        if tm not in lengths:
+            v = mask[tm]
+            n = int(v.numel()) if isinstance(v, torch.Tensor) else len(v)
+            lengths[tm] = (off, n)
+            order.append(torch.as_tensor(v, device=device).reshape(-1).to(torch.int64))
+            off += n
+    idx = torch.cat(order) if order else torch.zeros(1, dtype=torch.int64, device=device)
+    return idx, lengths
+
+
+def apply_mask(A, mask, meta, Dsize, axis, ndim, scatter_size=None):
+    """Gather kept indices along ``axis`` (scatter_size given: the adjoint scatter)."""
+    A = _check(A)
+    idx, lengths = _idx_buffer(mask, meta, A.device)
+    recs, items, _ = P.mask_plan(meta, axis, lengths)
+    if scatter_size is None:
+        out = torch.empty(Dsize, dtype=A.dtype, device=A.device)
+    else:
+        out = torch.zeros(scatter_size, dtype=A.dtype, device=A.device)
+    if len(items) == 0:
+        return out
+    drecs = torch.from_numpy(recs).to(A.device)
+    ditems = torch.from_numpy(items).to(A.device)
+    N.call('yb_mask_gather', _ptr(A), _ptr(out), A.element_size(), _ptr(drecs), _ptr(ditems), len(items), _ptr(idx),
+           int(scatter_size is not None), _stream())
+    return out
+
+
+def truncation_mask_data(S, slices, charges=None, tol=0, tol_block=0, D_block=float('inf'), D_total=float('inf'),
+                         truncate_multiplets=False):
+    """The truncation rule of yastn/tensor/linalg.py:637-735 in one device launch.
+
+    ``S`` is the flat float64 spectrum on the device, ``slices`` the (start, stop) of
+    each block, ``charges`` the block charges (needed when tol_block/D_block are dicts).
+    Returns (mask: bool CUDA tensor, kept: list of kept counts per block).
+    """
+    S = _check(S, 'S')
+    if S.dtype != torch.float64:
+        raise TypeError("truncation requires a real float64 spectrum")
+    n = S.numel()
+    nb = len(slices)
+    if truncate_multiplets:
+        tol_block, D_block = 0, float('inf')
+    blk = np.zeros((max(nb, 1), 4), dtype=np.int64)
+    tb = np.zeros(max(nb, 1), dtype=np.float64)
+    tol_null = 0. if isinstance(tol_block, dict) else tol_block
+    D_null = 0 if isinstance(D_block, dict) else D_block
+    for i, (lo, hi) in enumerate(slices):
+        t = tuple(charges[i]) if charges is not None else None
+        tb[i] = tol_block[t] if (isinstance(tol_block, dict) and t in tol_block) else tol_null
+        d = D_block[t] if (isinstance(D_block, dict) and t in D_block) else D_null
+        blk[i] = (lo, hi, -1 if d == float('inf') else int(d), 0)
+    dt = -1 if D_total == float('inf') else int(D_total)
+    mask = torch.empty(n, dtype=torch.uint8, device=S.device)
+    kept = torch.empty(max(nb, 1), dtype=torch.int64, device=S.device)
+    if nb == 0 or n == 0:
+        return mask.bool(), [0] * nb
+    dblk = torch.from_numpy(blk).to(S.device)
+    dtb = torch.from_numpy(tb).to(S.device)
+    N.call('yb_truncation_mask', _ptr(S), n, _ptr(dblk), _ptr(dtb), nb, float(tol), dt, int(bool(truncate_multiplets)),
+           _ptr(mask), _ptr(kept), _stream())
+    return mask.view(torch.bool), kept[:nb].tolist()
