@@ -1,0 +1,338 @@
+#!/usr/bin/env python
+"""Benchmark of the yastn_gb300 hot path on one or more GB300 GPUs (replicas).
+
+Workload (default ``--workload cfg1``): YASTN ``tensordot`` of two U(1) rank-4 FP64
+tensors, every leg D=64 over charges -3..3 (sector dims 2,7,14,18,14,7,2), contracting
+A's legs (2,3) with B's legs (0,1) under the fuse-to-matrix policy: merge A, merge B,
+one grouped GEMM over the 13 charge sectors (3.248 GFLOP), unmerge C. It is driven
+through the backend module with the metadata YASTN itself produced (recorded fixture)
+and data regenerated from YASTN's seeded normal draws. The same workload's truncated
+block SVD (svd_with_truncation, D_total=64) is timed as an extra field.
+
+One JSON line is printed by rank 0. ``--impl reference`` times the CPU restatement of
+the reference NumPy backend on the host cores for the same workload instead.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "tensordot TFLOP/s (block-sparse FP64, U(1) rank-4 D=64)"
+UNIT = "TFLOP/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument('--gpus', type=int, default=1)
+    p.add_argument('--steps', type=int, default=20)
+    p.add_argument('--warmup', type=int, default=5)
+    p.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    p.add_argument('--workload', default='cfg1', choices=['cfg1'])
+    p.add_argument('--no-svd', action='store_true', help='skip the extra svd_with_truncation timing')
+    return p.parse_args()
+
+
+# ----------------------------------------------------------------------------- workload (host side)
+
+class Cfg1:
+    name = "U(1) rank-4 D=64 tensordot A(2,3)xB(0,1), fuse_to_matrix, 13 sectors, FP64"
+
+    def __init__(self):
+        from yastn_gb300.workloads import load_trace, cfg1_inputs
+        from yastn_gb300 import _plans as P
+        self.tr = load_trace('cfg1')
+        self.A, self.B = cfg1_inputs(self.tr)
+        c = self.tr['calls']
+        self.mA = c[0]['args'][1:]
+        self.mB = c[1]['args'][1:]
+        self.mdot = c[2]['args'][2:]
+        self.mun = c[3]['args'][1]
+        self.mC = c[4]['args'][1:]
+        self.msvd = c[5]['args'][1:3]
+        self.mU = c[6]['args'][1]
+        self.mV = c[7]['args'][1]
+        self.mask_calls = [x['args'] for x in c[8:11]]
+        self.flops = P.dot_plan(self.mdot[0]).flops
+        self.bytes_merge = 16 * self.A.size  # read + write FP64 per merged element
+
+    # the reference NumPy path, restated by the oracle (CPU)
+    def cpu_step(self):
+        import oracle
+        Am = oracle.transpose_and_merge(self.A, *self.mA)
+        Bm = oracle.transpose_and_merge(self.B, *self.mB)
+        Cm = oracle.dot(Am, Bm, *self.mdot)
+        return oracle.unmerge(Cm, self.mun)
+
+
+def time_cpu(fn, budget_s, min_reps=3):
+    fn()
+    ts = []
+    t_end = time.perf_counter() + budget_s
+    while len(ts) < min_reps or time.perf_counter() < t_end:
+        t0 = time.perf_counter()
+        fn()
+        ts.append(time.perf_counter() - t0)
+    return float(np.median(ts)), len(ts)
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:  # pragma: no cover
+        return os.cpu_count()
+
+
+def run_reference(args, wl):
+    """--impl reference: the reference's NumPy path (oracle restatement) on host cores."""
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return
+    for _ in range(args.warmup):
+        wl.cpu_step()
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        wl.cpu_step()
+        ts.append(time.perf_counter() - t0)
+    t = float(np.mean(ts))
+    value = wl.flops / t / 1e12
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded yastn normal draws)",
+            "config": {"workload": wl.name, "policy": "fuse_to_matrix"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
+                             "sample": f"{args.steps} tensordot steps (numpy BLAS, all host threads)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ----------------------------------------------------------------------------- GPU side
+
+class Clocks:
+    """nvidia-smi clock/throttle samples taken while the timed region runs."""
+
+    def __init__(self, index):
+        self.f = tempfile.NamedTemporaryFile(mode='w+', suffix='.csv', delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(['nvidia-smi', f'--id={index}', f'--query-gpu={q}', '--format=csv,noheader,nounits',
+                                       '-lms', '200'], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:  # pragma: no cover
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(',') for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower() == 'active':
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp64_peak_tflops(torch, dev):
+    """cuBLAS DGEMM throughput on this GPU (4096^3, best of 5) as the FP64 roofline."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    for _ in range(2):
+        a @ b
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a @ b
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best
+
+
+def run_gpu(args, wl):
+    import torch
+    import torch.distributed as dist
+    from yastn_gb300 import backend as BK
+    from yastn_gb300 import ops, _native
+
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    if world > 1:
+        dist.init_process_group('nccl')
+    _native.lib()
+
+    dA = torch.from_numpy(wl.A).to(dev)
+    dB = torch.from_numpy(wl.B).to(dev)
+    hA = torch.from_numpy(wl.A).pin_memory()
+    hB = torch.from_numpy(wl.B).pin_memory()
+    hC = torch.empty(wl.A.size, dtype=torch.float64).pin_memory()
+    flush = torch.empty(L2_FLUSH_BYTES // 8, dtype=torch.float64, device=dev)
+    gemm_ev = []
+
+    def tensordot(a, b, record_gemm=False):
+        Am = BK.transpose_and_merge(a, *wl.mA)
+        Bm = BK.transpose_and_merge(b, *wl.mB)
+        if record_gemm:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+        Cm = BK.dot(Am, Bm, *wl.mdot)
+        if record_gemm:
+            e1.record()
+            gemm_ev.append((e0, e1))
+        return BK.unmerge(Cm, wl.mun)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # parity guard on this device before timing
+    C = tensordot(dA, dB).cpu().numpy()
+    chk = wl.tr['C_checksum']
+    assert abs(float(C.sum()) - chk['sum0']) <= 1e-9 * chk['abs0'], "tensordot result differs from the reference"
+
+    for _ in range(args.warmup):
+        tensordot(dA, dB)
+    barrier()
+    clocks = Clocks(local)
+    ev = []
+    launches0 = _native.LAUNCHES[0]
+    barrier()
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        tensordot(dA, dB, record_gemm=True)
+        e1.record()
+        ev.append((e0, e1))
+    barrier()
+    launches = _native.LAUNCHES[0] - launches0
+    t_step = sum(a.elapsed_time(b) for a, b in ev) / len(ev) * 1e-3
+    t_gemm = sum(a.elapsed_time(b) for a, b in gemm_ev) / len(gemm_ev) * 1e-3
+
+    # end to end through the public API with host buffers (pinned H2D, D2H of C)
+    for _ in range(2):
+        tensordot(hA.to(dev, non_blocking=True), hB.to(dev, non_blocking=True))
+    barrier()
+    e2e_ev = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a = hA.to(dev, non_blocking=True)
+        b = hB.to(dev, non_blocking=True)
+        c = tensordot(a, b)
+        hC.copy_(c, non_blocking=True)
+        e1.record()
+        e2e_ev.append((e0, e1))
+    barrier()
+    clk = clocks.stop()
+    t_e2e = sum(a.elapsed_time(b) for a, b in e2e_ev) / len(e2e_ev) * 1e-3
+
+    # the workload's truncated block SVD (extra field)
+    svd_ms = None
+    if not args.no_svd:
+        C = tensordot(dA, dB)
+
+        def svd_trunc():
+            M = BK.transpose_and_merge(C, *wl.mC)
+            U, S, V = BK.svd(M, *wl.msvd)
+            Uu = BK.unmerge(U, wl.mU)
+            Vu = BK.unmerge(V, wl.mV)
+            slices = sorted(tuple(m[4]) for m in wl.msvd[0])
+            mask, kept = ops.truncation_mask_data(S, slices, None, D_total=64)
+            out = []
+            for (Ain, mask_r, meta, Dsize, axis, ndim), data in zip(wl.mask_calls, (Uu, S, Vu)):
+                dmask = {k: torch.as_tensor(np.asarray(v, dtype=np.int64), device=dev) for k, v in mask_r.items()}
+                out.append(BK.apply_mask(data, dmask, meta, Dsize, axis, ndim))
+            return out, kept
+        svd_trunc()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            _, kept = svd_trunc()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        assert sorted(k for k in kept if k) == sorted(d[0] for d in wl.tr['S_kept_D'])
+        svd_ms = float(np.median(ts)) * 1e3
+
+    # max over ranks
+    t_max = t_step
+    if world > 1:
+        tt = torch.tensor([t_step, t_e2e], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max, t_e2e = float(tt[0]), float(tt[1])
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    peak = fp64_peak_tflops(torch, dev)
+    cpu_t, reps = time_cpu(wl.cpu_step, budget_s=8.0)
+    achieved = wl.flops / t_gemm / 1e12
+    line = {
+        "metric": METRIC, "value": world * wl.flops / t_max / 1e12, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded normal draws as yastn.rand, metadata recorded from yastn)",
+        "config": {"workload": wl.name, "flop_per_step": wl.flops, "parallelism": f"replicas{world}",
+                   "l2": "flushed between timed steps (256 MB write)"},
+        "roofline": {"bound": "tensor", "pipe": "FP64 (DFMA); peak = cuBLAS DGEMM measured live on this GPU",
+                     "kernel": "yb grouped_gemm_kernel<Real>", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None},
+        "cpu_baseline": {"value": wl.flops / cpu_t / 1e12, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
+                         "sample": f"{reps} tensordot steps of the same workload (numpy BLAS, median)"},
+        "e2e": {"value": world * wl.flops / t_e2e / 1e12, "unit": UNIT,
+                "h2d_bytes_per_step": int(wl.A.nbytes + wl.B.nbytes), "d2h_bytes_per_step": int(wl.A.nbytes)},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "extra": {"gemm_ms": t_gemm * 1e3, "svd_with_truncation_ms": svd_ms,
+                  "svd_with_truncation": "merge C, 13-block Jacobi SVD, unmerge U/V, device truncation D_total=64, "
+                                         "3 masks"},
+    }
+    print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    wl = Cfg1()
+    if args.impl == 'reference':
+        run_reference(args, wl)
+    else:
+        run_gpu(args, wl)
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,108 @@
+"""Family (b) on the GPU: grouped sector GEMMs (dot, transpose_dot_sum) and adjoints.
+
+Tolerance: max |C - C_ref| <= 1e-12 * max |C_ref| (FP64, norm-wise relative), the
+reference tests' 1e-12 (tests/tensor/test_tensordot.py:21).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from yastn_gb300 import ops
+from yastn_gb300.workloads import load_trace, cfg1_inputs, GOLDEN, _decode
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def dev(x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def host(t):
+    return t.detach().cpu().numpy()
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)) if b.size else 0.0
+
+
+@pytest.mark.parametrize('name', ['tensordot_fuse_to_matrix', 'tensordot_fuse_contracted', 'tensordot_no_fusion'])
+def test_dot_and_tds_on_reference_calls(name, cuda_device):
+    tr = load_trace(name)
+    n = 0
+    for c in tr['calls']:
+        if c['fn'] == 'dot':
+            A, B, meta, Dsize = c['args']
+            got = host(ops.dot(dev(A), dev(B), meta, Dsize))
+            assert got.dtype == c['out'][0].dtype
+            assert rel(got, c['out'][0]) <= TOL
+            n += 1
+        elif c['fn'] == 'transpose_dot_sum':
+            A, B, meta, Ar, Br, Ao, Bo, Dsize = c['args']
+            got = host(ops.transpose_dot_sum(dev(A), dev(B), meta, Ar, Br, Ao, Bo, Dsize))
+            assert rel(got, c['out'][0]) <= TOL
+            n += 1
+    assert n > 0
+
+
+@pytest.mark.parametrize('name', ['tensordot_fuse_to_matrix', 'tensordot_fuse_contracted'])
+def test_dot_adjoint_matches_oracle(name, cuda_device):
+    tr = load_trace(name)
+    rng = np.random.default_rng(5)
+    for c in tr['calls']:
+        if c['fn'] != 'dot':
+            continue
+        A, B, meta, Dsize = c['args']
+        dtype = np.promote_types(A.dtype, B.dtype)
+        Cb = rng.normal(size=Dsize).astype(dtype)
+        if np.iscomplexobj(Cb):
+            Cb = Cb + 1j * rng.normal(size=Dsize)
+        Ab, Bb = ops.dot_backward(dev(Cb), dev(A), dev(B), meta)
+        Ar, Br = oracle.dot_backward(Cb, A, B, meta)
+        assert rel(host(Ab), Ar) <= TOL and rel(host(Bb), Br) <= TOL
+
+
+def test_dot_golden_adjoint(cuda_device):
+    tr = load_trace('adjoints')
+    A = tr['_arrays']
+    c = [c for c in tr['calls'] if c['fn'] == 'dot_backward'][0]
+    Ab, Bb = ops.dot_backward(dev(A[c['Cb']]), dev(A[c['A']]), dev(A[c['B']]), c['meta'])
+    assert rel(host(Ab), A[c['Ab']]) <= TOL and rel(host(Bb), A[c['Bb']]) <= TOL
+
+
+def test_tds_golden_adjoint(cuda_device):
+    with open(os.path.join(GOLDEN, 'tds_adjoint.json')) as f:
+        args = json.load(f)['args']
+    meta, Ar, Br, Ao, Bo, _ = (_decode(a, None) for a in args)
+    z = np.load(os.path.join(GOLDEN, 'tds_adjoint.npz'))
+    Ab, Bb = ops.transpose_dot_sum_backward(dev(z['Cb']), dev(z['A']), dev(z['B']), meta, Ar, Br, Ao, Bo)
+    assert rel(host(Ab), z['Ab']) <= TOL and rel(host(Bb), z['Bb']) <= TOL
+
+
+def test_dot_empty_and_zero_k(cuda_device):
+    """Sectors with an empty contracted dimension give zero blocks; no sectors give an empty output."""
+    meta = (((0, 6), (2, 3), (0, 0), (2, 0), (0, 0), (0, 3)),)
+    A = torch.zeros(1, dtype=torch.float64, device='cuda')
+    B = torch.zeros(1, dtype=torch.float64, device='cuda')
+    got = host(ops.dot(A, B, meta, 6))
+    np.testing.assert_array_equal(got, np.zeros(6))
+    assert ops.dot(A, B, (), 0).numel() == 0
+
+
+def test_cfg1_full_size_dot(cuda_device):
+    """The benchmark's 13 sector GEMMs (n up to 822, 3.25 GFLOP) vs numpy BLAS."""
+    tr = load_trace('cfg1')
+    A, B = cfg1_inputs(tr)
+    c0, c1, c2 = tr['calls'][:3]
+    Am = oracle.transpose_and_merge(A, *c0['args'][1:])
+    Bm = oracle.transpose_and_merge(B, *c1['args'][1:])
+    _, _, meta, Dsize = c2['args']
+    got = host(ops.dot(dev(Am), dev(Bm), meta, Dsize))
+    ref = oracle.dot(Am, Bm, meta, Dsize)
+    assert rel(got, ref) <= TOL
+    chk = c2['out'][0].checksum
+    assert abs(float(got.sum()) - chk['sum0']) <= 1e-9 * chk['abs0']

@@ -1,0 +1,206 @@
+"""Family (c) on the GPU: block SVD / eigh (Jacobi), truncation, gauge fix, masks.
+
+Singular values and eigenvalues: max |S - S_ref| <= 1e-12 * max S_ref (FP64,
+norm-wise). Singular vectors are checked through gauge-invariant quantities:
+reconstruction |U S Vh - A| <= 1e-12 |A| and orthonormality <= 1e-12 (the reference
+checks reconstruction at 1e-10, tests/tensor/test_svd.py:22). Truncation masks and
+kept dimensions must match exactly.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from yastn_gb300 import ops
+from yastn_gb300.workloads import load_trace, GOLDEN
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def dev(x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def host(t):
+    return t.detach().cpu().numpy()
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)) if b.size else 0.0
+
+
+def check_svd(data, meta, U, S, V, S_ref):
+    assert rel(S, S_ref) <= TOL
+    for sl, D, slU, DU, slS, slV, DV in meta:
+        a = data[sl[0]:sl[1]].reshape(D)
+        u = U[slU[0]:slU[1]].reshape(DU)
+        s = S[slS[0]:slS[1]]
+        vh = V[slV[0]:slV[1]].reshape(DV)
+        if a.size == 0:
+            continue
+        assert np.all(np.diff(s) <= 0), "singular values not descending"
+        assert np.all(s >= 0)
+        scale = max(np.abs(a).max(), 1e-300)
+        assert np.abs((u * s) @ vh - a).max() <= TOL * scale * max(1, min(D))
+        k = DU[1]
+        assert np.abs(u.conj().T @ u - np.eye(k)).max() <= TOL * max(10, k)
+        assert np.abs(vh @ vh.conj().T - np.eye(k)).max() <= TOL * max(10, k)
+
+
+@pytest.mark.parametrize('name', ['svd', 'svd_ill', 'fix_signs'])
+def test_svd_on_reference_calls(name, cuda_device):
+    tr = load_trace(name)
+    n = 0
+    for c in tr['calls']:
+        if c['fn'] != 'svd':
+            continue
+        data, meta, sizes = c['args'][:3]
+        if np.iscomplexobj(data):
+            with pytest.raises(NotImplementedError):
+                ops.svd(dev(data), meta, sizes)
+            continue
+        U, S, V = (host(x) for x in ops.svd(dev(data), meta, sizes))
+        check_svd(data, meta, U, S, V, c['out'][1])
+        n += 1
+    if name != 'fix_signs':
+        assert n > 0
+
+
+def test_svd_vectors_match_oracle_after_gauge_fix(cuda_device):
+    """With distinct singular values the vectors agree with LAPACK's up to the gauge."""
+    rng = np.random.default_rng(7)
+    shapes = [(12, 12), (20, 7), (5, 16), (1, 1), (3, 1)]
+    meta, off, oU, oS, oV = [], 0, 0, 0, 0
+    for m, n in shapes:
+        k = min(m, n)
+        meta.append(((off, off + m * n), (m, n), (oU, oU + m * k), (m, k), (oS, oS + k), (oV, oV + k * n), (k, n)))
+        off += m * n; oU += m * k; oS += k; oV += k * n
+    meta = tuple(meta)
+    data = rng.normal(size=off)
+    U, S, V = ops.svd(dev(data), meta, (oU, oS, oV))
+    Uf, Vf, _ = ops.fix_svd_signs(U, V, meta)
+    Ur, Sr, Vr = oracle.svd(data, meta, (oU, oS, oV))
+    Urf, Vrf = oracle.fix_svd_signs(Ur, Vr, meta)
+    assert rel(host(S), Sr) <= TOL
+    assert rel(host(Uf), Urf) <= 1e-9 and rel(host(Vf), Vrf) <= 1e-9
+
+
+def test_svd_rank_deficient_and_zero_blocks(cuda_device):
+    """Zero singular values: vectors completed to orthonormal sets (LAPACK behaviour)."""
+    rng = np.random.default_rng(8)
+    blocks = [np.zeros((4, 6)), np.outer(rng.normal(size=5), rng.normal(size=3)),
+              rng.normal(size=(6, 2)) @ rng.normal(size=(2, 6)), np.zeros((3, 3))]
+    meta, off, oU, oS, oV, parts = [], 0, 0, 0, 0, []
+    for a in blocks:
+        m, n = a.shape
+        k = min(m, n)
+        meta.append(((off, off + m * n), (m, n), (oU, oU + m * k), (m, k), (oS, oS + k), (oV, oV + k * n), (k, n)))
+        off += m * n; oU += m * k; oS += k; oV += k * n
+        parts.append(a.ravel())
+    meta = tuple(meta)
+    data = np.concatenate(parts)
+    U, S, V = (host(x) for x in ops.svd(dev(data), meta, (oU, oS, oV)))
+    _, Sr, _ = oracle.svd(data, meta, (oU, oS, oV))
+    assert np.abs(S - Sr).max() <= TOL * max(1.0, np.abs(Sr).max())
+    check_svd(data, meta, U, S, V, Sr)
+
+
+def test_svd_empty(cuda_device):
+    U, S, V = ops.svd(torch.zeros(0, dtype=torch.float64, device='cuda'), (), (0, 0, 0))
+    assert U.numel() == S.numel() == V.numel() == 0
+
+
+def test_eigh_on_reference_calls(cuda_device):
+    tr = load_trace('eigh')
+    n = 0
+    for c in tr['calls']:
+        data, meta, sizes = c['args']
+        if np.iscomplexobj(data):
+            continue
+        S, U = (host(x) for x in ops.eigh(dev(data), meta, sizes))
+        assert rel(S, c['out'][0]) <= TOL
+        for sl, D, slU, DU, slS in meta:
+            a = data[sl[0]:sl[1]].reshape(D)
+            u = U[slU[0]:slU[1]].reshape(DU)
+            s = S[slS[0]:slS[1]]
+            assert np.all(np.diff(s) >= 0)
+            assert np.abs((u * s) @ u.T - a).max() <= TOL * max(1, np.abs(a).max()) * D[0]
+            assert np.abs(u.T @ u - np.eye(D[0])).max() <= TOL * max(10, D[0])
+        n += 1
+    assert n > 0
+
+
+def test_eigh_order_by_magnitude(cuda_device):
+    rng = np.random.default_rng(9)
+    a = rng.normal(size=(9, 9)); a = a + a.T
+    meta = (((0, 81), (9, 9), (0, 81), (9, 9), (0, 9)),)
+    S, U = (host(x) for x in ops.eigh(dev(a.ravel()), meta, (9, 81), order_by_magnitude=True))
+    ref = np.linalg.eigvalsh(a)
+    ref = ref[np.argsort(-np.abs(ref), kind='stable')]
+    assert rel(S, ref) <= TOL
+
+
+def _decode_opts(opts):
+    out = {}
+    for k, v in opts.items():
+        if isinstance(v, dict) and '__dict__' in v:
+            v = {tuple(kk): vv for kk, vv in v['__dict__']}
+        out[k] = v
+    return out
+
+
+def test_device_truncation_matches_reference_masks(cuda_device):
+    with open(os.path.join(GOLDEN, 'truncation.json')) as f:
+        cases = json.load(f)['cases']
+    for case in cases:
+        S = np.array(case['S'])
+        charges = [tuple(c) for c in case['charges']]
+        mask, kept = ops.truncation_mask_data(dev(S), case['slices'], charges, **_decode_opts(case['opts']))
+        ref = np.array(case['mask'], dtype=bool)
+        np.testing.assert_array_equal(host(mask), ref)
+        assert kept == [int(ref[lo:hi].sum()) for lo, hi in case['slices']]
+
+
+def test_fix_signs_golden_matrix(cuda_device):
+    """test_svd.py:159-186 golden gauge-fixed U (complex blocks) from oracle U, V."""
+    tr = load_trace('fix_signs')
+    svd_call = [c for c in tr['calls'] if c['fn'] == 'svd'][0]
+    fix_call = [c for c in tr['calls'] if c['fn'] == 'fix_svd_signs'][0]
+    Ui, Vi, meta = fix_call['args']
+    Uo, Vo, _ = ops.fix_svd_signs(dev(Ui), dev(Vi), meta)
+    assert rel(host(Uo), fix_call['out'][0]) <= TOL and rel(host(Vo), fix_call['out'][1]) <= TOL
+    gold = {k: np.array(v)[:, 0::2] + 1j * np.array(v)[:, 1::2] for k, v in tr['Ufixed'].items()}
+    Uo = host(Uo)
+    blocks = [Uo[m[2][0]:m[2][1]].reshape(m[3]) for m in meta]
+    assert any(b.shape == (3, 2) and np.abs(b - gold['(0,0)']).max() < TOL for b in blocks)
+
+
+def test_fix_signs_real_vs_oracle(cuda_device):
+    tr = load_trace('svd')
+    for c in tr['calls']:
+        if c['fn'] == 'fix_svd_signs' and not np.iscomplexobj(c['args'][0]):
+            Ui, Vi, meta = c['args']
+            Uo, Vo, _ = ops.fix_svd_signs(dev(Ui), dev(Vi), meta)
+            assert rel(host(Uo), c['out'][0]) <= TOL and rel(host(Vo), c['out'][1]) <= TOL
+
+
+@pytest.mark.parametrize('name', ['svd', 'svd_ill'])
+def test_apply_mask_on_reference_calls(name, cuda_device):
+    tr = load_trace(name)
+    n = 0
+    for c in tr['calls']:
+        if c['fn'] != 'apply_mask':
+            continue
+        A, mask, meta, Dsize, axis, ndim = c['args']
+        dmask = {k: dev(np.asarray(v, dtype=np.int64)) for k, v in mask.items()}
+        got = host(ops.apply_mask(dev(A), dmask, meta, Dsize, axis, ndim))
+        np.testing.assert_array_equal(got, c['out'][0])
+        g = np.random.default_rng(0).normal(size=Dsize).astype(A.dtype)
+        back = host(ops.apply_mask(dev(g), dmask, meta, None, axis, ndim, scatter_size=A.size))
+        np.testing.assert_array_equal(back, oracle.apply_mask_backward(g, mask, meta, A.size, axis, ndim))
+        n += 1
+    assert n > 0

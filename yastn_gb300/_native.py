@@ -69,10 +69,15 @@ def lib():
     return _lib
 
 
-def call(name, *args):
+# number of kernels launched through the library (callers state how many a call enqueues)
+LAUNCHES = [0]
+
+
+def call(name, *args, launches=1):
     """Call an entry point and raise NativeError on a non-zero status."""
     L = lib()
     st = getattr(L, name)(*args)
     if st != YB_OK:
         raise NativeError(name, st, L.yb_last_cuda_error() if st == YB_ERR_CUDA else 0)
+    LAUNCHES[0] += launches
     return st

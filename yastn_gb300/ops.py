@@ -208,11 +208,11 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps, tol_scale):
     shift = torch.empty(nb, dtype=torch.float64, device=dev) if mode != 0 else None
     st = _stream()
     N.call('yb_svd_init', _ptr(data), _ptr(work), _ptr(dblocks), nb, code, _ptr(counters),
-           _vp(shift.data_ptr() if shift is not None else 0), st)
+           _vp(shift.data_ptr() if shift is not None else 0), st, launches=1 + int(shift is not None))
     converged = False
     for sweep in range(max_sweeps):
         N.call('yb_svd_sweep', _ptr(work), _ptr(dblocks), nb, _ptr(dpairs), len(plan.pair_items), plan.max_rounds,
-               code, float(tol_scale), _ptr(counters), st)
+               code, float(tol_scale), _ptr(counters), st, launches=plan.max_rounds + 1)
         if sweep >= 2 and int(counters[:nb].max().item()) == 0:
             converged = True
             break
