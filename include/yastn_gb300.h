@@ -103,26 +103,41 @@ int yb_grouped_gemm(const void* a, const void* b, void* c, int dtype,
 /* ==== family (c): batched one-sided Jacobi SVD / symmetric eigendecomposition ==========
  * blocks: n_blocks records of YB_SVD_REC int64:
  *   [0] a offset [1] m [2] n [3] U offset [4] S offset [5] Vh offset
- *   [6] workspace X offset [7] workspace W offset [8] first pair item
+ *   [6] X offset (FP64 workspace) [7] W offset (FP64 workspace) [8] first pair item
  *   [9] k=min(m,n) [10] L=max(m,n) [11] N = k rounded up to even [12] 1 if m > n
+ *   [13] X offset (FP32 workspace) [14] W offset (FP32 workspace)
+ * X holds the k vectors (rows of A, or of A^T when m > n) of length L, W the k x k
+ * accumulated rotations (X = W X_0 throughout).
  * pair_items: int32 pairs (block, pair index 0..N/2-1) over all blocks.
- * Workspace (FP64): X holds k vectors of length L, W the k x k accumulated rotations.
- * counters: int64[2*n_blocks] (rotations in the last completed sweep | in this sweep).
- * Sequence: yb_svd_init, then yb_svd_sweep until counters[0:n_blocks] are all zero
- * (the host reads them between sweeps; its sweep cap maps to YB_ERR_NOT_CONVERGED),
- * then yb_svd_finalize. shift != NULL (eigh): per-block shifts c_b = ||A_b||_F + 1 are
- * computed and A_b + c_b I is decomposed (positive definite, so its SVD is its
- * eigendecomposition); finalize mode 1 writes eigenvalues ascending, mode 2 by
- * descending magnitude, both with eigenvectors as columns of U; mode 0 is the SVD.
+ * state: int64[4*n_blocks + 4]: per block (max |cos| of the sweep in progress as double
+ *   bits, converged flag, sweeps run in the current phase, unused), then the control
+ *   words of the grid barrier (count, generation, error flag, all-converged flag).
+ * Sequence (mixed precision): yb_svd_init (X32 = A or A^T, W32 = I); yb_svd_sweeps with
+ * precision 32; yb_svd_widen (W = double(W32)); the host orthonormalises W (Newton-Schulz
+ * with the grouped GEMM) and forms X = W X_0 (for eigh: yb_svd_shift_prefill, then
+ * X += W A); yb_svd_sweeps with precision 64; yb_svd_finalize. yb_svd_sweeps runs every
+ * sweep of a phase in one cooperative launch (rounds separated by a grid barrier with a
+ * bounded spin; on timeout the error control word is set and the kernel exits) and stops
+ * after the first sweep in which each block's largest rotation |cos| was <= tol_stop, or
+ * after max_sweeps (the host reads the state and maps non-convergence to an error).
+ * shift != NULL (eigh): per-block shifts c_b = ||A_b||_F + 1 are computed and A_b + c_b I
+ * is decomposed (positive definite, so its SVD is its eigendecomposition); finalize mode 1
+ * writes eigenvalues ascending, mode 2 by descending magnitude, with eigenvectors as
+ * columns of U; mode 0 is the SVD (S descending, zero singular values completed to
+ * orthonormal vectors).
  * Replaces svd (backend_torch.py:318-319, torch_svd_gesdd.py:15-21) and eigh
  * (backend_torch.py:369-384, torch_eig_sym.py:14-32) for FP64 blocks.
  */
 #define YB_SVD_REC 16
-int yb_svd_init(const void* a, void* work, const int64_t* blocks, int n_blocks, int dtype,
-                int64_t* counters, double* shift, void* stream);
-int yb_svd_sweep(void* work, const int64_t* blocks, int n_blocks, const int32_t* pair_items,
-                 int n_pair_items, int max_rounds, int dtype, double tol_scale,
-                 int64_t* counters, void* stream);
+int yb_svd_init(const void* a, void* work32, const int64_t* blocks, int n_blocks, int dtype,
+                int64_t* state, double* shift, void* stream);
+int yb_svd_sweeps(void* work, const int64_t* blocks, int n_blocks, const int32_t* pair_items,
+                  int n_pair_items, int max_rounds, int precision, int max_sweeps, double tol_stop,
+                  int64_t* state, void* stream);
+int yb_svd_widen(const void* work32, void* work64, const int64_t* blocks, int n_blocks,
+                 int64_t* state, void* stream);
+int yb_svd_shift_prefill(void* work64, const int64_t* blocks, int n_blocks, const double* shift,
+                         void* stream);
 int yb_svd_finalize(const void* work, void* U, double* S, void* Vh, const int64_t* blocks,
                     int n_blocks, int dtype, int max_k, int mode, const double* shift, void* stream);
 

@@ -338,6 +338,7 @@ def apply_mask_backward(C_b, mask, meta, size_A, axis, ndim):
     """Adjoint of :func:`apply_mask`; restates ``_backend_torch_backwards.py:270-279``."""
     out = np.zeros(size_A, dtype=C_b.dtype)
     for sln, Dn, sla, Da, tm in meta:
+        Da = (Da,) if isinstance(Da, int) else Da  # diagonal tensors carry an int length
         blk = out[_sl(sla)].reshape(Da)
         idx = [slice(None)] * len(Da)
         idx[axis] = np.asarray(mask[tm])
@@ -349,6 +350,7 @@ def embed_mask(A, mask, meta, Dsize, axis, ndim):
     """Inverse of :func:`apply_mask` into zeros; restates ``backend_np.py:636-643``."""
     out = np.zeros(Dsize, dtype=A.dtype)
     for sln, Dn, sla, Da, tm in meta:
+        Dn = (Dn,) if isinstance(Dn, int) else Dn
         blk = out[_sl(sln)].reshape(Dn)
         idx = [slice(None)] * len(Dn)
         idx[axis] = np.asarray(mask[tm])

@@ -104,3 +104,44 @@ def svd_adjoint_core(plan, Pm, Qm, S, gS, gU, gV, dtype):
         elif kind == 2:
             TR[tro:tro + m * k] = (gU[uo:uo + m * k].reshape(m, k) * rinv(s)[None, :]).ravel()
     return K, TR
+
+
+def jacobi_sweeps(X, W, blocks, dtype, tol_stop, max_sweeps):
+    """The round-robin one-sided Jacobi of csrc/yb_svd.cu (svd_sweeps_kernel), restated
+    sequentially with numpy on the plan's workspace layout. Returns (sweeps, converged)."""
+    eps = 2.0 ** -24 if dtype == np.float32 else 2.0 ** -53
+    return _sweeps(X, W, blocks, dtype, tol_stop, max_sweeps, eps)
+
+
+def _sweeps(X, W, blocks, dtype, tol_stop, max_sweeps, eps):
+    nb = len(blocks); conv = [False]*nb; nsw = [0]*nb
+    max_rounds = max(int(r[11]) - 1 for r in blocks)
+    for sw in range(max_sweeps):
+        maxcos = [0.0]*nb
+        for rd in range(max_rounds):
+            for b, r in enumerate(blocks):
+                if conv[b]: continue
+                k, L, N = int(r[9]), int(r[10]), int(r[11])
+                xo, wo = (int(r[13]), int(r[14])) if dtype == np.float32 else (int(r[6]), int(r[7]))
+                if rd >= N - 1: continue
+                for pi in range(N // 2):
+                    p, q = (N - 1, rd) if pi == 0 else ((rd + pi) % (N - 1), (rd - pi + N - 1) % (N - 1))
+                    if p >= k or q >= k: continue
+                    p, q = min(p, q), max(p, q)
+                    xp = X[xo + p*L: xo + (p+1)*L]; xq = X[xo + q*L: xo + (q+1)*L]
+                    al = float(np.dot(xp.astype(np.float64), xp)); be = float(np.dot(xq.astype(np.float64), xq)); ga = float(np.dot(xp.astype(np.float64), xq))
+                    if not (al > 0 and be > 0): continue
+                    c_ = abs(ga)/np.sqrt(al)/np.sqrt(be); maxcos[b] = max(maxcos[b], c_)
+                    if not c_ > np.sqrt(L)*eps: continue
+                    zeta = (be - al)/(2*ga); t = np.copysign(1.0, zeta)/(abs(zeta) + np.hypot(1.0, zeta)); cd = 1/np.sqrt(1+t*t)
+                    c, s = dtype(cd), dtype(cd*t)
+                    u, v = xp.copy(), xq.copy(); xp[:] = c*u - s*v; xq[:] = s*u + c*v
+                    wp = W[wo + p*k: wo+(p+1)*k]; wq = W[wo+q*k: wo+(q+1)*k]
+                    u, v = wp.copy(), wq.copy(); wp[:] = c*u - s*v; wq[:] = s*u + c*v
+        for b in range(nb):
+            if not conv[b]:
+                nsw[b] += 1
+                if maxcos[b] <= tol_stop: conv[b] = True
+        if all(conv): break
+    return nsw, conv
+

@@ -18,7 +18,7 @@ def lib():
 
 def test_header_declares_entry_points():
     names = N.declared_symbols()
-    for must in ('yb_block_copy', 'yb_grouped_gemm', 'yb_svd_init', 'yb_svd_sweep', 'yb_svd_finalize',
+    for must in ('yb_block_copy', 'yb_grouped_gemm', 'yb_svd_init', 'yb_svd_sweeps', 'yb_svd_widen', 'yb_svd_finalize',
                  'yb_svd_adjoint_core', 'yb_mask_gather', 'yb_fix_signs', 'yb_truncation_mask'):
         assert must in names
 

@@ -179,3 +179,59 @@ def test_svd_plan_pairs_cover_all_pairs():
                 if p < k and q < k:
                     seen.add((min(p, q), max(p, q)))
         assert seen == {(i, j) for i in range(k) for j in range(i + 1, k)}
+
+
+def test_mask_plan_diagonal_records():
+    """Diagonal tensors give (sln, Dn:int, sla, Da:int, tm) records (yastn/tensor/_merging.py:577-579)."""
+    meta = (((0, 2), 2, (3, 6), 3, (0,)), ((2, 3), 1, (0, 3), 3, (1,)))
+    recs, items, total = P.mask_plan(meta, 0, {(0,): (0, 2), (1,): (2, 1)})
+    assert total == 3 and recs[:, 2].tolist() == [1, 1] and recs[:, 5].tolist() == [1, 1]
+
+
+def test_mixed_precision_jacobi_schedule_on_plan_layout():
+    """FP32 sweeps -> widen -> Newton-Schulz (grouped GEMM plans) -> X = W X_0 (plan) ->
+    FP64 sweeps, on the plan's workspace offsets, reproduces LAPACK's singular values."""
+    rng = np.random.default_rng(0)
+    shapes = [(30, 30), (40, 17), (13, 35), (1, 5), (6, 6)]
+    meta, off, oU, oS, oV = [], 0, 0, 0, 0
+    for m, n in shapes:
+        k = min(m, n)
+        meta.append(((off, off + m * n), (m, n), (oU, oU + m * k), (m, k), (oS, oS + k), (oV, oV + k * n), (k, n)))
+        off += m * n; oU += m * k; oS += k; oV += k * n
+    meta = tuple(meta)
+    data = rng.normal(size=off)
+    data[meta[4][0][0]:meta[4][0][1]] = 0  # an all-zero block
+    plan = P.svd_plan(meta)
+    w32 = np.zeros(plan.n32, np.float32)
+    w64 = np.zeros(plan.n64)
+    for r in plan.blocks:
+        a, m, n, k, L = int(r[0]), int(r[1]), int(r[2]), int(r[9]), int(r[10])
+        A = data[a:a + m * n].reshape(m, n)
+        X0 = A.T if m > n else A
+        w32[int(r[13]):int(r[13]) + k * L] = X0.ravel().astype(np.float32)
+        w32[int(r[14]):int(r[14]) + k * k] = np.eye(k, dtype=np.float32).ravel()
+    nsw, conv = PI.jacobi_sweeps(w32, w32, plan.blocks, np.float32, 2e-5, 40)
+    assert all(conv)
+    for r in plan.blocks:
+        k = int(r[9])
+        w64[int(r[7]):int(r[7]) + k * k] = w32[int(r[14]):int(r[14]) + k * k]
+    w0, t0, n0, ws = plan.w_range
+    for _ in range(2):
+        w64[n0:n0 + ws] = w64[w0:w0 + ws]
+        PI.run_gemm(plan.gram, w64, w64, w64)
+        PI.run_gemm(plan.ns, w64, w64, w64, alpha=-0.5, beta=1.5)
+        w64[w0:w0 + ws] = w64[n0:n0 + ws]
+    for r in plan.blocks:
+        k = int(r[9])
+        Wb = w64[int(r[7]):int(r[7]) + k * k].reshape(k, k)
+        assert np.abs(Wb @ Wb.T - np.eye(k)).max() < 1e-14
+    PI.run_gemm(plan.xform, w64, data, w64)
+    nsw, conv = PI.jacobi_sweeps(w64, w64, plan.blocks, np.float64, 1e-10, 20)
+    assert all(conv) and max(nsw) <= 4
+    U, S, V = oracle.svd(data, meta, (oU, oS, oV))
+    for r, mt in zip(plan.blocks, meta):
+        k, L = int(r[9]), int(r[10])
+        X = w64[int(r[6]):int(r[6]) + k * L].reshape(k, L)
+        s = np.sort(np.linalg.norm(X, axis=1))[::-1]
+        sr = S[mt[4][0]:mt[4][1]]
+        assert np.abs(s - sr).max() <= 1e-13 * max(sr.max(), 1.0)

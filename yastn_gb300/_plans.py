@@ -341,41 +341,64 @@ def tds_plan(meta_dot, Areshape, Breshape, Aoffs, Boffs):
 # ----------------------------------------------------------------------------- SVD
 
 class SvdPlan:
-    def __init__(self, blocks, pair_items, max_rounds, work_elems, max_k, nominal_flops):
+    """Mixed-precision Jacobi plan: block records, pair items, workspace layout and the
+    grouped-GEMM plans of the Newton-Schulz orthonormalisation and of X = W X_0."""
+
+    def __init__(self, blocks, pair_items, max_rounds, max_k, nominal_flops, n64, n32, w_range, gram, ns, xform):
         self.blocks = blocks
         self.pair_items = pair_items
         self.max_rounds = max_rounds
-        self.work_elems = work_elems
         self.max_k = max_k
         self.nominal_flops = nominal_flops
+        self.n64 = n64          # FP64 workspace elements: [X | W | T | Wn]
+        self.n32 = n32          # FP32 workspace elements: [X32 | W32]
+        self.w_range = w_range  # (W start, T start, Wn start, total W size) in the FP64 workspace
+        self.gram, self.ns, self.xform = gram, ns, xform
         self._dev = {}
 
 
 def svd_plan(meta):
     """Jacobi plan for svd records (sl, D, slU, DU, slS, slV, DV) of yastn/tensor/linalg.py:323-380."""
     def build():
-        recs, pairs, woff, max_rounds, max_k, fl = [], [], 0, 0, 0, 0
-        for bi, (sl, D, slU, DU, slS, slV, DV) in enumerate(meta):
+        sel = []
+        for sl, D, slU, DU, slS, slV, DV in meta:
             m, n = D
             k = min(m, n)
             if k == 0:
                 continue
             if DU != (m, k) or DV != (k, n) or slS[1] - slS[0] != k:
                 raise PlanError("svd record is not a thin full-rank SVD")
-            L = max(m, n)
+            sel.append((sl, m, n, slU, slS, slV, k, max(m, n)))
+        xs = sum(k * L for *_, k, L in sel)
+        ws = sum(k * k for *_, k, L in sel)
+        w0, t0, n0 = xs, xs + ws, xs + 2 * ws
+        recs, pairs, gram, ns, xf = [], [], [], [], []
+        ox = ow = ox32 = 0
+        max_rounds = max_k = fl = 0
+        for bi, (sl, m, n, slU, slS, slV, k, L) in enumerate(sel):
             N = k + (k % 2)
             rec = np.zeros(SVD_REC, dtype=np.int64)
-            rec[:13] = (sl[0], m, n, slU[0], slS[0], slV[0], woff, woff + k * L, len(pairs), k, L, N, int(m > n))
-            woff += k * L + k * k
-            b = len(recs)
+            rec[:15] = (sl[0], m, n, slU[0], slS[0], slV[0], ox, w0 + ow, len(pairs), k, L, N, int(m > n),
+                        ox32, xs + ow)
             recs.append(rec)
-            pairs.extend((b, p) for p in range(N // 2))
+            pairs.extend((bi, p) for p in range(N // 2))
+            # T = W^T W ; Wn = 1.5 Wn - 0.5 W T (Wn holds a copy of W) ; X = W X_0
+            gram.append((t0 + ow, k, k, k, [(w0 + ow, w0 + ow, k, 1, k, k, 1, 0)]))
+            ns.append((n0 + ow, k, k, k, [(w0 + ow, t0 + ow, k, k, 1, k, 1, 0)]))
+            if m > n:
+                xf.append((ox, k, L, L, [(w0 + ow, sl[0], k, k, 1, 1, n, 0)]))
+            else:
+                xf.append((ox, k, L, L, [(w0 + ow, sl[0], k, k, 1, n, 1, 0)]))
+            ox += k * L
+            ox32 += k * L
+            ow += k * k
             max_rounds = max(max_rounds, N - 1)
             max_k = max(max_k, k)
             fl += 14 * L * k * k + 8 * k ** 3  # nominal Golub-Reinsch count
         blocks = np.stack(recs) if recs else np.zeros((0, SVD_REC), dtype=np.int64)
         items = np.array(pairs, dtype=np.int32).reshape(-1, 2)
-        return SvdPlan(blocks, items, max_rounds, woff, max_k, fl)
+        return SvdPlan(blocks, items, max_rounds, max_k, fl, xs + 3 * ws, xs + ws, (w0, t0, n0, ws),
+                       _pack_gemm(gram), _pack_gemm(ns), _pack_gemm(xf))
     return CACHE.get((meta,), ('svd',), build)
 
 
@@ -445,6 +468,8 @@ def mask_plan(meta, axis, lengths):
     to (offset in the concatenated index buffer, number of kept indices)."""
     recs, items, total = [], [], 0
     for sln, Dn, sla, Da, tm in meta:
+        if isinstance(Da, int):  # diagonal tensors carry their block length as an int
+            Da = (Da,)
         ioff, cnt = lengths[tm]
         pre = int(np.prod(Da[:axis], dtype=np.int64))
         post = int(np.prod(Da[axis + 1:], dtype=np.int64))

@@ -1,19 +1,25 @@
-// Family (c): batched one-sided (Hestenes) Jacobi SVD of all charge-sector blocks.
+// Family (c): batched one-sided (Hestenes) Jacobi SVD / symmetric eigendecomposition of
+// all charge-sector blocks, mixed precision.
 //
 // Each block A (m x n, row-major) is handled in its "wide" orientation: the k=min(m,n)
-// vectors to orthogonalise are the rows of A (m <= n) or of A^T (m > n), each of
-// length L=max(m,n), copied into a workspace X. A parallel round-robin ordering
-// (circle method over N = k rounded up to even) pairs all vectors in N-1 rounds of
-// N/2 disjoint pairs; one warp rotates one pair, all blocks advance in the same
-// launch. Rotations are accumulated in W (k x k, starting at I), so that
-// X_final = W X_0 with orthogonal rows; then S = row norms, the normalised rows give
-// Vh (wide) or U (tall), and W^T gives the other factor. The host launches sweeps
-// until no rotation was applied in a sweep or the sweep cap is hit (reported as
-// YB_ERR_NOT_CONVERGED by the host layer). No kernel waits on another CTA.
+// vectors to orthogonalise are the rows of A (m <= n) or of A^T (m > n), each of length
+// L=max(m,n), held in a workspace X; rotations are accumulated in W (k x k), so that
+// X = W X_0 at every step. A parallel round-robin ordering (circle method over
+// N = k rounded up to even) pairs all vectors in N-1 rounds of N/2 disjoint pairs; one
+// warp rotates one pair and all blocks advance together.
 //
-// A rotation is applied when |x_p.x_q| > tol * ||x_p|| ||x_q|| with tol = sqrt(L) * eps
-// (the threshold of LAPACK's one-sided Jacobi); the angle follows Rutishauser's
-// stable formula with hypot to avoid overflow.
+// GB300 has ~60x more FP32 than FP64 throughput, so the sweeps run in two phases:
+//   1. FP32 sweeps on (X32, W32) until no rotation is needed at FP32 precision;
+//   2. the host orthonormalises W = double(W32) with Newton-Schulz steps and forms
+//      X = W X_0 with the FP64 grouped GEMM; then FP64 sweeps polish (X, W) until a
+//      sweep whose largest |cos| was below tol_stop (typically 1-2 sweeps).
+// One persistent cooperative launch runs all the sweeps of a phase; rounds are separated
+// by a grid barrier whose spin is bounded (an error flag is raised and the kernel exits
+// if it ever times out). Finally S = row norms (descending), the normalised rows give Vh
+// (wide) or U (tall), and W^T gives the other factor.
+//
+// A rotation is applied when |x_p.x_q| > sqrt(L) eps ||x_p|| ||x_q|| (the threshold of
+// LAPACK's one-sided Jacobi); the angle follows Rutishauser's formula with hypot.
 #include <float.h>
 #include "yb_common.cuh"
 
@@ -21,11 +27,36 @@ namespace yb {
 namespace {
 
 constexpr int kWarps = 8;
+constexpr int kThreads = kWarps * 32;
+constexpr long long kSpinLimit = 1ll << 22;
 
 // record fields
-enum { R_A = 0, R_M, R_N, R_U, R_S, R_V, R_X, R_W, R_P, R_K, R_L, R_NP, R_T };
+enum { R_A = 0, R_M, R_N, R_U, R_S, R_V, R_X, R_W, R_P, R_K, R_L, R_NP, R_T, R_X32, R_W32 };
+// per-block state (int64): [0] max |cos| of the sweep in progress (double bits),
+// [1] converged flag, [2] sweeps run in the current phase, [3] unused
+enum { ST_MAXCOS = 0, ST_CONV = 1, ST_SWEEPS = 2, ST_REC = 4 };
+// control words after the per-block state: [0] barrier count [1] barrier generation
+// [2] error flag [3] all-converged flag
+enum { C_COUNT = 0, C_GEN = 1, C_ERR = 2, C_DONE = 3, C_REC = 4 };
 
-// Per-block Frobenius norm -> shift[b] (used to make a symmetric block positive definite).
+template <typename T>
+struct Eps;
+template <>
+struct Eps<float> {
+  static constexpr double v = 5.9604644775390625e-08;  // 2^-24
+};
+template <>
+struct Eps<double> {
+  static constexpr double v = 1.1102230246251565e-16;  // 2^-53
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Per-block Frobenius norm -> shift[b] (makes a symmetric block positive definite).
 __global__ void block_fro_kernel(const double* __restrict__ A, const int64_t* __restrict__ blocks,
                                  double* __restrict__ shift) {
   __shared__ double red[32];
@@ -34,27 +65,27 @@ __global__ void block_fro_kernel(const double* __restrict__ A, const int64_t* __
   const double* a = A + r[R_A];
   double acc = 0.0;
   for (int64_t e = threadIdx.x; e < cnt; e += blockDim.x) acc = fma(a[e], a[e], acc);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  acc = warp_sum(acc);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
     double tot = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
-    // ||A||_2 <= ||A||_F: A + shift*I is positive definite; the +1 keeps an all-zero block regular
+    // ||A||_2 <= ||A||_F: A + shift I is positive definite; +1 keeps an all-zero block regular
     shift[blockIdx.x] = sqrt(tot) + 1.0;
   }
 }
 
-__global__ void svd_init_kernel(const double* __restrict__ A, double* __restrict__ work,
-                                const int64_t* __restrict__ blocks, int64_t* __restrict__ counters,
-                                int n_blocks, const double* __restrict__ shift) {
+// X32 = float(A or A^T) (+ shift on the diagonal), W32 = I; resets the per-block state.
+__global__ void svd_init_kernel(const double* __restrict__ A, float* __restrict__ work32,
+                                const int64_t* __restrict__ blocks, int64_t* __restrict__ state,
+                                const double* __restrict__ shift) {
   const int64_t* r = blocks + (int64_t)blockIdx.y * YB_SVD_REC;
   const int64_t m = r[R_M], n = r[R_N], k = r[R_K], L = r[R_L];
   const bool tall = m > n;
   const int64_t xs = k * L, ws = k * k;
-  double* X = work + r[R_X];
-  double* W = work + r[R_W];
+  float* X = work32 + r[R_X32];
+  float* W = work32 + r[R_W32];
   const double* a = A + r[R_A];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < xs + ws;
        e += (int64_t)gridDim.x * blockDim.x) {
@@ -62,57 +93,89 @@ __global__ void svd_init_kernel(const double* __restrict__ A, double* __restrict
       const int64_t i = e / L, l = e - i * L;
       double v = tall ? a[l * n + i] : a[e];
       if (shift != nullptr && i == l) v += shift[blockIdx.y];
-      X[e] = v;
+      X[e] = (float)v;
     } else {
       const int64_t f = e - xs;
       const int64_t i = f / k, j = f - i * k;
-      W[f] = (i == j) ? 1.0 : 0.0;
+      W[f] = (i == j) ? 1.0f : 0.0f;
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    counters[blockIdx.y] = 1;             // rotations in the last completed sweep (1 = active)
-    counters[n_blocks + blockIdx.y] = 0;  // rotations in the sweep in progress
-  }
+  if (blockIdx.x == 0 && threadIdx.x < ST_REC) state[blockIdx.y * ST_REC + threadIdx.x] = 0;
 }
 
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
+// W64 = double(W32) (the host orthonormalises it next); resets the per-block state.
+__global__ void svd_widen_kernel(const float* __restrict__ work32, double* __restrict__ work64,
+                                 const int64_t* __restrict__ blocks, int64_t* __restrict__ state) {
+  const int64_t* r = blocks + (int64_t)blockIdx.y * YB_SVD_REC;
+  const int64_t k = r[R_K];
+  const float* W32 = work32 + r[R_W32];
+  double* W = work64 + r[R_W];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < k * k; e += (int64_t)gridDim.x * blockDim.x)
+    W[e] = (double)W32[e];
+  if (blockIdx.x == 0 && threadIdx.x < ST_REC) state[blockIdx.y * ST_REC + threadIdx.x] = 0;
 }
 
-__global__ void __launch_bounds__(kWarps * 32) svd_round_kernel(double* __restrict__ work,
-                                                                const int64_t* __restrict__ blocks,
-                                                                const int32_t* __restrict__ pair_items,
-                                                                int n_items, int round, double tol_scale,
-                                                                int64_t* __restrict__ counters,
-                                                                int n_blocks) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int item = blockIdx.x * kWarps + warp;
-  if (item >= n_items) return;
-  const int b = pair_items[2 * item];
-  const int pi = pair_items[2 * item + 1];
-  if (counters[b] == 0) return;  // block converged in the previous sweep
-  const int64_t* r = blocks + (int64_t)b * YB_SVD_REC;
-  const int64_t k = r[R_K], L = r[R_L], N = r[R_NP];
-  if (round >= N - 1) return;
-  int64_t p, q;
-  if (pi == 0) {
-    p = N - 1;
-    q = round;
-  } else {
-    p = (round + pi) % (N - 1);
-    q = (round - pi + (N - 1)) % (N - 1);
+// X = shift_b * W (eigh: the FP64 phase then adds W A with the grouped GEMM, X = W (A + shift I)).
+__global__ void svd_shift_prefill_kernel(double* __restrict__ work64, const int64_t* __restrict__ blocks,
+                                         const double* __restrict__ shift) {
+  const int64_t* r = blocks + (int64_t)blockIdx.y * YB_SVD_REC;
+  const int64_t k = r[R_K];
+  const double c = shift[blockIdx.y];
+  const double* W = work64 + r[R_W];
+  double* X = work64 + r[R_X];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < k * k; e += (int64_t)gridDim.x * blockDim.x)
+    X[e] = c * W[e];
+}
+
+// Grid barrier for a cooperative launch (all CTAs co-resident). The spin is bounded: on
+// timeout the error flag is raised and false is returned, and the caller exits.
+__device__ bool grid_barrier(unsigned long long* ctrl, unsigned nblocks) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned long long* gen = ctrl + C_GEN;
+    const unsigned long long g = *gen;
+    __threadfence();
+    const unsigned long long arrived = atomicAdd(ctrl + C_COUNT, 1ull) + 1ull;
+    if (arrived == nblocks) {
+      ctrl[C_COUNT] = 0ull;
+      __threadfence();
+      atomicAdd(ctrl + C_GEN, 1ull);
+    } else {
+      long long spins = 0;
+      while (*gen == g) {
+        __nanosleep(32);
+        if (++spins > kSpinLimit) {
+          atomicExch(ctrl + C_ERR, 1ull);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
   }
-  if (p >= k || q >= k) return;  // dummy vector of an odd count
-  if (p > q) { int64_t t = p; p = q; q = t; }
-  double* X = work + r[R_X];
-  double* W = work + r[R_W];
-  double* xp = X + p * L;
-  double* xq = X + q * L;
+  __syncthreads();
+  return ok != 0;
+}
+
+template <typename T>
+__device__ __forceinline__ void rotate_pair(T* __restrict__ X, T* __restrict__ W, int64_t k, int64_t L, int64_t p,
+                                            int64_t q, int lane, int64_t* st) {
+  T* xp = X + p * L;
+  T* xq = X + q * L;
+  // rows are rewritten by other SMs between rounds: loads bypass L1 (ld.global.cg)
   double al = 0.0, be = 0.0, ga = 0.0;
-  for (int64_t l = lane; l < L; l += 32) {
-    const double u = xp[l], v = xq[l];
+  int64_t l = lane;
+  for (; l + 96 < L; l += 128) {  // four independent loads in flight per row
+    const double u0 = __ldcg(xp + l), u1 = __ldcg(xp + l + 32), u2 = __ldcg(xp + l + 64), u3 = __ldcg(xp + l + 96);
+    const double v0 = __ldcg(xq + l), v1 = __ldcg(xq + l + 32), v2 = __ldcg(xq + l + 64), v3 = __ldcg(xq + l + 96);
+    al = fma(u0, u0, al); al = fma(u1, u1, al); al = fma(u2, u2, al); al = fma(u3, u3, al);
+    be = fma(v0, v0, be); be = fma(v1, v1, be); be = fma(v2, v2, be); be = fma(v3, v3, be);
+    ga = fma(u0, v0, ga); ga = fma(u1, v1, ga); ga = fma(u2, v2, ga); ga = fma(u3, v3, ga);
+  }
+  for (; l < L; l += 32) {
+    const double u = __ldcg(xp + l), v = __ldcg(xq + l);
     al = fma(u, u, al);
     be = fma(v, v, be);
     ga = fma(u, v, ga);
@@ -120,39 +183,91 @@ __global__ void __launch_bounds__(kWarps * 32) svd_round_kernel(double* __restri
   al = warp_sum(al);
   be = warp_sum(be);
   ga = warp_sum(ga);
-  const double tol = tol_scale * sqrt((double)L) * DBL_EPSILON;
-  if (!(fabs(ga) > tol * sqrt(al) * sqrt(be))) return;  // also skips zero vectors
+  if (!(al > 0.0 && be > 0.0)) return;
+  const double cosv = fabs(ga) / (sqrt(al) * sqrt(be));
+  if (lane == 0) atomicMax((unsigned long long*)(st + ST_MAXCOS), (unsigned long long)__double_as_longlong(cosv));
+  if (!(cosv > sqrt((double)L) * Eps<T>::v)) return;
   const double zeta = (be - al) / (2.0 * ga);
   const double t = copysign(1.0, zeta) / (fabs(zeta) + hypot(1.0, zeta));
-  const double c = 1.0 / sqrt(fma(t, t, 1.0));
-  const double s = c * t;
-  for (int64_t l = lane; l < L; l += 32) {
-    const double u = xp[l], v = xq[l];
-    xp[l] = fma(c, u, -s * v);
-    xq[l] = fma(s, u, c * v);
+  const double cd = 1.0 / sqrt(fma(t, t, 1.0));
+  const T c = (T)cd, s = (T)(cd * t);
+  for (int64_t j = lane; j < L; j += 32) {
+    const T u = __ldcg(xp + j), v = __ldcg(xq + j);
+    xp[j] = c * u - s * v;
+    xq[j] = s * u + c * v;
   }
-  double* wp = W + p * k;
-  double* wq = W + q * k;
-  for (int64_t l = lane; l < k; l += 32) {
-    const double u = wp[l], v = wq[l];
-    wp[l] = fma(c, u, -s * v);
-    wq[l] = fma(s, u, c * v);
+  T* wp = W + p * k;
+  T* wq = W + q * k;
+  for (int64_t j = lane; j < k; j += 32) {
+    const T u = __ldcg(wp + j), v = __ldcg(wq + j);
+    wp[j] = c * u - s * v;
+    wq[j] = s * u + c * v;
   }
-  if (lane == 0) atomicAdd((unsigned long long*)&counters[n_blocks + b], 1ull);
 }
 
-__global__ void svd_sweep_end_kernel(int64_t* counters, int n_blocks) {
-  for (int b = threadIdx.x; b < n_blocks; b += blockDim.x) {
-    if (counters[b] != 0) counters[b] = counters[n_blocks + b];
-    counters[n_blocks + b] = 0;
+// All sweeps of one precision phase in one cooperative launch.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) svd_sweeps_kernel(T* __restrict__ work, const int64_t* __restrict__ blocks,
+                                                              int n_blocks, const int32_t* __restrict__ pair_items,
+                                                              int n_items, int max_rounds, int max_sweeps,
+                                                              double tol_stop, int64_t* __restrict__ state) {
+  unsigned long long* ctrl = reinterpret_cast<unsigned long long*>(state + (int64_t)n_blocks * ST_REC);
+  __shared__ int any_active;
+  const int lane = threadIdx.x & 31;
+  const int64_t gwarp = (int64_t)blockIdx.x * kWarps + (threadIdx.x >> 5);
+  const int64_t nwarps = (int64_t)gridDim.x * kWarps;
+  const int rx = sizeof(T) == 4 ? R_X32 : R_X;
+  const int rw = sizeof(T) == 4 ? R_W32 : R_W;
+  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    for (int round = 0; round < max_rounds; ++round) {
+      for (int64_t item = gwarp; item < n_items; item += nwarps) {
+        const int b = pair_items[2 * item];
+        const int pi = pair_items[2 * item + 1];
+        int64_t* st = state + (int64_t)b * ST_REC;
+        if (((volatile int64_t*)st)[ST_CONV]) continue;
+        const int64_t* r = blocks + (int64_t)b * YB_SVD_REC;
+        const int64_t k = r[R_K], L = r[R_L], N = r[R_NP];
+        if (round >= N - 1) continue;
+        int64_t p, q;
+        if (pi == 0) {
+          p = N - 1;
+          q = round;
+        } else {
+          p = (round + pi) % (N - 1);
+          q = (round - pi + (N - 1)) % (N - 1);
+        }
+        if (p >= k || q >= k) continue;  // the dummy vector of an odd count
+        if (p > q) { const int64_t tq = p; p = q; q = tq; }
+        rotate_pair<T>(work + r[rx], work + r[rw], k, L, p, q, lane, st);
+      }
+      if (!grid_barrier(ctrl, gridDim.x)) return;
+    }
+    // sweep end: a block whose largest |cos| in this sweep was <= tol_stop is converged
+    if (blockIdx.x == 0) {
+      if (threadIdx.x == 0) any_active = 0;
+      __syncthreads();
+      for (int b = threadIdx.x; b < n_blocks; b += blockDim.x) {
+        int64_t* st = state + (int64_t)b * ST_REC;
+        if (st[ST_CONV]) continue;
+        const double mc = __longlong_as_double((long long)st[ST_MAXCOS]);
+        st[ST_SWEEPS] += 1;
+        st[ST_MAXCOS] = 0;
+        if (mc <= tol_stop) st[ST_CONV] = 1; else any_active = 1;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) ctrl[C_DONE] = any_active ? 0ull : 1ull;
+      __threadfence();
+    }
+    if (!grid_barrier(ctrl, gridDim.x)) return;
+    if (((volatile unsigned long long*)ctrl)[C_DONE]) return;
   }
 }
 
 // One CTA per block: singular values = row norms, sort descending (index tie-break),
 // write U, S, Vh; vectors of zero norm are completed to an orthonormal set.
-// mode 0: SVD (S descending). mode 1/2: symmetric eigendecomposition of a block that
-// was shifted by shift[b] (lambda = sigma - shift), eigenvectors = columns of W^T,
-// ordered ascending (1) or by |lambda| descending (2); Vh is not written.
+// mode 0: SVD. mode 1/2: symmetric eigendecomposition of a block shifted by shift[b]
+// (lambda = sigma - shift), eigenvectors = columns of W^T, ordered ascending (1) or by
+// |lambda| descending (2); Vh is not written.
 __global__ void __launch_bounds__(1024) svd_finalize_kernel(const double* __restrict__ work,
                                                             double* __restrict__ U, double* __restrict__ S,
                                                             double* __restrict__ Vh,
@@ -162,6 +277,7 @@ __global__ void __launch_bounds__(1024) svd_finalize_kernel(const double* __rest
   double* sig = reinterpret_cast<double*>(smem_raw);
   int* idx = reinterpret_cast<int*>(sig + pow2);
   __shared__ int n_zero;
+  __shared__ double kmin;
   const int64_t* r = blocks + (int64_t)blockIdx.x * YB_SVD_REC;
   const int64_t m = r[R_M], n = r[R_N], k = r[R_K], L = r[R_L];
   const bool tall = m > n;
@@ -185,8 +301,7 @@ __global__ void __launch_bounds__(1024) svd_finalize_kernel(const double* __rest
   }
   __syncthreads();
   if (mode != 0) {
-    // sort keys may be negative: shift them so that the -1 padding still sorts last
-    __shared__ double kmin;
+    // eigh sort keys may be negative: shift them so that the -1 padding still sorts last
     if (threadIdx.x == 0) {
       double mn = 0.0;
       for (int64_t i = 0; i < k; ++i) mn = fmin(mn, sig[i]);
@@ -219,7 +334,6 @@ __global__ void __launch_bounds__(1024) svd_finalize_kernel(const double* __rest
   double* Ub = U + r[R_U];
   double* Vb = Vh + r[R_V];
   if (mode != 0) {
-    // eigenvalue = (row norm) - shift, recomputed from X to avoid the key transform
     for (int64_t j = warp; j < k; j += nw) {
       const int64_t i = idx[j];
       double acc = 0.0;
@@ -255,8 +369,8 @@ __global__ void __launch_bounds__(1024) svd_finalize_kernel(const double* __rest
   // their vectors by unit vectors orthogonalised (twice) against all earlier ones.
   __shared__ double red[32];
   __shared__ double coef;
-  const int64_t stride_v = tall ? k : 1;     // distance between consecutive entries of one vector
-  const int64_t stride_j = tall ? 1 : n;     // distance between vectors
+  const int64_t stride_v = tall ? k : 1;  // distance between consecutive entries of one vector
+  const int64_t stride_j = tall ? 1 : n;  // distance between vectors
   double* base = tall ? Ub : Vb;
   for (int64_t j = k - n_zero; j < k; ++j) {
     for (int64_t cand = 0; cand < L; ++cand) {
@@ -304,36 +418,72 @@ __global__ void __launch_bounds__(1024) svd_finalize_kernel(const double* __rest
   }
 }
 
+template <typename T>
+int launch_sweeps(T* work, const int64_t* blocks, int n_blocks, const int32_t* pair_items, int n_items,
+                  int max_rounds, int max_sweeps, double tol_stop, int64_t* state, cudaStream_t s) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, svd_sweeps_kernel<T>, kThreads, 0);
+  if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
+  const int need = (n_items + kWarps - 1) / kWarps;
+  int grid = sms * per_sm;
+  if (grid > need) grid = need;
+  if (grid < 1) grid = 1;
+  // zero the barrier/control words (stream-ordered)
+  e = cudaMemsetAsync(state + (int64_t)n_blocks * ST_REC, 0, sizeof(int64_t) * C_REC, s);
+  if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
+  void* args[] = {&work, &blocks, &n_blocks, &pair_items, &n_items, &max_rounds, &max_sweeps, &tol_stop, &state};
+  e = cudaLaunchCooperativeKernel((const void*)svd_sweeps_kernel<T>, dim3(grid), dim3(kThreads), args, 0, s);
+  if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
+  return YB_OK;
+}
+
 }  // namespace
 }  // namespace yb
 
 extern "C" {
 
-int yb_svd_init(const void* a, void* work, const int64_t* blocks, int n_blocks, int dtype, int64_t* counters,
+int yb_svd_init(const void* a, void* work32, const int64_t* blocks, int n_blocks, int dtype, int64_t* state,
                 double* shift, void* stream) {
   if (n_blocks == 0) return YB_OK;
   if (dtype != YB_F64) return YB_ERR_INVALID;
-  if (!a || !work || !blocks || !counters) return YB_ERR_INVALID;
+  if (!a || !work32 || !blocks || !state) return YB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
-  if (shift != nullptr) {
-    yb::block_fro_kernel<<<n_blocks, 256, 0, s>>>((const double*)a, blocks, shift);
-  }
+  if (shift != nullptr) yb::block_fro_kernel<<<n_blocks, 256, 0, s>>>((const double*)a, blocks, shift);
   dim3 grid(64, (unsigned)n_blocks);
-  yb::svd_init_kernel<<<grid, 256, 0, s>>>((const double*)a, (double*)work, blocks, counters, n_blocks, shift);
+  yb::svd_init_kernel<<<grid, 256, 0, s>>>((const double*)a, (float*)work32, blocks, state, shift);
   return yb::check_launch();
 }
 
-int yb_svd_sweep(void* work, const int64_t* blocks, int n_blocks, const int32_t* pair_items, int n_pair_items,
-                 int max_rounds, int dtype, double tol, int64_t* counters, void* stream) {
-  if (n_blocks == 0 || n_pair_items == 0) return YB_OK;
-  if (dtype != YB_F64) return YB_ERR_INVALID;
+int yb_svd_sweeps(void* work, const int64_t* blocks, int n_blocks, const int32_t* pair_items, int n_pair_items,
+                  int max_rounds, int precision, int max_sweeps, double tol_stop, int64_t* state, void* stream) {
+  if (n_blocks == 0 || n_pair_items == 0 || max_sweeps <= 0) return YB_OK;
+  if (!work || !blocks || !pair_items || !state) return YB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
-  const int grid = (n_pair_items + yb::kWarps - 1) / yb::kWarps;
-  for (int rd = 0; rd < max_rounds; ++rd) {
-    yb::svd_round_kernel<<<grid, yb::kWarps * 32, 0, s>>>((double*)work, blocks, pair_items, n_pair_items, rd, tol,
-                                                          counters, n_blocks);
-  }
-  yb::svd_sweep_end_kernel<<<1, 256, 0, s>>>(counters, n_blocks);
+  if (precision == 32)
+    return yb::launch_sweeps<float>((float*)work, blocks, n_blocks, pair_items, n_pair_items, max_rounds, max_sweeps,
+                                    tol_stop, state, s);
+  if (precision == 64)
+    return yb::launch_sweeps<double>((double*)work, blocks, n_blocks, pair_items, n_pair_items, max_rounds,
+                                     max_sweeps, tol_stop, state, s);
+  return YB_ERR_INVALID;
+}
+
+int yb_svd_widen(const void* work32, void* work64, const int64_t* blocks, int n_blocks, int64_t* state,
+                 void* stream) {
+  if (n_blocks == 0) return YB_OK;
+  if (!work32 || !work64 || !blocks || !state) return YB_ERR_INVALID;
+  dim3 grid(64, (unsigned)n_blocks);
+  yb::svd_widen_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>((const float*)work32, (double*)work64, blocks, state);
+  return yb::check_launch();
+}
+
+int yb_svd_shift_prefill(void* work64, const int64_t* blocks, int n_blocks, const double* shift, void* stream) {
+  if (n_blocks == 0) return YB_OK;
+  if (!work64 || !blocks || !shift) return YB_ERR_INVALID;
+  dim3 grid(64, (unsigned)n_blocks);
+  yb::svd_shift_prefill_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>((double*)work64, blocks, shift);
   return yb::check_launch();
 }
 

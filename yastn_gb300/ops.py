@@ -197,32 +197,60 @@ def transpose_dot_sum_backward(C_b, A, B, meta_dot, Areshape, Breshape, Aorder, 
 
 # ----------------------------------------------------------------------------- family (c)
 
-def _jacobi(data, plan, U, S, V, mode, max_sweeps, tol_scale):
-    """Run the batched Jacobi of ``plan`` on ``data`` and write U, S (and Vh for mode 0)."""
+MAX_SWEEPS32 = 40
+TOL_STOP32 = 2.0e-5   # FP32 phase: a sweep whose largest rotation |cos| is below this is final
+TOL_STOP64 = 1.0e-10  # FP64 phase: idem (the next sweep would leave |cos| ~ 1e-20 + rounding)
+NS_STEPS = 2          # Newton-Schulz steps: non-orthogonality ~1e-6 -> 1e-12 -> ~eps
+
+
+def _svd_state_check(state, nb, phase, require_converged):
+    st = state.cpu().numpy()
+    if st[4 * nb + 2] != 0:
+        raise RuntimeError(f"yastn_gb300 svd: grid barrier timed out in the {phase} phase")
+    conv = st[1:4 * nb:4]
+    if require_converged and not conv.all():
+        raise torch.linalg.LinAlgError(f"yastn_gb300 svd: Jacobi did not converge ({phase} phase)")
+    return st[2:4 * nb:4]
+
+
+def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
+    """Mixed-precision batched Jacobi of ``plan`` on ``data``; writes U, S (and Vh for mode 0)."""
     nb = len(plan.blocks)
     dev = data.device
     code = _dtype_code(data.dtype)
     dblocks, dpairs = _dev(plan, 'svd', (plan.blocks, plan.pair_items), dev)
-    work = torch.empty(plan.work_elems, dtype=data.dtype, device=dev)
-    counters = torch.empty(2 * nb, dtype=torch.int64, device=dev)
+    w64 = torch.empty(plan.n64, dtype=torch.float64, device=dev)
+    w32 = torch.empty(plan.n32, dtype=torch.float32, device=dev)
+    state = torch.zeros(4 * nb + 4, dtype=torch.int64, device=dev)
     shift = torch.empty(nb, dtype=torch.float64, device=dev) if mode != 0 else None
+    sp = _vp(shift.data_ptr() if shift is not None else 0)
     st = _stream()
-    N.call('yb_svd_init', _ptr(data), _ptr(work), _ptr(dblocks), nb, code, _ptr(counters),
-           _vp(shift.data_ptr() if shift is not None else 0), st, launches=1 + int(shift is not None))
-    converged = False
-    for sweep in range(max_sweeps):
-        N.call('yb_svd_sweep', _ptr(work), _ptr(dblocks), nb, _ptr(dpairs), len(plan.pair_items), plan.max_rounds,
-               code, float(tol_scale), _ptr(counters), st, launches=plan.max_rounds + 1)
-        if sweep >= 2 and int(counters[:nb].max().item()) == 0:
-            converged = True
-            break
-    if not converged:
-        raise torch.linalg.LinAlgError(f"yastn_gb300: Jacobi did not converge in {max_sweeps} sweeps")
-    N.call('yb_svd_finalize', _ptr(work), _ptr(U), _ptr(S), _vp(V.data_ptr() if V is not None else 0), _ptr(dblocks),
-           nb, code, plan.max_k, mode, _vp(shift.data_ptr() if shift is not None else 0), st)
+    N.call('yb_svd_init', _ptr(data), _ptr(w32), _ptr(dblocks), nb, code, _ptr(state), sp, st,
+           launches=1 + int(shift is not None))
+    N.call('yb_svd_sweeps', _ptr(w32), _ptr(dblocks), nb, _ptr(dpairs), len(plan.pair_items), plan.max_rounds, 32,
+           MAX_SWEEPS32, TOL_STOP32, _ptr(state), st)
+    _svd_state_check(state, nb, 'FP32', False)
+    N.call('yb_svd_widen', _ptr(w32), _ptr(w64), _ptr(dblocks), nb, _ptr(state), st)
+    w0, t0, n0, ws = plan.w_range
+    W, Wn = w64[w0:w0 + ws], w64[n0:n0 + ws]
+    for _ in range(NS_STEPS):
+        Wn.copy_(W)
+        run_gemm(plan.gram, w64, w64, w64)
+        run_gemm(plan.ns, w64, w64, w64, alpha=-0.5, beta=1.5)
+        W.copy_(Wn)
+    if shift is not None:
+        N.call('yb_svd_shift_prefill', _ptr(w64), _ptr(dblocks), nb, _ptr(shift), st)
+        run_gemm(plan.xform, w64, data, w64, beta=1.0)
+    else:
+        run_gemm(plan.xform, w64, data, w64)
+    N.call('yb_svd_sweeps', _ptr(w64), _ptr(dblocks), nb, _ptr(dpairs), len(plan.pair_items), plan.max_rounds, 64,
+           max_sweeps, TOL_STOP64, _ptr(state), st)
+    _svd_state_check(state, nb, 'FP64', True)
+    N.call('yb_svd_finalize', _ptr(w64), _ptr(U), _ptr(S), _vp(V.data_ptr() if V is not None else 0), _ptr(dblocks),
+           nb, code, plan.max_k, mode, sp, st)
 
 
-def svd(data, meta, sizes, max_sweeps=MAX_SWEEPS, tol_scale=1.0):
+def svd(data, meta, sizes, max_sweeps=MAX_SWEEPS):
     """Thin SVD of every block (one-sided Jacobi); returns (U, S, Vh) flat tensors."""
     data = _check(data)
     if _dtype_code(data.dtype) != N.YB_F64:
@@ -234,7 +262,7 @@ def svd(data, meta, sizes, max_sweeps=MAX_SWEEPS, tol_scale=1.0):
     plan = P.svd_plan(meta)
     if len(plan.blocks) == 0:
         return U, S, V
-    _jacobi(data, plan, U, S, V, 0, max_sweeps, tol_scale)
+    _jacobi(data, plan, U, S, V, 0, max_sweeps)
     return U, S, V
 
 
@@ -283,7 +311,7 @@ def eigh(data, meta, sizes, order_by_magnitude=False, max_sweeps=MAX_SWEEPS):
     plan = P.svd_plan(svd_meta)
     if len(plan.blocks) == 0:
         return S, U
-    _jacobi(data, plan, U, S, None, 2 if order_by_magnitude else 1, max_sweeps, 1.0)
+    _jacobi(data, plan, U, S, None, 2 if order_by_magnitude else 1, max_sweeps)
     return S, U
 
 
