@@ -110,7 +110,8 @@ int yb_grouped_gemm(const void* a, const void* b, void* c, int dtype,
  * accumulated rotations (X = W X_0 throughout).
  * pair_items: int32 pairs (block, pair index 0..N/2-1) over all blocks.
  * state: int64[4*n_blocks + 4]: per block (max |cos| of the sweep in progress as double
- *   bits, converged flag, sweeps run in the current phase, unused), then the control
+ *   bits, converged flag, sweeps run in the current phase, largest |cos| of the last
+ *   completed sweep), then the control
  *   words of the grid barrier (count, generation, error flag, all-converged flag).
  * Sequence (mixed precision): yb_svd_init (X32 = A or A^T, W32 = I); yb_svd_sweeps with
  * precision 32; yb_svd_widen (W = double(W32)); the host orthonormalises W (Newton-Schulz

@@ -33,8 +33,8 @@ constexpr long long kSpinLimit = 1ll << 22;
 // record fields
 enum { R_A = 0, R_M, R_N, R_U, R_S, R_V, R_X, R_W, R_P, R_K, R_L, R_NP, R_T, R_X32, R_W32 };
 // per-block state (int64): [0] max |cos| of the sweep in progress (double bits),
-// [1] converged flag, [2] sweeps run in the current phase, [3] unused
-enum { ST_MAXCOS = 0, ST_CONV = 1, ST_SWEEPS = 2, ST_REC = 4 };
+// [1] converged flag, [2] sweeps run in the current phase, [3] largest |cos| of the last sweep
+enum { ST_MAXCOS = 0, ST_CONV = 1, ST_SWEEPS = 2, ST_LASTCOS = 3, ST_REC = 4 };
 // control words after the per-block state: [0] barrier count [1] barrier generation
 // [2] error flag [3] all-converged flag
 enum { C_COUNT = 0, C_GEN = 1, C_ERR = 2, C_DONE = 3, C_REC = 4 };
@@ -159,27 +159,56 @@ __device__ bool grid_barrier(unsigned long long* ctrl, unsigned nblocks) {
   return ok != 0;
 }
 
+constexpr int kChunk = 8;  // elements per lane per row kept in flight
+
+// Rotates rows (p, q) of X and W by one Jacobi rotation. Loads are issued a chunk at a
+// time (kChunk per lane and row, all before any store of the chunk) so that the L2
+// latency is paid once per chunk rather than once per element. Rows are rewritten by
+// other SMs between rounds, so loads bypass L1 (ld.global.cg).
+template <typename T>
+__device__ __forceinline__ void rotate_rows(T* __restrict__ a, T* __restrict__ b, int64_t len, int lane, T c, T s) {
+  for (int64_t base = 0; base < len; base += 32 * kChunk) {
+    T u[kChunk], v[kChunk];
+#pragma unroll
+    for (int j = 0; j < kChunk; ++j) {
+      const int64_t i = base + j * 32 + lane;
+      u[j] = (i < len) ? __ldcg(a + i) : T(0);
+      v[j] = (i < len) ? __ldcg(b + i) : T(0);
+    }
+#pragma unroll
+    for (int j = 0; j < kChunk; ++j) {
+      const int64_t i = base + j * 32 + lane;
+      if (i < len) {
+        a[i] = c * u[j] - s * v[j];
+        b[i] = s * u[j] + c * v[j];
+      }
+    }
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ void rotate_pair(T* __restrict__ X, T* __restrict__ W, int64_t k, int64_t L, int64_t p,
                                             int64_t q, int lane, int64_t* st) {
   T* xp = X + p * L;
   T* xq = X + q * L;
-  // rows are rewritten by other SMs between rounds: loads bypass L1 (ld.global.cg)
-  double al = 0.0, be = 0.0, ga = 0.0;
-  int64_t l = lane;
-  for (; l + 96 < L; l += 128) {  // four independent loads in flight per row
-    const double u0 = __ldcg(xp + l), u1 = __ldcg(xp + l + 32), u2 = __ldcg(xp + l + 64), u3 = __ldcg(xp + l + 96);
-    const double v0 = __ldcg(xq + l), v1 = __ldcg(xq + l + 32), v2 = __ldcg(xq + l + 64), v3 = __ldcg(xq + l + 96);
-    al = fma(u0, u0, al); al = fma(u1, u1, al); al = fma(u2, u2, al); al = fma(u3, u3, al);
-    be = fma(v0, v0, be); be = fma(v1, v1, be); be = fma(v2, v2, be); be = fma(v3, v3, be);
-    ga = fma(u0, v0, ga); ga = fma(u1, v1, ga); ga = fma(u2, v2, ga); ga = fma(u3, v3, ga);
+  // partial sums in the working precision (FP32 in the FP32 phase keeps the FP64 pipe free)
+  T al_ = 0, be_ = 0, ga_ = 0;
+  for (int64_t base = 0; base < L; base += 32 * kChunk) {
+    T u[kChunk], v[kChunk];
+#pragma unroll
+    for (int j = 0; j < kChunk; ++j) {
+      const int64_t i = base + j * 32 + lane;
+      u[j] = (i < L) ? __ldcg(xp + i) : T(0);
+      v[j] = (i < L) ? __ldcg(xq + i) : T(0);
+    }
+#pragma unroll
+    for (int j = 0; j < kChunk; ++j) {
+      al_ = fma(u[j], u[j], al_);
+      be_ = fma(v[j], v[j], be_);
+      ga_ = fma(u[j], v[j], ga_);
+    }
   }
-  for (; l < L; l += 32) {
-    const double u = __ldcg(xp + l), v = __ldcg(xq + l);
-    al = fma(u, u, al);
-    be = fma(v, v, be);
-    ga = fma(u, v, ga);
-  }
+  double al = al_, be = be_, ga = ga_;
   al = warp_sum(al);
   be = warp_sum(be);
   ga = warp_sum(ga);
@@ -191,18 +220,8 @@ __device__ __forceinline__ void rotate_pair(T* __restrict__ X, T* __restrict__ W
   const double t = copysign(1.0, zeta) / (fabs(zeta) + hypot(1.0, zeta));
   const double cd = 1.0 / sqrt(fma(t, t, 1.0));
   const T c = (T)cd, s = (T)(cd * t);
-  for (int64_t j = lane; j < L; j += 32) {
-    const T u = __ldcg(xp + j), v = __ldcg(xq + j);
-    xp[j] = c * u - s * v;
-    xq[j] = s * u + c * v;
-  }
-  T* wp = W + p * k;
-  T* wq = W + q * k;
-  for (int64_t j = lane; j < k; j += 32) {
-    const T u = __ldcg(wp + j), v = __ldcg(wq + j);
-    wp[j] = c * u - s * v;
-    wq[j] = s * u + c * v;
-  }
+  rotate_rows<T>(xp, xq, L, lane, c, s);
+  rotate_rows<T>(W + p * k, W + q * k, k, lane, c, s);
 }
 
 // All sweeps of one precision phase in one cooperative launch.
@@ -251,6 +270,7 @@ __global__ void __launch_bounds__(kThreads) svd_sweeps_kernel(T* __restrict__ wo
         if (st[ST_CONV]) continue;
         const double mc = __longlong_as_double((long long)st[ST_MAXCOS]);
         st[ST_SWEEPS] += 1;
+        st[ST_LASTCOS] = st[ST_MAXCOS];
         st[ST_MAXCOS] = 0;
         if (mc <= tol_stop) st[ST_CONV] = 1; else any_active = 1;
       }

@@ -198,8 +198,9 @@ def transpose_dot_sum_backward(C_b, A, B, meta_dot, Areshape, Breshape, Aorder, 
 # ----------------------------------------------------------------------------- family (c)
 
 MAX_SWEEPS32 = 40
-TOL_STOP32 = 2.0e-5   # FP32 phase: a sweep whose largest rotation |cos| is below this is final
-TOL_STOP64 = 1.0e-10  # FP64 phase: idem (the next sweep would leave |cos| ~ 1e-20 + rounding)
+TOL_STOP32 = 1.0e-4   # FP32 phase ends after a sweep whose largest rotation |cos| is below this
+TOL_STOP64 = 1.0e-8   # FP64 phase: idem; Jacobi converges quadratically, so the residual |cos|
+                      # after such a sweep is ~1e-16 for separated singular values
 NS_STEPS = 2          # Newton-Schulz steps: non-orthogonality ~1e-6 -> 1e-12 -> ~eps
 
 
