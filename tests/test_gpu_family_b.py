@@ -106,3 +106,54 @@ def test_cfg1_full_size_dot(cuda_device):
     assert rel(got, ref) <= TOL
     chk = c2['out'][0].checksum
     assert abs(float(got.sum()) - chk['sum0']) <= 1e-9 * chk['abs0']
+
+
+@pytest.mark.parametrize('name', ['tensordot_fuse_to_matrix', 'tensordot_fuse_contracted'])
+def test_dot_ozaki_on_reference_calls(name, cuda_device):
+    """Emulated FP64 (8 BF16 digit slices) within 1e-12 of the reference products."""
+    tr = load_trace(name)
+    n = 0
+    for c in tr['calls']:
+        if c['fn'] != 'dot' or np.iscomplexobj(c['args'][0]) or np.iscomplexobj(c['args'][1]):
+            continue
+        A, B, meta, Dsize = c['args']
+        got = host(ops.dot_ozaki(dev(A), dev(B), meta, Dsize))
+        assert rel(got, c['out'][0]) <= TOL
+        n += 1
+    assert n > 0
+
+
+def test_cfg1_full_size_dot_ozaki(cuda_device):
+    """The benchmark's 13 sector GEMMs emulated: error vs the FP64 oracle per slice count."""
+    tr = load_trace('cfg1')
+    A, B = cfg1_inputs(tr)
+    c0, c1, c2 = tr['calls'][:3]
+    Am = oracle.transpose_and_merge(A, *c0['args'][1:])
+    Bm = oracle.transpose_and_merge(B, *c1['args'][1:])
+    _, _, meta, Dsize = c2['args']
+    ref = oracle.dot(Am, Bm, meta, Dsize)
+    errs = {}
+    for s in (6, 7, 8):
+        errs[s] = rel(host(ops.dot_ozaki(dev(Am), dev(Bm), meta, Dsize, slices=s)), ref)
+    assert errs[8] <= TOL, errs
+    assert errs[7] <= 1e-10 and errs[6] <= 1e-8, errs
+
+
+def test_dot_ozaki_wide_dynamic_range(cuda_device):
+    """Per-block scales 10^U(-4,0) (the precision-study inputs): per-row exponents keep it exact."""
+    rng = np.random.default_rng(9)
+    shapes = [(40, 70, 30), (64, 64, 64), (3, 200, 5)]
+    meta, oa, ob, oc, As, Bs = [], 0, 0, 0, [], []
+    for m, k, n in shapes:
+        a = rng.normal(size=(m, k)) * 10 ** rng.uniform(-4, 0)
+        b = rng.normal(size=(k, n)) * 10 ** rng.uniform(-4, 0)
+        meta.append(((oc, oc + m * n), (m, n), (oa, oa + m * k), (m, k), (ob, ob + k * n), (k, n)))
+        oa += m * k; ob += k * n; oc += m * n
+        As.append(a.ravel()); Bs.append(b.ravel())
+    meta = tuple(meta)
+    A, B = np.concatenate(As), np.concatenate(Bs)
+    ref = oracle.dot(A, B, meta, oc)
+    got = host(ops.dot_ozaki(dev(A), dev(B), meta, oc))
+    for slc, Dc, *_ in meta:
+        r, g = ref[slc[0]:slc[1]], got[slc[0]:slc[1]]
+        assert np.abs(g - r).max() <= TOL * np.abs(r).max()

@@ -235,3 +235,56 @@ def test_mixed_precision_jacobi_schedule_on_plan_layout():
         s = np.sort(np.linalg.norm(X, axis=1))[::-1]
         sr = S[mt[4][0]:mt[4][1]]
         assert np.abs(s - sr).max() <= 1e-13 * max(sr.max(), 1.0)
+
+
+def _ozaki_digits(x, s):
+    """NumPy restatement of the split of csrc/yb_ozaki.cu (rows of x)."""
+    mx = np.abs(x).max(axis=1)
+    e = np.where(mx > 0, np.frexp(mx)[1], 0)
+    v = np.ldexp(x, -e[:, None])
+    digits = []
+    for _ in range(s):
+        y = v * 128.0
+        d = np.rint(y)
+        v = y - d
+        digits.append(d)
+    return e, digits
+
+
+@pytest.mark.parametrize('s', [6, 7, 8])
+def test_ozaki_split_and_slice_products(s):
+    """Digits are BF16-exact integers; the kept slice pairs reproduce A @ B to the bound."""
+    rng = np.random.default_rng(6)
+    A = rng.normal(size=(37, 150)) * 10.0 ** rng.uniform(-4, 0, size=(37, 1))
+    B = rng.normal(size=(150, 29))
+    ea, da = _ozaki_digits(A, s)
+    eb, db = _ozaki_digits(B.T, s)
+    for d in da + db:
+        assert np.all(np.abs(d) <= 128) and np.all(d == np.rint(d))
+        # exact in bfloat16: at most 8 significant bits
+        m, _ = np.frexp(np.abs(d[d != 0]))
+        assert np.all((m * 256) == np.rint(m * 256))
+    rec = sum(d * 2.0 ** (-7 * (t + 1)) for t, d in enumerate(da)) * 2.0 ** ea[:, None]
+    # remainder after s digits: |v_s| <= 1/2 at weight 2^{-7s}, row scale 2^{e_i}
+    assert np.all(np.abs(rec - A).max(axis=1) <= 0.5 * 2.0 ** (-7 * s) * 2.0 ** ea)
+    C = np.zeros((37, 29))
+    for ta in range(s):
+        for tb in range(s - ta):
+            P = da[ta] @ db[tb].T  # exact integers (< 2^53)
+            C += P * 2.0 ** (-7 * (ta + tb))
+    C *= 2.0 ** (ea[:, None] + eb[None, :] - 14)
+    ref = A @ B
+    # truncation of the dropped digits + FP64 rounding of both summations (K = 150)
+    bound = ((s + 2) * 2.0 ** (-7 * s) + 2 * 150 * 2.0 ** -53) * (np.abs(A) @ np.abs(B)).max()
+    assert np.abs(C - ref).max() <= bound
+
+
+def test_ozaki_plan_records():
+    tr = load_trace('tensordot_fuse_contracted')
+    c = [c for c in tr['calls'] if c['fn'] == 'dot' and not np.iscomplexobj(c['args'][0])][0]
+    _, _, meta, Dsize = c['args']
+    plan = P.ozaki_dot_plan(meta, 8)
+    assert len(plan.outs) == len(meta)
+    assert len({tuple(r[:1]) for r in plan.a_recs}) == len(plan.a_recs)  # each A block split once
+    assert all(r[7] % 16 == 0 and r[7] >= r[2] for r in plan.a_recs)
+    assert all(int(r[5]) % 16 == 0 for r in plan.a_recs) and all(int(r[5]) % 16 == 0 for r in plan.b_recs)

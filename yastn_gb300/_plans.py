@@ -338,6 +338,61 @@ def tds_plan(meta_dot, Areshape, Breshape, Aoffs, Boffs):
     return CACHE.get((meta_dot, Areshape, Breshape), ('tds',), build)
 
 
+class OzakiPlan:
+    """Split records and GEMM tiles of the split-operand (Ozaki) emulated FP64 dot."""
+
+    def __init__(self, a_recs, b_recs, outs, tiles, a_size, b_size, a_exps, b_exps, a_rows, b_rows, flops, s):
+        self.a_recs, self.b_recs, self.outs, self.tiles = a_recs, b_recs, outs, tiles
+        self.a_size, self.b_size, self.a_exps, self.b_exps = a_size, b_size, a_exps, b_exps
+        self.a_rows, self.b_rows = a_rows, b_rows
+        self.flops = flops
+        self.slices = s
+        self._dev = {}
+
+
+def ozaki_dot_plan(meta_dot, s):
+    """C[slc] = A[sla] @ B[slb] with A rows / B columns split into ``s`` BF16 digit slices."""
+    def build():
+        a_map, b_map, a_recs, b_recs = {}, {}, [], []
+        a_size = b_size = a_ex = b_ex = 0
+        outs, flops = [], 0
+        for slc, Dc, sla, Da, slb, Db in meta_dot:
+            m, K = Da
+            n = Db[1]
+            Kp = (K + 15) // 16 * 16
+            if sla[0] not in a_map:
+                a_map[sla[0]] = (a_size, a_ex)
+                a_recs.append((sla[0], m, K, K, 1, a_size, a_ex, Kp))
+                a_size += s * m * Kp
+                a_ex += m
+            if slb[0] not in b_map:
+                b_map[slb[0]] = (b_size, b_ex)
+                b_recs.append((slb[0], n, K, 1, n, b_size, b_ex, Kp))
+                b_size += s * n * Kp
+                b_ex += n
+            ao, ae = a_map[sla[0]]
+            bo, be = b_map[slb[0]]
+            outs.append((slc[0], m, n, n, ao, ae, bo, be, K, Kp, 0, 0, 0, 0, 0, 0))
+            flops += 2 * m * n * K
+        outs = np.array(outs, dtype=np.int64).reshape(-1, 16)
+        tiles = []
+        for oi, o in enumerate(outs):
+            m, n, K = int(o[1]), int(o[2]), int(o[8])
+            if m == 0 or n == 0:
+                continue
+            for tr in range((m + 63) // 64):
+                for tc in range((n + 63) // 64):
+                    tiles.append((K, oi, tr, tc))
+        tiles.sort(key=lambda x: -x[0])
+        tiles = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles], dtype=np.int32).reshape(-1, 4)
+        a_recs = np.array(a_recs, dtype=np.int64).reshape(-1, 8)
+        b_recs = np.array(b_recs, dtype=np.int64).reshape(-1, 8)
+        a_rows = int(a_recs[:, 1].max()) if len(a_recs) else 0
+        b_rows = int(b_recs[:, 1].max()) if len(b_recs) else 0
+        return OzakiPlan(a_recs, b_recs, outs, tiles, a_size, b_size, a_ex, b_ex, a_rows, b_rows, flops, s)
+    return CACHE.get((meta_dot,), ('ozaki_dot', s), build)
+
+
 # ----------------------------------------------------------------------------- SVD
 
 class SvdPlan:

@@ -1,0 +1,281 @@
+// Family (b'): FP64 sector GEMMs emulated with split operands on BF16 tensor cores
+// (Ozaki scheme, error-free splitting with per-row / per-column exponents).
+//
+// Splitting: every row i of A (and every column j of B) is scaled by a power of two
+// 2^-e so that its entries lie in (-1, 1), then peeled into s signed integer digits
+//     v = sum_{t<s} d_t 2^{-7(t+1)},  d_0 in [-128, 128], d_t in [-64, 64] (t > 0),
+// by repeated d = rint(128 v), v = 128 v - d (exact in FP64). Every digit is an integer
+// of at most 8 significant bits and is stored exactly as BF16. A slice pair (t_a, t_b)
+// contributes 2^{e_i + f_j - 14 - 7 (t_a + t_b)} (D_A[t_a] D_B[t_b])_ij; pairs with
+// t_a + t_b <= s - 1 are kept (s(s+1)/2 products), the rest are below the FP64 rounding
+// of the result for s = 8 (57 bits of each operand are represented).
+//
+// Exactness of the tensor-core products: a digit product is an integer of magnitude
+// <= 2^14; all pairs of one diagonal t = t_a + t_b share one FP32 accumulator over a
+// K-chunk of 128, so a partial sum is an integer below (t+1) * 128 * 2^13 < 2^24 and is
+// exact in FP32. After each chunk the diagonals are folded into FP64 accumulators
+// (smallest first); the final scale is applied with scalbn.
+//
+// GEMM kernel: 64x64 output tile per CTA, 8 warps each owning a 32x16 sub-tile (2x2
+// mma.sync.m16n8k16 tiles), K-step 16 staged in shared memory with cp.async (double
+// buffered, rows padded to 48 bytes so ldmatrix is bank-conflict free).
+#include <cuda_bf16.h>
+#include "yb_common.cuh"
+
+namespace yb {
+namespace {
+
+constexpr int kTile = 64;
+constexpr int kK = 16;
+constexpr int kRow = 24;  // smem row stride in bf16 elements (16 data + 8 pad = 48 bytes)
+constexpr int kChunkSteps = 8;  // K-chunk = 8 * 16 = 128 for exact FP32 diagonal sums
+constexpr int kThreads = 256;
+
+// ------------------------------------------------------------------ splitting
+// rec: [0] src offset [1] rows [2] K [3] row stride [4] col stride [5] dst offset (bf16)
+//      [6] exponent offset [7] Kp (K rounded up to 16)
+// dst layout: [slice][row][Kp] bf16, padding zero-filled.
+__device__ __forceinline__ void split_value(double a, int e, int s, __nv_bfloat16* dst, int64_t slice_stride) {
+  double v = scalbn(a, -e);
+  for (int t = 0; t < s; ++t) {
+    const double x = v * 128.0;
+    const double d = rint(x);
+    v = x - d;
+    dst[t * slice_stride] = __double2bfloat16(d);
+  }
+}
+
+__global__ void split_rows_warp_kernel(const double* __restrict__ src, __nv_bfloat16* __restrict__ slices,
+                                       int* __restrict__ exps, const int64_t* __restrict__ recs, int s) {
+  // one warp per row, lanes along K (rows with unit column stride)
+  const int64_t* r = recs + (int64_t)blockIdx.y * 8;
+  const int64_t rows = r[1], K = r[2], rs = r[3], cs = r[4], Kp = r[7];
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= rows) return;
+  const double* a = src + r[0] + row * rs;
+  double mx = 0.0;
+  for (int64_t l = lane; l < K; l += 32) mx = fmax(mx, fabs(a[l * cs]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  int e = 0;
+  if (mx > 0.0) frexp(mx, &e);  // mx = f 2^e, f in [0.5, 1): |a| < 2^e
+  if (lane == 0) exps[r[6] + row] = e;
+  const int64_t slice_stride = rows * Kp;
+  __nv_bfloat16* d = slices + r[5] + row * Kp;
+  for (int64_t l = lane; l < Kp; l += 32) {
+    if (l < K) {
+      split_value(a[l * cs], e, s, d + l, slice_stride);
+    } else {
+      for (int t = 0; t < s; ++t) d[l + t * slice_stride] = __double2bfloat16(0.0);
+    }
+  }
+}
+
+__global__ void split_rows_thread_kernel(const double* __restrict__ src, __nv_bfloat16* __restrict__ slices,
+                                         int* __restrict__ exps, const int64_t* __restrict__ recs, int s) {
+  // one thread per row, consecutive threads on consecutive rows (rows with unit row stride)
+  const int64_t* r = recs + (int64_t)blockIdx.y * 8;
+  const int64_t rows = r[1], K = r[2], rs = r[3], cs = r[4], Kp = r[7];
+  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= rows) return;
+  const double* a = src + r[0] + row * rs;
+  double mx = 0.0;
+  for (int64_t l = 0; l < K; ++l) mx = fmax(mx, fabs(a[l * cs]));
+  int e = 0;
+  if (mx > 0.0) frexp(mx, &e);
+  exps[r[6] + row] = e;
+  const int64_t slice_stride = rows * Kp;
+  __nv_bfloat16* d = slices + r[5] + row * Kp;
+  for (int64_t l = 0; l < Kp; ++l) {
+    if (l < K) {
+      split_value(a[l * cs], e, s, d + l, slice_stride);
+    } else {
+      for (int t = 0; t < s; ++t) d[l + t * slice_stride] = __double2bfloat16(0.0);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ GEMM
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
+  const unsigned saddr = (unsigned)__cvta_generic_to_shared(smem);
+  const int n = valid ? 16 : 0;
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(saddr), "l"(gmem), "r"(n));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+
+__device__ __forceinline__ void ldmatrix_x4(unsigned& r0, unsigned& r1, unsigned& r2, unsigned& r3, const void* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3) : "r"(a));
+}
+__device__ __forceinline__ void ldmatrix_x2(unsigned& r0, unsigned& r1, const void* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n" : "=r"(r0), "=r"(r1) : "r"(a));
+}
+__device__ __forceinline__ void mma_bf16(float* c, const unsigned* a, const unsigned* b) {
+  asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+               "{%0,%1,%2,%3};\n"
+               : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// out record: [0] c offset [1] m [2] n [3] ldc [4] A slices offset [5] A exp offset
+//             [6] B slices offset [7] B exp offset [8] K [9] Kp
+template <int S>
+__global__ void __launch_bounds__(kThreads, 1) ozaki_gemm_kernel(const __nv_bfloat16* __restrict__ As,
+                                                                 const int* __restrict__ Ae,
+                                                                 const __nv_bfloat16* __restrict__ Bs,
+                                                                 const int* __restrict__ Be, double* __restrict__ C,
+                                                                 const int64_t* __restrict__ outs,
+                                                                 const int32_t* __restrict__ tiles) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __nv_bfloat16* sA = reinterpret_cast<__nv_bfloat16*>(smem_raw);          // [2][S][64][kRow]
+  __nv_bfloat16* sB = sA + 2 * S * kTile * kRow;                           // [2][S][64][kRow]
+  const int4 tl = reinterpret_cast<const int4*>(tiles)[blockIdx.x];
+  const int64_t* o = outs + (int64_t)tl.x * 16;
+  const int64_t c_off = o[0], m = o[1], n = o[2], ldc = o[3];
+  const int64_t a_sl = o[4], a_ex = o[5], b_sl = o[6], b_ex = o[7], Kp = o[9];
+  const int64_t row0 = (int64_t)tl.y * kTile, col0 = (int64_t)tl.z * kTile;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wm = warp & 1, wn = warp >> 1;  // warp sub-tile: rows wm*32.., cols wn*16..
+
+  const int64_t a_stride = m * Kp, b_stride = n * Kp;
+  auto stage = [&](int buf, int64_t k0) {
+    // S slices x 64 rows x 16 k = S*128 chunks of 16 bytes for each operand
+    for (int c = threadIdx.x; c < S * kTile * 2; c += kThreads) {
+      const int t = c / (kTile * 2), rem = c % (kTile * 2), rr = rem >> 1, half = rem & 1;
+      const int64_t ga = row0 + rr, gb = col0 + rr;
+      const bool va = ga < m, vb = gb < n;
+      const __nv_bfloat16* srcA = As + a_sl + t * a_stride + (va ? ga : 0) * Kp + k0 + half * 8;
+      const __nv_bfloat16* srcB = Bs + b_sl + t * b_stride + (vb ? gb : 0) * Kp + k0 + half * 8;
+      cp_async16(sA + ((buf * S + t) * kTile + rr) * kRow + half * 8, srcA, va);
+      cp_async16(sB + ((buf * S + t) * kTile + rr) * kRow + half * 8, srcB, vb);
+    }
+    cp_async_commit();
+  };
+
+  float acc[S][2][2][4];
+  double acc64[2][2][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc64[i][j][v] = 0.0;
+#pragma unroll
+  for (int d = 0; d < S; ++d)
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[d][i][j][v] = 0.f;
+
+  const int64_t nsteps = Kp / kK;
+  if (nsteps > 0) stage(0, 0);
+  for (int64_t st = 0; st < nsteps; ++st) {
+    const int buf = st & 1;
+    cp_async_wait_all();
+    __syncthreads();
+    if (st + 1 < nsteps) stage(buf ^ 1, (st + 1) * kK);
+#pragma unroll
+    for (int ta = 0; ta < S; ++ta) {
+      unsigned af[2][4];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const __nv_bfloat16* p = sA + ((buf * S + ta) * kTile + wm * 32 + i * 16 + (lane & 15)) * kRow + (lane >> 4) * 8;
+        ldmatrix_x4(af[i][0], af[i][1], af[i][2], af[i][3], p);
+      }
+#pragma unroll
+      for (int tb = 0; tb < S - ta; ++tb) {
+        unsigned bf[2][2];
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          const __nv_bfloat16* p =
+              sB + ((buf * S + tb) * kTile + wn * 16 + j * 8 + (lane & 7)) * kRow + ((lane >> 3) & 1) * 8;
+          ldmatrix_x2(bf[j][0], bf[j][1], p);
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+          for (int j = 0; j < 2; ++j) mma_bf16(acc[ta + tb][i][j], af[i], bf[j]);
+      }
+    }
+    if (((st + 1) % kChunkSteps) == 0 || st + 1 == nsteps) {
+      // fold the exact FP32 diagonal sums into FP64, smallest diagonal first
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            double sum = 0.0;
+#pragma unroll
+            for (int d = S - 1; d >= 0; --d) {
+              sum = fma((double)acc[d][i][j][v], scalbn(1.0, -7 * d), sum);
+              acc[d][i][j][v] = 0.f;
+            }
+            acc64[i][j][v] += sum;
+          }
+    }
+  }
+  // epilogue: C = acc64 * 2^(e_i + f_j - 14)
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int64_t gi = row0 + wm * 32 + i * 16 + (lane >> 2) + (v >= 2 ? 8 : 0);
+        const int64_t gj = col0 + wn * 16 + j * 8 + (lane & 3) * 2 + (v & 1);
+        if (gi < m && gj < n) C[c_off + gi * ldc + gj] = scalbn(acc64[i][j][v], Ae[a_ex + gi] + Be[b_ex + gj] - 14);
+      }
+}
+
+template <int S>
+int launch_gemm(const void* As, const int* Ae, const void* Bs, const int* Be, double* C, const int64_t* outs,
+                const int32_t* tiles, int n_tiles, cudaStream_t s) {
+  const size_t smem = (size_t)2 * 2 * S * kTile * kRow * sizeof(__nv_bfloat16);
+  cudaError_t e = cudaFuncSetAttribute(ozaki_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
+  ozaki_gemm_kernel<S><<<n_tiles, kThreads, smem, s>>>((const __nv_bfloat16*)As, Ae, (const __nv_bfloat16*)Bs, Be, C,
+                                                       outs, tiles);
+  return check_launch();
+}
+
+}  // namespace
+}  // namespace yb
+
+extern "C" {
+
+int yb_ozaki_split(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs, int max_rows,
+                   int slices_count, int warp_per_row, void* stream) {
+  if (n_recs == 0 || max_rows == 0) return YB_OK;
+  if (!src || !slices || !exps || !recs || slices_count < 1 || slices_count > 8) return YB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (warp_per_row) {
+    dim3 grid((unsigned)((max_rows + 7) / 8), (unsigned)n_recs);
+    yb::split_rows_warp_kernel<<<grid, 256, 0, s>>>(src, (__nv_bfloat16*)slices, exps, recs, slices_count);
+  } else {
+    dim3 grid((unsigned)((max_rows + 127) / 128), (unsigned)n_recs);
+    yb::split_rows_thread_kernel<<<grid, 128, 0, s>>>(src, (__nv_bfloat16*)slices, exps, recs, slices_count);
+  }
+  return yb::check_launch();
+}
+
+int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps, double* c,
+                  const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count, void* stream) {
+  if (n_tiles == 0) return YB_OK;
+  if (!a_slices || !a_exps || !b_slices || !b_exps || !c || !outs || !tiles) return YB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (slices_count) {
+    case 6: return yb::launch_gemm<6>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, s);
+    case 7: return yb::launch_gemm<7>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, s);
+    case 8: return yb::launch_gemm<8>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, s);
+    default: return YB_ERR_INVALID;
+  }
+}
+
+}  // extern "C"

@@ -140,6 +140,38 @@ def dot(A, B, meta_dot, Dsize):
     return run_gemm(plan, A, B, out)
 
 
+OZAKI_SLICES = 8  # 57 bits per operand: FP64-grade products
+
+
+def dot_ozaki(A, B, meta_dot, Dsize, slices=OZAKI_SLICES):
+    """``dot`` with the FP64 sector GEMMs emulated on BF16 tensor cores (split operands).
+
+    Real float64 operands only. Each A row / B column is split into ``slices`` BF16 digit
+    planes (scratch of 2 * slices bytes per operand element); all slice-pair products
+    with digit-weight sum below ``slices`` are accumulated exactly in FP32 per K-chunk and
+    combined in FP64. ``slices=8`` reproduces the FP64 product to its rounding level.
+    """
+    A, B = promote(_check(A, 'A'), _check(B, 'B'))
+    if A.dtype != torch.float64:
+        raise NotImplementedError("yastn_gb300 dot_ozaki: real float64 operands only")
+    plan = P.ozaki_dot_plan(meta_dot, slices)
+    out = torch.zeros(Dsize, dtype=A.dtype, device=A.device)
+    if len(plan.tiles) == 0:
+        return out
+    dev = A.device
+    dar, dbr, dout, dtl = _dev(plan, 'ozaki', (plan.a_recs, plan.b_recs, plan.outs, plan.tiles), dev)
+    a_sl = torch.empty(plan.a_size, dtype=torch.bfloat16, device=dev)
+    b_sl = torch.empty(plan.b_size, dtype=torch.bfloat16, device=dev)
+    a_ex = torch.empty(max(plan.a_exps, 1), dtype=torch.int32, device=dev)
+    b_ex = torch.empty(max(plan.b_exps, 1), dtype=torch.int32, device=dev)
+    st = _stream()
+    N.call('yb_ozaki_split', _ptr(A), _ptr(a_sl), _ptr(a_ex), _ptr(dar), len(plan.a_recs), plan.a_rows, slices, 1, st)
+    N.call('yb_ozaki_split', _ptr(B), _ptr(b_sl), _ptr(b_ex), _ptr(dbr), len(plan.b_recs), plan.b_rows, slices, 0, st)
+    N.call('yb_ozaki_gemm', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
+           len(plan.tiles), slices, st)
+    return out
+
+
 def dot_backward(C_b, A, B, meta_dot, need_a=True, need_b=True):
     A, B = promote(_check(A, 'A'), _check(B, 'B'))
     C_b = _check(C_b, 'C_b')
