@@ -259,6 +259,28 @@ def run_gpu(args, wl):
     clk = clocks.stop()
     t_e2e = sum(a.elapsed_time(b) for a, b in e2e_ev) / len(e2e_ev) * 1e-3
 
+    # the same tensordot with the emulated FP64 GEMM (BF16 split operands), error vs native FP64
+    Cn = tensordot(dA, dB)
+    def tensordot_oz(a, b):
+        Am = BK.transpose_and_merge(a, *wl.mA)
+        Bm = BK.transpose_and_merge(b, *wl.mB)
+        return BK.unmerge(ops.dot_ozaki(Am, Bm, *wl.mdot), wl.mun)
+    Co = tensordot_oz(dA, dB)
+    oz_err = float((Co - Cn).abs().max() / Cn.abs().max())
+    for _ in range(args.warmup):
+        tensordot_oz(dA, dB)
+    torch.cuda.synchronize()
+    oz_ev = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        tensordot_oz(dA, dB)
+        e1.record()
+        oz_ev.append((e0, e1))
+    torch.cuda.synchronize()
+    t_oz = sum(a.elapsed_time(b) for a, b in oz_ev) / len(oz_ev) * 1e-3
+
     # the workload's truncated block SVD (extra field)
     svd_ms = None
     if not args.no_svd:
@@ -317,6 +339,9 @@ def run_gpu(args, wl):
         "gpu_launches": launches,
         "clocks": clk,
         "extra": {"gemm_ms": t_gemm * 1e3, "svd_with_truncation_ms": svd_ms,
+                  "tensordot_emulated_tflops": wl.flops / t_oz / 1e12, "tensordot_emulated_ms": t_oz * 1e3,
+                  "emulated_max_rel_err_vs_fp64": oz_err,
+                  "emulated": "FP64 GEMM as 36 BF16 slice-pair products (8 digit slices, mma.sync, FP32/FP64 accumulation)",
                   "svd_with_truncation": "merge C, 13-block Jacobi SVD, unmerge U/V, device truncation D_total=64, "
                                          "3 masks"},
     }

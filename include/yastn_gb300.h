@@ -101,25 +101,26 @@ int yb_grouped_gemm(const void* a, const void* b, void* c, int dtype,
                     double alpha, double beta, void* stream);
 
 /* ==== family (b'): FP64 sector GEMMs emulated on BF16 tensor cores (split operands) ====
- * yb_ozaki_split: every "row" of each record is scaled by 2^-e (|entries| < 1, e stored
- * as int32) and peeled into slices_count integer digits d_t (|d_0| <= 128, |d_t| <= 64)
- * with weights 2^{-7(t+1)}, stored exactly as BF16 in planes [slice][row][Kp].
+ * yb_ozaki_split: every row of each record (K contiguous entries) is scaled by 2^-e
+ * (|entries| < 1, e stored as int32) and written as slices_count balanced base-128
+ * digits (|d_0| <= 128, d_t in [-64, 63]) with weights 2^{-7(t+1)}, stored exactly as
+ * BF16 in planes [slice][row][Kp]. The host splits A blocks directly (their rows) and B
+ * blocks after transposing them with yb_block_copy (their columns).
  * recs: n_recs records of 8 int64: [0] source offset [1] rows [2] K [3] row stride
- *   [4] column stride (element (i, l) at src[off + i*rs + l*cs]) [5] destination offset
- *   (BF16 elements) [6] exponent offset [7] Kp = K rounded up to 16 (padding zeroed).
- *   A operands use their rows (rs = K, cs = 1, warp_per_row = 1); B operands use their
- *   columns (rs = 1, cs = n, warp_per_row = 0). max_rows: largest rows over records.
+ *   [4] 1 (column stride) [5] destination offset (BF16 elements, multiple of 16)
+ *   [6] exponent offset [7] Kp = K rounded up to 16 (padding zeroed).
+ *   max_rows: largest rows over records.
  * yb_ozaki_gemm: C = A B for every output record (16 int64): [0] c offset [1] m [2] n
  *   [3] ldc [4] A slices offset [5] A exponents offset [6] B slices offset
  *   [7] B exponents offset [8] K [9] Kp; tiles as for yb_grouped_gemm (64 x 64).
  *   Slice pairs with digit-weight sum below slices_count (6, 7 or 8) are multiplied with
- *   mma.sync BF16 -> FP32 (exact integer sums per 128-wide K-chunk) and combined in FP64.
+ *   mma.sync BF16 -> FP32 (exact integer sums per 400-wide K-chunk) and combined in FP64.
  *   slices_count = 8 represents 57 bits of each operand (FP64-grade products).
  * Replaces dot (backend_torch.py:549-550) for real FP64 operands when the emulated path
  * is selected; the native yb_grouped_gemm stays the default.
  */
 int yb_ozaki_split(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs,
-                   int max_rows, int slices_count, int warp_per_row, void* stream);
+                   int max_rows, int slices_count, void* stream);
 int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps,
                   double* c, const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
                   void* stream);

@@ -238,16 +238,17 @@ def test_mixed_precision_jacobi_schedule_on_plan_layout():
 
 
 def _ozaki_digits(x, s):
-    """NumPy restatement of the split of csrc/yb_ozaki.cu (rows of x)."""
+    """NumPy restatement of the split of csrc/yb_ozaki.cu (rows of x): balanced base-128
+    digits of Q = rint(x 2^{7s-e}) extracted from the low end with integer arithmetic."""
     mx = np.abs(x).max(axis=1)
     e = np.where(mx > 0, np.frexp(mx)[1], 0)
-    v = np.ldexp(x, -e[:, None])
-    digits = []
-    for _ in range(s):
-        y = v * 128.0
-        d = np.rint(y)
-        v = y - d
-        digits.append(d)
+    q = np.rint(np.ldexp(x, 7 * s - e[:, None])).astype(np.int64)
+    digits = [None] * s
+    for t in range(s - 1, 0, -1):
+        r = ((q + 64) & 127) - 64
+        digits[t] = r.astype(np.float64)
+        q = (q - r) >> 7
+    digits[0] = q.astype(np.float64)
     return e, digits
 
 
@@ -288,3 +289,10 @@ def test_ozaki_plan_records():
     assert len({tuple(r[:1]) for r in plan.a_recs}) == len(plan.a_recs)  # each A block split once
     assert all(r[7] % 16 == 0 and r[7] >= r[2] for r in plan.a_recs)
     assert all(int(r[5]) % 16 == 0 for r in plan.a_recs) and all(int(r[5]) % 16 == 0 for r in plan.b_recs)
+    # B blocks are split from their transposes: the copy plan reproduces B^T block by block
+    A, B, _, _ = c['args']
+    tasks, items = plan.bT.packed(False)
+    bT = PI.run_copy(tasks, items, B, np.zeros(plan.bT_size))
+    for rec, (slc, Dc, sla, Da, slb, Db) in zip(plan.b_recs, {m[4][0]: m for m in meta}.values()):
+        n, K = int(rec[1]), int(rec[2])
+        np.testing.assert_array_equal(bT[rec[0]:rec[0] + n * K].reshape(n, K), B[slb[0]:slb[1]].reshape(Db).T)

@@ -29,7 +29,7 @@ SIGNATURES = {
     'yb_svd_adjoint_core': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
     'yb_mask_gather': ([_vp, _vp, _i, _vp, _vp, _i, _vp, _i, _vp], _i),
     'yb_fix_signs': ([_vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp], _i),
-    'yb_ozaki_split': ([_vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp], _i),
+    'yb_ozaki_split': ([_vp, _vp, _vp, _vp, _i, _i, _i, _vp], _i),
     'yb_ozaki_gemm': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
     'yb_truncation_mask': ([_vp, _i64, _vp, _vp, _i, _d, _i64, _i, _vp, _vp, _vp], _i),
 }

@@ -351,10 +351,14 @@ class OzakiPlan:
 
 
 def ozaki_dot_plan(meta_dot, s):
-    """C[slc] = A[sla] @ B[slb] with A rows / B columns split into ``s`` BF16 digit slices."""
+    """C[slc] = A[sla] @ B[slb] with A rows / B columns split into ``s`` BF16 digit slices.
+
+    B blocks are first transposed (copy plan ``bT``) into K-contiguous rows, so both
+    operands are split row-wise with coalesced accesses.
+    """
     def build():
-        a_map, b_map, a_recs, b_recs = {}, {}, [], []
-        a_size = b_size = a_ex = b_ex = 0
+        a_map, b_map, a_recs, b_recs, bT_tasks = {}, {}, [], [], []
+        a_size = b_size = a_ex = b_ex = bT_size = 0
         outs, flops = [], 0
         for slc, Dc, sla, Da, slb, Db in meta_dot:
             m, K = Da
@@ -367,7 +371,9 @@ def ozaki_dot_plan(meta_dot, s):
                 a_ex += m
             if slb[0] not in b_map:
                 b_map[slb[0]] = (b_size, b_ex)
-                b_recs.append((slb[0], n, K, 1, n, b_size, b_ex, Kp))
+                bT_tasks.append((slb[0], bT_size, [n, K], [1, n], [K, 1]))
+                b_recs.append((bT_size, n, K, K, 1, b_size, b_ex, Kp))
+                bT_size += n * K
                 b_size += s * n * Kp
                 b_ex += n
             ao, ae = a_map[sla[0]]
@@ -389,7 +395,10 @@ def ozaki_dot_plan(meta_dot, s):
         b_recs = np.array(b_recs, dtype=np.int64).reshape(-1, 8)
         a_rows = int(a_recs[:, 1].max()) if len(a_recs) else 0
         b_rows = int(b_recs[:, 1].max()) if len(b_recs) else 0
-        return OzakiPlan(a_recs, b_recs, outs, tiles, a_size, b_size, a_ex, b_ex, a_rows, b_rows, flops, s)
+        plan = OzakiPlan(a_recs, b_recs, outs, tiles, a_size, b_size, a_ex, b_ex, a_rows, b_rows, flops, s)
+        plan.bT = CopyPlan([t for t in bT_tasks if t[2][0] * t[2][1] > 0], bT_size, bT_size)
+        plan.bT_size = bT_size
+        return plan
     return CACHE.get((meta_dot,), ('ozaki_dot', s), build)
 
 

@@ -2,19 +2,19 @@
 // (Ozaki scheme, error-free splitting with per-row / per-column exponents).
 //
 // Splitting: every row i of A (and every column j of B) is scaled by a power of two
-// 2^-e so that its entries lie in (-1, 1), then peeled into s signed integer digits
-//     v = sum_{t<s} d_t 2^{-7(t+1)},  d_0 in [-128, 128], d_t in [-64, 64] (t > 0),
-// by repeated d = rint(128 v), v = 128 v - d (exact in FP64). Every digit is an integer
-// of at most 8 significant bits and is stored exactly as BF16. A slice pair (t_a, t_b)
+// 2^-e so that its entries lie in (-1, 1), then written as s signed integer digits
+//     v = sum_{t<s} d_t 2^{-7(t+1)},  d_0 in [-128, 128], d_t in [-64, 63] (t > 0),
+// (balanced base-128 digits of rint(v 2^{7s}), integer arithmetic). Every digit is an
+// integer of at most 8 significant bits and is stored exactly as BF16. A slice pair (t_a, t_b)
 // contributes 2^{e_i + f_j - 14 - 7 (t_a + t_b)} (D_A[t_a] D_B[t_b])_ij; pairs with
 // t_a + t_b <= s - 1 are kept (s(s+1)/2 products), the rest are below the FP64 rounding
 // of the result for s = 8 (57 bits of each operand are represented).
 //
 // Exactness of the tensor-core products: a digit product is an integer of magnitude
-// <= 2^14; all pairs of one diagonal t = t_a + t_b share one FP32 accumulator over a
-// K-chunk of 128, so a partial sum is an integer below (t+1) * 128 * 2^13 < 2^24 and is
-// exact in FP32. After each chunk the diagonals are folded into FP64 accumulators
-// (smallest first); the final scale is applied with scalbn.
+// <= 2^14 (<= 2^13 unless both digits are leading ones); all pairs of one diagonal
+// t = t_a + t_b share one FP32 accumulator over a K-chunk of 400, so every partial sum is
+// an integer below 2^24 and is exact in FP32. After each chunk the diagonals are folded
+// into FP64 accumulators (smallest first); the final scale is applied with scalbn.
 //
 // GEMM kernel: 64x64 output tile per CTA, 8 warps each owning a 32x16 sub-tile (2x2
 // mma.sync.m16n8k16 tiles), K-step 16 staged in shared memory with cp.async (double
@@ -28,70 +28,58 @@ namespace {
 constexpr int kTile = 64;
 constexpr int kK = 16;
 constexpr int kRow = 24;  // smem row stride in bf16 elements (16 data + 8 pad = 48 bytes)
-constexpr int kChunkSteps = 8;  // K-chunk = 8 * 16 = 128 for exact FP32 diagonal sums
+// K-chunk of 25 * 16 = 400: on diagonal t the per-k sum of digit products is at most
+// 2 * 2^13 + (t - 1) * 2^12 = (t + 3) 2^12 <= 10 * 2^12 (t <= 7), so a chunk sum stays
+// below 400 * 10 * 2^12 < 2^24 and is exact in FP32.
+constexpr int kChunkSteps = 25;
 constexpr int kThreads = 256;
 
 // ------------------------------------------------------------------ splitting
-// rec: [0] src offset [1] rows [2] K [3] row stride [4] col stride [5] dst offset (bf16)
-//      [6] exponent offset [7] Kp (K rounded up to 16)
+// rec: [0] src offset [1] rows [2] K [3] row stride [4] col stride (must be 1)
+//      [5] dst offset (bf16) [6] exponent offset [7] Kp (K rounded up to 16)
 // dst layout: [slice][row][Kp] bf16, padding zero-filled.
-__device__ __forceinline__ void split_value(double a, int e, int s, __nv_bfloat16* dst, int64_t slice_stride) {
-  double v = scalbn(a, -e);
-  for (int t = 0; t < s; ++t) {
-    const double x = v * 128.0;
-    const double d = rint(x);
-    v = x - d;
-    dst[t * slice_stride] = __double2bfloat16(d);
+//
+// The digits are extracted with integer arithmetic: Q = rint(a 2^{7s-e}) (|Q| < 2^{7s}),
+// then balanced base-128 digits from the low end, d = ((Q + 64) & 127) - 64 in [-64, 63]
+// and Q = (Q - d) >> 7, leave the leading digit d_0 = Q in [-128, 128]. This represents
+// a 2^-e = sum_t d_t 2^{-7(t+1)} up to the rounding of Q (half a unit of the last digit).
+__device__ __forceinline__ void digits_of(double a, int e, int s, int* d) {
+  long long q = llrint(scalbn(a, 7 * s - e));
+  for (int t = s - 1; t >= 1; --t) {
+    const long long r = ((q + 64) & 127) - 64;
+    d[t] = (int)r;
+    q = (q - r) >> 7;
   }
+  d[0] = (int)q;
 }
 
-__global__ void split_rows_warp_kernel(const double* __restrict__ src, __nv_bfloat16* __restrict__ slices,
-                                       int* __restrict__ exps, const int64_t* __restrict__ recs, int s) {
-  // one warp per row, lanes along K (rows with unit column stride)
+__global__ void split_rows_kernel(const double* __restrict__ src, __nv_bfloat16* __restrict__ slices,
+                                  int* __restrict__ exps, const int64_t* __restrict__ recs, int s) {
+  // one warp per row (K contiguous), each lane two consecutive elements per step
   const int64_t* r = recs + (int64_t)blockIdx.y * 8;
-  const int64_t rows = r[1], K = r[2], rs = r[3], cs = r[4], Kp = r[7];
+  const int64_t rows = r[1], K = r[2], rs = r[3], Kp = r[7];
   const int lane = threadIdx.x & 31;
   const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (row >= rows) return;
   const double* a = src + r[0] + row * rs;
   double mx = 0.0;
-  for (int64_t l = lane; l < K; l += 32) mx = fmax(mx, fabs(a[l * cs]));
+  for (int64_t l = lane; l < K; l += 32) mx = fmax(mx, fabs(a[l]));
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   int e = 0;
   if (mx > 0.0) frexp(mx, &e);  // mx = f 2^e, f in [0.5, 1): |a| < 2^e
   if (lane == 0) exps[r[6] + row] = e;
   const int64_t slice_stride = rows * Kp;
-  __nv_bfloat16* d = slices + r[5] + row * Kp;
-  for (int64_t l = lane; l < Kp; l += 32) {
-    if (l < K) {
-      split_value(a[l * cs], e, s, d + l, slice_stride);
-    } else {
-      for (int t = 0; t < s; ++t) d[l + t * slice_stride] = __double2bfloat16(0.0);
-    }
-  }
-}
-
-__global__ void split_rows_thread_kernel(const double* __restrict__ src, __nv_bfloat16* __restrict__ slices,
-                                         int* __restrict__ exps, const int64_t* __restrict__ recs, int s) {
-  // one thread per row, consecutive threads on consecutive rows (rows with unit row stride)
-  const int64_t* r = recs + (int64_t)blockIdx.y * 8;
-  const int64_t rows = r[1], K = r[2], rs = r[3], cs = r[4], Kp = r[7];
-  const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= rows) return;
-  const double* a = src + r[0] + row * rs;
-  double mx = 0.0;
-  for (int64_t l = 0; l < K; ++l) mx = fmax(mx, fabs(a[l * cs]));
-  int e = 0;
-  if (mx > 0.0) frexp(mx, &e);
-  exps[r[6] + row] = e;
-  const int64_t slice_stride = rows * Kp;
-  __nv_bfloat16* d = slices + r[5] + row * Kp;
-  for (int64_t l = 0; l < Kp; ++l) {
-    if (l < K) {
-      split_value(a[l * cs], e, s, d + l, slice_stride);
-    } else {
-      for (int t = 0; t < s; ++t) d[l + t * slice_stride] = __double2bfloat16(0.0);
+  __nv_bfloat16* dst = slices + r[5] + row * Kp;
+  for (int64_t l = 2 * lane; l < Kp; l += 64) {
+    int d0[8], d1[8];
+    if (l < K) digits_of(a[l], e, s, d0); else for (int t = 0; t < 8; ++t) d0[t] = 0;
+    if (l + 1 < K) digits_of(a[l + 1], e, s, d1); else for (int t = 0; t < 8; ++t) d1[t] = 0;
+    for (int t = 0; t < s; ++t) {
+      __nv_bfloat162 v;
+      v.x = __int2bfloat16_rn(d0[t]);
+      v.y = __int2bfloat16_rn(d1[t]);
+      *reinterpret_cast<__nv_bfloat162*>(dst + t * slice_stride + l) = v;
     }
   }
 }
@@ -214,7 +202,7 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm_kernel(const __nv_bflo
             double sum = 0.0;
 #pragma unroll
             for (int d = S - 1; d >= 0; --d) {
-              sum = fma((double)acc[d][i][j][v], scalbn(1.0, -7 * d), sum);
+              sum = fma((double)acc[d][i][j][v], 1.0 / (double)(1ull << (7 * d)), sum);
               acc[d][i][j][v] = 0.f;
             }
             acc64[i][j][v] += sum;
@@ -251,17 +239,12 @@ int launch_gemm(const void* As, const int* Ae, const void* Bs, const int* Be, do
 extern "C" {
 
 int yb_ozaki_split(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs, int max_rows,
-                   int slices_count, int warp_per_row, void* stream) {
+                   int slices_count, void* stream) {
   if (n_recs == 0 || max_rows == 0) return YB_OK;
   if (!src || !slices || !exps || !recs || slices_count < 1 || slices_count > 8) return YB_ERR_INVALID;
-  cudaStream_t s = (cudaStream_t)stream;
-  if (warp_per_row) {
-    dim3 grid((unsigned)((max_rows + 7) / 8), (unsigned)n_recs);
-    yb::split_rows_warp_kernel<<<grid, 256, 0, s>>>(src, (__nv_bfloat16*)slices, exps, recs, slices_count);
-  } else {
-    dim3 grid((unsigned)((max_rows + 127) / 128), (unsigned)n_recs);
-    yb::split_rows_thread_kernel<<<grid, 128, 0, s>>>(src, (__nv_bfloat16*)slices, exps, recs, slices_count);
-  }
+  dim3 grid((unsigned)((max_rows + 7) / 8), (unsigned)n_recs);
+  yb::split_rows_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(src, (__nv_bfloat16*)slices, exps, recs,
+                                                                 slices_count);
   return yb::check_launch();
 }
 

@@ -164,9 +164,10 @@ def dot_ozaki(A, B, meta_dot, Dsize, slices=OZAKI_SLICES):
     b_sl = torch.empty(plan.b_size, dtype=torch.bfloat16, device=dev)
     a_ex = torch.empty(max(plan.a_exps, 1), dtype=torch.int32, device=dev)
     b_ex = torch.empty(max(plan.b_exps, 1), dtype=torch.int32, device=dev)
+    bT = run_copy(plan.bT, B, torch.empty(max(plan.bT_size, 1), dtype=B.dtype, device=dev))
     st = _stream()
-    N.call('yb_ozaki_split', _ptr(A), _ptr(a_sl), _ptr(a_ex), _ptr(dar), len(plan.a_recs), plan.a_rows, slices, 1, st)
-    N.call('yb_ozaki_split', _ptr(B), _ptr(b_sl), _ptr(b_ex), _ptr(dbr), len(plan.b_recs), plan.b_rows, slices, 0, st)
+    N.call('yb_ozaki_split', _ptr(A), _ptr(a_sl), _ptr(a_ex), _ptr(dar), len(plan.a_recs), plan.a_rows, slices, st)
+    N.call('yb_ozaki_split', _ptr(bT), _ptr(b_sl), _ptr(b_ex), _ptr(dbr), len(plan.b_recs), plan.b_rows, slices, st)
     N.call('yb_ozaki_gemm', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
            len(plan.tiles), slices, st)
     return out
