@@ -62,6 +62,23 @@ def _sl(x):
     return slice(x[0], x[1])
 
 
+# Sector GEMMs of ``dot`` for real FP64 operands: 'fp64' runs the native FP64 grouped GEMM;
+# 'emulated' runs the split-operand emulation on BF16 tensor cores (8 digit slices, results
+# within a few FP64 rounding errors of the native product, normwise per row/column scale).
+_GEMM_MODE = ['fp64']
+
+
+def set_gemm_mode(mode):
+    """Select 'fp64' (default) or 'emulated' sector GEMMs for real float64 ``dot``."""
+    if mode not in ('fp64', 'emulated'):
+        raise ValueError("gemm mode must be 'fp64' or 'emulated'")
+    _GEMM_MODE[0] = mode
+
+
+def get_gemm_mode():
+    return _GEMM_MODE[0]
+
+
 # ============================================================================ hot path
 
 class _TransposeAndMerge(torch.autograd.Function):
@@ -123,6 +140,8 @@ class _Dot(torch.autograd.Function):
     def forward(ctx, A, B, meta_dot, Dsize):
         ctx.save_for_backward(A, B)
         ctx.meta_dot = meta_dot
+        if _GEMM_MODE[0] == 'emulated' and A.dtype == torch.float64 and B.dtype == torch.float64:
+            return ops.dot_ozaki(A, B, meta_dot, Dsize)
         return ops.dot(A, B, meta_dot, Dsize)
 
     @staticmethod
