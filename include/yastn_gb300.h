@@ -125,6 +125,35 @@ int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices,
                   double* c, const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
                   void* stream);
 
+/* yb_ozaki_dot_static: yb_ozaki_split (A), yb_block_copy + yb_ozaki_split (B) and
+ * yb_ozaki_gemm in one call, with all scratch (digit planes, exponents, transposed B)
+ * placed in a device array built into the library instead of caller-provided memory.
+ * No counterpart in the reference: it exists for callers that cannot allocate device
+ * memory at call time (a host framework that owns the whole device memory budget and
+ * forbids allocations after start-up, or a caller for which an allocation would
+ * synchronise the device in the middle of its stream work). The caller still provides
+ * A, B, C and the plan records, laid out as for the separate calls: b_recs refer to the
+ * transposed copy of B (offsets from 0), bT_tasks/bT_items are the yb_block_copy plan of
+ * B's blocks into those transposes in 8-byte units (no YB_CP_VEC tasks). Limits and
+ * behaviour:
+ *   - the scratch holds YB_STATIC_SCRATCH_BYTES; the call returns YB_ERR_TOO_LARGE when
+ *     2*(a_slice_elems + b_slice_elems) + 8*bT_elems + 4*(a_exp_count + b_exp_count)
+ *     bytes (each region rounded up to 256 bytes) exceed it;
+ *   - it allocates nothing; the first call on a device resolves the array's device
+ *     address (cudaGetSymbolAddress, with that device current) and caches it, so that
+ *     first call should come before any stream capture;
+ *   - every call shares the array, which keeps the last call's contents; each region is
+ *     rewritten before it is read, and calls that overlap on the GPU race on it;
+ *   - C positions not covered by an output record are left untouched (zero them first). */
+#define YB_STATIC_SCRATCH_BYTES (16u << 20)
+int yb_ozaki_dot_static(const double* A, const double* B, double* C,
+                        const int64_t* a_recs, int n_a, int a_rows,
+                        const int64_t* b_recs, int n_b, int b_rows,
+                        const int64_t* bT_tasks, int n_bT_tasks, const int64_t* bT_items, int n_bT_items,
+                        const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
+                        int64_t a_slice_elems, int64_t b_slice_elems, int64_t a_exp_count,
+                        int64_t b_exp_count, int64_t bT_elems, void* stream);
+
 /* ==== family (c): batched one-sided Jacobi SVD / symmetric eigendecomposition ==========
  * blocks: n_blocks records of YB_SVD_REC int64:
  *   [0] a offset [1] m [2] n [3] U offset [4] S offset [5] Vh offset

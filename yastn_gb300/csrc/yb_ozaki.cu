@@ -20,6 +20,8 @@
 // mma.sync.m16n8k16 tiles), K-step 16 staged in shared memory with cp.async (double
 // buffered, rows padded to 48 bytes so ldmatrix is bank-conflict free).
 #include <cuda_bf16.h>
+#include <atomic>
+#include <mutex>
 #include "yb_common.cuh"
 
 namespace yb {
@@ -262,3 +264,80 @@ int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// yb_ozaki_dot_static: the same emulated dot with its scratch (digit planes, exponents and
+// the transposed B blocks) in a file-scope device array instead of caller memory, for
+// callers that cannot allocate device memory. Every GPU that loads the library holds the
+// array (YB_STATIC_SCRATCH_BYTES) until the process exits. All calls share it and it keeps
+// the last call's contents: every region is fully rewritten before it is read, and calls
+// that overlap on the GPU (different streams, or threads) race on it.
+static __device__ __align__(256) unsigned char g_ozaki_static_scratch[YB_STATIC_SCRATCH_BYTES];
+
+namespace yb {
+namespace {
+constexpr int kMaxDevices = 64;
+std::atomic<unsigned char*> g_static_ptr[kMaxDevices];
+std::mutex g_static_mu;
+
+// Device address of the static scratch for the current device. The first call on a device
+// resolves it with cudaGetSymbolAddress (with that device current) and caches it.
+int static_scratch(unsigned char** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
+  if (dev < 0 || dev >= kMaxDevices) return YB_ERR_INVALID;
+  unsigned char* p = g_static_ptr[dev].load(std::memory_order_acquire);
+  if (p == nullptr) {
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    p = g_static_ptr[dev].load(std::memory_order_acquire);
+    if (p == nullptr) {
+      void* q = nullptr;
+      e = cudaGetSymbolAddress(&q, g_ozaki_static_scratch);
+      if (e != cudaSuccess || q == nullptr) { set_cuda_error((int)e); return YB_ERR_CUDA; }
+      p = static_cast<unsigned char*>(q);
+      g_static_ptr[dev].store(p, std::memory_order_release);
+    }
+  }
+  *out = p;
+  return YB_OK;
+}
+
+inline int64_t align256(int64_t x) { return (x + 255) & ~(int64_t)255; }
+}  // namespace
+}  // namespace yb
+
+extern "C" int yb_ozaki_dot_static(const double* A, const double* B, double* C, const int64_t* a_recs, int n_a,
+                                   int a_rows, const int64_t* b_recs, int n_b, int b_rows, const int64_t* bT_tasks,
+                                   int n_bT_tasks, const int64_t* bT_items, int n_bT_items, const int64_t* outs,
+                                   const int32_t* tiles, int n_tiles, int slices_count, int64_t a_slice_elems,
+                                   int64_t b_slice_elems, int64_t a_exp_count, int64_t b_exp_count, int64_t bT_elems,
+                                   void* stream) {
+  if (n_tiles == 0) return YB_OK;
+  if (!A || !B || !C || !a_recs || !b_recs || !outs || !tiles || n_a < 0 || n_b < 0 || n_tiles < 0)
+    return YB_ERR_INVALID;
+  if (a_slice_elems < 0 || b_slice_elems < 0 || a_exp_count < 0 || b_exp_count < 0 || bT_elems < 0)
+    return YB_ERR_INVALID;
+  const int64_t off_a = 0;
+  const int64_t off_b = yb::align256(off_a + 2 * a_slice_elems);
+  const int64_t off_t = yb::align256(off_b + 2 * b_slice_elems);
+  const int64_t off_ea = yb::align256(off_t + 8 * bT_elems);
+  const int64_t off_eb = yb::align256(off_ea + 4 * a_exp_count);
+  const int64_t total = yb::align256(off_eb + 4 * b_exp_count);
+  if (total > (int64_t)YB_STATIC_SCRATCH_BYTES) return YB_ERR_TOO_LARGE;
+  unsigned char* base = nullptr;
+  int st = yb::static_scratch(&base);
+  if (st != YB_OK) return st;
+  double* bT = reinterpret_cast<double*>(base + off_t);
+  int* ea = reinterpret_cast<int*>(base + off_ea);
+  int* eb = reinterpret_cast<int*>(base + off_eb);
+  if (n_bT_items > 0) {
+    st = yb_block_copy(B, bT, 8, bT_tasks, n_bT_tasks, bT_items, n_bT_items, stream);
+    if (st != YB_OK) return st;
+  }
+  st = yb_ozaki_split(A, base + off_a, ea, a_recs, n_a, a_rows, slices_count, stream);
+  if (st != YB_OK) return st;
+  st = yb_ozaki_split(bT, base + off_b, eb, b_recs, n_b, b_rows, slices_count, stream);
+  if (st != YB_OK) return st;
+  return yb_ozaki_gemm(base + off_a, ea, base + off_b, eb, C, outs, tiles, n_tiles, slices_count, stream);
+}
