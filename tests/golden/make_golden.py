@@ -430,6 +430,67 @@ def scen_tds_adjoint():
     print("tds_adjoint: 1 call")
 
 
+def scen_cfg2():
+    """DMRG two-site effective-Hamiltonian matvec (``Env.Heff2``, yastn/tn/mps/_env.py:512-518)
+    for a spin-1/2 XXZ chain (Jz = Jxy = 1, MPO bond 5), virtual legs D=1024 over U(1)
+    charges -12..12 with dims ~ exp(-t^2/18) (empty sectors dropped), L, R, AA drawn with
+    rand(normal) after random_seed(0), fuse_contracted policy. Records the 10 backend calls
+    of one matvec (their array keys give the dataflow), the MPO blocks, and the lowest
+    Ritz value of the reference's eigs(ncv=30, which='SR', hermitian=True)."""
+    import yastn.tn.mps as mps
+    ops_ = yastn.operators.Spin12(sym='U1', backend='np')
+    N = 4
+    gen = mps.Generator(N=N, operators=ops_)
+    gen.random_seed(seed=0)
+    H = gen.mpo_from_latex(r"\sum_{i,j \in NN} (Jz sz_{i} sz_{j} + 0.5 Jxy (sp_{i} sm_{j} + sm_{i} sp_{j}))",
+                           {"Jz": 1.0, "Jxy": 1.0, "NN": [(i, i + 1) for i in range(N - 1)]})
+    psi = gen.random_mps(D_total=8)
+    env = mps.Env(psi, [H, psi]).setup_(to='first').setup_(to='last')
+    L0, R0 = env.F[(0, 1)], env.F[(3, 2)]
+    cfg = psi.config
+    cfg.backend.random_seed(0)
+    ts0 = tuple(range(-12, 13))
+    Ds0 = leg_dims(ts0, lambda t: np.exp(-t * t / 18), 1024)
+    ts, Ds = zip(*[(t, d) for t, d in zip(ts0, Ds0) if d > 0])
+    lL, lR = L0.get_legs(), R0.get_legs()
+    vl = lambda sg: yastn.Leg(cfg, s=sg, t=ts, D=Ds)
+    L = yastn.rand(cfg, legs=[vl(lL[0].s), lL[1], vl(lL[2].s)], distribution='normal')
+    R = yastn.rand(cfg, legs=[vl(lR[0].s), lR[1], vl(lR[2].s)], distribution='normal')
+    la = psi.pre_2site((1, 2)).get_legs()
+    AA = yastn.rand(cfg, legs=[vl(la[0].s), la[1], la[2], vl(la[3].s)], distribution='normal')
+    W1, W2 = H[1], H[2]
+
+    def heff2(v):
+        tmp = v @ R
+        tmp = yastn.tensordot(W2, tmp, axes=((2, 3), (3, 2)))
+        tmp = yastn.tensordot(W1, tmp, axes=((2, 3), (0, 3)))
+        tmp = yastn.tensordot(L, tmp, axes=((0, 1), (3, 0)))
+        return tmp * H.factor
+
+    rec = Recorder(bnp, big=5000)
+    out = heff2(AA)
+    rec.restore()
+    assert out.struct == AA.struct and out.slices == AA.slices
+    val, _ = yastn.eigs(heff2, AA, k=1, ncv=30, which='SR', hermitian=True)
+    keys = {}
+    for name, t in (('L', L), ('R', R), ('AA', AA), ('W1', W1), ('W2', W2)):
+        d = np.ascontiguousarray(t._data)
+        import hashlib
+        keys[name] = hashlib.sha1(d.tobytes() + str(d.dtype).encode()).hexdigest()
+    # map tensor names to the recorder's array keys (content digests)
+    name_of = {}
+    for dig, ent in rec.seen.items():
+        for name, k in keys.items():
+            if k == dig:
+                name_of[name] = ent['__array__']
+    extra = {'seed': 0, 'L_size': int(L.size), 'R_size': int(R.size), 'AA_size': int(AA.size),
+             'order': ['L', 'R', 'AA'], 'factor': float(H.factor), 'inputs': name_of,
+             'W1': [float(x) for x in W1._data], 'W2': [float(x) for x in W2._data],
+             'out_checksum': checksum(out._data), 'lanczos_ncv': 30, 'lanczos_lowest': float(val[0]),
+             'leg_t': list(ts), 'leg_D': list(Ds)}
+    save('cfg2', rec, extra)
+
+
 def _tup(x):
     if isinstance(x, list):
         return tuple(_tup(y) for y in x)
@@ -482,3 +543,4 @@ if __name__ == '__main__':
     scen_svd_ill()
     scen_tds_adjoint()
     scen_cfg1()
+    scen_cfg2()

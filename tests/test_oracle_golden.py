@@ -163,3 +163,20 @@ def test_oracle_ill_conditioned_svd():
     data, meta, sizes = c['args'][:3]
     U, S, V = oracle.svd(data, meta, sizes)
     assert _rel(S, c['out'][1]) < 1e-12
+
+
+def test_heff2_replay_and_lanczos_match_reference():
+    """The DMRG workload replayed through the oracle reproduces the reference's matvec
+    checksum and its 30-step Lanczos lowest Ritz value."""
+    from yastn_gb300.workloads import Heff2Workload, lanczos, ritz_lowest
+    wl = Heff2Workload()
+    env = wl.env(lambda x: x)
+    mv = lambda v: wl.matvec(v, env, oracle.dot, oracle.transpose_and_merge, lambda x, f: x * f)
+    out = mv(wl.data['AA'])
+    chk = wl.tr['out_checksum']
+    assert abs(float(out.sum()) - chk['sum0']) <= 1e-10 * chk['abs0']
+    assert out[:8].tolist() == pytest.approx(chk['head0'], rel=1e-12, abs=1e-12 * chk['abs0'] / out.size)
+    V, al, be = lanczos(mv, wl.data['AA'], wl.tr['lanczos_ncv'], np.dot, np.linalg.norm)
+    lam, _ = ritz_lowest(al, be)
+    assert abs(lam - wl.tr['lanczos_lowest']) <= 1e-10 * abs(wl.tr['lanczos_lowest'])
+    assert wl.flops == 630254080 or abs(wl.flops - 6.303e8) < 1e6

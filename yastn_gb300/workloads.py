@@ -112,3 +112,96 @@ def meta_mask_diag(struct_t, slices, mask_D, nsym=1):
         new_t.append(tuple(t)); new_sl.append((low, low + d))
         low += d
     return tuple(meta), tuple(new_t), tuple(new_sl), low
+
+
+class Heff2Workload:
+    """DMRG two-site effective-Hamiltonian matvec replayed from YASTN's recorded calls.
+
+    ``Env.Heff2`` (yastn/tn/mps/_env.py:512-518) for a spin-1/2 XXZ chain with virtual
+    legs D=1024 is four tensordots under the fuse_contracted policy; YASTN turns them into
+    10 backend calls (4 ``dot`` and 6 ``transpose_and_merge``) whose metadata and dataflow
+    (array keys) are stored in the ``cfg2`` fixture. ``matvec(v, dot, merge, scale)``
+    replays them with the given backend functions (GPU backend or CPU oracle).
+    """
+
+    def __init__(self, trace=None):
+        self.tr = trace or load_trace('cfg2')
+        rng = np.random.default_rng(self.tr['seed'])
+        sizes = {'L': self.tr['L_size'], 'R': self.tr['R_size'], 'AA': self.tr['AA_size']}
+        data = {}
+        for name in self.tr['order']:  # YASTN draws L, R, AA in this order after random_seed
+            data[name] = rng.normal(size=sizes[name])
+        data['W1'] = np.array(self.tr['W1'])
+        data['W2'] = np.array(self.tr['W2'])
+        self.data = data
+        self.keys = self.tr['inputs']  # tensor name -> array key of the recorded calls
+        self.calls = self.tr['calls']
+        self.factor = self.tr['factor']
+        from . import _plans as P
+        self.flops = sum(P.dot_plan(c['args'][2]).flops for c in self.calls if c['fn'] == 'dot')
+        # dataflow: per call, the array keys of its inputs (None for metadata) and of its output
+        self.steps = []
+        for c in self.calls:
+            keys = [a.key if isinstance(a, ArraySpec) else (_key_of(self.tr, a) if isinstance(a, np.ndarray) else None)
+                    for a in c['args']]
+            o = c['out'][0]
+            self.steps.append((c['fn'], keys, c['args'], o.key if isinstance(o, ArraySpec) else _key_of(self.tr, o)))
+
+    def matvec(self, v, env, dot, merge, scale):
+        """Heff2 applied to ``v``; ``env`` maps the fixed operands' keys to backend arrays."""
+        vals = dict(env)
+        vals[self.keys['AA']] = v
+        out = None
+        for fn, keys, args, okey in self.steps:
+            a = [vals[k] if k is not None else x for k, x in zip(keys, args)]
+            if fn == 'dot':
+                out = dot(a[0], a[1], a[2], a[3])
+            elif fn == 'transpose_and_merge':
+                out = merge(a[0], a[1], a[2], a[3], a[4])
+            else:
+                raise ValueError(fn)
+            vals[okey] = out
+        return scale(out, self.factor)
+
+    def env(self, convert):
+        """The fixed operands (L, R, W1, W2) converted by ``convert`` and keyed as in the calls."""
+        return {self.keys[n]: convert(self.data[n]) for n in ('L', 'R', 'W1', 'W2')}
+
+
+def _key_of(trace, arr):
+    """Key of a small stored array (stored arrays are deduplicated by content)."""
+    for k, v in trace['_arrays'].items():
+        if v.shape == arr.shape and v.dtype == arr.dtype and np.array_equal(v, arr):
+            return k
+    raise KeyError("array not in the trace")
+
+
+def lanczos(matvec, v0, ncv, vdot, norm):
+    """Hermitian Krylov expansion of YASTN's ``eigs`` (yastn/krylov/_krylov.py:177-238 with
+    yastn/tensor/_krylov.py:17-46): three-term Lanczos without restarts or breakdown checks
+    inside the loop. Works on numpy or torch vectors (``vdot``/``norm`` return scalars of
+    the same library, so a torch run stays on the device). Returns (V, alphas, betas)."""
+    V = [v0 / norm(v0)]
+    alphas, betas = [], []
+    for j in range(ncv):
+        w = matvec(V[-1])
+        a = vdot(V[j], w)
+        if j == 0:
+            w = w - a * V[j]
+        else:
+            w = w - betas[-1] * V[j - 1] - a * V[j]
+        b = norm(w)
+        alphas.append(a)
+        betas.append(b)
+        V.append(w / b)
+    return V, alphas, betas
+
+
+def ritz_lowest(alphas, betas):
+    """Lowest eigenvalue/vector of the Lanczos tridiagonal matrix (host, 'SR' ordering)."""
+    import scipy.linalg
+    a = np.array([float(x) for x in alphas])
+    b = np.array([float(x) for x in betas[:-1]])
+    w, v = scipy.linalg.eigh_tridiagonal(a, b)
+    i = int(np.argmin(w))
+    return float(w[i]), v[:, i]
