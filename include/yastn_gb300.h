@@ -87,8 +87,9 @@ int yb_block_copy(const void* src, void* dst, int unit_bytes,
  *   [0] a offset [1] b offset [2] k [3] a row stride [4] a col stride
  *   [5] b row stride [6] b col stride [7] flags (bit0: conj A, bit1: conj B)
  *   A_t[i,l] = a[a_off + i*a_rs + l*a_cs], B_t[l,j] = b[b_off + l*b_rs + j*b_cs].
- * tiles: n_tiles records of 4 int32: (output, tile row, tile col, unused), tile = 64x64,
- *   ordered by the host (largest K first).
+ * tiles: n_tiles records of 4 int32: (output, tile row, tile col, kind), ordered by the
+ *   host (largest work first). kind 0: a 64x64 tile; kind 1: a skinny tile covering all
+ *   m <= 8 rows and columns [256*col, 256*col + 256) (tile row must be 0).
  * dtype: YB_F64 or YB_C128 (alpha, beta are real).
  * Replaces dot (one term per output), transpose_dot_sum after the merge of its operands,
  * and the adjoint products A_b += C_b B^H, B_b += A^H C_b (terms grouped by operand block).

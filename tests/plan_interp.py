@@ -45,13 +45,16 @@ def run_copy(tasks, items, src, dst):
 def run_gemm(plan, a, b, c, alpha=1.0, beta=0.0):
     """Grouped sum-of-products GEMM records applied with numpy."""
     seen = {}
-    for oi, tr, tc, _ in plan.tiles:
-        seen.setdefault(int(oi), set()).add((int(tr), int(tc)))
+    for oi, tr, tc, kind in plan.tiles:
+        seen.setdefault(int(oi), set()).add((int(tr), int(tc), int(kind)))
     for oi, o in enumerate(plan.outs):
         c_off, m, n, ldc, t0, t1 = (int(x) for x in o[:6])
         if m == 0 or n == 0:
             continue
-        want = {(i, j) for i in range((m + 63) // 64) for j in range((n + 63) // 64)}
+        if m <= 8 and n > 64:  # skinny tiles: all rows x 256 columns
+            want = {(0, j, 1) for j in range((n + 255) // 256)}
+        else:
+            want = {(i, j, 0) for i in range((m + 63) // 64) for j in range((n + 63) // 64)}
         assert seen.get(oi, set()) == want, "tiles do not cover the output"
         acc = np.zeros((m, n), dtype=c.dtype)
         for t in range(t0, t1):

@@ -281,18 +281,29 @@ def test_ozaki_split_and_slice_products(s):
 
 
 def test_ozaki_plan_records():
-    tr = load_trace('tensordot_fuse_contracted')
-    c = [c for c in tr['calls'] if c['fn'] == 'dot' and not np.iscomplexobj(c['args'][0])][0]
-    _, _, meta, Dsize = c['args']
+    rng = np.random.default_rng(8)
+    shapes = [(40, 70, 30), (16, 16, 16), (3, 200, 5), (64, 20, 33)]
+    meta, oa, ob, oc = [], 0, 0, 0
+    for m, k, n in shapes:
+        meta.append(((oc, oc + m * n), (m, n), (oa, oa + m * k), (m, k), (ob, ob + k * n), (k, n)))
+        oa += m * k; ob += k * n; oc += m * n
+    meta = tuple(meta)
+    A, B = rng.normal(size=oa), rng.normal(size=ob)
     plan = P.ozaki_dot_plan(meta, 8)
-    assert len(plan.outs) == len(meta)
+    # sectors with a dimension below 16 go to the native kernel, the rest are split
+    assert len(plan.outs) == 3 and len(plan.native.outs) == 1
     assert len({tuple(r[:1]) for r in plan.a_recs}) == len(plan.a_recs)  # each A block split once
     assert all(r[7] % 16 == 0 and r[7] >= r[2] for r in plan.a_recs)
     assert all(int(r[5]) % 16 == 0 for r in plan.a_recs) and all(int(r[5]) % 16 == 0 for r in plan.b_recs)
     # B blocks are split from their transposes: the copy plan reproduces B^T block by block
-    A, B, _, _ = c['args']
     tasks, items = plan.bT.packed(False)
     bT = PI.run_copy(tasks, items, B, np.zeros(plan.bT_size))
-    for rec, (slc, Dc, sla, Da, slb, Db) in zip(plan.b_recs, {m[4][0]: m for m in meta}.values()):
+    big = [mt for mt in meta if min(mt[3][0], mt[3][1], mt[5][1]) >= 16]
+    for rec, (slc, Dc, sla, Da, slb, Db) in zip(plan.b_recs, big):
         n, K = int(rec[1]), int(rec[2])
         np.testing.assert_array_equal(bT[rec[0]:rec[0] + n * K].reshape(n, K), B[slb[0]:slb[1]].reshape(Db).T)
+    # the native part reproduces its sector
+    out = PI.run_gemm(plan.native, A, B, np.zeros(oc))
+    slc, Dc, sla, Da, slb, Db = meta[2]
+    np.testing.assert_allclose(out[slc[0]:slc[1]].reshape(Dc), A[sla[0]:sla[1]].reshape(Da) @ B[slb[0]:slb[1]].reshape(Db),
+                               rtol=1e-13)

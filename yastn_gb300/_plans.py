@@ -267,18 +267,27 @@ class GemmPlan:
         self._dev = {}
 
 
+SKINNY_ROWS, SKINNY_COLS = 8, 256
+
+
 def _tiles_for(outs, terms):
+    """Tiles (output, tile row, tile col, kind): kind 0 = 64x64, kind 1 = skinny (all m <= 8
+    rows x 256 columns), ordered by descending work so long tiles start first."""
     tiles = []
     for oi, o in enumerate(outs):
         m, n = int(o[1]), int(o[2])
         if m == 0 or n == 0:
             continue
         kk = int(sum(terms[t][2] for t in range(o[4], o[5])))
+        if m <= SKINNY_ROWS and n > GEMM_TILE:
+            for tc in range((n + SKINNY_COLS - 1) // SKINNY_COLS):
+                tiles.append((kk * m * 4, oi, 0, tc, 1))
+            continue
         for tr in range((m + GEMM_TILE - 1) // GEMM_TILE):
             for tc in range((n + GEMM_TILE - 1) // GEMM_TILE):
-                tiles.append((kk, oi, tr, tc))
+                tiles.append((kk * GEMM_TILE, oi, tr, tc, 0))
     tiles.sort(key=lambda x: -x[0])
-    arr = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles], dtype=np.int32).reshape(-1, 4)
+    arr = np.array([(oi, tr, tc, kind) for _, oi, tr, tc, kind in tiles], dtype=np.int32).reshape(-1, 4)
     return arr
 
 
@@ -350,6 +359,9 @@ class OzakiPlan:
         self._dev = {}
 
 
+OZAKI_MIN_DIM = 16  # sector GEMMs with m, n or k below this stay on the native FP64 kernel
+
+
 def ozaki_dot_plan(meta_dot, s):
     """C[slc] = A[sla] @ B[slb] with A rows / B columns split into ``s`` BF16 digit slices.
 
@@ -359,10 +371,13 @@ def ozaki_dot_plan(meta_dot, s):
     def build():
         a_map, b_map, a_recs, b_recs, bT_tasks = {}, {}, [], [], []
         a_size = b_size = a_ex = b_ex = bT_size = 0
-        outs, flops = [], 0
+        outs, flops, small = [], 0, []
         for slc, Dc, sla, Da, slb, Db in meta_dot:
             m, K = Da
             n = Db[1]
+            if min(m, n, K) < OZAKI_MIN_DIM:  # too small to profit: native FP64 sector GEMM
+                small.append((slc[0], m, n, n, [(sla[0], slb[0], K, K, 1, n, 1, 0)]))
+                continue
             Kp = (K + 15) // 16 * 16
             if sla[0] not in a_map:
                 a_map[sla[0]] = (a_size, a_ex)
@@ -398,6 +413,7 @@ def ozaki_dot_plan(meta_dot, s):
         plan = OzakiPlan(a_recs, b_recs, outs, tiles, a_size, b_size, a_ex, b_ex, a_rows, b_rows, flops, s)
         plan.bT = CopyPlan([t for t in bT_tasks if t[2][0] * t[2][1] > 0], bT_size, bT_size)
         plan.bT_size = bT_size
+        plan.native = _pack_gemm(small)
         return plan
     return CACHE.get((meta_dot,), ('ozaki_dot', s), build)
 

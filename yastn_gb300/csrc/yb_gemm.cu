@@ -3,7 +3,9 @@
 //   C_o = alpha * sum_{t in terms(o)} op(A_t) op(B_t) + beta * C_o
 //
 // One launch covers every 64x64 output tile of every sector; the host orders tiles
-// largest-K first so that the long tiles start early. On GB300 FP64 arithmetic runs at
+// largest-K first so that the long tiles start early. Outputs with at most 8 rows (the
+// contractions with a small MPO block, for instance) use "skinny" tiles instead: 8 rows x
+// 256 columns, one column per thread, op(A) staged in shared memory. On GB300 FP64 arithmetic runs at
 // about 1.2 TFLOP/s on the DFMA pipe (the DMMA m8n8k4 tensor path measured slower),
 // so a register-tiled DFMA kernel with shared-memory staging is FP64-bound: each thread
 // owns a 4x4 sub-tile and issues 16 independent FMAs per staged k.
@@ -16,6 +18,8 @@ constexpr int kTile = YB_GEMM_TILE;  // 64
 constexpr int kK = 16;
 constexpr int kThreads = 256;
 constexpr int kPad = 2;
+constexpr int kSkinnyRows = 8;   // rows of a skinny tile (outputs with m <= 8)
+constexpr int kSkinnyK = 64;     // K-chunk of op(A) staged for a skinny tile (64 x 8 <= 16 x 66)
 
 struct Real {
   using T = double;
@@ -56,6 +60,53 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_kernel(const typename F
   const int64_t* orec = outs + (int64_t)tl.x * YB_GEMM_OUT_REC;
   const int64_t c_off = orec[0], m = orec[1], n = orec[2], ldc = orec[3];
   const int64_t t0 = orec[4], t1 = orec[5];
+  if (tl.w == 1) {
+    // skinny tile: all m <= 8 rows x 256 columns, one column per thread (coalesced B and C)
+    T* Ak = &As[0][0];  // [64][8] chunk of op(A), broadcast from shared memory
+    const int64_t j = (int64_t)tl.z * kThreads + threadIdx.x;
+    T acc8[kSkinnyRows];
+#pragma unroll
+    for (int i = 0; i < kSkinnyRows; ++i) acc8[i] = F::zero();
+    for (int64_t t = t0; t < t1; ++t) {
+      const int64_t* trec = terms + t * YB_GEMM_TERM_REC;
+      const int64_t a_off = trec[0], b_off = trec[1], K = trec[2];
+      const int64_t a_rs = trec[3], a_cs = trec[4], b_rs = trec[5], b_cs = trec[6];
+      const int flags = (int)trec[7];
+      for (int64_t k0 = 0; k0 < K; k0 += kSkinnyK) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < kSkinnyK * kSkinnyRows; e += kThreads) {
+          const int i = e % kSkinnyRows, l = e / kSkinnyRows;
+          T v = F::zero();
+          if (i < m && k0 + l < K) {
+            v = A[a_off + i * a_rs + (k0 + l) * a_cs];
+            if (flags & 1) v = F::conj(v);
+          }
+          Ak[l * kSkinnyRows + i] = v;
+        }
+        __syncthreads();
+        if (j < n) {
+          const int64_t kn = min((int64_t)kSkinnyK, K - k0);
+          for (int64_t l = 0; l < kn; ++l) {
+            T b = B[b_off + (k0 + l) * b_rs + j * b_cs];
+            if (flags & 2) b = F::conj(b);
+#pragma unroll
+            for (int i = 0; i < kSkinnyRows; ++i) F::fma(acc8[i], Ak[l * kSkinnyRows + i], b);
+          }
+        }
+      }
+    }
+    if (j < n) {
+#pragma unroll
+      for (int i = 0; i < kSkinnyRows; ++i) {
+        if (i >= m) break;
+        T* p = C + c_off + i * ldc + j;
+        T v = F::scale(acc8[i], alpha);
+        if (beta != 0.0) v = F::add(v, F::scale(*p, beta));
+        *p = v;
+      }
+    }
+    return;
+  }
   const int64_t row0 = (int64_t)tl.y * kTile, col0 = (int64_t)tl.z * kTile;
 
   const int tx = threadIdx.x & 15;  // column group
