@@ -161,6 +161,7 @@ int yb_ozaki_dot_static(const double* A, const double* B, double* C,
  *   [6] X offset (FP64 workspace) [7] W offset (FP64 workspace) [8] first pair item
  *   [9] k=min(m,n) [10] L=max(m,n) [11] N = k rounded up to even [12] 1 if m > n
  *   [13] X offset (FP32 workspace) [14] W offset (FP32 workspace)
+ *   [15] number of super-vectors for yb_svd_block_sweeps (ceil(k / rows_per_super), even)
  * X holds the k vectors (rows of A, or of A^T when m > n) of length L, W the k x k
  * accumulated rotations (X = W X_0 throughout).
  * pair_items: int32 pairs (block, pair index 0..N/2-1) over all blocks.
@@ -168,8 +169,9 @@ int yb_ozaki_dot_static(const double* A, const double* B, double* C,
  *   bits, converged flag, sweeps run in the current phase, largest |cos| of the last
  *   completed sweep), then the control
  *   words of the grid barrier (count, generation, error flag, all-converged flag).
- * Sequence (mixed precision): yb_svd_init (X32 = A or A^T, W32 = I); yb_svd_sweeps with
- * precision 32; yb_svd_widen (W = double(W32)); the host orthonormalises W (Newton-Schulz
+ * Sequence (mixed precision): yb_svd_init (X32 = scale_b (A or A^T), W32 = I, with
+ * scale[b] a power of two that brings the block below 1 in magnitude; scale: double
+ * [n_blocks] scratch); yb_svd_sweeps with precision 32 (or yb_svd_block_sweeps); yb_svd_widen (W = double(W32)); the host orthonormalises W (Newton-Schulz
  * with the grouped GEMM) and forms X = W X_0 (for eigh: yb_svd_shift_prefill, then
  * X += W A); yb_svd_sweeps with precision 64; yb_svd_finalize. yb_svd_sweeps runs every
  * sweep of a phase in one cooperative launch (rounds separated by a grid barrier with a
@@ -186,10 +188,19 @@ int yb_ozaki_dot_static(const double* A, const double* B, double* C,
  */
 #define YB_SVD_REC 16
 int yb_svd_init(const void* a, void* work32, const int64_t* blocks, int n_blocks, int dtype,
-                int64_t* state, double* shift, void* stream);
+                int64_t* state, double* shift, double* scale, void* stream);
 int yb_svd_sweeps(void* work, const int64_t* blocks, int n_blocks, const int32_t* pair_items,
                   int n_pair_items, int max_rounds, int precision, int max_sweeps, double tol_stop,
                   int64_t* state, void* stream);
+/* yb_svd_block_sweeps: the FP32 phase with rows grouped into super-vectors of
+ * rows_per_super (16, 8 or 4) rows: one CTA per pair of super-vectors holds their rows in
+ * shared memory (2 * rows_per_super * lmax floats, lmax >= every L), runs up to
+ * inner_sweeps Jacobi sweeps among them and applies the accumulated rotation to the W rows.
+ * super_items: int32 pairs (block, super pair index 0..[15]/2-1); max_rounds = max([15]) - 1.
+ * Returns YB_ERR_TOO_LARGE if the rows do not fit in shared memory. */
+int yb_svd_block_sweeps(void* work32, const int64_t* blocks, int n_blocks, const int32_t* super_items,
+                        int n_items, int max_rounds, int rows_per_super, int max_sweeps, int inner_sweeps,
+                        double tol_stop, int lmax, int64_t* state, void* stream);
 int yb_svd_widen(const void* work32, void* work64, const int64_t* blocks, int n_blocks,
                  int64_t* state, void* stream);
 int yb_svd_shift_prefill(void* work64, const int64_t* blocks, int n_blocks, const double* shift,

@@ -116,6 +116,77 @@ def jacobi_sweeps(X, W, blocks, dtype, tol_stop, max_sweeps):
     return _sweeps(X, W, blocks, dtype, tol_stop, max_sweeps, eps)
 
 
+def block_jacobi_sweeps(X, W, blocks, br, inner_sweeps, tol_stop, max_sweeps):
+    """The blocked FP32 Jacobi of csrc/yb_svd.cu (svd_block_sweeps_kernel), restated
+    sequentially: super-vectors of ``br`` rows paired by the circle method, up to
+    ``inner_sweeps`` sweeps among the 2*br rows of a pair with the rotations accumulated in
+    Q, then W rows <- Q W rows. Returns (sweeps, converged)."""
+    eps = 2.0 ** -24
+    r2 = 2 * br
+    nb = len(blocks); conv = [False] * nb; nsw = [0] * nb
+    max_rounds = max(int(r[15]) - 1 for r in blocks)
+    for sw in range(max_sweeps):
+        maxcos = [0.0] * nb
+        for rd in range(max_rounds):
+            for b, r in enumerate(blocks):
+                k, L, NS = int(r[9]), int(r[10]), int(r[15])
+                if conv[b] or rd >= NS - 1:
+                    continue
+                xo, wo = int(r[13]), int(r[14])
+                Xb = X[xo:xo + k * L].reshape(k, L)
+                Wb = W[wo:wo + k * k].reshape(k, k)
+                for pi in range(NS // 2):
+                    P_, Q_ = (NS - 1, rd) if pi == 0 else ((rd + pi) % (NS - 1), (rd - pi + NS - 1) % (NS - 1))
+                    grow = [sv * br + i for sv in (P_, Q_) for i in range(br)]
+                    grow = [g if g < k else -1 for g in grow]
+                    Xs = np.zeros((r2, L), np.float32)
+                    for i, g in enumerate(grow):
+                        if g >= 0:
+                            Xs[i] = Xb[g]
+                    Qs = np.eye(r2, dtype=np.float32)
+                    any_rot = False
+                    for _ in range(inner_sweeps):
+                        rot = False
+                        for ir in range(r2 - 1):
+                            for w in range(br):
+                                p, q = (r2 - 1, ir) if w == 0 else ((ir + w) % (r2 - 1), (ir - w + r2 - 1) % (r2 - 1))
+                                p, q = min(p, q), max(p, q)
+                                if grow[p] < 0 or grow[q] < 0:
+                                    continue
+                                xp, xq = Xs[p].astype(np.float64), Xs[q].astype(np.float64)
+                                al, be, ga = float(xp @ xp), float(xq @ xq), float(xp @ xq)
+                                if not (al > 0 and be > 0):
+                                    continue
+                                c_ = abs(ga) / np.sqrt(al) / np.sqrt(be)
+                                maxcos[b] = max(maxcos[b], c_)
+                                if not c_ > np.sqrt(L) * eps:
+                                    continue
+                                zeta = (be - al) / (2 * ga)
+                                t = np.copysign(1.0, zeta) / (abs(zeta) + np.hypot(1.0, zeta))
+                                cd = 1 / np.sqrt(1 + t * t)
+                                c, s_ = np.float32(cd), np.float32(cd * t)
+                                for M in (Xs, Qs):
+                                    u, v = M[p].copy(), M[q].copy()
+                                    M[p] = c * u - s_ * v
+                                    M[q] = s_ * u + c * v
+                                rot = any_rot = True
+                        if not rot:
+                            break
+                    if any_rot:
+                        rows = [g for g in grow if g >= 0]
+                        idx = [i for i, g in enumerate(grow) if g >= 0]
+                        Xb[rows] = Xs[idx]
+                        Wb[rows] = (Qs[np.ix_(idx, idx)].astype(np.float64) @ Wb[rows].astype(np.float64)).astype(W.dtype)
+        for b in range(nb):
+            if not conv[b]:
+                nsw[b] += 1
+                if maxcos[b] <= tol_stop:
+                    conv[b] = True
+        if all(conv):
+            break
+    return nsw, conv
+
+
 def _sweeps(X, W, blocks, dtype, tol_stop, max_sweeps, eps):
     nb = len(blocks); conv = [False]*nb; nsw = [0]*nb
     max_rounds = max(int(r[11]) - 1 for r in blocks)

@@ -110,6 +110,34 @@ def test_svd_rank_deficient_and_zero_blocks(cuda_device):
     check_svd(data, meta, U, S, V, Sr)
 
 
+@pytest.mark.parametrize('blocked,rows', [(False, None), (True, 4), (True, 8), (True, 16)])
+def test_svd_fp32_phase_variants(blocked, rows, cuda_device):
+    """Both FP32 phases (one pair per warp; super-vectors of 4/8/16 rows in shared memory)
+    give LAPACK's singular values and an orthonormal factorisation."""
+    rng = np.random.default_rng(11)
+    shapes = [(200, 150), (64, 300), (37, 37), (5, 3), (1, 9), (90, 90)]
+    meta, off, oU, oS, oV = [], 0, 0, 0, 0
+    for m, n in shapes:
+        k = min(m, n)
+        meta.append(((off, off + m * n), (m, n), (oU, oU + m * k), (m, k), (oS, oS + k), (oV, oV + k * n), (k, n)))
+        off += m * n; oU += m * k; oS += k; oV += k * n
+    meta = tuple(meta)
+    data = rng.normal(size=off)
+    # a graded block: singular values over 12 decades
+    a = meta[5][0][0]
+    q1, _ = np.linalg.qr(rng.normal(size=(90, 90)))
+    q2, _ = np.linalg.qr(rng.normal(size=(90, 90)))
+    data[a:a + 8100] = ((q1 * np.logspace(0, -12, 90)) @ q2).ravel()
+    saved = ops.BLOCKED_FP32[0], ops.ROWS_PER_SUPER[0]
+    ops.BLOCKED_FP32[0], ops.ROWS_PER_SUPER[0] = blocked, rows
+    try:
+        U, S, V = (host(x) for x in ops.svd(dev(data), meta, (oU, oS, oV)))
+    finally:
+        ops.BLOCKED_FP32[0], ops.ROWS_PER_SUPER[0] = saved
+    _, Sr, _ = oracle.svd(data, meta, (oU, oS, oV))
+    check_svd(data, meta, U, S, V, Sr)
+
+
 def test_svd_empty(cuda_device):
     U, S, V = ops.svd(torch.zeros(0, dtype=torch.float64, device='cuda'), (), (0, 0, 0))
     assert U.numel() == S.numel() == V.numel() == 0

@@ -188,9 +188,11 @@ def test_mask_plan_diagonal_records():
     assert total == 3 and recs[:, 2].tolist() == [1, 1] and recs[:, 5].tolist() == [1, 1]
 
 
-def test_mixed_precision_jacobi_schedule_on_plan_layout():
-    """FP32 sweeps -> widen -> Newton-Schulz (grouped GEMM plans) -> X = W X_0 (plan) ->
-    FP64 sweeps, on the plan's workspace offsets, reproduces LAPACK's singular values."""
+@pytest.mark.parametrize('rows_per_super', [0, 4])
+def test_mixed_precision_jacobi_schedule_on_plan_layout(rows_per_super):
+    """FP32 sweeps (one pair per warp, or blocked on super-vectors) -> widen -> Newton-Schulz
+    (grouped GEMM plans) -> X = W X_0 (plan) -> FP64 sweeps, on the plan's workspace offsets,
+    reproduces LAPACK's singular values."""
     rng = np.random.default_rng(0)
     shapes = [(30, 30), (40, 17), (13, 35), (1, 5), (6, 6)]
     meta, off, oU, oS, oV = [], 0, 0, 0, 0
@@ -201,7 +203,7 @@ def test_mixed_precision_jacobi_schedule_on_plan_layout():
     meta = tuple(meta)
     data = rng.normal(size=off)
     data[meta[4][0][0]:meta[4][0][1]] = 0  # an all-zero block
-    plan = P.svd_plan(meta)
+    plan = P.svd_plan(meta, rows_per_super if rows_per_super else None)
     w32 = np.zeros(plan.n32, np.float32)
     w64 = np.zeros(plan.n64)
     for r in plan.blocks:
@@ -210,7 +212,13 @@ def test_mixed_precision_jacobi_schedule_on_plan_layout():
         X0 = A.T if m > n else A
         w32[int(r[13]):int(r[13]) + k * L] = X0.ravel().astype(np.float32)
         w32[int(r[14]):int(r[14]) + k * k] = np.eye(k, dtype=np.float32).ravel()
-    nsw, conv = PI.jacobi_sweeps(w32, w32, plan.blocks, np.float32, 1e-4, 40)
+    if rows_per_super:
+        assert plan.rows_per_super == rows_per_super
+        assert plan.blocks[:, 15].tolist() == [8, 6, 4, 2, 2]  # ceil(k / 4) rounded up to even
+        assert plan.super_rounds == 7 and len(plan.super_items) == 11
+        nsw, conv = PI.block_jacobi_sweeps(w32, w32, plan.blocks, rows_per_super, 3, 1e-4, 40)
+    else:
+        nsw, conv = PI.jacobi_sweeps(w32, w32, plan.blocks, np.float32, 1e-4, 40)
     assert all(conv)
     for r in plan.blocks:
         k = int(r[9])

@@ -424,9 +424,14 @@ class SvdPlan:
     """Mixed-precision Jacobi plan: block records, pair items, workspace layout and the
     grouped-GEMM plans of the Newton-Schulz orthonormalisation and of X = W X_0."""
 
-    def __init__(self, blocks, pair_items, max_rounds, max_k, nominal_flops, n64, n32, w_range, gram, ns, xform):
+    def __init__(self, blocks, pair_items, max_rounds, max_k, nominal_flops, n64, n32, w_range, gram, ns, xform,
+                 rows_per_super=0, super_items=None, super_rounds=0, lmax=0):
         self.blocks = blocks
         self.pair_items = pair_items
+        self.rows_per_super = rows_per_super  # 0: the FP32 phase uses the one-pair-per-warp kernel
+        self.super_items = super_items        # (block, super pair) items of the blocked FP32 phase
+        self.super_rounds = super_rounds
+        self.lmax = lmax
         self.max_rounds = max_rounds
         self.max_k = max_k
         self.nominal_flops = nominal_flops
@@ -437,8 +442,22 @@ class SvdPlan:
         self._dev = {}
 
 
-def svd_plan(meta):
-    """Jacobi plan for svd records (sl, D, slU, DU, slS, slV, DV) of yastn/tensor/linalg.py:323-380."""
+SVD_SMEM_BYTES = 220 * 1024  # shared memory a blocked-Jacobi CTA may take (GB300: 227 KB per CTA)
+
+
+def svd_rows_per_super(lmax, choices=(16, 8, 4)):
+    """Rows per super-vector of the blocked FP32 Jacobi: the largest choice whose CTA
+    (2 * rows * lmax + 4 * rows^2 floats of shared memory) fits; 0 if none does."""
+    for br in choices:
+        if (2 * br * lmax + 4 * br * br) * 4 <= SVD_SMEM_BYTES:
+            return br
+    return 0
+
+
+def svd_plan(meta, rows_per_super=None):
+    """Jacobi plan for svd records (sl, D, slU, DU, slS, slV, DV) of yastn/tensor/linalg.py:323-380.
+    ``rows_per_super`` fixes the super-vector height of the blocked FP32 phase (default: the
+    largest of 16, 8, 4 whose rows fit in shared memory)."""
     def build():
         sel = []
         for sl, D, slU, DU, slS, slV, DV in meta:
@@ -475,11 +494,22 @@ def svd_plan(meta):
             max_rounds = max(max_rounds, N - 1)
             max_k = max(max_k, k)
             fl += 14 * L * k * k + 8 * k ** 3  # nominal Golub-Reinsch count
+        lmax = max((L for *_, k, L in sel), default=0)
+        br = svd_rows_per_super(lmax) if rows_per_super is None else rows_per_super
+        supers, super_rounds = [], 0
+        for bi, (*_, k, L) in enumerate(sel):
+            if br:
+                ns_ = -(-k // br)
+                ns_ += ns_ % 2
+                recs[bi][15] = ns_
+                supers.extend((bi, p) for p in range(ns_ // 2))
+                super_rounds = max(super_rounds, ns_ - 1)
         blocks = np.stack(recs) if recs else np.zeros((0, SVD_REC), dtype=np.int64)
         items = np.array(pairs, dtype=np.int32).reshape(-1, 2)
         return SvdPlan(blocks, items, max_rounds, max_k, fl, xs + 3 * ws, xs + ws, (w0, t0, n0, ws),
-                       _pack_gemm(gram), _pack_gemm(ns), _pack_gemm(xf))
-    return CACHE.get((meta,), ('svd',), build)
+                       _pack_gemm(gram), _pack_gemm(ns), _pack_gemm(xf),
+                       br, np.array(supers, dtype=np.int32).reshape(-1, 2), super_rounds, lmax)
+    return CACHE.get((meta,), ('svd', rows_per_super), build)
 
 
 class SvdAdjointPlan:

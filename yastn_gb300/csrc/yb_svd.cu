@@ -31,7 +31,7 @@ constexpr int kThreads = kWarps * 32;
 constexpr long long kSpinLimit = 1ll << 22;
 
 // record fields
-enum { R_A = 0, R_M, R_N, R_U, R_S, R_V, R_X, R_W, R_P, R_K, R_L, R_NP, R_T, R_X32, R_W32 };
+enum { R_A = 0, R_M, R_N, R_U, R_S, R_V, R_X, R_W, R_P, R_K, R_L, R_NP, R_T, R_X32, R_W32, R_NSUP };
 // per-block state (int64): [0] max |cos| of the sweep in progress (double bits),
 // [1] converged flag, [2] sweeps run in the current phase, [3] largest |cos| of the last sweep
 enum { ST_MAXCOS = 0, ST_CONV = 1, ST_SWEEPS = 2, ST_LASTCOS = 3, ST_REC = 4 };
@@ -56,9 +56,67 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Per-block Frobenius norm -> shift[b] (makes a symmetric block positive definite).
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Jacobi rotation of a row pair from its warp-local partial sums al_ = |x_p|^2, be_ =
+// |x_q|^2, ga_ = x_p.x_q (Rutishauser's formulas): returns true (every lane) if the pair is
+// rotated, with (c, s). |cos| of the pair goes to the block's running maximum. GB300 runs
+// FP64 at 1/64 of the FP32 rate, so the FP32 phase keeps the whole computation in FP32,
+// and the FP64 phase does the scalar part on lane 0 only and broadcasts the result.
+template <typename T>
+struct Rotation;
+
+template <>
+struct Rotation<float> {
+  __device__ static bool get(float al_, float be_, float ga_, int64_t L, int lane, int64_t* st, float& c, float& s) {
+    const float al = warp_sum(al_), be = warp_sum(be_), ga = warp_sum(ga_);
+    if (!(al > 0.f && be > 0.f)) return false;
+    const float cosv = fabsf(ga) / (sqrtf(al) * sqrtf(be));
+    if (lane == 0) atomicMax((unsigned long long*)(st + 0), (unsigned long long)__double_as_longlong((double)cosv));
+    if (!(cosv > sqrtf((float)L) * 5.9604645e-08f)) return false;
+    const float zeta = (be - al) / (2.f * ga);
+    const float t = copysignf(1.f, zeta) / (fabsf(zeta) + hypotf(1.f, zeta));
+    c = 1.f / sqrtf(fmaf(t, t, 1.f));
+    s = c * t;
+    return true;
+  }
+};
+
+template <>
+struct Rotation<double> {
+  __device__ static bool get(double al_, double be_, double ga_, int64_t L, int lane, int64_t* st, double& c,
+                             double& s) {
+    const double al = warp_sum(al_), be = warp_sum(be_), ga = warp_sum(ga_);
+    int rot = 0;
+    if (lane == 0 && al > 0.0 && be > 0.0) {
+      const double cosv = fabs(ga) / (sqrt(al) * sqrt(be));
+      atomicMax((unsigned long long*)(st + 0), (unsigned long long)__double_as_longlong(cosv));
+      if (cosv > sqrt((double)L) * 1.1102230246251565e-16) {
+        const double zeta = (be - al) / (2.0 * ga);
+        const double t = copysign(1.0, zeta) / (fabs(zeta) + hypot(1.0, zeta));
+        c = 1.0 / sqrt(fma(t, t, 1.0));
+        s = c * t;
+        rot = 1;
+      }
+    }
+    rot = __shfl_sync(0xffffffffu, rot, 0);
+    if (!rot) return false;
+    c = __shfl_sync(0xffffffffu, c, 0);
+    s = __shfl_sync(0xffffffffu, s, 0);
+    return true;
+  }
+};
+
+// Per-block Frobenius norm -> shift[b] (eigh: makes a symmetric block positive definite)
+// and scale[b], a power of two that brings the FP32 copy of the block (shift included)
+// below 1 in magnitude, so that FP32 squares and dot products neither overflow nor lose
+// the block to underflow. The rotations, and so W, do not depend on the scale.
 __global__ void block_fro_kernel(const double* __restrict__ A, const int64_t* __restrict__ blocks,
-                                 double* __restrict__ shift) {
+                                 double* __restrict__ shift, double* __restrict__ scale) {
   __shared__ double red[32];
   const int64_t* r = blocks + (int64_t)blockIdx.x * YB_SVD_REC;
   const int64_t cnt = r[R_M] * r[R_N];
@@ -72,14 +130,23 @@ __global__ void block_fro_kernel(const double* __restrict__ A, const int64_t* __
     double tot = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
     // ||A||_2 <= ||A||_F: A + shift I is positive definite; +1 keeps an all-zero block regular
-    shift[blockIdx.x] = sqrt(tot) + 1.0;
+    const double fro = sqrt(tot);
+    double bound = fro;
+    if (shift != nullptr) {
+      shift[blockIdx.x] = fro + 1.0;
+      bound = 2.0 * fro + 1.0;
+    }
+    int e = 0;
+    if (bound > 0.0 && bound <= 1.0e300) frexp(bound, &e);
+    scale[blockIdx.x] = ldexp(1.0, -e);
   }
 }
 
 // X32 = float(A or A^T) (+ shift on the diagonal), W32 = I; resets the per-block state.
 __global__ void svd_init_kernel(const double* __restrict__ A, float* __restrict__ work32,
                                 const int64_t* __restrict__ blocks, int64_t* __restrict__ state,
-                                const double* __restrict__ shift) {
+                                const double* __restrict__ shift, const double* __restrict__ scale) {
+  const double sc = scale[blockIdx.y];
   const int64_t* r = blocks + (int64_t)blockIdx.y * YB_SVD_REC;
   const int64_t m = r[R_M], n = r[R_N], k = r[R_K], L = r[R_L];
   const bool tall = m > n;
@@ -93,7 +160,7 @@ __global__ void svd_init_kernel(const double* __restrict__ A, float* __restrict_
       const int64_t i = e / L, l = e - i * L;
       double v = tall ? a[l * n + i] : a[e];
       if (shift != nullptr && i == l) v += shift[blockIdx.y];
-      X[e] = (float)v;
+      X[e] = (float)(v * sc);
     } else {
       const int64_t f = e - xs;
       const int64_t i = f / k, j = f - i * k;
@@ -208,18 +275,8 @@ __device__ __forceinline__ void rotate_pair(T* __restrict__ X, T* __restrict__ W
       ga_ = fma(u[j], v[j], ga_);
     }
   }
-  double al = al_, be = be_, ga = ga_;
-  al = warp_sum(al);
-  be = warp_sum(be);
-  ga = warp_sum(ga);
-  if (!(al > 0.0 && be > 0.0)) return;
-  const double cosv = fabs(ga) / (sqrt(al) * sqrt(be));
-  if (lane == 0) atomicMax((unsigned long long*)(st + ST_MAXCOS), (unsigned long long)__double_as_longlong(cosv));
-  if (!(cosv > sqrt((double)L) * Eps<T>::v)) return;
-  const double zeta = (be - al) / (2.0 * ga);
-  const double t = copysign(1.0, zeta) / (fabs(zeta) + hypot(1.0, zeta));
-  const double cd = 1.0 / sqrt(fma(t, t, 1.0));
-  const T c = (T)cd, s = (T)(cd * t);
+  T c = 0, s = 0;
+  if (!Rotation<T>::get(al_, be_, ga_, L, lane, st + ST_MAXCOS, c, s)) return;
   rotate_rows<T>(xp, xq, L, lane, c, s);
   rotate_rows<T>(W + p * k, W + q * k, k, lane, c, s);
 }
@@ -281,6 +338,176 @@ __global__ void __launch_bounds__(kThreads) svd_sweeps_kernel(T* __restrict__ wo
     if (!grid_barrier(ctrl, gridDim.x)) return;
     if (((volatile unsigned long long*)ctrl)[C_DONE]) return;
   }
+}
+
+// ---------------------------------------------------------------------------------------
+// Blocked variant for the FP32 phase: rows are grouped into super-vectors of BR rows; the
+// circle method pairs super-vectors (R_NSUP of them, even), and one CTA per pair loads the
+// 2*BR rows into shared memory, runs up to inner_sweeps one-sided Jacobi sweeps among them
+// (circle method over the 2*BR rows, one warp per pair, rotations accumulated in a
+// 2BR x 2BR matrix Q), writes the rows back and applies Q to the matching rows of W
+// (column by column, in place). Outer rounds are separated by the grid barrier.
+template <typename T, int BR>
+__global__ void __launch_bounds__(BR * 32) svd_block_sweeps_kernel(T* __restrict__ work,
+                                                                   const int64_t* __restrict__ blocks, int n_blocks,
+                                                                   const int32_t* __restrict__ super_items,
+                                                                   int n_items, int max_rounds, int max_sweeps,
+                                                                   int inner_sweeps, double tol_stop, int lmax,
+                                                                   int64_t* __restrict__ state) {
+  constexpr int R2 = 2 * BR;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* Xs = reinterpret_cast<T*>(smem_raw);   // [R2][lmax]
+  T* Qs = Xs + (size_t)R2 * lmax;           // [R2][R2]
+  __shared__ int any_rot, any_active;
+  __shared__ int64_t grow[R2];              // global row of each local row (-1: absent)
+  unsigned long long* ctrl = reinterpret_cast<unsigned long long*>(state + (int64_t)n_blocks * ST_REC);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int rx = sizeof(T) == 4 ? R_X32 : R_X;
+  const int rw = sizeof(T) == 4 ? R_W32 : R_W;
+  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    for (int round = 0; round < max_rounds; ++round) {
+      for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+        const int b = super_items[2 * item];
+        const int pi = super_items[2 * item + 1];
+        int64_t* st = state + (int64_t)b * ST_REC;
+        if (((volatile int64_t*)st)[ST_CONV]) continue;
+        const int64_t* r = blocks + (int64_t)b * YB_SVD_REC;
+        const int64_t k = r[R_K], L = r[R_L], NS = r[R_NSUP];
+        if (round >= NS - 1) continue;
+        int64_t P, Q;
+        if (pi == 0) { P = NS - 1; Q = round; }
+        else { P = (round + pi) % (NS - 1); Q = (round - pi + (NS - 1)) % (NS - 1); }
+        T* X = work + r[rx];
+        T* W = work + r[rw];
+        __syncthreads();
+        if (threadIdx.x < R2) {
+          const int sv = threadIdx.x < BR ? (int)P : (int)Q;
+          const int64_t g = (int64_t)sv * BR + (threadIdx.x % BR);
+          grow[threadIdx.x] = (g < k) ? g : -1;
+        }
+        for (int e = threadIdx.x; e < R2 * R2; e += blockDim.x) Qs[e] = (e / R2 == e % R2) ? T(1) : T(0);
+        if (threadIdx.x == 0) any_rot = 0;
+        __syncthreads();
+        for (int64_t e = threadIdx.x; e < (int64_t)R2 * L; e += blockDim.x) {
+          const int i = (int)(e / L);
+          const int64_t l = e - (int64_t)i * L;
+          const int64_t g = grow[i];
+          Xs[(size_t)i * lmax + l] = (g >= 0) ? __ldcg(X + g * L + l) : T(0);
+        }
+        __syncthreads();
+        for (int inner = 0; inner < inner_sweeps; ++inner) {
+          __shared__ int rot_this;
+          if (threadIdx.x == 0) rot_this = 0;
+          __syncthreads();
+          for (int ir = 0; ir < R2 - 1; ++ir) {
+            int p, q;
+            if (warp == 0) { p = R2 - 1; q = ir; }
+            else { p = (ir + warp) % (R2 - 1); q = (ir - warp + (R2 - 1)) % (R2 - 1); }
+            if (p > q) { const int t = p; p = q; q = t; }
+            if (grow[p] >= 0 && grow[q] >= 0) {
+              T* xp = Xs + (size_t)p * lmax;
+              T* xq = Xs + (size_t)q * lmax;
+              T al_ = 0, be_ = 0, ga_ = 0;
+              for (int64_t l = lane; l < L; l += 32) {
+                const T u = xp[l], v = xq[l];
+                al_ = fma(u, u, al_);
+                be_ = fma(v, v, be_);
+                ga_ = fma(u, v, ga_);
+              }
+              T c = 0, s = 0;
+              if (Rotation<T>::get(al_, be_, ga_, L, lane, st + ST_MAXCOS, c, s)) {
+                for (int64_t l = lane; l < L; l += 32) {
+                  const T u = xp[l], v = xq[l];
+                  xp[l] = c * u - s * v;
+                  xq[l] = s * u + c * v;
+                }
+                for (int l = lane; l < R2; l += 32) {
+                  const T u = Qs[p * R2 + l], v = Qs[q * R2 + l];
+                  Qs[p * R2 + l] = c * u - s * v;
+                  Qs[q * R2 + l] = s * u + c * v;
+                }
+                if (lane == 0) { rot_this = 1; any_rot = 1; }
+              }
+            }
+            __syncthreads();
+          }
+          const int rotated = rot_this;
+          __syncthreads();  // every thread has read rot_this before the next sweep resets it
+          if (!rotated) break;
+        }
+        if (any_rot) {
+          for (int64_t e = threadIdx.x; e < (int64_t)R2 * L; e += blockDim.x) {
+            const int i = (int)(e / L);
+            const int64_t l = e - (int64_t)i * L;
+            const int64_t g = grow[i];
+            if (g >= 0) X[g * L + l] = Xs[(size_t)i * lmax + l];
+          }
+          // W rows: W_new = Q W_old for the 2*BR rows, one column per thread at a time
+          for (int64_t c = threadIdx.x; c < k; c += blockDim.x) {
+            T old[R2];
+#pragma unroll
+            for (int j = 0; j < R2; ++j) old[j] = (grow[j] >= 0) ? __ldcg(W + grow[j] * k + c) : T(0);
+#pragma unroll
+            for (int i = 0; i < R2; ++i) {
+              if (grow[i] < 0) continue;
+              T acc = 0;
+#pragma unroll
+              for (int j = 0; j < R2; ++j) acc = fma(Qs[i * R2 + j], old[j], acc);
+              W[grow[i] * k + c] = acc;
+            }
+          }
+        }
+      }
+      if (!grid_barrier(ctrl, gridDim.x)) return;
+    }
+    if (blockIdx.x == 0) {
+      if (threadIdx.x == 0) any_active = 0;
+      __syncthreads();
+      for (int b = threadIdx.x; b < n_blocks; b += blockDim.x) {
+        int64_t* st = state + (int64_t)b * ST_REC;
+        if (st[ST_CONV]) continue;
+        const double mc = __longlong_as_double((long long)st[ST_MAXCOS]);
+        st[ST_SWEEPS] += 1;
+        st[ST_LASTCOS] = st[ST_MAXCOS];
+        st[ST_MAXCOS] = 0;
+        if (mc <= tol_stop) st[ST_CONV] = 1; else any_active = 1;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) ctrl[C_DONE] = any_active ? 0ull : 1ull;
+      __threadfence();
+    }
+    if (!grid_barrier(ctrl, gridDim.x)) return;
+    if (((volatile unsigned long long*)ctrl)[C_DONE]) return;
+  }
+}
+
+template <typename T, int BR>
+int launch_block_sweeps(T* work, const int64_t* blocks, int n_blocks, const int32_t* items, int n_items,
+                        int max_rounds, int max_sweeps, int inner_sweeps, double tol_stop, int lmax, int64_t* state,
+                        cudaStream_t s) {
+  const size_t smem = ((size_t)2 * BR * lmax + (size_t)4 * BR * BR) * sizeof(T);
+  int dev = 0, sms = 0, per_sm = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
+  if (smem > (size_t)optin) return YB_ERR_TOO_LARGE;
+  e = cudaFuncSetAttribute(svd_block_sweeps_kernel<T, BR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, svd_block_sweeps_kernel<T, BR>, BR * 32, smem);
+  if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
+  if (per_sm < 1) return YB_ERR_TOO_LARGE;
+  int grid = sms * per_sm;
+  if (grid > n_items) grid = n_items;
+  if (grid < 1) grid = 1;
+  e = cudaMemsetAsync(state + (int64_t)n_blocks * ST_REC, 0, sizeof(int64_t) * C_REC, s);
+  if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
+  void* args[] = {&work, &blocks, &n_blocks, &items, &n_items, &max_rounds, &max_sweeps, &inner_sweeps, &tol_stop,
+                  &lmax, &state};
+  e = cudaLaunchCooperativeKernel((const void*)svd_block_sweeps_kernel<T, BR>, dim3(grid), dim3(BR * 32), args, smem,
+                                  s);
+  if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
+  return YB_OK;
 }
 
 // One CTA per block: singular values = row norms, sort descending (index tie-break),
@@ -465,14 +692,14 @@ int launch_sweeps(T* work, const int64_t* blocks, int n_blocks, const int32_t* p
 extern "C" {
 
 int yb_svd_init(const void* a, void* work32, const int64_t* blocks, int n_blocks, int dtype, int64_t* state,
-                double* shift, void* stream) {
+                double* shift, double* scale, void* stream) {
   if (n_blocks == 0) return YB_OK;
   if (dtype != YB_F64) return YB_ERR_INVALID;
-  if (!a || !work32 || !blocks || !state) return YB_ERR_INVALID;
+  if (!a || !work32 || !blocks || !state || !scale) return YB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
-  if (shift != nullptr) yb::block_fro_kernel<<<n_blocks, 256, 0, s>>>((const double*)a, blocks, shift);
+  yb::block_fro_kernel<<<n_blocks, 256, 0, s>>>((const double*)a, blocks, shift, scale);
   dim3 grid(64, (unsigned)n_blocks);
-  yb::svd_init_kernel<<<grid, 256, 0, s>>>((const double*)a, (float*)work32, blocks, state, shift);
+  yb::svd_init_kernel<<<grid, 256, 0, s>>>((const double*)a, (float*)work32, blocks, state, shift, scale);
   return yb::check_launch();
 }
 
@@ -488,6 +715,24 @@ int yb_svd_sweeps(void* work, const int64_t* blocks, int n_blocks, const int32_t
     return yb::launch_sweeps<double>((double*)work, blocks, n_blocks, pair_items, n_pair_items, max_rounds,
                                      max_sweeps, tol_stop, state, s);
   return YB_ERR_INVALID;
+}
+
+int yb_svd_block_sweeps(void* work32, const int64_t* blocks, int n_blocks, const int32_t* super_items,
+                        int n_items, int max_rounds, int rows_per_super, int max_sweeps, int inner_sweeps,
+                        double tol_stop, int lmax, int64_t* state, void* stream) {
+  if (n_blocks == 0 || n_items == 0 || max_sweeps <= 0) return YB_OK;
+  if (!work32 || !blocks || !super_items || !state || lmax <= 0 || inner_sweeps <= 0) return YB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  float* w = (float*)work32;
+  switch (rows_per_super) {
+    case 16: return yb::launch_block_sweeps<float, 16>(w, blocks, n_blocks, super_items, n_items, max_rounds,
+                                                      max_sweeps, inner_sweeps, tol_stop, lmax, state, s);
+    case 8: return yb::launch_block_sweeps<float, 8>(w, blocks, n_blocks, super_items, n_items, max_rounds, max_sweeps,
+                                                    inner_sweeps, tol_stop, lmax, state, s);
+    case 4: return yb::launch_block_sweeps<float, 4>(w, blocks, n_blocks, super_items, n_items, max_rounds, max_sweeps,
+                                                    inner_sweeps, tol_stop, lmax, state, s);
+    default: return YB_ERR_INVALID;
+  }
 }
 
 int yb_svd_widen(const void* work32, void* work64, const int64_t* blocks, int n_blocks, int64_t* state,

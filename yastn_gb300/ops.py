@@ -235,6 +235,9 @@ MAX_SWEEPS32 = 40
 TOL_STOP32 = 1.0e-4   # FP32 phase ends after a sweep whose largest rotation |cos| is below this
 TOL_STOP64 = 1.0e-8   # FP64 phase: idem; Jacobi converges quadratically, so the residual |cos|
                       # after such a sweep is ~1e-16 for separated singular values
+INNER_SWEEPS32 = 1    # blocked FP32 phase: Jacobi sweeps among the rows of a super pair per visit
+BLOCKED_FP32 = [True]  # FP32 phase on super-vectors in shared memory (False: one pair per warp)
+ROWS_PER_SUPER = [None]  # super-vector height (None: largest of 16, 8, 4 that fits)
 NS_STEPS = 2          # Newton-Schulz steps: non-orthogonality ~1e-6 -> 1e-12 -> ~eps
 
 
@@ -257,13 +260,20 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
     w64 = torch.empty(plan.n64, dtype=torch.float64, device=dev)
     w32 = torch.empty(plan.n32, dtype=torch.float32, device=dev)
     state = torch.zeros(4 * nb + 4, dtype=torch.int64, device=dev)
-    shift = torch.empty(nb, dtype=torch.float64, device=dev) if mode != 0 else None
+    aux = torch.empty(2 * nb, dtype=torch.float64, device=dev)  # [scale | shift]
+    shift = aux[nb:] if mode != 0 else None
     sp = _vp(shift.data_ptr() if shift is not None else 0)
     st = _stream()
-    N.call('yb_svd_init', _ptr(data), _ptr(w32), _ptr(dblocks), nb, code, _ptr(state), sp, st,
-           launches=1 + int(shift is not None))
-    N.call('yb_svd_sweeps', _ptr(w32), _ptr(dblocks), nb, _ptr(dpairs), len(plan.pair_items), plan.max_rounds, 32,
-           MAX_SWEEPS32, TOL_STOP32, _ptr(state), st)
+    N.call('yb_svd_init', _ptr(data), _ptr(w32), _ptr(dblocks), nb, code, _ptr(state), sp, _ptr(aux[:nb]), st,
+           launches=2)
+    if plan.rows_per_super and BLOCKED_FP32[0]:
+        (dsup,) = _dev(plan, 'svd_super', (plan.super_items,), dev)
+        N.call('yb_svd_block_sweeps', _ptr(w32), _ptr(dblocks), nb, _ptr(dsup), len(plan.super_items),
+               plan.super_rounds, plan.rows_per_super, MAX_SWEEPS32, INNER_SWEEPS32, TOL_STOP32, plan.lmax,
+               _ptr(state), st)
+    else:
+        N.call('yb_svd_sweeps', _ptr(w32), _ptr(dblocks), nb, _ptr(dpairs), len(plan.pair_items), plan.max_rounds,
+               32, MAX_SWEEPS32, TOL_STOP32, _ptr(state), st)
     _svd_state_check(state, nb, 'FP32', False)
     N.call('yb_svd_widen', _ptr(w32), _ptr(w64), _ptr(dblocks), nb, _ptr(state), st)
     w0, t0, n0, ws = plan.w_range
@@ -294,7 +304,7 @@ def svd(data, meta, sizes, max_sweeps=MAX_SWEEPS):
     U = torch.empty(sizes[0], dtype=data.dtype, device=dev)
     S = torch.empty(sizes[1], dtype=torch.float64, device=dev)
     V = torch.empty(sizes[2], dtype=data.dtype, device=dev)
-    plan = P.svd_plan(meta)
+    plan = P.svd_plan(meta, ROWS_PER_SUPER[0])
     if len(plan.blocks) == 0:
         return U, S, V
     _jacobi(data, plan, U, S, V, 0, max_sweeps)
@@ -353,7 +363,7 @@ def eigh(data, meta, sizes, order_by_magnitude=False, max_sweeps=MAX_SWEEPS):
 def fix_svd_signs(U, V, meta):
     """Gauge fix of every block; returns (U', Vh', phases)."""
     U, V = _check(U, 'U'), _check(V, 'V')
-    plan = P.svd_plan(meta)
+    plan = P.svd_plan(meta, ROWS_PER_SUPER[0])
     nb = len(plan.blocks)
     Uo, Vo = torch.empty_like(U), torch.empty_like(V)
     S_size = max((int(r[4] + r[9]) for r in plan.blocks), default=0)
@@ -368,7 +378,7 @@ def fix_svd_signs(U, V, meta):
 
 def fix_svd_signs_backward(gU, gV, phases, meta):
     """Adjoint of the real gauge fix: cotangents multiplied by the same +-1 phases."""
-    plan = P.svd_plan(meta)
+    plan = P.svd_plan(meta, ROWS_PER_SUPER[0])
     nb = len(plan.blocks)
     gU = torch.zeros(0) if gU is None else gU
     gV = torch.zeros(0) if gV is None else gV
