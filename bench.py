@@ -577,9 +577,11 @@ def run_gpu_cfg2(args, wl):
 
 def kernel_roofline(torch, dev, run_once, w, gemm_mode, reps=5):
     """Device time per entry point over ``reps`` eager matvecs (CUDA events on the launching
-    stream); the roofline of the entry point that takes the most time, with its algorithmic
-    work: BF16 tensor FLOP of the split-operand GEMM, FP64 FLOP of the native GEMM, or
-    16 bytes per FP64 element moved by the block copies."""
+    stream; the stream is first held by a spin kernel long enough for the host to enqueue
+    the whole matvec, so the events time back-to-back kernels, not host launch gaps); the
+    roofline of the entry point that takes the most time, with its algorithmic work: BF16
+    tensor FLOP of the split-operand GEMM, FP64 FLOP of the native GEMM, or 16 bytes per
+    FP64 element moved by the block copies."""
     from yastn_gb300 import _native, _plans as P, ops
     orig = _native.call
     ev = {}
@@ -596,6 +598,7 @@ def kernel_roofline(torch, dev, run_once, w, gemm_mode, reps=5):
     _native.call = spy
     try:
         for _ in range(reps):
+            torch.cuda._sleep(50_000_000)
             run_once()
         torch.cuda.synchronize()
     finally:

@@ -89,7 +89,7 @@ int yb_block_copy(const void* src, void* dst, int unit_bytes,
  *   A_t[i,l] = a[a_off + i*a_rs + l*a_cs], B_t[l,j] = b[b_off + l*b_rs + j*b_cs].
  * tiles: n_tiles records of 4 int32: (output, tile row, tile col, kind), ordered by the
  *   host (largest work first). kind 0: a 64x64 tile; kind 1: a skinny tile covering all
- *   m <= 8 rows and columns [256*col, 256*col + 256) (tile row must be 0).
+ *   m <= 8 rows and columns [1024*col, 1024*col + 1024) (tile row must be 0).
  * dtype: YB_F64 or YB_C128 (alpha, beta are real).
  * Replaces dot (one term per output), transpose_dot_sum after the merge of its operands,
  * and the adjoint products A_b += C_b B^H, B_b += A^H C_b (terms grouped by operand block).
@@ -97,6 +97,7 @@ int yb_block_copy(const void* src, void* dst, int unit_bytes,
 #define YB_GEMM_OUT_REC 8
 #define YB_GEMM_TERM_REC 8
 #define YB_GEMM_TILE 64
+#define YB_GEMM_SKINNY_COLS 1024
 int yb_grouped_gemm(const void* a, const void* b, void* c, int dtype,
                     const int64_t* outs, const int64_t* terms, const int32_t* tiles, int n_tiles,
                     double alpha, double beta, void* stream);

@@ -51,8 +51,8 @@ def run_gemm(plan, a, b, c, alpha=1.0, beta=0.0):
         c_off, m, n, ldc, t0, t1 = (int(x) for x in o[:6])
         if m == 0 or n == 0:
             continue
-        if m <= 8 and n > 64:  # skinny tiles: all rows x 256 columns
-            want = {(0, j, 1) for j in range((n + 255) // 256)}
+        if m <= 8 and n > 64:  # skinny tiles: all rows x 1024 columns
+            want = {(0, j, 1) for j in range((n + 1023) // 1024)}
         else:
             want = {(i, j, 0) for i in range((m + 63) // 64) for j in range((n + 63) // 64)}
         assert seen.get(oi, set()) == want, "tiles do not cover the output"

@@ -290,7 +290,7 @@ def test_ozaki_split_and_slice_products(s):
 
 def test_ozaki_plan_records():
     rng = np.random.default_rng(8)
-    shapes = [(40, 70, 30), (16, 16, 16), (3, 200, 5), (64, 20, 33)]
+    shapes = [(40, 70, 30), (16, 16, 16), (3, 200, 5), (64, 20, 33), (5, 8, 100), (4, 40, 300)]
     meta, oa, ob, oc = [], 0, 0, 0
     for m, k, n in shapes:
         meta.append(((oc, oc + m * n), (m, n), (oa, oa + m * k), (m, k), (ob, ob + k * n), (k, n)))
@@ -298,20 +298,21 @@ def test_ozaki_plan_records():
     meta = tuple(meta)
     A, B = rng.normal(size=oa), rng.normal(size=ob)
     plan = P.ozaki_dot_plan(meta, 8)
-    # sectors with a dimension below 16 go to the native kernel, the rest are split
-    assert len(plan.outs) == 3 and len(plan.native.outs) == 1
+    # short contractions (K < 16) and skinny outputs (m <= 8 < 64 < n) go to the native
+    # kernel, the rest (small m or n included) are split
+    assert len(plan.outs) == 4 and len(plan.native.outs) == 2
     assert len({tuple(r[:1]) for r in plan.a_recs}) == len(plan.a_recs)  # each A block split once
     assert all(r[7] % 16 == 0 and r[7] >= r[2] for r in plan.a_recs)
     assert all(int(r[5]) % 16 == 0 for r in plan.a_recs) and all(int(r[5]) % 16 == 0 for r in plan.b_recs)
     # B blocks are split from their transposes: the copy plan reproduces B^T block by block
     tasks, items = plan.bT.packed(False)
     bT = PI.run_copy(tasks, items, B, np.zeros(plan.bT_size))
-    big = [mt for mt in meta if min(mt[3][0], mt[3][1], mt[5][1]) >= 16]
+    big = [mt for mt in meta if mt[3][1] >= 16 and not (mt[3][0] <= 8 and mt[5][1] > 64)]
     for rec, (slc, Dc, sla, Da, slb, Db) in zip(plan.b_recs, big):
         n, K = int(rec[1]), int(rec[2])
         np.testing.assert_array_equal(bT[rec[0]:rec[0] + n * K].reshape(n, K), B[slb[0]:slb[1]].reshape(Db).T)
     # the native part reproduces its sector
     out = PI.run_gemm(plan.native, A, B, np.zeros(oc))
-    slc, Dc, sla, Da, slb, Db = meta[2]
-    np.testing.assert_allclose(out[slc[0]:slc[1]].reshape(Dc), A[sla[0]:sla[1]].reshape(Da) @ B[slb[0]:slb[1]].reshape(Db),
-                               rtol=1e-13)
+    for slc, Dc, sla, Da, slb, Db in meta[4:]:
+        np.testing.assert_allclose(out[slc[0]:slc[1]].reshape(Dc),
+                                   A[sla[0]:sla[1]].reshape(Da) @ B[slb[0]:slb[1]].reshape(Db), rtol=1e-13)

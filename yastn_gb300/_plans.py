@@ -267,12 +267,12 @@ class GemmPlan:
         self._dev = {}
 
 
-SKINNY_ROWS, SKINNY_COLS = 8, 256
+SKINNY_ROWS, SKINNY_COLS = 8, 1024
 
 
 def _tiles_for(outs, terms):
     """Tiles (output, tile row, tile col, kind): kind 0 = 64x64, kind 1 = skinny (all m <= 8
-    rows x 256 columns), ordered by descending work so long tiles start first."""
+    rows x 1024 columns), ordered by descending work so long tiles start first."""
     tiles = []
     for oi, o in enumerate(outs):
         m, n = int(o[1]), int(o[2])
@@ -281,7 +281,7 @@ def _tiles_for(outs, terms):
         kk = int(sum(terms[t][2] for t in range(o[4], o[5])))
         if m <= SKINNY_ROWS and n > GEMM_TILE:
             for tc in range((n + SKINNY_COLS - 1) // SKINNY_COLS):
-                tiles.append((kk * m * 4, oi, 0, tc, 1))
+                tiles.append((kk * m * 16, oi, 0, tc, 1))
             continue
         for tr in range((m + GEMM_TILE - 1) // GEMM_TILE):
             for tc in range((n + GEMM_TILE - 1) // GEMM_TILE):
@@ -359,7 +359,7 @@ class OzakiPlan:
         self._dev = {}
 
 
-OZAKI_MIN_DIM = 16  # sector GEMMs with m, n or k below this stay on the native FP64 kernel
+OZAKI_MIN_DIM = 16  # sector GEMMs contracting fewer indices than this stay on the native FP64 kernel
 
 
 def ozaki_dot_plan(meta_dot, s):
@@ -375,7 +375,8 @@ def ozaki_dot_plan(meta_dot, s):
         for slc, Dc, sla, Da, slb, Db in meta_dot:
             m, K = Da
             n = Db[1]
-            if min(m, n, K) < OZAKI_MIN_DIM:  # too small to profit: native FP64 sector GEMM
+            if K < OZAKI_MIN_DIM or (m <= SKINNY_ROWS and n > GEMM_TILE):
+                # short contractions and skinny outputs stay on the native FP64 kernel
                 small.append((slc[0], m, n, n, [(sla[0], slb[0], K, K, 1, n, 1, 0)]))
                 continue
             Kp = (K + 15) // 16 * 16

@@ -4,8 +4,8 @@
 //
 // One launch covers every 64x64 output tile of every sector; the host orders tiles
 // largest-K first so that the long tiles start early. Outputs with at most 8 rows (the
-// contractions with a small MPO block, for instance) use "skinny" tiles instead: 8 rows x
-// 256 columns, one column per thread, op(A) staged in shared memory. On GB300 FP64 arithmetic runs at
+// contractions with a small MPO block, for instance) use "skinny" tiles instead: all rows x
+// 1024 columns, four columns per thread, op(A) staged in shared memory. On GB300 FP64 arithmetic runs at
 // about 1.2 TFLOP/s on the DFMA pipe (the DMMA m8n8k4 tensor path measured slower),
 // so a register-tiled DFMA kernel with shared-memory staging is FP64-bound: each thread
 // owns a 4x4 sub-tile and issues 16 independent FMAs per staged k.
@@ -20,6 +20,8 @@ constexpr int kThreads = 256;
 constexpr int kPad = 2;
 constexpr int kSkinnyRows = 8;   // rows of a skinny tile (outputs with m <= 8)
 constexpr int kSkinnyK = 64;     // K-chunk of op(A) staged for a skinny tile (64 x 8 <= 16 x 66)
+constexpr int kSkinnyCpt = 4;    // columns per thread of a skinny tile
+constexpr int kSkinnyCols = kThreads * kSkinnyCpt;  // 1024 = YB_GEMM_SKINNY_COLS
 
 struct Real {
   using T = double;
@@ -44,6 +46,72 @@ struct Cplx {
   __device__ static T add(T a, T b) { return make_double2(a.x + b.x, a.y + b.y); }
 };
 
+// Skinny tile: C (M x kSkinnyCols slice) = alpha sum_t op(A_t) op(B_t) + beta C for M <= 8.
+// op(A) is staged in shared memory K-chunk by K-chunk ([kSkinnyK][8], broadcast reads);
+// each thread owns kSkinnyCpt columns, kThreads apart, so B loads and C stores coalesce.
+template <class F, int M>
+__device__ __forceinline__ void skinny_tile(const typename F::T* __restrict__ A, const typename F::T* __restrict__ B,
+                                            typename F::T* __restrict__ C, const int64_t* __restrict__ orec,
+                                            const int64_t* __restrict__ terms, int tcol, double alpha, double beta,
+                                            typename F::T* Ak) {
+  using T = typename F::T;
+  const int64_t c_off = orec[0], n = orec[2], ldc = orec[3], t0 = orec[4], t1 = orec[5];
+  const int64_t j0 = (int64_t)tcol * kSkinnyCols + threadIdx.x;
+  T acc[kSkinnyCpt][M];
+#pragma unroll
+  for (int u = 0; u < kSkinnyCpt; ++u)
+#pragma unroll
+    for (int i = 0; i < M; ++i) acc[u][i] = F::zero();
+  for (int64_t t = t0; t < t1; ++t) {
+    const int64_t* trec = terms + t * YB_GEMM_TERM_REC;
+    const int64_t a_off = trec[0], b_off = trec[1], K = trec[2];
+    const int64_t a_rs = trec[3], a_cs = trec[4], b_rs = trec[5], b_cs = trec[6];
+    const int flags = (int)trec[7];
+    for (int64_t k0 = 0; k0 < K; k0 += kSkinnyK) {
+      __syncthreads();
+      for (int e = threadIdx.x; e < kSkinnyK * M; e += kThreads) {
+        const int i = e % M, l = e / M;
+        T v = F::zero();
+        if (k0 + l < K) {
+          v = A[a_off + i * a_rs + (k0 + l) * a_cs];
+          if (flags & 1) v = F::conj(v);
+        }
+        Ak[l * M + i] = v;
+      }
+      __syncthreads();
+      const int64_t kn = min((int64_t)kSkinnyK, K - k0);
+      const T* Bk = B + b_off + k0 * b_rs;
+      for (int64_t l = 0; l < kn; ++l) {
+        T b[kSkinnyCpt];
+#pragma unroll
+        for (int u = 0; u < kSkinnyCpt; ++u) {
+          const int64_t j = j0 + u * kThreads;
+          b[u] = (j < n) ? Bk[l * b_rs + j * b_cs] : F::zero();
+          if (flags & 2) b[u] = F::conj(b[u]);
+        }
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+          const T a = Ak[l * M + i];
+#pragma unroll
+          for (int u = 0; u < kSkinnyCpt; ++u) F::fma(acc[u][i], a, b[u]);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < kSkinnyCpt; ++u) {
+    const int64_t j = j0 + u * kThreads;
+    if (j >= n) continue;
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      T* p = C + c_off + i * ldc + j;
+      T v = F::scale(acc[u][i], alpha);
+      if (beta != 0.0) v = F::add(v, F::scale(*p, beta));
+      *p = v;
+    }
+  }
+}
+
 template <class F>
 __global__ void __launch_bounds__(kThreads) grouped_gemm_kernel(const typename F::T* __restrict__ A,
                                                                  const typename F::T* __restrict__ B,
@@ -61,56 +129,28 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_kernel(const typename F
   const int64_t c_off = orec[0], m = orec[1], n = orec[2], ldc = orec[3];
   const int64_t t0 = orec[4], t1 = orec[5];
   if (tl.w == 1) {
-    // skinny tile: all m <= 8 rows x 256 columns, one column per thread (coalesced B and C)
-    T* Ak = &As[0][0];  // [64][8] chunk of op(A), broadcast from shared memory
-    const int64_t j = (int64_t)tl.z * kThreads + threadIdx.x;
-    T acc8[kSkinnyRows];
-#pragma unroll
-    for (int i = 0; i < kSkinnyRows; ++i) acc8[i] = F::zero();
-    for (int64_t t = t0; t < t1; ++t) {
-      const int64_t* trec = terms + t * YB_GEMM_TERM_REC;
-      const int64_t a_off = trec[0], b_off = trec[1], K = trec[2];
-      const int64_t a_rs = trec[3], a_cs = trec[4], b_rs = trec[5], b_cs = trec[6];
-      const int flags = (int)trec[7];
-      for (int64_t k0 = 0; k0 < K; k0 += kSkinnyK) {
-        __syncthreads();
-        for (int e = threadIdx.x; e < kSkinnyK * kSkinnyRows; e += kThreads) {
-          const int i = e % kSkinnyRows, l = e / kSkinnyRows;
-          T v = F::zero();
-          if (i < m && k0 + l < K) {
-            v = A[a_off + i * a_rs + (k0 + l) * a_cs];
-            if (flags & 1) v = F::conj(v);
-          }
-          Ak[l * kSkinnyRows + i] = v;
-        }
-        __syncthreads();
-        if (j < n) {
-          const int64_t kn = min((int64_t)kSkinnyK, K - k0);
-          for (int64_t l = 0; l < kn; ++l) {
-            T b = B[b_off + (k0 + l) * b_rs + j * b_cs];
-            if (flags & 2) b = F::conj(b);
-#pragma unroll
-            for (int i = 0; i < kSkinnyRows; ++i) F::fma(acc8[i], Ak[l * kSkinnyRows + i], b);
-          }
-        }
-      }
-    }
-    if (j < n) {
-#pragma unroll
-      for (int i = 0; i < kSkinnyRows; ++i) {
-        if (i >= m) break;
-        T* p = C + c_off + i * ldc + j;
-        T v = F::scale(acc8[i], alpha);
-        if (beta != 0.0) v = F::add(v, F::scale(*p, beta));
-        *p = v;
-      }
+    // skinny tile: the m <= 8 rows x kSkinnyCols columns, specialised on m so that no FP64
+    // FMA is spent on padding rows (FP64 issue rate, not bandwidth, bounds these tiles)
+    switch (m) {
+      case 1: skinny_tile<F, 1>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]); break;
+      case 2: skinny_tile<F, 2>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]); break;
+      case 3: skinny_tile<F, 3>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]); break;
+      case 4: skinny_tile<F, 4>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]); break;
+      case 5: skinny_tile<F, 5>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]); break;
+      case 6: skinny_tile<F, 6>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]); break;
+      case 7: skinny_tile<F, 7>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]); break;
+      default: skinny_tile<F, 8>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]); break;
     }
     return;
   }
   const int64_t row0 = (int64_t)tl.y * kTile, col0 = (int64_t)tl.z * kTile;
 
-  const int tx = threadIdx.x & 15;  // column group
-  const int ty = threadIdx.x >> 4;  // row group
+  // thread (ty, tx) owns rows 4ty..4ty+3 and columns 4tx..4tx+3; a warp covers 16 rows x 32
+  // columns, so the warps of a small sector's tile that fall outside it skip the FMAs
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ty = (warp >> 1) * 4 + (lane >> 3);  // row group
+  const int tx = (warp & 1) * 8 + (lane & 7);    // column group
+  const bool active = (row0 + (warp >> 1) * 16 < m) && (col0 + (warp & 1) * 32 < n);
   T acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
@@ -155,8 +195,10 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_kernel(const typename F
         Bs[l][j] = v;
       }
       __syncthreads();
+      const int kn = (int)min((int64_t)kK, K - k0);
 #pragma unroll
       for (int l = 0; l < kK; ++l) {
+        if (!active || l >= kn) break;
         T a[4], b[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) a[i] = As[l][ty * 4 + i];

@@ -130,6 +130,8 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm_kernel(const __nv_bflo
   const int64_t row0 = (int64_t)tl.y * kTile, col0 = (int64_t)tl.z * kTile;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wm = warp & 1, wn = warp >> 1;  // warp sub-tile: rows wm*32.., cols wn*16..
+  // a warp whose sub-tile lies wholly outside the sector (small m or n) only helps staging
+  const bool active = (row0 + wm * 32 < m) && (col0 + wn * 16 < n);
 
   const int64_t a_stride = m * Kp, b_stride = n * Kp;
   auto stage = [&](int buf, int64_t k0) {
@@ -170,6 +172,7 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm_kernel(const __nv_bflo
     cp_async_wait_all();
     __syncthreads();
     if (st + 1 < nsteps) stage(buf ^ 1, (st + 1) * kK);
+    if (!active) continue;
 #pragma unroll
     for (int ta = 0; ta < S; ++ta) {
       unsigned af[2][4];
@@ -194,20 +197,25 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm_kernel(const __nv_bflo
       }
     }
     if (((st + 1) % kChunkSteps) == 0 || st + 1 == nsteps) {
-      // fold the exact FP32 diagonal sums into FP64, smallest diagonal first
+      // fold the diagonal sums (exact integers below 2^24 in FP32) into FP64: the weighted
+      // sum sum_d acc_d 2^(-7d) is formed exactly in two int64 halves (diagonals 0..3 and
+      // 4..7, each below 2^46) on the integer pipe, and only the two halves are converted,
+      // which keeps the fold off GB300's narrow FP64 pipe
 #pragma unroll
       for (int i = 0; i < 2; ++i)
 #pragma unroll
         for (int j = 0; j < 2; ++j)
 #pragma unroll
           for (int v = 0; v < 4; ++v) {
-            double sum = 0.0;
+            long long hi = 0, lo = 0;
 #pragma unroll
-            for (int d = S - 1; d >= 0; --d) {
-              sum = fma((double)acc[d][i][j][v], 1.0 / (double)(1ull << (7 * d)), sum);
+            for (int d = 0; d < S; ++d) {
+              const long long q = (long long)__float2int_rn(acc[d][i][j][v]);
+              if (d < 4) hi += q << (7 * (3 - d));
+              else lo += q << (7 * (S - 1 - d));
               acc[d][i][j][v] = 0.f;
             }
-            acc64[i][j][v] += sum;
+            acc64[i][j][v] += fma((double)lo, 1.0 / (double)(1ll << (7 * (S - 1))), (double)hi * 0x1p-21);
           }
     }
   }

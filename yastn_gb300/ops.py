@@ -156,7 +156,7 @@ def dot_ozaki(A, B, meta_dot, Dsize, slices=OZAKI_SLICES):
         raise NotImplementedError("yastn_gb300 dot_ozaki: real float64 operands only")
     plan = P.ozaki_dot_plan(meta_dot, slices)
     out = torch.zeros(Dsize, dtype=A.dtype, device=A.device)
-    run_gemm(plan.native, A, B, out)  # sectors with a dimension below 16: native FP64
+    run_gemm(plan.native, A, B, out)  # short (K < 16) and skinny sectors: native FP64
     if len(plan.tiles) == 0:
         return out
     dev = A.device
