@@ -56,8 +56,16 @@ int yb_last_cuda_error(void);
  *   strides and extents of the record are then in pairs)
  *   [YB_CP_SIZE+i] extent, [YB_CP_SSTR+i] src stride, [YB_CP_DSTR+i] dst stride (units),
  *   [YB_CP_MAGIC+i], [YB_CP_SHIFT+i] fast-division constants of extent i
- * items: n_items pairs (task index, first unit); each item covers up to
- *   YB_COPY_ITEM_UNITS units of its task.
+ *   [YB_CP_KIND] 0: a plain task (above); 1: a tiled transpose, for a task whose source is
+ *   contiguous along a dim other than the destination-contiguous innermost one. Its dims
+ *   are then the outer dims followed by two tile dims, y (the source-contiguous dim) and
+ *   x (the destination-contiguous dim), whose extents count YB_COPY_TILE-wide tiles and
+ *   whose strides are per tile (YB_COPY_TILE x the element stride; the source stride of y
+ *   and the destination stride of x are YB_COPY_TILE); [YB_CP_NX], [YB_CP_NY] hold the
+ *   element extents of x and y, [YB_CP_COUNT] the number of tiles. A CTA moves a tile
+ *   through shared memory, reading along y and writing along x, both coalesced.
+ * items: n_items pairs (task index, first unit or tile); each item covers up to
+ *   YB_COPY_ITEM_UNITS units (YB_COPY_ITEM_TILES tiles for kind 1) of its task.
  * unit_bytes: element size, 8 (FP64) or 16 (complex128); src/dst must be 16-byte aligned
  *   when any task has YB_CP_VEC set.
  * Replaces the per-block copy loops of transpose_and_merge / unmerge and their adjoints.
@@ -68,13 +76,18 @@ int yb_last_cuda_error(void);
 #define YB_CP_NDIM 2
 #define YB_CP_COUNT 3
 #define YB_CP_VEC 4
+#define YB_CP_KIND 5
+#define YB_CP_NX 6
+#define YB_CP_NY 7
 #define YB_CP_MAXD 8
 #define YB_CP_SIZE 8
 #define YB_CP_SSTR 16
 #define YB_CP_DSTR 24
 #define YB_CP_MAGIC 32
 #define YB_CP_SHIFT 40
-#define YB_COPY_ITEM_UNITS 8192
+#define YB_COPY_ITEM_UNITS 2048
+#define YB_COPY_TILE 32
+#define YB_COPY_ITEM_TILES 2
 int yb_block_copy(const void* src, void* dst, int unit_bytes,
                   const int64_t* tasks, int n_tasks,
                   const int64_t* items, int n_items, void* stream);

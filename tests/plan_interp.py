@@ -22,6 +22,10 @@ def run_copy(tasks, items, src, dst):
     for ti, rec in enumerate(tasks):
         ndim, count, vec = int(rec[P.CP_NDIM]), int(rec[P.CP_COUNT]), int(rec[P.CP_VEC])
         firsts = sorted(covered.get(ti, []))
+        if rec[P.CP_KIND] == 1:
+            assert firsts == list(range(0, count, P.COPY_ITEM_TILES)), "items do not tile the task"
+            _run_tiles(rec, src, dst)
+            continue
         assert firsts == list(range(0, count, P.COPY_ITEM_UNITS)), "items do not tile the task"
         idx = np.arange(count, dtype=np.int64)
         so = np.full(count, rec[P.CP_SRC], dtype=np.int64)
@@ -40,6 +44,28 @@ def run_copy(tasks, items, src, dst):
         else:
             dst[do] = src[so]
     return dst
+
+
+def _run_tiles(rec, src, dst):
+    """A kind-1 (tiled transpose) record: tile index -> (outer dims, tile y, tile x) by the
+    record's fast-division constants, then the elements of the tile clipped to (NY, NX)."""
+    T = P.COPY_TILE
+    ndim, count = int(rec[P.CP_NDIM]), int(rec[P.CP_COUNT])
+    nx, ny = int(rec[P.CP_NX]), int(rec[P.CP_NY])
+    ss_x, ds_y = int(rec[P.CP_SSTR + ndim - 1]) // T, int(rec[P.CP_DSTR + ndim - 2]) // T
+    assert rec[P.CP_SSTR + ndim - 2] == T and rec[P.CP_DSTR + ndim - 1] == T
+    for t in range(count):
+        idx, so, do, pos = t, int(rec[P.CP_SRC]), int(rec[P.CP_DST]), {}
+        for d in range(ndim - 1, -1, -1):
+            size = int(rec[P.CP_SIZE + d])
+            q = int(fast_div_np(idx, int(rec[P.CP_MAGIC + d]), int(rec[P.CP_SHIFT + d])))
+            assert q == idx // size, "fast division constants are wrong"
+            r = idx - q * size
+            so += r * int(rec[P.CP_SSTR + d]); do += r * int(rec[P.CP_DSTR + d]); pos[d] = r
+            idx = q
+        ex, ey = min(T, nx - pos[ndim - 1] * T), min(T, ny - pos[ndim - 2] * T)
+        xi, yi = np.meshgrid(np.arange(ex), np.arange(ey), indexing='ij')
+        dst[do + yi * ds_y + xi] = src[so + xi * ss_x + yi]
 
 
 def run_gemm(plan, a, b, c, alpha=1.0, beta=0.0):

@@ -260,6 +260,64 @@ def _ozaki_digits(x, s):
     return e, digits
 
 
+def _ozaki_digits_bits(x, s):
+    """The integer-only split of csrc/yb_ozaki.cu restated with numpy int64: row exponent
+    from the bit patterns, Q = rint(x 2^{7s-e}) by a round-half-even shift of the
+    mantissa, digits from U = Q + 64 (1 + 128 + ... + 128^{s-2})."""
+    bits = np.ascontiguousarray(x).view(np.int64)
+    mag = bits & np.int64(0x7fffffffffffffff)
+    mx = mag.max(axis=1)
+    e = np.zeros(len(x), dtype=np.int64)
+    normal = mx >= (1 << 52)
+    e[normal] = (mx[normal] >> 52) - 1022
+    sub = (~normal) & (mx > 0)
+    e[sub] = np.frexp(mx[sub].view(np.float64))[1]
+    E = mag >> 52
+    M = mag & np.int64((1 << 52) - 1)
+    ex = np.where(E != 0, E - 1075, -1074)
+    M = np.where(E != 0, M | np.int64(1 << 52), M)
+    up = ex + 7 * s - e[:, None]
+    q = np.zeros_like(M)
+    left = up >= 0
+    q[left] = M[left] << up[left]
+    sh = np.minimum(-up, 63)
+    r = ~left
+    qr = M[r] >> sh[r]
+    rem = M[r] & ((np.int64(1) << sh[r]) - 1)
+    half = np.int64(1) << (sh[r] - 1)
+    qr = qr + ((rem > half) | ((rem == half) & ((qr & 1) == 1)))
+    q[r] = qr
+    q = np.where(mag == 0, 0, q)
+    q = np.where(bits < 0, -q, q)
+    bias = 0
+    for _ in range(s - 1):
+        bias = (bias << 7) | 64
+    u = q + np.int64(bias)
+    digits = [((u >> (7 * (s - 1 - t))) & 127) - 64 for t in range(1, s)]
+    return e, [(u >> (7 * (s - 1))).astype(np.float64)] + [d.astype(np.float64) for d in digits]
+
+
+@pytest.mark.parametrize('s', [6, 7, 8])
+def test_ozaki_integer_split_matches_rint_split(s):
+    """The bit-level split (no FP64 arithmetic) gives exactly the digits of rint(x 2^{7s-e}):
+    normal, subnormal, zero and negative entries, and exact rounding ties."""
+    rng = np.random.default_rng(12)
+    x = rng.normal(size=(6, 40)) * 10.0 ** rng.uniform(-30, 30, size=(6, 1))
+    x[1, :5] = 0.0
+    x[2] = rng.normal(size=40) * 1e-310           # a subnormal row
+    x[3, 7] = -x[3, 7]
+    e = np.frexp(np.abs(x[4]).max())[1]
+    x[4, 10] = (2 ** 40 + 0.5) * 2.0 ** (e - 7 * s)   # ties at the last digit
+    x[4, 11] = (2 ** 40 + 1.5) * 2.0 ** (e - 7 * s)
+    x[4, 12] = -(2 ** 40 + 0.5) * 2.0 ** (e - 7 * s)
+    x[5] = 0.0                                     # an all-zero row
+    e_ref, d_ref = _ozaki_digits(x, s)
+    e_bit, d_bit = _ozaki_digits_bits(x, s)
+    np.testing.assert_array_equal(e_ref, e_bit)
+    for a, b in zip(d_ref, d_bit):
+        np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize('s', [6, 7, 8])
 def test_ozaki_split_and_slice_products(s):
     """Digits are BF16-exact integers; the kept slice pairs reproduce A @ B to the bound."""

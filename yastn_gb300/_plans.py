@@ -14,7 +14,8 @@ import numpy as np
 # record layout constants (must match include/yastn_gb300.h)
 COPY_REC, CP_SRC, CP_DST, CP_NDIM, CP_COUNT, CP_VEC = 48, 0, 1, 2, 3, 4
 CP_MAXD, CP_SIZE, CP_SSTR, CP_DSTR, CP_MAGIC, CP_SHIFT = 8, 8, 16, 24, 32, 40
-COPY_ITEM_UNITS = 8192
+CP_KIND, CP_NX, CP_NY = 5, 6, 7
+COPY_ITEM_UNITS, COPY_TILE, COPY_ITEM_TILES = 2048, 32, 2
 GEMM_OUT_REC, GEMM_TERM_REC, GEMM_TILE = 8, 8, 64
 SVD_REC = 16
 MASK_REC = 8
@@ -128,6 +129,34 @@ def _collapse(sizes, ss, ds):
     return [x[0] for x in out], [x[1] for x in out], [x[2] for x in out]
 
 
+def _transpose_task(so, do, sizes, ss, ds):
+    """Tiled-transpose record (kind 1) for a collapsed task whose destination is contiguous
+    along the innermost dim x and whose source is contiguous along another dim y; None if
+    the task is not such a transpose (or too narrow to profit)."""
+    last = len(sizes) - 1
+    if last < 1 or ds[last] != 1 or ss[last] == 1 or sizes[last] < 4:
+        return None
+    ys = [j for j in range(last) if ss[j] == 1 and sizes[j] >= 4]
+    if not ys:
+        return None
+    y = ys[-1]
+    outer = [j for j in range(last) if j != y]
+    T = COPY_TILE
+    ty, tx = -(-sizes[y] // T), -(-sizes[last] // T)
+    dims = [(sizes[j], ss[j], ds[j]) for j in outer] + [(ty, T, T * ds[y]), (tx, T * ss[last], T)]
+    count = int(np.prod([d[0] for d in dims], dtype=np.int64))
+    if count >= 2 ** 31:
+        raise PlanError("copy task larger than 2^31 tiles")
+    rec = np.zeros(COPY_REC, dtype=np.int64)
+    rec[CP_SRC], rec[CP_DST], rec[CP_NDIM], rec[CP_COUNT], rec[CP_VEC] = so, do, len(dims), count, 0
+    rec[CP_KIND], rec[CP_NX], rec[CP_NY] = 1, sizes[last], sizes[y]
+    for i, (n, a, b) in enumerate(dims):
+        m, sh = fast_div_consts(n)
+        rec[CP_SIZE + i], rec[CP_SSTR + i], rec[CP_DSTR + i] = n, a, b
+        rec[CP_MAGIC + i], rec[CP_SHIFT + i] = m, sh
+    return rec
+
+
 class CopyPlan:
     """Host copy of a family-(a) plan: tasks, items, element coverage."""
 
@@ -153,6 +182,11 @@ class CopyPlan:
             sizes, ss, ds = _collapse(sizes, ss, ds)
             if len(sizes) > CP_MAXD:
                 raise PlanError(f"copy task with {len(sizes)} non-collapsible dims (max {CP_MAXD})")
+            tr = _transpose_task(so, do, sizes, ss, ds)
+            if tr is not None:
+                recs.append(tr)
+                items.extend((ti, f) for f in range(0, int(tr[CP_COUNT]), COPY_ITEM_TILES))
+                continue
             vec = 0
             if vec_ok and ss[-1] == 1 and ds[-1] == 1 and sizes[-1] % 2 == 0 and so % 2 == 0 and do % 2 == 0 \
                     and all(x % 2 == 0 for x in ss[:-1]) and all(x % 2 == 0 for x in ds[:-1]):

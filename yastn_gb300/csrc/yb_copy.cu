@@ -10,6 +10,7 @@
 // Work is split into items of up to YB_COPY_ITEM_UNITS units of one task; one CTA
 // handles one item. Within an item consecutive threads take consecutive units of the
 // innermost dim (destination-contiguous after collapsing), so stores are coalesced.
+// Tasks that transpose (source contiguous along another dim) are tiled instead.
 #include "yb_common.cuh"
 
 namespace yb {
@@ -61,6 +62,47 @@ __device__ __forceinline__ void copy_units(const Unit* __restrict__ src, Unit* _
   }
 }
 
+// Kind-1 tasks: tiles of YB_COPY_TILE x YB_COPY_TILE elements staged in shared memory.
+// The tile index is decomposed over the record's dims like a unit index; the remainders
+// of the last two dims are the tile's y and x positions. Each warp reads tile rows along
+// y (source-contiguous) and, after the barrier, writes tile rows along x
+// (destination-contiguous), so both sides are coalesced.
+template <typename Elem>
+__device__ __forceinline__ void copy_tiles(const Elem* __restrict__ src, Elem* __restrict__ dst, const int64_t* rec,
+                                           int64_t first, Elem (*tile)[YB_COPY_TILE + 1]) {
+  constexpr int T = YB_COPY_TILE;
+  const int ndim = (int)rec[YB_CP_NDIM];
+  const int64_t count = rec[YB_CP_COUNT];
+  const int64_t nx = rec[YB_CP_NX], ny = rec[YB_CP_NY];
+  const int64_t ss_x = rec[YB_CP_SSTR + ndim - 1] / T, ds_y = rec[YB_CP_DSTR + ndim - 2] / T;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = kThreads >> 5;
+  const int64_t last = min(count, first + (int64_t)YB_COPY_ITEM_TILES);
+  for (int64_t t = first; t < last; ++t) {
+    uint32_t idx = (uint32_t)t;
+    int64_t so = rec[YB_CP_SRC], dof = rec[YB_CP_DST], tx = 0, ty = 0;
+#pragma unroll
+    for (int d = YB_CP_MAXD - 1; d >= 0; --d) {
+      if (d < ndim) {
+        const uint32_t size = (uint32_t)rec[YB_CP_SIZE + d];
+        const uint32_t q = fast_div(idx, (uint32_t)rec[YB_CP_MAGIC + d], (uint32_t)rec[YB_CP_SHIFT + d]);
+        const int64_t r = (int64_t)(idx - q * size);
+        so += r * rec[YB_CP_SSTR + d];
+        dof += r * rec[YB_CP_DSTR + d];
+        if (d == ndim - 1) tx = r;
+        if (d == ndim - 2) ty = r;
+        idx = q;
+      }
+    }
+    const int ex = (int)min((int64_t)T, nx - tx * T), ey = (int)min((int64_t)T, ny - ty * T);
+    __syncthreads();  // the previous tile has been written out
+    for (int xi = warp; xi < ex; xi += nwarps)
+      if (lane < ey) tile[xi][lane] = __ldg(src + so + xi * ss_x + lane);
+    __syncthreads();
+    for (int yi = warp; yi < ey; yi += nwarps)
+      if (lane < ex) dst[dof + yi * ds_y + lane] = tile[lane][yi];
+  }
+}
+
 // Elem is the element type of the data (double for FP64, double2 for complex128). FP64
 // tasks flagged YB_CP_VEC move pairs of elements as one 16-byte unit.
 template <typename Elem>
@@ -68,12 +110,15 @@ __global__ void __launch_bounds__(kThreads) block_copy_kernel(const Elem* __rest
                                                                const int64_t* __restrict__ tasks,
                                                                const int64_t* __restrict__ items) {
   __shared__ int64_t rec[YB_COPY_REC];
+  __shared__ Elem tile[YB_COPY_TILE][YB_COPY_TILE + 1];
   const int64_t* item = items + 2 * (int64_t)blockIdx.x;
   const int64_t task = item[0];
   const int64_t first = item[1];
   if (threadIdx.x < YB_COPY_REC) rec[threadIdx.x] = tasks[task * YB_COPY_REC + threadIdx.x];
   __syncthreads();
-  if (sizeof(Elem) == 8 && rec[YB_CP_VEC] != 0)
+  if (rec[YB_CP_KIND] == 1)
+    copy_tiles<Elem>(src, dst, rec, first, tile);
+  else if (sizeof(Elem) == 8 && rec[YB_CP_VEC] != 0)
     copy_units<double2>(reinterpret_cast<const double2*>(src), reinterpret_cast<double2*>(dst), rec, first);
   else
     copy_units<Elem>(src, dst, rec, first);

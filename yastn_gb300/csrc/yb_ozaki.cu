@@ -41,18 +41,44 @@ constexpr int kThreads = 256;
 //      [5] dst offset (bf16) [6] exponent offset [7] Kp (K rounded up to 16)
 // dst layout: [slice][row][Kp] bf16, padding zero-filled.
 //
-// The digits are extracted with integer arithmetic: Q = rint(a 2^{7s-e}) (|Q| < 2^{7s}),
-// then balanced base-128 digits from the low end, d = ((Q + 64) & 127) - 64 in [-64, 63]
-// and Q = (Q - d) >> 7, leave the leading digit d_0 = Q in [-128, 128]. This represents
+// The digits are extracted with integer arithmetic only (GB300's FP64 pipe is narrow):
+// Q = rint(a 2^{7s-e}) (|Q| < 2^{7s}) is formed from a's mantissa and exponent bits by a
+// shift with round-half-to-even, then the balanced base-128 digits follow from
+// U = Q + 64 (1 + 128 + ... + 128^{s-2}): d_t = ((U >> 7(s-1-t)) & 127) - 64 for t >= 1 and
+// the leading digit d_0 = U >> 7(s-1) in [-128, 128] (arithmetic shift). This represents
 // a 2^-e = sum_t d_t 2^{-7(t+1)} up to the rounding of Q (half a unit of the last digit).
-__device__ __forceinline__ void digits_of(double a, int e, int s, int* d) {
-  long long q = llrint(scalbn(a, 7 * s - e));
-  for (int t = s - 1; t >= 1; --t) {
-    const long long r = ((q + 64) & 127) - 64;
-    d[t] = (int)r;
-    q = (q - r) >> 7;
+__device__ __forceinline__ long long scaled_rint(long long bits, int e, int s) {
+  const long long mag = bits & 0x7fffffffffffffffll;
+  if (mag == 0) return 0;
+  const int E = (int)(mag >> 52);
+  long long M = mag & 0xfffffffffffffll;
+  int ex = -1074;  // a = M 2^ex
+  if (E != 0) {
+    M |= 1ll << 52;
+    ex = E - 1075;
   }
-  d[0] = (int)q;
+  const int up = ex + 7 * s - e;  // Q = rint(M 2^up)
+  long long q;
+  if (up >= 0) {
+    q = M << up;  // |Q| < 2^{7s}: up <= 7s - 53
+  } else {
+    const int sh = min(-up, 63);
+    q = M >> sh;
+    const unsigned long long rem = (unsigned long long)M & ((1ull << sh) - 1ull);
+    const unsigned long long half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (q & 1))) ++q;
+  }
+  return bits < 0 ? -q : q;
+}
+
+__device__ __forceinline__ void digits_of(long long bits, int e, int s, int* d) {
+  long long bias = 0;
+  for (int t = 0; t < s - 1; ++t) bias = (bias << 7) | 64;
+  const long long u = scaled_rint(bits, e, s) + bias;
+#pragma unroll
+  for (int t = 1; t < 8; ++t)
+    if (t < s) d[t] = (int)((u >> (7 * (s - 1 - t))) & 127) - 64;
+  d[0] = (int)(u >> (7 * (s - 1)));
 }
 
 __global__ void split_rows_kernel(const double* __restrict__ src, __nv_bfloat16* __restrict__ slices,
@@ -63,20 +89,22 @@ __global__ void split_rows_kernel(const double* __restrict__ src, __nv_bfloat16*
   const int lane = threadIdx.x & 31;
   const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (row >= rows) return;
-  const double* a = src + r[0] + row * rs;
-  double mx = 0.0;
-  for (int64_t l = lane; l < K; l += 32) mx = fmax(mx, fabs(a[l]));
+  const long long* a = reinterpret_cast<const long long*>(src + r[0] + row * rs);
+  // row maximum of |a| on the bit patterns (non-negative doubles order as integers)
+  long long mx = 0;
+  for (int64_t l = lane; l < K; l += 32) mx = max(mx, __ldg(a + l) & 0x7fffffffffffffffll);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  int e = 0;
-  if (mx > 0.0) frexp(mx, &e);  // mx = f 2^e, f in [0.5, 1): |a| < 2^e
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  int e = 0;  // max |a| = f 2^e, f in [0.5, 1): |a| < 2^e
+  if (mx >= (1ll << 52)) e = (int)(mx >> 52) - 1022;
+  else if (mx > 0) frexp(__longlong_as_double(mx), &e);
   if (lane == 0) exps[r[6] + row] = e;
   const int64_t slice_stride = rows * Kp;
   __nv_bfloat16* dst = slices + r[5] + row * Kp;
   for (int64_t l = 2 * lane; l < Kp; l += 64) {
     int d0[8], d1[8];
-    if (l < K) digits_of(a[l], e, s, d0); else for (int t = 0; t < 8; ++t) d0[t] = 0;
-    if (l + 1 < K) digits_of(a[l + 1], e, s, d1); else for (int t = 0; t < 8; ++t) d1[t] = 0;
+    if (l < K) digits_of(__ldg(a + l), e, s, d0); else for (int t = 0; t < 8; ++t) d0[t] = 0;
+    if (l + 1 < K) digits_of(__ldg(a + l + 1), e, s, d1); else for (int t = 0; t < 8; ++t) d1[t] = 0;
     for (int t = 0; t < s; ++t) {
       __nv_bfloat162 v;
       v.x = __int2bfloat16_rn(d0[t]);
