@@ -17,6 +17,11 @@ native FP64 result is measured every run and must stay below 1e-10); the native 
 path and the workload's truncated block SVD (svd_with_truncation, D_total=64) are
 reported as extra fields.
 
+``--workload cfg5``: the precision study, the same tensordot on U(1) tensors with D=128
+per leg over charges -16..16 and every block scaled by 10^U(-4,0) (sector GEMMs up to
+946^3), reporting emulated and native FP64 TFLOP/s and the largest relative error per
+sector result of both against the FP64 oracle.
+
 One JSON line is printed by rank 0. ``--impl reference`` times the CPU restatement of
 the reference NumPy backend on the host cores for the same workload instead.
 """
@@ -45,7 +50,7 @@ def parse():
     p.add_argument('--steps', type=int, default=20)
     p.add_argument('--warmup', type=int, default=5)
     p.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
-    p.add_argument('--workload', default='cfg2', choices=['cfg1', 'cfg2'])
+    p.add_argument('--workload', default='cfg2', choices=['cfg1', 'cfg2', 'cfg5'])
     p.add_argument('--gemm', default='emulated', choices=['emulated', 'fp64'],
                    help='sector-GEMM mode of the headline (cfg2)')
     p.add_argument('--no-svd', action='store_true', help='skip the extra svd_with_truncation timing')
@@ -56,6 +61,9 @@ def parse():
 
 class Cfg1:
     name = "U(1) rank-4 D=64 tensordot A(2,3)xB(0,1), fuse_to_matrix, 13 sectors, FP64"
+    metric = METRIC
+    has_svd = True
+    ozaki_traffic = 78263296 + 8303872  # dram bytes read + written by one launch (ncu, this workload)
 
     def __init__(self):
         from yastn_gb300.workloads import load_trace, cfg1_inputs
@@ -82,6 +90,27 @@ class Cfg1:
         Bm = oracle.transpose_and_merge(self.B, *self.mB)
         Cm = oracle.dot(Am, Bm, *self.mdot)
         return oracle.unmerge(Cm, self.mun)
+
+
+class Cfg5(Cfg1):
+    name = ("precision study: U(1) rank-4 D=128 per leg over t=-16..16, blocks scaled by 10^U(-4,0), "
+            "tensordot A(2,3)xB(0,1), fuse_to_matrix, sector GEMMs up to 946^3, FP64")
+    metric = "tensordot TFLOP/s (precision study U(1) D=128/leg, per-block scales 1e-4..1, FP64, <=1e-10 rel)"
+    has_svd = False
+    ozaki_traffic = None
+
+    def __init__(self):
+        from yastn_gb300.workloads import load_trace, cfg5_inputs
+        from yastn_gb300 import _plans as P
+        self.tr = load_trace('cfg5')
+        self.A, self.B = cfg5_inputs(self.tr)
+        c = self.tr['calls']
+        self.mA = c[0]['args'][1:]
+        self.mB = c[1]['args'][1:]
+        self.mdot = c[2]['args'][2:]
+        self.mun = c[3]['args'][1]
+        self.flops = P.dot_plan(self.mdot[0]).flops
+        self.bytes_merge = 16 * self.A.size
 
 
 class Cfg2:
@@ -138,7 +167,7 @@ def run_reference(args, wl):
         ts.append(time.perf_counter() - t0)
     t = float(np.mean(ts))
     value = wl.flops / t / 1e12
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+    line = {"impl": "reference", "metric": wl.metric, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded yastn normal draws)",
             "config": {"workload": wl.name, "policy": "fuse_to_matrix"},
@@ -294,6 +323,7 @@ def run_gpu(args, wl):
     BK.set_gemm_mode('fp64')
     Cn = tensordot(dA, dB)
     assert abs(float(Cn.sum()) - chk['sum0']) <= 1e-9 * chk['abs0'], "tensordot result differs from the reference"
+    sector_err = per_sector_errors(torch, BK, wl, dA, dB)
     for _ in range(args.warmup):
         tensordot(dA, dB)
     barrier()
@@ -362,7 +392,7 @@ def run_gpu(args, wl):
 
     # the workload's truncated block SVD (extra field)
     svd_ms = None
-    if not args.no_svd:
+    if wl.has_svd and not args.no_svd:
         C = tensordot(dA, dB)
 
         def svd_trunc():
@@ -403,17 +433,18 @@ def run_gpu(args, wl):
     cpu_t, reps = time_cpu(wl.cpu_step, budget_s=8.0)
     achieved = tensor_flops / t_gemm / 1e12
     line = {
-        "metric": METRIC, "value": world * wl.flops / t_max / 1e12, "unit": UNIT, "n_gpus": world,
+        "metric": wl.metric, "value": world * wl.flops / t_max / 1e12, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 (sector GEMMs emulated: 8 bf16 digit slices, fp32/fp64 accumulation)",
         "data": "synthetic (seeded normal draws as yastn.rand, metadata recorded from yastn)",
         "config": {"workload": wl.name, "flop_per_step": wl.flops, "parallelism": f"replicas{world}",
                    "gemm_mode": "emulated", "l2": "flushed between timed steps (256 MB write)",
-                   "max_rel_err_vs_fp64": emu_err},
+                   "max_rel_err_vs_fp64": emu_err,
+                   "max_rel_err_per_sector_vs_oracle": sector_err},
         "roofline": {"bound": "tensor", "kernel": "yb ozaki_gemm_kernel<8> (mma.sync bf16, 36 slice-pair products)",
                      "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s", "frac": achieved / bf16_peak,
-                     "peak_source": peak_src, "traffic": 78263296 + 8303872,
+                     "peak_source": peak_src, "traffic": wl.ozaki_traffic,
                      "traffic_note": "dram bytes read+written by one launch, ncu capture on this workload"},
         "cpu_baseline": {"value": wl.flops / cpu_t / 1e12, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
                          "sample": f"{reps} tensordot steps of the same workload (numpy BLAS, median)"},
@@ -433,6 +464,32 @@ def run_gpu(args, wl):
     print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
+
+
+def per_sector_errors(torch, BK, wl, dA, dB):
+    """Max relative error per sector result (max |C_s - C_s^ref| / max |C_s^ref| over the
+    sector) of the native and the emulated GEMM modes against the FP64 oracle (NumPy)."""
+    import oracle
+    Am = oracle.transpose_and_merge(wl.A, *wl.mA)
+    Bm = oracle.transpose_and_merge(wl.B, *wl.mB)
+    ref = oracle.dot(Am, Bm, *wl.mdot)
+    dAm = BK.transpose_and_merge(dA, *wl.mA)
+    dBm = BK.transpose_and_merge(dB, *wl.mB)
+    out = {}
+    mode0 = BK.get_gemm_mode()
+    for mode in ('fp64', 'emulated'):
+        BK.set_gemm_mode(mode)
+        got = BK.dot(dAm, dBm, *wl.mdot).cpu().numpy()
+        worst = 0.0
+        for slc, *_ in wl.mdot[0]:
+            r, g = ref[slc[0]:slc[1]], got[slc[0]:slc[1]]
+            mx = np.abs(r).max() if r.size else 0.0
+            if mx > 0:
+                worst = max(worst, float(np.abs(g - r).max() / mx))
+        out[mode] = worst
+    BK.set_gemm_mode(mode0)
+    assert out['fp64'] <= 1e-12 and out['emulated'] <= 1e-10, out
+    return out
 
 
 def bf16_peak_tflops():
@@ -634,7 +691,7 @@ def kernel_roofline(torch, dev, run_once, w, gemm_mode, reps=5):
 
 def main():
     args = parse()
-    wl = Cfg1() if args.workload == 'cfg1' else Cfg2()
+    wl = {'cfg1': Cfg1, 'cfg2': Cfg2, 'cfg5': Cfg5}[args.workload]()
     if args.impl == 'reference':
         run_reference(args, wl)
     elif args.workload == 'cfg2':

@@ -528,6 +528,39 @@ def scen_cfg1():
     save('cfg1', rec, extra)
 
 
+def scen_cfg5():
+    """Precision-study workload: U(1) rank-4 tensors with D=128 per leg over t=-16..16,
+    sector dims ~ exp(-t^2/50) (empty sectors dropped), signatures (1,1,-1,-1), entries
+    N(0,1) from rand(normal) after random_seed(0) (A then B), every block then scaled by
+    10^u, u ~ U(-4, 0) drawn in block order from default_rng(1) (A's blocks, then B's).
+    tensordot(A, B, ((2,3),(0,1))) under fuse_to_matrix: fused sectors up to ~946, sector
+    GEMMs up to ~946 x 946 x 946. (Per-leg D=4096 over t=-16..16 would give ~1.1e13 nonzero
+    elements; D=128 per leg gives the stated ~900^3 sector GEMMs.)"""
+    cfg = yastn.make_config(sym='U1', backend='np', tensordot_policy='fuse_to_matrix')
+    bnp.random_seed(0)
+    ts0 = tuple(range(-16, 17))
+    Ds0 = leg_dims(ts0, lambda t: np.exp(-t * t / 50), 128)
+    ts, Ds = zip(*[(t, d) for t, d in zip(ts0, Ds0) if d > 0])
+    legs = [yastn.Leg(cfg, s=sg, t=ts, D=Ds) for sg in (1, 1, -1, -1)]
+    A = yastn.rand(cfg, legs=legs, distribution='normal')
+    B = yastn.rand(cfg, legs=legs, distribution='normal')
+    rng = np.random.default_rng(1)
+    scales = {}
+    for name, T in (('A', A), ('B', B)):
+        sc = 10.0 ** rng.uniform(-4, 0, size=len(T.struct.t))
+        for sl, f in zip(T.slices, sc):
+            T._data[sl.slcs[0][0]:sl.slcs[0][1]] *= f
+        scales[name] = [float(x) for x in sc]
+    rec = Recorder(bnp, big=5000)
+    C = yastn.tensordot(A, B, axes=((2, 3), (0, 1)))
+    rec.restore()
+    extra = {'leg_t': list(ts), 'leg_D': list(Ds), 'signatures': [1, 1, -1, -1], 'seed': 0, 'scale_seed': 1,
+             'A_size': int(A.size), 'B_size': int(B.size),
+             'A_slices': [list(x.slcs[0]) for x in A.slices], 'B_slices': [list(x.slcs[0]) for x in B.slices],
+             'A_scales': scales['A'], 'B_scales': scales['B'], 'C_checksum': checksum(C._data)}
+    save('cfg5', rec, extra)
+
+
 def _arr_from(rec, x):
     return rec.arrays[x['__array__']]
 
@@ -544,3 +577,4 @@ if __name__ == '__main__':
     scen_tds_adjoint()
     scen_cfg1()
     scen_cfg2()
+    scen_cfg5()

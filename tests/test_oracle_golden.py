@@ -145,6 +145,25 @@ def test_cfg1_fixture_consistent_with_regenerated_inputs():
     assert second.checksum['head0'] == [float(x) for x in B[:8]]
 
 
+def test_cfg5_replay_matches_reference_checksum():
+    """The precision-study workload (per-block scales over four decades) regenerates from
+    its seeds, and the oracle's tensordot reproduces the reference's result checksum."""
+    from yastn_gb300.workloads import cfg5_inputs
+    tr = load_trace('cfg5')
+    A, B = cfg5_inputs(tr)
+    c0, c1, c2, c3 = tr['calls']
+    assert c0['args'][0].checksum['head0'] == [float(x) for x in A[:8]]
+    assert abs(c1['args'][0].checksum['sum0'] - float(B.sum())) <= 1e-9 * c1['args'][0].checksum['abs0']
+    Am = oracle.transpose_and_merge(A, *c0['args'][1:])
+    Bm = oracle.transpose_and_merge(B, *c1['args'][1:])
+    Cm = oracle.dot(Am, Bm, *c2['args'][2:])
+    C = oracle.unmerge(Cm, c3['args'][1])
+    chk = tr['C_checksum']
+    assert C.size == chk['n']
+    assert abs(float(C.sum()) - chk['sum0']) <= 1e-10 * chk['abs0']
+    assert abs(float((C * C).sum()) - chk['sq0']) <= 1e-10 * chk['sq0']
+
+
 def test_oracle_tds_adjoint_matches_reference_autograd():
     import numpy as np
     from yastn_gb300.workloads import GOLDEN

@@ -14,7 +14,8 @@
 // <= 2^14 (<= 2^13 unless both digits are leading ones); all pairs of one diagonal
 // t = t_a + t_b share one FP32 accumulator over a K-chunk of 400, so every partial sum is
 // an integer below 2^24 and is exact in FP32. After each chunk the diagonals are folded
-// into FP64 accumulators (smallest first); the final scale is applied with scalbn.
+// exactly into two int64 halves, which are added to FP64 accumulators; the final scale
+// is an exponent-field add.
 //
 // GEMM kernel: 64x64 output tile per CTA, 8 warps each owning a 32x16 sub-tile (2x2
 // mma.sync.m16n8k16 tiles), K-step 16 staged in shared memory with cp.async (double
@@ -115,6 +116,29 @@ __global__ void split_rows_kernel(const double* __restrict__ src, __nv_bfloat16*
 }
 
 // ------------------------------------------------------------------ GEMM
+// Exact conversions built on the integer pipe (GB300 issues FP64 arithmetic at a small
+// fraction of its integer rate): v 2^E for an integer |v| < 2^53 is assembled from the
+// leading-bit position, the mantissa bits and the biased exponent; results outside the
+// normal range go through scalbn.
+__device__ __forceinline__ double int_to_double_scaled(long long v, int E) {
+  if (v == 0) return 0.0;
+  const unsigned long long sgn = v < 0 ? 0x8000000000000000ull : 0ull;
+  const unsigned long long mag = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  const int p = 63 - __clzll((long long)mag);  // leading bit; p <= 52 keeps every bit
+  const int be = 1023 + p + E;
+  const unsigned long long frac = (mag << (52 - p)) & 0xfffffffffffffull;
+  if (be >= 1 && be <= 2046) return __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) | frac));
+  return scalbn(__longlong_as_double((long long)(sgn | (1023ull + (unsigned long long)p) << 52 | frac)) , E);
+}
+
+// x 2^E by an exponent-field add when x and the result are normal doubles.
+__device__ __forceinline__ double scale_pow2(double x, int E) {
+  const long long b = __double_as_longlong(x);
+  const int be = (int)((b >> 52) & 0x7ff);
+  if (be == 0 || be == 0x7ff || be + E < 1 || be + E > 2046) return scalbn(x, E);
+  return __longlong_as_double(b + ((long long)E << 52));
+}
+
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
   const unsigned saddr = (unsigned)__cvta_generic_to_shared(smem);
   const int n = valid ? 16 : 0;
@@ -243,7 +267,7 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm_kernel(const __nv_bflo
               else lo += q << (7 * (S - 1 - d));
               acc[d][i][j][v] = 0.f;
             }
-            acc64[i][j][v] += fma((double)lo, 1.0 / (double)(1ll << (7 * (S - 1))), (double)hi * 0x1p-21);
+            acc64[i][j][v] += int_to_double_scaled(hi, -21) + int_to_double_scaled(lo, -7 * (S - 1));
           }
     }
   }
@@ -256,7 +280,7 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm_kernel(const __nv_bflo
       for (int v = 0; v < 4; ++v) {
         const int64_t gi = row0 + wm * 32 + i * 16 + (lane >> 2) + (v >= 2 ? 8 : 0);
         const int64_t gj = col0 + wn * 16 + j * 8 + (lane & 3) * 2 + (v & 1);
-        if (gi < m && gj < n) C[c_off + gi * ldc + gj] = scalbn(acc64[i][j][v], Ae[a_ex + gi] + Be[b_ex + gj] - 14);
+        if (gi < m && gj < n) C[c_off + gi * ldc + gj] = scale_pow2(acc64[i][j][v], Ae[a_ex + gi] + Be[b_ex + gj] - 14);
       }
 }
 

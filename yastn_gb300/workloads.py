@@ -75,6 +75,22 @@ def cfg1_inputs(trace=None):
     return A, B
 
 
+def cfg5_inputs(trace=None):
+    """Data of the precision-study tensors (U(1), D=128 per leg over t=-16..16).
+
+    Normal draws as ``cfg1_inputs`` (A then B from ``default_rng(seed)``), then every block
+    multiplied by its recorded scale 10^u, u ~ U(-4, 0) (block order, A's blocks first).
+    """
+    trace = trace or load_trace('cfg5')
+    rng = np.random.default_rng(trace['seed'])
+    A = rng.normal(size=trace['A_size'])
+    B = rng.normal(size=trace['B_size'])
+    for X, sls, scs in ((A, trace['A_slices'], trace['A_scales']), (B, trace['B_slices'], trace['B_scales'])):
+        for (lo, hi), f in zip(sls, scs):
+            X[lo:hi] *= f
+    return A, B
+
+
 def meta_mask(struct_t, struct_D, slices, mask_D, axis, nsym=1):
     """Metadata of ``apply_mask`` for a non-diagonal tensor.
 
