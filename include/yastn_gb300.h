@@ -183,42 +183,45 @@ int yb_ozaki_dot_static(const double* A, const double* B, double* C,
  *   bits, converged flag, sweeps run in the current phase, largest |cos| of the last
  *   completed sweep), then the control
  *   words of the grid barrier (count, generation, error flag, all-converged flag).
- * Sequence (mixed precision): yb_svd_init (X32 = scale_b (A or A^T), W32 = I, with
+ * dtype: YB_F64 (workspaces float / double) or YB_C128 (complex64 / complex128, element
+ *   offsets as above); tall complex blocks start from X_0 = A^H.
+ * Sequence (mixed precision): yb_svd_init (X32 = scale_b (A or A^H), W32 = I, with
  * scale[b] a power of two that brings the block below 1 in magnitude; scale: double
- * [n_blocks] scratch); yb_svd_sweeps with precision 32 (or yb_svd_block_sweeps); yb_svd_widen (W = double(W32)); the host orthonormalises W (Newton-Schulz
- * with the grouped GEMM) and forms X = W X_0 (for eigh: yb_svd_shift_prefill, then
+ * [n_blocks] scratch); yb_svd_sweeps with precision 32 (or yb_svd_block_sweeps);
+ * yb_svd_widen (W = widen(W32)); the host orthonormalises W (Newton-Schulz with the
+ * grouped GEMM, T = W^H W) and forms X = W X_0 (for eigh: yb_svd_shift_prefill, then
  * X += W A); yb_svd_sweeps with precision 64; yb_svd_finalize. yb_svd_sweeps runs every
  * sweep of a phase in one cooperative launch (rounds separated by a grid barrier with a
  * bounded spin; on timeout the error control word is set and the kernel exits) and stops
  * after the first sweep in which each block's largest rotation |cos| was <= tol_stop, or
  * after max_sweeps (the host reads the state and maps non-convergence to an error).
  * shift != NULL (eigh): per-block shifts c_b = ||A_b||_F + 1 are computed and A_b + c_b I
- * is decomposed (positive definite, so its SVD is its eigendecomposition); finalize mode 1
- * writes eigenvalues ascending, mode 2 by descending magnitude, with eigenvectors as
- * columns of U; mode 0 is the SVD (S descending, zero singular values completed to
- * orthonormal vectors).
+ * is decomposed (Hermitian positive definite, so its SVD is its eigendecomposition);
+ * finalize mode 1 writes eigenvalues ascending, mode 2 by descending magnitude, with
+ * eigenvectors as columns of U (= W^H); mode 0 is the SVD (S descending, zero singular
+ * values completed to orthonormal vectors).
  * Replaces svd (backend_torch.py:318-319, torch_svd_gesdd.py:15-21) and eigh
- * (backend_torch.py:369-384, torch_eig_sym.py:14-32) for FP64 blocks.
+ * (backend_torch.py:369-384, torch_eig_sym.py:14-32) for FP64 and complex128 blocks.
  */
 #define YB_SVD_REC 16
 int yb_svd_init(const void* a, void* work32, const int64_t* blocks, int n_blocks, int dtype,
                 int64_t* state, double* shift, double* scale, void* stream);
 int yb_svd_sweeps(void* work, const int64_t* blocks, int n_blocks, const int32_t* pair_items,
-                  int n_pair_items, int max_rounds, int precision, int max_sweeps, double tol_stop,
-                  int64_t* state, void* stream);
+                  int n_pair_items, int max_rounds, int precision, int dtype, int max_sweeps,
+                  double tol_stop, int64_t* state, void* stream);
 /* yb_svd_block_sweeps: the FP32 phase with rows grouped into super-vectors of
  * rows_per_super (16, 8 or 4) rows: one CTA per pair of super-vectors holds their rows in
- * shared memory (2 * rows_per_super * lmax floats, lmax >= every L), runs up to
+ * shared memory (2 * rows_per_super * lmax FP32 elements, lmax >= every L), runs up to
  * inner_sweeps Jacobi sweeps among them and applies the accumulated rotation to the W rows.
  * super_items: int32 pairs (block, super pair index 0..[15]/2-1); max_rounds = max([15]) - 1.
  * Returns YB_ERR_TOO_LARGE if the rows do not fit in shared memory. */
 int yb_svd_block_sweeps(void* work32, const int64_t* blocks, int n_blocks, const int32_t* super_items,
-                        int n_items, int max_rounds, int rows_per_super, int max_sweeps, int inner_sweeps,
-                        double tol_stop, int lmax, int64_t* state, void* stream);
-int yb_svd_widen(const void* work32, void* work64, const int64_t* blocks, int n_blocks,
+                        int n_items, int max_rounds, int rows_per_super, int dtype, int max_sweeps,
+                        int inner_sweeps, double tol_stop, int lmax, int64_t* state, void* stream);
+int yb_svd_widen(const void* work32, void* work64, const int64_t* blocks, int n_blocks, int dtype,
                  int64_t* state, void* stream);
-int yb_svd_shift_prefill(void* work64, const int64_t* blocks, int n_blocks, const double* shift,
-                         void* stream);
+int yb_svd_shift_prefill(void* work64, const int64_t* blocks, int n_blocks, int dtype,
+                         const double* shift, void* stream);
 int yb_svd_finalize(const void* work, void* U, double* S, void* Vh, const int64_t* blocks,
                     int n_blocks, int dtype, int max_k, int mode, const double* shift, void* stream);
 

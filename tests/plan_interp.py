@@ -138,7 +138,7 @@ def svd_adjoint_core(plan, Pm, Qm, S, gS, gU, gV, dtype):
 def jacobi_sweeps(X, W, blocks, dtype, tol_stop, max_sweeps):
     """The round-robin one-sided Jacobi of csrc/yb_svd.cu (svd_sweeps_kernel), restated
     sequentially with numpy on the plan's workspace layout. Returns (sweeps, converged)."""
-    eps = 2.0 ** -24 if dtype == np.float32 else 2.0 ** -53
+    eps = 2.0 ** -24 if dtype in (np.float32, np.complex64) else 2.0 ** -53
     return _sweeps(X, W, blocks, dtype, tol_stop, max_sweeps, eps)
 
 
@@ -222,13 +222,29 @@ def _sweeps(X, W, blocks, dtype, tol_stop, max_sweeps, eps):
             for b, r in enumerate(blocks):
                 if conv[b]: continue
                 k, L, N = int(r[9]), int(r[10]), int(r[11])
-                xo, wo = (int(r[13]), int(r[14])) if dtype == np.float32 else (int(r[6]), int(r[7]))
+                xo, wo = (int(r[13]), int(r[14])) if dtype in (np.float32, np.complex64) else (int(r[6]), int(r[7]))
                 if rd >= N - 1: continue
                 for pi in range(N // 2):
                     p, q = (N - 1, rd) if pi == 0 else ((rd + pi) % (N - 1), (rd - pi + N - 1) % (N - 1))
                     if p >= k or q >= k: continue
                     p, q = min(p, q), max(p, q)
                     xp = X[xo + p*L: xo + (p+1)*L]; xq = X[xo + q*L: xo + (q+1)*L]
+                    wp = W[wo + p*k: wo+(p+1)*k]; wq = W[wo+q*k: wo+(q+1)*k]
+                    if np.iscomplexobj(X):
+                        # complex rows: align the phase of x_q (ph = ga/|ga|), then a real rotation
+                        x64p, x64q = xp.astype(np.complex128), xq.astype(np.complex128)
+                        al = float(np.vdot(x64p, x64p).real); be = float(np.vdot(x64q, x64q).real)
+                        gac = complex(np.sum(x64p * np.conj(x64q)))
+                        if not (al > 0 and be > 0): continue
+                        g = abs(gac); c_ = g/np.sqrt(al)/np.sqrt(be); maxcos[b] = max(maxcos[b], c_)
+                        if not c_ > np.sqrt(L)*eps: continue
+                        ph = gac / g
+                        zeta = (be - al)/(2*g); t = np.copysign(1.0, zeta)/(abs(zeta) + np.hypot(1.0, zeta)); cd = 1/np.sqrt(1+t*t)
+                        c, s = cd, cd*t
+                        for Pp, Pq in ((xp, xq), (wp, wq)):
+                            u, v = Pp.copy(), ph * Pq
+                            Pp[:] = c*u - s*v; Pq[:] = s*u + c*v
+                        continue
                     al = float(np.dot(xp.astype(np.float64), xp)); be = float(np.dot(xq.astype(np.float64), xq)); ga = float(np.dot(xp.astype(np.float64), xq))
                     if not (al > 0 and be > 0): continue
                     c_ = abs(ga)/np.sqrt(al)/np.sqrt(be); maxcos[b] = max(maxcos[b], c_)
@@ -236,7 +252,6 @@ def _sweeps(X, W, blocks, dtype, tol_stop, max_sweeps, eps):
                     zeta = (be - al)/(2*ga); t = np.copysign(1.0, zeta)/(abs(zeta) + np.hypot(1.0, zeta)); cd = 1/np.sqrt(1+t*t)
                     c, s = dtype(cd), dtype(cd*t)
                     u, v = xp.copy(), xq.copy(); xp[:] = c*u - s*v; xq[:] = s*u + c*v
-                    wp = W[wo + p*k: wo+(p+1)*k]; wq = W[wo+q*k: wo+(q+1)*k]
                     u, v = wp.copy(), wq.copy(); wp[:] = c*u - s*v; wq[:] = s*u + c*v
         for b in range(nb):
             if not conv[b]:

@@ -38,7 +38,12 @@ def test_invalid_arguments_are_rejected_on_host(lib):
     assert lib.yb_block_copy(null, null, 8, null, 1, null, 1, null) == N.YB_ERR_INVALID
     assert lib.yb_block_copy(null, null, 8, null, 0, null, 0, null) == N.YB_OK  # nothing to do
     assert lib.yb_grouped_gemm(null, null, null, 0, null, null, null, 3, 1.0, 0.0, null) == N.YB_ERR_INVALID
-    assert lib.yb_svd_init(null, null, null, 2, 1, null, null, null, null) == N.YB_ERR_INVALID  # complex not yet
+    assert lib.yb_svd_init(null, null, null, 2, 7, null, null, null, null) == N.YB_ERR_INVALID  # unknown dtype
+    assert lib.yb_svd_init(null, null, null, 2, N.YB_C128, null, null, null, null) == N.YB_ERR_INVALID  # null data
+    assert lib.yb_svd_sweeps(null, null, 1, null, 1, 1, 32, 7, 1, 0.0, null, null) == N.YB_ERR_INVALID
+    assert lib.yb_svd_widen(null, null, null, 1, N.YB_F64, null, null) == N.YB_ERR_INVALID
+    assert lib.yb_svd_block_sweeps(null, null, 1, null, 1, 1, 16, N.YB_F64, 1, 1, 0.0, 0, null, null) == \
+        N.YB_ERR_INVALID
     assert lib.yb_svd_finalize(null, null, null, null, null, 1, 0, 10000, 0, null, null) == N.YB_ERR_TOO_LARGE
     assert lib.yb_svd_finalize(null, null, null, null, null, 1, 0, 10, 1, null, null) == N.YB_ERR_INVALID
     assert lib.yb_truncation_mask(null, 20000, null, null, 1, 0.0, -1, 0, null, null, null) == N.YB_ERR_TOO_LARGE

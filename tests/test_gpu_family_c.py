@@ -59,11 +59,6 @@ def test_svd_on_reference_calls(name, cuda_device):
         if c['fn'] != 'svd':
             continue
         data, meta, sizes = c['args'][:3]
-        if np.iscomplexobj(data):
-            with pytest.raises(NotImplementedError):
-                ops.svd(dev(data), meta, sizes)
-            n += 1
-            continue
         U, S, V = (host(x) for x in ops.svd(dev(data), meta, sizes))
         check_svd(data, meta, U, S, V, c['out'][1])
         n += 1
@@ -138,6 +133,50 @@ def test_svd_fp32_phase_variants(blocked, rows, cuda_device):
     check_svd(data, meta, U, S, V, Sr)
 
 
+@pytest.mark.parametrize('blocked,rows', [(False, None), (True, 8), (True, 16)])
+def test_complex_svd_and_eigh(blocked, rows, cuda_device):
+    """complex128 blocks (wide, tall, square, rank-deficient, graded): LAPACK's singular
+    values, U S Vh = A, unitary factors; Hermitian eigh with the same kernels."""
+    rng = np.random.default_rng(13)
+    shapes = [(120, 70), (33, 150), (40, 40), (6, 2), (1, 5)]
+    blocks = [rng.normal(size=sh) + 1j * rng.normal(size=sh) for sh in shapes]
+    q1, _ = np.linalg.qr(rng.normal(size=(50, 50)) + 1j * rng.normal(size=(50, 50)))
+    q2, _ = np.linalg.qr(rng.normal(size=(50, 50)) + 1j * rng.normal(size=(50, 50)))
+    blocks.append((q1 * np.logspace(0, -11, 50)) @ q2)                          # graded
+    blocks.append(np.outer(rng.normal(size=7) + 1j, rng.normal(size=9) - 2j))   # rank one
+    meta, off, oU, oS, oV, parts = [], 0, 0, 0, 0, []
+    for a in blocks:
+        m, n = a.shape
+        k = min(m, n)
+        meta.append(((off, off + m * n), (m, n), (oU, oU + m * k), (m, k), (oS, oS + k), (oV, oV + k * n), (k, n)))
+        off += m * n; oU += m * k; oS += k; oV += k * n
+        parts.append(a.ravel())
+    meta = tuple(meta)
+    data = np.concatenate(parts)
+    saved = ops.BLOCKED_FP32[0], ops.ROWS_PER_SUPER[0]
+    ops.BLOCKED_FP32[0], ops.ROWS_PER_SUPER[0] = blocked, rows
+    try:
+        U, S, V = (host(x) for x in ops.svd(dev(data), meta, (oU, oS, oV)))
+        # Hermitian eigh on H = B + B^H of the square blocks
+        hs = [a + a.conj().T for a in blocks if a.shape[0] == a.shape[1]]
+        hmeta, ho, hu, hsz = [], 0, 0, 0
+        for h in hs:
+            d = h.shape[0]
+            hmeta.append(((ho, ho + d * d), (d, d), (hu, hu + d * d), (d, d), (hsz, hsz + d)))
+            ho += d * d; hu += d * d; hsz += d
+        hdata = np.concatenate([h.ravel() for h in hs])
+        E, Q = (host(x) for x in ops.eigh(dev(hdata), tuple(hmeta), (hsz, hu)))
+    finally:
+        ops.BLOCKED_FP32[0], ops.ROWS_PER_SUPER[0] = saved
+    _, Sr, _ = oracle.svd(data, meta, (oU, oS, oV))
+    assert np.abs(S - Sr).max() <= TOL * max(1.0, np.abs(Sr).max())
+    check_svd(data, meta, U, S, V, Sr)
+    for h, (sl, D, slU, DU, slS) in zip(hs, hmeta):
+        e, q = E[slS[0]:slS[1]], Q[slU[0]:slU[1]].reshape(DU)
+        assert np.abs(e - np.linalg.eigvalsh(h)).max() <= TOL * np.abs(h).max() * D[0]
+        assert np.abs((q * e) @ q.conj().T - h).max() <= TOL * np.abs(h).max() * D[0]
+
+
 def test_svd_empty(cuda_device):
     U, S, V = ops.svd(torch.zeros(0, dtype=torch.float64, device='cuda'), (), (0, 0, 0))
     assert U.numel() == S.numel() == V.numel() == 0
@@ -148,8 +187,6 @@ def test_eigh_on_reference_calls(cuda_device):
     n = 0
     for c in tr['calls']:
         data, meta, sizes = c['args']
-        if np.iscomplexobj(data):
-            continue
         S, U = (host(x) for x in ops.eigh(dev(data), meta, sizes))
         assert rel(S, c['out'][0]) <= TOL
         for sl, D, slU, DU, slS in meta:
@@ -157,8 +194,8 @@ def test_eigh_on_reference_calls(cuda_device):
             u = U[slU[0]:slU[1]].reshape(DU)
             s = S[slS[0]:slS[1]]
             assert np.all(np.diff(s) >= 0)
-            assert np.abs((u * s) @ u.T - a).max() <= TOL * max(1, np.abs(a).max()) * D[0]
-            assert np.abs(u.T @ u - np.eye(D[0])).max() <= TOL * max(10, D[0])
+            assert np.abs((u * s) @ u.conj().T - a).max() <= TOL * max(1, np.abs(a).max()) * D[0]
+            assert np.abs(u.conj().T @ u - np.eye(DU[1])).max() <= TOL * max(10, DU[1])
         n += 1
     assert n > 0
 

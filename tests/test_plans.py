@@ -245,6 +245,58 @@ def test_mixed_precision_jacobi_schedule_on_plan_layout(rows_per_super):
         assert np.abs(s - sr).max() <= 1e-13 * max(sr.max(), 1.0)
 
 
+def test_mixed_precision_jacobi_schedule_complex():
+    """Complex blocks: FP32 phase on complex64 rows with phase-aligned rotations, widen,
+    Newton-Schulz with T = W^H W, X = W X_0 (X_0 = A^H for tall blocks), FP64 phase; the
+    finalize rules (wide: U = W^H, Vh rows = x_i / s_i; tall: U columns = conj(x_i) / s_i,
+    Vh = W) reproduce LAPACK's singular values and A."""
+    rng = np.random.default_rng(3)
+    shapes = [(20, 20), (31, 12), (9, 26), (1, 4)]
+    meta, off, oU, oS, oV = [], 0, 0, 0, 0
+    for m, n in shapes:
+        k = min(m, n)
+        meta.append(((off, off + m * n), (m, n), (oU, oU + m * k), (m, k), (oS, oS + k), (oV, oV + k * n), (k, n)))
+        off += m * n; oU += m * k; oS += k; oV += k * n
+    meta = tuple(meta)
+    data = rng.normal(size=off) + 1j * rng.normal(size=off)
+    plan = P.svd_plan(meta, None, True)
+    w32 = np.zeros(plan.n32, np.complex64)
+    w64 = np.zeros(plan.n64, np.complex128)
+    for r in plan.blocks:
+        a, m, n, k, L = int(r[0]), int(r[1]), int(r[2]), int(r[9]), int(r[10])
+        A = data[a:a + m * n].reshape(m, n)
+        X0 = A.conj().T if m > n else A
+        w32[int(r[13]):int(r[13]) + k * L] = X0.ravel().astype(np.complex64)
+        w32[int(r[14]):int(r[14]) + k * k] = np.eye(k, dtype=np.complex64).ravel()
+    nsw, conv = PI.jacobi_sweeps(w32, w32, plan.blocks, np.complex64, 1e-4, 40)
+    assert all(conv)
+    for r in plan.blocks:
+        k = int(r[9])
+        w64[int(r[7]):int(r[7]) + k * k] = w32[int(r[14]):int(r[14]) + k * k]
+    w0, t0, n0, ws = plan.w_range
+    for _ in range(2):
+        w64[n0:n0 + ws] = w64[w0:w0 + ws]
+        PI.run_gemm(plan.gram, w64, w64, w64)
+        PI.run_gemm(plan.ns, w64, w64, w64, alpha=-0.5, beta=1.5)
+        w64[w0:w0 + ws] = w64[n0:n0 + ws]
+    PI.run_gemm(plan.xform, w64, data, w64)
+    nsw, conv = PI.jacobi_sweeps(w64, w64, plan.blocks, np.complex128, 1e-8, 20)
+    assert all(conv)
+    _, Sr, _ = oracle.svd(data, meta, (oU, oS, oV))
+    for r, mt in zip(plan.blocks, meta):
+        a, m, n, k, L = int(r[0]), int(r[1]), int(r[2]), int(r[9]), int(r[10])
+        X = w64[int(r[6]):int(r[6]) + k * L].reshape(k, L)
+        Wb = w64[int(r[7]):int(r[7]) + k * k].reshape(k, k)
+        s = np.linalg.norm(X, axis=1)
+        if m > n:
+            U, Vh = (X.conj() / s[:, None]).T, Wb
+        else:
+            U, Vh = Wb.conj().T, X / s[:, None]
+        A = data[a:a + m * n].reshape(m, n)
+        assert np.abs((U * s) @ Vh - A).max() <= 1e-13 * np.abs(A).max()
+        assert np.abs(np.sort(s)[::-1] - Sr[mt[4][0]:mt[4][1]]).max() <= 1e-13 * max(s.max(), 1.0)
+
+
 def _ozaki_digits(x, s):
     """NumPy restatement of the split of csrc/yb_ozaki.cu (rows of x): balanced base-128
     digits of Q = rint(x 2^{7s-e}) extracted from the low end with integer arithmetic."""

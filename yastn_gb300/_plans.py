@@ -480,19 +480,21 @@ class SvdPlan:
 SVD_SMEM_BYTES = 220 * 1024  # shared memory a blocked-Jacobi CTA may take (GB300: 227 KB per CTA)
 
 
-def svd_rows_per_super(lmax, choices=(16, 8, 4)):
+def svd_rows_per_super(lmax, choices=(16, 8, 4), elem_bytes=4):
     """Rows per super-vector of the blocked FP32 Jacobi: the largest choice whose CTA
-    (2 * rows * lmax + 4 * rows^2 floats of shared memory) fits; 0 if none does."""
+    (2 * rows * lmax + 4 * rows^2 elements of shared memory, 8-byte elements for complex64)
+    fits; 0 if none does."""
     for br in choices:
-        if (2 * br * lmax + 4 * br * br) * 4 <= SVD_SMEM_BYTES:
+        if (2 * br * lmax + 4 * br * br) * elem_bytes <= SVD_SMEM_BYTES:
             return br
     return 0
 
 
-def svd_plan(meta, rows_per_super=None):
+def svd_plan(meta, rows_per_super=None, cplx=False):
     """Jacobi plan for svd records (sl, D, slU, DU, slS, slV, DV) of yastn/tensor/linalg.py:323-380.
     ``rows_per_super`` fixes the super-vector height of the blocked FP32 phase (default: the
-    largest of 16, 8, 4 whose rows fit in shared memory)."""
+    largest of 16, 8, 4 whose rows fit in shared memory). ``cplx``: complex128 blocks (the
+    Gram product of Newton-Schulz is W^H W and tall blocks start from X_0 = A^H)."""
     def build():
         sel = []
         for sl, D, slU, DU, slS, slV, DV in meta:
@@ -517,10 +519,10 @@ def svd_plan(meta, rows_per_super=None):
             recs.append(rec)
             pairs.extend((bi, p) for p in range(N // 2))
             # T = W^T W ; Wn = 1.5 Wn - 0.5 W T (Wn holds a copy of W) ; X = W X_0
-            gram.append((t0 + ow, k, k, k, [(w0 + ow, w0 + ow, k, 1, k, k, 1, 0)]))
+            gram.append((t0 + ow, k, k, k, [(w0 + ow, w0 + ow, k, 1, k, k, 1, int(cplx))]))
             ns.append((n0 + ow, k, k, k, [(w0 + ow, t0 + ow, k, k, 1, k, 1, 0)]))
             if m > n:
-                xf.append((ox, k, L, L, [(w0 + ow, sl[0], k, k, 1, 1, n, 0)]))
+                xf.append((ox, k, L, L, [(w0 + ow, sl[0], k, k, 1, 1, n, 2 * int(cplx))]))
             else:
                 xf.append((ox, k, L, L, [(w0 + ow, sl[0], k, k, 1, n, 1, 0)]))
             ox += k * L
@@ -530,7 +532,7 @@ def svd_plan(meta, rows_per_super=None):
             max_k = max(max_k, k)
             fl += 14 * L * k * k + 8 * k ** 3  # nominal Golub-Reinsch count
         lmax = max((L for *_, k, L in sel), default=0)
-        br = svd_rows_per_super(lmax) if rows_per_super is None else rows_per_super
+        br = svd_rows_per_super(lmax, elem_bytes=8 if cplx else 4) if rows_per_super is None else rows_per_super
         supers, super_rounds = [], 0
         for bi, (*_, k, L) in enumerate(sel):
             if br:
@@ -544,7 +546,7 @@ def svd_plan(meta, rows_per_super=None):
         return SvdPlan(blocks, items, max_rounds, max_k, fl, xs + 3 * ws, xs + ws, (w0, t0, n0, ws),
                        _pack_gemm(gram), _pack_gemm(ns), _pack_gemm(xf),
                        br, np.array(supers, dtype=np.int32).reshape(-1, 2), super_rounds, lmax)
-    return CACHE.get((meta,), ('svd', rows_per_super), build)
+    return CACHE.get((meta,), ('svd', rows_per_super, cplx), build)
 
 
 class SvdAdjointPlan:

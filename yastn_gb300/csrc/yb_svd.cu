@@ -1,25 +1,29 @@
-// Family (c): batched one-sided (Hestenes) Jacobi SVD / symmetric eigendecomposition of
-// all charge-sector blocks, mixed precision.
+// Family (c): batched one-sided (Hestenes) Jacobi SVD / Hermitian eigendecomposition of
+// all charge-sector blocks, mixed precision, real (FP64) or complex (complex128) data.
 //
 // Each block A (m x n, row-major) is handled in its "wide" orientation: the k=min(m,n)
-// vectors to orthogonalise are the rows of A (m <= n) or of A^T (m > n), each of length
+// vectors to orthogonalise are the rows of A (m <= n) or of A^H (m > n), each of length
 // L=max(m,n), held in a workspace X; rotations are accumulated in W (k x k), so that
 // X = W X_0 at every step. A parallel round-robin ordering (circle method over
 // N = k rounded up to even) pairs all vectors in N-1 rounds of N/2 disjoint pairs; one
 // warp rotates one pair and all blocks advance together.
 //
 // GB300 has ~60x more FP32 than FP64 throughput, so the sweeps run in two phases:
-//   1. FP32 sweeps on (X32, W32) until no rotation is needed at FP32 precision;
-//   2. the host orthonormalises W = double(W32) with Newton-Schulz steps and forms
+//   1. FP32 sweeps on (X32, W32) (float or complex64) until the rows are orthogonal to
+//      about 1e-4 (a blocked variant keeps super-vectors of rows in shared memory);
+//   2. the host orthonormalises W = widen(W32) with Newton-Schulz steps and forms
 //      X = W X_0 with the FP64 grouped GEMM; then FP64 sweeps polish (X, W) until a
-//      sweep whose largest |cos| was below tol_stop (typically 1-2 sweeps).
+//      sweep whose largest |cos| was below tol_stop (typically 2-3 sweeps).
 // One persistent cooperative launch runs all the sweeps of a phase; rounds are separated
 // by a grid barrier whose spin is bounded (an error flag is raised and the kernel exits
 // if it ever times out). Finally S = row norms (descending), the normalised rows give Vh
-// (wide) or U (tall), and W^T gives the other factor.
+// (wide) or U (tall, conjugated), and W^H gives the other factor.
 //
-// A rotation is applied when |x_p.x_q| > sqrt(L) eps ||x_p|| ||x_q|| (the threshold of
-// LAPACK's one-sided Jacobi); the angle follows Rutishauser's formula with hypot.
+// A rotation is applied when |<x_p, x_q>| > sqrt(L) eps ||x_p|| ||x_q|| (the threshold of
+// LAPACK's one-sided Jacobi); the angle follows Rutishauser's formula with hypot. For
+// complex rows the phase u = g/|g| of g = <x_p, x_q> = sum_l x_p[l] conj(x_q[l]) is first
+// moved onto x_q, which makes the pair's inner product real, and the real rotation of
+// (|x_p|^2, |x_q|^2, |g|) follows: x_p <- c x_p - s u x_q, x_q <- s x_p + c u x_q (unitary).
 #include <float.h>
 #include "yb_common.cuh"
 
@@ -50,6 +54,93 @@ struct Eps<double> {
   static constexpr double v = 1.1102230246251565e-16;  // 2^-53
 };
 
+// Numeric traits of the four working types: float, double, complex64 (float2) and
+// complex128 (double2). R is the real type; fmac(x, y, acc) = acc + x conj(y).
+template <typename T>
+struct Num;
+template <>
+struct Num<float> {
+  using R = float;
+  static constexpr bool cplx = false;
+  __device__ static float zero() { return 0.f; }
+  __device__ static float one() { return 1.f; }
+  __device__ static float abs2(float x) { return x * x; }
+  __device__ static float fmac(float x, float y, float acc) { return fmaf(x, y, acc); }
+  __device__ static float fma_(float a, float b, float acc) { return fmaf(a, b, acc); }
+  __device__ static float mul(float a, float b) { return a * b; }
+  __device__ static float scale(float s, float a) { return s * a; }
+  __device__ static float conj(float a) { return a; }
+  __device__ static float add(float a, float b) { return a + b; }
+  __device__ static float sub(float a, float b) { return a - b; }
+};
+template <>
+struct Num<double> {
+  using R = double;
+  static constexpr bool cplx = false;
+  __device__ static double zero() { return 0.0; }
+  __device__ static double one() { return 1.0; }
+  __device__ static double abs2(double x) { return x * x; }
+  __device__ static double fmac(double x, double y, double acc) { return fma(x, y, acc); }
+  __device__ static double fma_(double a, double b, double acc) { return fma(a, b, acc); }
+  __device__ static double mul(double a, double b) { return a * b; }
+  __device__ static double scale(double s, double a) { return s * a; }
+  __device__ static double conj(double a) { return a; }
+  __device__ static double add(double a, double b) { return a + b; }
+  __device__ static double sub(double a, double b) { return a - b; }
+};
+template <>
+struct Num<float2> {
+  using R = float;
+  static constexpr bool cplx = true;
+  __device__ static float2 zero() { return make_float2(0.f, 0.f); }
+  __device__ static float2 one() { return make_float2(1.f, 0.f); }
+  __device__ static float abs2(float2 x) { return fmaf(x.x, x.x, x.y * x.y); }
+  __device__ static float2 fmac(float2 x, float2 y, float2 acc) {
+    return make_float2(fmaf(x.x, y.x, fmaf(x.y, y.y, acc.x)), fmaf(x.y, y.x, fmaf(-x.x, y.y, acc.y)));
+  }
+  __device__ static float2 fma_(float2 a, float2 b, float2 acc) {
+    return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, acc.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, acc.y)));
+  }
+  __device__ static float2 mul(float2 a, float2 b) { return fma_(a, b, zero()); }
+  __device__ static float2 scale(float s, float2 a) { return make_float2(s * a.x, s * a.y); }
+  __device__ static float2 conj(float2 a) { return make_float2(a.x, -a.y); }
+  __device__ static float2 add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+  __device__ static float2 sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+};
+template <>
+struct Num<double2> {
+  using R = double;
+  static constexpr bool cplx = true;
+  __device__ static double2 zero() { return make_double2(0.0, 0.0); }
+  __device__ static double2 one() { return make_double2(1.0, 0.0); }
+  __device__ static double abs2(double2 x) { return fma(x.x, x.x, x.y * x.y); }
+  __device__ static double2 fmac(double2 x, double2 y, double2 acc) {
+    return make_double2(fma(x.x, y.x, fma(x.y, y.y, acc.x)), fma(x.y, y.x, fma(-x.x, y.y, acc.y)));
+  }
+  __device__ static double2 fma_(double2 a, double2 b, double2 acc) {
+    return make_double2(fma(a.x, b.x, fma(-a.y, b.y, acc.x)), fma(a.x, b.y, fma(a.y, b.x, acc.y)));
+  }
+  __device__ static double2 mul(double2 a, double2 b) { return fma_(a, b, zero()); }
+  __device__ static double2 scale(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+  __device__ static double2 conj(double2 a) { return make_double2(a.x, -a.y); }
+  __device__ static double2 add(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+  __device__ static double2 sub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+};
+
+// conversions between the storage types
+__device__ __forceinline__ float to32(double v) { return (float)v; }
+__device__ __forceinline__ float2 to32(double2 v) { return make_float2((float)v.x, (float)v.y); }
+__device__ __forceinline__ double to64(float v) { return (double)v; }
+__device__ __forceinline__ double2 to64(float2 v) { return make_double2((double)v.x, (double)v.y); }
+__device__ __forceinline__ double cabs2(double v) { return v * v; }
+__device__ __forceinline__ double cabs2(double2 v) { return fma(v.x, v.x, v.y * v.y); }
+__device__ __forceinline__ double cconj_(double v) { return v; }
+__device__ __forceinline__ double2 cconj_(double2 v) { return make_double2(v.x, -v.y); }
+__device__ __forceinline__ double add_real(double v, double c) { return v + c; }
+__device__ __forceinline__ double2 add_real(double2 v, double c) { return make_double2(v.x + c, v.y); }
+__device__ __forceinline__ double rscale(double v, double s) { return v * s; }
+__device__ __forceinline__ double2 rscale(double2 v, double s) { return make_double2(v.x * s, v.y * s); }
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -63,66 +154,116 @@ __device__ __forceinline__ float warp_sum(float v) {
 }
 
 // Jacobi rotation of a row pair from its warp-local partial sums al_ = |x_p|^2, be_ =
-// |x_q|^2, ga_ = x_p.x_q (Rutishauser's formulas): returns true (every lane) if the pair is
-// rotated, with (c, s). |cos| of the pair goes to the block's running maximum. GB300 runs
-// FP64 at 1/64 of the FP32 rate, so the FP32 phase keeps the whole computation in FP32,
-// and the FP64 phase does the scalar part on lane 0 only and broadcasts the result.
+// |x_q|^2, ga_ = <x_p, x_q> (Rutishauser's formulas): returns true (every lane) if the pair
+// is rotated, with (c, s) and the phase u (1 for real rows). |cos| of the pair goes to the
+// block's running maximum. GB300 runs FP64 at 1/64 of the FP32 rate, so the FP32 phase
+// keeps the whole computation in FP32, and the FP64 phase does the scalar part on lane 0
+// only and broadcasts the result.
 template <typename T>
-struct Rotation;
-
+__device__ __forceinline__ void warp_sum_t(T& v);
 template <>
-struct Rotation<float> {
-  __device__ static bool get(float al_, float be_, float ga_, int64_t L, int lane, int64_t* st, float& c, float& s) {
-    const float al = warp_sum(al_), be = warp_sum(be_), ga = warp_sum(ga_);
-    if (!(al > 0.f && be > 0.f)) return false;
-    const float cosv = fabsf(ga) / (sqrtf(al) * sqrtf(be));
-    if (lane == 0) atomicMax((unsigned long long*)(st + 0), (unsigned long long)__double_as_longlong((double)cosv));
-    if (!(cosv > sqrtf((float)L) * 5.9604645e-08f)) return false;
-    const float zeta = (be - al) / (2.f * ga);
-    const float t = copysignf(1.f, zeta) / (fabsf(zeta) + hypotf(1.f, zeta));
-    c = 1.f / sqrtf(fmaf(t, t, 1.f));
+__device__ __forceinline__ void warp_sum_t<float>(float& v) { v = warp_sum(v); }
+template <>
+__device__ __forceinline__ void warp_sum_t<double>(double& v) { v = warp_sum(v); }
+template <>
+__device__ __forceinline__ void warp_sum_t<float2>(float2& v) { v.x = warp_sum(v.x); v.y = warp_sum(v.y); }
+template <>
+__device__ __forceinline__ void warp_sum_t<double2>(double2& v) { v.x = warp_sum(v.x); v.y = warp_sum(v.y); }
+
+__device__ __forceinline__ float gabs(float g) { return fabsf(g); }
+__device__ __forceinline__ double gabs(double g) { return fabs(g); }
+__device__ __forceinline__ float gabs(float2 g) { return hypotf(g.x, g.y); }
+__device__ __forceinline__ double gabs(double2 g) { return hypot(g.x, g.y); }
+
+template <typename T>
+struct Rotation {
+  using R = typename Num<T>::R;
+  // scalar part: from the summed (al, be, g) to (c, s, u); |cos| to the running maximum
+  __device__ static bool scalar(R al, R be, T ga, int64_t L, int64_t* st, R& c, R& s, T& u) {
+    if (!(al > R(0) && be > R(0))) return false;
+    const R g = gabs(ga);
+    const R cosv = g / (sqrt(al) * sqrt(be));
+    atomicMax((unsigned long long*)st, (unsigned long long)__double_as_longlong((double)cosv));
+    if (!(cosv > sqrt((R)L) * (R)Eps<R>::v)) return false;
+    R zeta;
+    if constexpr (Num<T>::cplx) {
+      u.x = ga.x / g;
+      u.y = ga.y / g;
+      zeta = (be - al) / (R(2) * g);
+    } else {
+      u = R(1);
+      zeta = (be - al) / (R(2) * ga);
+    }
+    const R t = copysign(R(1), zeta) / (fabs(zeta) + hypot(R(1), zeta));
+    c = R(1) / sqrt(fma(t, t, R(1)));
     s = c * t;
     return true;
   }
-};
-
-template <>
-struct Rotation<double> {
-  __device__ static bool get(double al_, double be_, double ga_, int64_t L, int lane, int64_t* st, double& c,
-                             double& s) {
-    const double al = warp_sum(al_), be = warp_sum(be_), ga = warp_sum(ga_);
-    int rot = 0;
-    if (lane == 0 && al > 0.0 && be > 0.0) {
-      const double cosv = fabs(ga) / (sqrt(al) * sqrt(be));
-      atomicMax((unsigned long long*)(st + 0), (unsigned long long)__double_as_longlong(cosv));
-      if (cosv > sqrt((double)L) * 1.1102230246251565e-16) {
-        const double zeta = (be - al) / (2.0 * ga);
-        const double t = copysign(1.0, zeta) / (fabs(zeta) + hypot(1.0, zeta));
-        c = 1.0 / sqrt(fma(t, t, 1.0));
-        s = c * t;
-        rot = 1;
+  __device__ static bool get(R al_, R be_, T ga_, int64_t L, int lane, int64_t* st, R& c, R& s, T& u) {
+    const R al = warp_sum(al_), be = warp_sum(be_);
+    warp_sum_t<T>(ga_);
+    if constexpr (sizeof(R) == 4) {
+      // FP32: every lane computes the same (cheap) scalar part; one lane records |cos|
+      if (!(al > R(0) && be > R(0))) return false;
+      const R g = gabs(ga_);
+      const R cosv = g / (sqrtf(al) * sqrtf(be));
+      if (lane == 0) atomicMax((unsigned long long*)st, (unsigned long long)__double_as_longlong((double)cosv));
+      if (!(cosv > sqrtf((float)L) * 5.9604645e-08f)) return false;
+      R zeta;
+      if constexpr (Num<T>::cplx) {
+        u.x = ga_.x / g;
+        u.y = ga_.y / g;
+        zeta = (be - al) / (2.f * g);
+      } else {
+        u = 1.f;
+        zeta = (be - al) / (2.f * ga_);
       }
+      const R t = copysignf(1.f, zeta) / (fabsf(zeta) + hypotf(1.f, zeta));
+      c = 1.f / sqrtf(fmaf(t, t, 1.f));
+      s = c * t;
+      return true;
+    } else {
+      int rot = 0;
+      if (lane == 0) rot = scalar(al, be, ga_, L, st, c, s, u) ? 1 : 0;
+      rot = __shfl_sync(0xffffffffu, rot, 0);
+      if (!rot) return false;
+      c = __shfl_sync(0xffffffffu, c, 0);
+      s = __shfl_sync(0xffffffffu, s, 0);
+      if constexpr (Num<T>::cplx) {
+        u.x = __shfl_sync(0xffffffffu, u.x, 0);
+        u.y = __shfl_sync(0xffffffffu, u.y, 0);
+      } else {
+        u = 1.0;
+      }
+      return true;
     }
-    rot = __shfl_sync(0xffffffffu, rot, 0);
-    if (!rot) return false;
-    c = __shfl_sync(0xffffffffu, c, 0);
-    s = __shfl_sync(0xffffffffu, s, 0);
-    return true;
   }
 };
+
+// (a, b) <- (c a - s u b, s a + c u b)
+template <typename T>
+__device__ __forceinline__ void rot2(T& a, T& b, typename Num<T>::R c, typename Num<T>::R s, T u) {
+  T bu = b;
+  if constexpr (Num<T>::cplx) bu = Num<T>::mul(u, b);
+  const T na = Num<T>::sub(Num<T>::scale(c, a), Num<T>::scale(s, bu));
+  const T nb = Num<T>::add(Num<T>::scale(s, a), Num<T>::scale(c, bu));
+  a = na;
+  b = nb;
+}
 
 // Per-block Frobenius norm -> shift[b] (eigh: makes a symmetric block positive definite)
 // and scale[b], a power of two that brings the FP32 copy of the block (shift included)
 // below 1 in magnitude, so that FP32 squares and dot products neither overflow nor lose
 // the block to underflow. The rotations, and so W, do not depend on the scale.
-__global__ void block_fro_kernel(const double* __restrict__ A, const int64_t* __restrict__ blocks,
+template <typename TI>
+__global__ void block_fro_kernel(const TI* __restrict__ A, const int64_t* __restrict__ blocks,
                                  double* __restrict__ shift, double* __restrict__ scale) {
   __shared__ double red[32];
   const int64_t* r = blocks + (int64_t)blockIdx.x * YB_SVD_REC;
   const int64_t cnt = r[R_M] * r[R_N];
-  const double* a = A + r[R_A];
+  const TI* a = A + r[R_A];
   double acc = 0.0;
-  for (int64_t e = threadIdx.x; e < cnt; e += blockDim.x) acc = fma(a[e], a[e], acc);
+  for (int64_t e = threadIdx.x; e < cnt; e += blockDim.x) acc += cabs2(a[e]);
   acc = warp_sum(acc);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
   __syncthreads();
@@ -142,8 +283,9 @@ __global__ void block_fro_kernel(const double* __restrict__ A, const int64_t* __
   }
 }
 
-// X32 = float(A or A^T) (+ shift on the diagonal), W32 = I; resets the per-block state.
-__global__ void svd_init_kernel(const double* __restrict__ A, float* __restrict__ work32,
+// X32 = scale_b (A or A^H) (+ shift on the diagonal) in FP32, W32 = I; resets the state.
+template <typename TI, typename T32>
+__global__ void svd_init_kernel(const TI* __restrict__ A, T32* __restrict__ work32,
                                 const int64_t* __restrict__ blocks, int64_t* __restrict__ state,
                                 const double* __restrict__ shift, const double* __restrict__ scale) {
   const double sc = scale[blockIdx.y];
@@ -151,47 +293,49 @@ __global__ void svd_init_kernel(const double* __restrict__ A, float* __restrict_
   const int64_t m = r[R_M], n = r[R_N], k = r[R_K], L = r[R_L];
   const bool tall = m > n;
   const int64_t xs = k * L, ws = k * k;
-  float* X = work32 + r[R_X32];
-  float* W = work32 + r[R_W32];
-  const double* a = A + r[R_A];
+  T32* X = work32 + r[R_X32];
+  T32* W = work32 + r[R_W32];
+  const TI* a = A + r[R_A];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < xs + ws;
        e += (int64_t)gridDim.x * blockDim.x) {
     if (e < xs) {
       const int64_t i = e / L, l = e - i * L;
-      double v = tall ? a[l * n + i] : a[e];
-      if (shift != nullptr && i == l) v += shift[blockIdx.y];
-      X[e] = (float)(v * sc);
+      TI v = tall ? cconj_(a[l * n + i]) : a[e];
+      if (shift != nullptr && i == l) v = add_real(v, shift[blockIdx.y]);
+      X[e] = to32(rscale(v, sc));
     } else {
       const int64_t f = e - xs;
       const int64_t i = f / k, j = f - i * k;
-      W[f] = (i == j) ? 1.0f : 0.0f;
+      W[f] = (i == j) ? Num<T32>::one() : Num<T32>::zero();
     }
   }
   if (blockIdx.x == 0 && threadIdx.x < ST_REC) state[blockIdx.y * ST_REC + threadIdx.x] = 0;
 }
 
-// W64 = double(W32) (the host orthonormalises it next); resets the per-block state.
-__global__ void svd_widen_kernel(const float* __restrict__ work32, double* __restrict__ work64,
+// W64 = widen(W32) (the host orthonormalises it next); resets the per-block state.
+template <typename T32, typename T64>
+__global__ void svd_widen_kernel(const T32* __restrict__ work32, T64* __restrict__ work64,
                                  const int64_t* __restrict__ blocks, int64_t* __restrict__ state) {
   const int64_t* r = blocks + (int64_t)blockIdx.y * YB_SVD_REC;
   const int64_t k = r[R_K];
-  const float* W32 = work32 + r[R_W32];
-  double* W = work64 + r[R_W];
+  const T32* W32 = work32 + r[R_W32];
+  T64* W = work64 + r[R_W];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < k * k; e += (int64_t)gridDim.x * blockDim.x)
-    W[e] = (double)W32[e];
+    W[e] = to64(W32[e]);
   if (blockIdx.x == 0 && threadIdx.x < ST_REC) state[blockIdx.y * ST_REC + threadIdx.x] = 0;
 }
 
 // X = shift_b * W (eigh: the FP64 phase then adds W A with the grouped GEMM, X = W (A + shift I)).
-__global__ void svd_shift_prefill_kernel(double* __restrict__ work64, const int64_t* __restrict__ blocks,
+template <typename T64>
+__global__ void svd_shift_prefill_kernel(T64* __restrict__ work64, const int64_t* __restrict__ blocks,
                                          const double* __restrict__ shift) {
   const int64_t* r = blocks + (int64_t)blockIdx.y * YB_SVD_REC;
   const int64_t k = r[R_K];
   const double c = shift[blockIdx.y];
-  const double* W = work64 + r[R_W];
-  double* X = work64 + r[R_X];
+  const T64* W = work64 + r[R_W];
+  T64* X = work64 + r[R_X];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < k * k; e += (int64_t)gridDim.x * blockDim.x)
-    X[e] = c * W[e];
+    X[e] = rscale(W[e], c);
 }
 
 // Grid barrier for a cooperative launch (all CTAs co-resident). The spin is bounded: on
@@ -233,21 +377,23 @@ constexpr int kChunk = 8;  // elements per lane per row kept in flight
 // latency is paid once per chunk rather than once per element. Rows are rewritten by
 // other SMs between rounds, so loads bypass L1 (ld.global.cg).
 template <typename T>
-__device__ __forceinline__ void rotate_rows(T* __restrict__ a, T* __restrict__ b, int64_t len, int lane, T c, T s) {
+__device__ __forceinline__ void rotate_rows(T* __restrict__ a, T* __restrict__ b, int64_t len, int lane,
+                                            typename Num<T>::R c, typename Num<T>::R s, T u) {
   for (int64_t base = 0; base < len; base += 32 * kChunk) {
-    T u[kChunk], v[kChunk];
+    T x[kChunk], y[kChunk];
 #pragma unroll
     for (int j = 0; j < kChunk; ++j) {
       const int64_t i = base + j * 32 + lane;
-      u[j] = (i < len) ? __ldcg(a + i) : T(0);
-      v[j] = (i < len) ? __ldcg(b + i) : T(0);
+      x[j] = (i < len) ? __ldcg(a + i) : Num<T>::zero();
+      y[j] = (i < len) ? __ldcg(b + i) : Num<T>::zero();
     }
 #pragma unroll
     for (int j = 0; j < kChunk; ++j) {
       const int64_t i = base + j * 32 + lane;
       if (i < len) {
-        a[i] = c * u[j] - s * v[j];
-        b[i] = s * u[j] + c * v[j];
+        rot2<T>(x[j], y[j], c, s, u);
+        a[i] = x[j];
+        b[i] = y[j];
       }
     }
   }
@@ -256,29 +402,32 @@ __device__ __forceinline__ void rotate_rows(T* __restrict__ a, T* __restrict__ b
 template <typename T>
 __device__ __forceinline__ void rotate_pair(T* __restrict__ X, T* __restrict__ W, int64_t k, int64_t L, int64_t p,
                                             int64_t q, int lane, int64_t* st) {
+  using R = typename Num<T>::R;
   T* xp = X + p * L;
   T* xq = X + q * L;
   // partial sums in the working precision (FP32 in the FP32 phase keeps the FP64 pipe free)
-  T al_ = 0, be_ = 0, ga_ = 0;
+  R al_ = 0, be_ = 0;
+  T ga_ = Num<T>::zero();
   for (int64_t base = 0; base < L; base += 32 * kChunk) {
-    T u[kChunk], v[kChunk];
+    T x[kChunk], y[kChunk];
 #pragma unroll
     for (int j = 0; j < kChunk; ++j) {
       const int64_t i = base + j * 32 + lane;
-      u[j] = (i < L) ? __ldcg(xp + i) : T(0);
-      v[j] = (i < L) ? __ldcg(xq + i) : T(0);
+      x[j] = (i < L) ? __ldcg(xp + i) : Num<T>::zero();
+      y[j] = (i < L) ? __ldcg(xq + i) : Num<T>::zero();
     }
 #pragma unroll
     for (int j = 0; j < kChunk; ++j) {
-      al_ = fma(u[j], u[j], al_);
-      be_ = fma(v[j], v[j], be_);
-      ga_ = fma(u[j], v[j], ga_);
+      al_ += Num<T>::abs2(x[j]);
+      be_ += Num<T>::abs2(y[j]);
+      ga_ = Num<T>::fmac(x[j], y[j], ga_);
     }
   }
-  T c = 0, s = 0;
-  if (!Rotation<T>::get(al_, be_, ga_, L, lane, st + ST_MAXCOS, c, s)) return;
-  rotate_rows<T>(xp, xq, L, lane, c, s);
-  rotate_rows<T>(W + p * k, W + q * k, k, lane, c, s);
+  R c = 0, s = 0;
+  T u = Num<T>::one();
+  if (!Rotation<T>::get(al_, be_, ga_, L, lane, st + ST_MAXCOS, c, s, u)) return;
+  rotate_rows<T>(xp, xq, L, lane, c, s, u);
+  rotate_rows<T>(W + p * k, W + q * k, k, lane, c, s, u);
 }
 
 // All sweeps of one precision phase in one cooperative launch.
@@ -292,8 +441,8 @@ __global__ void __launch_bounds__(kThreads) svd_sweeps_kernel(T* __restrict__ wo
   const int lane = threadIdx.x & 31;
   const int64_t gwarp = (int64_t)blockIdx.x * kWarps + (threadIdx.x >> 5);
   const int64_t nwarps = (int64_t)gridDim.x * kWarps;
-  const int rx = sizeof(T) == 4 ? R_X32 : R_X;
-  const int rw = sizeof(T) == 4 ? R_W32 : R_W;
+  const int rx = sizeof(typename Num<T>::R) == 4 ? R_X32 : R_X;
+  const int rw = sizeof(typename Num<T>::R) == 4 ? R_W32 : R_W;
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     for (int round = 0; round < max_rounds; ++round) {
       for (int64_t item = gwarp; item < n_items; item += nwarps) {
@@ -355,6 +504,7 @@ __global__ void __launch_bounds__(BR * 32) svd_block_sweeps_kernel(T* __restrict
                                                                    int inner_sweeps, double tol_stop, int lmax,
                                                                    int64_t* __restrict__ state) {
   constexpr int R2 = 2 * BR;
+  using R = typename Num<T>::R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* Xs = reinterpret_cast<T*>(smem_raw);   // [R2][lmax]
   T* Qs = Xs + (size_t)R2 * lmax;           // [R2][R2]
@@ -362,8 +512,8 @@ __global__ void __launch_bounds__(BR * 32) svd_block_sweeps_kernel(T* __restrict
   __shared__ int64_t grow[R2];              // global row of each local row (-1: absent)
   unsigned long long* ctrl = reinterpret_cast<unsigned long long*>(state + (int64_t)n_blocks * ST_REC);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int rx = sizeof(T) == 4 ? R_X32 : R_X;
-  const int rw = sizeof(T) == 4 ? R_W32 : R_W;
+  const int rx = sizeof(typename Num<T>::R) == 4 ? R_X32 : R_X;
+  const int rw = sizeof(typename Num<T>::R) == 4 ? R_W32 : R_W;
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     for (int round = 0; round < max_rounds; ++round) {
       for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
@@ -385,14 +535,15 @@ __global__ void __launch_bounds__(BR * 32) svd_block_sweeps_kernel(T* __restrict
           const int64_t g = (int64_t)sv * BR + (threadIdx.x % BR);
           grow[threadIdx.x] = (g < k) ? g : -1;
         }
-        for (int e = threadIdx.x; e < R2 * R2; e += blockDim.x) Qs[e] = (e / R2 == e % R2) ? T(1) : T(0);
+        for (int e = threadIdx.x; e < R2 * R2; e += blockDim.x)
+          Qs[e] = (e / R2 == e % R2) ? Num<T>::one() : Num<T>::zero();
         if (threadIdx.x == 0) any_rot = 0;
         __syncthreads();
         for (int64_t e = threadIdx.x; e < (int64_t)R2 * L; e += blockDim.x) {
           const int i = (int)(e / L);
           const int64_t l = e - (int64_t)i * L;
           const int64_t g = grow[i];
-          Xs[(size_t)i * lmax + l] = (g >= 0) ? __ldcg(X + g * L + l) : T(0);
+          Xs[(size_t)i * lmax + l] = (g >= 0) ? __ldcg(X + g * L + l) : Num<T>::zero();
         }
         __syncthreads();
         for (int inner = 0; inner < inner_sweeps; ++inner) {
@@ -407,24 +558,28 @@ __global__ void __launch_bounds__(BR * 32) svd_block_sweeps_kernel(T* __restrict
             if (grow[p] >= 0 && grow[q] >= 0) {
               T* xp = Xs + (size_t)p * lmax;
               T* xq = Xs + (size_t)q * lmax;
-              T al_ = 0, be_ = 0, ga_ = 0;
+              R al_ = 0, be_ = 0;
+              T ga_ = Num<T>::zero();
               for (int64_t l = lane; l < L; l += 32) {
-                const T u = xp[l], v = xq[l];
-                al_ = fma(u, u, al_);
-                be_ = fma(v, v, be_);
-                ga_ = fma(u, v, ga_);
+                const T a = xp[l], b = xq[l];
+                al_ += Num<T>::abs2(a);
+                be_ += Num<T>::abs2(b);
+                ga_ = Num<T>::fmac(a, b, ga_);
               }
-              T c = 0, s = 0;
-              if (Rotation<T>::get(al_, be_, ga_, L, lane, st + ST_MAXCOS, c, s)) {
+              R c = 0, s = 0;
+              T u = Num<T>::one();
+              if (Rotation<T>::get(al_, be_, ga_, L, lane, st + ST_MAXCOS, c, s, u)) {
                 for (int64_t l = lane; l < L; l += 32) {
-                  const T u = xp[l], v = xq[l];
-                  xp[l] = c * u - s * v;
-                  xq[l] = s * u + c * v;
+                  T a = xp[l], b = xq[l];
+                  rot2<T>(a, b, c, s, u);
+                  xp[l] = a;
+                  xq[l] = b;
                 }
                 for (int l = lane; l < R2; l += 32) {
-                  const T u = Qs[p * R2 + l], v = Qs[q * R2 + l];
-                  Qs[p * R2 + l] = c * u - s * v;
-                  Qs[q * R2 + l] = s * u + c * v;
+                  T a = Qs[p * R2 + l], b = Qs[q * R2 + l];
+                  rot2<T>(a, b, c, s, u);
+                  Qs[p * R2 + l] = a;
+                  Qs[q * R2 + l] = b;
                 }
                 if (lane == 0) { rot_this = 1; any_rot = 1; }
               }
@@ -446,13 +601,13 @@ __global__ void __launch_bounds__(BR * 32) svd_block_sweeps_kernel(T* __restrict
           for (int64_t c = threadIdx.x; c < k; c += blockDim.x) {
             T old[R2];
 #pragma unroll
-            for (int j = 0; j < R2; ++j) old[j] = (grow[j] >= 0) ? __ldcg(W + grow[j] * k + c) : T(0);
+            for (int j = 0; j < R2; ++j) old[j] = (grow[j] >= 0) ? __ldcg(W + grow[j] * k + c) : Num<T>::zero();
 #pragma unroll
             for (int i = 0; i < R2; ++i) {
               if (grow[i] < 0) continue;
-              T acc = 0;
+              T acc = Num<T>::zero();
 #pragma unroll
-              for (int j = 0; j < R2; ++j) acc = fma(Qs[i * R2 + j], old[j], acc);
+              for (int j = 0; j < R2; ++j) acc = Num<T>::fma_(Qs[i * R2 + j], old[j], acc);
               W[grow[i] * k + c] = acc;
             }
           }
@@ -512,12 +667,12 @@ int launch_block_sweeps(T* work, const int64_t* blocks, int n_blocks, const int3
 
 // One CTA per block: singular values = row norms, sort descending (index tie-break),
 // write U, S, Vh; vectors of zero norm are completed to an orthonormal set.
-// mode 0: SVD. mode 1/2: symmetric eigendecomposition of a block shifted by shift[b]
-// (lambda = sigma - shift), eigenvectors = columns of W^T, ordered ascending (1) or by
+// mode 0: SVD. mode 1/2: Hermitian eigendecomposition of a block shifted by shift[b]
+// (lambda = sigma - shift), eigenvectors = columns of W^H, ordered ascending (1) or by
 // |lambda| descending (2); Vh is not written.
-__global__ void __launch_bounds__(1024) svd_finalize_kernel(const double* __restrict__ work,
-                                                            double* __restrict__ U, double* __restrict__ S,
-                                                            double* __restrict__ Vh,
+template <typename T>
+__global__ void __launch_bounds__(1024) svd_finalize_kernel(const T* __restrict__ work, T* __restrict__ U,
+                                                            double* __restrict__ S, T* __restrict__ Vh,
                                                             const int64_t* __restrict__ blocks, int pow2,
                                                             int mode, const double* __restrict__ shift) {
   extern __shared__ unsigned char smem_raw[];
@@ -528,8 +683,8 @@ __global__ void __launch_bounds__(1024) svd_finalize_kernel(const double* __rest
   const int64_t* r = blocks + (int64_t)blockIdx.x * YB_SVD_REC;
   const int64_t m = r[R_M], n = r[R_N], k = r[R_K], L = r[R_L];
   const bool tall = m > n;
-  const double* X = work + r[R_X];
-  const double* W = work + r[R_W];
+  const T* X = work + r[R_X];
+  const T* W = work + r[R_W];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   if (threadIdx.x == 0) n_zero = 0;
   for (int i = threadIdx.x; i < pow2; i += blockDim.x) {
@@ -539,7 +694,7 @@ __global__ void __launch_bounds__(1024) svd_finalize_kernel(const double* __rest
   __syncthreads();
   for (int64_t i = warp; i < k; i += nw) {
     double acc = 0.0;
-    for (int64_t l = lane; l < L; l += 32) acc = fma(X[i * L + l], X[i * L + l], acc);
+    for (int64_t l = lane; l < L; l += 32) acc += cabs2(X[i * L + l]);
     acc = warp_sum(acc);
     if (lane == 0) {
       const double sv = sqrt(acc);
@@ -578,19 +733,19 @@ __global__ void __launch_bounds__(1024) svd_finalize_kernel(const double* __rest
     }
   }
   double* Sb = S + r[R_S];
-  double* Ub = U + r[R_U];
-  double* Vb = Vh + r[R_V];
+  T* Ub = U + r[R_U];
+  T* Vb = Vh + r[R_V];
   if (mode != 0) {
     for (int64_t j = warp; j < k; j += nw) {
       const int64_t i = idx[j];
       double acc = 0.0;
-      for (int64_t l = lane; l < L; l += 32) acc = fma(X[i * L + l], X[i * L + l], acc);
+      for (int64_t l = lane; l < L; l += 32) acc += cabs2(X[i * L + l]);
       acc = warp_sum(acc);
       if (lane == 0) Sb[j] = sqrt(acc) - shift[blockIdx.x];
     }
     for (int64_t e = threadIdx.x; e < k * k; e += blockDim.x) {
       const int64_t j = e / k, c = e - j * k;
-      Ub[c * k + j] = W[(int64_t)idx[j] * k + c];
+      Ub[c * k + j] = cconj_(W[(int64_t)idx[j] * k + c]);
     }
     return;
   }
@@ -598,65 +753,84 @@ __global__ void __launch_bounds__(1024) svd_finalize_kernel(const double* __rest
     Sb[j] = sig[j];
     if (!(sig[j] > 0.0)) atomicAdd(&n_zero, 1);
   }
-  // normalised rows -> Vh (wide) or U columns (tall); W rows -> U columns (wide) or Vh rows (tall)
+  // wide (X_0 = A): Vh rows = x_j / s_j, U = W^H; tall (X_0 = A^H): U columns = conj(x_j) / s_j,
+  // Vh = W
   for (int64_t e = threadIdx.x; e < k * L; e += blockDim.x) {
     const int64_t j = e / L, l = e - j * L;
     const double sv = sig[j];
-    const double v = (sv > 0.0) ? X[(int64_t)idx[j] * L + l] / sv : 0.0;
-    if (tall) Ub[l * k + j] = v; else Vb[j * n + l] = v;
+    const T x = X[(int64_t)idx[j] * L + l];
+    const T v = (sv > 0.0) ? rscale(x, 1.0 / sv) : rscale(x, 0.0);
+    if (tall) Ub[l * k + j] = cconj_(v); else Vb[j * n + l] = v;
   }
   for (int64_t e = threadIdx.x; e < k * k; e += blockDim.x) {
     const int64_t j = e / k, c = e - j * k;
-    const double w = W[(int64_t)idx[j] * k + c];
-    if (tall) Vb[j * n + c] = w; else Ub[c * k + j] = w;
+    const T w = W[(int64_t)idx[j] * k + c];
+    if (tall) Vb[j * n + c] = w; else Ub[c * k + j] = cconj_(w);
   }
   __syncthreads();
   if (n_zero == 0) return;
   // completion: zero singular values sit at the end (positions k - n_zero .. k-1); replace
   // their vectors by unit vectors orthogonalised (twice) against all earlier ones.
-  __shared__ double red[32];
-  __shared__ double coef;
+  __shared__ double red[2][32];
+  __shared__ double coef[2];
   const int64_t stride_v = tall ? k : 1;  // distance between consecutive entries of one vector
   const int64_t stride_j = tall ? 1 : n;  // distance between vectors
-  double* base = tall ? Ub : Vb;
+  T* base = tall ? Ub : Vb;
   for (int64_t j = k - n_zero; j < k; ++j) {
     for (int64_t cand = 0; cand < L; ++cand) {
-      double* vj = base + j * stride_j;
-      for (int64_t l = threadIdx.x; l < L; l += blockDim.x) vj[l * stride_v] = (l == cand) ? 1.0 : 0.0;
+      T* vj = base + j * stride_j;
+      for (int64_t l = threadIdx.x; l < L; l += blockDim.x)
+        vj[l * stride_v] = (l == cand) ? Num<T>::one() : Num<T>::zero();
       __syncthreads();
       for (int pass = 0; pass < 2; ++pass) {
         for (int64_t i = 0; i < j; ++i) {
-          const double* vi = base + i * stride_j;
-          double acc = 0.0;
-          for (int64_t l = threadIdx.x; l < L; l += blockDim.x) acc = fma(vi[l * stride_v], vj[l * stride_v], acc);
-          acc = warp_sum(acc);
-          if (lane == 0) red[warp] = acc;
-          __syncthreads();
-          if (threadIdx.x == 0) {
-            double tot = 0.0;
-            for (int w = 0; w < nw; ++w) tot += red[w];
-            coef = tot;
+          const T* vi = base + i * stride_j;
+          // <v_i, v_j> = sum conj(v_i) v_j
+          T acc = Num<T>::zero();
+          for (int64_t l = threadIdx.x; l < L; l += blockDim.x)
+            acc = Num<T>::fmac(vj[l * stride_v], vi[l * stride_v], acc);
+          warp_sum_t<T>(acc);
+          if (lane == 0) {
+            if constexpr (Num<T>::cplx) {
+              red[0][warp] = acc.x;
+              red[1][warp] = acc.y;
+            } else {
+              red[0][warp] = acc;
+            }
           }
           __syncthreads();
-          const double cf = coef;
-          for (int64_t l = threadIdx.x; l < L; l += blockDim.x) vj[l * stride_v] -= cf * vi[l * stride_v];
+          if (threadIdx.x == 0) {
+            double re = 0.0, im = 0.0;
+            for (int w = 0; w < nw; ++w) {
+              re += red[0][w];
+              if constexpr (Num<T>::cplx) im += red[1][w];
+            }
+            coef[0] = re;
+            coef[1] = im;
+          }
+          __syncthreads();
+          T cf;
+          if constexpr (Num<T>::cplx) cf = make_double2(coef[0], coef[1]);
+          else cf = coef[0];
+          for (int64_t l = threadIdx.x; l < L; l += blockDim.x)
+            vj[l * stride_v] = Num<T>::sub(vj[l * stride_v], Num<T>::mul(cf, vi[l * stride_v]));
           __syncthreads();
         }
       }
       double acc = 0.0;
-      for (int64_t l = threadIdx.x; l < L; l += blockDim.x) acc = fma(vj[l * stride_v], vj[l * stride_v], acc);
+      for (int64_t l = threadIdx.x; l < L; l += blockDim.x) acc += cabs2(vj[l * stride_v]);
       acc = warp_sum(acc);
-      if (lane == 0) red[warp] = acc;
+      if (lane == 0) red[0][warp] = acc;
       __syncthreads();
       if (threadIdx.x == 0) {
         double tot = 0.0;
-        for (int w = 0; w < nw; ++w) tot += red[w];
-        coef = sqrt(tot);
+        for (int w = 0; w < nw; ++w) tot += red[0][w];
+        coef[0] = sqrt(tot);
       }
       __syncthreads();
-      const double nrm = coef;
+      const double nrm = coef[0];
       if (nrm > 0.5) {
-        for (int64_t l = threadIdx.x; l < L; l += blockDim.x) vj[l * stride_v] /= nrm;
+        for (int64_t l = threadIdx.x; l < L; l += blockDim.x) vj[l * stride_v] = rscale(vj[l * stride_v], 1.0 / nrm);
         __syncthreads();
         break;
       }
@@ -689,87 +863,140 @@ int launch_sweeps(T* work, const int64_t* blocks, int n_blocks, const int32_t* p
 }  // namespace
 }  // namespace yb
 
+namespace yb {
+
+template <typename T>
+int block_sweeps_t(T* w, const int64_t* blocks, int n_blocks, const int32_t* super_items, int n_items,
+                          int max_rounds, int rows_per_super, int max_sweeps, int inner_sweeps, double tol_stop,
+                          int lmax, int64_t* state, cudaStream_t s) {
+  switch (rows_per_super) {
+    case 16: return yb::launch_block_sweeps<T, 16>(w, blocks, n_blocks, super_items, n_items, max_rounds, max_sweeps,
+                                                  inner_sweeps, tol_stop, lmax, state, s);
+    case 8: return yb::launch_block_sweeps<T, 8>(w, blocks, n_blocks, super_items, n_items, max_rounds, max_sweeps,
+                                                inner_sweeps, tol_stop, lmax, state, s);
+    case 4: return yb::launch_block_sweeps<T, 4>(w, blocks, n_blocks, super_items, n_items, max_rounds, max_sweeps,
+                                                inner_sweeps, tol_stop, lmax, state, s);
+    default: return YB_ERR_INVALID;
+  }
+}
+
+template <typename T>
+int finalize_t(const void* work, void* U, double* S, void* Vh, const int64_t* blocks, int n_blocks, int pow2,
+                      int mode, const double* shift, cudaStream_t s) {
+  const size_t smem = (size_t)pow2 * (sizeof(double) + sizeof(int));
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(yb::svd_finalize_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
+  }
+  yb::svd_finalize_kernel<T><<<n_blocks, 1024, smem, s>>>((const T*)work, (T*)U, S, (T*)Vh, blocks, pow2, mode,
+                                                          shift);
+  return yb::check_launch();
+}
+
+}  // namespace yb
+
 extern "C" {
 
 int yb_svd_init(const void* a, void* work32, const int64_t* blocks, int n_blocks, int dtype, int64_t* state,
                 double* shift, double* scale, void* stream) {
   if (n_blocks == 0) return YB_OK;
-  if (dtype != YB_F64) return YB_ERR_INVALID;
+  if (dtype != YB_F64 && dtype != YB_C128) return YB_ERR_INVALID;
   if (!a || !work32 || !blocks || !state || !scale) return YB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
-  yb::block_fro_kernel<<<n_blocks, 256, 0, s>>>((const double*)a, blocks, shift, scale);
   dim3 grid(64, (unsigned)n_blocks);
-  yb::svd_init_kernel<<<grid, 256, 0, s>>>((const double*)a, (float*)work32, blocks, state, shift, scale);
+  if (dtype == YB_F64) {
+    yb::block_fro_kernel<double><<<n_blocks, 256, 0, s>>>((const double*)a, blocks, shift, scale);
+    yb::svd_init_kernel<double, float><<<grid, 256, 0, s>>>((const double*)a, (float*)work32, blocks, state, shift,
+                                                            scale);
+  } else {
+    yb::block_fro_kernel<double2><<<n_blocks, 256, 0, s>>>((const double2*)a, blocks, shift, scale);
+    yb::svd_init_kernel<double2, float2><<<grid, 256, 0, s>>>((const double2*)a, (float2*)work32, blocks, state,
+                                                              shift, scale);
+  }
   return yb::check_launch();
 }
 
 int yb_svd_sweeps(void* work, const int64_t* blocks, int n_blocks, const int32_t* pair_items, int n_pair_items,
-                  int max_rounds, int precision, int max_sweeps, double tol_stop, int64_t* state, void* stream) {
+                  int max_rounds, int precision, int dtype, int max_sweeps, double tol_stop, int64_t* state,
+                  void* stream) {
   if (n_blocks == 0 || n_pair_items == 0 || max_sweeps <= 0) return YB_OK;
   if (!work || !blocks || !pair_items || !state) return YB_ERR_INVALID;
+  if (dtype != YB_F64 && dtype != YB_C128) return YB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
-  if (precision == 32)
+  const bool c = dtype == YB_C128;
+  if (precision == 32 && !c)
     return yb::launch_sweeps<float>((float*)work, blocks, n_blocks, pair_items, n_pair_items, max_rounds, max_sweeps,
                                     tol_stop, state, s);
-  if (precision == 64)
+  if (precision == 32 && c)
+    return yb::launch_sweeps<float2>((float2*)work, blocks, n_blocks, pair_items, n_pair_items, max_rounds,
+                                     max_sweeps, tol_stop, state, s);
+  if (precision == 64 && !c)
     return yb::launch_sweeps<double>((double*)work, blocks, n_blocks, pair_items, n_pair_items, max_rounds,
                                      max_sweeps, tol_stop, state, s);
+  if (precision == 64 && c)
+    return yb::launch_sweeps<double2>((double2*)work, blocks, n_blocks, pair_items, n_pair_items, max_rounds,
+                                      max_sweeps, tol_stop, state, s);
   return YB_ERR_INVALID;
 }
 
 int yb_svd_block_sweeps(void* work32, const int64_t* blocks, int n_blocks, const int32_t* super_items,
-                        int n_items, int max_rounds, int rows_per_super, int max_sweeps, int inner_sweeps,
-                        double tol_stop, int lmax, int64_t* state, void* stream) {
+                        int n_items, int max_rounds, int rows_per_super, int dtype, int max_sweeps,
+                        int inner_sweeps, double tol_stop, int lmax, int64_t* state, void* stream) {
   if (n_blocks == 0 || n_items == 0 || max_sweeps <= 0) return YB_OK;
   if (!work32 || !blocks || !super_items || !state || lmax <= 0 || inner_sweeps <= 0) return YB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
-  float* w = (float*)work32;
-  switch (rows_per_super) {
-    case 16: return yb::launch_block_sweeps<float, 16>(w, blocks, n_blocks, super_items, n_items, max_rounds,
-                                                      max_sweeps, inner_sweeps, tol_stop, lmax, state, s);
-    case 8: return yb::launch_block_sweeps<float, 8>(w, blocks, n_blocks, super_items, n_items, max_rounds, max_sweeps,
-                                                    inner_sweeps, tol_stop, lmax, state, s);
-    case 4: return yb::launch_block_sweeps<float, 4>(w, blocks, n_blocks, super_items, n_items, max_rounds, max_sweeps,
-                                                    inner_sweeps, tol_stop, lmax, state, s);
-    default: return YB_ERR_INVALID;
-  }
+  if (dtype == YB_F64)
+    return yb::block_sweeps_t<float>((float*)work32, blocks, n_blocks, super_items, n_items, max_rounds, rows_per_super,
+                                 max_sweeps, inner_sweeps, tol_stop, lmax, state, s);
+  if (dtype == YB_C128)
+    return yb::block_sweeps_t<float2>((float2*)work32, blocks, n_blocks, super_items, n_items, max_rounds,
+                                  rows_per_super, max_sweeps, inner_sweeps, tol_stop, lmax, state, s);
+  return YB_ERR_INVALID;
 }
 
-int yb_svd_widen(const void* work32, void* work64, const int64_t* blocks, int n_blocks, int64_t* state,
+int yb_svd_widen(const void* work32, void* work64, const int64_t* blocks, int n_blocks, int dtype, int64_t* state,
                  void* stream) {
   if (n_blocks == 0) return YB_OK;
   if (!work32 || !work64 || !blocks || !state) return YB_ERR_INVALID;
   dim3 grid(64, (unsigned)n_blocks);
-  yb::svd_widen_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>((const float*)work32, (double*)work64, blocks, state);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == YB_F64)
+    yb::svd_widen_kernel<float, double><<<grid, 256, 0, s>>>((const float*)work32, (double*)work64, blocks, state);
+  else if (dtype == YB_C128)
+    yb::svd_widen_kernel<float2, double2><<<grid, 256, 0, s>>>((const float2*)work32, (double2*)work64, blocks,
+                                                               state);
+  else
+    return YB_ERR_INVALID;
   return yb::check_launch();
 }
 
-int yb_svd_shift_prefill(void* work64, const int64_t* blocks, int n_blocks, const double* shift, void* stream) {
+int yb_svd_shift_prefill(void* work64, const int64_t* blocks, int n_blocks, int dtype, const double* shift,
+                         void* stream) {
   if (n_blocks == 0) return YB_OK;
   if (!work64 || !blocks || !shift) return YB_ERR_INVALID;
   dim3 grid(64, (unsigned)n_blocks);
-  yb::svd_shift_prefill_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>((double*)work64, blocks, shift);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == YB_F64)
+    yb::svd_shift_prefill_kernel<double><<<grid, 256, 0, s>>>((double*)work64, blocks, shift);
+  else if (dtype == YB_C128)
+    yb::svd_shift_prefill_kernel<double2><<<grid, 256, 0, s>>>((double2*)work64, blocks, shift);
+  else
+    return YB_ERR_INVALID;
   return yb::check_launch();
 }
 
 int yb_svd_finalize(const void* work, void* U, double* S, void* Vh, const int64_t* blocks, int n_blocks, int dtype,
                     int max_k, int mode, const double* shift, void* stream) {
   if (n_blocks == 0) return YB_OK;
-  if (dtype != YB_F64) return YB_ERR_INVALID;
+  if (dtype != YB_F64 && dtype != YB_C128) return YB_ERR_INVALID;
   if (mode < 0 || mode > 2 || (mode != 0 && shift == nullptr)) return YB_ERR_INVALID;
   if (max_k > 8192) return YB_ERR_TOO_LARGE;
   int pow2 = 1;
   while (pow2 < max_k) pow2 <<= 1;
-  const size_t smem = (size_t)pow2 * (sizeof(double) + sizeof(int));
   cudaStream_t s = (cudaStream_t)stream;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(yb::svd_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
-  }
-  yb::svd_finalize_kernel<<<n_blocks, 1024, smem, s>>>((const double*)work, (double*)U, S, (double*)Vh, blocks, pow2,
-                                                       mode, shift);
-  return yb::check_launch();
+  if (dtype == YB_F64) return yb::finalize_t<double>(work, U, S, Vh, blocks, n_blocks, pow2, mode, shift, s);
+  return yb::finalize_t<double2>(work, U, S, Vh, blocks, n_blocks, pow2, mode, shift, s);
 }
 
 }  // extern "C"

@@ -256,9 +256,10 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
     nb = len(plan.blocks)
     dev = data.device
     code = _dtype_code(data.dtype)
+    cplx = code == N.YB_C128
     dblocks, dpairs = _dev(plan, 'svd', (plan.blocks, plan.pair_items), dev)
-    w64 = torch.empty(plan.n64, dtype=torch.float64, device=dev)
-    w32 = torch.empty(plan.n32, dtype=torch.float32, device=dev)
+    w64 = torch.empty(plan.n64, dtype=torch.complex128 if cplx else torch.float64, device=dev)
+    w32 = torch.empty(plan.n32, dtype=torch.complex64 if cplx else torch.float32, device=dev)
     state = torch.zeros(4 * nb + 4, dtype=torch.int64, device=dev)
     aux = torch.empty(2 * nb, dtype=torch.float64, device=dev)  # [scale | shift]
     shift = aux[nb:] if mode != 0 else None
@@ -269,13 +270,13 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
     if plan.rows_per_super and BLOCKED_FP32[0]:
         (dsup,) = _dev(plan, 'svd_super', (plan.super_items,), dev)
         N.call('yb_svd_block_sweeps', _ptr(w32), _ptr(dblocks), nb, _ptr(dsup), len(plan.super_items),
-               plan.super_rounds, plan.rows_per_super, MAX_SWEEPS32, INNER_SWEEPS32, TOL_STOP32, plan.lmax,
+               plan.super_rounds, plan.rows_per_super, code, MAX_SWEEPS32, INNER_SWEEPS32, TOL_STOP32, plan.lmax,
                _ptr(state), st)
     else:
         N.call('yb_svd_sweeps', _ptr(w32), _ptr(dblocks), nb, _ptr(dpairs), len(plan.pair_items), plan.max_rounds,
-               32, MAX_SWEEPS32, TOL_STOP32, _ptr(state), st)
+               32, code, MAX_SWEEPS32, TOL_STOP32, _ptr(state), st)
     _svd_state_check(state, nb, 'FP32', False)
-    N.call('yb_svd_widen', _ptr(w32), _ptr(w64), _ptr(dblocks), nb, _ptr(state), st)
+    N.call('yb_svd_widen', _ptr(w32), _ptr(w64), _ptr(dblocks), nb, code, _ptr(state), st)
     w0, t0, n0, ws = plan.w_range
     W, Wn = w64[w0:w0 + ws], w64[n0:n0 + ws]
     for _ in range(NS_STEPS):
@@ -284,12 +285,12 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
         run_gemm(plan.ns, w64, w64, w64, alpha=-0.5, beta=1.5)
         W.copy_(Wn)
     if shift is not None:
-        N.call('yb_svd_shift_prefill', _ptr(w64), _ptr(dblocks), nb, _ptr(shift), st)
+        N.call('yb_svd_shift_prefill', _ptr(w64), _ptr(dblocks), nb, code, _ptr(shift), st)
         run_gemm(plan.xform, w64, data, w64, beta=1.0)
     else:
         run_gemm(plan.xform, w64, data, w64)
     N.call('yb_svd_sweeps', _ptr(w64), _ptr(dblocks), nb, _ptr(dpairs), len(plan.pair_items), plan.max_rounds, 64,
-           max_sweeps, TOL_STOP64, _ptr(state), st)
+           code, max_sweeps, TOL_STOP64, _ptr(state), st)
     _svd_state_check(state, nb, 'FP64', True)
     N.call('yb_svd_finalize', _ptr(w64), _ptr(U), _ptr(S), _vp(V.data_ptr() if V is not None else 0), _ptr(dblocks),
            nb, code, plan.max_k, mode, sp, st)
@@ -298,13 +299,11 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
 def svd(data, meta, sizes, max_sweeps=MAX_SWEEPS):
     """Thin SVD of every block (one-sided Jacobi); returns (U, S, Vh) flat tensors."""
     data = _check(data)
-    if _dtype_code(data.dtype) != N.YB_F64:
-        raise NotImplementedError("yastn_gb300 svd: complex128 Jacobi is not implemented yet")
     dev = data.device
     U = torch.empty(sizes[0], dtype=data.dtype, device=dev)
     S = torch.empty(sizes[1], dtype=torch.float64, device=dev)
     V = torch.empty(sizes[2], dtype=data.dtype, device=dev)
-    plan = P.svd_plan(meta, ROWS_PER_SUPER[0])
+    plan = P.svd_plan(meta, ROWS_PER_SUPER[0], data.is_complex())
     if len(plan.blocks) == 0:
         return U, S, V
     _jacobi(data, plan, U, S, V, 0, max_sweeps)
@@ -341,19 +340,17 @@ def svd_backward(U, S, V, gU, gS, gV, meta, data_size, dtype):
 
 
 def eigh(data, meta, sizes, order_by_magnitude=False, max_sweeps=MAX_SWEEPS):
-    """Symmetric eigendecomposition of every block (records (sl, D, slU, DU, slS) of
+    """Hermitian eigendecomposition of every block (records (sl, D, slU, DU, slS) of
     yastn/backend/backend_np.py:461-474): eigenvalues ascending, or by descending
     magnitude when ``order_by_magnitude`` (yastn/backend/linalg/torch_eig_sym.py:25-32)."""
     data = _check(data)
-    if _dtype_code(data.dtype) != N.YB_F64:
-        raise NotImplementedError("yastn_gb300 eigh: complex128 (Hermitian) Jacobi is not implemented yet")
     if data.requires_grad:
         raise NotImplementedError("yastn_gb300 eigh: the adjoint is not implemented yet")
     dev = data.device
     S = torch.zeros(sizes[0], dtype=torch.float64, device=dev)
     U = torch.zeros(sizes[1], dtype=data.dtype, device=dev)
     svd_meta = tuple((sl, D, slU, DU, slS, (0, 0), (DU[1], D[1])) for sl, D, slU, DU, slS in meta)
-    plan = P.svd_plan(svd_meta)
+    plan = P.svd_plan(svd_meta, ROWS_PER_SUPER[0], data.is_complex())
     if len(plan.blocks) == 0:
         return S, U
     _jacobi(data, plan, U, S, None, 2 if order_by_magnitude else 1, max_sweeps)
