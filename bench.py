@@ -50,7 +50,7 @@ def parse():
     p.add_argument('--steps', type=int, default=20)
     p.add_argument('--warmup', type=int, default=5)
     p.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
-    p.add_argument('--workload', default='cfg2', choices=['cfg1', 'cfg2', 'cfg5'])
+    p.add_argument('--workload', default='cfg2', choices=['cfg1', 'cfg2', 'cfg3', 'cfg5'])
     p.add_argument('--gemm', default='emulated', choices=['emulated', 'fp64'],
                    help='sector-GEMM mode of the headline (cfg2)')
     p.add_argument('--no-svd', action='store_true', help='skip the extra svd_with_truncation timing')
@@ -63,6 +63,8 @@ class Cfg1:
     name = "U(1) rank-4 D=64 tensordot A(2,3)xB(0,1), fuse_to_matrix, 13 sectors, FP64"
     metric = METRIC
     has_svd = True
+    complex_gemm = False
+    trunc = {'D_total': 64}
     ozaki_traffic = 78263296 + 8303872  # dram bytes read + written by one launch (ncu, this workload)
 
     def __init__(self):
@@ -90,6 +92,42 @@ class Cfg1:
         Bm = oracle.transpose_and_merge(self.B, *self.mB)
         Cm = oracle.dot(Am, Bm, *self.mdot)
         return oracle.unmerge(Cm, self.mun)
+
+
+class Cfg3(Cfg1):
+    name = ("U(1)xU(1) (N,Sz) complex128 rank-4, 11 charges per leg with geometric(0.15) dims on 1..64 "
+            "(leg total 116, 595 blocks per tensor), tensordot A(2,3)xB(0,1), fuse_contracted, 595 complex "
+            "sector GEMMs")
+    metric = "tensordot TFLOP/s (block-sparse complex128, U(1)xU(1) 595 blocks, <=1e-10 rel)"
+    has_svd = True
+    ozaki_traffic = None
+    complex_gemm = True
+
+    def __init__(self):
+        from yastn_gb300.workloads import load_trace, cfg3_inputs
+        from yastn_gb300 import _plans as P
+        self.tr = load_trace('cfg3')
+        self.A, self.B = cfg3_inputs(self.tr)
+        c = self.tr['calls']
+        self.mA = c[0]['args'][1:]
+        self.mB = c[1]['args'][1:]
+        self.mdot = c[2]['args'][2:]
+        self.mun = None
+        self.mC = c[3]['args'][1:]
+        self.msvd = c[4]['args'][1:3]
+        self.mU = c[5]['args'][1]
+        self.mV = c[6]['args'][1]
+        self.mask_calls = [x['args'] for x in c[7:10]]
+        self.trunc = {'tol': 1e-8}
+        # complex multiply-add = 8 real flops
+        self.flops = 4 * P.dot_plan(self.mdot[0]).flops
+        self.bytes_merge = 32 * self.A.size
+
+    def cpu_step(self):
+        import oracle
+        Am = oracle.transpose_and_merge(self.A, *self.mA)
+        Bm = oracle.transpose_and_merge(self.B, *self.mB)
+        return oracle.dot(Am, Bm, *self.mdot)
 
 
 class Cfg5(Cfg1):
@@ -169,8 +207,9 @@ def run_reference(args, wl):
     value = wl.flops / t / 1e12
     line = {"impl": "reference", "metric": wl.metric, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded yastn normal draws)",
-            "config": {"workload": wl.name, "policy": "fuse_to_matrix"},
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128" if wl.complex_gemm else "f64",
+            "data": "synthetic (seeded yastn normal draws)",
+            "config": {"workload": wl.name},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
                              "sample": f"{args.steps} tensordot steps (numpy BLAS, all host threads)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -284,7 +323,7 @@ def run_gpu(args, wl):
     dB = torch.from_numpy(wl.B).to(dev)
     hA = torch.from_numpy(wl.A).pin_memory()
     hB = torch.from_numpy(wl.B).pin_memory()
-    hC = torch.empty(wl.A.size, dtype=torch.float64).pin_memory()
+
     flush = torch.empty(L2_FLUSH_BYTES // 8, dtype=torch.float64, device=dev)
     kern_ev = []
 
@@ -299,7 +338,7 @@ def run_gpu(args, wl):
         if record:
             e1.record()
             kern_ev.append((e0, e1))
-        return BK.unmerge(Cm, wl.mun)
+        return Cm if wl.mun is None else BK.unmerge(Cm, wl.mun)
 
     def barrier():
         if world > 1:
@@ -322,8 +361,10 @@ def run_gpu(args, wl):
     # native FP64 path: parity guard against the reference checksum, then timing
     BK.set_gemm_mode('fp64')
     Cn = tensordot(dA, dB)
-    assert abs(float(Cn.sum()) - chk['sum0']) <= 1e-9 * chk['abs0'], "tensordot result differs from the reference"
+    assert abs(float(Cn.real.sum()) - chk['sum0']) <= 1e-9 * chk['abs0'], "tensordot result differs from the reference"
+    hC = torch.empty(Cn.numel(), dtype=Cn.dtype).pin_memory()
     sector_err = per_sector_errors(torch, BK, wl, dA, dB)
+    plain_ms = plain_per_block_ms(torch, BK, wl, dA, dB, flush)
     for _ in range(args.warmup):
         tensordot(dA, dB)
     barrier()
@@ -361,16 +402,17 @@ def run_gpu(args, wl):
     clk = clocks.stop()
     t_e2e, _ = _tflops_of(e2e_ev, wl.flops)
 
-    # the dominant kernel alone (split-operand GEMM), for the roofline
+    # the dominant kernel alone (split-operand GEMM; the native grouped GEMM for complex
+    # data), for the roofline
     from yastn_gb300._plans import ozaki_dot_plan
-    oz = ozaki_dot_plan(wl.mdot[0], ops.OZAKI_SLICES)
+    top_kernel = 'yb_grouped_gemm' if wl.complex_gemm else 'yb_ozaki_gemm'
     Am = BK.transpose_and_merge(dA, *wl.mA)
     Bm = BK.transpose_and_merge(dB, *wl.mB)
     orig = _native.call
     gemm_ev = []
 
     def spy(name, *a, **k):
-        if name == 'yb_ozaki_gemm':
+        if name == top_kernel:
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             r = orig(name, *a, **k)
@@ -382,12 +424,19 @@ def run_gpu(args, wl):
     try:
         for _ in range(args.steps):
             flush.zero_()
-            ops.dot_ozaki(Am, Bm, *wl.mdot)
+            if wl.complex_gemm:
+                ops.dot(Am, Bm, *wl.mdot)
+            else:
+                ops.dot_ozaki(Am, Bm, *wl.mdot)
         barrier()
     finally:
         _native.call = orig
     t_gemm = sum(a.elapsed_time(b) for a, b in gemm_ev) / len(gemm_ev) * 1e-3
-    tensor_flops = oz.flops * ops.OZAKI_SLICES * (ops.OZAKI_SLICES + 1) // 2
+    if wl.complex_gemm:
+        tensor_flops = wl.flops
+    else:
+        oz = ozaki_dot_plan(wl.mdot[0], ops.OZAKI_SLICES)
+        tensor_flops = oz.flops * ops.OZAKI_SLICES * (ops.OZAKI_SLICES + 1) // 2
     BK.set_gemm_mode('fp64')
 
     # the workload's truncated block SVD (extra field)
@@ -401,7 +450,7 @@ def run_gpu(args, wl):
             Uu = BK.unmerge(U, wl.mU)
             Vu = BK.unmerge(V, wl.mV)
             slices = sorted(tuple(m[4]) for m in wl.msvd[0])
-            mask, kept = ops.truncation_mask_data(S, slices, None, D_total=64)
+            mask, kept = ops.truncation_mask_data(S, slices, None, **wl.trunc)
             out = []
             for (Ain, mask_r, meta, Dsize, axis, ndim), data in zip(wl.mask_calls, (Uu, S, Vu)):
                 dmask = {k: torch.as_tensor(np.asarray(v, dtype=np.int64), device=dev) for k, v in mask_r.items()}
@@ -432,38 +481,79 @@ def run_gpu(args, wl):
     bf16_peak, peak_src = bf16_peak_tflops()
     cpu_t, reps = time_cpu(wl.cpu_step, budget_s=8.0)
     achieved = tensor_flops / t_gemm / 1e12
+    if wl.complex_gemm:
+        roof = {"bound": "fp64", "kernel": "yb grouped_gemm_kernel<Cplx> (FP64 DFMA, 64x64 tiles, all sectors)",
+                "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                "peak_source": "measured live: cuBLAS DGEMM 4096^3 (complex GEMM runs on the same FP64 pipe)",
+                "traffic": None}
+    else:
+        roof = {"bound": "tensor", "kernel": "yb ozaki_gemm_kernel<8> (mma.sync bf16, 36 slice-pair products)",
+                "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s", "frac": achieved / bf16_peak,
+                "peak_source": peak_src, "traffic": wl.ozaki_traffic,
+                "traffic_note": "dram bytes read+written by one launch, ncu capture on this workload"}
     line = {
         "metric": wl.metric, "value": world * wl.flops / t_max / 1e12, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64 (sector GEMMs emulated: 8 bf16 digit slices, fp32/fp64 accumulation)",
+        "dtype": ("c128 (native FP64 complex sector GEMMs)" if wl.complex_gemm else
+                  "f64 (sector GEMMs emulated: 8 bf16 digit slices, fp32/fp64 accumulation)"),
         "data": "synthetic (seeded normal draws as yastn.rand, metadata recorded from yastn)",
         "config": {"workload": wl.name, "flop_per_step": wl.flops, "parallelism": f"replicas{world}",
-                   "gemm_mode": "emulated", "l2": "flushed between timed steps (256 MB write)",
+                   "gemm_mode": "fp64 (complex)" if wl.complex_gemm else "emulated",
+                   "l2": "flushed between timed steps (256 MB write)",
                    "max_rel_err_vs_fp64": emu_err,
                    "max_rel_err_per_sector_vs_oracle": sector_err},
-        "roofline": {"bound": "tensor", "kernel": "yb ozaki_gemm_kernel<8> (mma.sync bf16, 36 slice-pair products)",
-                     "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s", "frac": achieved / bf16_peak,
-                     "peak_source": peak_src, "traffic": wl.ozaki_traffic,
-                     "traffic_note": "dram bytes read+written by one launch, ncu capture on this workload"},
+        "roofline": roof,
         "cpu_baseline": {"value": wl.flops / cpu_t / 1e12, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
                          "sample": f"{reps} tensordot steps of the same workload (numpy BLAS, median)"},
         "e2e": {"value": world * wl.flops / t_e2e / 1e12, "unit": UNIT,
-                "h2d_bytes_per_step": int(wl.A.nbytes + wl.B.nbytes), "d2h_bytes_per_step": int(wl.A.nbytes)},
+                "h2d_bytes_per_step": int(wl.A.nbytes + wl.B.nbytes),
+                "d2h_bytes_per_step": int(hC.numel() * hC.element_size())},
         "gpu_launches": launches,
         "clocks": clk,
-        "extra": {"dot_ms": t_dot * 1e3, "ozaki_gemm_kernel_ms": t_gemm * 1e3,
+        "extra": {"dot_ms": t_dot * 1e3, "top_kernel_ms": t_gemm * 1e3,
+                  "plain_per_block_dot_ms": plain_ms,
+                  "plain_per_block_dot": "the same sector GEMMs as one torch.matmul (cuBLAS) launch per block "
+                                         "from a host loop, FP64 (the reference torch backend's kernel_dot pattern)",
+                  "grouped_vs_plain_per_block_dot": plain_ms / (t_native_gemm * 1e3),
                   "native_fp64_tflops": native_tflops, "native_fp64_ms_per_step": t_native * 1e3,
                   "native_fp64_gemm_tflops": native_gemm_tflops,
                   "native_fp64_gemm_frac_of_cublas_dgemm": native_gemm_tflops / fp64_peak,
                   "fp64_peak_cublas_dgemm_tflops": fp64_peak,
                   "svd_with_truncation_ms": svd_ms,
-                  "svd_with_truncation": "merge C, 13-block mixed-precision Jacobi SVD, unmerge U/V, device "
-                                         "truncation D_total=64, 3 masks (FP64 results)"},
+                  "svd_with_truncation": f"merge C, {len(wl.msvd[0]) if wl.has_svd else 0}-block mixed-precision "
+                                         f"Jacobi SVD, unmerge U/V, device truncation {wl.trunc}, 3 masks"},
     }
     print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
+
+
+def plain_per_block_ms(torch, BK, wl, dA, dB, flush, reps=5):
+    """The sector GEMMs of the same dot as one cuBLAS launch per block from a host loop (the
+    pattern of the reference torch backend's kernel_dot): device time per dot, FP64."""
+    Am = BK.transpose_and_merge(dA, *wl.mA)
+    Bm = BK.transpose_and_merge(dB, *wl.mB)
+    meta, Dsize = wl.mdot
+    C = torch.zeros(Dsize, dtype=Am.dtype, device=Am.device)
+    views = [(C[slc[0]:slc[1]].view(Dc), Am[sla[0]:sla[1]].view(Da), Bm[slb[0]:slb[1]].view(Db))
+             for slc, Dc, sla, Da, slb, Db in meta]
+
+    def once():
+        for c, a, b in views:
+            torch.matmul(a, b, out=c)
+    once()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        once()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return float(np.median(ts))
 
 
 def per_sector_errors(torch, BK, wl, dA, dB):
@@ -477,7 +567,7 @@ def per_sector_errors(torch, BK, wl, dA, dB):
     dBm = BK.transpose_and_merge(dB, *wl.mB)
     out = {}
     mode0 = BK.get_gemm_mode()
-    for mode in ('fp64', 'emulated'):
+    for mode in (('fp64',) if wl.complex_gemm else ('fp64', 'emulated')):
         BK.set_gemm_mode(mode)
         got = BK.dot(dAm, dBm, *wl.mdot).cpu().numpy()
         worst = 0.0
@@ -488,7 +578,7 @@ def per_sector_errors(torch, BK, wl, dA, dB):
                 worst = max(worst, float(np.abs(g - r).max() / mx))
         out[mode] = worst
     BK.set_gemm_mode(mode0)
-    assert out['fp64'] <= 1e-12 and out['emulated'] <= 1e-10, out
+    assert out['fp64'] <= 1e-12 and out.get('emulated', 0.0) <= 1e-10, out
     return out
 
 
@@ -691,7 +781,7 @@ def kernel_roofline(torch, dev, run_once, w, gemm_mode, reps=5):
 
 def main():
     args = parse()
-    wl = {'cfg1': Cfg1, 'cfg2': Cfg2, 'cfg5': Cfg5}[args.workload]()
+    wl = {'cfg1': Cfg1, 'cfg2': Cfg2, 'cfg3': Cfg3, 'cfg5': Cfg5}[args.workload]()
     if args.impl == 'reference':
         run_reference(args, wl)
     elif args.workload == 'cfg2':

@@ -561,6 +561,47 @@ def scen_cfg5():
     save('cfg5', rec, extra)
 
 
+def cfg3_legs():
+    """Charges and sector dims of the U(1)xU(1) complex workload: the 11 (N, Sz) charges of
+    smallest |N| + |Sz| (N in -6..6, Sz in -3..3; 11 charges give 595 blocks in the rank-4
+    tensor), sector dims drawn from a geometric distribution (p = 0.15) clipped to 1..64
+    with default_rng(0). The dims are not rescaled to a leg total of 512: with ~600 blocks
+    that would need ~4e9 complex elements (68 GB) per tensor and fused SVD sectors of
+    ~33000; the block count and the dim distribution are kept (leg total 116)."""
+    charges = sorted(((n, sz) for n in range(-6, 7) for sz in range(-3, 4)),
+                     key=lambda c: (abs(c[0]) + abs(c[1]), c))[:11]
+    D = np.clip(np.random.default_rng(0).geometric(0.15, size=11), 1, 64)
+    order = sorted(range(11), key=lambda i: charges[i])
+    return tuple(charges[i] for i in order), tuple(int(D[i]) for i in order)
+
+
+def scen_cfg3():
+    """U(1)xU(1) complex128 workload with many small uneven blocks: rank-4 tensors with the
+    legs of cfg3_legs (signatures (1,1,-1,-1), 595 blocks each), real and imaginary parts of
+    every entry N(0,1) drawn from default_rng(0) (A: real part, imaginary part; then B);
+    tensordot(A, B, ((2,3),(0,1))) under the default policy, then
+    svd_with_truncation(C, axes=((0,1),(2,3)), tol=1e-8)."""
+    cfg = yastn.make_config(sym='U1xU1', backend='np', default_dtype='complex128')
+    ts, Ds = cfg3_legs()
+    legs = [yastn.Leg(cfg, s=sg, t=ts, D=Ds) for sg in (1, 1, -1, -1)]
+    A = yastn.zeros(cfg, legs=legs, dtype='complex128')
+    B = yastn.zeros(cfg, legs=legs, dtype='complex128')
+    rng = np.random.default_rng(0)
+    for T in (A, B):
+        T._data = rng.normal(size=T.size) + 1j * rng.normal(size=T.size)
+    rec = Recorder(bnp, big=5000)
+    C = yastn.tensordot(A, B, axes=((2, 3), (0, 1)))
+    U, S, V = yastn.svd_with_truncation(C, axes=((0, 1), (2, 3)), tol=1e-8)
+    rec.restore()
+    scall = [c for c in rec.calls if c['fn'] == 'svd'][0]
+    extra = {'leg_t': [list(t) for t in ts], 'leg_D': list(Ds), 'signatures': [1, 1, -1, -1], 'seed': 0,
+             'n_blocks': len(A.struct.t), 'A_size': int(A.size), 'B_size': int(B.size),
+             'C_checksum': checksum(C._data), 'S_kept_t': [list(t) for t in S.struct.t],
+             'S_kept_D': [list(d) for d in S.struct.D], 'S_kept_checksum': checksum(S._data),
+             'svd_S_checksum': scall['out'][1].get('checksum') if isinstance(scall['out'][1], dict) else None}
+    save('cfg3', rec, extra)
+
+
 def _arr_from(rec, x):
     return rec.arrays[x['__array__']]
 
@@ -577,4 +618,5 @@ if __name__ == '__main__':
     scen_tds_adjoint()
     scen_cfg1()
     scen_cfg2()
+    scen_cfg3()
     scen_cfg5()

@@ -145,6 +145,25 @@ def test_cfg1_fixture_consistent_with_regenerated_inputs():
     assert second.checksum['head0'] == [float(x) for x in B[:8]]
 
 
+def test_cfg3_replay_matches_reference_checksum():
+    """The U(1)xU(1) complex workload regenerates from its seed and the oracle's tensordot
+    (two merges and 595 complex sector GEMMs) reproduces the reference's checksum of C."""
+    from yastn_gb300.workloads import cfg3_inputs
+    tr = load_trace('cfg3')
+    A, B = cfg3_inputs(tr)
+    c0, c1, c2 = tr['calls'][:3]
+    assert c0['args'][0].checksum['head0'] == [float(x) for x in A.real[:8]]
+    assert c1['args'][0].checksum['head1'] == [float(x) for x in B.imag[:8]]
+    Am = oracle.transpose_and_merge(A, *c0['args'][1:])
+    Bm = oracle.transpose_and_merge(B, *c1['args'][1:])
+    C = oracle.dot(Am, Bm, *c2['args'][2:])
+    chk = tr['C_checksum']
+    assert C.size == chk['n']
+    for i, part in enumerate((C.real, C.imag)):
+        assert abs(float(part.sum()) - chk[f'sum{i}']) <= 1e-10 * chk[f'abs{i}']
+        assert abs(float((part * part).sum()) - chk[f'sq{i}']) <= 1e-10 * chk[f'sq{i}']
+
+
 def test_cfg5_replay_matches_reference_checksum():
     """The precision-study workload (per-block scales over four decades) regenerates from
     its seeds, and the oracle's tensordot reproduces the reference's result checksum."""

@@ -75,6 +75,16 @@ def cfg1_inputs(trace=None):
     return A, B
 
 
+def cfg3_inputs(trace=None):
+    """Data of the U(1)xU(1) complex128 tensors: real and imaginary parts N(0,1) from
+    ``default_rng(seed)``, A's real part, A's imaginary part, then B's."""
+    trace = trace or load_trace('cfg3')
+    rng = np.random.default_rng(trace['seed'])
+    A = rng.normal(size=trace['A_size']) + 1j * rng.normal(size=trace['A_size'])
+    B = rng.normal(size=trace['B_size']) + 1j * rng.normal(size=trace['B_size'])
+    return A, B
+
+
 def cfg5_inputs(trace=None):
     """Data of the precision-study tensors (U(1), D=128 per leg over t=-16..16).
 
