@@ -441,6 +441,18 @@ def truncation_mask_data(S, slices, charges=None, tol=0, tol_block=0, D_block=fl
         raise TypeError("truncation requires a real float64 spectrum")
     n = S.numel()
     nb = len(slices)
+    # the kernel locates blocks by binary search over ascending starts: order them here and
+    # return the kept counts in the caller's order
+    order = sorted(range(nb), key=lambda i: slices[i][0])
+    if order != list(range(nb)):
+        slices = [slices[i] for i in order]
+        charges = None if charges is None else [charges[i] for i in order]
+        mask, kept_sorted = truncation_mask_data(S, slices, charges, tol, tol_block, D_block, D_total,
+                                                 truncate_multiplets)
+        kept = [0] * nb
+        for j, i in enumerate(order):
+            kept[i] = kept_sorted[j]
+        return mask, kept
     if truncate_multiplets:
         tol_block, D_block = 0, float('inf')
     blk = np.zeros((max(nb, 1), 4), dtype=np.int64)
