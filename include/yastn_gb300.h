@@ -235,6 +235,16 @@ int yb_svd_finalize(const void* work, void* U, double* S, void* Vh, const int64_
 int yb_svd_adjoint_core(const void* P, const void* Q, const double* S, const double* gS, void* K,
                         const void* gU, const void* gVh, void* TR, const int64_t* blocks,
                         int n_blocks, int dtype, void* stream);
+/* yb_eigh_adjoint_core: the inner matrix K of the eigh adjoint dA = U K op(U)^T per block,
+ * from X = op(U)^T gU (k x k, grouped GEMM): symeig != 0 (order_by_magnitude, SYMEIG of
+ * yastn/backend/linalg/torch_eig_sym.py:43-54, op(U) = U): K_ij = X_ij (d_j - d_i) /
+ * ((d_j - d_i)^2 + eps); symeig == 0 (torch.linalg.eigh's adjoint, op(U) = conj(U)):
+ * K_ij = (X_ij - conj X_ji) / (2 (d_j - d_i)); K_ii = gD_i (gD may be NULL: 0, or
+ * i Im X_ii for symeig == 0). blocks: records of 4 int64 (X/K offset, k, d offset, 0).
+ * Replaces SYMEIG.backward and torch.linalg.eigh's backward (backend_torch.py:369-384). */
+int yb_eigh_adjoint_core(const void* X, const double* D, const double* gD, void* K,
+                         const int64_t* blocks, int n_blocks, int dtype, int symeig, double eps,
+                         void* stream);
 
 /* ==== masks / gauge ================================================================== */
 /* Gather along one axis: out[sln].reshape(pre, Dn_ax, post)[:, i, :] =

@@ -17,7 +17,7 @@ __all__ = [
     'unmerge', 'unmerge_backward',
     'dot', 'dot_backward', 'transpose_dot_sum', 'transpose_dot_sum_backward',
     'svd', 'svd_block_backward', 'svd_backward',
-    'eigh', 'eigh_block_backward', 'fix_svd_signs',
+    'eigh', 'eigh_block_backward', 'eigh_block_backward_hermitian', 'eigh_backward', 'fix_svd_signs',
     'apply_mask', 'apply_mask_backward', 'embed_mask',
     'truncation_mask', 'rand_normal',
 ]
@@ -317,6 +317,37 @@ def eigh_block_backward(d, u, gd, gu, eps=1.0e-12):
     if gu is not None:
         inner = inner + F * (ut @ gu)
     return u @ inner @ ut
+
+
+def eigh_block_backward_hermitian(d, u, gd, gu):
+    """Adjoint of torch.linalg.eigh, the path of ``eigh`` without order_by_magnitude
+    (backend_torch.py:376-378): U (diag(gD) + skew(U^H gU) / E) U^H with skew(X) =
+    (X - X^H) / 2 and E_ij = d_j - d_i (E_ii = 1; the diagonal is gD when given)."""
+    X = u.conj().T @ gu if gu is not None else np.zeros((len(d), len(d)), dtype=u.dtype)
+    X = 0.5 * (X - X.conj().T)
+    E = d[None, :] - d[:, None]
+    np.fill_diagonal(E, 1.0)
+    inner = X / E
+    if gd is not None:
+        np.fill_diagonal(inner, gd)
+    return u @ inner @ u.conj().T
+
+
+def eigh_backward(U, S, gU, gS, meta, data_size, dtype, order_by_magnitude=False, eps=1.0e-12):
+    """Adjoint of ``eigh`` over all blocks: SYMEIG's broadened formula when
+    ``order_by_magnitude`` (torch_eig_sym.py:43-54), torch.linalg.eigh's otherwise."""
+    out = np.zeros(data_size, dtype=dtype)
+    for sl, D, slU, DU, slS in meta:
+        u = U[_sl(slU)].reshape(DU)
+        d = S[_sl(slS)]
+        gu = None if gU is None else gU[_sl(slU)].reshape(DU)
+        gd = None if gS is None else gS[_sl(slS)]
+        if order_by_magnitude:
+            blk = eigh_block_backward(d, u, gd, gu, eps)
+        else:
+            blk = eigh_block_backward_hermitian(d, u, gd, gu)
+        out[_sl(sl)] = blk.ravel()
+    return out
 
 
 # ---------------------------------------------------------------- masks

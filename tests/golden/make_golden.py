@@ -389,6 +389,56 @@ def scen_adjoints():
     print(f"adjoints: {len(calls)} calls")
 
 
+def scen_eigh_adjoint():
+    """Reference eigh adjoints from the torch backend on CPU (backend_torch.py:369-384):
+    order_by_magnitude=True goes through SYMEIG (torch_eig_sym.py:43-54, broadened F,
+    ad_decomp_reg=1e-12), False through torch.linalg.eigh's own adjoint. Blocks of 5, 8, 3
+    (one with a degenerate pair); real symmetric for both modes, complex Hermitian for the
+    torch.linalg.eigh mode with a cotangent whose diag(U^H gU) is real (gauge invariant)."""
+    import torch
+    import yastn.backend.backend_torch as bt
+    g = torch.Generator().manual_seed(21)
+    arrays, calls = {}, []
+
+    def put(x):
+        key = f"a{len(arrays)}"
+        arrays[key] = x.detach().resolve_conj().cpu().numpy().copy()
+        return key
+
+    for dtype, by_mag in ((torch.float64, True), (torch.float64, False), (torch.complex128, False)):
+        sizes_ = [5, 8, 3]
+        meta, off, offU, offS, parts = [], 0, 0, 0, []
+        for i, d in enumerate(sizes_):
+            a = torch.randn(d, d, dtype=dtype, generator=g)
+            h = a + a.mH
+            if i == 1:  # a degenerate pair: eigenvalues (1, 1, ...) in a random basis
+                q, _ = torch.linalg.qr(torch.randn(d, d, dtype=dtype, generator=g))
+                ev = torch.linspace(-3, 4, d, dtype=torch.float64)
+                ev[2] = ev[3]
+                h = (q * ev.to(dtype)) @ q.mH
+            parts.append(h.reshape(-1))
+            meta.append(((off, off + d * d), (d, d), (offU, offU + d * d), (d, d), (offS, offS + d)))
+            off += d * d; offU += d * d; offS += d
+        data = torch.cat(parts)
+        d_ = data.clone().requires_grad_(True)
+        S, U = bt.eigh(d_, tuple(meta), (offS, offU), order_by_magnitude=by_mag)
+        gS = torch.randn(offS, dtype=torch.float64, generator=g)
+        gU = torch.randn(offU, dtype=dtype, generator=g)
+        if dtype.is_complex:  # remove the gauge-dependent part: diag(U^H gU) real
+            for sl, D, slU, DU, slS in meta:
+                u = U[slice(*slU)].detach().view(DU)
+                gu = gU[slice(*slU)].view(DU)
+                x = torch.diagonal(u.mH @ gu)
+                gu -= u * (1j * x.imag)
+        (grad,) = torch.autograd.grad((S, U), (d_,), grad_outputs=(gS, gU))
+        calls.append({'fn': 'eigh_backward', 'order_by_magnitude': by_mag, 'meta': meta, 'data': put(data),
+                      'S': put(S), 'U': put(U), 'gS': put(gS), 'gU': put(gU), 'grad': put(grad)})
+    with open(os.path.join(HERE, 'eigh_adjoint.json'), 'w') as f:
+        json.dump({'scenario': 'eigh_adjoint', 'calls': calls}, f, separators=(',', ':'))
+    np.savez_compressed(os.path.join(HERE, 'eigh_adjoint.npz'), **arrays)
+    print(f"eigh_adjoint: {len(calls)} calls")
+
+
 def scen_svd_ill():
     """The ill-conditioned fixture of the reference tests (test_svd.py:335-341), where
     LAPACK gesdd can fail; records the backend calls of its truncated SVD."""
@@ -614,6 +664,7 @@ if __name__ == '__main__':
     scen_truncation()
     scen_eigh()
     scen_adjoints()
+    scen_eigh_adjoint()
     scen_svd_ill()
     scen_tds_adjoint()
     scen_cfg1()

@@ -260,3 +260,23 @@ def _sweeps(X, W, blocks, dtype, tol_stop, max_sweeps, eps):
         if all(conv): break
     return nsw, conv
 
+
+
+def eigh_adjoint_core(X, D, gD, recs, symeig, eps=1.0e-12):
+    """The inner-matrix kernel of csrc/yb_adjoint.cu (eigh_adjoint_core_kernel) with numpy."""
+    K = np.empty_like(X)
+    for off, k, doff, _ in (tuple(int(v) for v in r) for r in recs):
+        x = X[off:off + k * k].reshape(k, k)
+        d = D[doff:doff + k]
+        E = d[None, :] - d[:, None]
+        if symeig:
+            kb = x * (E / (E * E + eps))
+        else:
+            np.fill_diagonal(E, 1.0)
+            kb = 0.5 * (x - x.conj().T) / E
+        if gD is not None:
+            np.fill_diagonal(kb, gD[doff:doff + k])
+        elif symeig:
+            np.fill_diagonal(kb, 0)
+        K[off:off + k * k] = kb.ravel()
+    return K

@@ -127,3 +127,49 @@ def test_fix_signs_adjoint_real(cuda_device):
     u = dev(U).requires_grad_(True)
     v = dev(V).requires_grad_(True)
     assert torch.autograd.gradcheck(lambda a, b: B.fix_svd_signs(a, b, meta), (u, v), eps=1e-6, atol=1e-8)
+
+
+def test_eigh_adjoint_matches_reference_autograd(cuda_device):
+    """The eigh adjoint on the reference's own U, S and cotangents (SYMEIG path and
+    torch.linalg.eigh path, real and complex, a degenerate pair included)."""
+    import json, os
+    from yastn_gb300 import ops
+    from yastn_gb300.workloads import GOLDEN, _decode
+    with open(os.path.join(GOLDEN, 'eigh_adjoint.json')) as f:
+        calls = json.load(f)['calls']
+    z = np.load(os.path.join(GOLDEN, 'eigh_adjoint.npz'))
+    for c in calls:
+        meta = _decode(c['meta'], None)
+        U, S, gU, gS, ref = (torch.from_numpy(z[c[k]]).cuda() for k in ('U', 'S', 'gU', 'gS', 'grad'))
+        g = ops.eigh_backward(U, S, gU, gS, meta, ref.numel(), ref.dtype, c['order_by_magnitude']).cpu().numpy()
+        r = ref.cpu().numpy()
+        assert np.abs(g - r).max() <= 1e-10 * np.abs(r).max(), c['order_by_magnitude']
+
+
+@pytest.mark.parametrize('by_mag', [False, True])
+def test_gradcheck_eigh(by_mag, cuda_device):
+    """Finite differences of a gauge-invariant loss through the backend's eigh."""
+    from yastn_gb300 import backend as BK
+    rng = np.random.default_rng(4)
+    meta, off, offU, offS, parts = [], 0, 0, 0, []
+    for d in (4, 6):
+        a = rng.normal(size=(d, d))
+        parts.append((a + a.T).ravel())
+        meta.append(((off, off + d * d), (d, d), (offU, offU + d * d), (d, d), (offS, offS + d)))
+        off += d * d; offU += d * d; offS += d
+    meta = tuple(meta)
+    data = torch.from_numpy(np.concatenate(parts)).cuda().requires_grad_(True)
+    w = torch.from_numpy(rng.normal(size=offS)).cuda()
+
+    def loss(x):
+        S, U = BK.eigh(x, meta, (offS, offU), order_by_magnitude=by_mag)
+        # eigenvalues and a gauge-invariant function of the eigenvectors (|U|^4)
+        return (S * w).sum() + (U.abs() ** 4).sum()
+
+    def sym(x):  # keep the perturbation symmetric per block
+        out = []
+        for sl, D, *_ in meta:
+            b = x[sl[0]:sl[1]].view(D)
+            out.append(((b + b.T) / 2).reshape(-1))
+        return torch.cat(out)
+    assert torch.autograd.gradcheck(lambda x: loss(sym(x)), (data,), eps=1e-6, atol=1e-6, rtol=1e-5)

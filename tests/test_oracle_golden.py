@@ -183,6 +183,21 @@ def test_cfg5_replay_matches_reference_checksum():
     assert abs(float((C * C).sum()) - chk['sq0']) <= 1e-10 * chk['sq0']
 
 
+def test_oracle_eigh_adjoint_matches_reference_autograd():
+    """Both eigh adjoints (SYMEIG with order_by_magnitude, torch.linalg.eigh otherwise; real
+    and complex Hermitian, a degenerate pair included) against the reference's autograd."""
+    import numpy as np
+    from yastn_gb300.workloads import GOLDEN, _decode
+    with open(os.path.join(GOLDEN, 'eigh_adjoint.json')) as f:
+        calls = json.load(f)['calls']
+    z = np.load(os.path.join(GOLDEN, 'eigh_adjoint.npz'))
+    for c in calls:
+        meta = _decode(c['meta'], None)
+        g = oracle.eigh_backward(z[c['U']], z[c['S']], z[c['gU']], z[c['gS']], meta, z[c['data']].size,
+                                 z[c['data']].dtype, c['order_by_magnitude'])
+        assert _rel(g, z[c['grad']]) < 1e-10, c['order_by_magnitude']
+
+
 def test_oracle_tds_adjoint_matches_reference_autograd():
     import numpy as np
     from yastn_gb300.workloads import GOLDEN

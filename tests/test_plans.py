@@ -297,6 +297,25 @@ def test_mixed_precision_jacobi_schedule_complex():
         assert np.abs(np.sort(s)[::-1] - Sr[mt[4][0]:mt[4][1]]).max() <= 1e-13 * max(s.max(), 1.0)
 
 
+def test_eigh_adjoint_plan_reproduces_reference_autograd():
+    """X = op(U)^T gU, the inner matrix, T = U K, dA = T op(U)^T on the packed records
+    reproduce the reference's eigh gradients (SYMEIG and torch.linalg.eigh, real and complex)."""
+    import json, os
+    from yastn_gb300.workloads import GOLDEN, _decode
+    with open(os.path.join(GOLDEN, 'eigh_adjoint.json')) as f:
+        calls = json.load(f)['calls']
+    z = np.load(os.path.join(GOLDEN, 'eigh_adjoint.npz'))
+    for c in calls:
+        meta = _decode(c['meta'], None)
+        U, S, gU, gS, ref = (z[c[k]] for k in ('U', 'S', 'gU', 'gS', 'grad'))
+        plan = P.eigh_adjoint_plan(meta, c['order_by_magnitude'], np.iscomplexobj(U))
+        X = PI.run_gemm(plan.gX, U, gU, np.zeros(plan.kk, dtype=U.dtype))
+        K = PI.eigh_adjoint_core(X, S, gS, plan.recs, c['order_by_magnitude'])
+        T = PI.run_gemm(plan.gT, U, K, np.zeros(plan.kk, dtype=U.dtype))
+        dA = PI.run_gemm(plan.gA, T, U, np.zeros(ref.size, dtype=ref.dtype))
+        assert np.abs(dA - ref).max() <= 1e-10 * np.abs(ref).max(), c['order_by_magnitude']
+
+
 def _ozaki_digits(x, s):
     """NumPy restatement of the split of csrc/yb_ozaki.cu (rows of x): balanced base-128
     digits of Q = rint(x 2^{7s-e}) extracted from the low end with integer arithmetic."""

@@ -28,6 +28,7 @@ SIGNATURES = {
     'yb_svd_shift_prefill': ([_vp, _vp, _i, _i, _vp, _vp], _i),
     'yb_svd_finalize': ([_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp, _vp], _i),
     'yb_svd_adjoint_core': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
+    'yb_eigh_adjoint_core': ([_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _vp], _i),
     'yb_mask_gather': ([_vp, _vp, _i, _vp, _vp, _i, _vp, _i, _vp], _i),
     'yb_fix_signs': ([_vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp], _i),
     'yb_ozaki_split': ([_vp, _vp, _vp, _vp, _i, _i, _i, _vp], _i),

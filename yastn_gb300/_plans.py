@@ -590,6 +590,36 @@ def svd_adjoint_plan(meta):
     return CACHE.get((meta,), ('svd_adjoint',), build)
 
 
+class EighAdjointPlan:
+    def __init__(self, recs, kk, gX, gT, gA):
+        self.recs, self.kk, self.gX, self.gT, self.gA = recs, kk, gX, gT, gA
+        self._dev = {}
+
+
+def eigh_adjoint_plan(meta, symeig, cplx):
+    """Grouped-GEMM plans of the eigh adjoint dA = U K op(U)^T on all blocks (records
+    (sl, D, slU, DU, slS) of yastn/backend/backend_np.py:461-474): X = op(U)^T gU, then
+    T = U K, dA = T op(U)^T; op(U) = U for SYMEIG (torch_eig_sym.py:43-54), conj(U) for
+    torch.linalg.eigh's adjoint (complex data)."""
+    def build():
+        conj = int(cplx and not symeig)
+        recs, lX, lT, lA = [], [], [], []
+        kk = 0
+        for sl, D, slU, DU, slS in meta:
+            k = DU[1]
+            if k == 0:
+                continue
+            m = DU[0]
+            recs.append((kk, k, slS[0], 0))
+            lX.append((kk, k, k, k, [(slU[0], slU[0], m, 1, k, k, 1, conj)]))   # X = op(U)^T gU
+            lT.append((kk, m, k, k, [(slU[0], kk, k, k, 1, k, 1, 0)]))          # T = U K (into the X buffer)
+            lA.append((sl[0], m, m, m, [(kk, slU[0], k, k, 1, 1, k, 2 * conj)]))  # dA = T op(U)^T
+            kk += k * k
+        recs = np.array(recs, dtype=np.int64).reshape(-1, 4)
+        return EighAdjointPlan(recs, kk, _pack_gemm(lX), _pack_gemm(lT), _pack_gemm(lA))
+    return CACHE.get((meta,), ('eigh_adjoint', bool(symeig), bool(cplx)), build)
+
+
 def tds_backward_plans(meta_dot, Areshape, Breshape, Aoffs, Boffs):
     """Adjoint of transpose_dot_sum on the permuted (Dl, Dr) operand matrices:
     At_b[a] = sum C_b[sl] Bt[b]^H, Bt_b[b] = sum At[a]^H C_b[sl] (grouped by operand)."""

@@ -203,6 +203,26 @@ class _Svd(torch.autograd.Function):
         return dA, None, None, None, None, None
 
 
+class _Eigh(torch.autograd.Function):
+    """eigh (backend_torch.py:369-384): batched Jacobi forward; the adjoint of SYMEIG
+    (order_by_magnitude, yastn/backend/linalg/torch_eig_sym.py:43-54) or of
+    torch.linalg.eigh, on all blocks at once."""
+
+    @staticmethod
+    def forward(ctx, data, meta, sizes, order_by_magnitude, ad_decomp_reg):
+        S, U = ops.eigh(data, meta, sizes, order_by_magnitude)
+        ctx.save_for_backward(S, U)
+        ctx.meta, ctx.n, ctx.dtype = meta, data.numel(), data.dtype
+        ctx.by_mag, ctx.eps = order_by_magnitude, ad_decomp_reg
+        return S, U
+
+    @staticmethod
+    def backward(ctx, gS, gU):
+        S, U = ctx.saved_tensors
+        dA = ops.eigh_backward(U, S, gU, gS, ctx.meta, ctx.n, ctx.dtype, ctx.by_mag, ctx.eps)
+        return dA, None, None, None, None
+
+
 class _FixSigns(torch.autograd.Function):
     """fix_svd_signs (backend_torch.py:353-366) for real data: the phases are +-1 and
     constant almost everywhere, so the adjoint multiplies the cotangents by them."""
@@ -542,7 +562,7 @@ def pinv(A, rcond=None, hermitian=False, out=None, atol=None, rtol=None):
 def eigh(data, meta=None, sizes=(1, 1), order_by_magnitude=False, ad_decomp_reg=1.0e-12):
     if meta is None:
         _not_hot('eigh of a single dense matrix')
-    return ops.eigh(data, meta, sizes, order_by_magnitude)
+    return _Eigh.apply(data, meta, sizes, order_by_magnitude, ad_decomp_reg)
 
 
 @torch.no_grad()

@@ -110,8 +110,70 @@ __global__ void svd_adjoint_core_kernel(const typename Elt<Cx>::T* __restrict__ 
   }
 }
 
+// Adjoint of the block Hermitian eigendecomposition A = U diag(d) U^H. X = op(U)^T gU
+// (k x k per block, from the grouped GEMM) becomes the inner matrix K of dA = U K op(U)^T:
+//   symeig (order by magnitude, yastn/backend/linalg/torch_eig_sym.py:43-54; op(U) = U):
+//     K_ij = r_eps(d_j - d_i) X_ij off the diagonal, K_ii = gd_i
+//   torch.linalg.eigh (op(U) = conj(U)):
+//     K_ij = (X_ij - conj X_ji) / (2 (d_j - d_i)) off the diagonal, K_ii = gd_i, or
+//     i Im(X_ii) without gd
+// with r_eps(x) = x / (x^2 + eps). Record per block: [0] X/K offset [1] k [2] d offset.
+template <bool Cx>
+__global__ void eigh_adjoint_core_kernel(const typename Elt<Cx>::T* __restrict__ X, const double* __restrict__ D,
+                                         const double* __restrict__ gD, typename Elt<Cx>::T* __restrict__ K,
+                                         const int64_t* __restrict__ blocks, int symeig, double eps) {
+  using T = typename Elt<Cx>::T;
+  const int64_t* r = blocks + (int64_t)blockIdx.y * 4;
+  const int64_t off = r[0], k = r[1];
+  const double* d = D + r[2];
+  const T* Xb = X + off;
+  T* Kb = K + off;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < k * k; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / k, j = e - i * k;
+    T v;
+    if (i == j) {
+      const double g = gD ? gD[r[2] + i] : 0.0;
+      if constexpr (Cx) v = make_double2(g, (symeig || gD) ? 0.0 : Xb[e].y);
+      else v = g;
+    } else {
+      const double x = d[j] - d[i];
+      if (symeig) {
+        const double f = x / (x * x + eps);
+        if constexpr (Cx) v = make_double2(f * Xb[e].x, f * Xb[e].y);
+        else v = f * Xb[e];
+      } else {
+        const double f = 0.5 / x;
+        if constexpr (Cx) {
+          const double2 a = Xb[e], b = Xb[j * k + i];
+          v = make_double2(f * (a.x - b.x), f * (a.y + b.y));
+        } else {
+          v = f * (Xb[e] - Xb[j * k + i]);
+        }
+      }
+    }
+    Kb[e] = v;
+  }
+}
+
 }  // namespace
 }  // namespace yb
+
+extern "C" int yb_eigh_adjoint_core(const void* X, const double* D, const double* gD, void* K,
+                                    const int64_t* blocks, int n_blocks, int dtype, int symeig, double eps,
+                                    void* stream) {
+  if (n_blocks == 0) return YB_OK;
+  if (!X || !D || !K || !blocks) return YB_ERR_INVALID;
+  dim3 grid(16, (unsigned)n_blocks);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == YB_F64)
+    yb::eigh_adjoint_core_kernel<false><<<grid, 256, 0, s>>>((const double*)X, D, gD, (double*)K, blocks, symeig, eps);
+  else if (dtype == YB_C128)
+    yb::eigh_adjoint_core_kernel<true><<<grid, 256, 0, s>>>((const double2*)X, D, gD, (double2*)K, blocks, symeig,
+                                                            eps);
+  else
+    return YB_ERR_INVALID;
+  return yb::check_launch();
+}
 
 extern "C" int yb_svd_adjoint_core(const void* P, const void* Q, const double* S, const double* gS, void* K,
                                    const void* gU, const void* gVh, void* TR, const int64_t* blocks, int n_blocks,

@@ -344,8 +344,6 @@ def eigh(data, meta, sizes, order_by_magnitude=False, max_sweeps=MAX_SWEEPS):
     yastn/backend/backend_np.py:461-474): eigenvalues ascending, or by descending
     magnitude when ``order_by_magnitude`` (yastn/backend/linalg/torch_eig_sym.py:25-32)."""
     data = _check(data)
-    if data.requires_grad:
-        raise NotImplementedError("yastn_gb300 eigh: the adjoint is not implemented yet")
     dev = data.device
     S = torch.zeros(sizes[0], dtype=torch.float64, device=dev)
     U = torch.zeros(sizes[1], dtype=data.dtype, device=dev)
@@ -355,6 +353,29 @@ def eigh(data, meta, sizes, order_by_magnitude=False, max_sweeps=MAX_SWEEPS):
         return S, U
     _jacobi(data, plan, U, S, None, 2 if order_by_magnitude else 1, max_sweeps)
     return S, U
+
+
+def eigh_backward(U, S, gU, gS, meta, data_size, dtype, order_by_magnitude=False, eps=1.0e-12):
+    """Adjoint of ``eigh`` on every block in 4 launches: X = op(U)^T gU, the inner matrix K
+    (csrc/yb_adjoint.cu), T = U K, dA = T op(U)^T. order_by_magnitude follows SYMEIG
+    (yastn/backend/linalg/torch_eig_sym.py:43-54), otherwise torch.linalg.eigh's adjoint."""
+    cplx = U.is_complex()
+    plan = P.eigh_adjoint_plan(meta, bool(order_by_magnitude), cplx)
+    dev = U.device
+    dA = torch.zeros(data_size, dtype=dtype, device=dev)
+    if len(plan.recs) == 0:
+        return dA
+    gU = torch.zeros_like(U) if gU is None else gU.contiguous().to(U.dtype)
+    gS = None if gS is None else gS.contiguous().to(torch.float64)
+    X = torch.empty(plan.kk, dtype=U.dtype, device=dev)
+    K = torch.empty(plan.kk, dtype=U.dtype, device=dev)
+    run_gemm(plan.gX, U, gU, X)
+    (drecs,) = _dev(plan, 'eigh_adj', (plan.recs,), dev)
+    N.call('yb_eigh_adjoint_core', _ptr(X), _ptr(S), _vp(gS.data_ptr() if gS is not None else 0), _ptr(K),
+           _ptr(drecs), len(plan.recs), _dtype_code(U.dtype), int(bool(order_by_magnitude)), float(eps), _stream())
+    run_gemm(plan.gT, U, K, X)
+    run_gemm(plan.gA, X, U, dA)
+    return dA
 
 
 def fix_svd_signs(U, V, meta):
