@@ -54,6 +54,8 @@ def parse():
     p.add_argument('--gemm', default='emulated', choices=['emulated', 'fp64'],
                    help='sector-GEMM mode of the headline (cfg2)')
     p.add_argument('--no-svd', action='store_true', help='skip the extra svd_with_truncation timing')
+    p.add_argument('--headline-only', action='store_true',
+                   help='cfg2: run only the headline GEMM mode (for kernel launch lists)')
     return p.parse_args()
 
 
@@ -621,7 +623,10 @@ def run_gpu_cfg2(args, wl):
         torch.cuda.synchronize()
 
     results = {}
-    for mode in (['fp64', 'emulated'] if args.gemm == 'emulated' else ['fp64']):
+    modes = ['fp64', 'emulated'] if args.gemm == 'emulated' else ['fp64']
+    if args.headline_only:
+        modes = [args.gemm]
+    for mode in modes:
         BK.set_gemm_mode(mode)
         v0 = h_v0.to(dev)
         # eager run: parity with the reference's eigs, and plan/device caches warmed
