@@ -139,6 +139,16 @@ int yb_ozaki_split(const double* src, void* slices, int* exps, const int64_t* re
 int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps,
                   double* c, const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
                   void* stream);
+/* yb_ozaki_gemm_tc: yb_ozaki_gemm on the tcgen05 tensor cores with the 8 digit-diagonal
+ * accumulators in tensor memory. Same records; tiles are (output, tile row, tile col, 0)
+ * of 128 rows x 64 columns. A CTA that gives up on a bounded wait writes nothing for its
+ * tile and sets the status word read by yb_ozaki_device_error. */
+int yb_ozaki_gemm_tc(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps,
+                     double* c, const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
+                     void* stream);
+/* yb_ozaki_device_error: copies the tcgen05 kernel's status word to *out (0: no failure),
+ * synchronising the stream, and clears it when reset != 0. */
+int yb_ozaki_device_error(int* out, int reset, void* stream);
 
 /* yb_ozaki_dot_static: yb_ozaki_split (A), yb_block_copy + yb_ozaki_split (B) and
  * yb_ozaki_gemm in one call, with all scratch (digit planes, exponents, transposed B)

@@ -183,3 +183,31 @@ def test_dot_small_and_ragged_sectors(emulated, cuda_device):
     for slc, Dc, *_ in meta:
         r, g = ref[slc[0]:slc[1]], got[slc[0]:slc[1]]
         assert np.abs(g - r).max() <= TOL * max(np.abs(r).max(), 1e-300), Dc
+
+
+@pytest.mark.parametrize('name', ['cfg1', 'small'])
+def test_ozaki_tcgen05_matches_mma_sync(name, cuda_device):
+    """The tcgen05/TMEM kernel and the mma.sync kernel form the same exact diagonal sums and
+    the same folds: their products agree bit for bit; no CTA reports a failed wait."""
+    if name == 'cfg1':
+        tr = load_trace('cfg1')
+        A, B = cfg1_inputs(tr)
+        c0, c1, c2 = tr['calls'][:3]
+        A = oracle.transpose_and_merge(A, *c0['args'][1:])
+        B = oracle.transpose_and_merge(B, *c1['args'][1:])
+        _, _, meta, Dsize = c2['args']
+    else:
+        meta, A, B, Dsize = _small_sector_problem(22)
+    saved = ops.OZAKI_TC[0]
+    try:
+        ops.OZAKI_TC[0] = True
+        assert ops.ozaki_device_error(reset=True) == 0
+        got_tc = host(ops.dot_ozaki(dev(A), dev(B), meta, Dsize))
+        assert ops.ozaki_device_error(reset=True) == 0
+        ops.OZAKI_TC[0] = False
+        got_mma = host(ops.dot_ozaki(dev(A), dev(B), meta, Dsize))
+    finally:
+        ops.OZAKI_TC[0] = saved
+    np.testing.assert_array_equal(got_tc, got_mma)
+    ref = oracle.dot(A, B, meta, Dsize)
+    assert rel(got_tc, ref) <= TOL

@@ -393,6 +393,7 @@ class OzakiPlan:
         self._dev = {}
 
 
+OZAKI_TC_M, OZAKI_TC_N = 128, 64  # output tile of the tcgen05 emulated GEMM
 OZAKI_MIN_DIM = 16  # sector GEMMs contracting fewer indices than this stay on the native FP64 kernel
 
 
@@ -441,6 +442,15 @@ def ozaki_dot_plan(meta_dot, s):
                     tiles.append((K, oi, tr, tc))
         tiles.sort(key=lambda x: -x[0])
         tiles = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles], dtype=np.int32).reshape(-1, 4)
+        # 128 x 64 tiles of the tcgen05 kernel
+        tiles_tc = []
+        for oi, o in enumerate(outs):
+            m, n, K = int(o[1]), int(o[2]), int(o[8])
+            for tr in range((m + OZAKI_TC_M - 1) // OZAKI_TC_M):
+                for tc in range((n + OZAKI_TC_N - 1) // OZAKI_TC_N):
+                    tiles_tc.append((K, oi, tr, tc))
+        tiles_tc.sort(key=lambda x: -x[0])
+        tiles_tc = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles_tc], dtype=np.int32).reshape(-1, 4)
         a_recs = np.array(a_recs, dtype=np.int64).reshape(-1, 8)
         b_recs = np.array(b_recs, dtype=np.int64).reshape(-1, 8)
         a_rows = int(a_recs[:, 1].max()) if len(a_recs) else 0
@@ -449,6 +459,7 @@ def ozaki_dot_plan(meta_dot, s):
         plan.bT = CopyPlan([t for t in bT_tasks if t[2][0] * t[2][1] > 0], bT_size, bT_size)
         plan.bT_size = bT_size
         plan.native = _pack_gemm(small)
+        plan.tiles_tc = tiles_tc
         return plan
     return CACHE.get((meta_dot,), ('ozaki_dot', s), build)
 

@@ -295,6 +295,224 @@ int launch_gemm(const void* As, const int* Ae, const void* Bs, const int* Be, do
   return check_launch();
 }
 
+// ------------------------------------------------------------------ GEMM, tcgen05 / TMEM
+// The same products on the 5th-generation tensor cores: a CTA computes a 128 x 64 output
+// tile; the 8 digit diagonals are FP32 accumulators of 128 lanes x 64 columns in tensor
+// memory (8 x 64 = all 512 TMEM columns, so one CTA per SM). One thread issues the 36
+// tcgen05.mma (M=128, N=64, K=16, BF16 -> FP32) of a K-step, reading the digit tiles from
+// shared memory through matrix descriptors (canonical K-major layout without swizzle:
+// 8 x 16-byte core matrices, 128 bytes apart along K and 256 bytes apart along M/N);
+// tcgen05.commit arrives on the stage's mbarrier when they complete. The operands stream
+// through a 4-stage cp.async ring (48 KB per stage); a stage is refilled once the MMAs that
+// read it have completed. At the end of every 400-long K-chunk all 4 warps read their 32
+// TMEM lanes (tcgen05.ld) and fold the 8 diagonals exactly into two int64 halves and FP64
+// registers (the next chunk's first MMAs overwrite the accumulators). Every mbarrier wait is
+// bounded: on a timeout the CTA records yb_ozaki_device_error, waits (bounded) for its
+// MMAs, frees its TMEM and writes nothing.
+constexpr int kTcM = 128;
+constexpr int kTcN = 64;
+constexpr int kTcStages = 4;
+constexpr int kTcThreads = 128;
+constexpr long long kTcSpinLimit = 1ll << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: canonical K-major, no swizzle, LBO = 128 B (between the two
+// 8-element core matrices of a 16-long K step), SBO = 256 B (between 8-row groups)
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
+         ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+  for (long long it = 0; it < kTcSpinLimit; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void tc_ld8(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+
+template <int S>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    ozaki_gemm_tc_kernel(const __nv_bfloat16* __restrict__ As, const int* __restrict__ Ae,
+                         const __nv_bfloat16* __restrict__ Bs, const int* __restrict__ Be, double* __restrict__ C,
+                         const int64_t* __restrict__ outs, const int32_t* __restrict__ tiles, int* __restrict__ err) {
+  constexpr uint32_t kATile = kTcM * kK * 2;  // 4096 B: one slice's 128 x 16 digit tile
+  constexpr uint32_t kBTile = kTcN * kK * 2;  // 2048 B
+  constexpr uint32_t kStage = S * (kATile + kBTile);
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ uint32_t tmem_slot;
+  __shared__ __align__(8) uint64_t mbar[kTcStages];
+  __shared__ int failed;
+  __shared__ long long last_step;  // last K-step whose MMAs were committed (-1: none)
+  const int4 tl = reinterpret_cast<const int4*>(tiles)[blockIdx.x];
+  const int64_t* o = outs + (int64_t)tl.x * 16;
+  const int64_t c_off = o[0], m = o[1], n = o[2], ldc = o[3];
+  const int64_t a_sl = o[4], a_ex = o[5], b_sl = o[6], b_ex = o[7], Kp = o[9];
+  const int64_t row0 = (int64_t)tl.y * kTcM, col0 = (int64_t)tl.z * kTcN;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t sbase = smem_u32(smem);
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int i = 0; i < kTcStages; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[i])));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    failed = 0;
+    last_step = -1;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_slot;
+
+  const int64_t a_stride = m * Kp, b_stride = n * Kp;
+  auto load = [&](int stage, int64_t k0) {
+    // S slices x (128 A rows + 64 B rows) x 2 chunks of 16 bytes
+    for (int c = tid; c < S * (kTcM + kTcN) * 2; c += kTcThreads) {
+      const bool isA = c < S * kTcM * 2;
+      const int cc = isA ? c : c - S * kTcM * 2;
+      const int rows = isA ? kTcM : kTcN;
+      const int t = cc / (rows * 2), rem = cc % (rows * 2), r = rem >> 1, half = rem & 1;
+      const uint32_t dst = (uint32_t)stage * kStage + (isA ? (uint32_t)t * kATile : S * kATile + (uint32_t)t * kBTile) +
+                           (uint32_t)(r >> 3) * 256 + (uint32_t)half * 128 + (uint32_t)(r & 7) * 16;
+      const int64_t g = (isA ? row0 : col0) + r;
+      const bool valid = g < (isA ? m : n);
+      const __nv_bfloat16* src = isA ? As + a_sl + t * a_stride + (valid ? g : 0) * Kp + k0 + half * 8
+                                     : Bs + b_sl + t * b_stride + (valid ? g : 0) * Kp + k0 + half * 8;
+      cp_async16(smem + dst, src, valid);
+    }
+    cp_async_commit();
+  };
+
+  const int64_t nsteps = Kp / kK;
+  for (int i = 0; i < kTcStages - 1; ++i) {
+    if (i < nsteps) load(i, (int64_t)i * kK); else cp_async_commit();
+  }
+  double acc64[kTcN];
+#pragma unroll
+  for (int j = 0; j < kTcN; ++j) acc64[j] = 0.0;
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
+                         ((uint32_t)(kTcM >> 4) << 24);  // F32 accumulate, BF16 A/B, K-major, N=64, M=128
+
+  for (int64_t st = 0; st < nsteps; ++st) {
+    const int stage = (int)(st % kTcStages);
+    asm volatile("cp.async.wait_group %0;" ::"n"(kTcStages - 2));
+    asm volatile("fence.proxy.async.shared::cta;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (tid == 0 && !failed) {
+      const bool first = (st % kChunkSteps) == 0;
+      const uint32_t a0 = sbase + (uint32_t)stage * kStage, b0 = a0 + S * kATile;
+#pragma unroll
+      for (int ta = 0; ta < S; ++ta)
+#pragma unroll
+        for (int tb = 0; tb < S - ta; ++tb)
+          tc_mma(tmem + (uint32_t)((ta + tb) * kTcN), umma_desc(a0 + ta * kATile), umma_desc(b0 + tb * kBTile), idesc,
+                 (first && ta == 0) ? 0u : 1u);
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(&mbar[stage])));
+      last_step = st;
+    }
+    // refill the stage of step st-1 with step st + kTcStages - 1 once its MMAs are done
+    const int64_t ls = st + kTcStages - 1;
+    if (ls < nsteps) {
+      if (st >= 1 && !mbar_wait(smem_u32(&mbar[(st - 1) % kTcStages]), (uint32_t)(((st - 1) / kTcStages) & 1)))
+        failed = 1;
+      load((int)(ls % kTcStages), ls * kK);
+    } else {
+      cp_async_commit();
+    }
+    if (((st + 1) % kChunkSteps) == 0 || st + 1 == nsteps) {
+      if (!mbar_wait(smem_u32(&mbar[stage]), (uint32_t)((st / kTcStages) & 1))) failed = 1;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      // fold the 8 diagonals of this thread's row exactly (integer pipe) into FP64
+#pragma unroll
+      for (int cb = 0; cb < kTcN / 8; ++cb) {
+        long long hi[8], lo[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) hi[j] = lo[j] = 0;
+#pragma unroll
+        for (int d = 0; d < S; ++d) {
+          uint32_t v[8];
+          tc_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(d * kTcN + cb * 8), v);
+          asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const long long q = (long long)__float2int_rn(__uint_as_float(v[j]));
+            if (d < 4) hi[j] += q << (7 * (3 - d));
+            else lo[j] += q << (7 * (S - 1 - d));
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          acc64[cb * 8 + j] += int_to_double_scaled(hi[j], -21) + int_to_double_scaled(lo[j], -7 * (S - 1));
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncthreads();  // every lane has read the accumulators before the next chunk overwrites them
+    }
+  }
+  asm volatile("cp.async.wait_group 0;");
+  __syncthreads();
+  if (failed) {
+    // MMAs complete in issue order: waiting for the last commit covers all of them
+    if (tid == 0) atomicExch(err, 1);
+    const long long ls_ = last_step;
+    if (ls_ >= 0) mbar_wait(smem_u32(&mbar[ls_ % kTcStages]), (uint32_t)((ls_ / kTcStages) & 1));
+  } else {
+    // epilogue through shared memory (the stages are free): row-major 128 x 64 doubles,
+    // padded rows; then coalesced stores with the row/column exponents applied
+    double* tileC = reinterpret_cast<double*>(smem);
+    const int r = warp * 32 + lane;
+#pragma unroll
+    for (int j = 0; j < kTcN; ++j) tileC[r * (kTcN + 1) + j] = acc64[j];
+    __syncthreads();
+    for (int e = tid; e < kTcM * kTcN; e += kTcThreads) {
+      const int rr = e / kTcN, cc = e % kTcN;
+      const int64_t gi = row0 + rr, gj = col0 + cc;
+      if (gi < m && gj < n)
+        C[c_off + gi * ldc + gj] = scale_pow2(tileC[rr * (kTcN + 1) + cc], Ae[a_ex + gi] + Be[b_ex + gj] - 14);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+}
+
+template <int S>
+int launch_gemm_tc(const void* As, const int* Ae, const void* Bs, const int* Be, double* C, const int64_t* outs,
+                   const int32_t* tiles, int n_tiles, int* err, cudaStream_t s) {
+  const size_t smem = (size_t)kTcStages * S * (kTcM + kTcN) * kK * 2;
+  static_assert((size_t)kTcM * (kTcN + 1) * 8 <= (size_t)kTcStages * 6 * (kTcM + kTcN) * kK * 2,
+                "epilogue tile must fit in the stage buffers");
+  cudaError_t e =
+      cudaFuncSetAttribute(ozaki_gemm_tc_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
+  ozaki_gemm_tc_kernel<S><<<n_tiles, kTcThreads, smem, s>>>((const __nv_bfloat16*)As, Ae, (const __nv_bfloat16*)Bs,
+                                                            Be, C, outs, tiles, err);
+  return check_launch();
+}
+
 }  // namespace
 }  // namespace yb
 
@@ -321,6 +539,39 @@ int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices,
     case 8: return yb::launch_gemm<8>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, s);
     default: return YB_ERR_INVALID;
   }
+}
+
+// Status word of the tcgen05 kernel (1 after a CTA gave up on a bounded wait).
+static __device__ int g_ozaki_tc_error;
+
+int yb_ozaki_gemm_tc(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps, double* c,
+                     const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count, void* stream) {
+  if (n_tiles == 0) return YB_OK;
+  if (!a_slices || !a_exps || !b_slices || !b_exps || !c || !outs || !tiles) return YB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  int* err = nullptr;
+  cudaError_t e = cudaGetSymbolAddress((void**)&err, g_ozaki_tc_error);
+  if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
+  switch (slices_count) {
+    case 6: return yb::launch_gemm_tc<6>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
+    case 7: return yb::launch_gemm_tc<7>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
+    case 8: return yb::launch_gemm_tc<8>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
+    default: return YB_ERR_INVALID;
+  }
+}
+
+int yb_ozaki_device_error(int* out, int reset, void* stream) {
+  if (!out) return YB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaMemcpyFromSymbolAsync(out, g_ozaki_tc_error, sizeof(int), 0, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && reset) {
+    const int zero = 0;
+    e = cudaMemcpyToSymbolAsync(g_ozaki_tc_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
+  return YB_OK;
 }
 
 }  // extern "C"

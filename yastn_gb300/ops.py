@@ -143,6 +143,9 @@ def dot(A, B, meta_dot, Dsize):
 OZAKI_SLICES = 8  # 57 bits per operand: FP64-grade products
 
 
+OZAKI_TC = [True]  # emulated GEMM on tcgen05/TMEM (False: the mma.sync kernel)
+
+
 def dot_ozaki(A, B, meta_dot, Dsize, slices=OZAKI_SLICES):
     """``dot`` with the FP64 sector GEMMs emulated on BF16 tensor cores (split operands).
 
@@ -160,7 +163,9 @@ def dot_ozaki(A, B, meta_dot, Dsize, slices=OZAKI_SLICES):
     if len(plan.tiles) == 0:
         return out
     dev = A.device
-    dar, dbr, dout, dtl = _dev(plan, 'ozaki', (plan.a_recs, plan.b_recs, plan.outs, plan.tiles), dev)
+    tc = OZAKI_TC[0]
+    dar, dbr, dout, dtl = _dev(plan, 'ozaki_tc' if tc else 'ozaki',
+                               (plan.a_recs, plan.b_recs, plan.outs, plan.tiles_tc if tc else plan.tiles), dev)
     a_sl = torch.empty(plan.a_size, dtype=torch.bfloat16, device=dev)
     b_sl = torch.empty(plan.b_size, dtype=torch.bfloat16, device=dev)
     a_ex = torch.empty(max(plan.a_exps, 1), dtype=torch.int32, device=dev)
@@ -169,9 +174,21 @@ def dot_ozaki(A, B, meta_dot, Dsize, slices=OZAKI_SLICES):
     st = _stream()
     N.call('yb_ozaki_split', _ptr(A), _ptr(a_sl), _ptr(a_ex), _ptr(dar), len(plan.a_recs), plan.a_rows, slices, st)
     N.call('yb_ozaki_split', _ptr(bT), _ptr(b_sl), _ptr(b_ex), _ptr(dbr), len(plan.b_recs), plan.b_rows, slices, st)
-    N.call('yb_ozaki_gemm', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
-           len(plan.tiles), slices, st)
+    if tc:
+        N.call('yb_ozaki_gemm_tc', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
+               len(plan.tiles_tc), slices, st)
+    else:
+        N.call('yb_ozaki_gemm', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
+               len(plan.tiles), slices, st)
     return out
+
+
+def ozaki_device_error(reset=True):
+    """Status word of the tcgen05 emulated GEMM (synchronises the current stream)."""
+    import ctypes
+    v = ctypes.c_int(0)
+    N.call('yb_ozaki_device_error', ctypes.addressof(v), int(bool(reset)), _stream(), launches=0)
+    return v.value
 
 
 def dot_backward(C_b, A, B, meta_dot, need_a=True, need_b=True):
