@@ -67,7 +67,7 @@ class Cfg1:
     has_svd = True
     complex_gemm = False
     trunc = {'D_total': 64}
-    ozaki_traffic = 78263296 + 8303872  # dram bytes read + written by one launch (ncu, this workload)
+    ozaki_traffic = None
 
     def __init__(self):
         from yastn_gb300.workloads import load_trace, cfg1_inputs
@@ -407,14 +407,14 @@ def run_gpu(args, wl):
     # the dominant kernel alone (split-operand GEMM; the native grouped GEMM for complex
     # data), for the roofline
     from yastn_gb300._plans import ozaki_dot_plan
-    top_kernel = 'yb_grouped_gemm' if wl.complex_gemm else 'yb_ozaki_gemm'
+    top_kernel = 'yb_ozaki_gemm'  # either emulated GEMM kernel (tcgen05 or mma.sync)
     Am = BK.transpose_and_merge(dA, *wl.mA)
     Bm = BK.transpose_and_merge(dB, *wl.mB)
     orig = _native.call
     gemm_ev = []
 
     def spy(name, *a, **k):
-        if name == top_kernel:
+        if name.startswith(top_kernel):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             r = orig(name, *a, **k)
@@ -426,19 +426,16 @@ def run_gpu(args, wl):
     try:
         for _ in range(args.steps):
             flush.zero_()
-            if wl.complex_gemm:
-                ops.dot(Am, Bm, *wl.mdot)
-            else:
-                ops.dot_ozaki(Am, Bm, *wl.mdot)
+            ops.dot_ozaki(Am, Bm, *wl.mdot)
         barrier()
     finally:
         _native.call = orig
     t_gemm = sum(a.elapsed_time(b) for a, b in gemm_ev) / len(gemm_ev) * 1e-3
-    if wl.complex_gemm:
-        tensor_flops = wl.flops
-    else:
-        oz = ozaki_dot_plan(wl.mdot[0], ops.OZAKI_SLICES)
-        tensor_flops = oz.flops * ops.OZAKI_SLICES * (ops.OZAKI_SLICES + 1) // 2
+    oz = ozaki_dot_plan(wl.mdot[0], ops.OZAKI_SLICES, wl.complex_gemm)
+    tensor_flops = oz.flops * ops.OZAKI_SLICES * (ops.OZAKI_SLICES + 1) // 2
+    use_tc = oz.prefer_tc if ops.OZAKI_TC[0] is None else ops.OZAKI_TC[0]
+    top_name = 'tcgen05 (TMEM accumulators)' if use_tc else 'mma.sync'
+
     BK.set_gemm_mode('fp64')
 
     # the workload's truncated block SVD (extra field)
@@ -483,25 +480,21 @@ def run_gpu(args, wl):
     bf16_peak, peak_src = bf16_peak_tflops()
     cpu_t, reps = time_cpu(wl.cpu_step, budget_s=8.0)
     achieved = tensor_flops / t_gemm / 1e12
-    if wl.complex_gemm:
-        roof = {"bound": "fp64", "kernel": "yb grouped_gemm_kernel<Cplx> (FP64 DFMA, 64x64 tiles, all sectors)",
-                "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
-                "peak_source": "measured live: cuBLAS DGEMM 4096^3 (complex GEMM runs on the same FP64 pipe)",
-                "traffic": None}
-    else:
-        roof = {"bound": "tensor", "kernel": "yb ozaki_gemm_kernel<8> (mma.sync bf16, 36 slice-pair products)",
-                "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s", "frac": achieved / bf16_peak,
-                "peak_source": peak_src, "traffic": wl.ozaki_traffic,
-                "traffic_note": "dram bytes read+written by one launch, ncu capture on this workload"}
+    cplx_note = ', 2 real products per complex sector' if wl.complex_gemm else ''
+    roof = {"bound": "tensor",
+            "kernel": f"yb ozaki GEMM on {top_name}, bf16 digit products (36 slice pairs{cplx_note})",
+            "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s", "frac": achieved / bf16_peak,
+            "peak_source": peak_src, "traffic": wl.ozaki_traffic,
+            "traffic_note": "dram bytes read+written by one launch, ncu capture on this workload"}
     line = {
         "metric": wl.metric, "value": world * wl.flops / t_max / 1e12, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": ("c128 (native FP64 complex sector GEMMs)" if wl.complex_gemm else
+        "dtype": ("c128 (sector GEMMs emulated: 2 real products of 8 bf16 digit slices)" if wl.complex_gemm else
                   "f64 (sector GEMMs emulated: 8 bf16 digit slices, fp32/fp64 accumulation)"),
         "data": "synthetic (seeded normal draws as yastn.rand, metadata recorded from yastn)",
         "config": {"workload": wl.name, "flop_per_step": wl.flops, "parallelism": f"replicas{world}",
-                   "gemm_mode": "fp64 (complex)" if wl.complex_gemm else "emulated",
+                   "gemm_mode": "emulated",
                    "l2": "flushed between timed steps (256 MB write)",
                    "max_rel_err_vs_fp64": emu_err,
                    "max_rel_err_per_sector_vs_oracle": sector_err},
@@ -569,7 +562,7 @@ def per_sector_errors(torch, BK, wl, dA, dB):
     dBm = BK.transpose_and_merge(dB, *wl.mB)
     out = {}
     mode0 = BK.get_gemm_mode()
-    for mode in (('fp64',) if wl.complex_gemm else ('fp64', 'emulated')):
+    for mode in ('fp64', 'emulated'):
         BK.set_gemm_mode(mode)
         got = BK.dot(dAm, dBm, *wl.mdot).cpu().numpy()
         worst = 0.0

@@ -139,9 +139,18 @@ int yb_ozaki_split(const double* src, void* slices, int* exps, const int64_t* re
 int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps,
                   double* c, const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
                   void* stream);
+/* yb_ozaki_split_tiled: yb_ozaki_split writing the digit planes in the tile layout of
+ * yb_ozaki_gemm_tc: per slice, tile_rows (128 for A, 64 for B) x 16 blocks, each in the
+ * canonical K-major core-matrix order (byte offset of (row r, k) in a block:
+ * (r/8)*256 + (k/8)*128 + (r%8)*16 + (k%8)*2), blocks ordered (row tile, K step); the
+ * rows are padded with zeros to a multiple of tile_rows (record [5] = slice-0 offset, slice
+ * stride = padded rows x Kp). */
+int yb_ozaki_split_tiled(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs,
+                         int max_rows, int slices_count, int tile_rows, void* stream);
 /* yb_ozaki_gemm_tc: yb_ozaki_gemm on the tcgen05 tensor cores with the 8 digit-diagonal
- * accumulators in tensor memory. Same records; tiles are (output, tile row, tile col, 0)
- * of 128 rows x 64 columns. A CTA that gives up on a bounded wait writes nothing for its
+ * accumulators in tensor memory, operands from yb_ozaki_split_tiled (output records [4],
+ * [6] = the A / B slice-0 offsets in the tile layout); tiles are (output, tile row, tile
+ * col, 0) of 128 rows x 64 columns. A CTA that gives up on a bounded wait writes nothing for its
  * tile and sets the status word read by yb_ozaki_device_error. */
 int yb_ozaki_gemm_tc(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps,
                      double* c, const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,

@@ -21,7 +21,8 @@ def cfg3():
     return tr, A, B
 
 
-def test_cfg3_tensordot(cfg3, cuda_device):
+@pytest.mark.parametrize('mode', ['fp64', 'emulated'])
+def test_cfg3_tensordot(mode, cfg3, cuda_device):
     tr, A, B = cfg3
     c0, c1, c2 = tr['calls'][:3]
     Am = oracle.transpose_and_merge(A, *c0['args'][1:])
@@ -30,7 +31,12 @@ def test_cfg3_tensordot(cfg3, cuda_device):
     dAm = BK.transpose_and_merge(torch.from_numpy(A).cuda(), *c0['args'][1:])
     dBm = BK.transpose_and_merge(torch.from_numpy(B).cuda(), *c1['args'][1:])
     np.testing.assert_array_equal(dAm.cpu().numpy(), Am)
-    got = BK.dot(dAm, dBm, *c2['args'][2:]).cpu().numpy()
+    saved = BK.get_gemm_mode()
+    BK.set_gemm_mode(mode)
+    try:
+        got = BK.dot(dAm, dBm, *c2['args'][2:]).cpu().numpy()
+    finally:
+        BK.set_gemm_mode(saved)
     for slc, Dc, *_ in c2['args'][2]:
         r, g = ref[slc[0]:slc[1]], got[slc[0]:slc[1]]
         if r.size:

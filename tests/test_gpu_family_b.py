@@ -163,26 +163,37 @@ SMALL_SHAPES = [(1, 16, 1), (1, 40, 1), (7, 33, 3), (15, 17, 129), (70, 20, 2), 
                 (3, 5, 2000), (5, 8, 100), (64, 3, 64), (66, 15, 65), (33, 1, 31)]
 
 
-def _small_sector_problem(seed):
+def _small_sector_problem(seed, cplx=False):
     rng = np.random.default_rng(seed)
     meta, oa, ob, oc = [], 0, 0, 0
     for m, k, n in SMALL_SHAPES:
         meta.append(((oc, oc + m * n), (m, n), (oa, oa + m * k), (m, k), (ob, ob + k * n), (k, n)))
         oa += m * k; ob += k * n; oc += m * n
-    return tuple(meta), rng.normal(size=oa), rng.normal(size=ob), oc
+    A, B = rng.normal(size=oa), rng.normal(size=ob)
+    if cplx:
+        A, B = A + 1j * rng.normal(size=oa), B - 1j * rng.normal(size=ob)
+    return tuple(meta), A, B, oc
 
 
 @pytest.mark.parametrize('emulated', [False, True])
-def test_dot_small_and_ragged_sectors(emulated, cuda_device):
+@pytest.mark.parametrize('cplx', [False, True])
+def test_dot_small_and_ragged_sectors(emulated, cplx, cuda_device):
     """Sectors with m or n below a warp's share of a tile (skipped warps), K not a multiple of
-    the K-step, skinny and tall outputs: native and emulated against the oracle, per sector."""
-    meta, A, B, oc = _small_sector_problem(21)
+    the K-step, skinny and tall outputs: native and emulated (complex: two real products with
+    doubled K), both GEMM kernels, against the oracle per sector."""
+    meta, A, B, oc = _small_sector_problem(21, cplx)
     ref = oracle.dot(A, B, meta, oc)
-    f = ops.dot_ozaki if emulated else ops.dot
-    got = host(f(dev(A), dev(B), meta, oc))
-    for slc, Dc, *_ in meta:
-        r, g = ref[slc[0]:slc[1]], got[slc[0]:slc[1]]
-        assert np.abs(g - r).max() <= TOL * max(np.abs(r).max(), 1e-300), Dc
+    saved = ops.OZAKI_TC[0]
+    try:
+        for tc in ((True, False) if emulated else (None,)):
+            ops.OZAKI_TC[0] = tc
+            f = ops.dot_ozaki if emulated else ops.dot
+            got = host(f(dev(A), dev(B), meta, oc))
+            for slc, Dc, *_ in meta:
+                r, g = ref[slc[0]:slc[1]], got[slc[0]:slc[1]]
+                assert np.abs(g - r).max() <= TOL * max(np.abs(r).max(), 1e-300), (Dc, tc)
+    finally:
+        ops.OZAKI_TC[0] = saved
 
 
 @pytest.mark.parametrize('name', ['cfg1', 'small'])

@@ -297,6 +297,52 @@ def test_mixed_precision_jacobi_schedule_complex():
         assert np.abs(np.sort(s)[::-1] - Sr[mt[4][0]:mt[4][1]]).max() <= 1e-13 * max(s.max(), 1.0)
 
 
+def _split_rows_view(src, rec):
+    """The real rows the split kernels read for one record (modes of csrc/yb_ozaki.cu)."""
+    s0, rows, K, rs, mode = (int(x) for x in rec[:5])
+    if mode == 0:
+        return np.stack([src[s0 + r * rs: s0 + r * rs + K] for r in range(rows)])
+    half = K // 2
+    out = []
+    for r in range(rows):
+        z = src[s0 + r * rs: s0 + r * rs + half]
+        out.append({1: np.concatenate([z.real, z.imag]), 2: np.concatenate([z.real, -z.imag]),
+                    3: np.concatenate([z.imag, z.real])}[mode])
+    return np.stack(out)
+
+
+def test_ozaki_complex_plan_reproduces_complex_products():
+    """Complex sectors as two real products with doubled K: A rows [re | im], B^T rows
+    [re | -im] and [im | re], outputs interleaved with column stride 2."""
+    rng = np.random.default_rng(17)
+    shapes = [(40, 30, 20), (16, 16, 17), (5, 40, 9), (3, 8, 100)]
+    meta, oa, ob, oc = [], 0, 0, 0
+    for m, k, n in shapes:
+        meta.append(((oc, oc + m * n), (m, n), (oa, oa + m * k), (m, k), (ob, ob + k * n), (k, n)))
+        oa += m * k; ob += k * n; oc += m * n
+    meta = tuple(meta)
+    A = rng.normal(size=oa) + 1j * rng.normal(size=oa)
+    B = rng.normal(size=ob) + 1j * rng.normal(size=ob)
+    plan = P.ozaki_dot_plan(meta, 8, True)
+    assert len(plan.outs) == 2 * 3 and len(plan.native.outs) == 1       # (3, 8, 100) is short: native
+    assert sorted(set(int(r[4]) for r in plan.a_recs)) == [1]
+    assert sorted(int(r[4]) for r in plan.b_recs) == [2, 2, 2, 3, 3, 3]
+    tasks, items = plan.bT.packed(False)
+    bT = PI.run_copy(tasks, items, B, np.zeros(plan.bT_size, dtype=complex))
+    a_rows = {int(r[5]): _split_rows_view(A, r) for r in plan.a_recs}
+    b_rows = {int(r[5]): _split_rows_view(bT, r) for r in plan.b_recs}
+    Cd = np.zeros(2 * oc)
+    for o in plan.outs:
+        c_off, m, n, ldc, ao, _, bo, _, Kr, Kp, cs = (int(x) for x in o[:11])
+        part = a_rows[ao] @ b_rows[bo].T
+        for i in range(m):
+            Cd[c_off + i * ldc + cs * np.arange(n)] = part[i]
+    C = Cd[0::2] + 1j * Cd[1::2]
+    for (slc, Dc, sla, Da, slb, Db), o in zip(meta[:3], range(3)):
+        ref = A[sla[0]:sla[1]].reshape(Da) @ B[slb[0]:slb[1]].reshape(Db)
+        np.testing.assert_allclose(C[slc[0]:slc[1]].reshape(Dc), ref, rtol=1e-12, atol=1e-12)
+
+
 def test_eigh_adjoint_plan_reproduces_reference_autograd():
     """X = op(U)^T gU, the inner matrix, T = U K, dA = T op(U)^T on the packed records
     reproduce the reference's eigh gradients (SYMEIG and torch.linalg.eigh, real and complex)."""

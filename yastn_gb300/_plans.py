@@ -397,16 +397,34 @@ OZAKI_TC_M, OZAKI_TC_N = 128, 64  # output tile of the tcgen05 emulated GEMM
 OZAKI_MIN_DIM = 16  # sector GEMMs contracting fewer indices than this stay on the native FP64 kernel
 
 
-def ozaki_dot_plan(meta_dot, s):
+def _tiled_recs(recs, s, th):
+    """Split records with destinations in the tcgen05 tile layout: each operand block takes
+    s * ceil(rows / th) * th * Kp digits. Returns (records, total size, old offset -> new)."""
+    out = recs.copy()
+    size, remap = 0, {}
+    for i, r in enumerate(recs):
+        rows, Kp = int(r[1]), int(r[7])
+        remap[int(r[5])] = size
+        out[i, 5] = size
+        size += s * (-(-rows // th) * th) * Kp
+    return out, size, remap
+
+
+def ozaki_dot_plan(meta_dot, s, cplx=False):
     """C[slc] = A[sla] @ B[slb] with A rows / B columns split into ``s`` BF16 digit slices.
 
     B blocks are first transposed (copy plan ``bT``) into K-contiguous rows, so both
-    operands are split row-wise with coalesced accesses.
+    operands are split row-wise with coalesced accesses. Complex blocks (``cplx``) become
+    two real products with doubled K, C_r = [A_r, A_i][B_r; -B_i] and
+    C_i = [A_r, A_i][B_i; B_r]: A is split once in mode 1 ([re | im] rows), each B^T block
+    twice (modes 2 and 3), and the two outputs of a sector write the real and imaginary
+    parts of the complex result (column stride 2 in FP64 units).
     """
     def build():
         a_map, b_map, a_recs, b_recs, bT_tasks = {}, {}, [], [], []
         a_size = b_size = a_ex = b_ex = bT_size = 0
         outs, flops, small = [], 0, []
+        f = 2 if cplx else 1  # FP64 words per element
         for slc, Dc, sla, Da, slb, Db in meta_dot:
             m, K = Da
             n = Db[1]
@@ -414,23 +432,28 @@ def ozaki_dot_plan(meta_dot, s):
                 # short contractions and skinny outputs stay on the native FP64 kernel
                 small.append((slc[0], m, n, n, [(sla[0], slb[0], K, K, 1, n, 1, 0)]))
                 continue
-            Kp = (K + 15) // 16 * 16
+            Kr = f * K  # length of the real rows that are split
+            Kp = (Kr + 15) // 16 * 16
             if sla[0] not in a_map:
                 a_map[sla[0]] = (a_size, a_ex)
-                a_recs.append((sla[0], m, K, K, 1, a_size, a_ex, Kp))
+                a_recs.append((sla[0], m, Kr, K, int(cplx), a_size, a_ex, Kp))
                 a_size += s * m * Kp
                 a_ex += m
             if slb[0] not in b_map:
-                b_map[slb[0]] = (b_size, b_ex)
                 bT_tasks.append((slb[0], bT_size, [n, K], [1, n], [K, 1]))
-                b_recs.append((bT_size, n, K, K, 1, b_size, b_ex, Kp))
+                parts = []
+                for mode in ((2, 3) if cplx else (0,)):
+                    b_recs.append((bT_size, n, Kr, K, mode, b_size, b_ex, Kp))
+                    parts.append((b_size, b_ex))
+                    b_size += s * n * Kp
+                    b_ex += n
+                b_map[slb[0]] = parts
                 bT_size += n * K
-                b_size += s * n * Kp
-                b_ex += n
             ao, ae = a_map[sla[0]]
-            bo, be = b_map[slb[0]]
-            outs.append((slc[0], m, n, n, ao, ae, bo, be, K, Kp, 0, 0, 0, 0, 0, 0))
-            flops += 2 * m * n * K
+            for part, (bo, be) in enumerate(b_map[slb[0]]):
+                # complex: part 0 = real part (even FP64 words), part 1 = imaginary part
+                outs.append((f * slc[0] + part, m, n, f * n, ao, ae, bo, be, Kr, Kp, f, 0, 0, 0, 0, 0))
+            flops += (8 if cplx else 2) * m * n * K
         outs = np.array(outs, dtype=np.int64).reshape(-1, 16)
         tiles = []
         for oi, o in enumerate(outs):
@@ -460,8 +483,22 @@ def ozaki_dot_plan(meta_dot, s):
         plan.bT_size = bT_size
         plan.native = _pack_gemm(small)
         plan.tiles_tc = tiles_tc
+        # tcgen05 operands: digit planes in tile layout (rows padded to 128 for A, 64 for B)
+        plan.a_recs_tc, plan.a_size_tc, a_off_tc = _tiled_recs(a_recs, s, OZAKI_TC_M)
+        plan.b_recs_tc, plan.b_size_tc, b_off_tc = _tiled_recs(b_recs, s, OZAKI_TC_N)
+        outs_tc = outs.copy()
+        if len(outs_tc):
+            outs_tc[:, 4] = [a_off_tc[int(x)] for x in outs[:, 4]]
+            outs_tc[:, 6] = [b_off_tc[int(x)] for x in outs[:, 6]]
+        plan.outs_tc = outs_tc
+        # padded MMA work of the two tilings: the tcgen05 kernel (128 x 64 tiles) when its
+        # padding costs little more than the 64 x 64 tiles of the mma.sync kernel
+        w64 = sum(-(-int(o[1]) // 64) * 64 * -(-int(o[2]) // 64) * 64 * int(o[9]) for o in outs)
+        w128 = sum(-(-int(o[1]) // OZAKI_TC_M) * OZAKI_TC_M * -(-int(o[2]) // OZAKI_TC_N) * OZAKI_TC_N * int(o[9])
+                   for o in outs)
+        plan.prefer_tc = bool(len(outs)) and w128 <= 1.1 * w64
         return plan
-    return CACHE.get((meta_dot,), ('ozaki_dot', s), build)
+    return CACHE.get((meta_dot,), ('ozaki_dot', s, bool(cplx)), build)
 
 
 # ----------------------------------------------------------------------------- SVD

@@ -62,14 +62,15 @@ def _sl(x):
     return slice(x[0], x[1])
 
 
-# Sector GEMMs of ``dot`` for real FP64 operands: 'fp64' runs the native FP64 grouped GEMM;
+# Sector GEMMs of ``dot`` for FP64 / complex128 operands: 'fp64' runs the native grouped GEMM;
 # 'emulated' runs the split-operand emulation on BF16 tensor cores (8 digit slices, results
 # within a few FP64 rounding errors of the native product, normwise per row/column scale).
 _GEMM_MODE = ['fp64']
+_EMULATED = (torch.float64, torch.complex128)
 
 
 def set_gemm_mode(mode):
-    """Select 'fp64' (default) or 'emulated' sector GEMMs for real float64 ``dot``."""
+    """Select 'fp64' (default) or 'emulated' sector GEMMs for float64 / complex128 ``dot``."""
     if mode not in ('fp64', 'emulated'):
         raise ValueError("gemm mode must be 'fp64' or 'emulated'")
     _GEMM_MODE[0] = mode
@@ -140,7 +141,7 @@ class _Dot(torch.autograd.Function):
     def forward(ctx, A, B, meta_dot, Dsize):
         ctx.save_for_backward(A, B)
         ctx.meta_dot = meta_dot
-        if _GEMM_MODE[0] == 'emulated' and A.dtype == torch.float64 and B.dtype == torch.float64:
+        if _GEMM_MODE[0] == 'emulated' and A.dtype in _EMULATED and B.dtype in _EMULATED:
             return ops.dot_ozaki(A, B, meta_dot, Dsize)
         return ops.dot(A, B, meta_dot, Dsize)
 

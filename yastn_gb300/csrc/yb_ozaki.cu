@@ -38,8 +38,12 @@ constexpr int kChunkSteps = 25;
 constexpr int kThreads = 256;
 
 // ------------------------------------------------------------------ splitting
-// rec: [0] src offset [1] rows [2] K [3] row stride [4] col stride (must be 1)
+// rec: [0] src offset [1] rows [2] K [3] row stride [4] mode
 //      [5] dst offset (bf16) [6] exponent offset [7] Kp (K rounded up to 16)
+// mode 0: a real row of K contiguous FP64 values (offsets and stride in elements);
+// modes 1-3: a complex128 row of K/2 values (offsets and stride in complex elements) read
+// as the real row [re | im] (1), [re | -im] (2) or [im | re] (3), the operands of the two
+// real products C_r = [A_r, A_i][B_r; -B_i] and C_i = [A_r, A_i][B_i; B_r] of a complex GEMM.
 // dst layout: [slice][row][Kp] bf16, padding zero-filled.
 //
 // The digits are extracted with integer arithmetic only (GB300's FP64 pipe is narrow):
@@ -82,18 +86,44 @@ __device__ __forceinline__ void digits_of(long long bits, int e, int s, int* d) 
   d[0] = (int)(u >> (7 * (s - 1)));
 }
 
+// Bit pattern of element l of the split row (see the record modes above).
+struct RowSrc {
+  const double* base;
+  int64_t half;  // K/2 for the complex modes
+  int mode;
+  __device__ __forceinline__ long long operator()(int64_t l) const {
+    if (mode == 0) return __ldg(reinterpret_cast<const long long*>(base) + l);
+    const bool first = l < half;
+    const int64_t j = first ? l : l - half;
+    const long long* c = reinterpret_cast<const long long*>(base) + 2 * j;
+    const long long re = __ldg(c), im = __ldg(c + 1);
+    if (mode == 1) return first ? re : im;
+    if (mode == 2) return first ? re : (long long)((unsigned long long)im ^ 0x8000000000000000ull);
+    return first ? im : re;
+  }
+};
+
+__device__ __forceinline__ RowSrc row_src(const double* src, const int64_t* r, int64_t row) {
+  const int mode = (int)r[4];
+  RowSrc rs;
+  rs.mode = mode;
+  rs.half = r[2] / 2;
+  rs.base = src + (mode == 0 ? r[0] + row * r[3] : 2 * (r[0] + row * r[3]));
+  return rs;
+}
+
 __global__ void split_rows_kernel(const double* __restrict__ src, __nv_bfloat16* __restrict__ slices,
                                   int* __restrict__ exps, const int64_t* __restrict__ recs, int s) {
   // one warp per row (K contiguous), each lane two consecutive elements per step
   const int64_t* r = recs + (int64_t)blockIdx.y * 8;
-  const int64_t rows = r[1], K = r[2], rs = r[3], Kp = r[7];
+  const int64_t rows = r[1], K = r[2], Kp = r[7];
   const int lane = threadIdx.x & 31;
   const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (row >= rows) return;
-  const long long* a = reinterpret_cast<const long long*>(src + r[0] + row * rs);
+  const RowSrc a = row_src(src, r, row);
   // row maximum of |a| on the bit patterns (non-negative doubles order as integers)
   long long mx = 0;
-  for (int64_t l = lane; l < K; l += 32) mx = max(mx, __ldg(a + l) & 0x7fffffffffffffffll);
+  for (int64_t l = lane; l < K; l += 32) mx = max(mx, a(l) & 0x7fffffffffffffffll);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   int e = 0;  // max |a| = f 2^e, f in [0.5, 1): |a| < 2^e
@@ -104,13 +134,57 @@ __global__ void split_rows_kernel(const double* __restrict__ src, __nv_bfloat16*
   __nv_bfloat16* dst = slices + r[5] + row * Kp;
   for (int64_t l = 2 * lane; l < Kp; l += 64) {
     int d0[8], d1[8];
-    if (l < K) digits_of(__ldg(a + l), e, s, d0); else for (int t = 0; t < 8; ++t) d0[t] = 0;
-    if (l + 1 < K) digits_of(__ldg(a + l + 1), e, s, d1); else for (int t = 0; t < 8; ++t) d1[t] = 0;
+    if (l < K) digits_of(a(l), e, s, d0); else for (int t = 0; t < 8; ++t) d0[t] = 0;
+    if (l + 1 < K) digits_of(a(l + 1), e, s, d1); else for (int t = 0; t < 8; ++t) d1[t] = 0;
     for (int t = 0; t < s; ++t) {
       __nv_bfloat162 v;
       v.x = __int2bfloat16_rn(d0[t]);
       v.y = __int2bfloat16_rn(d1[t]);
       *reinterpret_cast<__nv_bfloat162*>(dst + t * slice_stride + l) = v;
+    }
+  }
+}
+
+// The same split written in the tensor-core tile layout of the tcgen05 GEMM: per slice, the
+// rows are grouped in tiles of TH (128 for A, 64 for B) and K in steps of 16; every
+// (row tile, K step) is one contiguous TH x 16 block in the canonical K-major layout of the
+// tcgen05 matrix descriptors (8-row x 16-byte core matrices: byte offset of (row r, k) is
+// (r/8)*256 + (k/8)*128 + (r%8)*16 + (k%8)*2), so a GEMM stage is a few bulk copies. Rows
+// from the operand's row count up to the next multiple of TH are written as zeros.
+__global__ void split_rows_tiled_kernel(const double* __restrict__ src, __nv_bfloat16* __restrict__ slices,
+                                        int* __restrict__ exps, const int64_t* __restrict__ recs, int s, int TH) {
+  const int64_t* r = recs + (int64_t)blockIdx.y * 8;
+  const int64_t rows = r[1], K = r[2], Kp = r[7];
+  const int64_t rows_p = (rows + TH - 1) / TH * TH;
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= rows_p) return;
+  const bool live = row < rows;
+  const RowSrc a = row_src(src, r, live ? row : 0);
+  long long mx = 0;
+  if (live)
+    for (int64_t l = lane; l < K; l += 32) mx = max(mx, a(l) & 0x7fffffffffffffffll);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  int e = 0;
+  if (mx >= (1ll << 52)) e = (int)(mx >> 52) - 1022;
+  else if (mx > 0) frexp(__longlong_as_double(mx), &e);
+  if (live && lane == 0) exps[r[6] + row] = e;
+  const int64_t slice_stride = rows_p * Kp;
+  const int64_t ksteps = Kp / 16;
+  __nv_bfloat16* base = slices + r[5] + (row / TH) * ksteps * (int64_t)TH * 16;
+  const int rr = (int)(row % TH);
+  const int64_t in_tile = (int64_t)(rr >> 3) * 128 + (rr & 7) * 8;  // elements
+  for (int64_t l = 2 * lane; l < Kp; l += 64) {
+    int d0[8], d1[8];
+    if (live && l < K) digits_of(a(l), e, s, d0); else for (int t = 0; t < 8; ++t) d0[t] = 0;
+    if (live && l + 1 < K) digits_of(a(l + 1), e, s, d1); else for (int t = 0; t < 8; ++t) d1[t] = 0;
+    const int64_t off = (l >> 4) * (int64_t)TH * 16 + in_tile + ((l & 15) >> 3) * 64 + (l & 7);
+    for (int t = 0; t < s; ++t) {
+      __nv_bfloat162 v;
+      v.x = __int2bfloat16_rn(d0[t]);
+      v.y = __int2bfloat16_rn(d1[t]);
+      *reinterpret_cast<__nv_bfloat162*>(base + t * slice_stride + off) = v;
     }
   }
 }
@@ -164,7 +238,8 @@ __device__ __forceinline__ void mma_bf16(float* c, const unsigned* a, const unsi
 }
 
 // out record: [0] c offset [1] m [2] n [3] ldc [4] A slices offset [5] A exp offset
-//             [6] B slices offset [7] B exp offset [8] K [9] Kp
+//             [6] B slices offset [7] B exp offset [8] K [9] Kp [10] output column stride
+//             (0 or 1: contiguous; 2: the real or imaginary part of complex output)
 template <int S>
 __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm_kernel(const __nv_bfloat16* __restrict__ As,
                                                                  const int* __restrict__ Ae,
@@ -179,6 +254,7 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm_kernel(const __nv_bflo
   const int64_t* o = outs + (int64_t)tl.x * 16;
   const int64_t c_off = o[0], m = o[1], n = o[2], ldc = o[3];
   const int64_t a_sl = o[4], a_ex = o[5], b_sl = o[6], b_ex = o[7], Kp = o[9];
+  const int64_t ccs = o[10] > 0 ? o[10] : 1;  // output column stride (2: one part of complex data)
   const int64_t row0 = (int64_t)tl.y * kTile, col0 = (int64_t)tl.z * kTile;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wm = warp & 1, wn = warp >> 1;  // warp sub-tile: rows wm*32.., cols wn*16..
@@ -280,7 +356,8 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm_kernel(const __nv_bflo
       for (int v = 0; v < 4; ++v) {
         const int64_t gi = row0 + wm * 32 + i * 16 + (lane >> 2) + (v >= 2 ? 8 : 0);
         const int64_t gj = col0 + wn * 16 + j * 8 + (lane & 3) * 2 + (v & 1);
-        if (gi < m && gj < n) C[c_off + gi * ldc + gj] = scale_pow2(acc64[i][j][v], Ae[a_ex + gi] + Be[b_ex + gj] - 14);
+        if (gi < m && gj < n)
+          C[c_off + gi * ldc + gj * ccs] = scale_pow2(acc64[i][j][v], Ae[a_ex + gi] + Be[b_ex + gj] - 14);
       }
 }
 
@@ -349,6 +426,12 @@ __device__ __forceinline__ void tc_ld8(uint32_t taddr, uint32_t* r) {
                : "r"(taddr));
 }
 
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+
 template <int S>
 __global__ void __launch_bounds__(kTcThreads, 1)
     ozaki_gemm_tc_kernel(const __nv_bfloat16* __restrict__ As, const int* __restrict__ Ae,
@@ -359,13 +442,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   constexpr uint32_t kStage = S * (kATile + kBTile);
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint32_t tmem_slot;
-  __shared__ __align__(8) uint64_t mbar[kTcStages];
+  __shared__ __align__(8) uint64_t full[kTcStages], empty[kTcStages], accb;
   __shared__ int failed;
-  __shared__ long long last_step;  // last K-step whose MMAs were committed (-1: none)
   const int4 tl = reinterpret_cast<const int4*>(tiles)[blockIdx.x];
   const int64_t* o = outs + (int64_t)tl.x * 16;
   const int64_t c_off = o[0], m = o[1], n = o[2], ldc = o[3];
   const int64_t a_sl = o[4], a_ex = o[5], b_sl = o[6], b_ex = o[7], Kp = o[9];
+  const int64_t ccs = o[10] > 0 ? o[10] : 1;  // output column stride (2: one part of complex data)
   const int64_t row0 = (int64_t)tl.y * kTcM, col0 = (int64_t)tl.z * kTcN;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t sbase = smem_u32(smem);
@@ -376,109 +459,109 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    for (int i = 0; i < kTcStages; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[i])));
+    for (int i = 0; i < kTcStages; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[i])));
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&accb)));
     asm volatile("fence.mbarrier_init.release.cluster;");
     failed = 0;
-    last_step = -1;
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_slot;
 
-  const int64_t a_stride = m * Kp, b_stride = n * Kp;
-  auto load = [&](int stage, int64_t k0) {
-    // S slices x (128 A rows + 64 B rows) x 2 chunks of 16 bytes
-    for (int c = tid; c < S * (kTcM + kTcN) * 2; c += kTcThreads) {
-      const bool isA = c < S * kTcM * 2;
-      const int cc = isA ? c : c - S * kTcM * 2;
-      const int rows = isA ? kTcM : kTcN;
-      const int t = cc / (rows * 2), rem = cc % (rows * 2), r = rem >> 1, half = rem & 1;
-      const uint32_t dst = (uint32_t)stage * kStage + (isA ? (uint32_t)t * kATile : S * kATile + (uint32_t)t * kBTile) +
-                           (uint32_t)(r >> 3) * 256 + (uint32_t)half * 128 + (uint32_t)(r & 7) * 16;
-      const int64_t g = (isA ? row0 : col0) + r;
-      const bool valid = g < (isA ? m : n);
-      const __nv_bfloat16* src = isA ? As + a_sl + t * a_stride + (valid ? g : 0) * Kp + k0 + half * 8
-                                     : Bs + b_sl + t * b_stride + (valid ? g : 0) * Kp + k0 + half * 8;
-      cp_async16(smem + dst, src, valid);
+  // digit planes in tile layout: per slice, (row tile, K step) blocks of 128 x 16 (A) / 64 x 16 (B)
+  const int64_t ksteps = Kp / kK;
+  const int64_t a_slice = (m + kTcM - 1) / kTcM * kTcM * Kp, b_slice = (n + kTcN - 1) / kTcN * kTcN * Kp;
+  const __nv_bfloat16* a_tiles = As + a_sl + (int64_t)tl.y * ksteps * (kTcM * kK);
+  const __nv_bfloat16* b_tiles = Bs + b_sl + (int64_t)tl.z * ksteps * (kTcN * kK);
+  // producer (thread 0): one stage = S A tiles + S B tiles, each one bulk copy
+  auto issue = [&](int stage, int64_t step) {
+    const uint32_t fb = smem_u32(&full[stage]);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(kStage) : "memory");
+    const uint32_t d0 = sbase + (uint32_t)stage * kStage;
+    for (int t = 0; t < S; ++t) {
+      bulk_load(d0 + t * kATile, a_tiles + t * a_slice + step * (kTcM * kK), kATile, fb);
+      bulk_load(d0 + S * kATile + t * kBTile, b_tiles + t * b_slice + step * (kTcN * kK), kBTile, fb);
     }
-    cp_async_commit();
   };
-
-  const int64_t nsteps = Kp / kK;
-  for (int i = 0; i < kTcStages - 1; ++i) {
-    if (i < nsteps) load(i, (int64_t)i * kK); else cp_async_commit();
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
+                         ((uint32_t)(kTcM >> 4) << 24);  // F32 accumulate, BF16 A/B, K-major, N=64, M=128
+  int64_t issued = 0, consumed = 0;  // steps loaded / steps whose MMAs were issued (thread 0)
+  if (tid == 0) {
+    for (; issued < kTcStages && issued < ksteps; ++issued) issue((int)issued, issued);
   }
   double acc64[kTcN];
 #pragma unroll
   for (int j = 0; j < kTcN; ++j) acc64[j] = 0.0;
-  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
-                         ((uint32_t)(kTcM >> 4) << 24);  // F32 accumulate, BF16 A/B, K-major, N=64, M=128
-
-  for (int64_t st = 0; st < nsteps; ++st) {
-    const int stage = (int)(st % kTcStages);
-    asm volatile("cp.async.wait_group %0;" ::"n"(kTcStages - 2));
-    asm volatile("fence.proxy.async.shared::cta;");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    if (tid == 0 && !failed) {
-      const bool first = (st % kChunkSteps) == 0;
-      const uint32_t a0 = sbase + (uint32_t)stage * kStage, b0 = a0 + S * kATile;
+  const int64_t nchunks = (ksteps + kChunkSteps - 1) / kChunkSteps;
+  for (int64_t ch = 0; ch < nchunks; ++ch) {
+    const int64_t s0 = ch * kChunkSteps, s1 = min(ksteps, s0 + kChunkSteps);
+    if (tid == 0) {
+      for (int64_t st = s0; st < s1 && !failed; ++st) {
+        const int stage = (int)(st % kTcStages);
+        if (!mbar_wait(smem_u32(&full[stage]), (uint32_t)((st / kTcStages) & 1))) { failed = 1; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t a0 = sbase + (uint32_t)stage * kStage, b0 = a0 + S * kATile;
 #pragma unroll
-      for (int ta = 0; ta < S; ++ta)
+        for (int ta = 0; ta < S; ++ta)
 #pragma unroll
-        for (int tb = 0; tb < S - ta; ++tb)
-          tc_mma(tmem + (uint32_t)((ta + tb) * kTcN), umma_desc(a0 + ta * kATile), umma_desc(b0 + tb * kBTile), idesc,
-                 (first && ta == 0) ? 0u : 1u);
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          smem_u32(&mbar[stage])));
-      last_step = st;
-    }
-    // refill the stage of step st-1 with step st + kTcStages - 1 once its MMAs are done
-    const int64_t ls = st + kTcStages - 1;
-    if (ls < nsteps) {
-      if (st >= 1 && !mbar_wait(smem_u32(&mbar[(st - 1) % kTcStages]), (uint32_t)(((st - 1) / kTcStages) & 1)))
-        failed = 1;
-      load((int)(ls % kTcStages), ls * kK);
-    } else {
-      cp_async_commit();
-    }
-    if (((st + 1) % kChunkSteps) == 0 || st + 1 == nsteps) {
-      if (!mbar_wait(smem_u32(&mbar[stage]), (uint32_t)((st / kTcStages) & 1))) failed = 1;
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      // fold the 8 diagonals of this thread's row exactly (integer pipe) into FP64
-#pragma unroll
-      for (int cb = 0; cb < kTcN / 8; ++cb) {
-        long long hi[8], lo[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) hi[j] = lo[j] = 0;
-#pragma unroll
-        for (int d = 0; d < S; ++d) {
-          uint32_t v[8];
-          tc_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(d * kTcN + cb * 8), v);
-          asm volatile("tcgen05.wait::ld.sync.aligned;");
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const long long q = (long long)__float2int_rn(__uint_as_float(v[j]));
-            if (d < 4) hi[j] += q << (7 * (3 - d));
-            else lo[j] += q << (7 * (S - 1 - d));
-          }
+          for (int tb = 0; tb < S - ta; ++tb)
+            tc_mma(tmem + (uint32_t)((ta + tb) * kTcN), umma_desc(a0 + ta * kATile), umma_desc(b0 + tb * kBTile),
+                   idesc, (st == s0 && ta == 0) ? 0u : 1u);
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(&empty[stage])));
+        consumed = st + 1;
+        // refill the stage of step st-1 (its MMAs ran while those of step st were queued)
+        if (st >= 1 && issued < ksteps && issued == st - 1 + kTcStages) {
+          const int ps = (int)((st - 1) % kTcStages);
+          if (!mbar_wait(smem_u32(&empty[ps]), (uint32_t)(((st - 1) / kTcStages) & 1))) { failed = 1; break; }
+          issue(ps, issued);
+          ++issued;
         }
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-          acc64[cb * 8 + j] += int_to_double_scaled(hi[j], -21) + int_to_double_scaled(lo[j], -7 * (S - 1));
       }
-      asm volatile("tcgen05.fence::before_thread_sync;");
-      __syncthreads();  // every lane has read the accumulators before the next chunk overwrites them
+      // the accumulators of this chunk are complete once every MMA issued so far is
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(&accb)));
     }
+    if (!mbar_wait(smem_u32(&accb), (uint32_t)(ch & 1))) failed = 1;
+    asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+    for (int cb = 0; cb < kTcN / 8; ++cb) {
+      long long hi[8], lo[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) hi[j] = lo[j] = 0;
+#pragma unroll
+      for (int d = 0; d < S; ++d) {
+        uint32_t v[8];
+        tc_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(d * kTcN + cb * 8), v);
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const long long q = (long long)__float2int_rn(__uint_as_float(v[j]));
+          if (d < 4) hi[j] += q << (7 * (3 - d));
+          else lo[j] += q << (7 * (S - 1 - d));
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        acc64[cb * 8 + j] += int_to_double_scaled(hi[j], -21) + int_to_double_scaled(lo[j], -7 * (S - 1));
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();  // every lane has read the accumulators before the next chunk overwrites them
+    if (failed) break;
   }
-  asm volatile("cp.async.wait_group 0;");
-  __syncthreads();
   if (failed) {
-    // MMAs complete in issue order: waiting for the last commit covers all of them
-    if (tid == 0) atomicExch(err, 1);
-    const long long ls_ = last_step;
-    if (ls_ >= 0) mbar_wait(smem_u32(&mbar[ls_ % kTcStages]), (uint32_t)((ls_ / kTcStages) & 1));
+    // drain: the bulk copies issued but not consumed, and the MMAs (complete in issue order)
+    if (tid == 0) {
+      atomicExch(err, 1);
+      for (int64_t j = consumed; j < issued; ++j)
+        mbar_wait(smem_u32(&full[j % kTcStages]), (uint32_t)((j / kTcStages) & 1));
+      if (consumed > 0)
+        mbar_wait(smem_u32(&empty[(consumed - 1) % kTcStages]), (uint32_t)(((consumed - 1) / kTcStages) & 1));
+    }
   } else {
     // epilogue through shared memory (the stages are free): row-major 128 x 64 doubles,
     // padded rows; then coalesced stores with the row/column exponents applied
@@ -491,7 +574,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const int rr = e / kTcN, cc = e % kTcN;
       const int64_t gi = row0 + rr, gj = col0 + cc;
       if (gi < m && gj < n)
-        C[c_off + gi * ldc + gj] = scale_pow2(tileC[rr * (kTcN + 1) + cc], Ae[a_ex + gi] + Be[b_ex + gj] - 14);
+        C[c_off + gi * ldc + gj * ccs] = scale_pow2(tileC[rr * (kTcN + 1) + cc], Ae[a_ex + gi] + Be[b_ex + gj] - 14);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -525,6 +608,18 @@ int yb_ozaki_split(const double* src, void* slices, int* exps, const int64_t* re
   dim3 grid((unsigned)((max_rows + 7) / 8), (unsigned)n_recs);
   yb::split_rows_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(src, (__nv_bfloat16*)slices, exps, recs,
                                                                  slices_count);
+  return yb::check_launch();
+}
+
+int yb_ozaki_split_tiled(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs, int max_rows,
+                         int slices_count, int tile_rows, void* stream) {
+  if (n_recs == 0 || max_rows == 0) return YB_OK;
+  if (!src || !slices || !exps || !recs || slices_count < 1 || slices_count > 8) return YB_ERR_INVALID;
+  if (tile_rows != 64 && tile_rows != 128) return YB_ERR_INVALID;
+  const int rows_p = (max_rows + tile_rows - 1) / tile_rows * tile_rows;
+  dim3 grid((unsigned)((rows_p + 7) / 8), (unsigned)n_recs);
+  yb::split_rows_tiled_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(src, (__nv_bfloat16*)slices, exps, recs,
+                                                                       slices_count, tile_rows);
   return yb::check_launch();
 }
 

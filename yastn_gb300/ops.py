@@ -143,41 +143,49 @@ def dot(A, B, meta_dot, Dsize):
 OZAKI_SLICES = 8  # 57 bits per operand: FP64-grade products
 
 
-OZAKI_TC = [True]  # emulated GEMM on tcgen05/TMEM (False: the mma.sync kernel)
+OZAKI_TC = [None]  # emulated GEMM kernel: None = per dot by tile padding, True = tcgen05/TMEM, False = mma.sync
 
 
 def dot_ozaki(A, B, meta_dot, Dsize, slices=OZAKI_SLICES):
     """``dot`` with the FP64 sector GEMMs emulated on BF16 tensor cores (split operands).
 
-    Real float64 operands only. Each A row / B column is split into ``slices`` BF16 digit
+    float64 or complex128 operands (a complex product is two real products with doubled
+    K). Each A row / B column is split into ``slices`` BF16 digit
     planes (scratch of 2 * slices bytes per operand element); all slice-pair products
     with digit-weight sum below ``slices`` are accumulated exactly in FP32 per K-chunk and
     combined in FP64. ``slices=8`` reproduces the FP64 product to its rounding level.
     """
     A, B = promote(_check(A, 'A'), _check(B, 'B'))
-    if A.dtype != torch.float64:
-        raise NotImplementedError("yastn_gb300 dot_ozaki: real float64 operands only")
-    plan = P.ozaki_dot_plan(meta_dot, slices)
+    plan = P.ozaki_dot_plan(meta_dot, slices, A.is_complex())
     out = torch.zeros(Dsize, dtype=A.dtype, device=A.device)
     run_gemm(plan.native, A, B, out)  # short (K < 16) and skinny sectors: native FP64
     if len(plan.tiles) == 0:
         return out
     dev = A.device
-    tc = OZAKI_TC[0]
-    dar, dbr, dout, dtl = _dev(plan, 'ozaki_tc' if tc else 'ozaki',
-                               (plan.a_recs, plan.b_recs, plan.outs, plan.tiles_tc if tc else plan.tiles), dev)
-    a_sl = torch.empty(plan.a_size, dtype=torch.bfloat16, device=dev)
-    b_sl = torch.empty(plan.b_size, dtype=torch.bfloat16, device=dev)
+    tc = plan.prefer_tc if OZAKI_TC[0] is None else OZAKI_TC[0]
+    if tc:
+        dar, dbr, dout, dtl = _dev(plan, 'ozaki_tc', (plan.a_recs_tc, plan.b_recs_tc, plan.outs_tc, plan.tiles_tc),
+                                   dev)
+    else:
+        dar, dbr, dout, dtl = _dev(plan, 'ozaki', (plan.a_recs, plan.b_recs, plan.outs, plan.tiles), dev)
+    a_sl = torch.empty(plan.a_size_tc if tc else plan.a_size, dtype=torch.bfloat16, device=dev)
+    b_sl = torch.empty(plan.b_size_tc if tc else plan.b_size, dtype=torch.bfloat16, device=dev)
     a_ex = torch.empty(max(plan.a_exps, 1), dtype=torch.int32, device=dev)
     b_ex = torch.empty(max(plan.b_exps, 1), dtype=torch.int32, device=dev)
     bT = run_copy(plan.bT, B, torch.empty(max(plan.bT_size, 1), dtype=B.dtype, device=dev))
     st = _stream()
-    N.call('yb_ozaki_split', _ptr(A), _ptr(a_sl), _ptr(a_ex), _ptr(dar), len(plan.a_recs), plan.a_rows, slices, st)
-    N.call('yb_ozaki_split', _ptr(bT), _ptr(b_sl), _ptr(b_ex), _ptr(dbr), len(plan.b_recs), plan.b_rows, slices, st)
     if tc:
+        N.call('yb_ozaki_split_tiled', _ptr(A), _ptr(a_sl), _ptr(a_ex), _ptr(dar), len(plan.a_recs), plan.a_rows,
+               slices, P.OZAKI_TC_M, st)
+        N.call('yb_ozaki_split_tiled', _ptr(bT), _ptr(b_sl), _ptr(b_ex), _ptr(dbr), len(plan.b_recs), plan.b_rows,
+               slices, P.OZAKI_TC_N, st)
         N.call('yb_ozaki_gemm_tc', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
                len(plan.tiles_tc), slices, st)
     else:
+        N.call('yb_ozaki_split', _ptr(A), _ptr(a_sl), _ptr(a_ex), _ptr(dar), len(plan.a_recs), plan.a_rows, slices,
+               st)
+        N.call('yb_ozaki_split', _ptr(bT), _ptr(b_sl), _ptr(b_ex), _ptr(dbr), len(plan.b_recs), plan.b_rows, slices,
+               st)
         N.call('yb_ozaki_gemm', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
                len(plan.tiles), slices, st)
     return out
