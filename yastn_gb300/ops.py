@@ -143,7 +143,8 @@ def dot(A, B, meta_dot, Dsize):
 OZAKI_SLICES = 8  # 57 bits per operand: FP64-grade products
 
 
-OZAKI_TC = [None]  # emulated GEMM kernel: None = per dot by tile padding, True = tcgen05/TMEM, False = mma.sync
+OZAKI_TC = [None]  # emulated GEMM kernel: None = autotuned per dot, True = tcgen05/TMEM, False = mma.sync
+OZAKI_AUTOTUNE = [True]  # False: choose by the tile-padding estimate without timing
 
 
 def dot_ozaki(A, B, meta_dot, Dsize, slices=OZAKI_SLICES):
@@ -161,8 +162,35 @@ def dot_ozaki(A, B, meta_dot, Dsize, slices=OZAKI_SLICES):
     run_gemm(plan.native, A, B, out)  # short (K < 16) and skinny sectors: native FP64
     if len(plan.tiles) == 0:
         return out
+    if OZAKI_TC[0] is not None:
+        tc = OZAKI_TC[0]
+    else:
+        if getattr(plan, 'tuned_tc', None) is None:
+            plan.tuned_tc = _autotune_ozaki(plan, A, B, out, slices)
+        tc = plan.tuned_tc
+    _ozaki_run(plan, A, B, out, slices, tc)
+    return out
+
+
+def _autotune_ozaki(plan, A, B, out, slices):
+    """Kernel choice for one dot metadata: the tcgen05 and the mma.sync kernels produce the
+    same bits, so the first call times both (CUDA events; skipped during stream capture,
+    where the tile-padding estimate decides) and the plan keeps the faster."""
+    if not OZAKI_AUTOTUNE[0] or torch.cuda.is_current_stream_capturing():
+        return plan.prefer_tc
+    times = {}
+    for tc in (False, True, False, True):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _ozaki_run(plan, A, B, out, slices, tc)
+        e1.record()
+        e1.synchronize()
+        times[tc] = e0.elapsed_time(e1)  # the second (warm) measurement of each kernel is kept
+    return times[True] < times[False]
+
+
+def _ozaki_run(plan, A, B, out, slices, tc):
     dev = A.device
-    tc = plan.prefer_tc if OZAKI_TC[0] is None else OZAKI_TC[0]
     if tc:
         dar, dbr, dout, dtl = _dev(plan, 'ozaki_tc', (plan.a_recs_tc, plan.b_recs_tc, plan.outs_tc, plan.tiles_tc),
                                    dev)
@@ -188,7 +216,6 @@ def dot_ozaki(A, B, meta_dot, Dsize, slices=OZAKI_SLICES):
                st)
         N.call('yb_ozaki_gemm', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
                len(plan.tiles), slices, st)
-    return out
 
 
 def ozaki_device_error(reset=True):
