@@ -181,6 +181,7 @@ def _autotune_ozaki(plan, A, B, out, slices):
     times = {}
     for tc in (False, True, False, True):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda._sleep(2_000_000)  # hold the stream while the host enqueues: time the GPU, not the host
         e0.record()
         _ozaki_run(plan, A, B, out, slices, tc)
         e1.record()
