@@ -433,7 +433,7 @@ def run_gpu(args, wl):
     t_gemm = sum(a.elapsed_time(b) for a, b in gemm_ev) / len(gemm_ev) * 1e-3
     oz = ozaki_dot_plan(wl.mdot[0], ops.OZAKI_SLICES, wl.complex_gemm)
     tensor_flops = oz.flops * ops.OZAKI_SLICES * (ops.OZAKI_SLICES + 1) // 2
-    use_tc = oz.prefer_tc if ops.OZAKI_TC[0] is None else ops.OZAKI_TC[0]
+    use_tc = getattr(oz, 'tuned_tc', oz.prefer_tc) if ops.OZAKI_TC[0] is None else ops.OZAKI_TC[0]
     top_name = 'tcgen05 (TMEM accumulators)' if use_tc else 'mma.sync'
 
     BK.set_gemm_mode('fp64')
