@@ -432,7 +432,33 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_
                : "memory");
 }
 
-template <int S>
+__device__ __forceinline__ void bulk_load_mc(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar,
+                                             uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1], %2, [%3], %4;"
+      ::"r"(dst), "l"(src), "r"(bytes), "r"(mbar), "h"(mask)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar, uint16_t mask, bool multicast) {
+  if (multicast)
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+                 ::"r"(mbar), "h"(mask));
+  else
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
+}
+
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// CS CTAs of a cluster compute CS adjacent 64-column tiles of the same 128-row tile: they
+// need the same A digit tiles, so CTA r bulk-copies the A slices t with t % CS == r to all
+// of them (multicast), and each loads its own B tiles. A stage is refilled once the MMAs of
+// every CTA of the cluster have read it: each CTA's tcgen05.commit arrives on that stage's
+// "empty" barrier in all CTAs (initialised with CS arrivals). A tile past the sector's last
+// column tile (tile record w = 1, a ragged end) only serves its A share and its commits.
+template <int S, int CS>
 __global__ void __launch_bounds__(kTcThreads, 1)
     ozaki_gemm_tc_kernel(const __nv_bfloat16* __restrict__ As, const int* __restrict__ Ae,
                          const __nv_bfloat16* __restrict__ Bs, const int* __restrict__ Be, double* __restrict__ C,
@@ -440,11 +466,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   constexpr uint32_t kATile = kTcM * kK * 2;  // 4096 B: one slice's 128 x 16 digit tile
   constexpr uint32_t kBTile = kTcN * kK * 2;  // 2048 B
   constexpr uint32_t kStage = S * (kATile + kBTile);
+  constexpr uint16_t kMask = (uint16_t)((1u << CS) - 1u);
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint32_t tmem_slot;
   __shared__ __align__(8) uint64_t full[kTcStages], empty[kTcStages], accb;
   __shared__ int failed;
   const int4 tl = reinterpret_cast<const int4*>(tiles)[blockIdx.x];
+  const bool phantom = tl.w == 1;
   const int64_t* o = outs + (int64_t)tl.x * 16;
   const int64_t c_off = o[0], m = o[1], n = o[2], ldc = o[3];
   const int64_t a_sl = o[4], a_ex = o[5], b_sl = o[6], b_ex = o[7], Kp = o[9];
@@ -452,6 +480,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int64_t row0 = (int64_t)tl.y * kTcM, col0 = (int64_t)tl.z * kTcN;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t sbase = smem_u32(smem);
+  uint32_t rank = 0;
+  if (CS > 1) asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -461,7 +491,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   if (tid == 0) {
     for (int i = 0; i < kTcStages; ++i) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[i])));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&empty[i])), "r"(CS));
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&accb)));
     asm volatile("fence.mbarrier_init.release.cluster;");
@@ -469,6 +499,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
+  if (CS > 1) cluster_sync();  // every CTA's barriers exist before anyone copies or commits into them
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_slot;
 
@@ -477,14 +508,19 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int64_t a_slice = (m + kTcM - 1) / kTcM * kTcM * Kp, b_slice = (n + kTcN - 1) / kTcN * kTcN * Kp;
   const __nv_bfloat16* a_tiles = As + a_sl + (int64_t)tl.y * ksteps * (kTcM * kK);
   const __nv_bfloat16* b_tiles = Bs + b_sl + (int64_t)tl.z * ksteps * (kTcN * kK);
-  // producer (thread 0): one stage = S A tiles + S B tiles, each one bulk copy
+  const uint32_t stage_bytes = S * kATile + (phantom ? 0u : S * kBTile);
+  // producer (thread 0): this CTA's share of the A tiles (to every CTA of the cluster) and its B tiles
   auto issue = [&](int stage, int64_t step) {
     const uint32_t fb = smem_u32(&full[stage]);
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(kStage) : "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(stage_bytes) : "memory");
     const uint32_t d0 = sbase + (uint32_t)stage * kStage;
     for (int t = 0; t < S; ++t) {
-      bulk_load(d0 + t * kATile, a_tiles + t * a_slice + step * (kTcM * kK), kATile, fb);
-      bulk_load(d0 + S * kATile + t * kBTile, b_tiles + t * b_slice + step * (kTcN * kK), kBTile, fb);
+      if (t % CS == (int)rank) {
+        const void* src = a_tiles + t * a_slice + step * (kTcM * kK);
+        if (CS > 1) bulk_load_mc(d0 + t * kATile, src, kATile, fb, kMask);
+        else bulk_load(d0 + t * kATile, src, kATile, fb);
+      }
+      if (!phantom) bulk_load(d0 + S * kATile + t * kBTile, b_tiles + t * b_slice + step * (kTcN * kK), kBTile, fb);
     }
   };
   const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
@@ -505,14 +541,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         if (!mbar_wait(smem_u32(&full[stage]), (uint32_t)((st / kTcStages) & 1))) { failed = 1; break; }
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t a0 = sbase + (uint32_t)stage * kStage, b0 = a0 + S * kATile;
+        if (!phantom) {
 #pragma unroll
-        for (int ta = 0; ta < S; ++ta)
+          for (int ta = 0; ta < S; ++ta)
 #pragma unroll
-          for (int tb = 0; tb < S - ta; ++tb)
-            tc_mma(tmem + (uint32_t)((ta + tb) * kTcN), umma_desc(a0 + ta * kATile), umma_desc(b0 + tb * kBTile),
-                   idesc, (st == s0 && ta == 0) ? 0u : 1u);
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-            smem_u32(&empty[stage])));
+            for (int tb = 0; tb < S - ta; ++tb)
+              tc_mma(tmem + (uint32_t)((ta + tb) * kTcN), umma_desc(a0 + ta * kATile), umma_desc(b0 + tb * kBTile),
+                     idesc, (st == s0 && ta == 0) ? 0u : 1u);
+        }
+        tc_commit(smem_u32(&empty[stage]), kMask, CS > 1);
         consumed = st + 1;
         // refill the stage of step st-1 (its MMAs ran while those of step st were queued)
         if (st >= 1 && issued < ksteps && issued == st - 1 + kTcStages) {
@@ -523,38 +560,39 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
       }
       // the accumulators of this chunk are complete once every MMA issued so far is
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          smem_u32(&accb)));
+      tc_commit(smem_u32(&accb), kMask, false);
     }
     if (!mbar_wait(smem_u32(&accb), (uint32_t)(ch & 1))) failed = 1;
     asm volatile("tcgen05.fence::after_thread_sync;");
+    if (!phantom) {
 #pragma unroll
-    for (int cb = 0; cb < kTcN / 8; ++cb) {
-      long long hi[8], lo[8];
+      for (int cb = 0; cb < kTcN / 8; ++cb) {
+        long long hi[8], lo[8];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) hi[j] = lo[j] = 0;
+        for (int j = 0; j < 8; ++j) hi[j] = lo[j] = 0;
 #pragma unroll
-      for (int d = 0; d < S; ++d) {
-        uint32_t v[8];
-        tc_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(d * kTcN + cb * 8), v);
-        asm volatile("tcgen05.wait::ld.sync.aligned;");
+        for (int d = 0; d < S; ++d) {
+          uint32_t v[8];
+          tc_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(d * kTcN + cb * 8), v);
+          asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const long long q = (long long)__float2int_rn(__uint_as_float(v[j]));
-          if (d < 4) hi[j] += q << (7 * (3 - d));
-          else lo[j] += q << (7 * (S - 1 - d));
+          for (int j = 0; j < 8; ++j) {
+            const long long q = (long long)__float2int_rn(__uint_as_float(v[j]));
+            if (d < 4) hi[j] += q << (7 * (3 - d));
+            else lo[j] += q << (7 * (S - 1 - d));
+          }
         }
-      }
 #pragma unroll
-      for (int j = 0; j < 8; ++j)
-        acc64[cb * 8 + j] += int_to_double_scaled(hi[j], -21) + int_to_double_scaled(lo[j], -7 * (S - 1));
+        for (int j = 0; j < 8; ++j)
+          acc64[cb * 8 + j] += int_to_double_scaled(hi[j], -21) + int_to_double_scaled(lo[j], -7 * (S - 1));
+      }
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();  // every lane has read the accumulators before the next chunk overwrites them
     if (failed) break;
   }
   if (failed) {
-    // drain: the bulk copies issued but not consumed, and the MMAs (complete in issue order)
+    // drain: the bulk copies expected but not consumed, and the MMAs (complete in issue order)
     if (tid == 0) {
       atomicExch(err, 1);
       for (int64_t j = consumed; j < issued; ++j)
@@ -563,37 +601,59 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         mbar_wait(smem_u32(&empty[(consumed - 1) % kTcStages]), (uint32_t)(((consumed - 1) / kTcStages) & 1));
     }
   } else {
-    // epilogue through shared memory (the stages are free): row-major 128 x 64 doubles,
-    // padded rows; then coalesced stores with the row/column exponents applied
-    double* tileC = reinterpret_cast<double*>(smem);
-    const int r = warp * 32 + lane;
+    if (tid == 0) {
+      // every CTA of the cluster has committed its last MMAs on this CTA's stage barriers
+      for (int64_t j = max((int64_t)0, ksteps - kTcStages); j < ksteps; ++j)
+        if (!mbar_wait(smem_u32(&empty[j % kTcStages]), (uint32_t)((j / kTcStages) & 1))) atomicExch(err, 1);
+    }
+    if (!phantom) {
+      // epilogue through shared memory (the stages are free): row-major 128 x 64 doubles,
+      // padded rows; then coalesced stores with the row/column exponents applied
+      double* tileC = reinterpret_cast<double*>(smem);
+      const int r = warp * 32 + lane;
 #pragma unroll
-    for (int j = 0; j < kTcN; ++j) tileC[r * (kTcN + 1) + j] = acc64[j];
-    __syncthreads();
-    for (int e = tid; e < kTcM * kTcN; e += kTcThreads) {
-      const int rr = e / kTcN, cc = e % kTcN;
-      const int64_t gi = row0 + rr, gj = col0 + cc;
-      if (gi < m && gj < n)
-        C[c_off + gi * ldc + gj * ccs] = scale_pow2(tileC[rr * (kTcN + 1) + cc], Ae[a_ex + gi] + Be[b_ex + gj] - 14);
+      for (int j = 0; j < kTcN; ++j) tileC[r * (kTcN + 1) + j] = acc64[j];
+      __syncthreads();
+      for (int e = tid; e < kTcM * kTcN; e += kTcThreads) {
+        const int rr = e / kTcN, cc = e % kTcN;
+        const int64_t gi = row0 + rr, gj = col0 + cc;
+        if (gi < m && gj < n)
+          C[c_off + gi * ldc + gj * ccs] =
+              scale_pow2(tileC[rr * (kTcN + 1) + cc], Ae[a_ex + gi] + Be[b_ex + gj] - 14);
+      }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
+  if (CS > 1) cluster_sync();  // no CTA leaves while a peer may still copy or commit into it
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
 }
 
-template <int S>
+template <int S, int CS>
 int launch_gemm_tc(const void* As, const int* Ae, const void* Bs, const int* Be, double* C, const int64_t* outs,
                    const int32_t* tiles, int n_tiles, int* err, cudaStream_t s) {
   const size_t smem = (size_t)kTcStages * S * (kTcM + kTcN) * kK * 2;
   static_assert((size_t)kTcM * (kTcN + 1) * 8 <= (size_t)kTcStages * 6 * (kTcM + kTcN) * kK * 2,
                 "epilogue tile must fit in the stage buffers");
-  cudaError_t e =
-      cudaFuncSetAttribute(ozaki_gemm_tc_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (n_tiles % CS != 0) return YB_ERR_INVALID;
+  auto kern = ozaki_gemm_tc_kernel<S, CS>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
-  ozaki_gemm_tc_kernel<S><<<n_tiles, kTcThreads, smem, s>>>((const __nv_bfloat16*)As, Ae, (const __nv_bfloat16*)Bs,
-                                                            Be, C, outs, tiles, err);
-  return check_launch();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)n_tiles);
+  cfg.blockDim = dim3(kTcThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, kern, (const __nv_bfloat16*)As, Ae, (const __nv_bfloat16*)Bs, Be, C, outs, tiles, err);
+  if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
+  return YB_OK;
 }
 
 }  // namespace
@@ -640,19 +700,22 @@ int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices,
 static __device__ int g_ozaki_tc_error;
 
 int yb_ozaki_gemm_tc(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps, double* c,
-                     const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count, void* stream) {
+                     const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count, int cluster,
+                     void* stream) {
   if (n_tiles == 0) return YB_OK;
   if (!a_slices || !a_exps || !b_slices || !b_exps || !c || !outs || !tiles) return YB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
   int* err = nullptr;
   cudaError_t e = cudaGetSymbolAddress((void**)&err, g_ozaki_tc_error);
   if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
-  switch (slices_count) {
-    case 6: return yb::launch_gemm_tc<6>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
-    case 7: return yb::launch_gemm_tc<7>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
-    case 8: return yb::launch_gemm_tc<8>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
-    default: return YB_ERR_INVALID;
-  }
+#define YB_TC_CASE(S_, CS_) \
+  if (slices_count == S_ && cluster == CS_) \
+    return yb::launch_gemm_tc<S_, CS_>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
+  YB_TC_CASE(8, 1) YB_TC_CASE(8, 2) YB_TC_CASE(8, 4)
+  YB_TC_CASE(7, 1) YB_TC_CASE(7, 2) YB_TC_CASE(7, 4)
+  YB_TC_CASE(6, 1) YB_TC_CASE(6, 2) YB_TC_CASE(6, 4)
+#undef YB_TC_CASE
+  return YB_ERR_INVALID;
 }
 
 int yb_ozaki_device_error(int* out, int reset, void* stream) {
