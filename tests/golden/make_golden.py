@@ -652,6 +652,211 @@ def scen_cfg3():
     save('cfg3', rec, extra)
 
 
+class OpRecorder:
+    """Records every call into a backend module and the torch operations applied to tensors
+    outside those calls (a TorchFunctionMode), as the op list of yastn_gb300.replay: tensors
+    become dataflow keys; tensors the sequence never produced become stored constants.
+    ``checkpoint`` is transparent: the function it wraps is recorded step by step, between
+    markers."""
+
+    def __init__(self, module):
+        import torch
+        from torch.overrides import TorchFunctionMode
+        self.torch = torch
+        self.module = module
+        self.ops, self.consts, self.keys, self.refs = [], {}, {}, []
+        self.depth = 0
+        self.active = False
+        self.orig = {}
+        rec = self
+
+        class Mode(TorchFunctionMode):
+            def __torch_function__(mode, func, types, args=(), kwargs=None):
+                kwargs = kwargs or {}
+                out = func(*args, **kwargs)
+                if rec.active and rec.depth == 0:
+                    rec._torch_op(func, args, kwargs, out)
+                return out
+        self.mode = Mode()
+        for nm in module.__all__:
+            f = getattr(module, nm)
+            if callable(f) and not isinstance(f, type):
+                self.orig[nm] = f
+                setattr(module, nm, self._wrap(nm, f))
+
+    def restore(self):
+        for nm, f in self.orig.items():
+            setattr(self.module, nm, f)
+
+    def key(self, t, name=None):
+        k = self.keys.get(id(t))
+        if k is None:
+            k = name or f"t{len(self.keys)}"
+            self.keys[id(t)] = k
+            self.refs.append(t)
+        return k
+
+    def _enc(self, x):
+        torch = self.torch
+        if isinstance(x, torch.Tensor):
+            if id(x) not in self.keys:  # a constant made before recording
+                k = self.key(x, f"c{len(self.consts)}")
+                self.consts[k] = x.detach().resolve_conj().cpu().numpy().copy()
+            return {'__t__': self.keys[id(x)]}
+        if isinstance(x, np.ndarray):
+            k = f"c{len(self.consts)}"
+            self.consts[k] = np.array(x, copy=True)
+            return {'__t__': k}
+        if isinstance(x, tuple) or isinstance(x, torch.Size):
+            return [self._enc(y) for y in x]
+        if isinstance(x, list):
+            return {'__list__': [self._enc(y) for y in x]}
+        if isinstance(x, dict):
+            return {'__dict__': [[self._enc(k), self._enc(v)] for k, v in x.items()]}
+        if isinstance(x, slice):
+            return {'__slice__': [x.start, x.stop, x.step]}
+        if isinstance(x, torch.dtype):
+            return {'__dtype__': str(x).replace('torch.', '')}
+        if isinstance(x, torch.device):
+            return {'__device__': 1}
+        if x is Ellipsis:
+            return {'__ellipsis__': 1}
+        if isinstance(x, str) and x == 'cpu':
+            return {'__devstr__': 1}
+        if isinstance(x, (np.integer,)):
+            return int(x)
+        if isinstance(x, (np.floating,)):
+            return float(x)
+        if isinstance(x, (np.bool_,)):
+            return bool(x)
+        if isinstance(x, (int, float, bool, str)) or x is None:
+            return x
+        raise TypeError(f"cannot record argument of type {type(x)}")
+
+    def _outs(self, out):
+        torch = self.torch
+        if isinstance(out, torch.Tensor):
+            return self.key(out)
+        if isinstance(out, (tuple, list)) and any(isinstance(o, torch.Tensor) for o in out):
+            return [self.key(o) if isinstance(o, torch.Tensor) else None for o in out]
+        return None
+
+    def _wrap(self, nm, f):
+        rec = self
+
+        def wrapped(*args, **kwargs):
+            if not rec.active or rec.depth > 0:
+                return f(*args, **kwargs)
+            if nm == 'checkpoint':  # transparent: record the wrapped function's steps
+                fn, fargs = args[0], args[1:]
+                rec.ops.append({'k': 'mark', 'fn': 'checkpoint_begin'})
+                out = fn(*fargs)
+                rec.ops.append({'k': 'mark', 'fn': 'checkpoint_end'})
+                return out
+            rec.depth += 1
+            try:
+                a = [rec._enc(x) for x in args]
+                kw = {k: rec._enc(v) for k, v in kwargs.items()}
+                out = f(*args, **kwargs)
+                o = rec._outs(out)
+            finally:
+                rec.depth -= 1
+            rec.ops.append({'k': 'b', 'fn': nm, 'a': a, 'kw': kw, 'o': o})
+            return out
+        return wrapped
+
+    def _torch_op(self, func, args, kwargs, out):
+        torch = self.torch
+        name = getattr(func, '__name__', '')
+        qual = getattr(func, '__qualname__', '')
+        inplace = name == '__setitem__' or (name.endswith('_') and not name.startswith('_'))
+        tensor_out = isinstance(out, torch.Tensor) or (isinstance(out, (tuple, list)) and
+                                                         any(isinstance(o, torch.Tensor) for o in out))
+        if not (tensor_out or inplace):
+            return
+        self.depth += 1
+        try:
+            if qual.startswith('getset_descriptor') or type(func).__name__ == 'method-wrapper':
+                attr = getattr(getattr(func, '__self__', None), '__name__', None)
+                fn = 'a:' + str(attr)
+                a = [self._enc(args[0])]
+            elif qual.startswith(('TensorBase.', 'Tensor.', '_TensorBase.')):
+                fn = 'm:' + name
+                a = [self._enc(x) for x in args]
+            else:
+                fn = 'f:' + name
+                a = [self._enc(x) for x in args]
+            kw = {k: self._enc(v) for k, v in kwargs.items()}
+            o = self._outs(out) if tensor_out else None
+        finally:
+            self.depth -= 1
+        self.ops.append({'k': 't', 'fn': fn, 'a': a, 'kw': kw, 'o': o})
+
+    def __enter__(self):
+        self.active = True
+        self.mode.__enter__()
+        return self
+
+    def __exit__(self, *exc):
+        self.mode.__exit__(*exc)
+        self.active = False
+
+
+def scen_ctmrg(chi=24, sweeps=8, name='ctmrg_z2_d6'):
+    """Differentiable CTMRG of an iPEPS on a 1x1 unit cell (yastn.tn.fpeps): Z2 symmetry,
+    site tensor with bond D=6 (3+3 over parities) and physical d=2 (1+1), rand(normal) after
+    random_seed(0); EnvCTM(init='eye'), ctmrg_ with D_total=chi for a fixed number of sweeps
+    (moves 'hv', SVD projectors: use_qr=False, checkpoint_move='nonreentrant'); energy of the
+    transverse-field Ising model per site E = -h <Z> - sum over the two bonds <X X> with
+    h = 3, and its gradient with respect to the site tensor (backward through torch
+    autograd of the reference torch backend, on CPU). Records the forward call sequence
+    (OpRecorder), the site tensor, E and the gradient."""
+    import time
+    import torch
+    import yastn.tn.fpeps as fpeps
+    import yastn.backend.backend_torch as bt
+    torch.set_default_dtype(torch.float64)
+    cfg = yastn.make_config(sym='Z2', backend=bt, default_dtype='float64')
+    cfg.backend.random_seed(0)
+    vl = yastn.Leg(cfg, s=1, t=(0, 1), D=(3, 3))
+    pl = yastn.Leg(cfg, s=1, t=(0, 1), D=(1, 1))
+    A = yastn.rand(cfg, legs=[vl.conj(), vl, vl, vl.conj(), pl], distribution='normal')
+    op = yastn.operators.Spin12(sym='Z2', backend=bt, default_dtype='float64')
+    Z, X = op.z(), op.x()
+    A._data.requires_grad_(True)
+    rec = OpRecorder(bt)
+    rec.key(A._data, 'in:A')
+    t0 = time.time()
+    with rec:
+        psi = fpeps.Peps(fpeps.SquareLattice(dims=(1, 1), boundary='infinite'), tensors={(0, 0): A})
+        env = fpeps.EnvCTM(psi, init='eye', leg=yastn.Leg(cfg, s=1, t=(0, 1), D=(1, 1)))
+        for _ in env.ctmrg_(opts_svd={'D_total': chi}, max_sweeps=sweeps, iterator=True, use_qr=False,
+                            checkpoint_move='nonreentrant'):
+            pass
+        ez = env.measure_1site(Z)
+        exx = env.measure_nn(X, X)
+        E = -3.0 * sum(ez.values()) - sum(exx.values())
+    t_fwd = time.time() - t0
+    rec.restore()
+    ekey = rec.key(E)
+    t1 = time.time()
+    E.backward()
+    t_bwd = time.time() - t1
+    grad = A._data.grad.detach().numpy().copy()
+    arrays = dict(rec.consts)
+    arrays['in:A'] = A._data.detach().numpy().copy()
+    arrays['ref:grad'] = grad
+    payload = {'scenario': name, 'ops': rec.ops, 'inputs': {'A': 'in:A'}, 'outputs': {'E': ekey},
+               'E': float(E.detach()), 'chi': chi, 'sweeps': sweeps, 'D': 6, 'h': 3.0,
+               'cpu_seconds': {'forward': t_fwd, 'backward': t_bwd}}
+    with open(os.path.join(HERE, name + '.json'), 'w') as f:
+        json.dump(payload, f, separators=(',', ':'))
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **arrays)
+    nb = sum(1 for o in rec.ops if o['k'] == 'b')
+    print(f"{name}: {len(rec.ops)} ops ({nb} backend calls), E = {float(E.detach()):.12f}, "
+          f"fwd {t_fwd:.1f} s, bwd {t_bwd:.1f} s")
+
+
 def _arr_from(rec, x):
     return rec.arrays[x['__array__']]
 
@@ -671,3 +876,4 @@ if __name__ == '__main__':
     scen_cfg2()
     scen_cfg3()
     scen_cfg5()
+    scen_ctmrg()

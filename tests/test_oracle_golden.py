@@ -233,3 +233,18 @@ def test_heff2_replay_and_lanczos_match_reference():
     lam, _ = ritz_lowest(al, be)
     assert abs(lam - wl.tr['lanczos_lowest']) <= 1e-10 * abs(wl.tr['lanczos_lowest'])
     assert wl.flops == 630254080 or abs(wl.flops - 6.303e8) < 1e6
+
+
+def test_ctmrg_recording_dataflow_is_closed():
+    """The recorded CTMRG sequence only uses tensors it produced, its input or its stored
+    constants, and its output (the energy) is produced by it."""
+    from yastn_gb300.replay import load_replay, check_dataflow
+    r = load_replay('ctmrg_z2_d6')
+    n, used = check_dataflow(r)
+    produced = set()
+    for op in r.ops:
+        o = op.get('o')
+        produced.update(o if isinstance(o, list) else [o])
+    assert r.outputs['E'] in produced and 'in:A' in used
+    calls = r.backend_calls()
+    assert calls['svd'] == 32 and calls['dot'] == 697 and calls['transpose_and_merge'] == 1045

@@ -1,0 +1,158 @@
+"""Replay of a recorded sequence of backend calls and tensor operations.
+
+YASTN's algorithms (CTMRG, DMRG, ...) drive the backend through the functions of the backend
+module plus a few torch operations on the blocks' data (scalar scalings, reshapes, in-place
+block writes). A recording made with the reference backend (tests/golden/make_golden.py,
+``scen_ctmrg``) stores that sequence: for every step the function name, the arguments
+(metadata tuples and Python values verbatim, tensors as keys of the dataflow) and the keys of
+its results. ``CallReplay.run`` executes the same sequence with another backend module —
+the same names and signatures, e.g. ``yastn_gb300.backend`` — on another device, so the
+whole algorithm, forward and (through the backend's autograd Functions) backward, runs on
+the GPU without YASTN itself. Data-dependent decisions the algorithm took on the host
+(truncated dimensions, ...) are part of the recorded metadata; the replay reproduces them
+when its values agree with the recording's.
+"""
+import json
+import os
+
+import numpy as np
+import torch
+
+from .workloads import GOLDEN
+
+__all__ = ['CallReplay', 'load_replay']
+
+
+def load_replay(name, directory=GOLDEN):
+    with open(os.path.join(directory, name + '.json')) as f:
+        payload = json.load(f)
+    npz = os.path.join(directory, name + '.npz')
+    arrays = dict(np.load(npz)) if os.path.exists(npz) else {}
+    return CallReplay(payload, arrays)
+
+
+_DTYPES = {'float64': torch.float64, 'complex128': torch.complex128, 'float32': torch.float32,
+           'complex64': torch.complex64, 'bool': torch.bool, 'int64': torch.int64, 'int32': torch.int32,
+           'uint8': torch.uint8}
+
+
+class CallReplay:
+    """A recorded call sequence (see the module docstring)."""
+
+    def __init__(self, payload, arrays):
+        self.payload = payload
+        self.ops = payload['ops']
+        self.arrays = arrays
+        self.inputs = payload.get('inputs', {})
+        self.outputs = payload.get('outputs', {})
+
+    def backend_calls(self):
+        """Names of the backend functions the sequence calls, with counts."""
+        out = {}
+        for op in self.ops:
+            if op['k'] == 'b':
+                out[op['fn']] = out.get(op['fn'], 0) + 1
+        return out
+
+    def run(self, backend, device, inputs, constants_dtype=None):
+        """Execute the sequence. ``inputs`` maps recorded input names to tensors; returns the
+        dict of every produced tensor by key (outputs under ``self.outputs``)."""
+        dev = torch.device(device)
+        env = {}
+        for name, key in self.inputs.items():
+            env[key] = inputs[name]
+        consts = {}
+
+        def dec(x):
+            if isinstance(x, list):
+                return tuple(dec(y) for y in x)
+            if isinstance(x, dict):
+                if '__t__' in x:
+                    k = x['__t__']
+                    if k in env:
+                        return env[k]
+                    if k not in consts:
+                        consts[k] = torch.from_numpy(np.ascontiguousarray(self.arrays[k])).to(dev)
+                    return consts[k]
+                if '__list__' in x:
+                    return [dec(y) for y in x['__list__']]
+                if '__dict__' in x:
+                    return {dec(k): dec(v) for k, v in x['__dict__']}
+                if '__slice__' in x:
+                    return slice(*x['__slice__'])
+                if '__dtype__' in x:
+                    return _DTYPES[x['__dtype__']]
+                if '__device__' in x:
+                    return dev
+                if '__devstr__' in x:
+                    return str(dev)
+                if '__ellipsis__' in x:
+                    return Ellipsis
+                raise ValueError(f"unknown encoding {list(x)}")
+            return x
+
+        for op in self.ops:
+            if op['k'] == 'mark':
+                continue
+            args = dec(op['a'])
+            kwargs = {k: dec(v) for k, v in op.get('kw', {}).items()}
+            if op['k'] == 'b':
+                out = getattr(backend, op['fn'])(*args, **kwargs)
+            else:
+                out = _torch_call(op['fn'], args, kwargs)
+            keys = op.get('o')
+            if keys is None:
+                continue
+            if isinstance(keys, list):
+                for k, v in zip(keys, out):
+                    if k is not None:
+                        env[k] = v
+            else:
+                env[keys] = out
+        return env
+
+
+def check_dataflow(replay):
+    """Every tensor argument is an input, a stored constant or the result of an earlier step;
+    returns (number of steps, set of keys used)."""
+    have = set(replay.inputs.values()) | set(replay.arrays)
+    used = set()
+
+    def walk(x):
+        if isinstance(x, list):
+            for y in x:
+                walk(y)
+        elif isinstance(x, dict):
+            if '__t__' in x:
+                k = x['__t__']
+                if k not in have:
+                    raise KeyError(f"tensor {k} used before it is produced")
+                used.add(k)
+            else:
+                for v in x.values():
+                    walk(v)
+    n = 0
+    for op in replay.ops:
+        if op['k'] == 'mark':
+            continue
+        walk(op['a'])
+        walk(list(op.get('kw', {}).values()))
+        o = op.get('o')
+        if isinstance(o, list):
+            have.update(k for k in o if k is not None)
+        elif o is not None:
+            have.add(o)
+        n += 1
+    return n, used
+
+
+def _torch_call(name, args, kwargs):
+    kind, _, fn = name.partition(':')
+    if kind == 'm':  # a Tensor method
+        if fn == '__setitem__':
+            args[0][args[1]] = args[2]
+            return None
+        return getattr(args[0], fn)(*args[1:], **kwargs)
+    if kind == 'a':  # a Tensor attribute
+        return getattr(args[0], fn)
+    return getattr(torch, fn)(*args, **kwargs)
