@@ -202,10 +202,14 @@ int yb_ozaki_dot_static(const double* A, const double* B, double* C,
  * X holds the k vectors (rows of A, or of A^T when m > n) of length L, W the k x k
  * accumulated rotations (X = W X_0 throughout).
  * pair_items: int32 pairs (block, pair index 0..N/2-1) over all blocks.
- * state: int64[4*n_blocks + 4]: per block (max |cos| of the sweep in progress as double
+ * state: int64[6*n_blocks + 4]: per block (max |cos| of the sweep in progress as double
  *   bits, converged flag, sweeps run in the current phase, largest |cos| of the last
- *   completed sweep), then the control
- *   words of the grid barrier (count, generation, error flag, all-converged flag).
+ *   completed sweep, and the squared noise row norms of the FP32 and FP64 phases as double
+ *   bits: (1e-5 scale_b ||A_b||_F)^2 and (1e-14 ||A_b||_F)^2, written by yb_svd_init), then
+ *   the control words of the grid barrier (count, generation, error flag, all-converged
+ *   flag). A pair with a row at or below its phase's noise norm is not rotated and does not
+ *   count for convergence (rank-deficient blocks would otherwise keep O(1) cosines among
+ *   their rounding-noise rows).
  * dtype: YB_F64 (workspaces float / double) or YB_C128 (complex64 / complex128, element
  *   offsets as above); tall complex blocks start from X_0 = A^H.
  * Sequence (mixed precision): yb_svd_init (X32 = scale_b (A or A^H), W32 = I, with
@@ -221,8 +225,9 @@ int yb_ozaki_dot_static(const double* A, const double* B, double* C,
  * shift != NULL (eigh): per-block shifts c_b = ||A_b||_F + 1 are computed and A_b + c_b I
  * is decomposed (Hermitian positive definite, so its SVD is its eigendecomposition);
  * finalize mode 1 writes eigenvalues ascending, mode 2 by descending magnitude, with
- * eigenvectors as columns of U (= W^H); mode 0 is the SVD (S descending, zero singular
- * values completed to orthonormal vectors).
+ * eigenvectors as columns of U (= W^H); mode 0 is the SVD (S descending; the vectors of
+ * singular values at or below the FP64 noise norm completed to orthonormal vectors; state
+ * as left by the sweeps, or NULL for a zero noise norm).
  * Replaces svd (backend_torch.py:318-319, torch_svd_gesdd.py:15-21) and eigh
  * (backend_torch.py:369-384, torch_eig_sym.py:14-32) for FP64 and complex128 blocks.
  */
@@ -246,7 +251,8 @@ int yb_svd_widen(const void* work32, void* work64, const int64_t* blocks, int n_
 int yb_svd_shift_prefill(void* work64, const int64_t* blocks, int n_blocks, int dtype,
                          const double* shift, void* stream);
 int yb_svd_finalize(const void* work, void* U, double* S, void* Vh, const int64_t* blocks,
-                    int n_blocks, int dtype, int max_k, int mode, const double* shift, void* stream);
+                    int n_blocks, int dtype, int max_k, int mode, const double* shift,
+                    const int64_t* state, void* stream);
 
 /* SVD adjoint core (torch_svd_gesdd.py:296-428): per block record YB_ADJ_REC int64:
  *   [0] dA offset [1] m [2] n [3] U/gU offset [4] S/gS offset [5] Vh/gVh offset

@@ -105,6 +105,31 @@ def test_svd_rank_deficient_and_zero_blocks(cuda_device):
     check_svd(data, meta, U, S, V, Sr)
 
 
+@pytest.mark.parametrize('cplx', [False, True])
+def test_svd_large_rank_deficient_blocks(cplx, cuda_device):
+    """Blocks of low numerical rank (products of thin factors, as the projector blocks of a
+    corner transfer matrix step): the rounding-noise rows are left out of the rotations and
+    their vectors completed, so Jacobi converges and the factorisation stays orthonormal."""
+    rng = np.random.default_rng(21)
+    specs = [(432, 432, 100), (300, 120, 40), (80, 250, 30), (256, 256, 200), (64, 64, 64)]
+    blocks = []
+    for m, n, r in specs:
+        f = lambda *sh: rng.normal(size=sh) + (1j * rng.normal(size=sh) if cplx else 0)
+        blocks.append((f(m, r) * np.logspace(0, -6, r)) @ f(r, n))
+    meta, off, oU, oS, oV, parts = [], 0, 0, 0, 0, []
+    for a in blocks:
+        m, n = a.shape
+        k = min(m, n)
+        meta.append(((off, off + m * n), (m, n), (oU, oU + m * k), (m, k), (oS, oS + k), (oV, oV + k * n), (k, n)))
+        off += m * n; oU += m * k; oS += k; oV += k * n
+        parts.append(a.ravel())
+    meta = tuple(meta)
+    data = np.concatenate(parts)
+    U, S, V = (host(x) for x in ops.svd(dev(data), meta, (oU, oS, oV)))
+    _, Sr, _ = oracle.svd(data, meta, (oU, oS, oV))
+    check_svd(data, meta, U, S, V, Sr)
+
+
 @pytest.mark.parametrize('blocked,rows', [(False, None), (True, 4), (True, 8), (True, 16)])
 def test_svd_fp32_phase_variants(blocked, rows, cuda_device):
     """Both FP32 phases (one pair per warp; super-vectors of 4/8/16 rows in shared memory)

@@ -37,8 +37,13 @@ constexpr long long kSpinLimit = 1ll << 22;
 // record fields
 enum { R_A = 0, R_M, R_N, R_U, R_S, R_V, R_X, R_W, R_P, R_K, R_L, R_NP, R_T, R_X32, R_W32, R_NSUP };
 // per-block state (int64): [0] max |cos| of the sweep in progress (double bits),
-// [1] converged flag, [2] sweeps run in the current phase, [3] largest |cos| of the last sweep
-enum { ST_MAXCOS = 0, ST_CONV = 1, ST_SWEEPS = 2, ST_LASTCOS = 3, ST_REC = 4 };
+// [1] converged flag, [2] sweeps run in the current phase, [3] largest |cos| of the last sweep,
+// [4], [5] squared row norms (double bits) at or below which a row is rounding noise in the
+// FP32 / FP64 phase: a pair with such a row is neither rotated nor counted for convergence,
+// and the finalisation completes the vectors of those rows like those of zero values
+enum { ST_MAXCOS = 0, ST_CONV = 1, ST_SWEEPS = 2, ST_LASTCOS = 3, ST_THR32 = 4, ST_THR64 = 5, ST_REC = 6 };
+constexpr double kNoise32 = 1e-5;   // noise row norm relative to ||A||_F in the FP32 phase
+constexpr double kNoise64 = 1e-14;  // idem in the FP64 phase (a few FP64 roundings of ||A||_F)
 // control words after the per-block state: [0] barrier count [1] barrier generation
 // [2] error flag [3] all-converged flag
 enum { C_COUNT = 0, C_GEN = 1, C_ERR = 2, C_DONE = 3, C_REC = 4 };
@@ -179,8 +184,8 @@ template <typename T>
 struct Rotation {
   using R = typename Num<T>::R;
   // scalar part: from the summed (al, be, g) to (c, s, u); |cos| to the running maximum
-  __device__ static bool scalar(R al, R be, T ga, int64_t L, int64_t* st, R& c, R& s, T& u) {
-    if (!(al > R(0) && be > R(0))) return false;
+  __device__ static bool scalar(R al, R be, T ga, int64_t L, int64_t* st, R& c, R& s, T& u, R thr2) {
+    if (!(al > thr2 && be > thr2 && al > R(0) && be > R(0))) return false;
     const R g = gabs(ga);
     const R cosv = g / (sqrt(al) * sqrt(be));
     atomicMax((unsigned long long*)st, (unsigned long long)__double_as_longlong((double)cosv));
@@ -199,12 +204,13 @@ struct Rotation {
     s = c * t;
     return true;
   }
-  __device__ static bool get(R al_, R be_, T ga_, int64_t L, int lane, int64_t* st, R& c, R& s, T& u) {
+  // thr2: squared noise norm of the phase; a pair with a row at or below it is left alone
+  __device__ static bool get(R al_, R be_, T ga_, int64_t L, int lane, int64_t* st, R& c, R& s, T& u, R thr2) {
     const R al = warp_sum(al_), be = warp_sum(be_);
     warp_sum_t<T>(ga_);
     if constexpr (sizeof(R) == 4) {
       // FP32: every lane computes the same (cheap) scalar part; one lane records |cos|
-      if (!(al > R(0) && be > R(0))) return false;
+      if (!(al > thr2 && be > thr2 && al > R(0) && be > R(0))) return false;
       const R g = gabs(ga_);
       const R cosv = g / (sqrtf(al) * sqrtf(be));
       if (lane == 0) atomicMax((unsigned long long*)st, (unsigned long long)__double_as_longlong((double)cosv));
@@ -224,7 +230,7 @@ struct Rotation {
       return true;
     } else {
       int rot = 0;
-      if (lane == 0) rot = scalar(al, be, ga_, L, st, c, s, u) ? 1 : 0;
+      if (lane == 0) rot = scalar(al, be, ga_, L, st, c, s, u, thr2) ? 1 : 0;
       rot = __shfl_sync(0xffffffffu, rot, 0);
       if (!rot) return false;
       c = __shfl_sync(0xffffffffu, c, 0);
@@ -257,7 +263,8 @@ __device__ __forceinline__ void rot2(T& a, T& b, typename Num<T>::R c, typename 
 // the block to underflow. The rotations, and so W, do not depend on the scale.
 template <typename TI>
 __global__ void block_fro_kernel(const TI* __restrict__ A, const int64_t* __restrict__ blocks,
-                                 double* __restrict__ shift, double* __restrict__ scale) {
+                                 double* __restrict__ shift, double* __restrict__ scale,
+                                 int64_t* __restrict__ state) {
   __shared__ double red[32];
   const int64_t* r = blocks + (int64_t)blockIdx.x * YB_SVD_REC;
   const int64_t cnt = r[R_M] * r[R_N];
@@ -280,6 +287,10 @@ __global__ void block_fro_kernel(const TI* __restrict__ A, const int64_t* __rest
     int e = 0;
     if (bound > 0.0 && bound <= 1.0e300) frexp(bound, &e);
     scale[blockIdx.x] = ldexp(1.0, -e);
+    // the FP32 phase works on scale * A, the FP64 phase on A itself
+    const double t32 = kNoise32 * fro * ldexp(1.0, -e), t64 = kNoise64 * fro;
+    state[(int64_t)blockIdx.x * ST_REC + ST_THR32] = __double_as_longlong(t32 * t32);
+    state[(int64_t)blockIdx.x * ST_REC + ST_THR64] = __double_as_longlong(t64 * t64);
   }
 }
 
@@ -309,7 +320,7 @@ __global__ void svd_init_kernel(const TI* __restrict__ A, T32* __restrict__ work
       W[f] = (i == j) ? Num<T32>::one() : Num<T32>::zero();
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x < ST_REC) state[blockIdx.y * ST_REC + threadIdx.x] = 0;
+  if (blockIdx.x == 0 && threadIdx.x < ST_THR32) state[blockIdx.y * ST_REC + threadIdx.x] = 0;
 }
 
 // W64 = widen(W32) (the host orthonormalises it next); resets the per-block state.
@@ -322,7 +333,7 @@ __global__ void svd_widen_kernel(const T32* __restrict__ work32, T64* __restrict
   T64* W = work64 + r[R_W];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < k * k; e += (int64_t)gridDim.x * blockDim.x)
     W[e] = to64(W32[e]);
-  if (blockIdx.x == 0 && threadIdx.x < ST_REC) state[blockIdx.y * ST_REC + threadIdx.x] = 0;
+  if (blockIdx.x == 0 && threadIdx.x < ST_THR32) state[blockIdx.y * ST_REC + threadIdx.x] = 0;
 }
 
 // X = shift_b * W (eigh: the FP64 phase then adds W A with the grouped GEMM, X = W (A + shift I)).
@@ -425,7 +436,8 @@ __device__ __forceinline__ void rotate_pair(T* __restrict__ X, T* __restrict__ W
   }
   R c = 0, s = 0;
   T u = Num<T>::one();
-  if (!Rotation<T>::get(al_, be_, ga_, L, lane, st + ST_MAXCOS, c, s, u)) return;
+  const R thr2 = (R)__longlong_as_double((long long)st[sizeof(R) == 4 ? ST_THR32 : ST_THR64]);
+  if (!Rotation<T>::get(al_, be_, ga_, L, lane, st + ST_MAXCOS, c, s, u, thr2)) return;
   rotate_rows<T>(xp, xq, L, lane, c, s, u);
   rotate_rows<T>(W + p * k, W + q * k, k, lane, c, s, u);
 }
@@ -568,7 +580,8 @@ __global__ void __launch_bounds__(BR * 32) svd_block_sweeps_kernel(T* __restrict
               }
               R c = 0, s = 0;
               T u = Num<T>::one();
-              if (Rotation<T>::get(al_, be_, ga_, L, lane, st + ST_MAXCOS, c, s, u)) {
+              const R thr2 = (R)__longlong_as_double((long long)st[ST_THR32]);
+              if (Rotation<T>::get(al_, be_, ga_, L, lane, st + ST_MAXCOS, c, s, u, thr2)) {
                 for (int64_t l = lane; l < L; l += 32) {
                   T a = xp[l], b = xq[l];
                   rot2<T>(a, b, c, s, u);
@@ -674,10 +687,13 @@ template <typename T>
 __global__ void __launch_bounds__(1024) svd_finalize_kernel(const T* __restrict__ work, T* __restrict__ U,
                                                             double* __restrict__ S, T* __restrict__ Vh,
                                                             const int64_t* __restrict__ blocks, int pow2,
-                                                            int mode, const double* __restrict__ shift) {
+                                                            int mode, const double* __restrict__ shift,
+                                                            const int64_t* __restrict__ state) {
   extern __shared__ unsigned char smem_raw[];
+  // [sig: pow2 doubles][complex: pow2 doubles][idx: pow2 ints]
   double* sig = reinterpret_cast<double*>(smem_raw);
-  int* idx = reinterpret_cast<int*>(sig + pow2);
+  double* cim = sig + pow2;
+  int* idx = reinterpret_cast<int*>(cim + (Num<T>::cplx ? pow2 : 0));
   __shared__ int n_zero;
   __shared__ double kmin;
   const int64_t* r = blocks + (int64_t)blockIdx.x * YB_SVD_REC;
@@ -749,9 +765,13 @@ __global__ void __launch_bounds__(1024) svd_finalize_kernel(const T* __restrict_
     }
     return;
   }
+  // rows at the rounding-noise level were not rotated: their vectors are completed like
+  // those of zero values (the values themselves are kept)
+  const double zthr = state ? sqrt(__longlong_as_double((long long)state[(int64_t)blockIdx.x * ST_REC + ST_THR64]))
+                            : 0.0;
   for (int j = threadIdx.x; j < k; j += blockDim.x) {
     Sb[j] = sig[j];
-    if (!(sig[j] > 0.0)) atomicAdd(&n_zero, 1);
+    if (!(sig[j] > zthr && sig[j] > 0.0)) atomicAdd(&n_zero, 1);
   }
   // wide (X_0 = A): Vh rows = x_j / s_j, U = W^H; tall (X_0 = A^H): U columns = conj(x_j) / s_j,
   // Vh = W
@@ -759,7 +779,7 @@ __global__ void __launch_bounds__(1024) svd_finalize_kernel(const T* __restrict_
     const int64_t j = e / L, l = e - j * L;
     const double sv = sig[j];
     const T x = X[(int64_t)idx[j] * L + l];
-    const T v = (sv > 0.0) ? rscale(x, 1.0 / sv) : rscale(x, 0.0);
+    const T v = (sv > zthr && sv > 0.0) ? rscale(x, 1.0 / sv) : rscale(x, 0.0);
     if (tall) Ub[l * k + j] = cconj_(v); else Vb[j * n + l] = v;
   }
   for (int64_t e = threadIdx.x; e < k * k; e += blockDim.x) {
@@ -769,69 +789,102 @@ __global__ void __launch_bounds__(1024) svd_finalize_kernel(const T* __restrict_
   }
   __syncthreads();
   if (n_zero == 0) return;
-  // completion: zero singular values sit at the end (positions k - n_zero .. k-1); replace
-  // their vectors by unit vectors orthogonalised (twice) against all earlier ones.
-  __shared__ double red[2][32];
-  __shared__ double coef[2];
+  // completion: the small values sit at the end (positions k - n_zero .. k-1); each of their
+  // vectors becomes a unit vector e_c orthogonalised against all earlier vectors by two passes
+  // of classical Gram-Schmidt (all coefficients of a pass at once). Candidates c run on from
+  // the last one tried; one whose residual exceeds 0.5 sqrt((L - j) / L) is taken (the
+  // residuals of all L unit vectors have squares summing to L - j, so one always qualifies).
+  // The coefficients of a pass live in shared memory: real parts in the sig array (no longer
+  // needed), imaginary parts in the complex area.
   const int64_t stride_v = tall ? k : 1;  // distance between consecutive entries of one vector
   const int64_t stride_j = tall ? 1 : n;  // distance between vectors
   T* base = tall ? Ub : Vb;
+  __shared__ double red[32];
+  __shared__ double nrm_s;
+  double* cre = sig;
+  int64_t cand = 0;
   for (int64_t j = k - n_zero; j < k; ++j) {
-    for (int64_t cand = 0; cand < L; ++cand) {
-      T* vj = base + j * stride_j;
+    T* vj = base + j * stride_j;
+    const double need = 0.5 * sqrt((double)(L - j) / (double)L);
+    for (int64_t tries = 0; tries < L; ++tries, cand = (cand + 1 == L ? 0 : cand + 1)) {
       for (int64_t l = threadIdx.x; l < L; l += blockDim.x)
         vj[l * stride_v] = (l == cand) ? Num<T>::one() : Num<T>::zero();
       __syncthreads();
       for (int pass = 0; pass < 2; ++pass) {
-        for (int64_t i = 0; i < j; ++i) {
-          const T* vi = base + i * stride_j;
-          // <v_i, v_j> = sum conj(v_i) v_j
-          T acc = Num<T>::zero();
-          for (int64_t l = threadIdx.x; l < L; l += blockDim.x)
-            acc = Num<T>::fmac(vj[l * stride_v], vi[l * stride_v], acc);
-          warp_sum_t<T>(acc);
-          if (lane == 0) {
+        // coefficients c_i = <v_i, v_j> = sum_l conj(v_i[l]) v_j[l], i < j
+        if (tall) {
+          // vectors are contiguous across i for a fixed l: one thread per i
+          for (int64_t i = threadIdx.x; i < j; i += blockDim.x) {
+            T acc = Num<T>::zero();
+            for (int64_t l = 0; l < L; ++l) acc = Num<T>::fmac(vj[l * stride_v], base[l * stride_v + i], acc);
             if constexpr (Num<T>::cplx) {
-              red[0][warp] = acc.x;
-              red[1][warp] = acc.y;
+              cre[i] = acc.x;
+              cim[i] = acc.y;
             } else {
-              red[0][warp] = acc;
+              cre[i] = acc;
             }
           }
-          __syncthreads();
-          if (threadIdx.x == 0) {
-            double re = 0.0, im = 0.0;
-            for (int w = 0; w < nw; ++w) {
-              re += red[0][w];
-              if constexpr (Num<T>::cplx) im += red[1][w];
+        } else {
+          // vectors are contiguous along l: one warp per i
+          for (int64_t i = warp; i < j; i += nw) {
+            T acc = Num<T>::zero();
+            for (int64_t l = lane; l < L; l += 32) acc = Num<T>::fmac(vj[l], base[i * stride_j + l], acc);
+            warp_sum_t<T>(acc);
+            if (lane == 0) {
+              if constexpr (Num<T>::cplx) {
+                cre[i] = acc.x;
+                cim[i] = acc.y;
+              } else {
+                cre[i] = acc;
+              }
             }
-            coef[0] = re;
-            coef[1] = im;
           }
-          __syncthreads();
-          T cf;
-          if constexpr (Num<T>::cplx) cf = make_double2(coef[0], coef[1]);
-          else cf = coef[0];
-          for (int64_t l = threadIdx.x; l < L; l += blockDim.x)
-            vj[l * stride_v] = Num<T>::sub(vj[l * stride_v], Num<T>::mul(cf, vi[l * stride_v]));
-          __syncthreads();
         }
+        __syncthreads();
+        // v_j -= sum_i c_i v_i
+        if (tall) {
+          // row l of U holds entry l of every vector: one warp per l
+          for (int64_t l = warp; l < L; l += nw) {
+            T acc = Num<T>::zero();
+            for (int64_t i = lane; i < j; i += 32) {
+              T cf;
+              if constexpr (Num<T>::cplx) cf = make_double2(cre[i], cim[i]);
+              else cf = cre[i];
+              acc = Num<T>::add(acc, Num<T>::mul(cf, base[l * stride_v + i]));
+            }
+            warp_sum_t<T>(acc);
+            if (lane == 0) vj[l * stride_v] = Num<T>::sub(vj[l * stride_v], acc);
+          }
+        } else {
+          for (int64_t l = threadIdx.x; l < L; l += blockDim.x) {
+            T v = vj[l];
+            for (int64_t i = 0; i < j; ++i) {
+              T cf;
+              if constexpr (Num<T>::cplx) cf = make_double2(cre[i], cim[i]);
+              else cf = cre[i];
+              v = Num<T>::sub(v, Num<T>::mul(cf, base[i * stride_j + l]));
+            }
+            vj[l] = v;
+          }
+        }
+        __syncthreads();
       }
       double acc = 0.0;
       for (int64_t l = threadIdx.x; l < L; l += blockDim.x) acc += cabs2(vj[l * stride_v]);
       acc = warp_sum(acc);
-      if (lane == 0) red[0][warp] = acc;
+      if (lane == 0) red[warp] = acc;
       __syncthreads();
       if (threadIdx.x == 0) {
         double tot = 0.0;
-        for (int w = 0; w < nw; ++w) tot += red[0][w];
-        coef[0] = sqrt(tot);
+        for (int w = 0; w < nw; ++w) tot += red[w];
+        nrm_s = sqrt(tot);
       }
       __syncthreads();
-      const double nrm = coef[0];
-      if (nrm > 0.5) {
+      const double nrm = nrm_s;
+      if (nrm > need) {
         for (int64_t l = threadIdx.x; l < L; l += blockDim.x) vj[l * stride_v] = rscale(vj[l * stride_v], 1.0 / nrm);
         __syncthreads();
+        cand = (cand + 1 == L ? 0 : cand + 1);
         break;
       }
       __syncthreads();
@@ -882,15 +935,15 @@ int block_sweeps_t(T* w, const int64_t* blocks, int n_blocks, const int32_t* sup
 
 template <typename T>
 int finalize_t(const void* work, void* U, double* S, void* Vh, const int64_t* blocks, int n_blocks, int pow2,
-                      int mode, const double* shift, cudaStream_t s) {
-  const size_t smem = (size_t)pow2 * (sizeof(double) + sizeof(int));
+                      int mode, const double* shift, const int64_t* state, cudaStream_t s) {
+  const size_t smem = (size_t)pow2 * (sizeof(double) * (Num<T>::cplx ? 2 : 1) + sizeof(int));
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(yb::svd_finalize_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
   }
   yb::svd_finalize_kernel<T><<<n_blocks, 1024, smem, s>>>((const T*)work, (T*)U, S, (T*)Vh, blocks, pow2, mode,
-                                                          shift);
+                                                          shift, state);
   return yb::check_launch();
 }
 
@@ -906,11 +959,11 @@ int yb_svd_init(const void* a, void* work32, const int64_t* blocks, int n_blocks
   cudaStream_t s = (cudaStream_t)stream;
   dim3 grid(64, (unsigned)n_blocks);
   if (dtype == YB_F64) {
-    yb::block_fro_kernel<double><<<n_blocks, 256, 0, s>>>((const double*)a, blocks, shift, scale);
+    yb::block_fro_kernel<double><<<n_blocks, 256, 0, s>>>((const double*)a, blocks, shift, scale, state);
     yb::svd_init_kernel<double, float><<<grid, 256, 0, s>>>((const double*)a, (float*)work32, blocks, state, shift,
                                                             scale);
   } else {
-    yb::block_fro_kernel<double2><<<n_blocks, 256, 0, s>>>((const double2*)a, blocks, shift, scale);
+    yb::block_fro_kernel<double2><<<n_blocks, 256, 0, s>>>((const double2*)a, blocks, shift, scale, state);
     yb::svd_init_kernel<double2, float2><<<grid, 256, 0, s>>>((const double2*)a, (float2*)work32, blocks, state,
                                                               shift, scale);
   }
@@ -987,7 +1040,7 @@ int yb_svd_shift_prefill(void* work64, const int64_t* blocks, int n_blocks, int 
 }
 
 int yb_svd_finalize(const void* work, void* U, double* S, void* Vh, const int64_t* blocks, int n_blocks, int dtype,
-                    int max_k, int mode, const double* shift, void* stream) {
+                    int max_k, int mode, const double* shift, const int64_t* state, void* stream) {
   if (n_blocks == 0) return YB_OK;
   if (dtype != YB_F64 && dtype != YB_C128) return YB_ERR_INVALID;
   if (mode < 0 || mode > 2 || (mode != 0 && shift == nullptr)) return YB_ERR_INVALID;
@@ -995,8 +1048,8 @@ int yb_svd_finalize(const void* work, void* U, double* S, void* Vh, const int64_
   int pow2 = 1;
   while (pow2 < max_k) pow2 <<= 1;
   cudaStream_t s = (cudaStream_t)stream;
-  if (dtype == YB_F64) return yb::finalize_t<double>(work, U, S, Vh, blocks, n_blocks, pow2, mode, shift, s);
-  return yb::finalize_t<double2>(work, U, S, Vh, blocks, n_blocks, pow2, mode, shift, s);
+  if (dtype == YB_F64) return yb::finalize_t<double>(work, U, S, Vh, blocks, n_blocks, pow2, mode, shift, state, s);
+  return yb::finalize_t<double2>(work, U, S, Vh, blocks, n_blocks, pow2, mode, shift, state, s);
 }
 
 }  // extern "C"

@@ -294,14 +294,18 @@ ROWS_PER_SUPER = [None]  # super-vector height (None: largest of 16, 8, 4 that f
 NS_STEPS = 2          # Newton-Schulz steps: non-orthogonality ~1e-6 -> 1e-12 -> ~eps
 
 
+SVD_STATE_REC = 6     # int64 words of per-block Jacobi state (yb_svd.cu)
+
+
 def _svd_state_check(state, nb, phase, require_converged):
     st = state.cpu().numpy()
-    if st[4 * nb + 2] != 0:
+    R = SVD_STATE_REC
+    if st[R * nb + 2] != 0:
         raise RuntimeError(f"yastn_gb300 svd: grid barrier timed out in the {phase} phase")
-    conv = st[1:4 * nb:4]
+    conv = st[1:R * nb:R]
     if require_converged and not conv.all():
         raise torch.linalg.LinAlgError(f"yastn_gb300 svd: Jacobi did not converge ({phase} phase)")
-    return st[2:4 * nb:4]
+    return st[2:R * nb:R]
 
 
 def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
@@ -313,7 +317,7 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
     dblocks, dpairs = _dev(plan, 'svd', (plan.blocks, plan.pair_items), dev)
     w64 = torch.empty(plan.n64, dtype=torch.complex128 if cplx else torch.float64, device=dev)
     w32 = torch.empty(plan.n32, dtype=torch.complex64 if cplx else torch.float32, device=dev)
-    state = torch.zeros(4 * nb + 4, dtype=torch.int64, device=dev)
+    state = torch.zeros(SVD_STATE_REC * nb + 4, dtype=torch.int64, device=dev)
     aux = torch.empty(2 * nb, dtype=torch.float64, device=dev)  # [scale | shift]
     shift = aux[nb:] if mode != 0 else None
     sp = _vp(shift.data_ptr() if shift is not None else 0)
@@ -346,7 +350,7 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
            code, max_sweeps, TOL_STOP64, _ptr(state), st)
     _svd_state_check(state, nb, 'FP64', True)
     N.call('yb_svd_finalize', _ptr(w64), _ptr(U), _ptr(S), _vp(V.data_ptr() if V is not None else 0), _ptr(dblocks),
-           nb, code, plan.max_k, mode, sp, st)
+           nb, code, plan.max_k, mode, sp, _ptr(state), st)
 
 
 def svd(data, meta, sizes, max_sweeps=MAX_SWEEPS):
