@@ -22,6 +22,14 @@ per leg over charges -16..16 and every block scaled by 10^U(-4,0) (sector GEMMs 
 946^3), reporting emulated and native FP64 TFLOP/s and the largest relative error per
 sector result of both against the FP64 oracle.
 
+``--workload cfg4``: differentiable iPEPS CTMRG (1x1 cell, Z2, D=6, d=2, 8 CTM iterations with
+truncated block-SVD projectors, transverse-field Ising energy at h=3 and its gradient) at
+environment dimension chi=24: the reference's own call sequence, recorded from YASTN, replayed
+through the backend, forward and backward, every step. Reported in ms per forward+backward
+(lower is better), with the energy and gradient checked against the reference's every run,
+next to the plain FP64 path (one torch launch per block, torch's SVD; ``yastn_gb300.plain``)
+on the same GPU and on the host cores.
+
 One JSON line is printed by rank 0. ``--impl reference`` times the CPU restatement of
 the reference NumPy backend on the host cores for the same workload instead.
 """
@@ -50,7 +58,7 @@ def parse():
     p.add_argument('--steps', type=int, default=20)
     p.add_argument('--warmup', type=int, default=5)
     p.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
-    p.add_argument('--workload', default='cfg2', choices=['cfg1', 'cfg2', 'cfg3', 'cfg5'])
+    p.add_argument('--workload', default='cfg2', choices=['cfg1', 'cfg2', 'cfg3', 'cfg4', 'cfg5'])
     p.add_argument('--gemm', default='emulated', choices=['emulated', 'fp64'],
                    help='sector-GEMM mode of the headline (cfg2)')
     p.add_argument('--no-svd', action='store_true', help='skip the extra svd_with_truncation timing')
@@ -153,6 +161,33 @@ class Cfg5(Cfg1):
         self.bytes_merge = 16 * self.A.size
 
 
+class Cfg4:
+    """Differentiable CTMRG (forward + backward) from the recorded call sequence."""
+    name = ("differentiable iPEPS CTMRG, 1x1 cell, Z2, D=6, d=2, chi=24, 8 CTM iterations, TFIM h=3 energy "
+            "+ gradient (recorded YASTN call sequence replayed: 32 block SVDs of 2x432^2, 697 dots, "
+            "1045 merges per forward), FP64")
+    metric = "CTMRG fwd+bwd ms (iPEPS Z2 D=6 chi=24, 8 CTM iterations, FP64, <=1e-10 rel)"
+
+    def __init__(self):
+        from yastn_gb300.replay import load_replay
+        self.r = load_replay('ctmrg_z2_d6')
+        self.A = self.r.arrays['in:A']
+        self.E_ref = self.r.payload['E']
+        self.grad_ref = self.r.arrays['ref:grad']
+
+    def step(self, torch, backend, device, A_host=None, pinned=None):
+        """One forward + backward; returns (E, grad) as device tensors."""
+        if pinned is not None:
+            A = pinned.to(device, non_blocking=True)
+        else:
+            A = torch.from_numpy(self.A).to(device)
+        A.requires_grad_(True)
+        env = self.r.run(backend, device, {'A': A})
+        E = env[self.r.outputs['E']]
+        E.backward()
+        return E.detach(), A.grad
+
+
 class Cfg2:
     """DMRG two-site Heff2 matvec inside 30 Lanczos steps (YASTN eigs, ncv=30, 'SR')."""
     name = ("DMRG two-site Heff2 x 30 Lanczos steps: U(1) spin-1/2 XXZ (Jz=Jxy=1, MPO bond 5), virtual D=1024 "
@@ -198,6 +233,8 @@ def run_reference(args, wl):
         return
     if isinstance(wl, Cfg2):
         return run_reference_cfg2(args, wl)
+    if isinstance(wl, Cfg4):
+        return run_reference_cfg4(args, wl)
     for _ in range(args.warmup):
         wl.cpu_step()
     ts = []
@@ -237,6 +274,32 @@ def run_reference_cfg2(args, wl, sample_ncv=5):
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
                              "sample": f"{sample_ncv} of {wl.ncv} Lanczos steps per step (numpy BLAS, all threads)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_reference_cfg4(args, wl):
+    """Reference arm for CTMRG: the recorded sequence on the host cores with one torch
+    operation per block (the reference torch backend's structure, LAPACK SVD, all threads).
+    One forward+backward takes ~10 s, so at most 3 timed steps and 1 warm-up are run."""
+    import torch
+    from yastn_gb300.plain import PlainBackend
+    steps, warm = min(args.steps, 3), min(args.warmup, 1)
+    for _ in range(warm):
+        wl.step(torch, PlainBackend(), 'cpu')
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        E, g = wl.step(torch, PlainBackend(), 'cpu')
+        ts.append(time.perf_counter() - t0)
+    t = float(np.mean(ts)) * 1e3
+    err = abs(float(E) - wl.E_ref) / abs(wl.E_ref)
+    line = {"impl": "reference", "metric": wl.metric, "value": t, "unit": "ms", "n_gpus": args.gpus,
+            "steps": steps, "warmup": warm, "ms_per_step": t, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded N(0,1) site tensor, recorded call sequence)",
+            "config": {"workload": wl.name, "energy_rel_err_vs_reference": err},
+            "cpu_baseline": {"value": t, "unit": "ms", "cores": torch.get_num_threads(), "kind": "port",
+                             "sample": f"{steps} full forward+backward steps, one torch CPU op per block (LAPACK SVD)"},
+            "e2e": {"value": t, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
@@ -720,6 +783,168 @@ def run_gpu_cfg2(args, wl):
         dist.destroy_process_group()
 
 
+def run_gpu_cfg4(args, wl):
+    """CTMRG forward+backward through the backend, timed per step (CUDA events bracket the
+    whole step, which includes the host's replay of the call sequence and YASTN's host-side
+    decisions); the plain per-block FP64 path on the same GPU and on the host cores beside it."""
+    import torch
+    import torch.distributed as dist
+    from yastn_gb300 import backend as BK
+    from yastn_gb300 import _native, ops
+    from yastn_gb300.plain import PlainBackend
+
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    if world > 1:
+        dist.init_process_group('nccl')
+    _native.lib()
+    flush = torch.empty(L2_FLUSH_BYTES // 8, dtype=torch.float64, device=dev)
+    pinned = torch.from_numpy(wl.A).pin_memory()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def check(E, g):
+        e = abs(float(E) - wl.E_ref) / abs(wl.E_ref)
+        gh = g.cpu().numpy()
+        ge = float(np.abs(gh - wl.grad_ref).max() / np.abs(wl.grad_ref).max())
+        return e, ge
+
+    for _ in range(args.warmup):
+        E, g = wl.step(torch, BK, dev)
+    e_err, g_err = check(E, g)
+    assert e_err <= 1e-10 and g_err <= 1e-8, (e_err, g_err)
+    barrier()
+    clocks = Clocks(local)
+    l0 = _native.LAUNCHES[0]
+    ts = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        E, g = wl.step(torch, BK, dev)
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    launches = (_native.LAUNCHES[0] - l0) // max(args.steps, 1)
+    barrier()
+    # end to end: the site tensor from pinned host memory, energy and gradient back to the host
+    te = []
+    gh = torch.empty(pinned.shape, dtype=torch.float64).pin_memory()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        E, g = wl.step(torch, BK, dev, pinned=pinned)
+        gh.copy_(g)
+        Eh = float(E)
+        te.append((time.perf_counter() - t0) * 1e3)
+    clk = clocks.stop()
+    e_err, g_err = check(E, g)
+    # the same sequence on the plain per-block FP64 path (torch ops, cuSOLVER SVD) on this GPU
+    plain = PlainBackend()
+    wl.step(torch, plain, dev)
+    tp = []
+    for _ in range(min(args.steps, 2)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Ep, gp = wl.step(torch, plain, dev)
+        torch.cuda.synchronize()
+        tp.append((time.perf_counter() - t0) * 1e3)
+    ep_err, gp_err = check(Ep, gp)
+    roof = svd_roofline(torch, dev, lambda: wl.step(torch, BK, dev))
+    t_max, t_e2e = float(np.mean(ts)), float(np.mean(te))
+    if world > 1:
+        tt = torch.tensor([t_max, t_e2e], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max, t_e2e = float(tt[0]), float(tt[1])
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    t0 = time.perf_counter()
+    wl.step(torch, plain, 'cpu')
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    line = {
+        "metric": wl.metric, "value": t_max, "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded N(0,1) site tensor; call sequence recorded from YASTN)",
+        "config": {"workload": wl.name, "parallelism": f"replicas{world}",
+                   "l2": "flushed between timed steps (256 MB write)",
+                   "energy_rel_err_vs_reference": e_err, "grad_rel_err_vs_reference": g_err,
+                   "plain_per_block_gpu_ms": float(np.mean(tp)),
+                   "plain_per_block_gpu": "the same sequence with one torch launch per block, torch.linalg.svd "
+                                          "(cuSOLVER), torch autograd + the reference's broadened SVD adjoint",
+                   "plain_over_fused": float(np.mean(tp)) / t_max,
+                   "plain_energy_rel_err": ep_err, "plain_grad_rel_err": gp_err},
+        "roofline": roof,
+        "cpu_baseline": {"value": cpu_ms, "unit": "ms", "cores": torch.get_num_threads(), "kind": "port",
+                         "sample": "one full forward+backward, one torch CPU op per block (LAPACK SVD)"},
+        "e2e": {"value": t_e2e, "unit": "ms", "h2d_bytes_per_step": int(pinned.numel() * 8),
+                "d2h_bytes_per_step": int(pinned.numel() * 8 + 8)},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def svd_roofline(torch, dev, run_once):
+    """Device time per entry point over one instrumented step and the roofline of the FP64
+    Jacobi sweeps (the dominant kernel of the CTMRG step): algorithmic work per launch =
+    sum over blocks of sweeps x k(k-1)/2 pairs x (12 L + 6 k) real FLOP (three length-L dot
+    products and the rotation of two X rows and two W rows; x4 for complex), against the
+    FP64 rate of this GPU (cuBLAS DGEMM, measured live)."""
+    from yastn_gb300 import _native, ops
+    orig_call, orig_check, orig_jac = _native.call, ops._svd_state_check, ops._jacobi
+    ev, work, cur = {}, [], {}
+
+    def spy(name, *a, **k):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        r = orig_call(name, *a, **k)
+        e1.record()
+        key = name + (':fp64' if name == 'yb_svd_sweeps' and a[6] == 64 else '')
+        ev.setdefault(key, []).append((e0, e1))
+        return r
+
+    def jac(data, plan, *a, **k):
+        cur['kL'] = [(int(r[9]), int(r[10])) for r in plan.blocks]
+        cur['cplx'] = data.is_complex()
+        return orig_jac(data, plan, *a, **k)
+
+    def check(state, nb, phase, req):
+        sw = orig_check(state, nb, phase, req)
+        if phase == 'FP64':
+            f = sum(int(s) * k * (k - 1) // 2 * (12 * L + 6 * k) for s, (k, L) in zip(sw, cur['kL']))
+            work.append(f * (4 if cur['cplx'] else 1))
+        return sw
+    _native.call, ops._svd_state_check, ops._jacobi = spy, check, jac
+    try:
+        run_once()
+        torch.cuda.synchronize()
+    finally:
+        _native.call, ops._svd_state_check, ops._jacobi = orig_call, orig_check, orig_jac
+    tot = {k: sum(a.elapsed_time(b) for a, b in v) * 1e-3 for k, v in ev.items()}
+    t64 = tot.get('yb_svd_sweeps:fp64', 0.0)
+    n64 = len(ev.get('yb_svd_sweeps:fp64', []))
+    peak = fp64_peak_tflops(torch, dev)
+    achieved = sum(work) / t64 / 1e12 if t64 > 0 else 0.0
+    return {"bound": "fp64", "kernel": "yb_svd_sweeps (FP64 phase)", "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": "measured live: cuBLAS DGEMM 4096^3",
+            "traffic": None, "launches": n64, "ms_per_launch": t64 / max(n64, 1) * 1e3,
+            "device_ms_per_step": {k: v * 1e3 for k, v in sorted(tot.items(), key=lambda x: -x[1])[:8]}}
+
+
 def kernel_roofline(torch, dev, run_once, w, gemm_mode, reps=5):
     """Device time per entry point over ``reps`` eager matvecs (CUDA events on the launching
     stream; the stream is first held by a spin kernel long enough for the host to enqueue
@@ -779,11 +1004,13 @@ def kernel_roofline(torch, dev, run_once, w, gemm_mode, reps=5):
 
 def main():
     args = parse()
-    wl = {'cfg1': Cfg1, 'cfg2': Cfg2, 'cfg3': Cfg3, 'cfg5': Cfg5}[args.workload]()
+    wl = {'cfg1': Cfg1, 'cfg2': Cfg2, 'cfg3': Cfg3, 'cfg4': Cfg4, 'cfg5': Cfg5}[args.workload]()
     if args.impl == 'reference':
         run_reference(args, wl)
     elif args.workload == 'cfg2':
         run_gpu_cfg2(args, wl)
+    elif args.workload == 'cfg4':
+        run_gpu_cfg4(args, wl)
     else:
         run_gpu(args, wl)
 

@@ -114,6 +114,17 @@ int yb_block_copy(const void* src, void* dst, int unit_bytes,
 int yb_grouped_gemm(const void* a, const void* b, void* c, int dtype,
                     const int64_t* outs, const int64_t* terms, const int32_t* tiles, int n_tiles,
                     double alpha, double beta, void* stream);
+/* yb_gemm_reduce: the second pass of a split-K product. The host splits the K range of
+ * outputs whose few tiles would leave most SMs idle into chunks, computes each chunk's
+ * product into its own slot of a workspace P (yb_grouped_gemm with alpha 1, beta 0), then
+ *   C_o = alpha * sum_{c < chunks} P[p_off + c*m*n + i*n + j] + beta * C_o
+ * summed in chunk order. recs: YB_GEMM_RED_REC int64 per output: [0] c offset [1] m [2] n
+ * [3] ldc [4] p offset [5] chunks. tasks: int32 pairs (record, item) covering each
+ * output's m*n elements in items of YB_GEMM_RED_ITEM. */
+#define YB_GEMM_RED_REC 8
+#define YB_GEMM_RED_ITEM 1024
+int yb_gemm_reduce(void* c, const void* p, int dtype, const int64_t* recs, const int32_t* tasks,
+                   int n_tasks, double alpha, double beta, void* stream);
 
 /* ==== family (b'): FP64 sector GEMMs emulated on BF16 tensor cores (split operands) ====
  * yb_ozaki_split: every row of each record (K contiguous entries) is scaled by 2^-e

@@ -69,7 +69,30 @@ def _run_tiles(rec, src, dst):
 
 
 def run_gemm(plan, a, b, c, alpha=1.0, beta=0.0):
-    """Grouped sum-of-products GEMM records applied with numpy."""
+    """Grouped sum-of-products GEMM records applied with numpy (the direct outputs, then the
+    split-K partial products into a workspace and their ordered reduction)."""
+    _run_outs(plan.outs, plan.terms, plan.tiles, a, b, c, alpha, beta)
+    sp = getattr(plan, 'split', None)
+    if sp is not None:
+        ws = np.full(sp.ws, np.nan, dtype=c.dtype)
+        _run_outs(sp.outs, sp.terms, sp.tiles, a, b, ws, 1.0, 0.0)
+        assert not np.isnan(ws).any(), "split-K chunks do not cover the workspace"
+        items = {}
+        for ri, it in sp.tasks:
+            items.setdefault(int(ri), set()).add(int(it))
+        for ri, r in enumerate(sp.red):
+            c_off, m, n, ldc, p_off, chunks = (int(x) for x in r[:6])
+            assert items.get(ri, set()) == set(range((m * n + 1023) // 1024)), "reduction tasks do not cover"
+            acc = np.zeros(m * n, dtype=c.dtype)
+            for ch in range(chunks):
+                acc += ws[p_off + ch * m * n: p_off + (ch + 1) * m * n]
+            rows = c_off + np.arange(m)[:, None] * ldc + np.arange(n)[None, :]
+            c[rows] = alpha * acc.reshape(m, n) + (beta * c[rows] if beta != 0 else 0)
+    return c
+
+
+def _run_outs(outs, terms, tiles, a, b, c, alpha, beta):
+    plan = type('Recs', (), {'outs': outs, 'terms': terms, 'tiles': tiles})
     seen = {}
     for oi, tr, tc, kind in plan.tiles:
         seen.setdefault(int(oi), set()).add((int(tr), int(tc), int(kind)))

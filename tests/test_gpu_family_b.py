@@ -93,6 +93,28 @@ def test_dot_empty_and_zero_k(cuda_device):
     assert ops.dot(A, B, (), 0).numel() == 0
 
 
+@pytest.mark.parametrize('cplx', [False, True])
+def test_split_k_dots(cplx, cuda_device):
+    """Outputs with few tiles and a long contracted dimension (split-K: chunk products and
+    an ordered reduction) against the oracle, forward and adjoint, real and complex."""
+    from yastn_gb300 import _plans as P
+    rng = np.random.default_rng(12)
+    shapes = [(1, 373248, 1), (3, 3000, 2000), (100, 1500, 100), (5, 7, 9)]
+    meta, oa, ob, oc = [], 0, 0, 0
+    for m, k, n in shapes:
+        meta.append(((oc, oc + m * n), (m, n), (oa, oa + m * k), (m, k), (ob, ob + k * n), (k, n)))
+        oa += m * k; ob += k * n; oc += m * n
+    meta = tuple(meta)
+    assert P.dot_plan(meta).split is not None
+    f = lambda n: rng.normal(size=n) + (1j * rng.normal(size=n) if cplx else 0)
+    A, B, Cb = f(oa), f(ob), f(oc)
+    got = host(ops.dot(dev(A), dev(B), meta, oc))
+    assert rel(got, oracle.dot(A, B, meta, oc)) <= TOL
+    Ab, Bb = ops.dot_backward(dev(Cb), dev(A), dev(B), meta)
+    Ar, Br = oracle.dot_backward(Cb, A, B, meta)
+    assert rel(host(Ab), Ar) <= TOL and rel(host(Bb), Br) <= TOL
+
+
 def test_cfg1_full_size_dot(cuda_device):
     """The benchmark's 13 sector GEMMs (n up to 822, 3.25 GFLOP) vs numpy BLAS."""
     tr = load_trace('cfg1')

@@ -97,6 +97,48 @@ def test_dot_plans_reproduce_reference(name):
     assert n > 0
 
 
+def _meta_dot(shapes):
+    meta, oa, ob, oc = [], 0, 0, 0
+    for m, k, n in shapes:
+        meta.append(((oc, oc + m * n), (m, n), (oa, oa + m * k), (m, k), (ob, ob + k * n), (k, n)))
+        oa += m * k; ob += k * n; oc += m * n
+    return tuple(meta), oa, ob, oc
+
+
+@pytest.mark.parametrize('shapes', [
+    [(1, 20000, 1)],                                   # a long dot product: one tile, K cut in chunks
+    [(3, 3000, 2000), (100, 1500, 100), (5, 7, 9)],    # skinny and square long-K outputs beside a short one
+    [(200, 1200, 150), (200, 1200, 150)],              # two dense blocks, 24 tiles: K cut in five
+])
+def test_split_k_plans_cover_and_reproduce(shapes):
+    """Plans with few tiles and long K split the K range: the chunks cover the workspace,
+    the reduction tasks cover every output, and the result is the product (dot and adjoint)."""
+    meta, oa, ob, oc = _meta_dot(shapes)
+    plan = P.dot_plan(meta)
+    assert plan.split is not None
+    rng = np.random.default_rng(4)
+    A, B = rng.normal(size=oa), rng.normal(size=ob)
+    out = PI.run_gemm(plan, A, B, np.zeros(oc))
+    ref = oracle.dot(A, B, meta, oc)
+    assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max() * np.sqrt(max(k for _, k, _ in shapes))
+    # alpha/beta applied once, by the reduction
+    c0 = rng.normal(size=oc)
+    out2 = PI.run_gemm(plan, A, B, c0.copy(), alpha=-0.5, beta=1.5)
+    assert np.abs(out2 - (-0.5 * ref + 1.5 * c0)).max() <= 1e-11 * np.abs(ref).max()
+    Cb = rng.normal(size=oc)
+    pa, pb = P.dot_backward_plans(meta)
+    Ab = PI.run_gemm(pa, Cb, B, np.zeros(oa))
+    Bb = PI.run_gemm(pb, A, Cb, np.zeros(ob))
+    Ab_r, Bb_r = oracle.dot_backward(Cb, A, B, meta)
+    assert np.abs(Ab - Ab_r).max() <= 1e-11 * np.abs(Ab_r).max()
+    assert np.abs(Bb - Bb_r).max() <= 1e-11 * np.abs(Bb_r).max()
+
+
+def test_split_k_not_used_when_tiles_fill_the_gpu():
+    meta, *_ = _meta_dot([(64, 4096, 64)] * 400)
+    assert P.dot_plan(meta).split is None
+
+
 def test_tds_plans_reproduce_reference():
     import yastn_gb300._plans as PP
     tr = load_trace('tensordot_no_fusion')

@@ -293,15 +293,32 @@ def transpose_plan(axes, meta_transpose, size):
 # ----------------------------------------------------------------------------- grouped GEMM
 
 class GemmPlan:
-    def __init__(self, outs, terms, tiles, flops):
+    """Grouped GEMM records: the outputs computed directly (outs, terms, tiles) and, when
+    some outputs' K range is split, their partial products and reduction (``split``)."""
+
+    def __init__(self, outs, terms, tiles, flops, split=None):
         self.outs = outs
         self.terms = terms
         self.tiles = tiles
         self.flops = flops  # real multiply-adds x 2 (complex counted by the caller)
+        self.split = split
         self._dev = {}
 
 
+class SplitK:
+    """Partial products of split outputs into a workspace (outs/terms/tiles addressed in it),
+    and the reduction records (c offset, m, n, ldc, p offset, chunks) with their tasks."""
+
+    def __init__(self, outs, terms, tiles, red, tasks, ws):
+        self.outs, self.terms, self.tiles = outs, terms, tiles
+        self.red, self.tasks, self.ws = red, tasks, ws
+
+
 SKINNY_ROWS, SKINNY_COLS = 8, 1024
+GEMM_RED_REC, GEMM_RED_ITEM = 8, 1024
+SPLITK_MAX_TILES = 304   # plans with this many tiles (2 per SM) are not split
+SPLITK_UNITS = 608       # tiles x chunks aimed at after splitting (4 per SM)
+SPLITK_MIN_K = 256       # shortest K chunk
 
 
 def _tiles_for(outs, terms):
@@ -325,8 +342,47 @@ def _tiles_for(outs, terms):
     return arr
 
 
-def _pack_gemm(out_list):
-    """out_list: [(c_off, m, n, ldc, [term tuples])] -> GemmPlan."""
+def _n_tiles(m, n):
+    if m == 0 or n == 0:
+        return 0
+    if m <= SKINNY_ROWS and n > GEMM_TILE:
+        return (n + SKINNY_COLS - 1) // SKINNY_COLS
+    return ((m + GEMM_TILE - 1) // GEMM_TILE) * ((n + GEMM_TILE - 1) // GEMM_TILE)
+
+
+def _split_chunk_k(out_list):
+    """K per chunk when the plan has too few tiles to fill the GPU and some output's K is
+    long (None: no split). Work is counted as tiles x K."""
+    tiles = sum(_n_tiles(m, n) for _, m, n, _, _ in out_list)
+    if tiles == 0 or tiles >= SPLITK_MAX_TILES:
+        return None
+    work = sum(_n_tiles(m, n) * sum(t[2] for t in tl) for _, m, n, _, tl in out_list)
+    ck = max(SPLITK_MIN_K, -(-work // SPLITK_UNITS))
+    ck = -(-ck // 16) * 16
+    if not any(sum(t[2] for t in tl) >= 2 * ck for _, m, n, _, tl in out_list if m and n):
+        return None
+    return ck
+
+
+def _chunks(tl, ck):
+    """Cut a term list into chunks of at most ``ck`` contracted indices (terms longer than
+    ``ck`` are cut into pieces; consecutive short ones share a chunk)."""
+    chunks, cur, cur_k = [], [], 0
+    for t in tl:
+        a_off, b_off, k, ars, acs, brs, bcs, fl = t
+        for k0 in range(0, k, ck):
+            kp = min(ck, k - k0)
+            if cur and cur_k + kp > ck:
+                chunks.append(cur)
+                cur, cur_k = [], 0
+            cur.append((a_off + k0 * acs, b_off + k0 * brs, kp, ars, acs, brs, bcs, fl))
+            cur_k += kp
+    if cur:
+        chunks.append(cur)
+    return chunks
+
+
+def _records(out_list):
     outs, terms, flops = [], [], 0
     for c_off, m, n, ldc, tl in out_list:
         t0 = len(terms)
@@ -336,7 +392,38 @@ def _pack_gemm(out_list):
         outs.append((c_off, m, n, ldc, t0, len(terms), 0, 0))
     outs = np.array(outs, dtype=np.int64).reshape(-1, GEMM_OUT_REC)
     terms = np.array(terms, dtype=np.int64).reshape(-1, GEMM_TERM_REC)
-    return GemmPlan(outs, terms, _tiles_for(outs, terms), flops)
+    return outs, terms, flops
+
+
+def _pack_gemm(out_list):
+    """out_list: [(c_off, m, n, ldc, [term tuples])] -> GemmPlan. When the outputs make
+    too few tiles for the GPU, outputs with a long K are split into K chunks computed into
+    a workspace and summed by a reduction pass (split-K)."""
+    ck = _split_chunk_k(out_list)
+    split = None
+    if ck is not None:
+        direct, parts, red, tasks, ws = [], [], [], [], 0
+        for c_off, m, n, ldc, tl in out_list:
+            if m == 0 or n == 0 or sum(t[2] for t in tl) < 2 * ck:
+                direct.append((c_off, m, n, ldc, tl))
+                continue
+            ch = _chunks(tl, ck)
+            for ci, cl in enumerate(ch):
+                parts.append((ws + ci * m * n, m, n, n, cl))
+            ri = len(red)
+            red.append((c_off, m, n, ldc, ws, len(ch), 0, 0))
+            tasks.extend((ri, it) for it in range((m * n + GEMM_RED_ITEM - 1) // GEMM_RED_ITEM))
+            ws += len(ch) * m * n
+        po, pt, _ = _records(parts)
+        split = SplitK(po, pt, _tiles_for(po, pt), np.array(red, dtype=np.int64).reshape(-1, GEMM_RED_REC),
+                       np.array(tasks, dtype=np.int32).reshape(-1, 2), ws)
+        out_list = direct
+    outs, terms, _ = _records(out_list)
+    flops = sum(2 * m * n * t[2] for _, m, n, _, tl in out_list for t in tl)
+    if split is not None:
+        flops += sum(2 * int(o[1]) * int(o[2]) * int(t[2]) for o in split.outs
+                     for t in split.terms[int(o[4]):int(o[5])])
+    return GemmPlan(outs, terms, _tiles_for(outs, terms), flops, split)
 
 
 def dot_plan(meta_dot):

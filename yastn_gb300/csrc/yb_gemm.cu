@@ -229,8 +229,52 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_kernel(const typename F
   }
 }
 
+// Split-K reduction: C_o = alpha * sum_{c < chunks} P[p_off + c m n + i n + j] + beta * C_o,
+// the partial products summed in chunk order (deterministic). One CTA per task of
+// YB_GEMM_RED_ITEM consecutive elements of one output.
+template <class F>
+__global__ void __launch_bounds__(kThreads) gemm_reduce_kernel(typename F::T* __restrict__ C,
+                                                                const typename F::T* __restrict__ P,
+                                                                const int64_t* __restrict__ recs,
+                                                                const int32_t* __restrict__ tasks, double alpha,
+                                                                double beta) {
+  using T = typename F::T;
+  const int2 tk = reinterpret_cast<const int2*>(tasks)[blockIdx.x];
+  const int64_t* r = recs + (int64_t)tk.x * YB_GEMM_RED_REC;
+  const int64_t c_off = r[0], n = r[2], ldc = r[3], p_off = r[4], chunks = r[5];
+  const int64_t mn = r[1] * n;
+  const int64_t e0 = (int64_t)tk.y * YB_GEMM_RED_ITEM;
+  const int64_t e1 = min(e0 + (int64_t)YB_GEMM_RED_ITEM, mn);
+  for (int64_t e = e0 + threadIdx.x; e < e1; e += kThreads) {
+    T acc = F::zero();
+    for (int64_t c = 0; c < chunks; ++c) acc = F::add(acc, P[p_off + c * mn + e]);
+    const int64_t i = e / n, j = e - i * n;
+    T* p = C + c_off + i * ldc + j;
+    T v = F::scale(acc, alpha);
+    if (beta != 0.0) v = F::add(v, F::scale(*p, beta));
+    *p = v;
+  }
+}
+
 }  // namespace
 }  // namespace yb
+
+extern "C" int yb_gemm_reduce(void* c, const void* p, int dtype, const int64_t* recs, const int32_t* tasks,
+                              int n_tasks, double alpha, double beta, void* stream) {
+  if (n_tasks == 0) return YB_OK;
+  if (!c || !p || !recs || !tasks || n_tasks < 0) return YB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == YB_F64) {
+    yb::gemm_reduce_kernel<yb::Real><<<n_tasks, yb::kThreads, 0, s>>>((double*)c, (const double*)p, recs, tasks,
+                                                                      alpha, beta);
+  } else if (dtype == YB_C128) {
+    yb::gemm_reduce_kernel<yb::Cplx><<<n_tasks, yb::kThreads, 0, s>>>((double2*)c, (const double2*)p, recs,
+                                                                      tasks, alpha, beta);
+  } else {
+    return YB_ERR_INVALID;
+  }
+  return yb::check_launch();
+}
 
 extern "C" int yb_grouped_gemm(const void* a, const void* b, void* c, int dtype, const int64_t* outs,
                                const int64_t* terms, const int32_t* tiles, int n_tiles, double alpha,

@@ -120,11 +120,21 @@ def transpose_backward(data_b, axes, meta_transpose):
 # ----------------------------------------------------------------------------- family (b)
 
 def run_gemm(plan, a, b, c, alpha=1.0, beta=0.0):
-    if len(plan.tiles) == 0:
-        return c
-    do, dtm, dti = _dev(plan, 'gemm', (plan.outs, plan.terms, plan.tiles), a.device)
-    N.call('yb_grouped_gemm', _ptr(a), _ptr(b), _ptr(c), _dtype_code(c.dtype), _ptr(do), _ptr(dtm), _ptr(dti),
-           len(plan.tiles), float(alpha), float(beta), _stream())
+    code = _dtype_code(c.dtype)
+    if len(plan.tiles):
+        do, dtm, dti = _dev(plan, 'gemm', (plan.outs, plan.terms, plan.tiles), a.device)
+        N.call('yb_grouped_gemm', _ptr(a), _ptr(b), _ptr(c), code, _ptr(do), _ptr(dtm), _ptr(dti),
+               len(plan.tiles), float(alpha), float(beta), _stream())
+    sp = plan.split
+    if sp is not None:
+        # split-K: chunk products into a workspace, then the ordered sum into C
+        ws = torch.empty(sp.ws, dtype=c.dtype, device=c.device)
+        do, dtm, dti, dred, dtask = _dev(plan, 'gemm_split', (sp.outs, sp.terms, sp.tiles, sp.red, sp.tasks),
+                                         a.device)
+        N.call('yb_grouped_gemm', _ptr(a), _ptr(b), _ptr(ws), code, _ptr(do), _ptr(dtm), _ptr(dti),
+               len(sp.tiles), 1.0, 0.0, _stream())
+        N.call('yb_gemm_reduce', _ptr(c), _ptr(ws), code, _ptr(dred), _ptr(dtask), len(sp.tasks), float(alpha),
+               float(beta), _stream())
     return c
 
 
