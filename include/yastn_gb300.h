@@ -210,6 +210,11 @@ int yb_ozaki_dot_static(const double* A, const double* B, double* C,
  *   [9] k=min(m,n) [10] L=max(m,n) [11] N = k rounded up to even [12] 1 if m > n
  *   [13] X offset (FP32 workspace) [14] W offset (FP32 workspace)
  *   [15] number of super-vectors for yb_svd_block_sweeps (ceil(k / rows_per_super), even)
+ *   [16] 1: QR-preconditioned (see yb_svd_qr; then [10] = k, the rows of R being k long)
+ *   [17] L = max(m,n) of the QR workspaces [18] Z offset (k x L: X_0, then Q^T)
+ *   [19] offset of the Householder vectors (k x L) [20] offset of tau (k)
+ *   [21] offset of R's rows (k x k) [22] offset of the sorted W written by yb_svd_finalize
+ *   (all FP64 workspace offsets; [23] unused)
  * X holds the k vectors (rows of A, or of A^T when m > n) of length L, W the k x k
  * accumulated rotations (X = W X_0 throughout).
  * pair_items: int32 pairs (block, pair index 0..N/2-1) over all blocks.
@@ -242,7 +247,7 @@ int yb_ozaki_dot_static(const double* A, const double* B, double* C,
  * Replaces svd (backend_torch.py:318-319, torch_svd_gesdd.py:15-21) and eigh
  * (backend_torch.py:369-384, torch_eig_sym.py:14-32) for FP64 and complex128 blocks.
  */
-#define YB_SVD_REC 16
+#define YB_SVD_REC 24
 int yb_svd_init(const void* a, void* work32, const int64_t* blocks, int n_blocks, int dtype,
                 int64_t* state, double* shift, double* scale, void* stream);
 int yb_svd_sweeps(void* work, const int64_t* blocks, int n_blocks, const int32_t* pair_items,
@@ -261,7 +266,21 @@ int yb_svd_widen(const void* work32, void* work64, const int64_t* blocks, int n_
                  int64_t* state, void* stream);
 int yb_svd_shift_prefill(void* work64, const int64_t* blocks, int n_blocks, int dtype,
                          const double* shift, void* stream);
-int yb_svd_finalize(const void* work, void* U, double* S, void* Vh, const int64_t* blocks,
+/* yb_svd_qr: the QR-preconditioned start (every block of the records has [16] = 1), in
+ * place of yb_svd_init. Per block: scale and noise norms as yb_svd_init (the FP32 noise
+ * norm is FP64's, 1e-14 scale_b ||A_b||_F), Z = X_0 in FP64, the Householder QR of M = Z^T
+ * (M's columns are Z's rows: A^T for wide/square blocks, conj(A) for tall ones) in one
+ * cooperative launch (groups of CTAs per block, group barriers with a bounded spin; on
+ * timeout qctrl's error word is set), R's rows to [21], the FP32 start X32 = scale_b R and
+ * W32 = I, the Householder vectors and tau kept, and Q^T formed in Z. The sweeps then run
+ * on R's rows (row length k); yb_svd_finalize writes U's columns (wide) or Vh's rows (tall)
+ * from X and the sorted W to [22]; the host completes Vh = conj(W_sorted) Q^T (wide) or
+ * U = conj(Q) W_sorted^T (tall) with grouped GEMMs. qctrl: int64[qctrl_words] scratch,
+ * at least 4 words (4 per CTA group used). On a graded spectrum Jacobi from R's rows needs
+ * a few FP64 sweeps where Jacobi from A's rows needs tens. */
+int yb_svd_qr(const void* a, void* work64, void* work32, const int64_t* blocks, int n_blocks, int dtype,
+              int64_t* state, double* scale, int64_t* qctrl, int qctrl_words, void* stream);
+int yb_svd_finalize(void* work, void* U, double* S, void* Vh, const int64_t* blocks,
                     int n_blocks, int dtype, int max_k, int mode, const double* shift,
                     const int64_t* state, void* stream);
 

@@ -303,3 +303,63 @@ def eigh_adjoint_core(X, D, gD, recs, symeig, eps=1.0e-12):
             np.fill_diagonal(kb, 0)
         K[off:off + k * k] = kb.ravel()
     return K
+
+
+def qr_precondition(w64, w32, blocks, data, scale):
+    """numpy statement of yb_svd_qr on the plan layout: Z = X_0 (A, or A^H for tall blocks),
+    Householder QR of M = Z^T (LAPACK larfg conventions; M <- H^H M), R's rows, the FP32
+    start X32 = scale R, W32 = I, the reflectors and tau, and Q^T formed in Z."""
+    for b, r in enumerate(blocks):
+        a, m, n, k, L = int(r[0]), int(r[1]), int(r[2]), int(r[9]), int(r[17])
+        A = data[a:a + m * n].reshape(m, n)
+        Z = (A.conj().T if m > n else A).astype(w64.dtype).copy()
+        tau = np.zeros(k, dtype=w64.dtype)
+        for j in range(k):
+            alpha, x = Z[j, j], Z[j, j + 1:]
+            xn = float(np.sum(np.abs(x) ** 2))
+            if xn == 0.0 and np.imag(alpha) == 0:
+                tau[j] = 0
+            else:
+                beta = -np.copysign(np.sqrt(abs(alpha) ** 2 + xn), np.real(alpha))
+                tau[j] = (beta - alpha) / beta
+                Z[j, j + 1:] = x / (alpha - beta)
+                Z[j, j] = beta
+            v = np.concatenate([[1.0], Z[j, j + 1:]]).astype(w64.dtype)
+            t = np.conj(tau[j])
+            for c in range(j + 1, k):
+                w = np.sum(np.conj(v) * Z[c, j:])
+                Z[c, j:] -= t * w * v
+        RR = np.triu(Z[:, :k].T)  # R[i, c] = Z[c, i] for c >= i
+        w64[int(r[21]):int(r[21]) + k * k] = RR.ravel()
+        w32[int(r[13]):int(r[13]) + k * k] = (scale[b] * RR).ravel().astype(w32.dtype)
+        w32[int(r[14]):int(r[14]) + k * k] = np.eye(k, dtype=w32.dtype).ravel()
+        V = np.triu(Z, 1)
+        w64[int(r[19]):int(r[19]) + k * L] = V.ravel()
+        w64[int(r[20]):int(r[20]) + k] = tau
+        Q = np.eye(k, L, dtype=w64.dtype)  # rows of Q^T
+        for j in range(k - 1, -1, -1):
+            v = np.concatenate([[1.0], V[j, j + 1:]]).astype(w64.dtype)
+            for c in range(j, k):
+                w = np.sum(np.conj(v) * Q[c, j:])
+                Q[c, j:] -= tau[j] * w * v
+        w64[int(r[18]):int(r[18]) + k * L] = Q.ravel()
+
+
+def finalize_qr(w64, blocks, U, S, V):
+    """numpy statement of yb_svd_finalize for QR-preconditioned blocks (no completion):
+    singular values descending; wide: U columns = x_j / s_j, WS = conj(W) sorted; tall:
+    Vh rows = conj(x_j) / s_j, WS = W sorted."""
+    for r in blocks:
+        m, n, k = int(r[1]), int(r[2]), int(r[9])
+        X = w64[int(r[6]):int(r[6]) + k * k].reshape(k, k)
+        W = w64[int(r[7]):int(r[7]) + k * k].reshape(k, k)
+        sig = np.linalg.norm(X, axis=1)
+        idx = np.argsort(-sig, kind='stable')
+        S[int(r[4]):int(r[4]) + k] = sig[idx]
+        Y = X[idx] / sig[idx][:, None]
+        if m > n:
+            V[int(r[5]):int(r[5]) + k * n] = Y.conj().ravel()
+            w64[int(r[22]):int(r[22]) + k * k] = W[idx].ravel()
+        else:
+            U[int(r[3]):int(r[3]) + m * k] = Y.T.ravel()
+            w64[int(r[22]):int(r[22]) + k * k] = W[idx].conj().ravel()

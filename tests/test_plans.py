@@ -287,6 +287,68 @@ def test_mixed_precision_jacobi_schedule_on_plan_layout(rows_per_super):
         assert np.abs(s - sr).max() <= 1e-13 * max(sr.max(), 1.0)
 
 
+@pytest.mark.parametrize('cplx', [False, True])
+def test_qr_preconditioned_jacobi_on_plan_layout(cplx):
+    """The QR-preconditioned SVD on the plan layout: Householder QR of M = X_0^T (records
+    [16..22]), FP32 phase on R's rows, Newton-Schulz, X = W R by the xform plan, FP64
+    phase, the finalize rules and the closing GEMMs (Vh = conj(W) Q^T for wide blocks,
+    U = conj(Q) W^T for tall ones) give LAPACK's singular values and A = U S Vh with
+    orthonormal factors, on random and graded blocks."""
+    rng = np.random.default_rng(9)
+    shapes = [(24, 24), (31, 12), (9, 26), (1, 4), (5, 1), (40, 40)]
+    meta, off, oU, oS, oV = [], 0, 0, 0, 0
+    for m, n in shapes:
+        k = min(m, n)
+        meta.append(((off, off + m * n), (m, n), (oU, oU + m * k), (m, k), (oS, oS + k), (oV, oV + k * n), (k, n)))
+        off += m * n; oU += m * k; oS += k; oV += k * n
+    meta = tuple(meta)
+    f = lambda *sh: rng.normal(size=sh) + (1j * rng.normal(size=sh) if cplx else 0)
+    data = f(off)
+    q1, _ = np.linalg.qr(f(40, 40))
+    q2, _ = np.linalg.qr(f(40, 40))
+    a5 = meta[5][0][0]
+    data[a5:a5 + 1600] = ((q1 * np.logspace(0, -12, 40)) @ q2).ravel()   # graded over 12 decades
+    plan = P.svd_plan(meta, None, cplx, qr=True)
+    assert plan.qr and all(int(r[10]) == int(r[9]) for r in plan.blocks)
+    ct, rt = (np.complex128, np.complex64) if cplx else (np.float64, np.float32)
+    w32 = np.zeros(plan.n32, rt)
+    w64 = np.zeros(plan.n64, ct)
+    scale = []
+    for r in plan.blocks:
+        A = data[int(r[0]):int(r[0]) + int(r[1]) * int(r[2])]
+        scale.append(2.0 ** -np.frexp(np.linalg.norm(A))[1])
+    PI.qr_precondition(w64, w32, plan.blocks, data, scale)
+    nsw, conv = PI.jacobi_sweeps(w32, w32, plan.blocks, rt, 1e-4, 40)
+    assert all(conv)
+    for r in plan.blocks:
+        k = int(r[9])
+        w64[int(r[7]):int(r[7]) + k * k] = w32[int(r[14]):int(r[14]) + k * k]
+    w0, t0, n0, ws = plan.w_range
+    for _ in range(2):
+        w64[n0:n0 + ws] = w64[w0:w0 + ws]
+        PI.run_gemm(plan.gram, w64, w64, w64)
+        PI.run_gemm(plan.ns, w64, w64, w64, alpha=-0.5, beta=1.5)
+        w64[w0:w0 + ws] = w64[n0:n0 + ws]
+    PI.run_gemm(plan.xform, w64, w64, w64)
+    nsw, conv = PI.jacobi_sweeps(w64, w64, plan.blocks, ct, 1e-8, 20)
+    assert all(conv) and max(nsw) <= 4, nsw
+    U, S, V = np.zeros(oU, ct), np.zeros(oS), np.zeros(oV, ct)
+    PI.finalize_qr(w64, plan.blocks, U, S, V)
+    PI.run_gemm(plan.qfin_v, w64, w64, V)
+    PI.run_gemm(plan.qfin_u, w64, w64, U)
+    _, Sr, _ = oracle.svd(data, meta, (oU, oS, oV))
+    assert np.abs(S - Sr).max() <= 1e-13 * np.abs(Sr).max()
+    for sl, D, slU, DU, slS, slV, DV in meta:
+        u = U[slU[0]:slU[1]].reshape(DU)
+        vh = V[slV[0]:slV[1]].reshape(DV)
+        s = S[slS[0]:slS[1]]
+        a = data[sl[0]:sl[1]].reshape(D)
+        assert np.abs((u * s) @ vh - a).max() <= 1e-13 * max(np.abs(a).max(), 1e-300)
+        k = DU[1]
+        assert np.abs(u.conj().T @ u - np.eye(k)).max() <= 1e-13
+        assert np.abs(vh @ vh.conj().T - np.eye(k)).max() <= 1e-13
+
+
 def test_mixed_precision_jacobi_schedule_complex():
     """Complex blocks: FP32 phase on complex64 rows with phase-aligned rotations, widen,
     Newton-Schulz with T = W^H W, X = W X_0 (X_0 = A^H for tall blocks), FP64 phase; the

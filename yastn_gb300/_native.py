@@ -23,6 +23,7 @@ SIGNATURES = {
     'yb_gemm_reduce': ([_vp, _vp, _i, _vp, _vp, _i, _d, _d, _vp], _i),
     'yb_grouped_gemm': ([_vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _d, _d, _vp], _i),
     'yb_svd_init': ([_vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp], _i),
+    'yb_svd_qr': ([_vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _i, _vp], _i),
     'yb_svd_sweeps': ([_vp, _vp, _i, _vp, _i, _i, _i, _i, _i, _d, _vp, _vp], _i),
     'yb_svd_widen': ([_vp, _vp, _vp, _i, _i, _vp, _vp], _i),
     'yb_svd_block_sweeps': ([_vp, _vp, _i, _vp, _i, _i, _i, _i, _i, _i, _d, _i, _vp, _vp], _i),

@@ -17,7 +17,7 @@ CP_MAXD, CP_SIZE, CP_SSTR, CP_DSTR, CP_MAGIC, CP_SHIFT = 8, 8, 16, 24, 32, 40
 CP_KIND, CP_NX, CP_NY = 5, 6, 7
 COPY_ITEM_UNITS, COPY_TILE, COPY_ITEM_TILES = 2048, 32, 2
 GEMM_OUT_REC, GEMM_TERM_REC, GEMM_TILE = 8, 8, 64
-SVD_REC = 16
+SVD_REC = 24
 MASK_REC = 8
 
 
@@ -600,8 +600,10 @@ class SvdPlan:
     grouped-GEMM plans of the Newton-Schulz orthonormalisation and of X = W X_0."""
 
     def __init__(self, blocks, pair_items, max_rounds, max_k, nominal_flops, n64, n32, w_range, gram, ns, xform,
-                 rows_per_super=0, super_items=None, super_rounds=0, lmax=0):
+                 rows_per_super=0, super_items=None, super_rounds=0, lmax=0, qr=False, qfin_u=None, qfin_v=None):
         self.blocks = blocks
+        self.qr = qr            # QR-preconditioned: Jacobi on R's rows, then U or Vh by qfin_u / qfin_v
+        self.qfin_u, self.qfin_v = qfin_u, qfin_v
         self.pair_items = pair_items
         self.rows_per_super = rows_per_super  # 0: the FP32 phase uses the one-pair-per-warp kernel
         self.super_items = super_items        # (block, super pair) items of the blocked FP32 phase
@@ -630,11 +632,15 @@ def svd_rows_per_super(lmax, choices=(16, 8, 4), elem_bytes=4):
     return 0
 
 
-def svd_plan(meta, rows_per_super=None, cplx=False):
+def svd_plan(meta, rows_per_super=None, cplx=False, qr=False):
     """Jacobi plan for svd records (sl, D, slU, DU, slS, slV, DV) of yastn/tensor/linalg.py:323-380.
     ``rows_per_super`` fixes the super-vector height of the blocked FP32 phase (default: the
     largest of 16, 8, 4 whose rows fit in shared memory). ``cplx``: complex128 blocks (the
-    Gram product of Newton-Schulz is W^H W and tall blocks start from X_0 = A^H)."""
+    Gram product of Newton-Schulz is W^H W and tall blocks start from X_0 = A^H). ``qr``:
+    every block starts from the rows of R of a Householder QR (yb_svd_qr), the sweeps run on
+    k x k rows, and the factor not built from X's rows follows from Q by a grouped GEMM.
+
+    FP64 workspace: [X | W | T | Wn] and, with ``qr``, [Z | Householder vectors | tau | R]."""
     def build():
         sel = []
         for sl, D, slU, DU, slS, slV, DV in meta:
@@ -645,33 +651,48 @@ def svd_plan(meta, rows_per_super=None, cplx=False):
             if DU != (m, k) or DV != (k, n) or slS[1] - slS[0] != k:
                 raise PlanError("svd record is not a thin full-rank SVD")
             sel.append((sl, m, n, slU, slS, slV, k, max(m, n)))
-        xs = sum(k * L for *_, k, L in sel)
+        lj = (lambda k, L: k) if qr else (lambda k, L: L)  # row length of the Jacobi vectors
+        xs = sum(k * lj(k, L) for *_, k, L in sel)
         ws = sum(k * k for *_, k, L in sel)
         w0, t0, n0 = xs, xs + ws, xs + 2 * ws
-        recs, pairs, gram, ns, xf = [], [], [], [], []
-        ox = ow = ox32 = 0
+        zs = sum(k * L for *_, k, L in sel) if qr else 0
+        q0 = xs + 3 * ws                       # Z, then the Householder vectors, tau, R
+        v0, tau0, r0 = q0 + zs, q0 + 2 * zs, q0 + 2 * zs + sum(k for *_, k, L in sel)
+        recs, pairs, gram, ns, xf, qfu, qfv = [], [], [], [], [], [], []
+        ox = ow = ox32 = oz = otau = 0
         max_rounds = max_k = fl = 0
         for bi, (sl, m, n, slU, slS, slV, k, L) in enumerate(sel):
             N = k + (k % 2)
+            Lx = lj(k, L)
             rec = np.zeros(SVD_REC, dtype=np.int64)
-            rec[:15] = (sl[0], m, n, slU[0], slS[0], slV[0], ox, w0 + ow, len(pairs), k, L, N, int(m > n),
+            rec[:15] = (sl[0], m, n, slU[0], slS[0], slV[0], ox, w0 + ow, len(pairs), k, Lx, N, int(m > n),
                         ox32, xs + ow)
             recs.append(rec)
             pairs.extend((bi, p) for p in range(N // 2))
-            # T = W^T W ; Wn = 1.5 Wn - 0.5 W T (Wn holds a copy of W) ; X = W X_0
+            # T = W^T W ; Wn = 1.5 Wn - 0.5 W T (Wn holds a copy of W) ; X = W X_0 (QR: X = W R)
             gram.append((t0 + ow, k, k, k, [(w0 + ow, w0 + ow, k, 1, k, k, 1, int(cplx))]))
             ns.append((n0 + ow, k, k, k, [(w0 + ow, t0 + ow, k, k, 1, k, 1, 0)]))
-            if m > n:
+            if qr:
+                rec[16:23] = (1, L, q0 + oz, v0 + oz, tau0 + otau, r0 + ow, t0 + ow)
+                xf.append((ox, k, k, k, [(w0 + ow, r0 + ow, k, k, 1, k, 1, 0)]))
+                if m > n:   # U (m x k) = conj(Q) W_sorted^T: A_t[l, c] = conj(Z[c L + l]), B_t[c, j] = WS[j k + c]
+                    qfu.append((slU[0], m, k, k, [(q0 + oz, t0 + ow, k, 1, L, 1, k, int(cplx))]))
+                else:       # Vh (k x n) = conj(W_sorted) Q^T (the conjugate is in WS)
+                    qfv.append((slV[0], k, n, n, [(t0 + ow, q0 + oz, k, k, 1, L, 1, 0)]))
+                oz += k * L
+                otau += k
+            elif m > n:
                 xf.append((ox, k, L, L, [(w0 + ow, sl[0], k, k, 1, 1, n, 2 * int(cplx))]))
             else:
                 xf.append((ox, k, L, L, [(w0 + ow, sl[0], k, k, 1, n, 1, 0)]))
-            ox += k * L
-            ox32 += k * L
+            ox += k * Lx
+            ox32 += k * Lx
             ow += k * k
             max_rounds = max(max_rounds, N - 1)
             max_k = max(max_k, k)
             fl += 14 * L * k * k + 8 * k ** 3  # nominal Golub-Reinsch count
-        lmax = max((L for *_, k, L in sel), default=0)
+        lmax = max((lj(k, L) for *_, k, L in sel), default=0)
+        n64 = xs + 3 * ws + (2 * zs + sum(k for *_, k, L in sel) + ws if qr else 0)
         br = svd_rows_per_super(lmax, elem_bytes=8 if cplx else 4) if rows_per_super is None else rows_per_super
         supers, super_rounds = [], 0
         for bi, (*_, k, L) in enumerate(sel):
@@ -683,10 +704,11 @@ def svd_plan(meta, rows_per_super=None, cplx=False):
                 super_rounds = max(super_rounds, ns_ - 1)
         blocks = np.stack(recs) if recs else np.zeros((0, SVD_REC), dtype=np.int64)
         items = np.array(pairs, dtype=np.int32).reshape(-1, 2)
-        return SvdPlan(blocks, items, max_rounds, max_k, fl, xs + 3 * ws, xs + ws, (w0, t0, n0, ws),
+        return SvdPlan(blocks, items, max_rounds, max_k, fl, n64, xs + ws, (w0, t0, n0, ws),
                        _pack_gemm(gram), _pack_gemm(ns), _pack_gemm(xf),
-                       br, np.array(supers, dtype=np.int32).reshape(-1, 2), super_rounds, lmax)
-    return CACHE.get((meta,), ('svd', rows_per_super, cplx), build)
+                       br, np.array(supers, dtype=np.int32).reshape(-1, 2), super_rounds, lmax,
+                       qr, _pack_gemm(qfu) if qr else None, _pack_gemm(qfv) if qr else None)
+    return CACHE.get((meta,), ('svd', rows_per_super, cplx, qr), build)
 
 
 class SvdAdjointPlan:

@@ -35,7 +35,8 @@ constexpr int kThreads = kWarps * 32;
 constexpr long long kSpinLimit = 1ll << 22;
 
 // record fields
-enum { R_A = 0, R_M, R_N, R_U, R_S, R_V, R_X, R_W, R_P, R_K, R_L, R_NP, R_T, R_X32, R_W32, R_NSUP };
+enum { R_A = 0, R_M, R_N, R_U, R_S, R_V, R_X, R_W, R_P, R_K, R_L, R_NP, R_T, R_X32, R_W32, R_NSUP,
+       R_QR, R_LQ, R_Z, R_VQ, R_TAU, R_RR, R_WS };
 // per-block state (int64): [0] max |cos| of the sweep in progress (double bits),
 // [1] converged flag, [2] sweeps run in the current phase, [3] largest |cos| of the last sweep,
 // [4], [5] squared row norms (double bits) at or below which a row is rounding noise in the
@@ -265,6 +266,8 @@ template <typename TI>
 __global__ void block_fro_kernel(const TI* __restrict__ A, const int64_t* __restrict__ blocks,
                                  double* __restrict__ shift, double* __restrict__ scale,
                                  int64_t* __restrict__ state) {
+  // QR-preconditioned blocks start the FP32 phase from the rows of R, where small singular
+  // values are explicit row norms rather than cancellations: its noise norm is FP64's
   __shared__ double red[32];
   const int64_t* r = blocks + (int64_t)blockIdx.x * YB_SVD_REC;
   const int64_t cnt = r[R_M] * r[R_N];
@@ -288,7 +291,7 @@ __global__ void block_fro_kernel(const TI* __restrict__ A, const int64_t* __rest
     if (bound > 0.0 && bound <= 1.0e300) frexp(bound, &e);
     scale[blockIdx.x] = ldexp(1.0, -e);
     // the FP32 phase works on scale * A, the FP64 phase on A itself
-    const double t32 = kNoise32 * fro * ldexp(1.0, -e), t64 = kNoise64 * fro;
+    const double t32 = (r[R_QR] ? kNoise64 : kNoise32) * fro * ldexp(1.0, -e), t64 = kNoise64 * fro;
     state[(int64_t)blockIdx.x * ST_REC + ST_THR32] = __double_as_longlong(t32 * t32);
     state[(int64_t)blockIdx.x * ST_REC + ST_THR64] = __double_as_longlong(t64 * t64);
   }
@@ -321,6 +324,11 @@ __global__ void svd_init_kernel(const TI* __restrict__ A, T32* __restrict__ work
     }
   }
   if (blockIdx.x == 0 && threadIdx.x < ST_THR32) state[blockIdx.y * ST_REC + threadIdx.x] = 0;
+}
+
+// Resets the sweep words (0..3) of each block's state (the noise norms stay).
+__global__ void svd_state_reset_kernel(int64_t* __restrict__ state) {
+  if (threadIdx.x < ST_THR32) state[blockIdx.x * ST_REC + threadIdx.x] = 0;
 }
 
 // W64 = widen(W32) (the host orthonormalises it next); resets the per-block state.
@@ -683,8 +691,162 @@ int launch_block_sweeps(T* work, const int64_t* blocks, int n_blocks, const int3
 // mode 0: SVD. mode 1/2: Hermitian eigendecomposition of a block shifted by shift[b]
 // (lambda = sigma - shift), eigenvectors = columns of W^H, ordered ascending (1) or by
 // |lambda| descending (2); Vh is not written.
+// ---------------------------------------------------------------- QR preconditioning
+// A block whose spectrum is graded (singular values spread over many decades, as in the
+// projector blocks of a corner transfer matrix step) keeps one-sided Jacobi busy for tens of
+// FP64 sweeps when started from the rows of A, where the small singular values are hidden
+// in cancellations. Started from the rows of the triangular factor R of a Householder QR,
+// they are explicit (graded row norms): the FP32 phase then resolves the whole spectrum and
+// FP64 needs a few sweeps. With M = X_0^T (A^T for wide/square blocks, conj(A) for tall
+// ones; M's columns are the rows of X_0) and M = Q R:
+//   wide:  A = R^T Q^T;      W R = S Y  =>  U = Y^T,  Vh = conj(W) Q^T
+//   tall:  A = conj(Q R);                 =>  U = conj(Q) W^T,  Vh = conj(Y)
+// (Y: rows of X = W R normalised, W: the accumulated rotations). Z holds M's columns as
+// rows (Z = X_0, k rows of length L); the factorisation leaves R in Z's upper part and the
+// Householder vectors below the diagonal (LAPACK's geqr2 layout, transposed); Q^T is then
+// formed in place (org2r, backward accumulation).
+
+// Z = X_0 in FP64 (A, or A^H for tall blocks).
 template <typename T>
-__global__ void __launch_bounds__(1024) svd_finalize_kernel(const T* __restrict__ work, T* __restrict__ U,
+__global__ void svd_qr_load_kernel(const T* __restrict__ A, T* __restrict__ work, const int64_t* __restrict__ blocks) {
+  const int64_t* r = blocks + (int64_t)blockIdx.y * YB_SVD_REC;
+  if (!r[R_QR]) return;
+  const int64_t m = r[R_M], n = r[R_N], k = r[R_K], L = r[R_LQ];
+  const bool tall = m > n;
+  const T* a = A + r[R_A];
+  T* Z = work + r[R_Z];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < k * L; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / L, l = e - i * L;
+    Z[e] = tall ? cconj_(a[l * n + i]) : a[e];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T ldcg_t(const T* p) { return __ldcg(p); }
+
+// Householder reflector of row j of Z on its elements [j, L) (LAPACK larfg): beta real,
+// tau = (beta - alpha) / beta, v = x / (alpha - beta) with v_0 = 1 implicit; Z[j] = beta,
+// v stored in Z[j+1..L), tau in tau[j]. One warp.
+template <typename T>
+__device__ void qr_reflector(T* __restrict__ z, T* __restrict__ tau, int64_t j, int64_t L, int lane) {
+  __syncwarp();  // the row was just rewritten by other lanes of this warp
+  double xn = 0.0;
+  for (int64_t l = j + 1 + lane; l < L; l += 32) xn += cabs2(ldcg_t(z + l));
+  xn = warp_sum(xn);
+  const T alpha = ldcg_t(z + j);
+  double ar, ai;
+  if constexpr (Num<T>::cplx) { ar = alpha.x; ai = alpha.y; } else { ar = alpha; ai = 0.0; }
+  if (xn == 0.0 && ai == 0.0) {
+    if (lane == 0) tau[j] = Num<T>::zero();
+    return;
+  }
+  const double beta = -copysign(sqrt(ar * ar + ai * ai + xn), ar);
+  T tv, sc;
+  if constexpr (Num<T>::cplx) {
+    tv = make_double2((beta - ar) / beta, -ai / beta);
+    // 1 / (alpha - beta)
+    const double dr = ar - beta, di = ai, d2 = dr * dr + di * di;
+    sc = make_double2(dr / d2, -di / d2);
+  } else {
+    tv = (beta - ar) / beta;
+    sc = 1.0 / (ar - beta);
+  }
+  for (int64_t l = j + 1 + lane; l < L; l += 32) z[l] = Num<T>::mul(sc, ldcg_t(z + l));
+  if (lane == 0) {
+    if constexpr (Num<T>::cplx) z[j] = make_double2(beta, 0.0); else z[j] = beta;
+    tau[j] = tv;
+  }
+}
+
+// Applies I - t v v^H (v_0 = 1 at element j, v_l at elements l > j of vrow) to a row segment
+// x[j..L) of Z: w = x_j + sum_l conj(v_l) x_l; x_j -= t w; x_l -= t w v_l. One warp.
+template <typename T>
+__device__ __forceinline__ void qr_apply(T* __restrict__ x, const T* __restrict__ vrow, T t, int64_t j, int64_t L,
+                                         int lane) {
+  const T xj = ldcg_t(x + j);
+  T w = Num<T>::zero();
+  for (int64_t l = j + 1 + lane; l < L; l += 32) w = Num<T>::fmac(ldcg_t(x + l), ldcg_t(vrow + l), w);
+  warp_sum_t<T>(w);
+  w = Num<T>::add(w, xj);
+  const T tw = Num<T>::mul(t, w);
+  if (lane == 0) x[j] = Num<T>::sub(xj, tw);
+  for (int64_t l = j + 1 + lane; l < L; l += 32) x[l] = Num<T>::sub(ldcg_t(x + l), Num<T>::mul(tw, ldcg_t(vrow + l)));
+  __syncwarp();
+}
+
+// One cooperative launch: groups of `group` CTAs factor one block at a time (group barriers
+// between Householder steps), write R's rows (FP64, RR) and the FP32 Jacobi start
+// X32 = scale R, W32 = I, keep the reflectors (VQ, tau), and form Q^T in Z. Row c of Z is
+// handled by warp c mod (8 group) of the group throughout, so a row is only ever rewritten by
+// the warp that reads it; the reflector of row j+1 is made by its warp right after its update.
+template <typename T, typename T32>
+__global__ void __launch_bounds__(kThreads) svd_qr_kernel(T* __restrict__ work, T32* __restrict__ work32,
+                                                          const int64_t* __restrict__ blocks, int n_blocks,
+                                                          int group, unsigned long long* __restrict__ qctrl,
+                                                          const double* __restrict__ scale) {
+  const int g = blockIdx.x / group, rank = blockIdx.x % group;
+  const int n_groups = gridDim.x / group;
+  if (g >= n_groups) return;
+  unsigned long long* ctrl = qctrl + (int64_t)g * C_REC;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t gw = (int64_t)rank * kWarps + warp, nwg = (int64_t)group * kWarps;
+  const int64_t gt = (int64_t)rank * kThreads + threadIdx.x, ngt = (int64_t)group * kThreads;
+  for (int b = g; b < n_blocks; b += n_groups) {
+    const int64_t* r = blocks + (int64_t)b * YB_SVD_REC;
+    if (!r[R_QR]) continue;
+    const int64_t k = r[R_K], L = r[R_LQ];
+    T* Z = work + r[R_Z];
+    T* V = work + r[R_VQ];
+    T* tau = work + r[R_TAU];
+    T* RR = work + r[R_RR];
+    T32* X32 = work32 + r[R_X32];
+    T32* W32 = work32 + r[R_W32];
+    const double sc = scale[b];
+    // factorisation
+    if (gw == 0) qr_reflector<T>(Z, tau, 0, L, lane);
+    if (!grid_barrier(ctrl, group)) return;
+    for (int64_t j = 0; j < k; ++j) {
+      const T* vrow = Z + j * L;
+      T t = ldcg_t(tau + j);
+      t = Num<T>::conj(t);  // M <- H^H M
+      const int64_t first = j + 1 + ((gw - (j + 1)) % nwg + nwg) % nwg;
+      for (int64_t c = first; c < k; c += nwg) {
+        qr_apply<T>(Z + c * L, vrow, t, j, L, lane);
+        if (c == j + 1) qr_reflector<T>(Z + c * L, tau, j + 1, L, lane);
+      }
+      if (!grid_barrier(ctrl, group)) return;
+    }
+    // R rows, the FP32 start, the reflectors
+    for (int64_t e = gt; e < k * k; e += ngt) {
+      const int64_t i = e / k, c = e - i * k;
+      const T v = (c >= i) ? ldcg_t(Z + c * L + i) : Num<T>::zero();
+      RR[e] = v;
+      X32[e] = to32(rscale(v, sc));
+      W32[e] = (i == c) ? Num<T32>::one() : Num<T32>::zero();
+    }
+    for (int64_t e = gt; e < k * L; e += ngt) {
+      const int64_t j = e / L, l = e - j * L;
+      V[e] = (l > j) ? ldcg_t(Z + e) : Num<T>::zero();
+    }
+    if (!grid_barrier(ctrl, group)) return;
+    for (int64_t e = gt; e < k * L; e += ngt) {
+      const int64_t i = e / L, l = e - i * L;
+      Z[e] = (i == l) ? Num<T>::one() : Num<T>::zero();
+    }
+    if (!grid_barrier(ctrl, group)) return;
+    // Q^T = (H_0 ... H_{k-1} [I; 0])^T, backward
+    for (int64_t j = k - 1; j >= 0; --j) {
+      const T* vrow = V + j * L;
+      const T t = ldcg_t(tau + j);
+      const int64_t first = j + ((gw - j) % nwg + nwg) % nwg;
+      for (int64_t c = first; c < k; c += nwg) qr_apply<T>(Z + c * L, vrow, t, j, L, lane);
+      if (!grid_barrier(ctrl, group)) return;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) svd_finalize_kernel(T* __restrict__ work, T* __restrict__ U,
                                                             double* __restrict__ S, T* __restrict__ Vh,
                                                             const int64_t* __restrict__ blocks, int pow2,
                                                             int mode, const double* __restrict__ shift,
@@ -774,45 +936,88 @@ __global__ void __launch_bounds__(1024) svd_finalize_kernel(const T* __restrict_
     if (!(sig[j] > zthr && sig[j] > 0.0)) atomicAdd(&n_zero, 1);
   }
   // wide (X_0 = A): Vh rows = x_j / s_j, U = W^H; tall (X_0 = A^H): U columns = conj(x_j) / s_j,
-  // Vh = W
+  // Vh = W. QR-preconditioned (X_0 = R): wide: U columns = x_j / s_j, and the sorted conj(W)
+  // goes to WS for Vh = conj(W) Q^T; tall: Vh rows = conj(x_j) / s_j, WS = sorted W for
+  // U = conj(Q) W^T (both products follow as grouped GEMMs).
+  const bool qr = r[R_QR] != 0;
+  const bool to_u = tall != qr;  // the factor built from the rows of X
   for (int64_t e = threadIdx.x; e < k * L; e += blockDim.x) {
     const int64_t j = e / L, l = e - j * L;
     const double sv = sig[j];
     const T x = X[(int64_t)idx[j] * L + l];
-    const T v = (sv > zthr && sv > 0.0) ? rscale(x, 1.0 / sv) : rscale(x, 0.0);
-    if (tall) Ub[l * k + j] = cconj_(v); else Vb[j * n + l] = v;
+    T v = (sv > zthr && sv > 0.0) ? rscale(x, 1.0 / sv) : rscale(x, 0.0);
+    if (tall) v = cconj_(v);
+    if (to_u) Ub[l * k + j] = v; else Vb[j * n + l] = v;
   }
+  T* WS = work + r[R_WS];
   for (int64_t e = threadIdx.x; e < k * k; e += blockDim.x) {
     const int64_t j = e / k, c = e - j * k;
     const T w = W[(int64_t)idx[j] * k + c];
-    if (tall) Vb[j * n + c] = w; else Ub[c * k + j] = cconj_(w);
+    if (qr) WS[e] = tall ? w : cconj_(w);
+    else if (tall) Vb[j * n + c] = w;
+    else Ub[c * k + j] = cconj_(w);
   }
   __syncthreads();
   if (n_zero == 0) return;
   // completion: the small values sit at the end (positions k - n_zero .. k-1); each of their
   // vectors becomes a unit vector e_c orthogonalised against all earlier vectors by two passes
-  // of classical Gram-Schmidt (all coefficients of a pass at once). Candidates c run on from
-  // the last one tried; one whose residual exceeds 0.5 sqrt((L - j) / L) is taken (the
-  // residuals of all L unit vectors have squares summing to L - j, so one always qualifies).
-  // The coefficients of a pass live in shared memory: real parts in the sig array (no longer
-  // needed), imaginary parts in the complex area.
-  const int64_t stride_v = tall ? k : 1;  // distance between consecutive entries of one vector
-  const int64_t stride_j = tall ? 1 : n;  // distance between vectors
-  T* base = tall ? Ub : Vb;
+  // of classical Gram-Schmidt (all coefficients of a pass at once). The candidate is the
+  // coordinate least covered by the earlier (orthonormal) vectors, c = argmin_l
+  // sum_{i<j} |v_i[l]|^2: its residual norm^2 is 1 minus that sum, at least (L - j) / L since
+  // the sums over l add up to j. The coefficients of a pass live in shared memory: real parts
+  // in the sig array (no longer needed), imaginary parts in the complex area.
+  const int64_t stride_v = to_u ? k : 1;  // distance between consecutive entries of one vector
+  const int64_t stride_j = to_u ? 1 : n;  // distance between vectors
+  T* base = to_u ? Ub : Vb;
   __shared__ double red[32];
+  __shared__ int64_t redi[32];
   __shared__ double nrm_s;
+  __shared__ int64_t cand_s;
   double* cre = sig;
-  int64_t cand = 0;
   for (int64_t j = k - n_zero; j < k; ++j) {
     T* vj = base + j * stride_j;
-    const double need = 0.5 * sqrt((double)(L - j) / (double)L);
-    for (int64_t tries = 0; tries < L; ++tries, cand = (cand + 1 == L ? 0 : cand + 1)) {
+    {
+      // coverage of each coordinate by v_0..v_{j-1}; block argmin (ties: the smaller l)
+      double bv = 3.0e300;
+      int64_t bl = L;
+      if (to_u) {
+        for (int64_t l = warp; l < L; l += nw) {
+          double acc = 0.0;
+          for (int64_t i = lane; i < j; i += 32) acc += cabs2(base[l * stride_v + i]);
+          acc = warp_sum(acc);
+          if (acc < bv) { bv = acc; bl = l; }
+        }
+      } else {
+        for (int64_t l = threadIdx.x; l < L; l += blockDim.x) {
+          double acc = 0.0;
+          for (int64_t i = 0; i < j; ++i) acc += cabs2(base[i * stride_j + l]);
+          if (acc < bv) { bv = acc; bl = l; }
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const long long ol = __shfl_xor_sync(0xffffffffu, (long long)bl, o);
+        if (ov < bv || (ov == bv && ol < bl)) { bv = ov; bl = ol; }
+      }
+      if (lane == 0) { red[warp] = bv; redi[warp] = bl; }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double v = red[0];
+        int64_t c = redi[0];
+        for (int w = 1; w < nw; ++w)
+          if (red[w] < v || (red[w] == v && redi[w] < c)) { v = red[w]; c = redi[w]; }
+        cand_s = c < L ? c : 0;
+      }
+      __syncthreads();
+    }
+    const int64_t cand = cand_s;
+    {
       for (int64_t l = threadIdx.x; l < L; l += blockDim.x)
         vj[l * stride_v] = (l == cand) ? Num<T>::one() : Num<T>::zero();
       __syncthreads();
       for (int pass = 0; pass < 2; ++pass) {
         // coefficients c_i = <v_i, v_j> = sum_l conj(v_i[l]) v_j[l], i < j
-        if (tall) {
+        if (to_u) {
           // vectors are contiguous across i for a fixed l: one thread per i
           for (int64_t i = threadIdx.x; i < j; i += blockDim.x) {
             T acc = Num<T>::zero();
@@ -842,7 +1047,7 @@ __global__ void __launch_bounds__(1024) svd_finalize_kernel(const T* __restrict_
         }
         __syncthreads();
         // v_j -= sum_i c_i v_i
-        if (tall) {
+        if (to_u) {
           // row l of U holds entry l of every vector: one warp per l
           for (int64_t l = warp; l < L; l += nw) {
             T acc = Num<T>::zero();
@@ -881,12 +1086,8 @@ __global__ void __launch_bounds__(1024) svd_finalize_kernel(const T* __restrict_
       }
       __syncthreads();
       const double nrm = nrm_s;
-      if (nrm > need) {
-        for (int64_t l = threadIdx.x; l < L; l += blockDim.x) vj[l * stride_v] = rscale(vj[l * stride_v], 1.0 / nrm);
-        __syncthreads();
-        cand = (cand + 1 == L ? 0 : cand + 1);
-        break;
-      }
+      for (int64_t l = threadIdx.x; l < L; l += blockDim.x)
+        vj[l * stride_v] = nrm > 0.0 ? rscale(vj[l * stride_v], 1.0 / nrm) : Num<T>::zero();
       __syncthreads();
     }
   }
@@ -933,8 +1134,39 @@ int block_sweeps_t(T* w, const int64_t* blocks, int n_blocks, const int32_t* sup
   }
 }
 
+template <typename T, typename T32>
+int qr_t(const void* a, void* work, void* work32, const int64_t* blocks, int n_blocks, int64_t* state, double* scale,
+         int64_t* qctrl, int qctrl_words, cudaStream_t s) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, yb::svd_qr_kernel<T, T32>, yb::kThreads, 0);
+  if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
+  const int capacity = sms * (per_sm < 1 ? 1 : per_sm);
+  int group = capacity / n_blocks;
+  group = group < 1 ? 1 : (group > 16 ? 16 : group);
+  int n_groups = capacity / group;
+  if (n_groups > n_blocks) n_groups = n_blocks;
+  if ((int64_t)n_groups * yb::C_REC > qctrl_words) n_groups = qctrl_words / yb::C_REC;
+  if (n_groups < 1) return YB_ERR_INVALID;
+  yb::block_fro_kernel<T><<<n_blocks, 256, 0, s>>>((const T*)a, blocks, nullptr, scale, state);
+  yb::svd_qr_load_kernel<T><<<dim3(64, (unsigned)n_blocks), 256, 0, s>>>((const T*)a, (T*)work, blocks);
+  e = cudaMemsetAsync(qctrl, 0, sizeof(int64_t) * (size_t)n_groups * yb::C_REC, s);
+  if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
+  T* w = (T*)work;
+  T32* w32 = (T32*)work32;
+  unsigned long long* qc = (unsigned long long*)qctrl;
+  void* args[] = {&w, &w32, &blocks, &n_blocks, &group, &qc, &scale};
+  e = cudaLaunchCooperativeKernel((const void*)yb::svd_qr_kernel<T, T32>, dim3(n_groups * group), dim3(yb::kThreads),
+                                  args, 0, s);
+  if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
+  yb::svd_state_reset_kernel<<<n_blocks, 32, 0, s>>>(state);
+  return yb::check_launch();
+}
+
 template <typename T>
-int finalize_t(const void* work, void* U, double* S, void* Vh, const int64_t* blocks, int n_blocks, int pow2,
+int finalize_t(void* work, void* U, double* S, void* Vh, const int64_t* blocks, int n_blocks, int pow2,
                       int mode, const double* shift, const int64_t* state, cudaStream_t s) {
   const size_t smem = (size_t)pow2 * (sizeof(double) * (Num<T>::cplx ? 2 : 1) + sizeof(int));
   if (smem > 48 * 1024) {
@@ -942,7 +1174,7 @@ int finalize_t(const void* work, void* U, double* S, void* Vh, const int64_t* bl
                                          (int)smem);
     if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
   }
-  yb::svd_finalize_kernel<T><<<n_blocks, 1024, smem, s>>>((const T*)work, (T*)U, S, (T*)Vh, blocks, pow2, mode,
+  yb::svd_finalize_kernel<T><<<n_blocks, 1024, smem, s>>>((T*)work, (T*)U, S, (T*)Vh, blocks, pow2, mode,
                                                           shift, state);
   return yb::check_launch();
 }
@@ -968,6 +1200,17 @@ int yb_svd_init(const void* a, void* work32, const int64_t* blocks, int n_blocks
                                                               shift, scale);
   }
   return yb::check_launch();
+}
+
+int yb_svd_qr(const void* a, void* work64, void* work32, const int64_t* blocks, int n_blocks, int dtype,
+              int64_t* state, double* scale, int64_t* qctrl, int qctrl_words, void* stream) {
+  if (n_blocks == 0) return YB_OK;
+  if (dtype != YB_F64 && dtype != YB_C128) return YB_ERR_INVALID;
+  if (!a || !work64 || !work32 || !blocks || !state || !scale || !qctrl) return YB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == YB_F64)
+    return yb::qr_t<double, float>(a, work64, work32, blocks, n_blocks, state, scale, qctrl, qctrl_words, s);
+  return yb::qr_t<double2, float2>(a, work64, work32, blocks, n_blocks, state, scale, qctrl, qctrl_words, s);
 }
 
 int yb_svd_sweeps(void* work, const int64_t* blocks, int n_blocks, const int32_t* pair_items, int n_pair_items,
@@ -1039,7 +1282,7 @@ int yb_svd_shift_prefill(void* work64, const int64_t* blocks, int n_blocks, int 
   return yb::check_launch();
 }
 
-int yb_svd_finalize(const void* work, void* U, double* S, void* Vh, const int64_t* blocks, int n_blocks, int dtype,
+int yb_svd_finalize(void* work, void* U, double* S, void* Vh, const int64_t* blocks, int n_blocks, int dtype,
                     int max_k, int mode, const double* shift, const int64_t* state, void* stream) {
   if (n_blocks == 0) return YB_OK;
   if (dtype != YB_F64 && dtype != YB_C128) return YB_ERR_INVALID;

@@ -302,6 +302,7 @@ INNER_SWEEPS32 = 1    # blocked FP32 phase: Jacobi sweeps among the rows of a su
 BLOCKED_FP32 = [True]  # FP32 phase on super-vectors in shared memory (False: one pair per warp)
 ROWS_PER_SUPER = [None]  # super-vector height (None: largest of 16, 8, 4 that fits)
 NS_STEPS = 2          # Newton-Schulz steps: non-orthogonality ~1e-6 -> 1e-12 -> ~eps
+SVD_QR = [True]       # svd: Jacobi on the rows of R of a Householder QR (few FP64 sweeps on graded spectra)
 
 
 SVD_STATE_REC = 6     # int64 words of per-block Jacobi state (yb_svd.cu)
@@ -332,8 +333,14 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
     shift = aux[nb:] if mode != 0 else None
     sp = _vp(shift.data_ptr() if shift is not None else 0)
     st = _stream()
-    N.call('yb_svd_init', _ptr(data), _ptr(w32), _ptr(dblocks), nb, code, _ptr(state), sp, _ptr(aux[:nb]), st,
-           launches=2)
+    qctrl = None
+    if plan.qr:
+        qctrl = torch.empty(4 * min(nb, 4096), dtype=torch.int64, device=dev)
+        N.call('yb_svd_qr', _ptr(data), _ptr(w64), _ptr(w32), _ptr(dblocks), nb, code, _ptr(state), _ptr(aux[:nb]),
+               _ptr(qctrl), qctrl.numel(), st, launches=4)
+    else:
+        N.call('yb_svd_init', _ptr(data), _ptr(w32), _ptr(dblocks), nb, code, _ptr(state), sp, _ptr(aux[:nb]), st,
+               launches=2)
     if plan.rows_per_super and BLOCKED_FP32[0]:
         (dsup,) = _dev(plan, 'svd_super', (plan.super_items,), dev)
         N.call('yb_svd_block_sweeps', _ptr(w32), _ptr(dblocks), nb, _ptr(dsup), len(plan.super_items),
@@ -343,6 +350,8 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
         N.call('yb_svd_sweeps', _ptr(w32), _ptr(dblocks), nb, _ptr(dpairs), len(plan.pair_items), plan.max_rounds,
                32, code, MAX_SWEEPS32, TOL_STOP32, _ptr(state), st)
     _svd_state_check(state, nb, 'FP32', False)
+    if qctrl is not None and bool(qctrl[2::4].any()):
+        raise RuntimeError("yastn_gb300 svd: QR group barrier timed out")
     N.call('yb_svd_widen', _ptr(w32), _ptr(w64), _ptr(dblocks), nb, code, _ptr(state), st)
     w0, t0, n0, ws = plan.w_range
     W, Wn = w64[w0:w0 + ws], w64[n0:n0 + ws]
@@ -351,7 +360,9 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
         run_gemm(plan.gram, w64, w64, w64)
         run_gemm(plan.ns, w64, w64, w64, alpha=-0.5, beta=1.5)
         W.copy_(Wn)
-    if shift is not None:
+    if plan.qr:
+        run_gemm(plan.xform, w64, w64, w64)  # X = W R
+    elif shift is not None:
         N.call('yb_svd_shift_prefill', _ptr(w64), _ptr(dblocks), nb, code, _ptr(shift), st)
         run_gemm(plan.xform, w64, data, w64, beta=1.0)
     else:
@@ -361,6 +372,9 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
     _svd_state_check(state, nb, 'FP64', True)
     N.call('yb_svd_finalize', _ptr(w64), _ptr(U), _ptr(S), _vp(V.data_ptr() if V is not None else 0), _ptr(dblocks),
            nb, code, plan.max_k, mode, sp, _ptr(state), st)
+    if plan.qr:  # the factor that comes from Q: Vh = conj(W) Q^T (wide), U = conj(Q) W^T (tall)
+        run_gemm(plan.qfin_v, w64, w64, V)
+        run_gemm(plan.qfin_u, w64, w64, U)
 
 
 def svd(data, meta, sizes, max_sweeps=MAX_SWEEPS):
@@ -370,7 +384,7 @@ def svd(data, meta, sizes, max_sweeps=MAX_SWEEPS):
     U = torch.empty(sizes[0], dtype=data.dtype, device=dev)
     S = torch.empty(sizes[1], dtype=torch.float64, device=dev)
     V = torch.empty(sizes[2], dtype=data.dtype, device=dev)
-    plan = P.svd_plan(meta, ROWS_PER_SUPER[0], data.is_complex())
+    plan = P.svd_plan(meta, ROWS_PER_SUPER[0], data.is_complex(), qr=SVD_QR[0])
     if len(plan.blocks) == 0:
         return U, S, V
     _jacobi(data, plan, U, S, V, 0, max_sweeps)
