@@ -214,7 +214,7 @@ int yb_ozaki_dot_static(const double* A, const double* B, double* C,
  *   [17] L = max(m,n) of the QR workspaces [18] Z offset (k x L: X_0, then Q^T)
  *   [19] offset of the Householder vectors (k x L) [20] offset of tau (k)
  *   [21] offset of R's rows (k x k) [22] offset of the sorted W written by yb_svd_finalize
- *   (all FP64 workspace offsets; [23] unused)
+ *   (all FP64 workspace offsets) [23] number of super-vectors of the blocked FP64 phase
  * X holds the k vectors (rows of A, or of A^T when m > n) of length L, W the k x k
  * accumulated rotations (X = W X_0 throughout).
  * pair_items: int32 pairs (block, pair index 0..N/2-1) over all blocks.
@@ -258,9 +258,11 @@ int yb_svd_sweeps(void* work, const int64_t* blocks, int n_blocks, const int32_t
  * shared memory (2 * rows_per_super * lmax FP32 elements, lmax >= every L), runs up to
  * inner_sweeps Jacobi sweeps among them and applies the accumulated rotation to the W rows.
  * super_items: int32 pairs (block, super pair index 0..[15]/2-1); max_rounds = max([15]) - 1.
+ * precision 32: the FP32 phase (rows_per_super 16, 8 or 4; super-vector count [15]);
+ * precision 64: the FP64 phase on the FP64 workspace (rows_per_super 4 or 8; count [23]).
  * Returns YB_ERR_TOO_LARGE if the rows do not fit in shared memory. */
 int yb_svd_block_sweeps(void* work32, const int64_t* blocks, int n_blocks, const int32_t* super_items,
-                        int n_items, int max_rounds, int rows_per_super, int dtype, int max_sweeps,
+                        int n_items, int max_rounds, int rows_per_super, int precision, int dtype, int max_sweeps,
                         int inner_sweeps, double tol_stop, int lmax, int64_t* state, void* stream);
 int yb_svd_widen(const void* work32, void* work64, const int64_t* blocks, int n_blocks, int dtype,
                  int64_t* state, void* stream);
@@ -276,8 +278,11 @@ int yb_svd_shift_prefill(void* work64, const int64_t* blocks, int n_blocks, int 
  * on R's rows (row length k); yb_svd_finalize writes U's columns (wide) or Vh's rows (tall)
  * from X and the sorted W to [22]; the host completes Vh = conj(W_sorted) Q^T (wide) or
  * U = conj(Q) W_sorted^T (tall) with grouped GEMMs. qctrl: int64[qctrl_words] scratch,
- * at least 4 words (4 per CTA group used). On a graded spectrum Jacobi from R's rows needs
- * a few FP64 sweeps where Jacobi from A's rows needs tens. */
+ * at least n_blocks + 4 words: per block a counter of published reflectors (warps wait on
+ * it with a bounded spin instead of a barrier per Householder step), then 4 words per CTA
+ * group (barrier count, generation, error flag, unused); on a timeout a group's error word
+ * (qctrl[n_blocks + 4 g + 2]) is set. On a graded spectrum Jacobi from R's rows needs a few
+ * FP64 sweeps where Jacobi from A's rows needs tens. */
 int yb_svd_qr(const void* a, void* work64, void* work32, const int64_t* blocks, int n_blocks, int dtype,
               int64_t* state, double* scale, int64_t* qctrl, int qctrl_words, void* stream);
 int yb_svd_finalize(void* work, void* U, double* S, void* Vh, const int64_t* blocks,

@@ -42,8 +42,10 @@ def test_invalid_arguments_are_rejected_on_host(lib):
     assert lib.yb_svd_init(null, null, null, 2, N.YB_C128, null, null, null, null) == N.YB_ERR_INVALID  # null data
     assert lib.yb_svd_sweeps(null, null, 1, null, 1, 1, 32, 7, 1, 0.0, null, null) == N.YB_ERR_INVALID
     assert lib.yb_svd_widen(null, null, null, 1, N.YB_F64, null, null) == N.YB_ERR_INVALID
-    assert lib.yb_svd_block_sweeps(null, null, 1, null, 1, 1, 16, N.YB_F64, 1, 1, 0.0, 0, null, null) == \
+    assert lib.yb_svd_block_sweeps(null, null, 1, null, 1, 1, 16, 32, N.YB_F64, 1, 1, 0.0, 0, null, null) == \
         N.YB_ERR_INVALID
+    assert lib.yb_svd_qr(null, null, null, null, 1, N.YB_F64, null, null, null, 8, null) == N.YB_ERR_INVALID
+    assert lib.yb_gemm_reduce(null, null, N.YB_F64, null, null, 1, 1.0, 0.0, null) == N.YB_ERR_INVALID
     assert lib.yb_svd_finalize(null, null, null, null, null, 1, 0, 10000, 0, null, null, null) == N.YB_ERR_TOO_LARGE
     assert lib.yb_svd_finalize(null, null, null, null, null, 1, 0, 10, 1, null, null, null) == N.YB_ERR_INVALID
     assert lib.yb_truncation_mask(null, 20000, null, null, 1, 0.0, -1, 0, null, null, null) == N.YB_ERR_TOO_LARGE

@@ -105,6 +105,37 @@ def test_svd_rank_deficient_and_zero_blocks(cuda_device):
     check_svd(data, meta, U, S, V, Sr)
 
 
+@pytest.mark.parametrize('qr,blocked64', [(True, True), (True, False), (False, True), (False, False)])
+@pytest.mark.parametrize('cplx', [False, True])
+def test_svd_start_and_fp64_phase_variants(qr, blocked64, cplx, cuda_device):
+    """Every combination of the start (QR-preconditioned or from A's rows) and of the FP64
+    phase (4-row super-vectors in shared memory, or one pair per warp) on random, graded,
+    rank-deficient, tall, wide and tiny blocks."""
+    rng = np.random.default_rng(31)
+    f = lambda *sh: rng.normal(size=sh) + (1j * rng.normal(size=sh) if cplx else 0)
+    q1, _ = np.linalg.qr(f(120, 120))
+    q2, _ = np.linalg.qr(f(120, 120))
+    blocks = [f(70, 50), f(33, 90), f(1, 5), f(6, 1), (q1 * np.logspace(0, -13, 120)) @ q2,
+              f(64, 20) @ f(20, 64), np.zeros((7, 9))]
+    meta, off, oU, oS, oV, parts = [], 0, 0, 0, 0, []
+    for a in blocks:
+        m, n = a.shape
+        k = min(m, n)
+        meta.append(((off, off + m * n), (m, n), (oU, oU + m * k), (m, k), (oS, oS + k), (oV, oV + k * n), (k, n)))
+        off += m * n; oU += m * k; oS += k; oV += k * n
+        parts.append(a.ravel())
+    meta = tuple(meta)
+    data = np.concatenate(parts)
+    saved = ops.SVD_QR[0], ops.BLOCKED_FP64[0]
+    ops.SVD_QR[0], ops.BLOCKED_FP64[0] = qr, blocked64
+    try:
+        U, S, V = (host(x) for x in ops.svd(dev(data), meta, (oU, oS, oV)))
+    finally:
+        ops.SVD_QR[0], ops.BLOCKED_FP64[0] = saved
+    _, Sr, _ = oracle.svd(data, meta, (oU, oS, oV))
+    check_svd(data, meta, U, S, V, Sr)
+
+
 @pytest.mark.parametrize('cplx', [False, True])
 def test_svd_large_rank_deficient_blocks(cplx, cuda_device):
     """Blocks of low numerical rank (products of thin factors, as the projector blocks of a

@@ -26,7 +26,7 @@ SIGNATURES = {
     'yb_svd_qr': ([_vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _i, _vp], _i),
     'yb_svd_sweeps': ([_vp, _vp, _i, _vp, _i, _i, _i, _i, _i, _d, _vp, _vp], _i),
     'yb_svd_widen': ([_vp, _vp, _vp, _i, _i, _vp, _vp], _i),
-    'yb_svd_block_sweeps': ([_vp, _vp, _i, _vp, _i, _i, _i, _i, _i, _i, _d, _i, _vp, _vp], _i),
+    'yb_svd_block_sweeps': ([_vp, _vp, _i, _vp, _i, _i, _i, _i, _i, _i, _i, _d, _i, _vp, _vp], _i),
     'yb_svd_shift_prefill': ([_vp, _vp, _i, _i, _vp, _vp], _i),
     'yb_svd_finalize': ([_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp, _vp, _vp], _i),
     'yb_svd_adjoint_core': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),

@@ -600,8 +600,11 @@ class SvdPlan:
     grouped-GEMM plans of the Newton-Schulz orthonormalisation and of X = W X_0."""
 
     def __init__(self, blocks, pair_items, max_rounds, max_k, nominal_flops, n64, n32, w_range, gram, ns, xform,
-                 rows_per_super=0, super_items=None, super_rounds=0, lmax=0, qr=False, qfin_u=None, qfin_v=None):
+                 rows_per_super=0, super_items=None, super_rounds=0, lmax=0, qr=False, qfin_u=None, qfin_v=None,
+                 rows_per_super64=0, super_items64=None, super_rounds64=0):
         self.blocks = blocks
+        self.rows_per_super64 = rows_per_super64  # blocked FP64 phase (0: one pair per warp)
+        self.super_items64, self.super_rounds64 = super_items64, super_rounds64
         self.qr = qr            # QR-preconditioned: Jacobi on R's rows, then U or Vh by qfin_u / qfin_v
         self.qfin_u, self.qfin_v = qfin_u, qfin_v
         self.pair_items = pair_items
@@ -620,6 +623,7 @@ class SvdPlan:
 
 
 SVD_SMEM_BYTES = 220 * 1024  # shared memory a blocked-Jacobi CTA may take (GB300: 227 KB per CTA)
+SVD_ROWS_PER_SUPER64 = 4     # super-vector height of the blocked FP64 phase
 
 
 def svd_rows_per_super(lmax, choices=(16, 8, 4), elem_bytes=4):
@@ -694,7 +698,9 @@ def svd_plan(meta, rows_per_super=None, cplx=False, qr=False):
         lmax = max((lj(k, L) for *_, k, L in sel), default=0)
         n64 = xs + 3 * ws + (2 * zs + sum(k for *_, k, L in sel) + ws if qr else 0)
         br = svd_rows_per_super(lmax, elem_bytes=8 if cplx else 4) if rows_per_super is None else rows_per_super
-        supers, super_rounds = [], 0
+        # FP64 phase: 4-row super-vectors (8 rows per CTA) keep every SM busy on few blocks
+        br64 = svd_rows_per_super(lmax, choices=(SVD_ROWS_PER_SUPER64,), elem_bytes=16 if cplx else 8)
+        supers, super_rounds, supers64, super_rounds64 = [], 0, [], 0
         for bi, (*_, k, L) in enumerate(sel):
             if br:
                 ns_ = -(-k // br)
@@ -702,12 +708,19 @@ def svd_plan(meta, rows_per_super=None, cplx=False, qr=False):
                 recs[bi][15] = ns_
                 supers.extend((bi, p) for p in range(ns_ // 2))
                 super_rounds = max(super_rounds, ns_ - 1)
+            if br64:
+                ns_ = -(-k // br64)
+                ns_ += ns_ % 2
+                recs[bi][23] = ns_
+                supers64.extend((bi, p) for p in range(ns_ // 2))
+                super_rounds64 = max(super_rounds64, ns_ - 1)
         blocks = np.stack(recs) if recs else np.zeros((0, SVD_REC), dtype=np.int64)
         items = np.array(pairs, dtype=np.int32).reshape(-1, 2)
         return SvdPlan(blocks, items, max_rounds, max_k, fl, n64, xs + ws, (w0, t0, n0, ws),
                        _pack_gemm(gram), _pack_gemm(ns), _pack_gemm(xf),
                        br, np.array(supers, dtype=np.int32).reshape(-1, 2), super_rounds, lmax,
-                       qr, _pack_gemm(qfu) if qr else None, _pack_gemm(qfv) if qr else None)
+                       qr, _pack_gemm(qfu) if qr else None, _pack_gemm(qfv) if qr else None,
+                       br64, np.array(supers64, dtype=np.int32).reshape(-1, 2), super_rounds64)
     return CACHE.get((meta,), ('svd', rows_per_super, cplx, qr), build)
 
 

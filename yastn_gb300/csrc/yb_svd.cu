@@ -36,7 +36,7 @@ constexpr long long kSpinLimit = 1ll << 22;
 
 // record fields
 enum { R_A = 0, R_M, R_N, R_U, R_S, R_V, R_X, R_W, R_P, R_K, R_L, R_NP, R_T, R_X32, R_W32, R_NSUP,
-       R_QR, R_LQ, R_Z, R_VQ, R_TAU, R_RR, R_WS };
+       R_QR, R_LQ, R_Z, R_VQ, R_TAU, R_RR, R_WS, R_NSUP64 };
 // per-block state (int64): [0] max |cos| of the sweep in progress (double bits),
 // [1] converged flag, [2] sweeps run in the current phase, [3] largest |cos| of the last sweep,
 // [4], [5] squared row norms (double bits) at or below which a row is rounding noise in the
@@ -542,7 +542,7 @@ __global__ void __launch_bounds__(BR * 32) svd_block_sweeps_kernel(T* __restrict
         int64_t* st = state + (int64_t)b * ST_REC;
         if (((volatile int64_t*)st)[ST_CONV]) continue;
         const int64_t* r = blocks + (int64_t)b * YB_SVD_REC;
-        const int64_t k = r[R_K], L = r[R_L], NS = r[R_NSUP];
+        const int64_t k = r[R_K], L = r[R_L], NS = r[sizeof(R) == 4 ? R_NSUP : R_NSUP64];
         if (round >= NS - 1) continue;
         int64_t P, Q;
         if (pi == 0) { P = NS - 1; Q = round; }
@@ -588,7 +588,7 @@ __global__ void __launch_bounds__(BR * 32) svd_block_sweeps_kernel(T* __restrict
               }
               R c = 0, s = 0;
               T u = Num<T>::one();
-              const R thr2 = (R)__longlong_as_double((long long)st[ST_THR32]);
+              const R thr2 = (R)__longlong_as_double((long long)st[sizeof(R) == 4 ? ST_THR32 : ST_THR64]);
               if (Rotation<T>::get(al_, be_, ga_, L, lane, st + ST_MAXCOS, c, s, u, thr2)) {
                 for (int64_t l = lane; l < L; l += 32) {
                   T a = xp[l], b = xq[l];
@@ -774,11 +774,41 @@ __device__ __forceinline__ void qr_apply(T* __restrict__ x, const T* __restrict_
   __syncwarp();
 }
 
-// One cooperative launch: groups of `group` CTAs factor one block at a time (group barriers
-// between Householder steps), write R's rows (FP64, RR) and the FP32 Jacobi start
-// X32 = scale R, W32 = I, keep the reflectors (VQ, tau), and form Q^T in Z. Row c of Z is
+// Waits (lane 0 polls, bounded) until *flag >= target; on timeout raises *err and returns
+// (the caller carries on with whatever it reads: the host sees the error word and fails).
+__device__ __forceinline__ void qr_wait(const unsigned long long* flag, unsigned long long target,
+                                        unsigned long long* err, int lane) {
+  if (lane == 0) {
+    long long spins = 0;
+    while (*(volatile const unsigned long long*)flag < target) {
+      __nanosleep(32);
+      if (++spins > kSpinLimit) {
+        atomicExch(err, 1ull);
+        break;
+      }
+    }
+    __threadfence();
+  }
+  __syncwarp();
+}
+
+__device__ __forceinline__ void qr_publish(unsigned long long* flag, unsigned long long value, int lane) {
+  __syncwarp();
+  if (lane == 0) {
+    __threadfence();
+    atomicMax(flag, value);
+  }
+}
+
+// One cooperative launch: groups of `group` CTAs factor one block at a time. Row c of Z is
 // handled by warp c mod (8 group) of the group throughout, so a row is only ever rewritten by
-// the warp that reads it; the reflector of row j+1 is made by its warp right after its update.
+// the warp that reads it, and the only exchange is each reflector: the warp owning row j+1
+// updates it first in step j, makes reflector j+1 and publishes it through the block's
+// ready counter (flags[b] = number of reflectors published); every warp waits for reflector j
+// before applying it, so warps run ahead of each other as far as the data allows. Then (one
+// group barrier) R's rows, the FP32 start X32 = scale R, W32 = I and the reflectors are
+// written; after a second barrier every warp forms its own columns of Q independently
+// (Q e_c = H_0 ... H_c e_c), in place of its rows of Z.
 template <typename T, typename T32>
 __global__ void __launch_bounds__(kThreads) svd_qr_kernel(T* __restrict__ work, T32* __restrict__ work32,
                                                           const int64_t* __restrict__ blocks, int n_blocks,
@@ -787,7 +817,8 @@ __global__ void __launch_bounds__(kThreads) svd_qr_kernel(T* __restrict__ work, 
   const int g = blockIdx.x / group, rank = blockIdx.x % group;
   const int n_groups = gridDim.x / group;
   if (g >= n_groups) return;
-  unsigned long long* ctrl = qctrl + (int64_t)g * C_REC;
+  unsigned long long* flags = qctrl;  // [n_blocks ready counters][C_REC words per group]
+  unsigned long long* ctrl = qctrl + n_blocks + (int64_t)g * C_REC;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t gw = (int64_t)rank * kWarps + warp, nwg = (int64_t)group * kWarps;
   const int64_t gt = (int64_t)rank * kThreads + threadIdx.x, ngt = (int64_t)group * kThreads;
@@ -801,21 +832,28 @@ __global__ void __launch_bounds__(kThreads) svd_qr_kernel(T* __restrict__ work, 
     T* RR = work + r[R_RR];
     T32* X32 = work32 + r[R_X32];
     T32* W32 = work32 + r[R_W32];
+    unsigned long long* ready = flags + b;
     const double sc = scale[b];
     // factorisation
-    if (gw == 0) qr_reflector<T>(Z, tau, 0, L, lane);
-    if (!grid_barrier(ctrl, group)) return;
+    if (gw == 0) {
+      qr_reflector<T>(Z, tau, 0, L, lane);
+      qr_publish(ready, 1ull, lane);
+    }
     for (int64_t j = 0; j < k; ++j) {
-      const T* vrow = Z + j * L;
-      T t = ldcg_t(tau + j);
-      t = Num<T>::conj(t);  // M <- H^H M
       const int64_t first = j + 1 + ((gw - (j + 1)) % nwg + nwg) % nwg;
+      if (first >= k) break;  // no rows of this warp below row j: none below any later row either
+      qr_wait(ready, (unsigned long long)(j + 1), ctrl + C_ERR, lane);
+      const T* vrow = Z + j * L;
+      const T t = Num<T>::conj(ldcg_t(tau + j));  // M <- H^H M
       for (int64_t c = first; c < k; c += nwg) {
         qr_apply<T>(Z + c * L, vrow, t, j, L, lane);
-        if (c == j + 1) qr_reflector<T>(Z + c * L, tau, j + 1, L, lane);
+        if (c == j + 1) {
+          qr_reflector<T>(Z + c * L, tau, j + 1, L, lane);
+          qr_publish(ready, (unsigned long long)(j + 2), lane);
+        }
       }
-      if (!grid_barrier(ctrl, group)) return;
     }
+    if (!grid_barrier(ctrl, group)) return;
     // R rows, the FP32 start, the reflectors
     for (int64_t e = gt; e < k * k; e += ngt) {
       const int64_t i = e / k, c = e - i * k;
@@ -829,19 +867,14 @@ __global__ void __launch_bounds__(kThreads) svd_qr_kernel(T* __restrict__ work, 
       V[e] = (l > j) ? ldcg_t(Z + e) : Num<T>::zero();
     }
     if (!grid_barrier(ctrl, group)) return;
-    for (int64_t e = gt; e < k * L; e += ngt) {
-      const int64_t i = e / L, l = e - i * L;
-      Z[e] = (i == l) ? Num<T>::one() : Num<T>::zero();
+    // Q's columns: row c of Z becomes (H_0 ... H_c e_c)^T
+    for (int64_t c = gw; c < k; c += nwg) {
+      T* x = Z + c * L;
+      for (int64_t l = lane; l < L; l += 32) x[l] = (l == c) ? Num<T>::one() : Num<T>::zero();
+      __syncwarp();
+      for (int64_t j = c; j >= 0; --j) qr_apply<T>(x, V + j * L, ldcg_t(tau + j), j, L, lane);
     }
     if (!grid_barrier(ctrl, group)) return;
-    // Q^T = (H_0 ... H_{k-1} [I; 0])^T, backward
-    for (int64_t j = k - 1; j >= 0; --j) {
-      const T* vrow = V + j * L;
-      const T t = ldcg_t(tau + j);
-      const int64_t first = j + ((gw - j) % nwg + nwg) % nwg;
-      for (int64_t c = first; c < k; c += nwg) qr_apply<T>(Z + c * L, vrow, t, j, L, lane);
-      if (!grid_barrier(ctrl, group)) return;
-    }
   }
 }
 
@@ -1123,9 +1156,12 @@ template <typename T>
 int block_sweeps_t(T* w, const int64_t* blocks, int n_blocks, const int32_t* super_items, int n_items,
                           int max_rounds, int rows_per_super, int max_sweeps, int inner_sweeps, double tol_stop,
                           int lmax, int64_t* state, cudaStream_t s) {
+  constexpr bool fp64 = sizeof(typename Num<T>::R) == 8;
   switch (rows_per_super) {
-    case 16: return yb::launch_block_sweeps<T, 16>(w, blocks, n_blocks, super_items, n_items, max_rounds, max_sweeps,
-                                                  inner_sweeps, tol_stop, lmax, state, s);
+    case 16:
+      if constexpr (fp64) return YB_ERR_INVALID;
+      else return yb::launch_block_sweeps<T, 16>(w, blocks, n_blocks, super_items, n_items, max_rounds, max_sweeps,
+                                                 inner_sweeps, tol_stop, lmax, state, s);
     case 8: return yb::launch_block_sweeps<T, 8>(w, blocks, n_blocks, super_items, n_items, max_rounds, max_sweeps,
                                                 inner_sweeps, tol_stop, lmax, state, s);
     case 4: return yb::launch_block_sweeps<T, 4>(w, blocks, n_blocks, super_items, n_items, max_rounds, max_sweeps,
@@ -1145,14 +1181,14 @@ int qr_t(const void* a, void* work, void* work32, const int64_t* blocks, int n_b
   if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
   const int capacity = sms * (per_sm < 1 ? 1 : per_sm);
   int group = capacity / n_blocks;
-  group = group < 1 ? 1 : (group > 16 ? 16 : group);
+  group = group < 1 ? 1 : (group > 64 ? 64 : group);
   int n_groups = capacity / group;
   if (n_groups > n_blocks) n_groups = n_blocks;
-  if ((int64_t)n_groups * yb::C_REC > qctrl_words) n_groups = qctrl_words / yb::C_REC;
+  if ((int64_t)n_groups * yb::C_REC + n_blocks > qctrl_words) n_groups = (qctrl_words - n_blocks) / yb::C_REC;
   if (n_groups < 1) return YB_ERR_INVALID;
   yb::block_fro_kernel<T><<<n_blocks, 256, 0, s>>>((const T*)a, blocks, nullptr, scale, state);
   yb::svd_qr_load_kernel<T><<<dim3(64, (unsigned)n_blocks), 256, 0, s>>>((const T*)a, (T*)work, blocks);
-  e = cudaMemsetAsync(qctrl, 0, sizeof(int64_t) * (size_t)n_groups * yb::C_REC, s);
+  e = cudaMemsetAsync(qctrl, 0, sizeof(int64_t) * ((size_t)n_groups * yb::C_REC + n_blocks), s);
   if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
   T* w = (T*)work;
   T32* w32 = (T32*)work32;
@@ -1237,11 +1273,22 @@ int yb_svd_sweeps(void* work, const int64_t* blocks, int n_blocks, const int32_t
 }
 
 int yb_svd_block_sweeps(void* work32, const int64_t* blocks, int n_blocks, const int32_t* super_items,
-                        int n_items, int max_rounds, int rows_per_super, int dtype, int max_sweeps,
+                        int n_items, int max_rounds, int rows_per_super, int precision, int dtype, int max_sweeps,
                         int inner_sweeps, double tol_stop, int lmax, int64_t* state, void* stream) {
   if (n_blocks == 0 || n_items == 0 || max_sweeps <= 0) return YB_OK;
   if (!work32 || !blocks || !super_items || !state || lmax <= 0 || inner_sweeps <= 0) return YB_ERR_INVALID;
+  if (precision != 32 && precision != 64) return YB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
+  if (precision == 64) {
+    if (rows_per_super != 4 && rows_per_super != 8) return YB_ERR_INVALID;
+    if (dtype == YB_F64)
+      return yb::block_sweeps_t<double>((double*)work32, blocks, n_blocks, super_items, n_items, max_rounds,
+                                        rows_per_super, max_sweeps, inner_sweeps, tol_stop, lmax, state, s);
+    if (dtype == YB_C128)
+      return yb::block_sweeps_t<double2>((double2*)work32, blocks, n_blocks, super_items, n_items, max_rounds,
+                                         rows_per_super, max_sweeps, inner_sweeps, tol_stop, lmax, state, s);
+    return YB_ERR_INVALID;
+  }
   if (dtype == YB_F64)
     return yb::block_sweeps_t<float>((float*)work32, blocks, n_blocks, super_items, n_items, max_rounds, rows_per_super,
                                  max_sweeps, inner_sweeps, tol_stop, lmax, state, s);

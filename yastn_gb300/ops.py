@@ -296,10 +296,12 @@ def transpose_dot_sum_backward(C_b, A, B, meta_dot, Areshape, Breshape, Aorder, 
 
 MAX_SWEEPS32 = 40
 TOL_STOP32 = 1.0e-4   # FP32 phase ends after a sweep whose largest rotation |cos| is below this
-TOL_STOP64 = 1.0e-8   # FP64 phase: idem; Jacobi converges quadratically, so the residual |cos|
-                      # after such a sweep is ~1e-16 for separated singular values
+TOL_STOP64 = 1.0e-8   # FP64 phase: idem; Jacobi converges quadratically (a sweep that starts at
+                      # max |cos| c leaves ~c^2), so the residual after such a sweep is ~1e-16
+TOL_STOP64_QR = 1.0e-7  # the same for the QR-preconditioned SVD (separated, graded rows: ~1e-14 left)
 INNER_SWEEPS32 = 1    # blocked FP32 phase: Jacobi sweeps among the rows of a super pair per visit
 BLOCKED_FP32 = [True]  # FP32 phase on super-vectors in shared memory (False: one pair per warp)
+BLOCKED_FP64 = [True]  # FP64 phase likewise, on 4-row super-vectors (False: one pair per warp)
 ROWS_PER_SUPER = [None]  # super-vector height (None: largest of 16, 8, 4 that fits)
 NS_STEPS = 2          # Newton-Schulz steps: non-orthogonality ~1e-6 -> 1e-12 -> ~eps
 SVD_QR = [True]       # svd: Jacobi on the rows of R of a Householder QR (few FP64 sweeps on graded spectra)
@@ -335,7 +337,7 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
     st = _stream()
     qctrl = None
     if plan.qr:
-        qctrl = torch.empty(4 * min(nb, 4096), dtype=torch.int64, device=dev)
+        qctrl = torch.zeros(nb + 4 * min(nb, 4096), dtype=torch.int64, device=dev)
         N.call('yb_svd_qr', _ptr(data), _ptr(w64), _ptr(w32), _ptr(dblocks), nb, code, _ptr(state), _ptr(aux[:nb]),
                _ptr(qctrl), qctrl.numel(), st, launches=4)
     else:
@@ -344,13 +346,13 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
     if plan.rows_per_super and BLOCKED_FP32[0]:
         (dsup,) = _dev(plan, 'svd_super', (plan.super_items,), dev)
         N.call('yb_svd_block_sweeps', _ptr(w32), _ptr(dblocks), nb, _ptr(dsup), len(plan.super_items),
-               plan.super_rounds, plan.rows_per_super, code, MAX_SWEEPS32, INNER_SWEEPS32, TOL_STOP32, plan.lmax,
-               _ptr(state), st)
+               plan.super_rounds, plan.rows_per_super, 32, code, MAX_SWEEPS32, INNER_SWEEPS32, TOL_STOP32,
+               plan.lmax, _ptr(state), st)
     else:
         N.call('yb_svd_sweeps', _ptr(w32), _ptr(dblocks), nb, _ptr(dpairs), len(plan.pair_items), plan.max_rounds,
                32, code, MAX_SWEEPS32, TOL_STOP32, _ptr(state), st)
     _svd_state_check(state, nb, 'FP32', False)
-    if qctrl is not None and bool(qctrl[2::4].any()):
+    if qctrl is not None and bool(qctrl[nb + 2::4].any()):
         raise RuntimeError("yastn_gb300 svd: QR group barrier timed out")
     N.call('yb_svd_widen', _ptr(w32), _ptr(w64), _ptr(dblocks), nb, code, _ptr(state), st)
     w0, t0, n0, ws = plan.w_range
@@ -367,8 +369,15 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
         run_gemm(plan.xform, w64, data, w64, beta=1.0)
     else:
         run_gemm(plan.xform, w64, data, w64)
-    N.call('yb_svd_sweeps', _ptr(w64), _ptr(dblocks), nb, _ptr(dpairs), len(plan.pair_items), plan.max_rounds, 64,
-           code, max_sweeps, TOL_STOP64, _ptr(state), st)
+    tol64 = TOL_STOP64_QR if plan.qr else TOL_STOP64
+    if plan.rows_per_super64 and BLOCKED_FP64[0]:
+        (dsup64,) = _dev(plan, 'svd_super64', (plan.super_items64,), dev)
+        N.call('yb_svd_block_sweeps', _ptr(w64), _ptr(dblocks), nb, _ptr(dsup64), len(plan.super_items64),
+               plan.super_rounds64, plan.rows_per_super64, 64, code, max_sweeps, 1, tol64, plan.lmax,
+               _ptr(state), st)
+    else:
+        N.call('yb_svd_sweeps', _ptr(w64), _ptr(dblocks), nb, _ptr(dpairs), len(plan.pair_items), plan.max_rounds,
+               64, code, max_sweeps, tol64, _ptr(state), st)
     _svd_state_check(state, nb, 'FP64', True)
     N.call('yb_svd_finalize', _ptr(w64), _ptr(U), _ptr(S), _vp(V.data_ptr() if V is not None else 0), _ptr(dblocks),
            nb, code, plan.max_k, mode, sp, _ptr(state), st)
