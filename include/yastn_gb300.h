@@ -102,7 +102,8 @@ int yb_block_copy(const void* src, void* dst, int unit_bytes,
  *   A_t[i,l] = a[a_off + i*a_rs + l*a_cs], B_t[l,j] = b[b_off + l*b_rs + j*b_cs].
  * tiles: n_tiles records of 4 int32: (output, tile row, tile col, kind), ordered by the
  *   host (largest work first). kind 0: a 64x64 tile; kind 1: a skinny tile covering all
- *   m <= 8 rows and columns [1024*col, 1024*col + 1024) (tile row must be 0).
+ *   m <= 16 rows and columns [w*col, w*col + w) with w = 1024 for m <= 8, 256 above (tile
+ *   row 0; the host's plans use skinny tiles for m <= 8).
  * dtype: YB_F64 or YB_C128 (alpha, beta are real).
  * Replaces dot (one term per output), transpose_dot_sum after the merge of its operands,
  * and the adjoint products A_b += C_b B^H, B_b += A^H C_b (terms grouped by operand block).

@@ -100,8 +100,10 @@ def _run_outs(outs, terms, tiles, a, b, c, alpha, beta):
         c_off, m, n, ldc, t0, t1 = (int(x) for x in o[:6])
         if m == 0 or n == 0:
             continue
-        if m <= 8 and n > 64:  # skinny tiles: all rows x 1024 columns
-            want = {(0, j, 1) for j in range((n + 1023) // 1024)}
+        if any(kd == 1 for _, _, kd in seen.get(oi, ())):  # skinny: all rows x 1024 columns (256 above 8 rows)
+            assert m <= 16, "skinny tiles take at most 16 rows"
+            w = P.skinny_cols(m)
+            want = {(0, j, 1) for j in range((n + w - 1) // w)}
         else:
             want = {(i, j, 0) for i in range((m + 63) // 64) for j in range((n + 63) // 64)}
         assert seen.get(oi, set()) == want, "tiles do not cover the output"

@@ -115,6 +115,35 @@ def test_split_k_dots(cplx, cuda_device):
     assert rel(host(Ab), Ar) <= TOL and rel(host(Bb), Br) <= TOL
 
 
+@pytest.mark.parametrize('cplx', [False, True])
+def test_skinny_tile_kinds(cplx, cuda_device):
+    """Outputs with 1..16 rows (skinny tiles up to the kernel's bound of 16) and with 1..16
+    columns (64x64 tiles; their adjoints make skinny outputs) against the oracle, forward
+    and adjoint."""
+    from yastn_gb300 import _plans as P
+    rng = np.random.default_rng(13)
+    shapes = [(r, 37, 700) for r in range(1, 17)] + [(700, 29, c) for c in range(1, 17)] + \
+             [(2592, 18, 9), (9, 9, 9), (64, 64, 64)]
+    meta, oa, ob, oc = [], 0, 0, 0
+    for m, k, n in shapes:
+        meta.append(((oc, oc + m * n), (m, n), (oa, oa + m * k), (m, k), (ob, ob + k * n), (k, n)))
+        oa += m * k; ob += k * n; oc += m * n
+    meta = tuple(meta)
+    f = lambda n: rng.normal(size=n) + (1j * rng.normal(size=n) if cplx else 0)
+    A, B, Cb = f(oa), f(ob), f(oc)
+    saved = P.SKINNY_ROWS
+    P.SKINNY_ROWS = 16
+    try:
+        got = host(ops.dot(dev(A), dev(B), meta, oc))
+        Ab, Bb = ops.dot_backward(dev(Cb), dev(A), dev(B), meta)
+    finally:
+        P.SKINNY_ROWS = saved
+        P.CACHE.by_id.clear(); P.CACHE.by_val.clear()
+    assert rel(got, oracle.dot(A, B, meta, oc)) <= TOL
+    Ar, Br = oracle.dot_backward(Cb, A, B, meta)
+    assert rel(host(Ab), Ar) <= TOL and rel(host(Bb), Br) <= TOL
+
+
 def test_cfg1_full_size_dot(cuda_device):
     """The benchmark's 13 sector GEMMs (n up to 822, 3.25 GFLOP) vs numpy BLAS."""
     tr = load_trace('cfg1')

@@ -134,6 +134,37 @@ def test_split_k_plans_cover_and_reproduce(shapes):
     assert np.abs(Bb - Bb_r).max() <= 1e-11 * np.abs(Bb_r).max()
 
 
+def test_skinny_tile_kinds_cover_and_reproduce():
+    """Outputs with at most 16 rows (skinny tiles, 1024 or 256 columns wide) beside 64x64
+    tiles: coverage and values, forward and adjoint, real and complex."""
+    shapes = [(3, 40, 300), (12, 20, 700), (16, 9, 2000), (500, 30, 5), (2592, 18, 9), (70, 7, 13),
+              (9, 9, 9), (64, 64, 64)]
+    meta, oa, ob, oc = _meta_dot(shapes)
+    saved = P.SKINNY_ROWS
+    P.SKINNY_ROWS = 16  # the kernel's bound (the default plans stop at 8 rows)
+    try:
+        plan = P.dot_plan(meta)
+    finally:
+        P.SKINNY_ROWS = saved
+    P.CACHE.by_id.clear(); P.CACHE.by_val.clear()
+    kinds = set(int(t[3]) for t in plan.tiles)
+    assert kinds == {0, 1}
+    rng = np.random.default_rng(8)
+    for cplx in (False, True):
+        f = lambda n: rng.normal(size=n) + (1j * rng.normal(size=n) if cplx else 0)
+        A, B, Cb = f(oa), f(ob), f(oc)
+        out = PI.run_gemm(plan, A, B, np.zeros(oc, dtype=A.dtype))
+        ref = oracle.dot(A, B, meta, oc)
+        assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
+        pa, pb = P.dot_backward_plans(meta)
+        Ab = PI.run_gemm(pa, Cb, B, np.zeros(oa, dtype=A.dtype))
+        Bb = PI.run_gemm(pb, A, Cb, np.zeros(ob, dtype=A.dtype))
+        Ab_r, Bb_r = oracle.dot_backward(Cb, A, B, meta)
+        assert np.abs(Ab - Ab_r).max() <= 1e-12 * np.abs(Ab_r).max()
+        assert np.abs(Bb - Bb_r).max() <= 1e-12 * np.abs(Bb_r).max()
+    P.CACHE.by_id.clear(); P.CACHE.by_val.clear()
+
+
 def test_split_k_not_used_when_tiles_fill_the_gpu():
     meta, *_ = _meta_dot([(64, 4096, 64)] * 400)
     assert P.dot_plan(meta).split is None

@@ -30,7 +30,7 @@ class PlanError(ValueError):
 class PlanCache:
     """LRU cache keyed by metadata identity with a by-value fallback."""
 
-    def __init__(self, maxsize=2048):
+    def __init__(self, maxsize=32768):
         self.by_id = OrderedDict()
         self.by_val = OrderedDict()
         self.maxsize = maxsize
@@ -314,7 +314,19 @@ class SplitK:
         self.red, self.tasks, self.ws = red, tasks, ws
 
 
-SKINNY_ROWS, SKINNY_COLS = 8, 1024
+SKINNY_ROWS, SKINNY_COLS = 8, 1024  # skinny tiles: up to 8 rows (the kernel takes 16), 1024 columns
+                                    # (256 above 8 rows)
+
+
+def skinny_cols(rows):
+    return SKINNY_COLS if rows <= 8 else SKINNY_COLS // 4
+
+
+def tile_kind(m, n):
+    """0: 64x64 tiles; 1: skinny tiles over the m <= 16 rows."""
+    if m <= SKINNY_ROWS and n > GEMM_TILE:
+        return 1
+    return 0
 GEMM_RED_REC, GEMM_RED_ITEM = 8, 1024
 SPLITK_MAX_TILES = 304   # plans with this many tiles (2 per SM) are not split
 SPLITK_UNITS = 608       # tiles x chunks aimed at after splitting (4 per SM)
@@ -322,16 +334,18 @@ SPLITK_MIN_K = 256       # shortest K chunk
 
 
 def _tiles_for(outs, terms):
-    """Tiles (output, tile row, tile col, kind): kind 0 = 64x64, kind 1 = skinny (all m <= 8
-    rows x 1024 columns), ordered by descending work so long tiles start first."""
+    """Tiles (output, tile row, tile col, kind): kind 0 = 64x64, kind 1 = skinny (all m <= 16
+    rows x 1024 columns, 256 above 8 rows), ordered by descending work so long tiles start
+    first."""
     tiles = []
     for oi, o in enumerate(outs):
         m, n = int(o[1]), int(o[2])
         if m == 0 or n == 0:
             continue
         kk = int(sum(terms[t][2] for t in range(o[4], o[5])))
-        if m <= SKINNY_ROWS and n > GEMM_TILE:
-            for tc in range((n + SKINNY_COLS - 1) // SKINNY_COLS):
+        if tile_kind(m, n):
+            w = skinny_cols(m)
+            for tc in range((n + w - 1) // w):
                 tiles.append((kk * m * 16, oi, 0, tc, 1))
             continue
         for tr in range((m + GEMM_TILE - 1) // GEMM_TILE):
@@ -345,8 +359,8 @@ def _tiles_for(outs, terms):
 def _n_tiles(m, n):
     if m == 0 or n == 0:
         return 0
-    if m <= SKINNY_ROWS and n > GEMM_TILE:
-        return (n + SKINNY_COLS - 1) // SKINNY_COLS
+    if tile_kind(m, n):
+        return (n + skinny_cols(m) - 1) // skinny_cols(m)
     return ((m + GEMM_TILE - 1) // GEMM_TILE) * ((n + GEMM_TILE - 1) // GEMM_TILE)
 
 
@@ -483,6 +497,7 @@ class OzakiPlan:
 OZAKI_TC_M, OZAKI_TC_N = 128, 64  # output tile of the tcgen05 emulated GEMM
 OZAKI_TC_CLUSTER = 1               # CTAs per cluster sharing A digit tiles (1, 2 or 4)
 OZAKI_MIN_DIM = 16  # sector GEMMs contracting fewer indices than this stay on the native FP64 kernel
+OZAKI_SKINNY_ROWS = 8  # sector GEMMs with at most this many rows (and more than 64 columns) too
 
 
 def _tiled_recs(recs, s, th):
@@ -516,7 +531,7 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
         for slc, Dc, sla, Da, slb, Db in meta_dot:
             m, K = Da
             n = Db[1]
-            if K < OZAKI_MIN_DIM or (m <= SKINNY_ROWS and n > GEMM_TILE):
+            if K < OZAKI_MIN_DIM or (m <= OZAKI_SKINNY_ROWS and n > GEMM_TILE):
                 # short contractions and skinny outputs stay on the native FP64 kernel
                 small.append((slc[0], m, n, n, [(sla[0], slb[0], K, K, 1, n, 1, 0)]))
                 continue

@@ -3,9 +3,11 @@
 //   C_o = alpha * sum_{t in terms(o)} op(A_t) op(B_t) + beta * C_o
 //
 // One launch covers every 64x64 output tile of every sector; the host orders tiles
-// largest-K first so that the long tiles start early. Outputs with at most 8 rows (the
+// largest-K first so that the long tiles start early. Outputs with few rows (the
 // contractions with a small MPO block, for instance) use "skinny" tiles instead: all rows x
-// 1024 columns, four columns per thread, op(A) staged in shared memory. On GB300 FP64 arithmetic runs at
+// 1024 columns, four columns per thread, op(A) staged in shared memory (the kernel takes up
+// to 16 rows, above 8 with 256 columns, one per thread; the host sends outputs of up to 8
+// rows, which measured faster than 64x64 tiles, while 9..16 rows did not). On GB300 FP64 arithmetic runs at
 // about 1.2 TFLOP/s on the DFMA pipe (the DMMA m8n8k4 tensor path measured slower),
 // so a register-tiled DFMA kernel with shared-memory staging is FP64-bound: each thread
 // owns a 4x4 sub-tile and issues 16 independent FMAs per staged k.
@@ -18,10 +20,7 @@ constexpr int kTile = YB_GEMM_TILE;  // 64
 constexpr int kK = 16;
 constexpr int kThreads = 256;
 constexpr int kPad = 2;
-constexpr int kSkinnyRows = 8;   // rows of a skinny tile (outputs with m <= 8)
-constexpr int kSkinnyK = 64;     // K-chunk of op(A) staged for a skinny tile (64 x 8 <= 16 x 66)
-constexpr int kSkinnyCpt = 4;    // columns per thread of a skinny tile
-constexpr int kSkinnyCols = kThreads * kSkinnyCpt;  // 1024 = YB_GEMM_SKINNY_COLS
+constexpr int kSkinnyK = 64;     // K-chunk of op(A) staged for a skinny tile (64 x 16 <= 16 x 66)
 
 struct Real {
   using T = double;
@@ -46,69 +45,96 @@ struct Cplx {
   __device__ static T add(T a, T b) { return make_double2(a.x + b.x, a.y + b.y); }
 };
 
-// Skinny tile: C (M x kSkinnyCols slice) = alpha sum_t op(A_t) op(B_t) + beta C for M <= 8.
-// op(A) is staged in shared memory K-chunk by K-chunk ([kSkinnyK][8], broadcast reads);
-// each thread owns kSkinnyCpt columns, kThreads apart, so B loads and C stores coalesce.
-template <class F, int M>
+// Skinny tile: C (M x kThreads*CPT slice) = alpha sum_t op(A_t) op(B_t) + beta C for at
+// most M rows (the block's mr <= M rows; M is the compiled bound). op(A) is staged in shared
+// memory K-chunk by K-chunk ([kSkinnyK][M], broadcast reads); each thread owns CPT columns,
+// kThreads apart, so B loads and C stores coalesce.
+template <class F, int M, int CPT>
 __device__ __forceinline__ void skinny_tile(const typename F::T* __restrict__ A, const typename F::T* __restrict__ B,
                                             typename F::T* __restrict__ C, const int64_t* __restrict__ orec,
                                             const int64_t* __restrict__ terms, int tcol, double alpha, double beta,
                                             typename F::T* Ak) {
   using T = typename F::T;
-  const int64_t c_off = orec[0], n = orec[2], ldc = orec[3], t0 = orec[4], t1 = orec[5];
-  const int64_t j0 = (int64_t)tcol * kSkinnyCols + threadIdx.x;
-  T acc[kSkinnyCpt][M];
+  const int64_t c_off = orec[0], ldc = orec[3], t0 = orec[4], t1 = orec[5];
+  const int64_t mr = orec[1], nc = orec[2];
+  const int64_t j0 = (int64_t)tcol * (kThreads * CPT) + threadIdx.x;
+  T acc[CPT][M];
 #pragma unroll
-  for (int u = 0; u < kSkinnyCpt; ++u)
+  for (int u = 0; u < CPT; ++u)
 #pragma unroll
     for (int i = 0; i < M; ++i) acc[u][i] = F::zero();
   for (int64_t t = t0; t < t1; ++t) {
     const int64_t* trec = terms + t * YB_GEMM_TERM_REC;
-    const int64_t a_off = trec[0], b_off = trec[1], K = trec[2];
-    const int64_t a_rs = trec[3], a_cs = trec[4], b_rs = trec[5], b_cs = trec[6];
+    const int64_t K = trec[2];
+    const T* La = A + trec[0];
+    const T* Ra = B + trec[1];
+    const int64_t l_is = trec[3], l_ls = trec[4], r_ls = trec[5], r_js = trec[6];
     const int flags = (int)trec[7];
+    const bool conjL = flags & 1, conjR = flags & 2;
     for (int64_t k0 = 0; k0 < K; k0 += kSkinnyK) {
       __syncthreads();
       for (int e = threadIdx.x; e < kSkinnyK * M; e += kThreads) {
         const int i = e % M, l = e / M;
         T v = F::zero();
-        if (k0 + l < K) {
-          v = A[a_off + i * a_rs + (k0 + l) * a_cs];
-          if (flags & 1) v = F::conj(v);
+        if (k0 + l < K && i < mr) {
+          v = La[i * l_is + (k0 + l) * l_ls];
+          if (conjL) v = F::conj(v);
         }
         Ak[l * M + i] = v;
       }
       __syncthreads();
       const int64_t kn = min((int64_t)kSkinnyK, K - k0);
-      const T* Bk = B + b_off + k0 * b_rs;
+      const T* Rk = Ra + k0 * r_ls;
       for (int64_t l = 0; l < kn; ++l) {
-        T b[kSkinnyCpt];
+        T b[CPT];
 #pragma unroll
-        for (int u = 0; u < kSkinnyCpt; ++u) {
+        for (int u = 0; u < CPT; ++u) {
           const int64_t j = j0 + u * kThreads;
-          b[u] = (j < n) ? Bk[l * b_rs + j * b_cs] : F::zero();
-          if (flags & 2) b[u] = F::conj(b[u]);
+          b[u] = (j < nc) ? Rk[l * r_ls + j * r_js] : F::zero();
+          if (conjR) b[u] = F::conj(b[u]);
         }
 #pragma unroll
         for (int i = 0; i < M; ++i) {
           const T a = Ak[l * M + i];
 #pragma unroll
-          for (int u = 0; u < kSkinnyCpt; ++u) F::fma(acc[u][i], a, b[u]);
+          for (int u = 0; u < CPT; ++u) F::fma(acc[u][i], a, b[u]);
         }
       }
     }
   }
 #pragma unroll
-  for (int u = 0; u < kSkinnyCpt; ++u) {
+  for (int u = 0; u < CPT; ++u) {
     const int64_t j = j0 + u * kThreads;
-    if (j >= n) continue;
+    if (j >= nc) continue;
 #pragma unroll
     for (int i = 0; i < M; ++i) {
+      if (i >= mr) break;
       T* p = C + c_off + i * ldc + j;
       T v = F::scale(acc[u][i], alpha);
       if (beta != 0.0) v = F::add(v, F::scale(*p, beta));
       *p = v;
     }
+  }
+}
+
+template <class F>
+__device__ __forceinline__ void skinny_dispatch(int64_t mr, const typename F::T* __restrict__ A,
+                                                const typename F::T* __restrict__ B, typename F::T* __restrict__ C,
+                                                const int64_t* __restrict__ orec, const int64_t* __restrict__ terms,
+                                                int tcol, double alpha, double beta, typename F::T* Ak) {
+  // FP64 issue rate, not bandwidth, bounds these tiles: no FMA is spent on padding rows up to 8
+  switch (mr) {
+    case 1: skinny_tile<F, 1, 4>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
+    case 2: skinny_tile<F, 2, 4>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
+    case 3: skinny_tile<F, 3, 4>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
+    case 4: skinny_tile<F, 4, 4>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
+    case 5: skinny_tile<F, 5, 4>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
+    case 6: skinny_tile<F, 6, 4>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
+    case 7: skinny_tile<F, 7, 4>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
+    case 8: skinny_tile<F, 8, 4>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
+    case 9: case 10: case 11: case 12:
+      skinny_tile<F, 12, 1>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
+    default: skinny_tile<F, 16, 1>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
   }
 }
 
@@ -128,21 +154,11 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_kernel(const typename F
   const int64_t* orec = outs + (int64_t)tl.x * YB_GEMM_OUT_REC;
   const int64_t c_off = orec[0], m = orec[1], n = orec[2], ldc = orec[3];
   const int64_t t0 = orec[4], t1 = orec[5];
-  if (tl.w == 1) {
-    // skinny tile: the m <= 8 rows x kSkinnyCols columns, specialised on m so that no FP64
-    // FMA is spent on padding rows (FP64 issue rate, not bandwidth, bounds these tiles)
-    switch (m) {
-      case 1: skinny_tile<F, 1>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]); break;
-      case 2: skinny_tile<F, 2>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]); break;
-      case 3: skinny_tile<F, 3>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]); break;
-      case 4: skinny_tile<F, 4>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]); break;
-      case 5: skinny_tile<F, 5>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]); break;
-      case 6: skinny_tile<F, 6>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]); break;
-      case 7: skinny_tile<F, 7>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]); break;
-      default: skinny_tile<F, 8>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]); break;
-    }
+  if (tl.w == 1) {  // skinny: the m <= 16 rows x 1024 (256) columns
+    skinny_dispatch<F>(m, A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]);
     return;
   }
+
   const int64_t row0 = (int64_t)tl.y * kTile, col0 = (int64_t)tl.z * kTile;
 
   // thread (ty, tx) owns rows 4ty..4ty+3 and columns 4tx..4tx+3; a warp covers 16 rows x 32

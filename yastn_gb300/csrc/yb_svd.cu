@@ -390,6 +390,7 @@ __device__ bool grid_barrier(unsigned long long* ctrl, unsigned nblocks) {
 }
 
 constexpr int kChunk = 8;  // elements per lane per row kept in flight
+constexpr int kLoadBatch = 8;  // independent loads per thread when a CTA stages rows
 
 // Rotates rows (p, q) of X and W by one Jacobi rotation. Loads are issued a chunk at a
 // time (kChunk per lane and row, all before any store of the chunk) so that the L2
@@ -559,11 +560,30 @@ __global__ void __launch_bounds__(BR * 32) svd_block_sweeps_kernel(T* __restrict
           Qs[e] = (e / R2 == e % R2) ? Num<T>::one() : Num<T>::zero();
         if (threadIdx.x == 0) any_rot = 0;
         __syncthreads();
-        for (int64_t e = threadIdx.x; e < (int64_t)R2 * L; e += blockDim.x) {
-          const int i = (int)(e / L);
-          const int64_t l = e - (int64_t)i * L;
-          const int64_t g = grow[i];
-          Xs[(size_t)i * lmax + l] = (g >= 0) ? __ldcg(X + g * L + l) : Num<T>::zero();
+        {
+          // the rows of the pair: kLoadBatch independent L2 loads in flight per thread
+          const unsigned tot = (unsigned)(R2 * L), Lu = (unsigned)L;
+          for (unsigned e0 = threadIdx.x; e0 < tot; e0 += blockDim.x * kLoadBatch) {
+            T v[kLoadBatch];
+#pragma unroll
+            for (int u = 0; u < kLoadBatch; ++u) {
+              const unsigned e = e0 + u * blockDim.x;
+              v[u] = Num<T>::zero();
+              if (e < tot) {
+                const unsigned i = e / Lu, l = e - i * Lu;
+                const int64_t g = grow[i];
+                if (g >= 0) v[u] = __ldcg(X + g * L + l);
+              }
+            }
+#pragma unroll
+            for (int u = 0; u < kLoadBatch; ++u) {
+              const unsigned e = e0 + u * blockDim.x;
+              if (e < tot) {
+                const unsigned i = e / Lu, l = e - i * Lu;
+                Xs[(size_t)i * lmax + l] = v[u];
+              }
+            }
+          }
         }
         __syncthreads();
         for (int inner = 0; inner < inner_sweeps; ++inner) {
@@ -612,9 +632,9 @@ __global__ void __launch_bounds__(BR * 32) svd_block_sweeps_kernel(T* __restrict
           if (!rotated) break;
         }
         if (any_rot) {
-          for (int64_t e = threadIdx.x; e < (int64_t)R2 * L; e += blockDim.x) {
-            const int i = (int)(e / L);
-            const int64_t l = e - (int64_t)i * L;
+          const unsigned tot = (unsigned)(R2 * L), Lu = (unsigned)L;
+          for (unsigned e = threadIdx.x; e < tot; e += blockDim.x) {
+            const unsigned i = e / Lu, l = e - i * Lu;
             const int64_t g = grow[i];
             if (g >= 0) X[g * L + l] = Xs[(size_t)i * lmax + l];
           }

@@ -56,51 +56,55 @@ class CallReplay:
 
     def run(self, backend, device, inputs, constants_dtype=None):
         """Execute the sequence. ``inputs`` maps recorded input names to tensors; returns the
-        dict of every produced tensor by key (outputs under ``self.outputs``)."""
+        dict of every produced tensor by key (outputs under ``self.outputs``).
+
+        The recorded arguments are decoded once per device (``_compiled``): metadata and other
+        tensor-free arguments become the same Python objects on every run (so the backend's
+        plan caches hit by identity), tensor references are resolved per run."""
         dev = torch.device(device)
         env = {}
         for name, key in self.inputs.items():
             env[key] = inputs[name]
         consts = {}
 
+        def tensor(k):
+            t = env.get(k)
+            if t is None:
+                t = consts.get(k)
+                if t is None:
+                    t = consts[k] = torch.from_numpy(np.ascontiguousarray(self.arrays[k])).to(dev)
+            return t
+
         def dec(x):
             if isinstance(x, list):
                 return tuple(dec(y) for y in x)
             if isinstance(x, dict):
                 if '__t__' in x:
-                    k = x['__t__']
-                    if k in env:
-                        return env[k]
-                    if k not in consts:
-                        consts[k] = torch.from_numpy(np.ascontiguousarray(self.arrays[k])).to(dev)
-                    return consts[k]
+                    return tensor(x['__t__'])
                 if '__list__' in x:
                     return [dec(y) for y in x['__list__']]
                 if '__dict__' in x:
                     return {dec(k): dec(v) for k, v in x['__dict__']}
-                if '__slice__' in x:
-                    return slice(*x['__slice__'])
-                if '__dtype__' in x:
-                    return _DTYPES[x['__dtype__']]
-                if '__device__' in x:
-                    return dev
-                if '__devstr__' in x:
-                    return str(dev)
-                if '__ellipsis__' in x:
-                    return Ellipsis
-                raise ValueError(f"unknown encoding {list(x)}")
+                return _decode_leaf(x, dev)
             return x
 
-        for op in self.ops:
-            if op['k'] == 'mark':
+        def arg(spec):
+            kind, v = spec
+            if kind == 'c':
+                return v
+            if kind == 'r':
+                return tensor(v)
+            return dec(v)
+
+        for kind, fn, aspec, kwspec, keys in self._compiled(dev):
+            if kind == 'mark':
                 continue
-            args = dec(op['a'])
-            kwargs = {k: dec(v) for k, v in op.get('kw', {}).items()}
-            if op['k'] == 'b':
-                out = getattr(backend, op['fn'])(*args, **kwargs)
+            args = tuple(arg(a) for a in aspec)
+            kwargs = {k: arg(v) for k, v in kwspec.items()}
+            if kind == 'b':
+                out = getattr(backend, fn)(*args, **kwargs)
             else:
-                out = _torch_call(op['fn'], args, kwargs)
-            keys = op.get('o')
+                out = _torch_call(fn, args, kwargs)
             if keys is None:
                 continue
             if isinstance(keys, list):
@@ -110,6 +114,59 @@ class CallReplay:
             else:
                 env[keys] = out
         return env
+
+    def _compiled(self, dev):
+        key = str(dev)
+        cache = self.__dict__.setdefault('_compiled_by_dev', {})
+        if key not in cache:
+            def spec(x):
+                if isinstance(x, dict) and '__t__' in x:
+                    return ('r', x['__t__'])
+                if _has_ref(x):
+                    return ('d', x)
+                return ('c', _decode_const(x, dev))
+            cache[key] = [(op['k'], op['fn'], None, None, None) if op['k'] == 'mark' else
+                          (op['k'], op['fn'], [spec(a) for a in op['a']],
+                           {k: spec(v) for k, v in op.get('kw', {}).items()}, op.get('o'))
+                          for op in self.ops]
+        return cache[key]
+
+
+def _has_ref(x):
+    if isinstance(x, list):
+        return any(_has_ref(y) for y in x)
+    if isinstance(x, dict):
+        if '__t__' in x:
+            return True
+        return any(_has_ref(v) for v in x.values())
+    return False
+
+
+def _decode_leaf(x, dev):
+    if '__slice__' in x:
+        return slice(*x['__slice__'])
+    if '__dtype__' in x:
+        return _DTYPES[x['__dtype__']]
+    if '__device__' in x:
+        return dev
+    if '__devstr__' in x:
+        return str(dev)
+    if '__ellipsis__' in x:
+        return Ellipsis
+    raise ValueError(f"unknown encoding {list(x)}")
+
+
+def _decode_const(x, dev):
+    """Decodes a tensor-free argument (lists become tuples, as in the recording's metadata)."""
+    if isinstance(x, list):
+        return tuple(_decode_const(y, dev) for y in x)
+    if isinstance(x, dict):
+        if '__list__' in x:
+            return [_decode_const(y, dev) for y in x['__list__']]
+        if '__dict__' in x:
+            return {_decode_const(k, dev): _decode_const(v, dev) for k, v in x['__dict__']}
+        return _decode_leaf(x, dev)
+    return x
 
 
 def check_dataflow(replay):
