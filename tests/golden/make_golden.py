@@ -861,7 +861,17 @@ def _arr_from(rec, x):
     return rec.arrays[x['__array__']]
 
 
-if __name__ == '__main__':
+def scen_ctmrg_chi144():
+    """The CTMRG scenario at the environment dimension of the benchmark configuration
+    (chi = 144; blocks of 2592 x 2592 in the projector SVDs)."""
+    scen_ctmrg(chi=144, name='ctmrg_z2_d6_chi144')
+
+
+if __name__ == '__main__' and len(sys.argv) > 2:
+    # python make_golden.py <reference tree> <scenario function> ...: only those
+    for fn in sys.argv[2:]:
+        globals()[fn]()
+elif __name__ == '__main__':
     for pol in ('fuse_to_matrix', 'fuse_contracted', 'no_fusion'):
         scen_tensordot(pol)
     scen_svd()
@@ -877,3 +887,4 @@ if __name__ == '__main__':
     scen_cfg3()
     scen_cfg5()
     scen_ctmrg()
+    scen_ctmrg_chi144()
