@@ -330,7 +330,7 @@ def tile_kind(m, n):
 GEMM_RED_REC, GEMM_RED_ITEM = 8, 1024
 SPLITK_MAX_TILES = 304   # plans with this many tiles (2 per SM) are not split
 SPLITK_UNITS = 608       # tiles x chunks aimed at after splitting (4 per SM)
-SPLITK_MIN_K = 256       # shortest K chunk
+SPLITK_MIN_K = 128       # shortest K chunk
 
 
 def _tiles_for(outs, terms):
@@ -421,7 +421,9 @@ def _pack_gemm(out_list):
             if m == 0 or n == 0 or sum(t[2] for t in tl) < 2 * ck:
                 direct.append((c_off, m, n, ldc, tl))
                 continue
-            ch = _chunks(tl, ck)
+            kk = sum(t[2] for t in tl)
+            nch = -(-kk // ck)
+            ch = _chunks(tl, -(-(-(-kk // nch)) // 16) * 16)  # nch near-equal chunks, multiples of 16
             for ci, cl in enumerate(ch):
                 parts.append((ws + ci * m * n, m, n, n, cl))
             ri = len(red)
