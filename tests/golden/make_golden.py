@@ -25,6 +25,7 @@ Nothing at run time (tests, bench, smoke) reads the reference tree; only this sc
 import json
 import os
 import sys
+import weakref
 
 import numpy as np
 
@@ -664,7 +665,8 @@ class OpRecorder:
         from torch.overrides import TorchFunctionMode
         self.torch = torch
         self.module = module
-        self.ops, self.consts, self.keys, self.refs = [], {}, {}, []
+        self.ops, self.consts, self.keys = [], {}, {}
+        self.count = 0
         self.depth = 0
         self.active = False
         self.orig = {}
@@ -691,9 +693,12 @@ class OpRecorder:
     def key(self, t, name=None):
         k = self.keys.get(id(t))
         if k is None:
-            k = name or f"t{len(self.keys)}"
+            self.count += 1
+            k = name or f"t{self.count}"
             self.keys[id(t)] = k
-            self.refs.append(t)
+            # forget the id when the tensor dies (ids are reused); holding every tensor alive
+            # instead does not fit in memory at chi = 144
+            weakref.finalize(t, self.keys.pop, id(t), None)
         return k
 
     def _enc(self, x):

@@ -391,6 +391,7 @@ __device__ bool grid_barrier(unsigned long long* ctrl, unsigned nblocks) {
 
 constexpr int kChunk = 8;  // elements per lane per row kept in flight
 constexpr int kLoadBatch = 8;  // independent loads per thread when a CTA stages rows
+constexpr int kRowRegs = 16;   // row elements per lane kept in registers in a blocked inner round
 
 // Rotates rows (p, q) of X and W by one Jacobi rotation. Loads are issued a chunk at a
 // time (kChunk per lane and row, all before any store of the chunk) so that the L2
@@ -600,21 +601,51 @@ __global__ void __launch_bounds__(BR * 32) svd_block_sweeps_kernel(T* __restrict
               T* xq = Xs + (size_t)q * lmax;
               R al_ = 0, be_ = 0;
               T ga_ = Num<T>::zero();
-              for (int64_t l = lane; l < L; l += 32) {
-                const T a = xp[l], b = xq[l];
-                al_ += Num<T>::abs2(a);
-                be_ += Num<T>::abs2(b);
-                ga_ = Num<T>::fmac(a, b, ga_);
+              // rows of at most 32 kRowRegs elements stay in registers between the inner
+              // products and the rotation (one shared-memory read and write per element)
+              // (only for CTAs of up to 256 threads: wider ones have 128 registers per thread)
+              constexpr int RR = (BR <= 8 && sizeof(T) * BR <= 64) ? kRowRegs : 1;
+              const bool in_regs = RR == kRowRegs && L <= 32 * kRowRegs;
+              T ra[RR], rb[RR];
+              if (in_regs) {
+#pragma unroll
+                for (int u = 0; u < RR; ++u) {
+                  const int l = lane + 32 * u;
+                  ra[u] = (l < L) ? xp[l] : Num<T>::zero();
+                  rb[u] = (l < L) ? xq[l] : Num<T>::zero();
+                  al_ += Num<T>::abs2(ra[u]);
+                  be_ += Num<T>::abs2(rb[u]);
+                  ga_ = Num<T>::fmac(ra[u], rb[u], ga_);
+                }
+              } else {
+                for (int64_t l = lane; l < L; l += 32) {
+                  const T a = xp[l], b = xq[l];
+                  al_ += Num<T>::abs2(a);
+                  be_ += Num<T>::abs2(b);
+                  ga_ = Num<T>::fmac(a, b, ga_);
+                }
               }
               R c = 0, s = 0;
               T u = Num<T>::one();
               const R thr2 = (R)__longlong_as_double((long long)st[sizeof(R) == 4 ? ST_THR32 : ST_THR64]);
               if (Rotation<T>::get(al_, be_, ga_, L, lane, st + ST_MAXCOS, c, s, u, thr2)) {
-                for (int64_t l = lane; l < L; l += 32) {
-                  T a = xp[l], b = xq[l];
-                  rot2<T>(a, b, c, s, u);
-                  xp[l] = a;
-                  xq[l] = b;
+                if (in_regs) {
+#pragma unroll
+                  for (int v = 0; v < RR; ++v) {
+                    const int l = lane + 32 * v;
+                    if (l < L) {
+                      rot2<T>(ra[v], rb[v], c, s, u);
+                      xp[l] = ra[v];
+                      xq[l] = rb[v];
+                    }
+                  }
+                } else {
+                  for (int64_t l = lane; l < L; l += 32) {
+                    T a = xp[l], b = xq[l];
+                    rot2<T>(a, b, c, s, u);
+                    xp[l] = a;
+                    xq[l] = b;
+                  }
                 }
                 for (int l = lane; l < R2; l += 32) {
                   T a = Qs[p * R2 + l], b = Qs[q * R2 + l];
