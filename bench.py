@@ -175,6 +175,28 @@ class Cfg4:
         self.E_ref = self.r.payload['E']
         self.grad_ref = self.r.arrays['ref:grad']
 
+    def flops(self):
+        """Algorithmic work of one step counted at the backend boundary from the recorded
+        metadata: forward sector-GEMM FLOP, nominal SVD FLOP (14 L k^2 + 8 k^3 per block),
+        and backward GEMM FLOP (two adjoint products per dot, the SVD adjoint's products)."""
+        import torch
+        from yastn_gb300 import _plans as P
+        from yastn_gb300.replay import _decode_const
+        fg = fs = bg = 0
+        for op in self.r.ops:
+            if op['k'] != 'b' or op['fn'] not in ('dot', 'svd'):
+                continue
+            meta = _decode_const(op['a'][2] if op['fn'] == 'dot' else op['a'][1], torch.device('cpu'))
+            if op['fn'] == 'dot':
+                fg += P.dot_plan(meta).flops
+                pa, pb = P.dot_backward_plans(meta)
+                bg += pa.flops + pb.flops
+            else:
+                fs += P.svd_plan(meta).nominal_flops
+                ap = P.svd_adjoint_plan(meta)
+                bg += sum(g.flops for g in (ap.gP, ap.gQ, ap.gT, ap.gR, ap.gA1, ap.gA2))
+        return fg, fs, bg
+
     def step(self, torch, backend, device, A_host=None, pinned=None):
         """One forward + backward; returns (E, grad) as device tensors."""
         if pinned is not None:
@@ -872,6 +894,7 @@ def run_gpu_cfg4(args, wl):
     t0 = time.perf_counter()
     wl.step(torch, plain, 'cpu')
     cpu_ms = (time.perf_counter() - t0) * 1e3
+    fg, fs, bg = wl.flops()
     line = {
         "metric": wl.metric, "value": t_max, "unit": "ms", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": False, "scaling": "weak",
@@ -884,7 +907,9 @@ def run_gpu_cfg4(args, wl):
                    "plain_per_block_gpu": "the same sequence with one torch launch per block, torch.linalg.svd "
                                           "(cuSOLVER), torch autograd + the reference's broadened SVD adjoint",
                    "plain_over_fused": float(np.mean(tp)) / t_max,
-                   "plain_energy_rel_err": ep_err, "plain_grad_rel_err": gp_err},
+                   "plain_energy_rel_err": ep_err, "plain_grad_rel_err": gp_err,
+                   "flop_per_step": {"forward_gemm": fg, "forward_svd_nominal": fs, "backward_gemm": bg},
+                   "effective_tflops": (fg + fs + bg) / (t_max * 1e-3) / 1e12},
         "roofline": roof,
         "cpu_baseline": {"value": cpu_ms, "unit": "ms", "cores": torch.get_num_threads(), "kind": "port",
                          "sample": "one full forward+backward, one torch CPU op per block (LAPACK SVD)"},

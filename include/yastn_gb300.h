@@ -288,7 +288,14 @@ int yb_svd_qr(const void* a, void* work64, void* work32, const int64_t* blocks, 
               int64_t* state, double* scale, int64_t* qctrl, int qctrl_words, void* stream);
 int yb_svd_finalize(void* work, void* U, double* S, void* Vh, const int64_t* blocks,
                     int n_blocks, int dtype, int max_k, int mode, const double* shift,
-                    const int64_t* state, void* stream);
+                    const int64_t* state, int64_t* n_small, void* stream);
+/* n_small (nullable, int64[n_blocks], zeroed by the caller): blocks whose completion would
+ * cost more than 2^22 element operations in one CTA (n_zero k L) are not completed by
+ * yb_svd_finalize; their count of small values is written there, and the caller completes
+ * them: candidates from yb_fill_candidates (G, L x n_zero per block, uniform in [-1, 1)),
+ * projected twice against the earlier vectors with grouped GEMMs, orthonormalised by yb_qr,
+ * copied into the factor. recs of yb_fill_candidates: int64 pairs (offset, count). */
+int yb_fill_candidates(void* G, const int64_t* recs, int n_recs, int dtype, void* stream);
 
 /* SVD adjoint core (torch_svd_gesdd.py:296-428): per block record YB_ADJ_REC int64:
  *   [0] dA offset [1] m [2] n [3] U/gU offset [4] S/gS offset [5] Vh/gVh offset
@@ -300,6 +307,26 @@ int yb_svd_finalize(void* work, void* U, double* S, void* Vh, const int64_t* blo
 int yb_svd_adjoint_core(const void* P, const void* Q, const double* S, const double* gS, void* K,
                         const void* gU, const void* gVh, void* TR, const int64_t* blocks,
                         int n_blocks, int dtype, void* stream);
+/* ==== QR (backend qr, backend_np.py:511-520, backend_torch.py:475-484) ===============
+ * yb_qr: reduced QR of every block, A = Q R with R's diagonal made positive (real), Q
+ * m x k and R k x n row-major (k = min(m, n)). Records YB_SVD_REC int64 with [16] = 2:
+ * [0] a offset [1] m [2] n [3] Q offset [5] R offset [9] k [17] m [18] Z offset (k x m)
+ * [19] reflector offset (k x m) [20] tau offset (k) [21] R rows offset (k x k), workspace
+ * offsets in FP64 (complex128) elements. The Householder factorisation is the one of
+ * yb_svd_qr applied to M = A (wide blocks: to A's first m columns; the host forms
+ * R[:, m:] = Q^H A[:, m:] with the grouped GEMM); R's part below the diagonal is zeroed.
+ * yb_qr_adjoint_sym / yb_trsm_rt: the two elementwise steps of the QR adjoint (real),
+ *   dA = (gQ' + Q copyltu(M)) R^{-T},  M = R gR^T - gQ'^T Q
+ * (gQ' = gQ, or gQ + A[:, m:] gR[:, m:]^T for wide blocks, whose dA[:, m:] = Q gR[:, m:]);
+ * the products are grouped GEMMs. Records YB_QRADJ_REC int64: [0] M offset [1] k
+ * [2] B offset [3] rows [4] ldb [5] R offset [6] ldr. copyltu: M <- tril(M) + tril(M,-1)^T.
+ * trsm_rt: B <- B R^{-T} (R upper triangular, back substitution per row). */
+#define YB_QRADJ_REC 8
+int yb_qr(const void* a, void* Q, void* R, void* work64, const int64_t* blocks, int n_blocks, int dtype,
+          int64_t* qctrl, int qctrl_words, void* stream);
+int yb_qr_adjoint_sym(void* M, const int64_t* recs, int n_blocks, int dtype, void* stream);
+int yb_trsm_rt(void* B, const void* R, const int64_t* recs, int n_blocks, int dtype, void* stream);
+
 /* yb_eigh_adjoint_core: the inner matrix K of the eigh adjoint dA = U K op(U)^T per block,
  * from X = op(U)^T gU (k x k, grouped GEMM): symeig != 0 (order_by_magnitude, SYMEIG of
  * yastn/backend/linalg/torch_eig_sym.py:43-54, op(U) = U): K_ij = X_ij (d_j - d_i) /

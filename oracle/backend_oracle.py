@@ -18,6 +18,7 @@ __all__ = [
     'dot', 'dot_backward', 'transpose_dot_sum', 'transpose_dot_sum_backward',
     'svd', 'svd_block_backward', 'svd_backward',
     'eigh', 'eigh_block_backward', 'eigh_block_backward_hermitian', 'eigh_backward', 'fix_svd_signs',
+    'qr', 'qr_block_backward', 'qr_backward',
     'apply_mask', 'apply_mask_backward', 'embed_mask',
     'truncation_mask', 'rand_normal',
 ]
@@ -331,6 +332,52 @@ def eigh_block_backward_hermitian(d, u, gd, gu):
     if gd is not None:
         np.fill_diagonal(inner, gd)
     return u @ inner @ u.conj().T
+
+
+def qr(data, meta, sizes):
+    """Reduced QR per block with R's diagonal made positive; restates
+    ``yastn/backend/backend_np.py:511-520`` (records ``(sl, D, slQ, DQ, slR, DR)``; a zero
+    diagonal entry keeps sign +1)."""
+    Q = np.empty(sizes[0], dtype=data.dtype)
+    R = np.empty(sizes[1], dtype=data.dtype)
+    for sl, D, slQ, DQ, slR, DR in meta:
+        q, r = scipy.linalg.qr(data[_sl(sl)].reshape(D), mode='economic')
+        sr = np.sign(np.real(np.diag(r)))
+        sr[sr == 0] = 1
+        Q[_sl(slQ)] = (q * sr).ravel()
+        R[_sl(slR)] = (sr.reshape(-1, 1) * r).ravel()
+    return Q, R
+
+
+def qr_block_backward(q, r, gq, gr, a):
+    """Adjoint of one block's reduced QR (real), the rule torch's autograd applies to the
+    reference's ``torch.linalg.qr`` + sign fix (``backend_torch.py:475-484``): with
+    U = r[:, :k], gU = gr[:, :k], gq' = gq (+ a[:, m:] gr[:, m:]^T for wide blocks),
+    M = U gU^T - gq'^T q, dA[:, :k] = (gq' + q copyltu(M)) U^{-T}, copyltu(M) = tril(M) +
+    tril(M, -1)^T, and dA[:, m:] = q gr[:, m:] for wide blocks."""
+    m, k = q.shape
+    n = r.shape[1]
+    u, gu, b = r[:, :k], gr[:, :k], gq.copy()
+    if n > m:
+        b = b + a[:, m:] @ gr[:, m:].T
+    M = u @ gu.T - b.T @ q
+    b = b + q @ (np.tril(M) + np.tril(M, -1).T)
+    da = np.zeros((m, n), dtype=q.dtype)
+    da[:, :k] = scipy.linalg.solve_triangular(u, b.T, lower=False).T
+    if n > m:
+        da[:, m:] = q @ gr[:, m:]
+    return da
+
+
+def qr_backward(Q, R, gQ, gR, data, meta):
+    """Block-sparse QR adjoint (real)."""
+    out = np.zeros(data.size, dtype=data.dtype)
+    for sl, D, slQ, DQ, slR, DR in meta:
+        q = Q[_sl(slQ)].reshape(DQ)
+        r = R[_sl(slR)].reshape(DR)
+        out[_sl(sl)] = qr_block_backward(q, r, gQ[_sl(slQ)].reshape(DQ), gR[_sl(slR)].reshape(DR),
+                                         data[_sl(sl)].reshape(D)).ravel()
+    return out
 
 
 def eigh_backward(U, S, gU, gS, meta, data_size, dtype, order_by_magnitude=False, eps=1.0e-12):

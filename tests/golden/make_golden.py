@@ -36,7 +36,7 @@ sys.path.insert(0, REF)
 import yastn  # noqa: E402
 import yastn.backend.backend_np as bnp  # noqa: E402
 
-HOT = ['transpose_and_merge', 'unmerge', 'dot', 'transpose_dot_sum', 'svd', 'eigh',
+HOT = ['transpose_and_merge', 'unmerge', 'dot', 'transpose_dot_sum', 'svd', 'eigh', 'qr',
        'fix_svd_signs', 'apply_mask', 'embed_mask']
 
 
@@ -197,6 +197,51 @@ def scen_svd():
     yastn.linalg.svd(a, axes=(0, 1), fix_signs=True)
     rec.restore()
     save('svd', rec)
+
+
+def _tup(x):
+    return tuple(_tup(y) for y in x) if isinstance(x, list) else x
+
+
+def scen_qr():
+    """yastn.linalg.qr (linalg.py:738-828; backend_np.py:511-520, positive diagonal of R) on
+    U(1) tensors with tall, square and wide blocks, float64 and complex128, including a
+    rank-deficient block; and the adjoint of the real calls from the torch backend on CPU
+    (backend_torch.py:475-484: torch.linalg.qr + the sign fix, differentiated by torch)."""
+    import torch
+    import yastn.backend.backend_torch as bt
+    cfg = yastn.make_config(sym='U1', backend='np')
+    bnp.random_seed(17)
+    rec = Recorder(bnp)
+    for dtype in ('float64', 'complex128'):
+        a = yastn.rand(config=cfg, s=(-1, 1), t=((-1, 0, 1), (-1, 0, 1)), D=((30, 7, 5), (4, 7, 40)), dtype=dtype)
+        yastn.linalg.qr(a, axes=(0, 1))
+        b = yastn.rand(config=cfg, s=(-1, -1, 1), t=((0, 1), (0, 1), (0, 1, 2)), D=((3, 4), (2, 5), (6, 9, 2)),
+                       dtype=dtype)
+        yastn.linalg.qr(b, axes=((0, 1), 2))
+    # a rank-deficient block: two equal columns
+    c = yastn.rand(config=cfg, s=(-1, 1), t=((0,), (0,)), D=((9,), (6,)))
+    blk = c[(0, 0)]
+    blk[:, 3] = blk[:, 1]
+    yastn.linalg.qr(c, axes=(0, 1))
+    rec.restore()
+    # adjoints of the real calls through the reference's torch backend
+    g = torch.Generator().manual_seed(5)
+    for call in rec.calls:
+        if call['fn'] != 'qr':
+            continue
+        data = rec.arrays[call['args'][0]['__array__']]
+        if np.iscomplexobj(data):
+            continue
+        meta = _tup(call['args'][1])
+        sizes = tuple(call['args'][2])
+        d_ = torch.from_numpy(data.copy()).requires_grad_(True)
+        Q, R = bt.qr(d_, meta, sizes)
+        gQ = torch.randn(sizes[0], dtype=torch.float64, generator=g)
+        gR = torch.randn(sizes[1], dtype=torch.float64, generator=g)
+        (grad,) = torch.autograd.grad((Q, R), (d_,), grad_outputs=(gQ, gR))
+        call['adjoint'] = {'gQ': rec._put(gQ.numpy()), 'gR': rec._put(gR.numpy()), 'grad': rec._put(grad.numpy())}
+    save('qr', rec)
 
 
 def scen_fix_signs():
@@ -881,6 +926,7 @@ elif __name__ == '__main__':
         scen_tensordot(pol)
     scen_svd()
     scen_fix_signs()
+    scen_qr()
     scen_truncation()
     scen_eigh()
     scen_adjoints()

@@ -326,3 +326,82 @@ def test_apply_mask_on_reference_calls(name, cuda_device):
         np.testing.assert_array_equal(back, oracle.apply_mask_backward(g, mask, meta, A.size, axis, ndim))
         n += 1
     assert n > 0
+
+
+def _qr_checks(data, meta, Q, R, Qr=None, Rr=None):
+    for sl, D, slQ, DQ, slR, DR in meta:
+        a = data[sl[0]:sl[1]].reshape(D)
+        q, r = Q[slQ[0]:slQ[1]].reshape(DQ), R[slR[0]:slR[1]].reshape(DR)
+        scale = max(np.abs(a).max(), 1e-300)
+        assert np.abs(q @ r - a).max() <= TOL * scale * max(D)
+        assert np.abs(q.conj().T @ q - np.eye(DQ[1])).max() <= TOL * max(10, DQ[1])
+        assert np.abs(np.tril(r[:, :DR[0]], -1)).max(initial=0) == 0
+        assert (np.real(np.diag(r)) >= 0).all() and np.abs(np.imag(np.diag(r))).max(initial=0) == 0
+        if Qr is not None and np.linalg.cond(a) < 1e6:  # a well-conditioned block's factors are unique
+            assert rel(q, Qr[slQ[0]:slQ[1]].reshape(DQ)) <= 1e-10
+            assert rel(r, Rr[slR[0]:slR[1]].reshape(DR)) <= 1e-10
+
+
+def test_qr_on_reference_calls(cuda_device):
+    """Batched Householder QR with R's diagonal made positive against the reference's NumPy
+    backend (tall, square, wide, complex, rank-deficient blocks), and the real adjoint
+    against the reference torch backend's autograd gradient."""
+    tr = load_trace('qr')
+    n = 0
+    for c in tr['calls']:
+        if c['fn'] != 'qr':
+            continue
+        data, meta, sizes = c['args']
+        Q, R = (host(x) for x in ops.qr(dev(data), meta, sizes))
+        _qr_checks(data, meta, Q, R, *c['out'])
+        full = all(np.linalg.matrix_rank(data[sl[0]:sl[1]].reshape(D)) == min(D) for sl, D, *_ in meta)
+        if 'adjoint' in c and full:
+            adj = c['adjoint']
+            g = host(ops.qr_backward(dev(c['out'][0]), dev(c['out'][1]), dev(adj['gQ']), dev(adj['gR']), dev(data),
+                                     meta))
+            assert rel(g, adj['grad']) <= 1e-10
+        n += 1
+    assert n == 5
+
+
+@pytest.mark.parametrize('cplx', [False, True])
+def test_qr_large_blocks(cplx, cuda_device):
+    """Blocks of 432 x 432, 600 x 200, 100 x 900, 2000 x 16 and a graded one against the
+    oracle; the adjoint of the real ones against the oracle's."""
+    rng = np.random.default_rng(41)
+    f = lambda *sh: rng.normal(size=sh) + (1j * rng.normal(size=sh) if cplx else 0)
+    q1, _ = np.linalg.qr(f(150, 150))
+    blocks = [f(432, 432), f(600, 200), f(100, 900), f(2000, 16), (q1 * np.logspace(0, -10, 150)) @ f(150, 150)]
+    meta, off, oQ, oR, parts = [], 0, 0, 0, []
+    for a in blocks:
+        m, n = a.shape
+        k = min(m, n)
+        meta.append(((off, off + m * n), (m, n), (oQ, oQ + m * k), (m, k), (oR, oR + k * n), (k, n)))
+        off += m * n; oQ += m * k; oR += k * n
+        parts.append(a.ravel())
+    meta = tuple(meta)
+    data = np.concatenate(parts)
+    Q, R = (host(x) for x in ops.qr(dev(data), meta, (oQ, oR)))
+    Qr, Rr = oracle.qr(data, meta, (oQ, oR))
+    _qr_checks(data, meta, Q, R, Qr, Rr)
+    if not cplx:
+        gQ, gR = rng.normal(size=oQ), rng.normal(size=oR)
+        meta_w = meta[:4]  # the graded block's adjoint amplifies by 1e10
+        g = host(ops.qr_backward(dev(Qr), dev(Rr), dev(gQ), dev(gR), dev(data), meta_w))
+        ref = oracle.qr_backward(Qr, Rr, gQ, gR, data, meta_w)
+        assert rel(g, ref) <= 1e-10
+
+
+def test_qr_autograd_gradcheck(cuda_device):
+    """torch.autograd.gradcheck of the backend's qr Function (central differences)."""
+    from yastn_gb300 import backend as BK
+    rng = np.random.default_rng(2)
+    shapes = [(5, 3), (4, 4), (2, 6)]
+    meta, off, oQ, oR = [], 0, 0, 0
+    for m, n in shapes:
+        k = min(m, n)
+        meta.append(((off, off + m * n), (m, n), (oQ, oQ + m * k), (m, k), (oR, oR + k * n), (k, n)))
+        off += m * n; oQ += m * k; oR += k * n
+    meta = tuple(meta)
+    x = dev(rng.normal(size=off)).requires_grad_(True)
+    assert torch.autograd.gradcheck(lambda d: BK.qr(d, meta, (oQ, oR)), (x,), eps=1e-6, atol=1e-7)

@@ -235,6 +235,36 @@ def test_heff2_replay_and_lanczos_match_reference():
     assert wl.flops == 630254080 or abs(wl.flops - 6.303e8) < 1e6
 
 
+def test_oracle_qr_and_adjoint_match_reference():
+    """qr (positive diagonal of R) against the reference's NumPy backend on tall, square,
+    wide, complex and rank-deficient blocks; the real adjoint against the reference torch
+    backend's autograd gradient."""
+    tr = load_trace('qr')
+    n_adj = 0
+    for c in tr['calls']:
+        if c['fn'] != 'qr':
+            continue
+        data, meta, sizes = c['args']
+        Q, R = oracle.qr(data, meta, sizes)
+        Qr, Rr = c['out']
+        for sl, D, slQ, DQ, slR, DR in meta:
+            a = data[sl[0]:sl[1]].reshape(D)
+            q, r = Q[slQ[0]:slQ[1]].reshape(DQ), R[slR[0]:slR[1]].reshape(DR)
+            assert _rel(q @ r, a) < 1e-13
+            assert np.abs(q.conj().T @ q - np.eye(DQ[1])).max() < 1e-13
+            assert (np.real(np.diag(r)) >= 0).all()
+            if np.linalg.matrix_rank(a) == min(D):  # unique factorisation
+                assert _rel(q, Qr[slQ[0]:slQ[1]].reshape(DQ)) < 1e-11
+                assert _rel(r, Rr[slR[0]:slR[1]].reshape(DR)) < 1e-11
+        full = all(np.linalg.matrix_rank(data[sl[0]:sl[1]].reshape(D)) == min(D) for sl, D, *_ in meta)
+        if 'adjoint' in c and full:  # (the adjoint of a rank-deficient block is not defined)
+            adj = c['adjoint']
+            g = oracle.qr_backward(Qr, Rr, adj['gQ'], adj['gR'], data, meta)
+            assert _rel(g, adj['grad']) < 1e-10
+            n_adj += 1
+    assert n_adj == 2
+
+
 def test_ctmrg_recording_dataflow_is_closed():
     """The recorded CTMRG sequence only uses tensors it produced, its input or its stored
     constants, and its output (the energy) is produced by it."""

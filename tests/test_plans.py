@@ -380,6 +380,44 @@ def test_qr_preconditioned_jacobi_on_plan_layout(cplx):
         assert np.abs(vh @ vh.conj().T - np.eye(k)).max() <= 1e-13
 
 
+def test_qr_adjoint_plan_reproduces_oracle():
+    """The QR adjoint's grouped-GEMM plans, the copyltu/back-substitution records and the copy
+    into dA (numpy statement of the two elementwise kernels) give the oracle's adjoint on
+    tall, square and wide blocks."""
+    rng = np.random.default_rng(6)
+    shapes = [(9, 4), (5, 5), (3, 8), (1, 6), (12, 1)]
+    meta, off, oQ, oR = [], 0, 0, 0
+    for m, n in shapes:
+        k = min(m, n)
+        meta.append(((off, off + m * n), (m, n), (oQ, oQ + m * k), (m, k), (oR, oR + k * n), (k, n)))
+        off += m * n; oQ += m * k; oR += k * n
+    meta = tuple(meta)
+    data = rng.normal(size=off)
+    Q, R = oracle.qr(data, meta, (oQ, oR))
+    gQ, gR = rng.normal(size=oQ), rng.normal(size=oR)
+    plan = P.qr_plan(meta)
+    Bw = gQ.copy()
+    M = np.zeros(plan.m_size)
+    PI.run_gemm(plan.w1, data, gR, Bw, beta=1.0)
+    PI.run_gemm(plan.m1, R, gR, M)
+    PI.run_gemm(plan.m2, Bw, Q, M, alpha=-1.0, beta=1.0)
+    for mo, k, b0, rows, ldb, r0, ldr, _ in plan.adj:
+        Mb = M[mo:mo + k * k].reshape(k, k)
+        Mb[:] = np.tril(Mb) + np.tril(Mb, -1).T
+    PI.run_gemm(plan.s1, Q, M, Bw, beta=1.0)
+    for mo, k, b0, rows, ldb, r0, ldr, _ in plan.adj:
+        Bb = Bw[b0:b0 + rows * ldb].reshape(rows, ldb)[:, :k]
+        U = np.stack([R[r0 + i * ldr: r0 + i * ldr + k] for i in range(k)])
+        Bb[:] = np.linalg.solve(np.triu(U), Bb.T).T
+    dA = np.zeros(off)
+    for so, do, sizes, ss, ds in plan.copies:
+        for i in range(sizes[0]):
+            dA[do + i * ds[0]: do + i * ds[0] + sizes[1]] = Bw[so + i * ss[0]: so + i * ss[0] + sizes[1]]
+    PI.run_gemm(plan.y1, Q, gR, dA)
+    ref = oracle.qr_backward(Q, R, gQ, gR, data, meta)
+    assert np.abs(dA - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
 def test_mixed_precision_jacobi_schedule_complex():
     """Complex blocks: FP32 phase on complex64 rows with phase-aligned rotations, widen,
     Newton-Schulz with T = W^H W, X = W X_0 (X_0 = A^H for tall blocks), FP64 phase; the

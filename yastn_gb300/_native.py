@@ -24,11 +24,15 @@ SIGNATURES = {
     'yb_grouped_gemm': ([_vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _d, _d, _vp], _i),
     'yb_svd_init': ([_vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp], _i),
     'yb_svd_qr': ([_vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _i, _vp], _i),
+    'yb_qr': ([_vp, _vp, _vp, _vp, _vp, _i, _i, _vp, _i, _vp], _i),
+    'yb_qr_adjoint_sym': ([_vp, _vp, _i, _i, _vp], _i),
+    'yb_trsm_rt': ([_vp, _vp, _vp, _i, _i, _vp], _i),
     'yb_svd_sweeps': ([_vp, _vp, _i, _vp, _i, _i, _i, _i, _i, _d, _vp, _vp], _i),
     'yb_svd_widen': ([_vp, _vp, _vp, _i, _i, _vp, _vp], _i),
     'yb_svd_block_sweeps': ([_vp, _vp, _i, _vp, _i, _i, _i, _i, _i, _i, _i, _d, _i, _vp, _vp], _i),
     'yb_svd_shift_prefill': ([_vp, _vp, _i, _i, _vp, _vp], _i),
-    'yb_svd_finalize': ([_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp, _vp, _vp], _i),
+    'yb_svd_finalize': ([_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp], _i),
+    'yb_fill_candidates': ([_vp, _vp, _i, _i, _vp], _i),
     'yb_svd_adjoint_core': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
     'yb_eigh_adjoint_core': ([_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _vp], _i),
     'yb_mask_gather': ([_vp, _vp, _i, _vp, _vp, _i, _vp, _i, _vp], _i),

@@ -741,6 +741,60 @@ def svd_plan(meta, rows_per_super=None, cplx=False, qr=False):
     return CACHE.get((meta,), ('svd', rows_per_super, cplx, qr), build)
 
 
+class QrPlan:
+    """Plan of ``qr`` (records of yb_qr, the FP64 workspace, the GEMM of R's right part for
+    wide blocks) and of its adjoint (grouped GEMMs, copyltu/TRSM records, the copy of the
+    solved rows into dA)."""
+
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+        self._dev = {}
+
+
+QRADJ_REC = 8
+
+
+def qr_plan(meta, cplx=False):
+    """Reduced QR records (sl, D, slQ, DQ, slR, DR) of yastn/tensor/linalg.py:795-828, as
+    computed by backend_np.py:511-520 (positive diagonal of R)."""
+    def build():
+        recs, right, adj = [], [], []
+        w1, m1, m2, s1, y1, copies = [], [], [], [], [], []
+        off = mo = 0
+        max_k = 0
+        for sl, D, slQ, DQ, slR, DR in meta:
+            m, n = D
+            k = min(m, n)
+            if k == 0:
+                continue
+            if DQ != (m, k) or DR != (k, n):
+                raise PlanError("qr record is not a reduced QR")
+            rec = np.zeros(SVD_REC, dtype=np.int64)
+            rec[[0, 1, 2, 3, 5, 9, 10]] = (sl[0], m, n, slQ[0], slR[0], k, k)
+            z, v, tau, rr = off, off + k * m, off + 2 * k * m, off + 2 * k * m + k
+            rec[16:22] = (2, m, z, v, tau, rr)
+            off = rr + k * k
+            recs.append(rec)
+            max_k = max(max_k, k)
+            q0, r0, a0 = slQ[0], slR[0], sl[0]
+            if n > m:   # R[:, m:] = Q^H A[:, m:]
+                right.append((r0 + m, k, n - m, n, [(q0, a0 + m, m, 1, k, n, 1, int(cplx))]))
+                w1.append((q0, m, m, k, [(a0 + m, r0 + m, n - m, n, 1, 1, n, 0)]))      # gQ' += A[:, m:] gV^T
+                y1.append((a0 + m, m, n - m, n, [(q0, r0 + m, m, k, 1, n, 1, 0)]))      # dA[:, m:] = Q gV
+            m1.append((mo, k, k, k, [(r0, r0, k, n, 1, 1, n, 0)]))                       # M = U gU^T
+            m2.append((mo, k, k, k, [(q0, q0, m, 1, k, k, 1, 0)]))                       # M -= gQ'^T Q
+            s1.append((q0, m, k, k, [(q0, mo, k, k, 1, k, 1, 0)]))                       # gQ' += Q copyltu(M)
+            adj.append((mo, k, q0, m, k, r0, n, 0))
+            copies.append((q0, a0, [m, k], [k, 1], [n, 1]))
+            mo += k * k
+        blocks = np.stack(recs) if recs else np.zeros((0, SVD_REC), dtype=np.int64)
+        return QrPlan(blocks=blocks, n64=max(off, 1), max_k=max_k, right=_pack_gemm(right),
+                      adj=np.array(adj, dtype=np.int64).reshape(-1, QRADJ_REC), m_size=max(mo, 1),
+                      w1=_pack_gemm(w1), m1=_pack_gemm(m1), m2=_pack_gemm(m2), s1=_pack_gemm(s1),
+                      y1=_pack_gemm(y1), copies=copies)
+    return CACHE.get((meta,), ('qr', cplx), build)
+
+
 class SvdAdjointPlan:
     def __init__(self, recs, kk, tr, gP, gQ, gT, gR, gA1, gA2):
         self.recs, self.kk, self.tr = recs, kk, tr

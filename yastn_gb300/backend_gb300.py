@@ -552,8 +552,27 @@ def eigvals(data, meta, sizeS, **kwargs):
     _not_hot('eigvals (non-Hermitian)')
 
 
+class _Qr(torch.autograd.Function):
+    """qr (backend_torch.py:475-484): batched Householder QR, positive diagonal of R; the
+    adjoint of real blocks by grouped GEMMs, a symmetrisation and a triangular solve."""
+
+    @staticmethod
+    def forward(ctx, data, meta, sizes):
+        Q, R = ops.qr(data, meta, sizes)
+        ctx.save_for_backward(data, Q, R)
+        ctx.meta = meta
+        return Q, R
+
+    @staticmethod
+    def backward(ctx, gQ, gR):
+        data, Q, R = ctx.saved_tensors
+        if Q.is_complex():
+            raise NotImplementedError("yastn_gb300 qr: the adjoint of complex blocks is not implemented")
+        return ops.qr_backward(Q, R, gQ, gR, data, ctx.meta), None, None
+
+
 def qr(data, meta, sizes):
-    _not_hot('qr')
+    return _Qr.apply(data, meta, sizes)
 
 
 def pinv(A, rcond=None, hermitian=False, out=None, atol=None, rtol=None):

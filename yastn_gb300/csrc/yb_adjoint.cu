@@ -20,6 +20,11 @@ namespace {
 
 __device__ __forceinline__ double rinv(double x) { return x / (x * x + 1.0e-12); }
 
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 template <bool Cx>
 struct Elt;
 template <>
@@ -155,8 +160,62 @@ __global__ void eigh_adjoint_core_kernel(const typename Elt<Cx>::T* __restrict__
   }
 }
 
+// QR adjoint (real): records YB_QRADJ_REC int64 per block: [0] M offset (k x k) [1] k
+// [2] B offset (rows x k, row-major, leading dimension [4]) [3] rows [4] ldb
+// [5] R offset (k x k upper triangle, leading dimension [6]) [6] ldr.
+// copyltu: M <- tril(M) + tril(M, -1)^T (the upper triangle mirrored from the lower).
+__global__ void qr_copyltu_kernel(double* __restrict__ M, const int64_t* __restrict__ recs) {
+  const int64_t* r = recs + (int64_t)blockIdx.y * YB_QRADJ_REC;
+  const int64_t k = r[1];
+  double* m = M + r[0];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < k * k; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / k, j = e - i * k;
+    if (i < j) m[e] = m[j * k + i];  // writes the upper triangle only, reads the lower
+  }
+}
+
+// B <- B R^{-T} row by row (R upper triangular): x R^T = b, i.e. R x^T = b^T by back
+// substitution, one warp per row, in place. Entries of x already solved are re-read from L2
+// (written by lane 0 of the same warp, ordered by __syncwarp).
+__global__ void trsm_rt_kernel(double* __restrict__ B, const double* __restrict__ Rm, const int64_t* __restrict__ recs) {
+  const int64_t* r = recs + (int64_t)blockIdx.y * YB_QRADJ_REC;
+  const int64_t k = r[1], rows = r[3], ldb = r[4], ldr = r[6];
+  double* b = B + r[2];
+  const double* R = Rm + r[5];
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t row = warp; row < rows; row += nwarps) {
+    double* x = b + row * ldb;
+    for (int64_t j = k - 1; j >= 0; --j) {
+      double acc = 0.0;
+      for (int64_t l = j + 1 + lane; l < k; l += 32) acc = fma(R[j * ldr + l], __ldcg(x + l), acc);
+      acc = warp_sum(acc);
+      if (lane == 0) x[j] = (__ldcg(x + j) - acc) / R[j * ldr + j];
+      __syncwarp();
+    }
+  }
+}
+
 }  // namespace
 }  // namespace yb
+
+extern "C" int yb_qr_adjoint_sym(void* M, const int64_t* recs, int n_blocks, int dtype, void* stream) {
+  if (n_blocks == 0) return YB_OK;
+  if (!M || !recs) return YB_ERR_INVALID;
+  if (dtype != YB_F64) return YB_ERR_INVALID;
+  yb::qr_copyltu_kernel<<<dim3(16, (unsigned)n_blocks), 256, 0, (cudaStream_t)stream>>>((double*)M, recs);
+  return yb::check_launch();
+}
+
+extern "C" int yb_trsm_rt(void* B, const void* R, const int64_t* recs, int n_blocks, int dtype, void* stream) {
+  if (n_blocks == 0) return YB_OK;
+  if (!B || !R || !recs) return YB_ERR_INVALID;
+  if (dtype != YB_F64) return YB_ERR_INVALID;
+  yb::trsm_rt_kernel<<<dim3(32, (unsigned)n_blocks), 256, 0, (cudaStream_t)stream>>>((double*)B, (const double*)R,
+                                                                                      recs);
+  return yb::check_launch();
+}
 
 extern "C" int yb_eigh_adjoint_core(const void* X, const double* D, const double* gD, void* K,
                                     const int64_t* blocks, int n_blocks, int dtype, int symeig, double eps,

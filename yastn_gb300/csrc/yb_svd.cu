@@ -757,18 +757,19 @@ int launch_block_sweeps(T* work, const int64_t* blocks, int n_blocks, const int3
 // Householder vectors below the diagonal (LAPACK's geqr2 layout, transposed); Q^T is then
 // formed in place (org2r, backward accumulation).
 
-// Z = X_0 in FP64 (A, or A^H for tall blocks).
+// Z = X_0 in FP64 (A, or A^H for tall blocks). Records with [16] = 2 (yb_qr, M = A): Z's
+// rows are the first k columns of A (length L = m).
 template <typename T>
 __global__ void svd_qr_load_kernel(const T* __restrict__ A, T* __restrict__ work, const int64_t* __restrict__ blocks) {
   const int64_t* r = blocks + (int64_t)blockIdx.y * YB_SVD_REC;
   if (!r[R_QR]) return;
   const int64_t m = r[R_M], n = r[R_N], k = r[R_K], L = r[R_LQ];
-  const bool tall = m > n;
+  const bool tall = m > n, plain = r[R_QR] == 2;
   const T* a = A + r[R_A];
   T* Z = work + r[R_Z];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < k * L; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = e / L, l = e - i * L;
-    Z[e] = tall ? cconj_(a[l * n + i]) : a[e];
+    Z[e] = plain ? a[l * n + i] : (tall ? cconj_(a[l * n + i]) : a[e]);
   }
 }
 
@@ -884,7 +885,7 @@ __global__ void __launch_bounds__(kThreads) svd_qr_kernel(T* __restrict__ work, 
     T32* X32 = work32 + r[R_X32];
     T32* W32 = work32 + r[R_W32];
     unsigned long long* ready = flags + b;
-    const double sc = scale[b];
+    const double sc = scale ? scale[b] : 0.0;  // no FP32 Jacobi start for yb_qr
     // factorisation
     if (gw == 0) {
       qr_reflector<T>(Z, tau, 0, L, lane);
@@ -910,8 +911,10 @@ __global__ void __launch_bounds__(kThreads) svd_qr_kernel(T* __restrict__ work, 
       const int64_t i = e / k, c = e - i * k;
       const T v = (c >= i) ? ldcg_t(Z + c * L + i) : Num<T>::zero();
       RR[e] = v;
-      X32[e] = to32(rscale(v, sc));
-      W32[e] = (i == c) ? Num<T32>::one() : Num<T32>::zero();
+      if (scale) {
+        X32[e] = to32(rscale(v, sc));
+        W32[e] = (i == c) ? Num<T32>::one() : Num<T32>::zero();
+      }
     }
     for (int64_t e = gt; e < k * L; e += ngt) {
       const int64_t j = e / L, l = e - j * L;
@@ -929,12 +932,62 @@ __global__ void __launch_bounds__(kThreads) svd_qr_kernel(T* __restrict__ work, 
   }
 }
 
+// Candidate vectors of the blocked completion: G (L x nz, row-major per record) filled with
+// values uniform in [-1, 1) from a counter-based hash of (record, element) (deterministic;
+// any full-rank draw works: the candidates are projected and orthonormalised afterwards).
+// recs: int64 pairs (offset, count) per record.
+template <typename T>
+__global__ void fill_candidates_kernel(T* __restrict__ G, const int64_t* __restrict__ recs) {
+  const int64_t off = recs[2 * blockIdx.y], cnt = recs[2 * blockIdx.y + 1];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < cnt; e += (int64_t)gridDim.x * blockDim.x) {
+    uint64_t h = (uint64_t)(off + e) * 0x9E3779B97F4A7C15ull + (uint64_t)blockIdx.y * 0xD1B54A32D192ED03ull;
+    h ^= h >> 31; h *= 0xBF58476D1CE4E5B9ull; h ^= h >> 29; h *= 0x94D049BB133111EBull; h ^= h >> 32;
+    const double u = (double)(h >> 11) * 0x1.0p-52 - 1.0;
+    if constexpr (Num<T>::cplx) {
+      const uint64_t h2 = h * 0x2545F4914F6CDD1Dull;
+      G[off + e] = make_double2(u, (double)(h2 >> 11) * 0x1.0p-52 - 1.0);
+    } else {
+      G[off + e] = u;
+    }
+  }
+}
+
+// yb_qr output: Q (m x k, row-major) from Z = Q^T and the square part of R (k x k of the
+// k x n rows) from R's rows, both with the signs that make R's diagonal positive (LAPACK's
+// diagonal is beta = -sign(Re alpha) |x|: s_c = -1 where it is negative, as the reference's
+// sign(diag(R)) fix; a zero diagonal keeps +1). R's entries below the diagonal are zero.
+template <typename T>
+__global__ void qr_finalize_kernel(const T* __restrict__ work, T* __restrict__ Q, T* __restrict__ Rout,
+                                   const int64_t* __restrict__ blocks) {
+  const int64_t* r = blocks + (int64_t)blockIdx.y * YB_SVD_REC;
+  const int64_t n = r[R_N], k = r[R_K], L = r[R_LQ];
+  const T* Z = work + r[R_Z];
+  const T* RR = work + r[R_RR];
+  T* q = Q + r[R_U];
+  T* rr = Rout + r[R_V];
+  auto sgn = [&](int64_t c) -> double {
+    const T d = RR[c * k + c];
+    double re;
+    if constexpr (Num<T>::cplx) re = d.x; else re = d;
+    return re < 0.0 ? -1.0 : 1.0;
+  };
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < L * k; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t l = e / k, c = e - l * k;
+    q[e] = rscale(Z[c * L + l], sgn(c));
+  }
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < k * k; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / k, c = e - i * k;
+    rr[i * n + c] = (c >= i) ? rscale(RR[e], sgn(i)) : Num<T>::zero();
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(1024) svd_finalize_kernel(T* __restrict__ work, T* __restrict__ U,
                                                             double* __restrict__ S, T* __restrict__ Vh,
                                                             const int64_t* __restrict__ blocks, int pow2,
                                                             int mode, const double* __restrict__ shift,
-                                                            const int64_t* __restrict__ state) {
+                                                            const int64_t* __restrict__ state,
+                                                            int64_t* __restrict__ n_small) {
   extern __shared__ unsigned char smem_raw[];
   // [sig: pow2 doubles][complex: pow2 doubles][idx: pow2 ints]
   double* sig = reinterpret_cast<double*>(smem_raw);
@@ -1043,6 +1096,13 @@ __global__ void __launch_bounds__(1024) svd_finalize_kernel(T* __restrict__ work
   }
   __syncthreads();
   if (n_zero == 0) return;
+  // large completions (n_zero k L above 2^22) are left to the host's blocked completion
+  // (random candidates projected with grouped GEMMs and orthonormalised by yb_qr): the count
+  // goes to n_small[b] and the vectors stay as written
+  if (n_small != nullptr && (double)n_zero * (double)k * (double)L > 4194304.0) {
+    if (threadIdx.x == 0) n_small[blockIdx.x] = n_zero;
+    return;
+  }
   // completion: the small values sit at the end (positions k - n_zero .. k-1); each of their
   // vectors becomes a unit vector e_c orthogonalised against all earlier vectors by two passes
   // of classical Gram-Schmidt (all coefficients of a pass at once). The candidate is the
@@ -1237,7 +1297,7 @@ int qr_t(const void* a, void* work, void* work32, const int64_t* blocks, int n_b
   if (n_groups > n_blocks) n_groups = n_blocks;
   if ((int64_t)n_groups * yb::C_REC + n_blocks > qctrl_words) n_groups = (qctrl_words - n_blocks) / yb::C_REC;
   if (n_groups < 1) return YB_ERR_INVALID;
-  yb::block_fro_kernel<T><<<n_blocks, 256, 0, s>>>((const T*)a, blocks, nullptr, scale, state);
+  if (state) yb::block_fro_kernel<T><<<n_blocks, 256, 0, s>>>((const T*)a, blocks, nullptr, scale, state);
   yb::svd_qr_load_kernel<T><<<dim3(64, (unsigned)n_blocks), 256, 0, s>>>((const T*)a, (T*)work, blocks);
   e = cudaMemsetAsync(qctrl, 0, sizeof(int64_t) * ((size_t)n_groups * yb::C_REC + n_blocks), s);
   if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
@@ -1248,21 +1308,21 @@ int qr_t(const void* a, void* work, void* work32, const int64_t* blocks, int n_b
   e = cudaLaunchCooperativeKernel((const void*)yb::svd_qr_kernel<T, T32>, dim3(n_groups * group), dim3(yb::kThreads),
                                   args, 0, s);
   if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
-  yb::svd_state_reset_kernel<<<n_blocks, 32, 0, s>>>(state);
+  if (state) yb::svd_state_reset_kernel<<<n_blocks, 32, 0, s>>>(state);
   return yb::check_launch();
 }
 
 template <typename T>
 int finalize_t(void* work, void* U, double* S, void* Vh, const int64_t* blocks, int n_blocks, int pow2,
-                      int mode, const double* shift, const int64_t* state, cudaStream_t s) {
+                      int mode, const double* shift, const int64_t* state, int64_t* n_small, cudaStream_t s) {
   const size_t smem = (size_t)pow2 * (sizeof(double) * (Num<T>::cplx ? 2 : 1) + sizeof(int));
-  if (smem > 48 * 1024) {
+  if (smem > 32 * 1024) {  // with the kernel's static shared memory the total passes 48 KB earlier
     cudaError_t e = cudaFuncSetAttribute(yb::svd_finalize_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
   }
   yb::svd_finalize_kernel<T><<<n_blocks, 1024, smem, s>>>((T*)work, (T*)U, S, (T*)Vh, blocks, pow2, mode,
-                                                          shift, state);
+                                                          shift, state, n_small);
   return yb::check_launch();
 }
 
@@ -1298,6 +1358,37 @@ int yb_svd_qr(const void* a, void* work64, void* work32, const int64_t* blocks, 
   if (dtype == YB_F64)
     return yb::qr_t<double, float>(a, work64, work32, blocks, n_blocks, state, scale, qctrl, qctrl_words, s);
   return yb::qr_t<double2, float2>(a, work64, work32, blocks, n_blocks, state, scale, qctrl, qctrl_words, s);
+}
+
+int yb_fill_candidates(void* G, const int64_t* recs, int n_recs, int dtype, void* stream) {
+  if (n_recs == 0) return YB_OK;
+  if (!G || !recs) return YB_ERR_INVALID;
+  const dim3 grid(32, (unsigned)n_recs);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == YB_F64) yb::fill_candidates_kernel<double><<<grid, 256, 0, s>>>((double*)G, recs);
+  else if (dtype == YB_C128) yb::fill_candidates_kernel<double2><<<grid, 256, 0, s>>>((double2*)G, recs);
+  else return YB_ERR_INVALID;
+  return yb::check_launch();
+}
+
+int yb_qr(const void* a, void* Q, void* R, void* work64, const int64_t* blocks, int n_blocks, int dtype,
+          int64_t* qctrl, int qctrl_words, void* stream) {
+  if (n_blocks == 0) return YB_OK;
+  if (dtype != YB_F64 && dtype != YB_C128) return YB_ERR_INVALID;
+  if (!a || !Q || !R || !work64 || !blocks || !qctrl) return YB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  const dim3 grid(64, (unsigned)n_blocks);
+  int st;
+  if (dtype == YB_F64) {
+    st = yb::qr_t<double, float>(a, work64, nullptr, blocks, n_blocks, nullptr, nullptr, qctrl, qctrl_words, s);
+    if (st != YB_OK) return st;
+    yb::qr_finalize_kernel<double><<<grid, 256, 0, s>>>((const double*)work64, (double*)Q, (double*)R, blocks);
+  } else {
+    st = yb::qr_t<double2, float2>(a, work64, nullptr, blocks, n_blocks, nullptr, nullptr, qctrl, qctrl_words, s);
+    if (st != YB_OK) return st;
+    yb::qr_finalize_kernel<double2><<<grid, 256, 0, s>>>((const double2*)work64, (double2*)Q, (double2*)R, blocks);
+  }
+  return yb::check_launch();
 }
 
 int yb_svd_sweeps(void* work, const int64_t* blocks, int n_blocks, const int32_t* pair_items, int n_pair_items,
@@ -1381,7 +1472,8 @@ int yb_svd_shift_prefill(void* work64, const int64_t* blocks, int n_blocks, int 
 }
 
 int yb_svd_finalize(void* work, void* U, double* S, void* Vh, const int64_t* blocks, int n_blocks, int dtype,
-                    int max_k, int mode, const double* shift, const int64_t* state, void* stream) {
+                    int max_k, int mode, const double* shift, const int64_t* state, int64_t* n_small,
+                    void* stream) {
   if (n_blocks == 0) return YB_OK;
   if (dtype != YB_F64 && dtype != YB_C128) return YB_ERR_INVALID;
   if (mode < 0 || mode > 2 || (mode != 0 && shift == nullptr)) return YB_ERR_INVALID;
@@ -1389,8 +1481,9 @@ int yb_svd_finalize(void* work, void* U, double* S, void* Vh, const int64_t* blo
   int pow2 = 1;
   while (pow2 < max_k) pow2 <<= 1;
   cudaStream_t s = (cudaStream_t)stream;
-  if (dtype == YB_F64) return yb::finalize_t<double>(work, U, S, Vh, blocks, n_blocks, pow2, mode, shift, state, s);
-  return yb::finalize_t<double2>(work, U, S, Vh, blocks, n_blocks, pow2, mode, shift, state, s);
+  if (dtype == YB_F64)
+    return yb::finalize_t<double>(work, U, S, Vh, blocks, n_blocks, pow2, mode, shift, state, n_small, s);
+  return yb::finalize_t<double2>(work, U, S, Vh, blocks, n_blocks, pow2, mode, shift, state, n_small, s);
 }
 
 }  // extern "C"

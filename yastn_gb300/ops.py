@@ -379,11 +379,68 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
         N.call('yb_svd_sweeps', _ptr(w64), _ptr(dblocks), nb, _ptr(dpairs), len(plan.pair_items), plan.max_rounds,
                64, code, max_sweeps, tol64, _ptr(state), st)
     _svd_state_check(state, nb, 'FP64', True)
+    n_small = torch.zeros(nb, dtype=torch.int64, device=dev) if mode == 0 else None
     N.call('yb_svd_finalize', _ptr(w64), _ptr(U), _ptr(S), _vp(V.data_ptr() if V is not None else 0), _ptr(dblocks),
-           nb, code, plan.max_k, mode, sp, _ptr(state), st)
+           nb, code, plan.max_k, mode, sp, _ptr(state), _vp(n_small.data_ptr() if n_small is not None else 0), st)
+    if n_small is not None:
+        nz = n_small.cpu().numpy()
+        if nz.any():
+            _complete(plan, U, V, nz, cplx)
     if plan.qr:  # the factor that comes from Q: Vh = conj(W) Q^T (wide), U = conj(Q) W^T (tall)
         run_gemm(plan.qfin_v, w64, w64, V)
         run_gemm(plan.qfin_u, w64, w64, U)
+
+
+def _complete(plan, U, V, nz, cplx):
+    """Blocked completion of the vectors of small singular values (blocks left by
+    yb_svd_finalize): per block, nz candidate vectors with entries uniform in [-1, 1)
+    (yb_fill_candidates), projected twice off the k - nz earlier vectors by grouped GEMMs
+    (C = V_g^H G, G -= V_g C), orthonormalised by the batched Householder QR, and copied into
+    the factor's last nz vectors (U columns or Vh rows, whichever the rows of X built)."""
+    key = (tuple(int(x) for x in nz),)
+    cache = plan.__dict__.setdefault('_completion', {})
+    if key not in cache:
+        by_target = {}
+        goff = coff = 0
+        for b, r in enumerate(plan.blocks):
+            z = int(nz[b])
+            if z == 0:
+                continue
+            m, n, k, tall, from_r = int(r[1]), int(r[2]), int(r[9]), bool(r[12]), bool(r[16])
+            to_u = tall != from_r
+            if to_u:
+                f0, sv, sj, Lv = int(r[3]), k, 1, m
+            else:
+                f0, sv, sj, Lv = int(r[5]), 1, n, n
+            j0 = k - z
+            t = by_target.setdefault(to_u, {'g1': [], 'g2': [], 'meta': [], 'fill': [], 'copies': [],
+                                            'G': 0, 'C': 0, 'Q': 0, 'R': 0})
+            g, c_, q_, r_ = t['G'], t['C'], t['Q'], t['R']
+            if j0 > 0:
+                t['g1'].append((c_, j0, z, z, [(f0, g, Lv, sj, sv, z, 1, int(cplx))]))
+                t['g2'].append((g, Lv, z, z, [(f0, c_, j0, sv, sj, z, 1, 0)]))
+            t['meta'].append(((g, g + Lv * z), (Lv, z), (q_, q_ + Lv * z), (Lv, z), (r_, r_ + z * z), (z, z)))
+            t['fill'].append((g, Lv * z))
+            t['copies'].append((q_, f0 + j0 * sj, [Lv, z], [z, 1], [sv, sj]))
+            t['G'] += Lv * z; t['C'] += j0 * z; t['Q'] += Lv * z; t['R'] += z * z
+        for t in by_target.values():
+            t['g1'], t['g2'] = P._pack_gemm(t['g1']), P._pack_gemm(t['g2'])
+            t['meta'] = tuple(t['meta'])
+            t['fill'] = np.array(t['fill'], dtype=np.int64).reshape(-1, 2)
+            t['copy'] = P.CopyPlan(t['copies'], sum(int(np.prod(c[2])) for c in t['copies']), 0)
+        cache[key] = by_target
+    dev = U.device
+    for to_u, t in cache[key].items():
+        F = U if to_u else V
+        G = torch.empty(max(t['G'], 1), dtype=F.dtype, device=dev)
+        C = torch.empty(max(t['C'], 1), dtype=F.dtype, device=dev)
+        N.call('yb_fill_candidates', _ptr(G), _ptr(_dev(t['g1'], 'fill', (t['fill'],), dev)[0]), len(t['fill']),
+               _dtype_code(F.dtype), _stream())
+        for _ in range(2):
+            run_gemm(t['g1'], F, G, C)
+            run_gemm(t['g2'], F, C, G, alpha=-1.0, beta=1.0)
+        Qc, _ = qr(G, t['meta'], (max(t['Q'], 1), max(t['R'], 1)))
+        run_copy(t['copy'], Qc, F)
 
 
 def svd(data, meta, sizes, max_sweeps=MAX_SWEEPS):
@@ -398,6 +455,57 @@ def svd(data, meta, sizes, max_sweeps=MAX_SWEEPS):
         return U, S, V
     _jacobi(data, plan, U, S, V, 0, max_sweeps)
     return U, S, V
+
+
+def qr(data, meta, sizes):
+    """Reduced QR of every block with R's diagonal made positive (backend_np.py:511-520):
+    the batched Householder factorisation of yb_svd_qr, then R[:, m:] = Q^H A[:, m:] for
+    wide blocks by a grouped GEMM. Returns (Q, R) flat tensors."""
+    data = _check(data)
+    dev = data.device
+    Q = torch.zeros(sizes[0], dtype=data.dtype, device=dev)
+    R = torch.zeros(sizes[1], dtype=data.dtype, device=dev)
+    plan = P.qr_plan(meta, data.is_complex())
+    nb = len(plan.blocks)
+    if nb == 0:
+        return Q, R
+    (dblocks,) = _dev(plan, 'qr', (plan.blocks,), dev)
+    work = torch.empty(plan.n64, dtype=data.dtype, device=dev)
+    qctrl = torch.zeros(nb + 4 * min(nb, 4096), dtype=torch.int64, device=dev)
+    N.call('yb_qr', _ptr(data), _ptr(Q), _ptr(R), _ptr(work), _ptr(dblocks), nb, _dtype_code(data.dtype),
+           _ptr(qctrl), qctrl.numel(), _stream(), launches=4)
+    run_gemm(plan.right, Q, data, R)
+    if bool(qctrl[nb + 2::4].any()):
+        raise RuntimeError("yastn_gb300 qr: QR group barrier timed out")
+    return Q, R
+
+
+def qr_backward(Q, R, gQ, gR, data, meta):
+    """Adjoint of ``qr`` for float64 blocks (the reduced-QR rule that torch's autograd
+    applies to the reference's torch.linalg.qr + sign fix, backend_torch.py:475-484):
+    dA = (gQ' + Q copyltu(M)) U^{-T}, M = U gU^T - gQ'^T Q, with U = R[:, :k], gU = gR[:, :k],
+    gQ' = gQ + A[:, m:] gR[:, m:]^T and dA[:, m:] = Q gR[:, m:] for wide blocks."""
+    plan = P.qr_plan(meta, Q.is_complex())
+    dev = Q.device
+    dA = torch.zeros(data.numel(), dtype=data.dtype, device=dev)
+    if len(plan.blocks) == 0:
+        return dA
+    Bw = torch.zeros_like(Q) if gQ is None else gQ.contiguous().to(Q.dtype).clone()
+    gR = torch.zeros_like(R) if gR is None else gR.contiguous().to(R.dtype)
+    M = torch.empty(plan.m_size, dtype=Q.dtype, device=dev)
+    run_gemm(plan.w1, data, gR, Bw, beta=1.0)
+    run_gemm(plan.m1, R, gR, M)
+    run_gemm(plan.m2, Bw, Q, M, alpha=-1.0, beta=1.0)
+    (drecs,) = _dev(plan, 'qradj', (plan.adj,), dev)
+    code = _dtype_code(Q.dtype)
+    N.call('yb_qr_adjoint_sym', _ptr(M), _ptr(drecs), len(plan.adj), code, _stream())
+    run_gemm(plan.s1, Q, M, Bw, beta=1.0)
+    N.call('yb_trsm_rt', _ptr(Bw), _ptr(R), _ptr(drecs), len(plan.adj), code, _stream())
+    if not hasattr(plan, 'copy_plan'):
+        plan.copy_plan = P.CopyPlan(plan.copies, sum(int(np.prod(c[2])) for c in plan.copies), data.numel())
+    run_copy(plan.copy_plan, Bw, dA)
+    run_gemm(plan.y1, Q, gR, dA)
+    return dA
 
 
 def svd_backward(U, S, V, gU, gS, gV, meta, data_size, dtype):
