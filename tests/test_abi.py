@@ -49,8 +49,8 @@ def test_invalid_arguments_are_rejected_on_host(lib):
     assert lib.yb_qr(null, null, null, null, null, 1, N.YB_F64, null, 8, null) == N.YB_ERR_INVALID
     assert lib.yb_qr_adjoint_sym(null, null, 1, N.YB_F64, null) == N.YB_ERR_INVALID
     assert lib.yb_trsm_rt(null, null, null, 1, N.YB_C128, null) == N.YB_ERR_INVALID
-    assert lib.yb_svd_finalize(null, null, null, null, null, 1, 0, 10000, 0, null, null, null) == N.YB_ERR_TOO_LARGE
-    assert lib.yb_svd_finalize(null, null, null, null, null, 1, 0, 10, 1, null, null, null) == N.YB_ERR_INVALID
+    assert lib.yb_svd_finalize(null, null, null, null, null, 1, 0, 10000, 0, null, null, null, null) == N.YB_ERR_TOO_LARGE
+    assert lib.yb_svd_finalize(null, null, null, null, null, 1, 0, 10, 1, null, null, null, null) == N.YB_ERR_INVALID
     assert lib.yb_truncation_mask(null, 20000, null, null, 1, 0.0, -1, 0, null, null, null) == N.YB_ERR_TOO_LARGE
     assert lib.yb_fix_signs(null, null, null, null, null, null, 1, 4, 0, 0, null) == N.YB_ERR_INVALID
     assert lib.yb_mask_gather(null, null, 8, null, null, 2, null, 0, null) == N.YB_ERR_INVALID
