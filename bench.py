@@ -62,6 +62,11 @@ def parse():
     p.add_argument('--gemm', default='emulated', choices=['emulated', 'fp64'],
                    help='sector-GEMM mode of the headline (cfg2)')
     p.add_argument('--no-svd', action='store_true', help='skip the extra svd_with_truncation timing')
+    p.add_argument('--chi', type=int, default=24, choices=[24, 144],
+                   help='cfg4: environment dimension of the recorded CTMRG run (144 = the configuration as written)')
+    p.add_argument('--no-plain', action='store_true', help='cfg4: skip the plain per-block GPU path and the host run')
+    p.add_argument('--no-checkpoint', action='store_true',
+                   help='cfg4: keep every CTM move for the backward instead of recomputing it (checkpoint_move)')
     p.add_argument('--headline-only', action='store_true',
                    help='cfg2: run only the headline GEMM mode (for kernel launch lists)')
     return p.parse_args()
@@ -163,14 +168,16 @@ class Cfg5(Cfg1):
 
 class Cfg4:
     """Differentiable CTMRG (forward + backward) from the recorded call sequence."""
-    name = ("differentiable iPEPS CTMRG, 1x1 cell, Z2, D=6, d=2, chi=24, 8 CTM iterations, TFIM h=3 energy "
-            "+ gradient (recorded YASTN call sequence replayed: 32 block SVDs of 2x432^2, 697 dots, "
-            "1045 merges per forward), FP64")
-    metric = "CTMRG fwd+bwd ms (iPEPS Z2 D=6 chi=24, 8 CTM iterations, FP64, <=1e-10 rel)"
 
-    def __init__(self):
+    def __init__(self, chi=24):
         from yastn_gb300.replay import load_replay
-        self.r = load_replay('ctmrg_z2_d6')
+        blocks = {24: "28 block SVDs of 2x432^2", 144: "24 block SVDs of 2x2592^2"}[chi]
+        self.name = (f"differentiable iPEPS CTMRG, 1x1 cell, Z2, D=6, d=2, chi={chi}, 8 CTM iterations, TFIM h=3 "
+                     f"energy + gradient (recorded YASTN call sequence replayed: {blocks} among 32 SVD calls, "
+                     "697 dots, 1045 merges per forward), FP64")
+        self.metric = f"CTMRG fwd+bwd ms (iPEPS Z2 D=6 chi={chi}, 8 CTM iterations, FP64, <=1e-10 rel)"
+        self.r = load_replay('ctmrg_z2_d6' if chi == 24 else f'ctmrg_z2_d6_chi{chi}')
+        self.cpu_recorded = self.r.payload.get('cpu_seconds')
         self.A = self.r.arrays['in:A']
         self.E_ref = self.r.payload['E']
         self.grad_ref = self.r.arrays['ref:grad']
@@ -197,14 +204,17 @@ class Cfg4:
                 bg += sum(g.flops for g in (ap.gP, ap.gQ, ap.gT, ap.gR, ap.gA1, ap.gA2))
         return fg, fs, bg
 
+    checkpoint = True
+
     def step(self, torch, backend, device, A_host=None, pinned=None):
-        """One forward + backward; returns (E, grad) as device tensors."""
+        """One forward + backward (each CTM move under non-reentrant checkpointing, as the
+        recorded run's checkpoint_move, unless ``checkpoint`` is off); returns (E, grad)."""
         if pinned is not None:
             A = pinned.to(device, non_blocking=True)
         else:
             A = torch.from_numpy(self.A).to(device)
         A.requires_grad_(True)
-        env = self.r.run(backend, device, {'A': A})
+        env = self.r.run(backend, device, {'A': A}, checkpoint=self.checkpoint)
         E = env[self.r.outputs['E']]
         E.backward()
         return E.detach(), A.grad
@@ -845,15 +855,16 @@ def run_gpu_cfg4(args, wl):
     clocks = Clocks(local)
     l0 = _native.LAUNCHES[0]
     ts = []
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        E, g = wl.step(torch, BK, dev)
-        e1.record()
-        torch.cuda.synchronize()
-        ts.append(e0.elapsed_time(e1))
+    with SvdSpy(torch) as spy:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            E, g = wl.step(torch, BK, dev)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
     launches = (_native.LAUNCHES[0] - l0) // max(args.steps, 1)
     barrier()
     # end to end: the site tensor from pinned host memory, energy and gradient back to the host
@@ -871,17 +882,19 @@ def run_gpu_cfg4(args, wl):
     e_err, g_err = check(E, g)
     # the same sequence on the plain per-block FP64 path (torch ops, cuSOLVER SVD) on this GPU
     plain = PlainBackend()
-    wl.step(torch, plain, dev)
-    tp = []
-    for _ in range(min(args.steps, 2)):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        Ep, gp = wl.step(torch, plain, dev)
-        torch.cuda.synchronize()
-        tp.append((time.perf_counter() - t0) * 1e3)
-    ep_err, gp_err = check(Ep, gp)
-    roof = svd_roofline(torch, dev, lambda: wl.step(torch, BK, dev))
+    tp, ep_err, gp_err = [float('nan')], None, None
+    if not args.no_plain:
+        wl.step(torch, plain, dev)
+        tp = []
+        for _ in range(min(args.steps, 2)):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            Ep, gp = wl.step(torch, plain, dev)
+            torch.cuda.synchronize()
+            tp.append((time.perf_counter() - t0) * 1e3)
+        ep_err, gp_err = check(Ep, gp)
+    roof = spy.roofline(dev, args.steps)
     t_max, t_e2e = float(np.mean(ts)), float(np.mean(te))
     if world > 1:
         tt = torch.tensor([t_max, t_e2e], dtype=torch.float64, device=dev)
@@ -891,9 +904,15 @@ def run_gpu_cfg4(args, wl):
         if world > 1:
             dist.destroy_process_group()
         return
-    t0 = time.perf_counter()
-    wl.step(torch, plain, 'cpu')
-    cpu_ms = (time.perf_counter() - t0) * 1e3
+    if args.no_plain:  # the reference's own run, recorded on the host that made the fixture
+        rec = wl.cpu_recorded or {}
+        cpu_ms, cpu_kind = (rec.get('forward', float('nan')) + rec.get('backward', float('nan'))) * 1e3, \
+            "reference (recorded run of YASTN's torch backend on 8 x86 threads, not this host)"
+    else:
+        t0 = time.perf_counter()
+        wl.step(torch, plain, 'cpu')
+        cpu_ms = (time.perf_counter() - t0) * 1e3
+        cpu_kind = "one full forward+backward, one torch CPU op per block (LAPACK SVD)"
     fg, fs, bg = wl.flops()
     line = {
         "metric": wl.metric, "value": t_max, "unit": "ms", "n_gpus": world, "steps": args.steps,
@@ -902,17 +921,19 @@ def run_gpu_cfg4(args, wl):
         "data": "synthetic (seeded N(0,1) site tensor; call sequence recorded from YASTN)",
         "config": {"workload": wl.name, "parallelism": f"replicas{world}",
                    "l2": "flushed between timed steps (256 MB write)",
+                   "checkpoint_move": "each CTM move recomputed in the backward (non-reentrant checkpoint)"
+                   if wl.checkpoint else "off: every move's intermediates kept for the backward",
                    "energy_rel_err_vs_reference": e_err, "grad_rel_err_vs_reference": g_err,
                    "plain_per_block_gpu_ms": float(np.mean(tp)),
                    "plain_per_block_gpu": "the same sequence with one torch launch per block, torch.linalg.svd "
                                           "(cuSOLVER), torch autograd + the reference's broadened SVD adjoint",
-                   "plain_over_fused": float(np.mean(tp)) / t_max,
+                   "plain_over_fused": float(np.mean(tp)) / t_max if not args.no_plain else None,
                    "plain_energy_rel_err": ep_err, "plain_grad_rel_err": gp_err,
                    "flop_per_step": {"forward_gemm": fg, "forward_svd_nominal": fs, "backward_gemm": bg},
                    "effective_tflops": (fg + fs + bg) / (t_max * 1e-3) / 1e12},
         "roofline": roof,
-        "cpu_baseline": {"value": cpu_ms, "unit": "ms", "cores": torch.get_num_threads(), "kind": "port",
-                         "sample": "one full forward+backward, one torch CPU op per block (LAPACK SVD)"},
+        "cpu_baseline": {"value": cpu_ms, "unit": "ms", "cores": torch.get_num_threads() if not args.no_plain else 8,
+                         "kind": "port" if not args.no_plain else "reference", "sample": cpu_kind},
         "e2e": {"value": t_e2e, "unit": "ms", "h2d_bytes_per_step": int(pinned.numel() * 8),
                 "d2h_bytes_per_step": int(pinned.numel() * 8 + 8)},
         "gpu_launches": launches,
@@ -923,53 +944,65 @@ def run_gpu_cfg4(args, wl):
         dist.destroy_process_group()
 
 
-def svd_roofline(torch, dev, run_once):
-    """Device time per entry point over one instrumented step and the roofline of the FP64
-    Jacobi sweeps (the FP64 kernel of the block SVDs): algorithmic work per launch =
-    sum over blocks of sweeps x k(k-1)/2 pairs x (12 L + 6 k) real FLOP (three length-L dot
-    products and the rotation of two X rows and two W rows; x4 for complex), against the
-    FP64 rate of this GPU (cuBLAS DGEMM, measured live)."""
-    from yastn_gb300 import _native, ops
-    orig_call, orig_check, orig_jac = _native.call, ops._svd_state_check, ops._jacobi
-    ev, work, cur = {}, [], {}
+class SvdSpy:
+    """Installed around the timed steps: CUDA events around every library call (per entry
+    point) and, for the roofline of the FP64 Jacobi sweeps (the FP64 kernel of the block
+    SVDs), their algorithmic work per launch = sum over blocks of sweeps x k(k-1)/2 pairs x
+    (12 L + 6 k) real FLOP (three length-L dot products and the rotation of two X rows and two
+    W rows; x4 for complex), against the FP64 rate of this GPU (cuBLAS DGEMM, measured live)."""
 
-    def spy(name, *a, **k):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        r = orig_call(name, *a, **k)
-        e1.record()
-        fp64 = (name == 'yb_svd_sweeps' and a[6] == 64) or (name == 'yb_svd_block_sweeps' and a[7] == 64)
-        key = 'fp64_sweeps' if fp64 else name
-        ev.setdefault(key, []).append((e0, e1))
-        return r
+    def __init__(self, torch):
+        from yastn_gb300 import _native, ops
+        self.torch, self.N, self.ops = torch, _native, ops
+        self.ev, self.work, self.cur = {}, [], {}
 
-    def jac(data, plan, *a, **k):
-        cur['kL'] = [(int(r[9]), int(r[10])) for r in plan.blocks]
-        cur['cplx'] = data.is_complex()
-        return orig_jac(data, plan, *a, **k)
+    def __enter__(self):
+        N, ops, torch = self.N, self.ops, self.torch
+        self.orig = (N.call, ops._svd_state_check, ops._jacobi)
+        orig_call, orig_check, orig_jac = self.orig
 
-    def check(state, nb, phase, req):
-        sw = orig_check(state, nb, phase, req)
-        if phase == 'FP64':
-            f = sum(int(s) * k * (k - 1) // 2 * (12 * L + 6 * k) for s, (k, L) in zip(sw, cur['kL']))
-            work.append(f * (4 if cur['cplx'] else 1))
-        return sw
-    _native.call, ops._svd_state_check, ops._jacobi = spy, check, jac
-    try:
-        run_once()
+        def spy(name, *a, **k):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            r = orig_call(name, *a, **k)
+            e1.record()
+            fp64 = (name == 'yb_svd_sweeps' and a[6] == 64) or (name == 'yb_svd_block_sweeps' and a[7] == 64)
+            self.ev.setdefault('fp64_sweeps' if fp64 else name, []).append((e0, e1))
+            return r
+
+        def jac(data, plan, *a, **k):
+            self.cur['kL'] = [(int(r[9]), int(r[10])) for r in plan.blocks]
+            self.cur['cplx'] = data.is_complex()
+            return orig_jac(data, plan, *a, **k)
+
+        def check(state, nb, phase, req):
+            sw = orig_check(state, nb, phase, req)
+            if phase == 'FP64':
+                f = sum(int(x) * k * (k - 1) // 2 * (12 * L + 6 * k) for x, (k, L) in zip(sw, self.cur['kL']))
+                self.work.append(f * (4 if self.cur['cplx'] else 1))
+            return sw
+        N.call, ops._svd_state_check, ops._jacobi = spy, check, jac
+        return self
+
+    def __exit__(self, *exc):
+        self.N.call, self.ops._svd_state_check, self.ops._jacobi = self.orig
+        return False
+
+    def roofline(self, dev, steps):
+        torch = self.torch
         torch.cuda.synchronize()
-    finally:
-        _native.call, ops._svd_state_check, ops._jacobi = orig_call, orig_check, orig_jac
-    tot = {k: sum(a.elapsed_time(b) for a, b in v) * 1e-3 for k, v in ev.items()}
-    t64 = tot.get('fp64_sweeps', 0.0)
-    n64 = len(ev.get('fp64_sweeps', []))
-    peak = fp64_peak_tflops(torch, dev)
-    achieved = sum(work) / t64 / 1e12 if t64 > 0 else 0.0
-    return {"bound": "fp64", "kernel": "Jacobi FP64 phase (yb_svd_block_sweeps / yb_svd_sweeps)",
-            "achieved": achieved, "peak": peak,
-            "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": "measured live: cuBLAS DGEMM 4096^3",
-            "traffic": None, "launches": n64, "ms_per_launch": t64 / max(n64, 1) * 1e3,
-            "device_ms_per_step": {k: v * 1e3 for k, v in sorted(tot.items(), key=lambda x: -x[1])[:8]}}
+        tot = {k: sum(a.elapsed_time(b) for a, b in v) * 1e-3 / steps for k, v in self.ev.items()}
+        t64 = tot.get('fp64_sweeps', 0.0)
+        n64 = len(self.ev.get('fp64_sweeps', [])) // steps
+        work = sum(self.work) / steps
+        peak = fp64_peak_tflops(torch, dev)
+        achieved = work / t64 / 1e12 if t64 > 0 else 0.0
+        return {"bound": "fp64", "kernel": "Jacobi FP64 phase (yb_svd_block_sweeps / yb_svd_sweeps)",
+                "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": "measured live: cuBLAS DGEMM 4096^3",
+                "traffic": None, "launches": n64, "ms_per_launch": t64 / max(n64, 1) * 1e3,
+                "measured": "CUDA events around every library call over the timed steps",
+                "device_ms_per_step": {k: v * 1e3 for k, v in sorted(tot.items(), key=lambda x: -x[1])[:8]}}
 
 
 def kernel_roofline(torch, dev, run_once, w, gemm_mode, reps=5):
@@ -1031,7 +1064,10 @@ def kernel_roofline(torch, dev, run_once, w, gemm_mode, reps=5):
 
 def main():
     args = parse()
-    wl = {'cfg1': Cfg1, 'cfg2': Cfg2, 'cfg3': Cfg3, 'cfg4': Cfg4, 'cfg5': Cfg5}[args.workload]()
+    wl = Cfg4(args.chi) if args.workload == 'cfg4' else \
+        {'cfg1': Cfg1, 'cfg2': Cfg2, 'cfg3': Cfg3, 'cfg5': Cfg5}[args.workload]()
+    if args.workload == 'cfg4':
+        wl.checkpoint = not args.no_checkpoint
     if args.impl == 'reference':
         run_reference(args, wl)
     elif args.workload == 'cfg2':

@@ -52,3 +52,16 @@ def test_ctmrg_gradient_finite_differences(replay, cuda_device):
             # the central difference carries O(h^2) truncation and the SVD adjoint the 1e-12
             # broadening: agreement to 1e-7 of the gradient norm (d is a unit vector)
             assert abs(fd - an) <= 1e-7 * float(g.norm()), (fd, an)
+
+
+def test_ctmrg_checkpointed_moves_match_reference(replay, cuda_device):
+    """The same run with every CTM move under non-reentrant checkpointing (the recorded
+    checkpoint_move markers): identical energy, and the gradient through the recomputed
+    moves matches the reference's."""
+    A = torch.from_numpy(replay.arrays['in:A']).cuda().requires_grad_(True)
+    env = replay.run(BK, 'cuda', {'A': A}, checkpoint=True)
+    E = env[replay.outputs['E']]
+    assert abs(float(E.detach()) - replay.payload['E']) <= 1e-10 * abs(replay.payload['E'])
+    E.backward()
+    g, ref = A.grad.cpu().numpy(), replay.arrays['ref:grad']
+    assert np.abs(g - ref).max() <= 1e-8 * np.abs(ref).max()

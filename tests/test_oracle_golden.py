@@ -265,6 +265,23 @@ def test_oracle_qr_and_adjoint_match_reference():
     assert n_adj == 2
 
 
+def test_ctmrg_checkpoint_segments():
+    """The checkpoint segments of the CTMRG recording: 16 CTM moves, each with its inputs
+    produced before it and its outputs read after it (or results)."""
+    import torch
+    from yastn_gb300.replay import load_replay
+    r = load_replay('ctmrg_z2_d6')
+    segs = r._segments(torch.device('cpu'))
+    ck = [s for s in segs if s[0] == 'ckpt']
+    assert len(ck) == 16
+    assert all(len(ins) > 0 and len(outs) > 0 for _, _, _, ins, outs, _ in ck)
+    # the segments and plain runs tile the op list in order
+    pos = 0
+    for kind, a, b, *_ in segs:
+        assert 0 <= a - pos <= 2 and b >= a  # markers between runs are skipped
+        pos = b
+
+
 def test_ctmrg_recording_dataflow_is_closed():
     """The recorded CTMRG sequence only uses tensors it produced, its input or its stored
     constants, and its output (the energy) is produced by it."""

@@ -17,6 +17,7 @@ import os
 
 import numpy as np
 import torch
+import torch.utils.checkpoint
 
 from .workloads import GOLDEN
 
@@ -54,19 +55,44 @@ class CallReplay:
                 out[op['fn']] = out.get(op['fn'], 0) + 1
         return out
 
-    def run(self, backend, device, inputs, constants_dtype=None):
+    def run(self, backend, device, inputs, constants_dtype=None, checkpoint=False):
         """Execute the sequence. ``inputs`` maps recorded input names to tensors; returns the
         dict of every produced tensor by key (outputs under ``self.outputs``).
 
         The recorded arguments are decoded once per device (``_compiled``): metadata and other
         tensor-free arguments become the same Python objects on every run (so the backend's
-        plan caches hit by identity), tensor references are resolved per run."""
+        plan caches hit by identity), tensor references are resolved per run.
+
+        ``checkpoint``: the segments the recording marks (YASTN's per-CTM-move checkpoint,
+        ``checkpoint_move``) run under ``torch.utils.checkpoint`` (non-reentrant): only their
+        inputs and the tensors used after them are kept for the backward, which recomputes
+        each segment; tensors a segment writes in place are cloned inside it first."""
         dev = torch.device(device)
         env = {}
         for name, key in self.inputs.items():
             env[key] = inputs[name]
         consts = {}
+        ops = self._compiled(dev)
+        if not checkpoint:
+            self._exec(ops, 0, len(ops), env, consts, backend, dev)
+            return env
+        i = 0
+        for kind, a, b, ins, outs, inplace in self._segments(dev):
+            if kind == 'plain':
+                self._exec(ops, a, b, env, consts, backend, dev)
+                continue
 
+            def seg(*tensors, a=a, b=b, ins=ins, outs=outs, inplace=inplace):
+                local = dict(zip(ins, tensors))
+                for k in inplace:
+                    local[k] = local[k].clone()
+                self._exec(ops, a, b, local, consts, backend, dev)
+                return tuple(local[k] for k in outs)
+            res = torch.utils.checkpoint.checkpoint(seg, *[env[k] for k in ins], use_reentrant=False)
+            env.update(zip(outs, res))
+        return env
+
+    def _exec(self, ops, a, b, env, consts, backend, dev):
         def tensor(k):
             t = env.get(k)
             if t is None:
@@ -96,10 +122,10 @@ class CallReplay:
                 return tensor(v)
             return dec(v)
 
-        for kind, fn, aspec, kwspec, keys in self._compiled(dev):
+        for kind, fn, aspec, kwspec, keys in ops[a:b]:
             if kind == 'mark':
                 continue
-            args = tuple(arg(a) for a in aspec)
+            args = tuple(arg(x) for x in aspec)
             kwargs = {k: arg(v) for k, v in kwspec.items()}
             if kind == 'b':
                 out = getattr(backend, fn)(*args, **kwargs)
@@ -113,7 +139,69 @@ class CallReplay:
                         env[k] = v
             else:
                 env[keys] = out
-        return env
+
+    def _segments(self, dev):
+        """[(kind, start, stop, inputs, outputs, in-place targets)] over the compiled ops:
+        'plain' runs of ops and 'ckpt' segments between checkpoint markers. A segment's inputs
+        are the tensors it reads that an earlier op (or the caller) produced; its outputs the
+        tensors it produces (or writes in place) that a later op reads or that are results."""
+        key = str(dev)
+        cache = self.__dict__.setdefault('_segments_by_dev', {})
+        if key in cache:
+            return cache[key]
+        ops = self._compiled(dev)
+        reads, writes = [], []
+        for kind, fn, aspec, kwspec, keys in ops:
+            r = set()
+            if kind != 'mark':
+                for sp in list(aspec) + list(kwspec.values()):
+                    _refs(sp, r)
+            w = set()
+            if isinstance(keys, list):
+                w.update(k for k in keys if k is not None)
+            elif keys is not None:
+                w.add(keys)
+            if kind == 't' and fn == 'm:__setitem__' and aspec[0][0] == 'r':
+                w.add(aspec[0][1])
+            reads.append(r)
+            writes.append(w)
+        later = [set() for _ in range(len(ops) + 1)]  # keys read at or after op i
+        for i in range(len(ops) - 1, -1, -1):
+            later[i] = later[i + 1] | reads[i]
+        results = set(self.outputs.values())
+        segs, i, start = [], 0, 0
+        produced = set(self.inputs.values())
+        while i < len(ops):
+            if ops[i][0] == 'mark' and ops[i][1] == 'checkpoint_begin':
+                j = i + 1
+                while not (ops[j][0] == 'mark' and ops[j][1] == 'checkpoint_end'):
+                    j += 1
+                if start < i:
+                    segs.append(('plain', start, i, (), (), ()))
+                made, ins, inplace = set(), [], []
+                for t in range(i + 1, j):
+                    for k in sorted(reads[t]):
+                        if k not in made and k in produced and k not in ins:
+                            ins.append(k)
+                    for k in sorted(writes[t]):
+                        if k in produced and k not in made and k not in inplace:
+                            inplace.append(k)
+                        made.add(k)
+                outs = sorted(k for k in made if k in later[j + 1] or k in results)
+                for k in inplace:
+                    if k not in ins:
+                        ins.append(k)
+                segs.append(('ckpt', i + 1, j, tuple(ins), tuple(outs), tuple(inplace)))
+                produced |= made
+                i = start = j + 1
+                continue
+            for w in writes[i]:
+                produced.add(w)
+            i += 1
+        if start < len(ops):
+            segs.append(('plain', start, len(ops), (), (), ()))
+        cache[key] = segs
+        return segs
 
     def _compiled(self, dev):
         key = str(dev)
@@ -130,6 +218,26 @@ class CallReplay:
                            {k: spec(v) for k, v in op.get('kw', {}).items()}, op.get('o'))
                           for op in self.ops]
         return cache[key]
+
+
+def _refs(spec, out):
+    kind, v = spec
+    if kind == 'r':
+        out.add(v)
+    elif kind == 'd':
+        _collect_refs(v, out)
+
+
+def _collect_refs(x, out):
+    if isinstance(x, list):
+        for y in x:
+            _collect_refs(y, out)
+    elif isinstance(x, dict):
+        if '__t__' in x:
+            out.add(x['__t__'])
+        else:
+            for v in x.values():
+                _collect_refs(v, out)
 
 
 def _has_ref(x):
