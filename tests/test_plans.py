@@ -418,6 +418,61 @@ def test_qr_adjoint_plan_reproduces_oracle():
     assert np.abs(dA - ref).max() <= 1e-12 * np.abs(ref).max()
 
 
+@pytest.mark.parametrize('qr_start', [False, True])
+def test_completion_plans_orthonormal_completion(qr_start):
+    """The blocked completion's records (candidate fill, the two projection GEMMs, the QR of
+    the candidates, the copy into the factor) applied with numpy: the factor's last nz
+    vectors of each block become orthonormal and orthogonal to the earlier ones, which stay
+    untouched."""
+    rng = np.random.default_rng(10)
+    shapes = [(30, 12), (9, 26), (20, 20), (7, 3)]
+    meta, oU, oS, oV, off = [], 0, 0, 0, 0
+    for m, n in shapes:
+        k = min(m, n)
+        meta.append(((off, off + m * n), (m, n), (oU, oU + m * k), (m, k), (oS, oS + k), (oV, oV + k * n), (k, n)))
+        off += m * n; oU += m * k; oS += k; oV += k * n
+    meta = tuple(meta)
+    plan = P.svd_plan(meta, None, False, qr=qr_start)
+    nz = [5, 4, 20, 1]  # the third block: every vector completed
+    U, V = np.zeros(oU), np.zeros(oV)
+    for r, z in zip(plan.blocks, nz):  # orthonormal leading vectors, zeros at the completed ones
+        m, n, k, tall, from_r = int(r[1]), int(r[2]), int(r[9]), bool(r[12]), bool(r[16])
+        to_u = tall != from_r
+        Lv = m if to_u else n
+        q, _ = np.linalg.qr(rng.normal(size=(Lv, k)))
+        q[:, k - z:] = 0
+        if to_u:
+            U[int(r[3]):int(r[3]) + m * k] = q.ravel()
+        else:
+            V[int(r[5]):int(r[5]) + k * n] = q.T.ravel()
+    U0, V0 = U.copy(), V.copy()
+    for cp in P.completion_plans(plan.blocks, nz):
+        F = U if cp.to_u else V
+        G = np.zeros(cp.G)
+        for g0, cnt in cp.fill:
+            G[g0:g0 + cnt] = rng.uniform(-1, 1, size=cnt)
+        C = np.zeros(max(cp.C, 1))
+        for _ in range(2):
+            PI.run_gemm(cp.g1, F, G, C)
+            PI.run_gemm(cp.g2, F, C, G, alpha=-1.0, beta=1.0)
+        Qc = np.zeros(cp.Q)
+        for sl, D, slQ, DQ, slR, DR in cp.meta:
+            q, _ = np.linalg.qr(G[sl[0]:sl[1]].reshape(D))
+            Qc[slQ[0]:slQ[1]] = q.ravel()
+        for so, do, sizes, ss, ds in cp.copy.tasks_list:
+            for i in range(sizes[0]):
+                for j in range(sizes[1]):
+                    F[do + i * ds[0] + j * ds[1]] = Qc[so + i * ss[0] + j * ss[1]]
+    for r, z, (sl, D, slU, DU, slS, slV, DV) in zip(plan.blocks, nz, meta):
+        u, vh = U[slU[0]:slU[1]].reshape(DU), V[slV[0]:slV[1]].reshape(DV)
+        u0, vh0 = U0[slU[0]:slU[1]].reshape(DU), V0[slV[0]:slV[1]].reshape(DV)
+        k = DU[1]
+        to_u = bool(r[12]) != bool(r[16])
+        f, f0 = (u, u0) if to_u else (vh.T, vh0.T)
+        assert np.abs(f.T @ f - np.eye(k)).max() < 1e-13
+        np.testing.assert_array_equal(f[:, :k - z], f0[:, :k - z])
+
+
 def test_mixed_precision_jacobi_schedule_complex():
     """Complex blocks: FP32 phase on complex64 rows with phase-aligned rotations, widen,
     Newton-Schulz with T = W^H W, X = W X_0 (X_0 = A^H for tall blocks), FP64 phase; the

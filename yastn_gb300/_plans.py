@@ -795,6 +795,57 @@ def qr_plan(meta, cplx=False):
     return CACHE.get((meta,), ('qr', cplx), build)
 
 
+class CompletionPlan:
+    """Blocked completion of the vectors of small singular values for one factor (U columns
+    when ``to_u``, else Vh rows): candidate fill records (offset, count), the grouped-GEMM
+    projections C = V_g^H G (g1) and G -= V_g C (g2), the QR records of the candidates, and
+    the copy of the orthonormalised candidates into the factor."""
+
+    def __init__(self, to_u, g1, g2, meta, fill, copy, sizes):
+        self.to_u, self.g1, self.g2, self.meta, self.fill, self.copy = to_u, g1, g2, meta, fill, copy
+        self.G, self.C, self.Q, self.R = sizes
+        self._dev = {}
+
+
+def completion_plans(blocks, nz, cplx=False):
+    """Completion plans of svd records ``blocks`` (SVD_REC) for the per-block counts ``nz`` of
+    vectors to complete (the last nz of each block's k). The vectors built from X's rows are
+    U's columns for tall blocks started from A's rows and for wide blocks started from R's,
+    else Vh's rows; V_g are the k - nz vectors before them."""
+    by_target = {}
+    for b, r in enumerate(blocks):
+        z = int(nz[b])
+        if z == 0:
+            continue
+        m, n, k, tall, from_r = int(r[1]), int(r[2]), int(r[9]), bool(r[12]), bool(r[16])
+        to_u = tall != from_r
+        if to_u:
+            f0, sv, sj, Lv = int(r[3]), k, 1, m
+        else:
+            f0, sv, sj, Lv = int(r[5]), 1, n, n
+        j0 = k - z
+        t = by_target.setdefault(to_u, {'g1': [], 'g2': [], 'meta': [], 'fill': [], 'copies': [],
+                                        'G': 0, 'C': 0, 'Q': 0, 'R': 0})
+        g, c_, q_, r_ = t['G'], t['C'], t['Q'], t['R']
+        if j0 > 0:
+            t['g1'].append((c_, j0, z, z, [(f0, g, Lv, sj, sv, z, 1, int(cplx))]))
+            t['g2'].append((g, Lv, z, z, [(f0, c_, j0, sv, sj, z, 1, 0)]))
+        t['meta'].append(((g, g + Lv * z), (Lv, z), (q_, q_ + Lv * z), (Lv, z), (r_, r_ + z * z), (z, z)))
+        t['fill'].append((g, Lv * z))
+        t['copies'].append((q_, f0 + j0 * sj, [Lv, z], [z, 1], [sv, sj]))
+        t['G'] += Lv * z
+        t['C'] += j0 * z
+        t['Q'] += Lv * z
+        t['R'] += z * z
+    out = []
+    for to_u, t in by_target.items():
+        out.append(CompletionPlan(to_u, _pack_gemm(t['g1']), _pack_gemm(t['g2']), tuple(t['meta']),
+                                  np.array(t['fill'], dtype=np.int64).reshape(-1, 2),
+                                  CopyPlan(t['copies'], sum(int(np.prod(c[2])) for c in t['copies']), 0),
+                                  (t['G'], t['C'], t['Q'], t['R'])))
+    return out
+
+
 class SvdAdjointPlan:
     def __init__(self, recs, kk, tr, gP, gQ, gT, gR, gA1, gA2):
         self.recs, self.kk, self.tr = recs, kk, tr

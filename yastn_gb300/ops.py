@@ -397,50 +397,22 @@ def _complete(plan, U, V, nz, cplx):
     (yb_fill_candidates), projected twice off the k - nz earlier vectors by grouped GEMMs
     (C = V_g^H G, G -= V_g C), orthonormalised by the batched Householder QR, and copied into
     the factor's last nz vectors (U columns or Vh rows, whichever the rows of X built)."""
-    key = (tuple(int(x) for x in nz),)
+    key = tuple(int(x) for x in nz)
     cache = plan.__dict__.setdefault('_completion', {})
     if key not in cache:
-        by_target = {}
-        goff = coff = 0
-        for b, r in enumerate(plan.blocks):
-            z = int(nz[b])
-            if z == 0:
-                continue
-            m, n, k, tall, from_r = int(r[1]), int(r[2]), int(r[9]), bool(r[12]), bool(r[16])
-            to_u = tall != from_r
-            if to_u:
-                f0, sv, sj, Lv = int(r[3]), k, 1, m
-            else:
-                f0, sv, sj, Lv = int(r[5]), 1, n, n
-            j0 = k - z
-            t = by_target.setdefault(to_u, {'g1': [], 'g2': [], 'meta': [], 'fill': [], 'copies': [],
-                                            'G': 0, 'C': 0, 'Q': 0, 'R': 0})
-            g, c_, q_, r_ = t['G'], t['C'], t['Q'], t['R']
-            if j0 > 0:
-                t['g1'].append((c_, j0, z, z, [(f0, g, Lv, sj, sv, z, 1, int(cplx))]))
-                t['g2'].append((g, Lv, z, z, [(f0, c_, j0, sv, sj, z, 1, 0)]))
-            t['meta'].append(((g, g + Lv * z), (Lv, z), (q_, q_ + Lv * z), (Lv, z), (r_, r_ + z * z), (z, z)))
-            t['fill'].append((g, Lv * z))
-            t['copies'].append((q_, f0 + j0 * sj, [Lv, z], [z, 1], [sv, sj]))
-            t['G'] += Lv * z; t['C'] += j0 * z; t['Q'] += Lv * z; t['R'] += z * z
-        for t in by_target.values():
-            t['g1'], t['g2'] = P._pack_gemm(t['g1']), P._pack_gemm(t['g2'])
-            t['meta'] = tuple(t['meta'])
-            t['fill'] = np.array(t['fill'], dtype=np.int64).reshape(-1, 2)
-            t['copy'] = P.CopyPlan(t['copies'], sum(int(np.prod(c[2])) for c in t['copies']), 0)
-        cache[key] = by_target
+        cache[key] = P.completion_plans(plan.blocks, nz, cplx)
     dev = U.device
-    for to_u, t in cache[key].items():
-        F = U if to_u else V
-        G = torch.empty(max(t['G'], 1), dtype=F.dtype, device=dev)
-        C = torch.empty(max(t['C'], 1), dtype=F.dtype, device=dev)
-        N.call('yb_fill_candidates', _ptr(G), _ptr(_dev(t['g1'], 'fill', (t['fill'],), dev)[0]), len(t['fill']),
-               _dtype_code(F.dtype), _stream())
+    for cp in cache[key]:
+        F = U if cp.to_u else V
+        G = torch.empty(max(cp.G, 1), dtype=F.dtype, device=dev)
+        C = torch.empty(max(cp.C, 1), dtype=F.dtype, device=dev)
+        (dfill,) = _dev(cp, 'fill', (cp.fill,), dev)
+        N.call('yb_fill_candidates', _ptr(G), _ptr(dfill), len(cp.fill), _dtype_code(F.dtype), _stream())
         for _ in range(2):
-            run_gemm(t['g1'], F, G, C)
-            run_gemm(t['g2'], F, C, G, alpha=-1.0, beta=1.0)
-        Qc, _ = qr(G, t['meta'], (max(t['Q'], 1), max(t['R'], 1)))
-        run_copy(t['copy'], Qc, F)
+            run_gemm(cp.g1, F, G, C)
+            run_gemm(cp.g2, F, C, G, alpha=-1.0, beta=1.0)
+        Qc, _ = qr(G, cp.meta, (max(cp.Q, 1), max(cp.R, 1)))
+        run_copy(cp.copy, Qc, F)
 
 
 def svd(data, meta, sizes, max_sweeps=MAX_SWEEPS):
