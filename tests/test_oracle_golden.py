@@ -265,6 +265,23 @@ def test_oracle_qr_and_adjoint_match_reference():
     assert n_adj == 2
 
 
+def test_ctmrg_checkpointed_replay_on_host_reproduces_reference():
+    """The chi=24 CTMRG sequence replayed on the host with the plain per-block torch backend
+    and each CTM move checkpointed: the reference's energy bit for bit and its gradient (the
+    recomputed moves feed the backward)."""
+    import torch
+    from yastn_gb300.plain import PlainBackend
+    from yastn_gb300.replay import load_replay
+    r = load_replay('ctmrg_z2_d6')
+    A = torch.from_numpy(r.arrays['in:A'].copy()).requires_grad_(True)
+    env = r.run(PlainBackend(), 'cpu', {'A': A}, checkpoint=True)
+    E = env[r.outputs['E']]
+    assert float(E.detach()) == r.payload['E']
+    E.backward()
+    g, ref = A.grad.numpy(), r.arrays['ref:grad']
+    assert np.abs(g - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
 def test_ctmrg_checkpoint_segments():
     """The checkpoint segments of the CTMRG recording: 16 CTM moves, each with its inputs
     produced before it and its outputs read after it (or results)."""
