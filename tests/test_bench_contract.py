@@ -1,0 +1,41 @@
+"""The benchmark's reference arm on the host cores (no GPU): one JSON line with the keys of
+the benchmark contract, for the default workload (DMRG Heff2 Lanczos), the tensordot
+workload and the CTMRG workload (its per-move checkpointed replay on the plain per-block
+torch path)."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+KEYS = {"metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+        "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e", "impl"}
+
+
+def _run(*args):
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+    res = subprocess.run([sys.executable, os.path.join(ROOT, 'bench.py'), '--impl', 'reference', *args],
+                         capture_output=True, text=True, timeout=600, env=env, cwd=ROOT)
+    assert res.returncode == 0, res.stderr[-2000:]
+    lines = [ln for ln in res.stdout.splitlines() if ln.startswith('{')]
+    assert len(lines) == 1
+    return json.loads(lines[0])
+
+
+@pytest.mark.parametrize('args', [
+    ('--steps', '1', '--warmup', '0'),
+    ('--workload', 'cfg1', '--steps', '1', '--warmup', '0'),
+    ('--workload', 'cfg4', '--steps', '1', '--warmup', '0'),
+])
+def test_reference_arm_line(args):
+    line = _run(*args)
+    assert KEYS <= set(line)
+    assert line["impl"] == "reference"
+    assert line["value"] > 0 and line["e2e"]["value"] == line["value"]
+    assert line["cpu_baseline"]["value"] == line["value"] and line["cpu_baseline"]["cores"] >= 1
+    assert isinstance(line["config"]["workload"], str)
+    if '--workload' in args and args[args.index('--workload') + 1] == 'cfg4':
+        assert line["unit"] == "ms" and line["higher_is_better"] is False
+        assert line["config"]["energy_rel_err_vs_reference"] <= 1e-12
