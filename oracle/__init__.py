@@ -6,7 +6,7 @@ This package restates, in plain NumPy/SciPy, the reference YASTN NumPy backend
 (``yastn/backend/_backend_torch_backwards.py``,
 ``yastn/backend/linalg/torch_svd_gesdd.py``, ``yastn/backend/linalg/torch_eig_sym.py``).
 
-It is the checker, never the product: only ``tests/``, ``__graft_entry__.smoke()``
+It checks results and is never the product: only ``tests/``, ``__graft_entry__.smoke()``
 and the ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import it.
 The GPU backend in ``yastn_gb300`` never calls into this package.
 
