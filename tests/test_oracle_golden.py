@@ -299,11 +299,12 @@ def test_ctmrg_checkpoint_segments():
         pos = b
 
 
-def test_ctmrg_recording_dataflow_is_closed():
-    """The recorded CTMRG sequence only uses tensors it produced, its input or its stored
-    constants, and its output (the energy) is produced by it."""
+@pytest.mark.parametrize('name', ['ctmrg_z2_d6', 'ctmrg_z2_d6_chi144'])
+def test_ctmrg_recording_dataflow_is_closed(name):
+    """The recorded CTMRG sequences (chi = 24 and 144) only use tensors they produced, their
+    input or their stored constants, and their output (the energy) is produced by them."""
     from yastn_gb300.replay import load_replay, check_dataflow
-    r = load_replay('ctmrg_z2_d6')
+    r = load_replay(name)
     n, used = check_dataflow(r)
     produced = set()
     for op in r.ops:
