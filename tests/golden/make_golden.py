@@ -852,7 +852,7 @@ class OpRecorder:
         self.active = False
 
 
-def scen_ctmrg(chi=24, sweeps=8, name='ctmrg_z2_d6'):
+def scen_ctmrg(chi=24, sweeps=8, name='ctmrg_z2_d6', use_qr=False):
     """Differentiable CTMRG of an iPEPS on a 1x1 unit cell (yastn.tn.fpeps): Z2 symmetry,
     site tensor with bond D=6 (3+3 over parities) and physical d=2 (1+1), rand(normal) after
     random_seed(0); EnvCTM(init='eye'), ctmrg_ with D_total=chi for a fixed number of sweeps
@@ -880,7 +880,7 @@ def scen_ctmrg(chi=24, sweeps=8, name='ctmrg_z2_d6'):
     with rec:
         psi = fpeps.Peps(fpeps.SquareLattice(dims=(1, 1), boundary='infinite'), tensors={(0, 0): A})
         env = fpeps.EnvCTM(psi, init='eye', leg=yastn.Leg(cfg, s=1, t=(0, 1), D=(1, 1)))
-        for _ in env.ctmrg_(opts_svd={'D_total': chi}, max_sweeps=sweeps, iterator=True, use_qr=False,
+        for _ in env.ctmrg_(opts_svd={'D_total': chi}, max_sweeps=sweeps, iterator=True, use_qr=use_qr,
                             checkpoint_move='nonreentrant'):
             pass
         ez = env.measure_1site(Z)
@@ -897,7 +897,7 @@ def scen_ctmrg(chi=24, sweeps=8, name='ctmrg_z2_d6'):
     arrays['in:A'] = A._data.detach().numpy().copy()
     arrays['ref:grad'] = grad
     payload = {'scenario': name, 'ops': rec.ops, 'inputs': {'A': 'in:A'}, 'outputs': {'E': ekey},
-               'E': float(E.detach()), 'chi': chi, 'sweeps': sweeps, 'D': 6, 'h': 3.0,
+               'E': float(E.detach()), 'chi': chi, 'sweeps': sweeps, 'D': 6, 'h': 3.0, 'use_qr': use_qr,
                'cpu_seconds': {'forward': t_fwd, 'backward': t_bwd}}
     with open(os.path.join(HERE, name + '.json'), 'w') as f:
         json.dump(payload, f, separators=(',', ':'))
@@ -909,6 +909,12 @@ def scen_ctmrg(chi=24, sweeps=8, name='ctmrg_z2_d6'):
 
 def _arr_from(rec, x):
     return rec.arrays[x['__array__']]
+
+
+def scen_ctmrg_qr():
+    """The chi=24 CTMRG scenario with YASTN's default projector path use_qr=True (QR of each
+    half-system, then the SVD of the product of the R factors)."""
+    scen_ctmrg(name='ctmrg_z2_d6_qr', use_qr=True)
 
 
 def scen_ctmrg_chi144():
@@ -938,4 +944,5 @@ elif __name__ == '__main__':
     scen_cfg3()
     scen_cfg5()
     scen_ctmrg()
+    scen_ctmrg_qr()
     scen_ctmrg_chi144()

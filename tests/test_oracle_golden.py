@@ -282,6 +282,27 @@ def test_ctmrg_checkpointed_replay_on_host_reproduces_reference():
     assert np.abs(g - ref).max() <= 1e-10 * np.abs(ref).max()
 
 
+def test_ctmrg_use_qr_replay_on_host_reproduces_reference():
+    """YASTN's default projector path (use_qr=True: a QR of each half-system, then the SVD of
+    the product of the R factors) replayed on the host with the plain per-block backend and
+    checkpointed moves: the reference's energy and gradient."""
+    import torch
+    from yastn_gb300.plain import PlainBackend
+    from yastn_gb300.replay import load_replay
+    r = load_replay('ctmrg_z2_d6_qr')
+    assert r.backend_calls()['qr'] > 0
+    A = torch.from_numpy(r.arrays['in:A'].copy()).requires_grad_(True)
+    env = r.run(PlainBackend(), 'cpu', {'A': A}, checkpoint=True)
+    E = env[r.outputs['E']]
+    assert abs(float(E.detach()) - r.payload['E']) <= 1e-12 * abs(r.payload['E'])
+    E.backward()
+    g, ref = A.grad.numpy(), r.arrays['ref:grad']
+    # the half-systems are rank-deficient: the QR adjoint's R^-T amplifies the rounding
+    # differences between two evaluations of the same sequence (1.6e-6 measured here; the
+    # reference's own gradient tests hold CTM gradients to 1e-3, tests/peps/test_ad.py:286)
+    assert np.abs(g - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
 def test_ctmrg_checkpoint_segments():
     """The checkpoint segments of the CTMRG recording: 16 CTM moves, each with its inputs
     produced before it and its outputs read after it (or results)."""
@@ -299,7 +320,7 @@ def test_ctmrg_checkpoint_segments():
         pos = b
 
 
-@pytest.mark.parametrize('name', ['ctmrg_z2_d6', 'ctmrg_z2_d6_chi144'])
+@pytest.mark.parametrize('name', ['ctmrg_z2_d6', 'ctmrg_z2_d6_chi144', 'ctmrg_z2_d6_qr'])
 def test_ctmrg_recording_dataflow_is_closed(name):
     """The recorded CTMRG sequences (chi = 24 and 144) only use tensors they produced, their
     input or their stored constants, and their output (the energy) is produced by them."""
@@ -312,4 +333,6 @@ def test_ctmrg_recording_dataflow_is_closed(name):
         produced.update(o if isinstance(o, list) else [o])
     assert r.outputs['E'] in produced and 'in:A' in used
     calls = r.backend_calls()
-    assert calls['svd'] == 32 and calls['dot'] == 697 and calls['transpose_and_merge'] == 1045
+    assert calls['svd'] == 32 and calls['dot'] == 697
+    assert calls['transpose_and_merge'] == (1109 if name.endswith('_qr') else 1045)
+    assert calls.get('qr', 0) == (64 if name.endswith('_qr') else 0)

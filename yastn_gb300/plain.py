@@ -6,7 +6,8 @@ yastn/backend/backend_torch.py), but every hot function loops over the blocks on
 and issues one torch launch per block — a permute-copy per merged piece
 (backend_torch.py:518-531), one ``matmul`` per sector GEMM (backend_torch.py:466-473),
 one ``torch.linalg.svd`` per block (cuSOLVER on the GPU, LAPACK on the host;
-backend_torch.py:318-319) — and autograd differentiates the torch operations themselves
+backend_torch.py:318-319), one ``torch.linalg.qr`` per block with the sign fix
+(backend_torch.py:475-484) — and autograd differentiates the torch operations themselves
 (the SVD through the reference's broadened adjoint, evaluated per block).
 Everything that is not on the hot path is taken from ``yastn_gb300.backend`` unchanged.
 It runs on any torch device, so the same object is the plain GPU path and the host-core
@@ -137,6 +138,18 @@ class PlainBackend:
     @staticmethod
     def svd(data, meta, sizes, fullrank_uv=False, ad_decomp_reg=1.0e-12, diagnostics=None, **kwargs):
         return _PlainSvd.apply(data, meta, sizes, ad_decomp_reg)
+
+    @staticmethod
+    def qr(data, meta, sizes):
+        Q = torch.zeros(sizes[0], dtype=data.dtype, device=data.device)
+        R = torch.zeros(sizes[1], dtype=data.dtype, device=data.device)
+        for sl, D, slQ, DQ, slR, DR in meta:
+            q, r = torch.linalg.qr(data[_sl(sl)].view(D))
+            sr = torch.sign(torch.real(torch.diagonal(r)))
+            sr = torch.where(sr == 0, torch.ones_like(sr), sr).to(data.dtype)
+            Q[_sl(slQ)].view(DQ)[...] = q * sr.reshape(1, -1)
+            R[_sl(slR)].view(DR)[...] = sr.reshape(-1, 1) * r
+        return Q, R
 
     @staticmethod
     def fix_svd_signs(Udata, Vhdata, meta):
