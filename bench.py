@@ -64,6 +64,8 @@ def parse():
     p.add_argument('--no-svd', action='store_true', help='skip the extra svd_with_truncation timing')
     p.add_argument('--chi', type=int, default=24, choices=[24, 144],
                    help='cfg4: environment dimension of the recorded CTMRG run (144 = the configuration as written)')
+    p.add_argument('--use-qr', action='store_true',
+                   help="cfg4 (chi=24): YASTN's default projector path use_qr=True (QR of each half-system)")
     p.add_argument('--no-plain', action='store_true', help='cfg4: skip the plain per-block GPU path and the host run')
     p.add_argument('--no-checkpoint', action='store_true',
                    help='cfg4: keep every CTM move for the backward instead of recomputing it (checkpoint_move)')
@@ -169,14 +171,21 @@ class Cfg5(Cfg1):
 class Cfg4:
     """Differentiable CTMRG (forward + backward) from the recorded call sequence."""
 
-    def __init__(self, chi=24):
+    def __init__(self, chi=24, use_qr=False):
         from yastn_gb300.replay import load_replay
+        if use_qr and chi != 24:
+            raise ValueError("the use_qr=True run is recorded at chi=24")
         blocks = {24: "28 block SVDs of 2x432^2", 144: "24 block SVDs of 2x2592^2"}[chi]
+        qr = ", use_qr=True: 64 block QRs of the half-systems" if use_qr else ""
         self.name = (f"differentiable iPEPS CTMRG, 1x1 cell, Z2, D=6, d=2, chi={chi}, 8 CTM iterations, TFIM h=3 "
                      f"energy + gradient (recorded YASTN call sequence replayed: {blocks} among 32 SVD calls, "
-                     "697 dots, 1045 merges per forward), FP64")
+                     f"697 dots per forward{qr}), FP64")
         self.metric = f"CTMRG fwd+bwd ms (iPEPS Z2 D=6 chi={chi}, 8 CTM iterations, FP64, <=1e-10 rel)"
-        self.r = load_replay('ctmrg_z2_d6' if chi == 24 else f'ctmrg_z2_d6_chi{chi}')
+        name = 'ctmrg_z2_d6' + ('_qr' if use_qr else '') + ('' if chi == 24 else f'_chi{chi}')
+        self.r = load_replay(name)
+        # with use_qr the QR adjoint of rank-deficient half-systems amplifies rounding (two host
+        # evaluations of the same sequence differ by 1.6e-6), so its gradient is held to 1e-5
+        self.grad_tol = 1e-5 if use_qr else 1e-8
         self.cpu_recorded = self.r.payload.get('cpu_seconds')
         self.A = self.r.arrays['in:A']
         self.E_ref = self.r.payload['E']
@@ -850,7 +859,7 @@ def run_gpu_cfg4(args, wl):
     for _ in range(args.warmup):
         E, g = wl.step(torch, BK, dev)
     e_err, g_err = check(E, g)
-    assert e_err <= 1e-10 and g_err <= 1e-8, (e_err, g_err)
+    assert e_err <= 1e-10 and g_err <= wl.grad_tol, (e_err, g_err)
     barrier()
     clocks = Clocks(local)
     l0 = _native.LAUNCHES[0]
@@ -1064,7 +1073,7 @@ def kernel_roofline(torch, dev, run_once, w, gemm_mode, reps=5):
 
 def main():
     args = parse()
-    wl = Cfg4(args.chi) if args.workload == 'cfg4' else \
+    wl = Cfg4(args.chi, args.use_qr) if args.workload == 'cfg4' else \
         {'cfg1': Cfg1, 'cfg2': Cfg2, 'cfg3': Cfg3, 'cfg5': Cfg5}[args.workload]()
     if args.workload == 'cfg4':
         wl.checkpoint = not args.no_checkpoint
