@@ -350,27 +350,29 @@ def qr(data, meta, sizes):
 
 
 def qr_block_backward(q, r, gq, gr, a):
-    """Adjoint of one block's reduced QR (real), the rule torch's autograd applies to the
-    reference's ``torch.linalg.qr`` + sign fix (``backend_torch.py:475-484``): with
-    U = r[:, :k], gU = gr[:, :k], gq' = gq (+ a[:, m:] gr[:, m:]^T for wide blocks),
-    M = U gU^T - gq'^T q, dA[:, :k] = (gq' + q copyltu(M)) U^{-T}, copyltu(M) = tril(M) +
-    tril(M, -1)^T, and dA[:, m:] = q gr[:, m:] for wide blocks."""
+    """Adjoint of one block's reduced QR, the rule torch's autograd applies to the reference's
+    ``torch.linalg.qr`` + sign fix (``backend_torch.py:475-484``; R's diagonal is real): with
+    U = r[:, :k], gU = gr[:, :k], gq' = gq (+ a[:, m:] gr[:, m:]^H for wide blocks),
+    M = U gU^H - gq'^H q, dA[:, :k] = (gq' + q copyltu(M)) U^{-H}, copyltu(M) =
+    tril(M, -1) + tril(M, -1)^H + Re diag(M), and dA[:, m:] = q gr[:, m:] for wide blocks
+    (gradients in torch's convention for complex tensors)."""
     m, k = q.shape
     n = r.shape[1]
     u, gu, b = r[:, :k], gr[:, :k], gq.copy()
     if n > m:
-        b = b + a[:, m:] @ gr[:, m:].T
-    M = u @ gu.T - b.T @ q
-    b = b + q @ (np.tril(M) + np.tril(M, -1).T)
+        b = b + a[:, m:] @ gr[:, m:].conj().T
+    M = u @ gu.conj().T - b.conj().T @ q
+    low = np.tril(M, -1)
+    b = b + q @ (low + low.conj().T + np.diag(np.real(np.diag(M))))
     da = np.zeros((m, n), dtype=q.dtype)
-    da[:, :k] = scipy.linalg.solve_triangular(u, b.T, lower=False).T
+    da[:, :k] = scipy.linalg.solve_triangular(u, b.conj().T, lower=False).conj().T
     if n > m:
         da[:, m:] = q @ gr[:, m:]
     return da
 
 
 def qr_backward(Q, R, gQ, gR, data, meta):
-    """Block-sparse QR adjoint (real)."""
+    """Block-sparse QR adjoint (real and complex)."""
     out = np.zeros(data.size, dtype=data.dtype)
     for sl, D, slQ, DQ, slR, DR in meta:
         q = Q[_sl(slQ)].reshape(DQ)

@@ -206,8 +206,9 @@ def _tup(x):
 def scen_qr():
     """yastn.linalg.qr (linalg.py:738-828; backend_np.py:511-520, positive diagonal of R) on
     U(1) tensors with tall, square and wide blocks, float64 and complex128, including a
-    rank-deficient block; and the adjoint of the real calls from the torch backend on CPU
-    (backend_torch.py:475-484: torch.linalg.qr + the sign fix, differentiated by torch)."""
+    rank-deficient block; and the adjoints from the torch backend on CPU (backend_torch.py:
+    475-484: torch.linalg.qr + the sign fix, differentiated by torch; complex gradients in
+    torch's convention)."""
     import torch
     import yastn.backend.backend_torch as bt
     cfg = yastn.make_config(sym='U1', backend='np')
@@ -225,20 +226,19 @@ def scen_qr():
     blk[:, 3] = blk[:, 1]
     yastn.linalg.qr(c, axes=(0, 1))
     rec.restore()
-    # adjoints of the real calls through the reference's torch backend
+    # adjoints through the reference's torch backend
     g = torch.Generator().manual_seed(5)
     for call in rec.calls:
         if call['fn'] != 'qr':
             continue
         data = rec.arrays[call['args'][0]['__array__']]
-        if np.iscomplexobj(data):
-            continue
         meta = _tup(call['args'][1])
         sizes = tuple(call['args'][2])
         d_ = torch.from_numpy(data.copy()).requires_grad_(True)
         Q, R = bt.qr(d_, meta, sizes)
-        gQ = torch.randn(sizes[0], dtype=torch.float64, generator=g)
-        gR = torch.randn(sizes[1], dtype=torch.float64, generator=g)
+        dt = torch.complex128 if np.iscomplexobj(data) else torch.float64
+        gQ = torch.randn(sizes[0], dtype=dt, generator=g)
+        gR = torch.randn(sizes[1], dtype=dt, generator=g)
         (grad,) = torch.autograd.grad((Q, R), (d_,), grad_outputs=(gQ, gR))
         call['adjoint'] = {'gQ': rec._put(gQ.numpy()), 'gR': rec._put(gR.numpy()), 'grad': rec._put(grad.numpy())}
     save('qr', rec)

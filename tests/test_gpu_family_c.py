@@ -355,7 +355,7 @@ def test_qr_on_reference_calls(cuda_device):
         Q, R = (host(x) for x in ops.qr(dev(data), meta, sizes))
         _qr_checks(data, meta, Q, R, *c['out'])
         full = all(np.linalg.matrix_rank(data[sl[0]:sl[1]].reshape(D)) == min(D) for sl, D, *_ in meta)
-        if 'adjoint' in c and full:
+        if 'adjoint' in c and full and not np.iscomplexobj(data):  # the GPU adjoint is real-only
             adj = c['adjoint']
             g = host(ops.qr_backward(dev(c['out'][0]), dev(c['out'][1]), dev(adj['gQ']), dev(adj['gR']), dev(data),
                                      meta))

@@ -237,8 +237,8 @@ def test_heff2_replay_and_lanczos_match_reference():
 
 def test_oracle_qr_and_adjoint_match_reference():
     """qr (positive diagonal of R) against the reference's NumPy backend on tall, square,
-    wide, complex and rank-deficient blocks; the real adjoint against the reference torch
-    backend's autograd gradient."""
+    wide, complex and rank-deficient blocks; the adjoint (real and complex) against the
+    reference torch backend's autograd gradient."""
     tr = load_trace('qr')
     n_adj = 0
     for c in tr['calls']:
@@ -262,7 +262,7 @@ def test_oracle_qr_and_adjoint_match_reference():
             g = oracle.qr_backward(Qr, Rr, adj['gQ'], adj['gR'], data, meta)
             assert _rel(g, adj['grad']) < 1e-10
             n_adj += 1
-    assert n_adj == 2
+    assert n_adj == 4
 
 
 def test_ctmrg_checkpointed_replay_on_host_reproduces_reference():
