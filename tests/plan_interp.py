@@ -365,3 +365,40 @@ def finalize_qr(w64, blocks, U, S, V):
         else:
             U[int(r[3]):int(r[3]) + m * k] = Y.T.ravel()
             w64[int(r[22]):int(r[22]) + k * k] = W[idx].conj().ravel()
+
+
+def qr_plain(work, blocks, data, Q, R):
+    """numpy statement of yb_qr on the plan layout ([16] = 2): Z = the first k columns of A as
+    rows (M = A), the same Householder factorisation as ``qr_precondition``, R's rows and the
+    reflectors kept, Q^T formed in Z, then the finalisation: Q (m x k) and the square part of
+    R with the signs that make R's diagonal positive (the right part R[:, m:] of wide blocks
+    is the host's grouped GEMM)."""
+    for r in blocks:
+        a, m, n, k, L = int(r[0]), int(r[1]), int(r[2]), int(r[9]), int(r[17])
+        A = data[a:a + m * n].reshape(m, n)
+        Z = A[:, :k].T.astype(work.dtype).copy()  # k rows of length L = m
+        tau = np.zeros(k, dtype=work.dtype)
+        for j in range(k):
+            alpha, x = Z[j, j], Z[j, j + 1:]
+            xn = float(np.sum(np.abs(x) ** 2))
+            if not (xn == 0.0 and np.imag(alpha) == 0):
+                beta = -np.copysign(np.sqrt(abs(alpha) ** 2 + xn), np.real(alpha))
+                tau[j] = (beta - alpha) / beta
+                Z[j, j + 1:] = x / (alpha - beta)
+                Z[j, j] = beta
+            v = np.concatenate([[1.0], Z[j, j + 1:]]).astype(work.dtype)
+            for c in range(j + 1, k):
+                w = np.sum(np.conj(v) * Z[c, j:])
+                Z[c, j:] -= np.conj(tau[j]) * w * v
+        RR = np.triu(Z[:, :k].T)
+        V = np.triu(Z, 1)
+        Qt = np.eye(k, L, dtype=work.dtype)
+        for j in range(k - 1, -1, -1):
+            v = np.concatenate([[1.0], V[j, j + 1:]]).astype(work.dtype)
+            for c in range(j, k):
+                w = np.sum(np.conj(v) * Qt[c, j:])
+                Qt[c, j:] -= tau[j] * w * v
+        sg = np.where(np.real(np.diag(RR)) < 0, -1.0, 1.0)
+        Q[int(r[3]):int(r[3]) + m * k] = (Qt.T * sg[None, :]).ravel()
+        Rb = R[int(r[5]):int(r[5]) + k * n].reshape(k, n)
+        Rb[:, :k] = sg[:, None] * RR

@@ -473,6 +473,29 @@ def test_completion_plans_orthonormal_completion(qr_start):
         np.testing.assert_array_equal(f[:, :k - z], f0[:, :k - z])
 
 
+@pytest.mark.parametrize('cplx', [False, True])
+def test_qr_plan_layout_reproduces_oracle(cplx):
+    """yb_qr's records ([16] = 2) and the grouped GEMM of R's right part, applied with numpy
+    (the kernel's Householder steps and sign fix), give the oracle's Q and R."""
+    rng = np.random.default_rng(12)
+    shapes = [(9, 4), (5, 5), (3, 8), (1, 6), (12, 1)]
+    meta, off, oQ, oR = [], 0, 0, 0
+    for m, n in shapes:
+        k = min(m, n)
+        meta.append(((off, off + m * n), (m, n), (oQ, oQ + m * k), (m, k), (oR, oR + k * n), (k, n)))
+        off += m * n; oQ += m * k; oR += k * n
+    meta = tuple(meta)
+    data = rng.normal(size=off) + (1j * rng.normal(size=off) if cplx else 0)
+    plan = P.qr_plan(meta, cplx)
+    assert all(int(r[16]) == 2 for r in plan.blocks)
+    dt = np.complex128 if cplx else np.float64
+    Q, R = np.zeros(oQ, dt), np.zeros(oR, dt)
+    PI.qr_plain(np.zeros(plan.n64, dt), plan.blocks, data, Q, R)
+    PI.run_gemm(plan.right, Q, data, R)
+    Qr, Rr = oracle.qr(data, meta, (oQ, oR))
+    assert np.abs(Q - Qr).max() < 1e-12 and np.abs(R - Rr).max() < 1e-12
+
+
 def test_mixed_precision_jacobi_schedule_complex():
     """Complex blocks: FP32 phase on complex64 rows with phase-aligned rotations, widen,
     Newton-Schulz with T = W^H W, X = W X_0 (X_0 = A^H for tall blocks), FP64 phase; the
