@@ -162,15 +162,11 @@ int yb_ozaki_split_tiled(const double* src, void* slices, int* exps, const int64
 /* yb_ozaki_gemm_tc: yb_ozaki_gemm on the tcgen05 tensor cores with the 8 digit-diagonal
  * accumulators in tensor memory, operands from yb_ozaki_split_tiled (output records [4],
  * [6] = the A / B slice-0 offsets in the tile layout); tiles are (output, tile row, tile
- * col, phantom) of 128 rows x 64 columns. cluster (1, 2 or 4): that many consecutive tiles
- * (the same output and tile row, adjacent tile columns; n_tiles a multiple of cluster) run as
- * one thread-block cluster sharing the A digit tiles through multicast bulk copies; a tile
- * with phantom = 1 (past the last column tile of its output) only serves its share of A.
- * A CTA that gives up on a bounded wait writes nothing for its tile and sets the status
- * word read by yb_ozaki_device_error. */
+ * col, 0) of 128 rows x 64 columns, one CTA each. A CTA that gives up on a bounded wait
+ * writes nothing for its tile and sets the status word read by yb_ozaki_device_error. */
 int yb_ozaki_gemm_tc(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps,
                      double* c, const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
-                     int cluster, void* stream);
+                     void* stream);
 /* yb_ozaki_device_error: copies the tcgen05 kernel's status word to *out (0: no failure),
  * synchronising the stream, and clears it when reset != 0. */
 int yb_ozaki_device_error(int* out, int reset, void* stream);

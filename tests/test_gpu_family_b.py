@@ -247,9 +247,8 @@ def test_dot_small_and_ragged_sectors(emulated, cplx, cuda_device):
         ops.OZAKI_TC[0] = saved
 
 
-@pytest.mark.parametrize('cluster', [1, 2, 4])
 @pytest.mark.parametrize('name', ['cfg1', 'small'])
-def test_ozaki_tcgen05_matches_mma_sync(name, cluster, cuda_device):
+def test_ozaki_tcgen05_matches_mma_sync(name, cuda_device):
     """The tcgen05/TMEM kernel and the mma.sync kernel form the same exact diagonal sums and
     the same folds: their products agree bit for bit; no CTA reports a failed wait."""
     if name == 'cfg1':
@@ -261,18 +260,16 @@ def test_ozaki_tcgen05_matches_mma_sync(name, cluster, cuda_device):
         _, _, meta, Dsize = c2['args']
     else:
         meta, A, B, Dsize = _small_sector_problem(22)
-    from yastn_gb300 import _plans as P
-    saved, saved_cs = ops.OZAKI_TC[0], P.OZAKI_TC_CLUSTER
+    saved = ops.OZAKI_TC[0]
     try:
         ops.OZAKI_TC[0] = True
-        P.OZAKI_TC_CLUSTER = cluster  # clusters of that many CTAs share the A digit tiles
         assert ops.ozaki_device_error(reset=True) == 0
         got_tc = host(ops.dot_ozaki(dev(A), dev(B), meta, Dsize))
         assert ops.ozaki_device_error(reset=True) == 0
         ops.OZAKI_TC[0] = False
         got_mma = host(ops.dot_ozaki(dev(A), dev(B), meta, Dsize))
     finally:
-        ops.OZAKI_TC[0], P.OZAKI_TC_CLUSTER = saved, saved_cs
+        ops.OZAKI_TC[0] = saved
     np.testing.assert_array_equal(got_tc, got_mma)
     ref = oracle.dot(A, B, meta, Dsize)
     assert rel(got_tc, ref) <= TOL

@@ -497,7 +497,6 @@ class OzakiPlan:
 
 
 OZAKI_TC_M, OZAKI_TC_N = 128, 64  # output tile of the tcgen05 emulated GEMM
-OZAKI_TC_CLUSTER = 1               # CTAs per cluster sharing A digit tiles (1, 2 or 4)
 OZAKI_MIN_DIM = 16  # sector GEMMs contracting fewer indices than this stay on the native FP64 kernel
 OZAKI_SKINNY_ROWS = 8  # sector GEMMs with at most this many rows (and more than 64 columns) too
 
@@ -570,19 +569,15 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
                     tiles.append((K, oi, tr, tc))
         tiles.sort(key=lambda x: -x[0])
         tiles = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles], dtype=np.int32).reshape(-1, 4)
-        # 128 x 64 tiles of the tcgen05 kernel, in groups of OZAKI_TC_CLUSTER adjacent column
-        # tiles of one row tile (one thread-block cluster sharing the A digit tiles); a ragged
-        # group is padded with phantom tiles (w = 1)
-        cs = OZAKI_TC_CLUSTER
-        groups = []
+        # 128 x 64 tiles of the tcgen05 kernel, longest K first
+        tiles_tc = []
         for oi, o in enumerate(outs):
             m, n, K = int(o[1]), int(o[2]), int(o[8])
-            nct = (n + OZAKI_TC_N - 1) // OZAKI_TC_N
             for tr in range((m + OZAKI_TC_M - 1) // OZAKI_TC_M):
-                for g in range((nct + cs - 1) // cs):
-                    groups.append((K, [(oi, tr, tc, int(tc >= nct)) for tc in range(g * cs, g * cs + cs)]))
-        groups.sort(key=lambda x: -x[0])
-        tiles_tc = np.array([t for _, grp in groups for t in grp], dtype=np.int32).reshape(-1, 4)
+                for tc in range((n + OZAKI_TC_N - 1) // OZAKI_TC_N):
+                    tiles_tc.append((K, oi, tr, tc))
+        tiles_tc.sort(key=lambda x: -x[0])
+        tiles_tc = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles_tc], dtype=np.int32).reshape(-1, 4)
         a_recs = np.array(a_recs, dtype=np.int64).reshape(-1, 8)
         b_recs = np.array(b_recs, dtype=np.int64).reshape(-1, 8)
         a_rows = int(a_recs[:, 1].max()) if len(a_recs) else 0
@@ -607,7 +602,7 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
                    for o in outs)
         plan.prefer_tc = bool(len(outs)) and w128 <= 1.1 * w64
         return plan
-    return CACHE.get((meta_dot,), ('ozaki_dot', s, bool(cplx), OZAKI_TC_CLUSTER), build)
+    return CACHE.get((meta_dot,), ('ozaki_dot', s, bool(cplx)), build)
 
 
 # ----------------------------------------------------------------------------- SVD

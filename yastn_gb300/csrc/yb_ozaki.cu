@@ -432,33 +432,11 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_
                : "memory");
 }
 
-__device__ __forceinline__ void bulk_load_mc(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar,
-                                             uint16_t mask) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1], %2, [%3], %4;"
-      ::"r"(dst), "l"(src), "r"(bytes), "r"(mbar), "h"(mask)
-      : "memory");
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
 }
 
-__device__ __forceinline__ void tc_commit(uint32_t mbar, uint16_t mask, bool multicast) {
-  if (multicast)
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
-                 ::"r"(mbar), "h"(mask));
-  else
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
-}
-
-__device__ __forceinline__ void cluster_sync() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
-// CS CTAs of a cluster compute CS adjacent 64-column tiles of the same 128-row tile: they
-// need the same A digit tiles, so CTA r bulk-copies the A slices t with t % CS == r to all
-// of them (multicast), and each loads its own B tiles. A stage is refilled once the MMAs of
-// every CTA of the cluster have read it: each CTA's tcgen05.commit arrives on that stage's
-// "empty" barrier in all CTAs (initialised with CS arrivals). A tile past the sector's last
-// column tile (tile record w = 1, a ragged end) only serves its A share and its commits.
-template <int S, int CS>
+template <int S>
 __global__ void __launch_bounds__(kTcThreads, 1)
     ozaki_gemm_tc_kernel(const __nv_bfloat16* __restrict__ As, const int* __restrict__ Ae,
                          const __nv_bfloat16* __restrict__ Bs, const int* __restrict__ Be, double* __restrict__ C,
@@ -466,13 +444,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   constexpr uint32_t kATile = kTcM * kK * 2;  // 4096 B: one slice's 128 x 16 digit tile
   constexpr uint32_t kBTile = kTcN * kK * 2;  // 2048 B
   constexpr uint32_t kStage = S * (kATile + kBTile);
-  constexpr uint16_t kMask = (uint16_t)((1u << CS) - 1u);
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint32_t tmem_slot;
   __shared__ __align__(8) uint64_t full[kTcStages], empty[kTcStages], accb;
   __shared__ int failed;
   const int4 tl = reinterpret_cast<const int4*>(tiles)[blockIdx.x];
-  const bool phantom = tl.w == 1;
   const int64_t* o = outs + (int64_t)tl.x * 16;
   const int64_t c_off = o[0], m = o[1], n = o[2], ldc = o[3];
   const int64_t a_sl = o[4], a_ex = o[5], b_sl = o[6], b_ex = o[7], Kp = o[9];
@@ -480,8 +456,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int64_t row0 = (int64_t)tl.y * kTcM, col0 = (int64_t)tl.z * kTcN;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t sbase = smem_u32(smem);
-  uint32_t rank = 0;
-  if (CS > 1) asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -491,7 +465,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   if (tid == 0) {
     for (int i = 0; i < kTcStages; ++i) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[i])));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&empty[i])), "r"(CS));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[i])));
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&accb)));
     asm volatile("fence.mbarrier_init.release.cluster;");
@@ -499,7 +473,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
-  if (CS > 1) cluster_sync();  // every CTA's barriers exist before anyone copies or commits into them
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_slot;
 
@@ -508,19 +481,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int64_t a_slice = (m + kTcM - 1) / kTcM * kTcM * Kp, b_slice = (n + kTcN - 1) / kTcN * kTcN * Kp;
   const __nv_bfloat16* a_tiles = As + a_sl + (int64_t)tl.y * ksteps * (kTcM * kK);
   const __nv_bfloat16* b_tiles = Bs + b_sl + (int64_t)tl.z * ksteps * (kTcN * kK);
-  const uint32_t stage_bytes = S * kATile + (phantom ? 0u : S * kBTile);
-  // producer (thread 0): this CTA's share of the A tiles (to every CTA of the cluster) and its B tiles
+  // producer (thread 0): the S digit tiles of A and of B of one K step
   auto issue = [&](int stage, int64_t step) {
     const uint32_t fb = smem_u32(&full[stage]);
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(stage_bytes) : "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(kStage) : "memory");
     const uint32_t d0 = sbase + (uint32_t)stage * kStage;
     for (int t = 0; t < S; ++t) {
-      if (t % CS == (int)rank) {
-        const void* src = a_tiles + t * a_slice + step * (kTcM * kK);
-        if (CS > 1) bulk_load_mc(d0 + t * kATile, src, kATile, fb, kMask);
-        else bulk_load(d0 + t * kATile, src, kATile, fb);
-      }
-      if (!phantom) bulk_load(d0 + S * kATile + t * kBTile, b_tiles + t * b_slice + step * (kTcN * kK), kBTile, fb);
+      bulk_load(d0 + t * kATile, a_tiles + t * a_slice + step * (kTcM * kK), kATile, fb);
+      bulk_load(d0 + S * kATile + t * kBTile, b_tiles + t * b_slice + step * (kTcN * kK), kBTile, fb);
     }
   };
   const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
@@ -541,15 +509,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         if (!mbar_wait(smem_u32(&full[stage]), (uint32_t)((st / kTcStages) & 1))) { failed = 1; break; }
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t a0 = sbase + (uint32_t)stage * kStage, b0 = a0 + S * kATile;
-        if (!phantom) {
 #pragma unroll
-          for (int ta = 0; ta < S; ++ta)
+        for (int ta = 0; ta < S; ++ta)
 #pragma unroll
-            for (int tb = 0; tb < S - ta; ++tb)
-              tc_mma(tmem + (uint32_t)((ta + tb) * kTcN), umma_desc(a0 + ta * kATile), umma_desc(b0 + tb * kBTile),
-                     idesc, (st == s0 && ta == 0) ? 0u : 1u);
-        }
-        tc_commit(smem_u32(&empty[stage]), kMask, CS > 1);
+          for (int tb = 0; tb < S - ta; ++tb)
+            tc_mma(tmem + (uint32_t)((ta + tb) * kTcN), umma_desc(a0 + ta * kATile), umma_desc(b0 + tb * kBTile),
+                   idesc, (st == s0 && ta == 0) ? 0u : 1u);
+        tc_commit(smem_u32(&empty[stage]));
         consumed = st + 1;
         // refill the stage of step st-1 (its MMAs ran while those of step st were queued)
         if (st >= 1 && issued < ksteps && issued == st - 1 + kTcStages) {
@@ -560,11 +526,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
       }
       // the accumulators of this chunk are complete once every MMA issued so far is
-      tc_commit(smem_u32(&accb), kMask, false);
+      tc_commit(smem_u32(&accb));
     }
     if (!mbar_wait(smem_u32(&accb), (uint32_t)(ch & 1))) failed = 1;
     asm volatile("tcgen05.fence::after_thread_sync;");
-    if (!phantom) {
+    {
 #pragma unroll
       for (int cb = 0; cb < kTcN / 8; ++cb) {
         long long hi[8], lo[8];
@@ -602,11 +568,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
   } else {
     if (tid == 0) {
-      // every CTA of the cluster has committed its last MMAs on this CTA's stage barriers
+      // the last MMAs have completed (they read the stage buffers the epilogue reuses)
       for (int64_t j = max((int64_t)0, ksteps - kTcStages); j < ksteps; ++j)
         if (!mbar_wait(smem_u32(&empty[j % kTcStages]), (uint32_t)((j / kTcStages) & 1))) atomicExch(err, 1);
     }
-    if (!phantom) {
+    {
       // epilogue through shared memory (the stages are free): row-major 128 x 64 doubles,
       // padded rows; then coalesced stores with the row/column exponents applied
       double* tileC = reinterpret_cast<double*>(smem);
@@ -625,35 +591,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
-  if (CS > 1) cluster_sync();  // no CTA leaves while a peer may still copy or commit into it
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
 }
 
-template <int S, int CS>
+template <int S>
 int launch_gemm_tc(const void* As, const int* Ae, const void* Bs, const int* Be, double* C, const int64_t* outs,
                    const int32_t* tiles, int n_tiles, int* err, cudaStream_t s) {
   const size_t smem = (size_t)kTcStages * S * (kTcM + kTcN) * kK * 2;
   static_assert((size_t)kTcM * (kTcN + 1) * 8 <= (size_t)kTcStages * 6 * (kTcM + kTcN) * kK * 2,
                 "epilogue tile must fit in the stage buffers");
-  if (n_tiles % CS != 0) return YB_ERR_INVALID;
-  auto kern = ozaki_gemm_tc_kernel<S, CS>;
+  auto kern = ozaki_gemm_tc_kernel<S>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)n_tiles);
-  cfg.blockDim = dim3(kTcThreads);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = CS;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  e = cudaLaunchKernelEx(&cfg, kern, (const __nv_bfloat16*)As, Ae, (const __nv_bfloat16*)Bs, Be, C, outs, tiles, err);
-  if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
-  return YB_OK;
+  kern<<<n_tiles, kTcThreads, smem, s>>>((const __nv_bfloat16*)As, Ae, (const __nv_bfloat16*)Bs, Be, C, outs, tiles,
+                                         err);
+  return check_launch();
 }
 
 }  // namespace
@@ -700,22 +652,19 @@ int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices,
 static __device__ int g_ozaki_tc_error;
 
 int yb_ozaki_gemm_tc(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps, double* c,
-                     const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count, int cluster,
-                     void* stream) {
+                     const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count, void* stream) {
   if (n_tiles == 0) return YB_OK;
   if (!a_slices || !a_exps || !b_slices || !b_exps || !c || !outs || !tiles) return YB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
   int* err = nullptr;
   cudaError_t e = cudaGetSymbolAddress((void**)&err, g_ozaki_tc_error);
   if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
-#define YB_TC_CASE(S_, CS_) \
-  if (slices_count == S_ && cluster == CS_) \
-    return yb::launch_gemm_tc<S_, CS_>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
-  YB_TC_CASE(8, 1) YB_TC_CASE(8, 2) YB_TC_CASE(8, 4)
-  YB_TC_CASE(7, 1) YB_TC_CASE(7, 2) YB_TC_CASE(7, 4)
-  YB_TC_CASE(6, 1) YB_TC_CASE(6, 2) YB_TC_CASE(6, 4)
-#undef YB_TC_CASE
-  return YB_ERR_INVALID;
+  switch (slices_count) {
+    case 8: return yb::launch_gemm_tc<8>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
+    case 7: return yb::launch_gemm_tc<7>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
+    case 6: return yb::launch_gemm_tc<6>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
+    default: return YB_ERR_INVALID;
+  }
 }
 
 int yb_ozaki_device_error(int* out, int reset, void* stream) {

@@ -219,7 +219,7 @@ def _ozaki_run(plan, A, B, out, slices, tc):
         N.call('yb_ozaki_split_tiled', _ptr(bT), _ptr(b_sl), _ptr(b_ex), _ptr(dbr), len(plan.b_recs), plan.b_rows,
                slices, P.OZAKI_TC_N, st)
         N.call('yb_ozaki_gemm_tc', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
-               len(plan.tiles_tc), slices, P.OZAKI_TC_CLUSTER, st)
+               len(plan.tiles_tc), slices, st)
     else:
         N.call('yb_ozaki_split', _ptr(A), _ptr(a_sl), _ptr(a_ex), _ptr(dar), len(plan.a_recs), plan.a_rows, slices,
                st)
