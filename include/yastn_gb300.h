@@ -151,37 +151,48 @@ int yb_ozaki_split(const double* src, void* slices, int* exps, const int64_t* re
 int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps,
                   double* c, const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
                   void* stream);
-/* yb_ozaki_split_tiled: yb_ozaki_split writing the digit planes in the tile layout of
- * yb_ozaki_gemm_tc: per slice, tile_rows (128 for A, 64 for B) x 16 blocks, each in the
- * canonical K-major core-matrix order (byte offset of (row r, k) in a block:
- * (r/8)*256 + (k/8)*128 + (r%8)*16 + (k%8)*2), blocks ordered (row tile, K step); the
- * rows are padded with zeros to a multiple of tile_rows (record [5] = slice-0 offset, slice
- * stride = padded rows x Kp). */
-int yb_ozaki_split_tiled(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs,
-                         int max_rows, int slices_count, int tile_rows, void* stream);
-/* yb_ozaki_gemm_tc: yb_ozaki_gemm on the tcgen05 tensor cores with the 8 digit-diagonal
- * accumulators in tensor memory, operands from yb_ozaki_split_tiled (output records [4],
- * [6] = the A / B slice-0 offsets in the tile layout); tiles are (output, tile row, tile
- * col, 0) of 128 rows x 64 columns, one CTA each. A CTA that gives up on a bounded wait
- * writes nothing for its tile and sets the status word read by yb_ozaki_device_error. */
-int yb_ozaki_gemm_tc(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps,
-                     double* c, const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
-                     void* stream);
+/* yb_ozaki_exponents: the per-row (axis 0, the A operands) or per-column (axis 1, the B
+ * operands) exponents e of the split, max |x| = f 2^e with f in [0.5, 1) (0 for a zero
+ * row/column). recs: n_recs records of 8 int64: [0] block offset (elements) [1] rows
+ * [2] cols [3] row stride (elements) [4] 1 for complex128 data (a row or column counts both
+ * parts) [5] exponents offset; max_len: largest rows (axis 0) or cols (axis 1). */
+int yb_ozaki_exponents(const void* x, int* exps, const int64_t* recs, int n_recs, int max_len, int axis,
+                       void* stream);
+/* yb_ozaki_gemm_fused: the emulated sector GEMMs on the tcgen05 tensor cores with the digit
+ * split fused in: each 128 x 64 output tile reads its FP64 (or complex128) operand tiles
+ * from A (row-major m x K blocks) and B (row-major K x n blocks) directly, writes their
+ * slices_count (6, 7 or 8) BF16 digits into shared memory, accumulates the digit-diagonal
+ * products in tensor memory (exact FP32 sums per 400-long K chunk) and rounds each chunk's
+ * exact integer combination once to FP64 -- the same bits as yb_ozaki_gemm. outs: 16 int64
+ * per output: [0] c offset (FP64 words) [1] m [2] n [3] ldc (FP64 words) [4] A block offset
+ * (elements) [5] A exponents offset [6] B block offset (elements) [7] B exponents offset
+ * [8] K [9] lda [10] output column stride (FP64 words) [11] complex part (0: C_r, 1: C_i)
+ * [12] 1 for complex128 operands [13] ldb; exps: from yb_ozaki_exponents (A rows, B
+ * columns); tiles: int32 (output, tile row, tile col, 0), one CTA each. A CTA that gives up
+ * on a bounded wait writes nothing for its tile and sets the status word read by
+ * yb_ozaki_device_error. Replaces dot (backend_torch.py:549-550) in the emulated mode. */
+int yb_ozaki_gemm_fused(const void* a, const void* b, const int* exps, double* c, const int64_t* outs,
+                        const int32_t* tiles, int n_tiles, int slices_count, void* stream);
 /* yb_ozaki_device_error: copies the tcgen05 kernel's status word to *out (0: no failure),
  * synchronising the stream, and clears it when reset != 0. */
 int yb_ozaki_device_error(int* out, int reset, void* stream);
 
-/* yb_ozaki_dot_static: yb_ozaki_split (A), yb_block_copy + yb_ozaki_split (B) and
- * yb_ozaki_gemm in one call, with all scratch (digit planes, exponents, transposed B)
- * placed in a device array built into the library instead of caller-provided memory.
+/* yb_ozaki_dot_static: a whole emulated dot in one call -- the native FP64 sectors
+ * (yb_grouped_gemm), yb_ozaki_split (A), yb_block_copy + yb_ozaki_split (B) and
+ * yb_ozaki_gemm -- with all scratch (digit planes, exponents, transposed B) placed in a
+ * device array built into the library instead of caller-provided memory.
  * No counterpart in the reference: it exists for callers that cannot allocate device
  * memory at call time (a host framework that owns the whole device memory budget and
  * forbids allocations after start-up, or a caller for which an allocation would
  * synchronise the device in the middle of its stream work). The caller still provides
  * A, B, C and the plan records, laid out as for the separate calls: b_recs refer to the
  * transposed copy of B (offsets from 0), bT_tasks/bT_items are the yb_block_copy plan of
- * B's blocks into those transposes in 8-byte units (no YB_CP_VEC tasks). Limits and
- * behaviour:
+ * B's blocks into those transposes in 8-byte units (no YB_CP_VEC tasks). The sectors the
+ * emulation does not take (K < 16, or at most 8 rows and more than 64 columns) come as
+ * yb_grouped_gemm records (nat_outs, nat_terms, nat_tiles; alpha 1, beta 0) and must be a
+ * direct plan without split-K, whose chunk workspace this call does not hold.
+ * Limits and behaviour:
+ *   - real FP64 only: dtype must be YB_F64 (YB_C128 returns YB_ERR_INVALID);
  *   - the scratch holds YB_STATIC_SCRATCH_BYTES; the call returns YB_ERR_TOO_LARGE when
  *     2*(a_slice_elems + b_slice_elems) + 8*bT_elems + 4*(a_exp_count + b_exp_count)
  *     bytes (each region rounded up to 256 bytes) exceed it;
@@ -192,11 +203,13 @@ int yb_ozaki_device_error(int* out, int reset, void* stream);
  *     rewritten before it is read, and calls that overlap on the GPU race on it;
  *   - C positions not covered by an output record are left untouched (zero them first). */
 #define YB_STATIC_SCRATCH_BYTES (16u << 20)
-int yb_ozaki_dot_static(const double* A, const double* B, double* C,
+int yb_ozaki_dot_static(const double* A, const double* B, double* C, int dtype,
                         const int64_t* a_recs, int n_a, int a_rows,
                         const int64_t* b_recs, int n_b, int b_rows,
                         const int64_t* bT_tasks, int n_bT_tasks, const int64_t* bT_items, int n_bT_items,
-                        const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
+                        const int64_t* outs, const int32_t* tiles, int n_tiles,
+                        const int64_t* nat_outs, const int64_t* nat_terms, const int32_t* nat_tiles,
+                        int n_nat_tiles, int slices_count,
                         int64_t a_slice_elems, int64_t b_slice_elems, int64_t a_exp_count,
                         int64_t b_exp_count, int64_t bT_elems, void* stream);
 
@@ -311,12 +324,14 @@ int yb_svd_adjoint_core(const void* P, const void* Q, const double* S, const dou
  * offsets in FP64 (complex128) elements. The Householder factorisation is the one of
  * yb_svd_qr applied to M = A (wide blocks: to A's first m columns; the host forms
  * R[:, m:] = Q^H A[:, m:] with the grouped GEMM); R's part below the diagonal is zeroed.
- * yb_qr_adjoint_sym / yb_trsm_rt: the two elementwise steps of the QR adjoint (real),
- *   dA = (gQ' + Q copyltu(M)) R^{-T},  M = R gR^T - gQ'^T Q
- * (gQ' = gQ, or gQ + A[:, m:] gR[:, m:]^T for wide blocks, whose dA[:, m:] = Q gR[:, m:]);
+ * yb_qr_adjoint_sym / yb_trsm_rt: the two elementwise steps of the QR adjoint (YB_F64 or
+ * YB_C128; the rule torch's autograd applies to the reference's qr, backend_torch.py:475-484),
+ *   dA = (gQ' + Q copyltu(M)) R^{-H},  M = R gR^H - gQ'^H Q
+ * (gQ' = gQ, or gQ + A[:, m:] gR[:, m:]^H for wide blocks, whose dA[:, m:] = Q gR[:, m:]);
  * the products are grouped GEMMs. Records YB_QRADJ_REC int64: [0] M offset [1] k
- * [2] B offset [3] rows [4] ldb [5] R offset [6] ldr. copyltu: M <- tril(M) + tril(M,-1)^T.
- * trsm_rt: B <- B R^{-T} (R upper triangular, back substitution per row). */
+ * [2] B offset [3] rows [4] ldb [5] R offset [6] ldr. copyltu: M <- tril(M, -1) +
+ * tril(M, -1)^H + Re diag(M). trsm_rt: B <- B R^{-H} (R upper triangular with a real
+ * diagonal, back substitution per row). */
 #define YB_QRADJ_REC 8
 int yb_qr(const void* a, void* Q, void* R, void* work64, const int64_t* blocks, int n_blocks, int dtype,
           int64_t* qctrl, int qctrl_words, void* stream);
@@ -357,6 +372,15 @@ int yb_mask_gather(const void* A, void* out, int unit_bytes, const int64_t* recs
 int yb_fix_signs(const void* Uin, const void* Vin, void* Uout, void* Vout, void* phases,
                  const int64_t* blocks, int n_blocks, int max_k, int dtype, int apply_given,
                  void* stream);
+/* yb_fix_signs_adjoint: the adjoint of fix_svd_signs as torch's autograd differentiates the
+ * reference's backend_torch.py:353-366 (YB_F64 or YB_C128; complex gradients in torch's
+ * convention). Uin/Vin: the forward's inputs; gU/gV: cotangents of its outputs; per column c
+ * with p the forward's phase (recomputed from Uin by the same row rule):
+ * dU[:, c] = gU[:, c] p, dVh[c, :] = gVh[c, :] conj(p), and for complex data
+ * dU[r, c] += -i (p / |U[r, c]|) Im(conj(G) p) at the selected row r, with
+ * G = sum_i U[i, c] conj(gU[i, c]) + sum_j conj(Vh[c, j]) gVh[c, j]. Records as yb_fix_signs. */
+int yb_fix_signs_adjoint(const void* Uin, const void* Vin, const void* gU, const void* gV, void* dU, void* dV,
+                         const int64_t* blocks, int n_blocks, int max_k, int dtype, void* stream);
 
 /* Fused truncation rule of yastn/tensor/linalg.py:637-735 over a flat spectrum.
  * S: n values; blk: n_blk records of 4 int64 (start, stop, D_block (or -1 = inf), unused);

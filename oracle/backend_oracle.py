@@ -18,6 +18,7 @@ __all__ = [
     'dot', 'dot_backward', 'transpose_dot_sum', 'transpose_dot_sum_backward',
     'svd', 'svd_block_backward', 'svd_backward',
     'eigh', 'eigh_block_backward', 'eigh_block_backward_hermitian', 'eigh_backward', 'fix_svd_signs',
+    'fix_svd_signs_backward',
     'qr', 'qr_block_backward', 'qr_backward',
     'apply_mask', 'apply_mask_backward', 'embed_mask',
     'truncation_mask', 'rand_normal',
@@ -217,6 +218,34 @@ def fix_svd_signs(U, V, meta):
         Ub *= phase.conj()[None, :]
         Vb *= phase[:, None]
     return U, V
+
+
+def fix_svd_signs_backward(U, V, gU, gV, meta):
+    """Adjoint of ``fix_svd_signs`` as torch's autograd differentiates the reference's
+    ``backend_torch.py:353-366`` (gradients in torch's convention for complex tensors,
+    grad = dL/dRe + i dL/dIm). Per column c with phase p = u/|u| of the selected entry
+    u = U[r*, c] (the row choice is piecewise constant):
+    gU[:, c] = gU'[:, c] p, gV[c, :] = gV'[c, :] conj(p), and, through p,
+    gU[r*, c] += -i (p / |u|) Im(conj(G) p) with G = sum_i U[i, c] conj(gU'[i, c]) +
+    sum_j conj(V[c, j]) gV'[c, j]; for real data the last term vanishes."""
+    dU = np.zeros_like(U)
+    dV = np.zeros_like(V)
+    amp = (np.abs(U) * (2 ** 40)).astype(np.int64)
+    for _, _, slU, DU, _, slV, DV in meta:
+        Ub, Vb = U[_sl(slU)].reshape(DU), V[_sl(slV)].reshape(DV)
+        gUb, gVb = gU[_sl(slU)].reshape(DU), gV[_sl(slV)].reshape(DV)
+        cols = np.arange(DU[1])
+        rows = np.argmax(amp[_sl(slU)].reshape(DU), axis=0)
+        u = Ub[rows, cols]
+        p = u / np.abs(u)
+        dUb = gUb * p[None, :]
+        dVb = gVb * p.conj()[:, None]
+        if np.iscomplexobj(U):
+            G = np.sum(Ub * gUb.conj(), axis=0) + np.sum(Vb.conj() * gVb, axis=1)
+            dUb[rows, cols] += -1j * (p / np.abs(u)) * np.imag(G.conj() * p)
+        dU[_sl(slU)] = dUb.ravel()
+        dV[_sl(slV)] = dVb.ravel()
+    return dU, dV
 
 
 def eigh(data, meta, sizes):

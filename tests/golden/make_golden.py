@@ -266,6 +266,48 @@ def scen_fix_signs():
     save('fix_signs', rec, extra)
 
 
+def scen_fix_signs_adjoint():
+    """Adjoint of fix_svd_signs through the reference torch backend on CPU
+    (backend_torch.py:353-366, differentiated by torch): U and Vh from the thin SVD of random
+    blocks (square, tall, wide; float64 and complex128, where the phase of each column's
+    largest entry carries a gradient), random cotangents of the fixed U and Vh, and the
+    gradients with respect to the unfixed U and Vh (torch's convention for complex tensors)."""
+    import torch
+    import yastn.backend.backend_torch as bt
+    g = torch.Generator().manual_seed(9)
+    arrays, calls = {}, []
+
+    def put(x):
+        key = f"a{len(arrays)}"
+        arrays[key] = x.detach().resolve_conj().cpu().numpy().copy()
+        return key
+
+    for dtype in (torch.float64, torch.complex128):
+        shapes = [(6, 6), (9, 4), (3, 8)]
+        meta, offU, offS, offV = [], 0, 0, 0
+        Us, Vs = [], []
+        for m, n in shapes:
+            k = min(m, n)
+            u, _, vh = torch.linalg.svd(torch.randn(m, n, dtype=dtype, generator=g), full_matrices=False)
+            Us.append(u.reshape(-1)); Vs.append(vh.reshape(-1))
+            meta.append(((0, 0), (m, n), (offU, offU + m * k), (m, k), (offS, offS + k), (offV, offV + k * n), (k, n)))
+            offU += m * k; offS += k; offV += k * n
+        meta = tuple(meta)
+        U = torch.cat(Us).requires_grad_(True)
+        V = torch.cat(Vs).requires_grad_(True)
+        Uf, Vf = bt.fix_svd_signs(U, V, meta)
+        gU = torch.randn(offU, dtype=dtype, generator=g)
+        gV = torch.randn(offV, dtype=dtype, generator=g)
+        dU, dV = torch.autograd.grad((Uf, Vf), (U, V), grad_outputs=(gU, gV))
+        calls.append({'fn': 'fix_svd_signs_backward', 'meta': [list(map(list, r)) for r in meta], 'U': put(U),
+                      'V': put(V), 'Uf': put(Uf), 'Vf': put(Vf), 'gU': put(gU), 'gV': put(gV), 'dU': put(dU),
+                      'dV': put(dV)})
+    with open(os.path.join(HERE, 'fix_signs_adjoint.json'), 'w') as f:
+        json.dump({'scenario': 'fix_signs_adjoint', 'calls': calls}, f, separators=(',', ':'))
+    np.savez_compressed(os.path.join(HERE, 'fix_signs_adjoint.npz'), **arrays)
+    print(f"fix_signs_adjoint: {len(calls)} cases")
+
+
 def scen_truncation():
     """Spectra and options of test_svd.py:189-266 and :344-388 with the reference's masks."""
     out = []
@@ -932,6 +974,7 @@ elif __name__ == '__main__':
         scen_tensordot(pol)
     scen_svd()
     scen_fix_signs()
+    scen_fix_signs_adjoint()
     scen_qr()
     scen_truncation()
     scen_eigh()

@@ -328,6 +328,40 @@ def test_apply_mask_on_reference_calls(name, cuda_device):
     assert n > 0
 
 
+@pytest.mark.parametrize('cplx', [False, True])
+def test_fix_signs_adjoint_vs_reference_autograd(cplx, cuda_device):
+    """yb_fix_signs_adjoint against torch's autograd of the reference's fix_svd_signs
+    (fixture) and the oracle: real, and complex with the gradient through the phases."""
+    import json, os
+    from yastn_gb300.workloads import GOLDEN, _decode
+    with open(os.path.join(GOLDEN, 'fix_signs_adjoint.json')) as f:
+        calls = json.load(f)['calls']
+    z = np.load(os.path.join(GOLDEN, 'fix_signs_adjoint.npz'))
+    c = [c for c in calls if np.iscomplexobj(z[c['U']]) == cplx][0]
+    meta = _decode(c['meta'], None)
+    U, V, gU, gV = (z[c[k]] for k in ('U', 'V', 'gU', 'gV'))
+    dU, dV = (host(x) for x in ops.fix_svd_signs_backward(dev(U), dev(V), dev(gU), dev(gV), meta))
+    assert rel(dU, z[c['dU']]) <= 1e-12 and rel(dV, z[c['dV']]) <= 1e-12
+
+
+def test_fix_signs_autograd_gradcheck_complex(cuda_device):
+    """torch.autograd.gradcheck of the backend's complex fix_svd_signs (the phases of the
+    columns' largest entries carry a gradient); U, Vh from a complex SVD, so no near-ties."""
+    from yastn_gb300 import backend as BK
+    rng = np.random.default_rng(8)
+    meta, offU, offS, offV, Us, Vs = [], 0, 0, 0, [], []
+    for m, n in ((5, 5), (6, 3), (2, 4)):
+        k = min(m, n)
+        u, _, vh = np.linalg.svd(rng.normal(size=(m, n)) + 1j * rng.normal(size=(m, n)), full_matrices=False)
+        Us.append(u.ravel()); Vs.append(vh.ravel())
+        meta.append(((0, 0), (m, n), (offU, offU + m * k), (m, k), (offS, offS + k), (offV, offV + k * n), (k, n)))
+        offU += m * k; offS += k; offV += k * n
+    meta = tuple(meta)
+    U = dev(np.concatenate(Us)).requires_grad_(True)
+    V = dev(np.concatenate(Vs)).requires_grad_(True)
+    assert torch.autograd.gradcheck(lambda a, b: BK.fix_svd_signs(a, b, meta), (U, V), eps=1e-7, atol=1e-6)
+
+
 def _qr_checks(data, meta, Q, R, Qr=None, Rr=None):
     for sl, D, slQ, DQ, slR, DR in meta:
         a = data[sl[0]:sl[1]].reshape(D)
@@ -344,8 +378,8 @@ def _qr_checks(data, meta, Q, R, Qr=None, Rr=None):
 
 def test_qr_on_reference_calls(cuda_device):
     """Batched Householder QR with R's diagonal made positive against the reference's NumPy
-    backend (tall, square, wide, complex, rank-deficient blocks), and the real adjoint
-    against the reference torch backend's autograd gradient."""
+    backend (tall, square, wide, complex, rank-deficient blocks), and the adjoint (real and
+    complex) against the reference torch backend's autograd gradient."""
     tr = load_trace('qr')
     n = 0
     for c in tr['calls']:
@@ -355,7 +389,7 @@ def test_qr_on_reference_calls(cuda_device):
         Q, R = (host(x) for x in ops.qr(dev(data), meta, sizes))
         _qr_checks(data, meta, Q, R, *c['out'])
         full = all(np.linalg.matrix_rank(data[sl[0]:sl[1]].reshape(D)) == min(D) for sl, D, *_ in meta)
-        if 'adjoint' in c and full and not np.iscomplexobj(data):  # the GPU adjoint is real-only
+        if 'adjoint' in c and full:
             adj = c['adjoint']
             g = host(ops.qr_backward(dev(c['out'][0]), dev(c['out'][1]), dev(adj['gQ']), dev(adj['gR']), dev(data),
                                      meta))
@@ -367,7 +401,7 @@ def test_qr_on_reference_calls(cuda_device):
 @pytest.mark.parametrize('cplx', [False, True])
 def test_qr_large_blocks(cplx, cuda_device):
     """Blocks of 432 x 432, 600 x 200, 100 x 900, 2000 x 16 and a graded one against the
-    oracle; the adjoint of the real ones against the oracle's."""
+    oracle; the adjoint (real and complex, the four ungraded blocks) against the oracle's."""
     rng = np.random.default_rng(41)
     f = lambda *sh: rng.normal(size=sh) + (1j * rng.normal(size=sh) if cplx else 0)
     q1, _ = np.linalg.qr(f(150, 150))
@@ -384,16 +418,17 @@ def test_qr_large_blocks(cplx, cuda_device):
     Q, R = (host(x) for x in ops.qr(dev(data), meta, (oQ, oR)))
     Qr, Rr = oracle.qr(data, meta, (oQ, oR))
     _qr_checks(data, meta, Q, R, Qr, Rr)
-    if not cplx:
-        gQ, gR = rng.normal(size=oQ), rng.normal(size=oR)
-        meta_w = meta[:4]  # the graded block's adjoint amplifies by 1e10
-        g = host(ops.qr_backward(dev(Qr), dev(Rr), dev(gQ), dev(gR), dev(data), meta_w))
-        ref = oracle.qr_backward(Qr, Rr, gQ, gR, data, meta_w)
-        assert rel(g, ref) <= 1e-10
+    gQ, gR = f(oQ), f(oR)
+    meta_w = meta[:4]  # the graded block's adjoint amplifies by 1e10
+    g = host(ops.qr_backward(dev(Qr), dev(Rr), dev(gQ), dev(gR), dev(data), meta_w))
+    ref = oracle.qr_backward(Qr, Rr, gQ, gR, data, meta_w)
+    assert rel(g, ref) <= 1e-10
 
 
-def test_qr_autograd_gradcheck(cuda_device):
-    """torch.autograd.gradcheck of the backend's qr Function (central differences)."""
+@pytest.mark.parametrize('cplx', [False, True])
+def test_qr_autograd_gradcheck(cplx, cuda_device):
+    """torch.autograd.gradcheck of the backend's qr Function (central differences; complex
+    inputs are checked by torch in its Wirtinger convention)."""
     from yastn_gb300 import backend as BK
     rng = np.random.default_rng(2)
     shapes = [(5, 3), (4, 4), (2, 6)]
@@ -403,5 +438,5 @@ def test_qr_autograd_gradcheck(cuda_device):
         meta.append(((off, off + m * n), (m, n), (oQ, oQ + m * k), (m, k), (oR, oR + k * n), (k, n)))
         off += m * n; oQ += m * k; oR += k * n
     meta = tuple(meta)
-    x = dev(rng.normal(size=off)).requires_grad_(True)
+    x = dev(rng.normal(size=off) + (1j * rng.normal(size=off) if cplx else 0)).requires_grad_(True)
     assert torch.autograd.gradcheck(lambda d: BK.qr(d, meta, (oQ, oR)), (x,), eps=1e-6, atol=1e-7)

@@ -80,6 +80,26 @@ def test_oracle_fix_signs_golden_matrix():
     assert any(b.shape == (2, 2) and np.abs(b - gold['(1,1)']).max() < 1e-12 for b in blocks)
 
 
+def test_oracle_fix_signs_adjoint_matches_reference_autograd():
+    """The adjoint of fix_svd_signs (real, and complex with the gradient through each column's
+    phase) against torch's autograd of the reference's backend_torch.fix_svd_signs."""
+    import json, os
+    from yastn_gb300.workloads import GOLDEN, _decode
+    with open(os.path.join(GOLDEN, 'fix_signs_adjoint.json')) as f:
+        calls = json.load(f)['calls']
+    z = np.load(os.path.join(GOLDEN, 'fix_signs_adjoint.npz'))
+    kinds = set()
+    for c in calls:
+        meta = _decode(c['meta'], None)
+        U, V, gU, gV = (z[c[k]] for k in ('U', 'V', 'gU', 'gV'))
+        Uf, Vf = oracle.fix_svd_signs(U, V, meta)
+        assert _rel(Uf, z[c['Uf']]) < 1e-14 and _rel(Vf, z[c['Vf']]) < 1e-14
+        dU, dV = oracle.fix_svd_signs_backward(U, V, gU, gV, meta)
+        assert _rel(dU, z[c['dU']]) < 1e-12 and _rel(dV, z[c['dV']]) < 1e-12
+        kinds.add(np.iscomplexobj(U))
+    assert kinds == {False, True}
+
+
 def _decode_opts(opts):
     out = {}
     for k, v in opts.items():

@@ -37,13 +37,14 @@ SIGNATURES = {
     'yb_eigh_adjoint_core': ([_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _vp], _i),
     'yb_mask_gather': ([_vp, _vp, _i, _vp, _vp, _i, _vp, _i, _vp], _i),
     'yb_fix_signs': ([_vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp], _i),
+    'yb_fix_signs_adjoint': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp], _i),
     'yb_ozaki_split': ([_vp, _vp, _vp, _vp, _i, _i, _i, _vp], _i),
-    'yb_ozaki_split_tiled': ([_vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp], _i),
+    'yb_ozaki_exponents': ([_vp, _vp, _vp, _i, _i, _i, _vp], _i),
     'yb_ozaki_gemm': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
-    'yb_ozaki_gemm_tc': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
+    'yb_ozaki_gemm_fused': ([_vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
     'yb_ozaki_device_error': ([_vp, _i, _vp], _i),
-    'yb_ozaki_dot_static': ([_vp, _vp, _vp, _vp, _i, _i, _vp, _i, _i, _vp, _i, _vp, _i, _vp, _vp, _i, _i,
-                             _i64, _i64, _i64, _i64, _i64, _vp], _i),
+    'yb_ozaki_dot_static': ([_vp, _vp, _vp, _i, _vp, _i, _i, _vp, _i, _i, _vp, _i, _vp, _i, _vp, _vp, _i,
+                             _vp, _vp, _vp, _i, _i, _i64, _i64, _i64, _i64, _i64, _vp], _i),
     'yb_truncation_mask': ([_vp, _i64, _vp, _vp, _i, _d, _i64, _i, _vp, _vp, _vp], _i),
 }
 

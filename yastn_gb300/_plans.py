@@ -409,11 +409,11 @@ def _records(out_list):
     return outs, terms, flops
 
 
-def _pack_gemm(out_list):
+def _pack_gemm(out_list, allow_split=True):
     """out_list: [(c_off, m, n, ldc, [term tuples])] -> GemmPlan. When the outputs make
     too few tiles for the GPU, outputs with a long K are split into K chunks computed into
-    a workspace and summed by a reduction pass (split-K)."""
-    ck = _split_chunk_k(out_list)
+    a workspace and summed by a reduction pass (split-K; not with ``allow_split=False``)."""
+    ck = _split_chunk_k(out_list) if allow_split else None
     split = None
     if ck is not None:
         direct, parts, red, tasks, ws = [], [], [], [], 0
@@ -501,17 +501,45 @@ OZAKI_MIN_DIM = 16  # sector GEMMs contracting fewer indices than this stay on t
 OZAKI_SKINNY_ROWS = 8  # sector GEMMs with at most this many rows (and more than 64 columns) too
 
 
-def _tiled_recs(recs, s, th):
-    """Split records with destinations in the tcgen05 tile layout: each operand block takes
-    s * ceil(rows / th) * th * Kp digits. Returns (records, total size, old offset -> new)."""
-    out = recs.copy()
-    size, remap = 0, {}
-    for i, r in enumerate(recs):
-        rows, Kp = int(r[1]), int(r[7])
-        remap[int(r[5])] = size
-        out[i, 5] = size
-        size += s * (-(-rows // th) * th) * Kp
-    return out, size, remap
+def _fused_records(plan, meta_dot, cplx):
+    """Records of the fused tcgen05 kernel (yb_ozaki_exponents + yb_ozaki_gemm_fused) for the
+    sectors ``plan`` emulates: exponent records per A block (rows) and per B block (columns),
+    one output record per sector (two for complex data: the real and the imaginary part,
+    C_r = [A_r, A_i][B_r; -B_i] and C_i = [A_r, A_i][B_i; B_r]) and 128 x 64 tiles, the
+    longest K first."""
+    a_map, b_map, ea, eb, outs = {}, {}, [], [], []
+    n_exp = 0
+    f = 2 if cplx else 1
+    for slc, Dc, sla, Da, slb, Db in meta_dot:
+        m, K = Da
+        n = Db[1]
+        if K < OZAKI_MIN_DIM or (m <= OZAKI_SKINNY_ROWS and n > GEMM_TILE):
+            continue
+        if sla[0] not in a_map:
+            a_map[sla[0]] = n_exp
+            ea.append((sla[0], m, K, K, int(cplx), n_exp, 0, 0))
+            n_exp += m
+        if slb[0] not in b_map:
+            b_map[slb[0]] = n_exp
+            eb.append((slb[0], K, n, n, int(cplx), n_exp, 0, 0))
+            n_exp += n
+        for part in range(f):
+            outs.append((f * slc[0] + part, m, n, f * n, sla[0], a_map[sla[0]], slb[0], b_map[slb[0]], K, K, f, part,
+                         int(cplx), n, 0, 0))
+    tiles = []
+    for oi, o in enumerate(outs):
+        m, n, K = int(o[1]), int(o[2]), int(o[8])
+        for tr in range(-(-m // OZAKI_TC_M)):
+            for tc in range(-(-n // OZAKI_TC_N)):
+                tiles.append((f * K, oi, tr, tc))
+    tiles.sort(key=lambda x: -x[0])
+    plan.exp_a = np.array(ea, dtype=np.int64).reshape(-1, 8)
+    plan.exp_b = np.array(eb, dtype=np.int64).reshape(-1, 8)
+    plan.exp_a_max = int(plan.exp_a[:, 1].max()) if len(ea) else 0
+    plan.exp_b_max = int(plan.exp_b[:, 2].max()) if len(eb) else 0
+    plan.n_exps = n_exp
+    plan.outs_f = np.array(outs, dtype=np.int64).reshape(-1, 16)
+    plan.tiles_f = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles], dtype=np.int32).reshape(-1, 4)
 
 
 def ozaki_dot_plan(meta_dot, s, cplx=False):
@@ -569,15 +597,6 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
                     tiles.append((K, oi, tr, tc))
         tiles.sort(key=lambda x: -x[0])
         tiles = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles], dtype=np.int32).reshape(-1, 4)
-        # 128 x 64 tiles of the tcgen05 kernel, longest K first
-        tiles_tc = []
-        for oi, o in enumerate(outs):
-            m, n, K = int(o[1]), int(o[2]), int(o[8])
-            for tr in range((m + OZAKI_TC_M - 1) // OZAKI_TC_M):
-                for tc in range((n + OZAKI_TC_N - 1) // OZAKI_TC_N):
-                    tiles_tc.append((K, oi, tr, tc))
-        tiles_tc.sort(key=lambda x: -x[0])
-        tiles_tc = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles_tc], dtype=np.int32).reshape(-1, 4)
         a_recs = np.array(a_recs, dtype=np.int64).reshape(-1, 8)
         b_recs = np.array(b_recs, dtype=np.int64).reshape(-1, 8)
         a_rows = int(a_recs[:, 1].max()) if len(a_recs) else 0
@@ -586,15 +605,8 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
         plan.bT = CopyPlan([t for t in bT_tasks if t[2][0] * t[2][1] > 0], bT_size, bT_size)
         plan.bT_size = bT_size
         plan.native = _pack_gemm(small)
-        plan.tiles_tc = tiles_tc
-        # tcgen05 operands: digit planes in tile layout (rows padded to 128 for A, 64 for B)
-        plan.a_recs_tc, plan.a_size_tc, a_off_tc = _tiled_recs(a_recs, s, OZAKI_TC_M)
-        plan.b_recs_tc, plan.b_size_tc, b_off_tc = _tiled_recs(b_recs, s, OZAKI_TC_N)
-        outs_tc = outs.copy()
-        if len(outs_tc):
-            outs_tc[:, 4] = [a_off_tc[int(x)] for x in outs[:, 4]]
-            outs_tc[:, 6] = [b_off_tc[int(x)] for x in outs[:, 6]]
-        plan.outs_tc = outs_tc
+        plan.native_direct = _pack_gemm(small, allow_split=False)  # no chunk workspace
+        _fused_records(plan, meta_dot, cplx)
         # padded MMA work of the two tilings: the tcgen05 kernel (128 x 64 tiles) when its
         # padding costs little more than the 64 x 64 tiles of the mma.sync kernel
         w64 = sum(-(-int(o[1]) // 64) * 64 * -(-int(o[2]) // 64) * 64 * int(o[9]) for o in outs)
@@ -772,12 +784,13 @@ def qr_plan(meta, cplx=False):
             recs.append(rec)
             max_k = max(max_k, k)
             q0, r0, a0 = slQ[0], slR[0], sl[0]
+            cj = int(cplx)  # conjugation flags of the complex adjoint (bit 0: A, bit 1: B)
             if n > m:   # R[:, m:] = Q^H A[:, m:]
-                right.append((r0 + m, k, n - m, n, [(q0, a0 + m, m, 1, k, n, 1, int(cplx))]))
-                w1.append((q0, m, m, k, [(a0 + m, r0 + m, n - m, n, 1, 1, n, 0)]))      # gQ' += A[:, m:] gV^T
+                right.append((r0 + m, k, n - m, n, [(q0, a0 + m, m, 1, k, n, 1, cj)]))
+                w1.append((q0, m, m, k, [(a0 + m, r0 + m, n - m, n, 1, 1, n, 2 * cj)]))  # gQ' += A[:, m:] gV^H
                 y1.append((a0 + m, m, n - m, n, [(q0, r0 + m, m, k, 1, n, 1, 0)]))      # dA[:, m:] = Q gV
-            m1.append((mo, k, k, k, [(r0, r0, k, n, 1, 1, n, 0)]))                       # M = U gU^T
-            m2.append((mo, k, k, k, [(q0, q0, m, 1, k, k, 1, 0)]))                       # M -= gQ'^T Q
+            m1.append((mo, k, k, k, [(r0, r0, k, n, 1, 1, n, 2 * cj)]))                  # M = U gU^H
+            m2.append((mo, k, k, k, [(q0, q0, m, 1, k, k, 1, cj)]))                      # M -= gQ'^H Q
             s1.append((q0, m, k, k, [(q0, mo, k, k, 1, k, 1, 0)]))                       # gQ' += Q copyltu(M)
             adj.append((mo, k, q0, m, k, r0, n, 0))
             copies.append((q0, a0, [m, k], [k, 1], [n, 1]))

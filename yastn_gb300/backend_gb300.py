@@ -225,20 +225,21 @@ class _Eigh(torch.autograd.Function):
 
 
 class _FixSigns(torch.autograd.Function):
-    """fix_svd_signs (backend_torch.py:353-366) for real data: the phases are +-1 and
-    constant almost everywhere, so the adjoint multiplies the cotangents by them."""
+    """fix_svd_signs (backend_torch.py:353-366); the adjoint (yb_fix_signs_adjoint) follows
+    torch's autograd of the reference: the cotangents times the phases and, for complex data,
+    the gradient through the phase of each column's largest entry."""
 
     @staticmethod
     def forward(ctx, U, V, meta):
-        Uo, Vo, ph = ops.fix_svd_signs(U, V, meta)
-        ctx.save_for_backward(ph)
+        Uo, Vo, _ = ops.fix_svd_signs(U, V, meta)
+        ctx.save_for_backward(U, V)
         ctx.meta = meta
         return Uo, Vo
 
     @staticmethod
     def backward(ctx, gU, gV):
-        (ph,) = ctx.saved_tensors
-        gUi, gVi = ops.fix_svd_signs_backward(gU, gV, ph, ctx.meta)
+        U, V = ctx.saved_tensors
+        gUi, gVi = ops.fix_svd_signs_backward(U, V, gU, gV, ctx.meta)
         return gUi, gVi, None
 
 
@@ -281,8 +282,6 @@ def svdvals(data, meta, sizeS, **kwargs):
 
 
 def fix_svd_signs(Udata, Vhdata, meta):
-    if Udata.is_complex() and (Udata.requires_grad or Vhdata.requires_grad):
-        raise NotImplementedError("yastn_gb300 fix_svd_signs: adjoint for complex phases is not implemented")
     return _FixSigns.apply(Udata, Vhdata, meta)
 
 
@@ -554,7 +553,8 @@ def eigvals(data, meta, sizeS, **kwargs):
 
 class _Qr(torch.autograd.Function):
     """qr (backend_torch.py:475-484): batched Householder QR, positive diagonal of R; the
-    adjoint of real blocks by grouped GEMMs, a symmetrisation and a triangular solve."""
+    adjoint (real and complex blocks) by grouped GEMMs, a symmetrisation and a triangular
+    solve."""
 
     @staticmethod
     def forward(ctx, data, meta, sizes):
@@ -566,8 +566,6 @@ class _Qr(torch.autograd.Function):
     @staticmethod
     def backward(ctx, gQ, gR):
         data, Q, R = ctx.saved_tensors
-        if Q.is_complex():
-            raise NotImplementedError("yastn_gb300 qr: the adjoint of complex blocks is not implemented")
         return ops.qr_backward(Q, R, gQ, gR, data, ctx.meta), None, None
 
 
@@ -581,7 +579,15 @@ def pinv(A, rcond=None, hermitian=False, out=None, atol=None, rtol=None):
 
 def eigh(data, meta=None, sizes=(1, 1), order_by_magnitude=False, ad_decomp_reg=1.0e-12):
     if meta is None:
-        _not_hot('eigh of a single dense matrix')
+        # one dense D x D matrix (YASTN's eigs diagonalises its Krylov matrix this way,
+        # yastn/krylov/_krylov.py:231): the batched kernel on a single block; (S ascending, U)
+        # as torch.linalg.eigh returns them (backend_torch.py:384)
+        D = int(data.shape[0])
+        if data.dim() != 2 or data.shape[1] != D:
+            raise ValueError("eigh of a dense matrix needs a square 2-D tensor")
+        meta1 = (((0, D * D), (D, D), (0, D * D), (D, D), (0, D)),)
+        S, U = _Eigh.apply(data.reshape(-1), meta1, (D, D * D), order_by_magnitude, ad_decomp_reg)
+        return S, U.reshape(D, D)
     return _Eigh.apply(data, meta, sizes, order_by_magnitude, ad_decomp_reg)
 
 

@@ -160,38 +160,66 @@ __global__ void eigh_adjoint_core_kernel(const typename Elt<Cx>::T* __restrict__
   }
 }
 
-// QR adjoint (real): records YB_QRADJ_REC int64 per block: [0] M offset (k x k) [1] k
+// QR adjoint: records YB_QRADJ_REC int64 per block: [0] M offset (k x k) [1] k
 // [2] B offset (rows x k, row-major, leading dimension [4]) [3] rows [4] ldb
 // [5] R offset (k x k upper triangle, leading dimension [6]) [6] ldr.
-// copyltu: M <- tril(M) + tril(M, -1)^T (the upper triangle mirrored from the lower).
+// copyltu: M <- tril(M, -1) + tril(M, -1)^H + Re diag(M) (the upper triangle mirrored from
+// the lower, conjugated for complex data, whose diagonal keeps its real part).
+template <bool Cx>
 __global__ void qr_copyltu_kernel(double* __restrict__ M, const int64_t* __restrict__ recs) {
   const int64_t* r = recs + (int64_t)blockIdx.y * YB_QRADJ_REC;
   const int64_t k = r[1];
-  double* m = M + r[0];
+  double* m = M + (Cx ? 2 : 1) * r[0];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < k * k; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = e / k, j = e - i * k;
-    if (i < j) m[e] = m[j * k + i];  // writes the upper triangle only, reads the lower
+    if (Cx) {
+      if (i < j) {  // writes the upper triangle only, reads the lower
+        m[2 * e] = m[2 * (j * k + i)];
+        m[2 * e + 1] = -m[2 * (j * k + i) + 1];
+      } else if (i == j) {
+        m[2 * e + 1] = 0.0;
+      }
+    } else {
+      if (i < j) m[e] = m[j * k + i];
+    }
   }
 }
 
-// B <- B R^{-T} row by row (R upper triangular): x R^T = b, i.e. R x^T = b^T by back
-// substitution, one warp per row, in place. Entries of x already solved are re-read from L2
-// (written by lane 0 of the same warp, ordered by __syncwarp).
+// B <- B R^{-H} row by row (R upper triangular with a real diagonal): x R^H = b, i.e.
+// x_j = (b_j - sum_{l > j} x_l conj(R_jl)) / R_jj by back substitution, one warp per row, in
+// place. Entries of x already solved are re-read from L2 (written by lane 0 of the same warp,
+// ordered by __syncwarp).
+template <bool Cx>
 __global__ void trsm_rt_kernel(double* __restrict__ B, const double* __restrict__ Rm, const int64_t* __restrict__ recs) {
+  constexpr int W = Cx ? 2 : 1;
   const int64_t* r = recs + (int64_t)blockIdx.y * YB_QRADJ_REC;
   const int64_t k = r[1], rows = r[3], ldb = r[4], ldr = r[6];
-  double* b = B + r[2];
-  const double* R = Rm + r[5];
+  double* b = B + W * r[2];
+  const double* R = Rm + W * r[5];
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t row = warp; row < rows; row += nwarps) {
-    double* x = b + row * ldb;
+    double* x = b + W * row * ldb;
     for (int64_t j = k - 1; j >= 0; --j) {
-      double acc = 0.0;
-      for (int64_t l = j + 1 + lane; l < k; l += 32) acc = fma(R[j * ldr + l], __ldcg(x + l), acc);
-      acc = warp_sum(acc);
-      if (lane == 0) x[j] = (__ldcg(x + j) - acc) / R[j * ldr + j];
+      double ar = 0.0, ai = 0.0;
+      for (int64_t l = j + 1 + lane; l < k; l += 32) {
+        if (Cx) {  // x_l conj(R_jl)
+          const double rr = R[2 * (j * ldr + l)], ri = R[2 * (j * ldr + l) + 1];
+          const double xr = __ldcg(x + 2 * l), xi = __ldcg(x + 2 * l + 1);
+          ar = fma(xr, rr, fma(xi, ri, ar));
+          ai = fma(xi, rr, fma(-xr, ri, ai));
+        } else {
+          ar = fma(R[j * ldr + l], __ldcg(x + l), ar);
+        }
+      }
+      ar = warp_sum(ar);
+      if (Cx) ai = warp_sum(ai);
+      if (lane == 0) {
+        const double d = R[W * (j * ldr + j)];  // real and positive
+        x[W * j] = (__ldcg(x + W * j) - ar) / d;
+        if (Cx) x[2 * j + 1] = (__ldcg(x + 2 * j + 1) - ai) / d;
+      }
       __syncwarp();
     }
   }
@@ -203,17 +231,22 @@ __global__ void trsm_rt_kernel(double* __restrict__ B, const double* __restrict_
 extern "C" int yb_qr_adjoint_sym(void* M, const int64_t* recs, int n_blocks, int dtype, void* stream) {
   if (n_blocks == 0) return YB_OK;
   if (!M || !recs) return YB_ERR_INVALID;
-  if (dtype != YB_F64) return YB_ERR_INVALID;
-  yb::qr_copyltu_kernel<<<dim3(16, (unsigned)n_blocks), 256, 0, (cudaStream_t)stream>>>((double*)M, recs);
+  const dim3 grid(16, (unsigned)n_blocks);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == YB_F64) yb::qr_copyltu_kernel<false><<<grid, 256, 0, s>>>((double*)M, recs);
+  else if (dtype == YB_C128) yb::qr_copyltu_kernel<true><<<grid, 256, 0, s>>>((double*)M, recs);
+  else return YB_ERR_INVALID;
   return yb::check_launch();
 }
 
 extern "C" int yb_trsm_rt(void* B, const void* R, const int64_t* recs, int n_blocks, int dtype, void* stream) {
   if (n_blocks == 0) return YB_OK;
   if (!B || !R || !recs) return YB_ERR_INVALID;
-  if (dtype != YB_F64) return YB_ERR_INVALID;
-  yb::trsm_rt_kernel<<<dim3(32, (unsigned)n_blocks), 256, 0, (cudaStream_t)stream>>>((double*)B, (const double*)R,
-                                                                                      recs);
+  const dim3 grid(32, (unsigned)n_blocks);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == YB_F64) yb::trsm_rt_kernel<false><<<grid, 256, 0, s>>>((double*)B, (const double*)R, recs);
+  else if (dtype == YB_C128) yb::trsm_rt_kernel<true><<<grid, 256, 0, s>>>((double*)B, (const double*)R, recs);
+  else return YB_ERR_INVALID;
   return yb::check_launch();
 }
 

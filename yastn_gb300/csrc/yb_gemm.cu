@@ -83,14 +83,22 @@ __device__ __forceinline__ void skinny_tile(const typename F::T* __restrict__ A,
         Ak[l * M + i] = v;
       }
       __syncthreads();
-      const int64_t kn = min((int64_t)kSkinnyK, K - k0);
-      const T* Rk = Ra + k0 * r_ls;
-      for (int64_t l = 0; l < kn; ++l) {
+      const int kn = (int)min((int64_t)kSkinnyK, K - k0);
+      // per-column pointers into op(B) computed once per chunk; the k loop only adds r_ls
+      const T* col[CPT];
+      bool live[CPT];
+#pragma unroll
+      for (int u = 0; u < CPT; ++u) {
+        const int64_t j = j0 + u * kThreads;
+        live[u] = j < nc;
+        col[u] = Ra + k0 * r_ls + (live[u] ? j * r_js : 0);
+      }
+      for (int l = 0; l < kn; ++l) {
         T b[CPT];
 #pragma unroll
         for (int u = 0; u < CPT; ++u) {
-          const int64_t j = j0 + u * kThreads;
-          b[u] = (j < nc) ? Rk[l * r_ls + j * r_js] : F::zero();
+          b[u] = live[u] ? __ldg(col[u]) : F::zero();
+          col[u] += r_ls;
           if (conjR) b[u] = F::conj(b[u]);
         }
 #pragma unroll
@@ -110,7 +118,7 @@ __device__ __forceinline__ void skinny_tile(const typename F::T* __restrict__ A,
     for (int i = 0; i < M; ++i) {
       if (i >= mr) break;
       T* p = C + c_off + i * ldc + j;
-      T v = F::scale(acc[u][i], alpha);
+      T v = alpha == 1.0 ? acc[u][i] : F::scale(acc[u][i], alpha);  // no FP64 multiply for alpha = 1
       if (beta != 0.0) v = F::add(v, F::scale(*p, beta));
       *p = v;
     }

@@ -243,6 +243,92 @@ __global__ void fix_signs_kernel(const double* __restrict__ Uin, const double* _
   }
 }
 
+
+// Adjoint of the gauge fix (torch's autograd of the reference's fix_svd_signs,
+// backend_torch.py:353-366; complex gradients in torch's convention): per column c, with
+// p = U[r*, c] / |U[r*, c]| at the forward's row choice r* (recomputed from U by the same rule),
+// dU[:, c] = gU[:, c] p, dVh[c, :] = gVh[c, :] conj(p), and for complex data
+// dU[r*, c] += -i (p / |U[r*, c]|) Im(conj(G) p), G = sum_i U[i, c] conj(gU[i, c]) +
+// sum_j conj(Vh[c, j]) gVh[c, j] (the gradient through the phase).
+template <bool Cx>
+__global__ void fix_signs_adjoint_kernel(const double* __restrict__ Uin, const double* __restrict__ Vin,
+                                         const double* __restrict__ gU, const double* __restrict__ gV,
+                                         double* __restrict__ dU, double* __restrict__ dV,
+                                         const int64_t* __restrict__ blocks) {
+  constexpr int W = Cx ? 2 : 1;
+  const int64_t* r = blocks + (int64_t)blockIdx.y * YB_SVD_REC;
+  const int64_t m = r[1], n = r[2], k = r[9];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+  if (c >= k) return;
+  const int64_t uo = W * r[3], vo = W * r[5];
+  const double* U = Uin + uo;
+  const double* V = Vin + vo;
+  long long best = -1;
+  int64_t brow = 0;
+  for (int64_t row = lane; row < m; row += 32) {
+    const double a = Cx ? hypot(U[2 * (row * k + c)], U[2 * (row * k + c) + 1]) : fabs(U[row * k + c]);
+    const long long amp = (long long)(a * 1099511627776.0);  // as the forward's int64(|U| 2^40)
+    if (amp > best) { best = amp; brow = row; }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const int64_t orow = __shfl_xor_sync(0xffffffffu, brow, o);
+    if (ob > best || (ob == best && orow < brow)) { best = ob; brow = orow; }
+  }
+  double pr, pi = 0.0, au;
+  if (Cx) {
+    const double ur = U[2 * (brow * k + c)], ui = U[2 * (brow * k + c) + 1];
+    au = hypot(ur, ui);
+    pr = ur / au;
+    pi = ui / au;
+  } else {
+    const double u = U[brow * k + c];
+    au = fabs(u);
+    pr = u / au;
+  }
+  double Gr = 0.0, Gi = 0.0;
+  for (int64_t row = lane; row < m; row += 32) {
+    const int64_t e = row * k + c;
+    if (Cx) {  // U conj(gU)
+      const double ur = U[2 * e], ui = U[2 * e + 1], gr = gU[uo + 2 * e], gi = gU[uo + 2 * e + 1];
+      Gr += ur * gr + ui * gi;
+      Gi += ui * gr - ur * gi;
+      dU[uo + 2 * e] = gr * pr - gi * pi;
+      dU[uo + 2 * e + 1] = gr * pi + gi * pr;
+    } else {
+      dU[uo + e] = gU[uo + e] * pr;
+    }
+  }
+  for (int64_t col = lane; col < n; col += 32) {
+    const int64_t e = c * n + col;
+    if (Cx) {  // conj(V) gV
+      const double vr = V[2 * e], vi = V[2 * e + 1], gr = gV[vo + 2 * e], gi = gV[vo + 2 * e + 1];
+      Gr += vr * gr + vi * gi;
+      Gi += vr * gi - vi * gr;
+      dV[vo + 2 * e] = gr * pr + gi * pi;
+      dV[vo + 2 * e + 1] = gi * pr - gr * pi;
+    } else {
+      dV[vo + e] = gV[vo + e] * pr;
+    }
+  }
+  if (Cx) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      Gr += __shfl_xor_sync(0xffffffffu, Gr, o);
+      Gi += __shfl_xor_sync(0xffffffffu, Gi, o);
+    }
+    __syncwarp();
+    if (lane == (int)(brow & 31)) {  // the lane that wrote dU[r*, c]
+      const double t = (Gr * pi - Gi * pr) / au;  // Im(conj(G) p) / |u|
+      const int64_t e = brow * k + c;
+      dU[uo + 2 * e] += pi * t;
+      dU[uo + 2 * e + 1] -= pr * t;
+    }
+  }
+}
+
 }  // namespace
 }  // namespace yb
 
@@ -293,6 +379,25 @@ int yb_fix_signs(const void* Uin, const void* Vin, void* Uout, void* Vout, void*
   else if (dtype == YB_C128)
     yb::fix_signs_kernel<true><<<grid, 256, 0, s>>>((const double*)Uin, (const double*)Vin, (double*)Uout,
                                                     (double*)Vout, (double*)phase_out, blocks, apply_given);
+  else
+    return YB_ERR_INVALID;
+  return yb::check_launch();
+}
+
+int yb_fix_signs_adjoint(const void* Uin, const void* Vin, const void* gU, const void* gV, void* dU, void* dV,
+                         const int64_t* blocks, int n_blocks, int max_k, int dtype, void* stream) {
+  if (n_blocks == 0 || max_k == 0) return YB_OK;
+  if (!Uin || !Vin || !gU || !gV || !dU || !dV || !blocks || max_k < 0) return YB_ERR_INVALID;
+  dim3 grid((unsigned)((max_k + 7) / 8), (unsigned)n_blocks);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == YB_F64)
+    yb::fix_signs_adjoint_kernel<false><<<grid, 256, 0, s>>>((const double*)Uin, (const double*)Vin,
+                                                             (const double*)gU, (const double*)gV, (double*)dU,
+                                                             (double*)dV, blocks);
+  else if (dtype == YB_C128)
+    yb::fix_signs_adjoint_kernel<true><<<grid, 256, 0, s>>>((const double*)Uin, (const double*)Vin,
+                                                            (const double*)gU, (const double*)gV, (double*)dU,
+                                                            (double*)dV, blocks);
   else
     return YB_ERR_INVALID;
   return yb::check_launch();

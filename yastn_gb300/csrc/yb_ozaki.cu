@@ -20,13 +20,14 @@
 // GEMM kernel: 64x64 output tile per CTA, 8 warps each owning a 32x16 sub-tile (2x2
 // mma.sync.m16n8k16 tiles), K-step 16 staged in shared memory with cp.async (double
 // buffered, rows padded to 48 bytes so ldmatrix is bank-conflict free).
-#include <cuda_bf16.h>
 #include <atomic>
 #include <mutex>
-#include "yb_common.cuh"
+#include "yb_ozaki_common.cuh"
 
 namespace yb {
 namespace {
+using oz::scaled_rint;
+using oz::scale_pow2;
 
 constexpr int kTile = 64;
 constexpr int kK = 16;
@@ -52,30 +53,6 @@ constexpr int kThreads = 256;
 // U = Q + 64 (1 + 128 + ... + 128^{s-2}): d_t = ((U >> 7(s-1-t)) & 127) - 64 for t >= 1 and
 // the leading digit d_0 = U >> 7(s-1) in [-128, 128] (arithmetic shift). This represents
 // a 2^-e = sum_t d_t 2^{-7(t+1)} up to the rounding of Q (half a unit of the last digit).
-__device__ __forceinline__ long long scaled_rint(long long bits, int e, int s) {
-  const long long mag = bits & 0x7fffffffffffffffll;
-  if (mag == 0) return 0;
-  const int E = (int)(mag >> 52);
-  long long M = mag & 0xfffffffffffffll;
-  int ex = -1074;  // a = M 2^ex
-  if (E != 0) {
-    M |= 1ll << 52;
-    ex = E - 1075;
-  }
-  const int up = ex + 7 * s - e;  // Q = rint(M 2^up)
-  long long q;
-  if (up >= 0) {
-    q = M << up;  // |Q| < 2^{7s}: up <= 7s - 53
-  } else {
-    const int sh = min(-up, 63);
-    q = M >> sh;
-    const unsigned long long rem = (unsigned long long)M & ((1ull << sh) - 1ull);
-    const unsigned long long half = 1ull << (sh - 1);
-    if (rem > half || (rem == half && (q & 1))) ++q;
-  }
-  return bits < 0 ? -q : q;
-}
-
 __device__ __forceinline__ void digits_of(long long bits, int e, int s, int* d) {
   long long bias = 0;
   for (int t = 0; t < s - 1; ++t) bias = (bias << 7) | 64;
@@ -145,50 +122,6 @@ __global__ void split_rows_kernel(const double* __restrict__ src, __nv_bfloat16*
   }
 }
 
-// The same split written in the tensor-core tile layout of the tcgen05 GEMM: per slice, the
-// rows are grouped in tiles of TH (128 for A, 64 for B) and K in steps of 16; every
-// (row tile, K step) is one contiguous TH x 16 block in the canonical K-major layout of the
-// tcgen05 matrix descriptors (8-row x 16-byte core matrices: byte offset of (row r, k) is
-// (r/8)*256 + (k/8)*128 + (r%8)*16 + (k%8)*2), so a GEMM stage is a few bulk copies. Rows
-// from the operand's row count up to the next multiple of TH are written as zeros.
-__global__ void split_rows_tiled_kernel(const double* __restrict__ src, __nv_bfloat16* __restrict__ slices,
-                                        int* __restrict__ exps, const int64_t* __restrict__ recs, int s, int TH) {
-  const int64_t* r = recs + (int64_t)blockIdx.y * 8;
-  const int64_t rows = r[1], K = r[2], Kp = r[7];
-  const int64_t rows_p = (rows + TH - 1) / TH * TH;
-  const int lane = threadIdx.x & 31;
-  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (row >= rows_p) return;
-  const bool live = row < rows;
-  const RowSrc a = row_src(src, r, live ? row : 0);
-  long long mx = 0;
-  if (live)
-    for (int64_t l = lane; l < K; l += 32) mx = max(mx, a(l) & 0x7fffffffffffffffll);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  int e = 0;
-  if (mx >= (1ll << 52)) e = (int)(mx >> 52) - 1022;
-  else if (mx > 0) frexp(__longlong_as_double(mx), &e);
-  if (live && lane == 0) exps[r[6] + row] = e;
-  const int64_t slice_stride = rows_p * Kp;
-  const int64_t ksteps = Kp / 16;
-  __nv_bfloat16* base = slices + r[5] + (row / TH) * ksteps * (int64_t)TH * 16;
-  const int rr = (int)(row % TH);
-  const int64_t in_tile = (int64_t)(rr >> 3) * 128 + (rr & 7) * 8;  // elements
-  for (int64_t l = 2 * lane; l < Kp; l += 64) {
-    int d0[8], d1[8];
-    if (live && l < K) digits_of(a(l), e, s, d0); else for (int t = 0; t < 8; ++t) d0[t] = 0;
-    if (live && l + 1 < K) digits_of(a(l + 1), e, s, d1); else for (int t = 0; t < 8; ++t) d1[t] = 0;
-    const int64_t off = (l >> 4) * (int64_t)TH * 16 + in_tile + ((l & 15) >> 3) * 64 + (l & 7);
-    for (int t = 0; t < s; ++t) {
-      __nv_bfloat162 v;
-      v.x = __int2bfloat16_rn(d0[t]);
-      v.y = __int2bfloat16_rn(d1[t]);
-      *reinterpret_cast<__nv_bfloat162*>(base + t * slice_stride + off) = v;
-    }
-  }
-}
-
 // ------------------------------------------------------------------ GEMM
 // Exact conversions built on the integer pipe (GB300 issues FP64 arithmetic at a small
 // fraction of its integer rate): v 2^E for an integer |v| < 2^53 is assembled from the
@@ -203,14 +136,6 @@ __device__ __forceinline__ double int_to_double_scaled(long long v, int E) {
   const unsigned long long frac = (mag << (52 - p)) & 0xfffffffffffffull;
   if (be >= 1 && be <= 2046) return __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) | frac));
   return scalbn(__longlong_as_double((long long)(sgn | (1023ull + (unsigned long long)p) << 52 | frac)) , E);
-}
-
-// x 2^E by an exponent-field add when x and the result are normal doubles.
-__device__ __forceinline__ double scale_pow2(double x, int E) {
-  const long long b = __double_as_longlong(x);
-  const int be = (int)((b >> 52) & 0x7ff);
-  if (be == 0 || be == 0x7ff || be + E < 1 || be + E > 2046) return scalbn(x, E);
-  return __longlong_as_double(b + ((long long)E << 52));
 }
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
@@ -372,242 +297,6 @@ int launch_gemm(const void* As, const int* Ae, const void* Bs, const int* Be, do
   return check_launch();
 }
 
-// ------------------------------------------------------------------ GEMM, tcgen05 / TMEM
-// The same products on the 5th-generation tensor cores: a CTA computes a 128 x 64 output
-// tile; the 8 digit diagonals are FP32 accumulators of 128 lanes x 64 columns in tensor
-// memory (8 x 64 = all 512 TMEM columns, so one CTA per SM). One thread issues the 36
-// tcgen05.mma (M=128, N=64, K=16, BF16 -> FP32) of a K-step, reading the digit tiles from
-// shared memory through matrix descriptors (canonical K-major layout without swizzle:
-// 8 x 16-byte core matrices, 128 bytes apart along K and 256 bytes apart along M/N);
-// tcgen05.commit arrives on the stage's mbarrier when they complete. The operands stream
-// through a 4-stage cp.async ring (48 KB per stage); a stage is refilled once the MMAs that
-// read it have completed. At the end of every 400-long K-chunk all 4 warps read their 32
-// TMEM lanes (tcgen05.ld) and fold the 8 diagonals exactly into two int64 halves and FP64
-// registers (the next chunk's first MMAs overwrite the accumulators). Every mbarrier wait is
-// bounded: on a timeout the CTA records yb_ozaki_device_error, waits (bounded) for its
-// MMAs, frees its TMEM and writes nothing.
-constexpr int kTcM = 128;
-constexpr int kTcN = 64;
-constexpr int kTcStages = 4;
-constexpr int kTcThreads = 128;
-constexpr long long kTcSpinLimit = 1ll << 24;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// shared-memory matrix descriptor: canonical K-major, no swizzle, LBO = 128 B (between the two
-// 8-element core matrices of a 16-long K step), SBO = 256 B (between 8-row groups)
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
-  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
-         ((uint64_t)1 << 46);
-}
-
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-  for (long long it = 0; it < kTcSpinLimit; ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(mbar), "r"(parity)
-        : "memory");
-    if (ok) return true;
-  }
-  return false;
-}
-
-__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-      "l"(a), "l"(b), "r"(idesc), "r"(acc));
-}
-
-__device__ __forceinline__ void tc_ld8(uint32_t taddr, uint32_t* r) {
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr));
-}
-
-__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(src), "r"(bytes), "r"(mbar)
-               : "memory");
-}
-
-__device__ __forceinline__ void tc_commit(uint32_t mbar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
-}
-
-template <int S>
-__global__ void __launch_bounds__(kTcThreads, 1)
-    ozaki_gemm_tc_kernel(const __nv_bfloat16* __restrict__ As, const int* __restrict__ Ae,
-                         const __nv_bfloat16* __restrict__ Bs, const int* __restrict__ Be, double* __restrict__ C,
-                         const int64_t* __restrict__ outs, const int32_t* __restrict__ tiles, int* __restrict__ err) {
-  constexpr uint32_t kATile = kTcM * kK * 2;  // 4096 B: one slice's 128 x 16 digit tile
-  constexpr uint32_t kBTile = kTcN * kK * 2;  // 2048 B
-  constexpr uint32_t kStage = S * (kATile + kBTile);
-  extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint32_t tmem_slot;
-  __shared__ __align__(8) uint64_t full[kTcStages], empty[kTcStages], accb;
-  __shared__ int failed;
-  const int4 tl = reinterpret_cast<const int4*>(tiles)[blockIdx.x];
-  const int64_t* o = outs + (int64_t)tl.x * 16;
-  const int64_t c_off = o[0], m = o[1], n = o[2], ldc = o[3];
-  const int64_t a_sl = o[4], a_ex = o[5], b_sl = o[6], b_ex = o[7], Kp = o[9];
-  const int64_t ccs = o[10] > 0 ? o[10] : 1;  // output column stride (2: one part of complex data)
-  const int64_t row0 = (int64_t)tl.y * kTcM, col0 = (int64_t)tl.z * kTcN;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t sbase = smem_u32(smem);
-
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
-                 "r"(512));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  if (tid == 0) {
-    for (int i = 0; i < kTcStages; ++i) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[i])));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[i])));
-    }
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&accb)));
-    asm volatile("fence.mbarrier_init.release.cluster;");
-    failed = 0;
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;");
-  const uint32_t tmem = tmem_slot;
-
-  // digit planes in tile layout: per slice, (row tile, K step) blocks of 128 x 16 (A) / 64 x 16 (B)
-  const int64_t ksteps = Kp / kK;
-  const int64_t a_slice = (m + kTcM - 1) / kTcM * kTcM * Kp, b_slice = (n + kTcN - 1) / kTcN * kTcN * Kp;
-  const __nv_bfloat16* a_tiles = As + a_sl + (int64_t)tl.y * ksteps * (kTcM * kK);
-  const __nv_bfloat16* b_tiles = Bs + b_sl + (int64_t)tl.z * ksteps * (kTcN * kK);
-  // producer (thread 0): the S digit tiles of A and of B of one K step
-  auto issue = [&](int stage, int64_t step) {
-    const uint32_t fb = smem_u32(&full[stage]);
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(kStage) : "memory");
-    const uint32_t d0 = sbase + (uint32_t)stage * kStage;
-    for (int t = 0; t < S; ++t) {
-      bulk_load(d0 + t * kATile, a_tiles + t * a_slice + step * (kTcM * kK), kATile, fb);
-      bulk_load(d0 + S * kATile + t * kBTile, b_tiles + t * b_slice + step * (kTcN * kK), kBTile, fb);
-    }
-  };
-  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
-                         ((uint32_t)(kTcM >> 4) << 24);  // F32 accumulate, BF16 A/B, K-major, N=64, M=128
-  int64_t issued = 0, consumed = 0;  // steps loaded / steps whose MMAs were issued (thread 0)
-  if (tid == 0) {
-    for (; issued < kTcStages && issued < ksteps; ++issued) issue((int)issued, issued);
-  }
-  double acc64[kTcN];
-#pragma unroll
-  for (int j = 0; j < kTcN; ++j) acc64[j] = 0.0;
-  const int64_t nchunks = (ksteps + kChunkSteps - 1) / kChunkSteps;
-  for (int64_t ch = 0; ch < nchunks; ++ch) {
-    const int64_t s0 = ch * kChunkSteps, s1 = min(ksteps, s0 + kChunkSteps);
-    if (tid == 0) {
-      for (int64_t st = s0; st < s1 && !failed; ++st) {
-        const int stage = (int)(st % kTcStages);
-        if (!mbar_wait(smem_u32(&full[stage]), (uint32_t)((st / kTcStages) & 1))) { failed = 1; break; }
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t a0 = sbase + (uint32_t)stage * kStage, b0 = a0 + S * kATile;
-#pragma unroll
-        for (int ta = 0; ta < S; ++ta)
-#pragma unroll
-          for (int tb = 0; tb < S - ta; ++tb)
-            tc_mma(tmem + (uint32_t)((ta + tb) * kTcN), umma_desc(a0 + ta * kATile), umma_desc(b0 + tb * kBTile),
-                   idesc, (st == s0 && ta == 0) ? 0u : 1u);
-        tc_commit(smem_u32(&empty[stage]));
-        consumed = st + 1;
-        // refill the stage of step st-1 (its MMAs ran while those of step st were queued)
-        if (st >= 1 && issued < ksteps && issued == st - 1 + kTcStages) {
-          const int ps = (int)((st - 1) % kTcStages);
-          if (!mbar_wait(smem_u32(&empty[ps]), (uint32_t)(((st - 1) / kTcStages) & 1))) { failed = 1; break; }
-          issue(ps, issued);
-          ++issued;
-        }
-      }
-      // the accumulators of this chunk are complete once every MMA issued so far is
-      tc_commit(smem_u32(&accb));
-    }
-    if (!mbar_wait(smem_u32(&accb), (uint32_t)(ch & 1))) failed = 1;
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    {
-#pragma unroll
-      for (int cb = 0; cb < kTcN / 8; ++cb) {
-        long long hi[8], lo[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) hi[j] = lo[j] = 0;
-#pragma unroll
-        for (int d = 0; d < S; ++d) {
-          uint32_t v[8];
-          tc_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(d * kTcN + cb * 8), v);
-          asm volatile("tcgen05.wait::ld.sync.aligned;");
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const long long q = (long long)__float2int_rn(__uint_as_float(v[j]));
-            if (d < 4) hi[j] += q << (7 * (3 - d));
-            else lo[j] += q << (7 * (S - 1 - d));
-          }
-        }
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-          acc64[cb * 8 + j] += int_to_double_scaled(hi[j], -21) + int_to_double_scaled(lo[j], -7 * (S - 1));
-      }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();  // every lane has read the accumulators before the next chunk overwrites them
-    if (failed) break;
-  }
-  if (failed) {
-    // drain: the bulk copies expected but not consumed, and the MMAs (complete in issue order)
-    if (tid == 0) {
-      atomicExch(err, 1);
-      for (int64_t j = consumed; j < issued; ++j)
-        mbar_wait(smem_u32(&full[j % kTcStages]), (uint32_t)((j / kTcStages) & 1));
-      if (consumed > 0)
-        mbar_wait(smem_u32(&empty[(consumed - 1) % kTcStages]), (uint32_t)(((consumed - 1) / kTcStages) & 1));
-    }
-  } else {
-    if (tid == 0) {
-      // the last MMAs have completed (they read the stage buffers the epilogue reuses)
-      for (int64_t j = max((int64_t)0, ksteps - kTcStages); j < ksteps; ++j)
-        if (!mbar_wait(smem_u32(&empty[j % kTcStages]), (uint32_t)((j / kTcStages) & 1))) atomicExch(err, 1);
-    }
-    {
-      // epilogue through shared memory (the stages are free): row-major 128 x 64 doubles,
-      // padded rows; then coalesced stores with the row/column exponents applied
-      double* tileC = reinterpret_cast<double*>(smem);
-      const int r = warp * 32 + lane;
-#pragma unroll
-      for (int j = 0; j < kTcN; ++j) tileC[r * (kTcN + 1) + j] = acc64[j];
-      __syncthreads();
-      for (int e = tid; e < kTcM * kTcN; e += kTcThreads) {
-        const int rr = e / kTcN, cc = e % kTcN;
-        const int64_t gi = row0 + rr, gj = col0 + cc;
-        if (gi < m && gj < n)
-          C[c_off + gi * ldc + gj * ccs] =
-              scale_pow2(tileC[rr * (kTcN + 1) + cc], Ae[a_ex + gi] + Be[b_ex + gj] - 14);
-      }
-    }
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;");
-  __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
-}
-
-template <int S>
-int launch_gemm_tc(const void* As, const int* Ae, const void* Bs, const int* Be, double* C, const int64_t* outs,
-                   const int32_t* tiles, int n_tiles, int* err, cudaStream_t s) {
-  const size_t smem = (size_t)kTcStages * S * (kTcM + kTcN) * kK * 2;
-  static_assert((size_t)kTcM * (kTcN + 1) * 8 <= (size_t)kTcStages * 6 * (kTcM + kTcN) * kK * 2,
-                "epilogue tile must fit in the stage buffers");
-  auto kern = ozaki_gemm_tc_kernel<S>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
-  kern<<<n_tiles, kTcThreads, smem, s>>>((const __nv_bfloat16*)As, Ae, (const __nv_bfloat16*)Bs, Be, C, outs, tiles,
-                                         err);
-  return check_launch();
-}
-
 }  // namespace
 }  // namespace yb
 
@@ -623,18 +312,6 @@ int yb_ozaki_split(const double* src, void* slices, int* exps, const int64_t* re
   return yb::check_launch();
 }
 
-int yb_ozaki_split_tiled(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs, int max_rows,
-                         int slices_count, int tile_rows, void* stream) {
-  if (n_recs == 0 || max_rows == 0) return YB_OK;
-  if (!src || !slices || !exps || !recs || slices_count < 1 || slices_count > 8) return YB_ERR_INVALID;
-  if (tile_rows != 64 && tile_rows != 128) return YB_ERR_INVALID;
-  const int rows_p = (max_rows + tile_rows - 1) / tile_rows * tile_rows;
-  dim3 grid((unsigned)((rows_p + 7) / 8), (unsigned)n_recs);
-  yb::split_rows_tiled_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(src, (__nv_bfloat16*)slices, exps, recs,
-                                                                       slices_count, tile_rows);
-  return yb::check_launch();
-}
-
 int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps, double* c,
                   const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count, void* stream) {
   if (n_tiles == 0) return YB_OK;
@@ -646,39 +323,6 @@ int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices,
     case 8: return yb::launch_gemm<8>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, s);
     default: return YB_ERR_INVALID;
   }
-}
-
-// Status word of the tcgen05 kernel (1 after a CTA gave up on a bounded wait).
-static __device__ int g_ozaki_tc_error;
-
-int yb_ozaki_gemm_tc(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps, double* c,
-                     const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count, void* stream) {
-  if (n_tiles == 0) return YB_OK;
-  if (!a_slices || !a_exps || !b_slices || !b_exps || !c || !outs || !tiles) return YB_ERR_INVALID;
-  cudaStream_t s = (cudaStream_t)stream;
-  int* err = nullptr;
-  cudaError_t e = cudaGetSymbolAddress((void**)&err, g_ozaki_tc_error);
-  if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
-  switch (slices_count) {
-    case 8: return yb::launch_gemm_tc<8>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
-    case 7: return yb::launch_gemm_tc<7>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
-    case 6: return yb::launch_gemm_tc<6>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
-    default: return YB_ERR_INVALID;
-  }
-}
-
-int yb_ozaki_device_error(int* out, int reset, void* stream) {
-  if (!out) return YB_ERR_INVALID;
-  cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = cudaMemcpyFromSymbolAsync(out, g_ozaki_tc_error, sizeof(int), 0, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e == cudaSuccess && reset) {
-    const int zero = 0;
-    e = cudaMemcpyToSymbolAsync(g_ozaki_tc_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  }
-  if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
-  return YB_OK;
 }
 
 }  // extern "C"
@@ -725,15 +369,18 @@ inline int64_t align256(int64_t x) { return (x + 255) & ~(int64_t)255; }
 }  // namespace
 }  // namespace yb
 
-extern "C" int yb_ozaki_dot_static(const double* A, const double* B, double* C, const int64_t* a_recs, int n_a,
-                                   int a_rows, const int64_t* b_recs, int n_b, int b_rows, const int64_t* bT_tasks,
-                                   int n_bT_tasks, const int64_t* bT_items, int n_bT_items, const int64_t* outs,
-                                   const int32_t* tiles, int n_tiles, int slices_count, int64_t a_slice_elems,
-                                   int64_t b_slice_elems, int64_t a_exp_count, int64_t b_exp_count, int64_t bT_elems,
-                                   void* stream) {
-  if (n_tiles == 0) return YB_OK;
-  if (!A || !B || !C || !a_recs || !b_recs || !outs || !tiles || n_a < 0 || n_b < 0 || n_tiles < 0)
-    return YB_ERR_INVALID;
+extern "C" int yb_ozaki_dot_static(const double* A, const double* B, double* C, int dtype, const int64_t* a_recs,
+                                   int n_a, int a_rows, const int64_t* b_recs, int n_b, int b_rows,
+                                   const int64_t* bT_tasks, int n_bT_tasks, const int64_t* bT_items, int n_bT_items,
+                                   const int64_t* outs, const int32_t* tiles, int n_tiles, const int64_t* nat_outs,
+                                   const int64_t* nat_terms, const int32_t* nat_tiles, int n_nat_tiles,
+                                   int slices_count, int64_t a_slice_elems, int64_t b_slice_elems, int64_t a_exp_count,
+                                   int64_t b_exp_count, int64_t bT_elems, void* stream) {
+  if (dtype != YB_F64) return YB_ERR_INVALID;  // the B transposes are sized for 8-byte elements
+  if (n_tiles == 0 && n_nat_tiles == 0) return YB_OK;
+  if (!A || !B || !C || n_a < 0 || n_b < 0 || n_tiles < 0 || n_nat_tiles < 0) return YB_ERR_INVALID;
+  if (n_tiles > 0 && (!a_recs || !b_recs || !outs || !tiles)) return YB_ERR_INVALID;
+  if (n_nat_tiles > 0 && (!nat_outs || !nat_terms || !nat_tiles)) return YB_ERR_INVALID;
   if (a_slice_elems < 0 || b_slice_elems < 0 || a_exp_count < 0 || b_exp_count < 0 || bT_elems < 0)
     return YB_ERR_INVALID;
   const int64_t off_a = 0;
@@ -743,8 +390,11 @@ extern "C" int yb_ozaki_dot_static(const double* A, const double* B, double* C, 
   const int64_t off_eb = yb::align256(off_ea + 4 * a_exp_count);
   const int64_t total = yb::align256(off_eb + 4 * b_exp_count);
   if (total > (int64_t)YB_STATIC_SCRATCH_BYTES) return YB_ERR_TOO_LARGE;
+  // sectors with K < 16 or skinny outputs: the native FP64 kernel, which needs no scratch
+  int st = yb_grouped_gemm(A, B, C, YB_F64, nat_outs, nat_terms, nat_tiles, n_nat_tiles, 1.0, 0.0, stream);
+  if (st != YB_OK || n_tiles == 0) return st;
   unsigned char* base = nullptr;
-  int st = yb::static_scratch(&base);
+  st = yb::static_scratch(&base);
   if (st != YB_OK) return st;
   double* bT = reinterpret_cast<double*>(base + off_t);
   int* ea = reinterpret_cast<int*>(base + off_ea);

@@ -153,7 +153,7 @@ def dot(A, B, meta_dot, Dsize):
 OZAKI_SLICES = 8  # 57 bits per operand: FP64-grade products
 
 
-OZAKI_TC = [None]  # emulated GEMM kernel: None = autotuned per dot, True = tcgen05/TMEM, False = mma.sync
+OZAKI_TC = [None]  # emulated GEMM kernel: None = autotuned per dot, True = tcgen05 (split fused in), False = mma.sync
 OZAKI_AUTOTUNE = [True]  # False: choose by the tile-padding estimate without timing
 
 
@@ -202,31 +202,26 @@ def _autotune_ozaki(plan, A, B, out, slices):
 
 def _ozaki_run(plan, A, B, out, slices, tc):
     dev = A.device
+    st = _stream()
     if tc:
-        dar, dbr, dout, dtl = _dev(plan, 'ozaki_tc', (plan.a_recs_tc, plan.b_recs_tc, plan.outs_tc, plan.tiles_tc),
-                                   dev)
-    else:
-        dar, dbr, dout, dtl = _dev(plan, 'ozaki', (plan.a_recs, plan.b_recs, plan.outs, plan.tiles), dev)
-    a_sl = torch.empty(plan.a_size_tc if tc else plan.a_size, dtype=torch.bfloat16, device=dev)
-    b_sl = torch.empty(plan.b_size_tc if tc else plan.b_size, dtype=torch.bfloat16, device=dev)
+        # tcgen05 kernel with the split fused in: exponents, then one GEMM launch reading A and B
+        dea, deb, dout, dtl = _dev(plan, 'ozaki_fused', (plan.exp_a, plan.exp_b, plan.outs_f, plan.tiles_f), dev)
+        ex = torch.empty(max(plan.n_exps, 1), dtype=torch.int32, device=dev)
+        N.call('yb_ozaki_exponents', _ptr(A), _ptr(ex), _ptr(dea), len(plan.exp_a), plan.exp_a_max, 0, st)
+        N.call('yb_ozaki_exponents', _ptr(B), _ptr(ex), _ptr(deb), len(plan.exp_b), plan.exp_b_max, 1, st)
+        N.call('yb_ozaki_gemm_fused', _ptr(A), _ptr(B), _ptr(ex), _ptr(out), _ptr(dout), _ptr(dtl),
+               len(plan.tiles_f), slices, st)
+        return
+    dar, dbr, dout, dtl = _dev(plan, 'ozaki', (plan.a_recs, plan.b_recs, plan.outs, plan.tiles), dev)
+    a_sl = torch.empty(plan.a_size, dtype=torch.bfloat16, device=dev)
+    b_sl = torch.empty(plan.b_size, dtype=torch.bfloat16, device=dev)
     a_ex = torch.empty(max(plan.a_exps, 1), dtype=torch.int32, device=dev)
     b_ex = torch.empty(max(plan.b_exps, 1), dtype=torch.int32, device=dev)
     bT = run_copy(plan.bT, B, torch.empty(max(plan.bT_size, 1), dtype=B.dtype, device=dev))
-    st = _stream()
-    if tc:
-        N.call('yb_ozaki_split_tiled', _ptr(A), _ptr(a_sl), _ptr(a_ex), _ptr(dar), len(plan.a_recs), plan.a_rows,
-               slices, P.OZAKI_TC_M, st)
-        N.call('yb_ozaki_split_tiled', _ptr(bT), _ptr(b_sl), _ptr(b_ex), _ptr(dbr), len(plan.b_recs), plan.b_rows,
-               slices, P.OZAKI_TC_N, st)
-        N.call('yb_ozaki_gemm_tc', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
-               len(plan.tiles_tc), slices, st)
-    else:
-        N.call('yb_ozaki_split', _ptr(A), _ptr(a_sl), _ptr(a_ex), _ptr(dar), len(plan.a_recs), plan.a_rows, slices,
-               st)
-        N.call('yb_ozaki_split', _ptr(bT), _ptr(b_sl), _ptr(b_ex), _ptr(dbr), len(plan.b_recs), plan.b_rows, slices,
-               st)
-        N.call('yb_ozaki_gemm', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
-               len(plan.tiles), slices, st)
+    N.call('yb_ozaki_split', _ptr(A), _ptr(a_sl), _ptr(a_ex), _ptr(dar), len(plan.a_recs), plan.a_rows, slices, st)
+    N.call('yb_ozaki_split', _ptr(bT), _ptr(b_sl), _ptr(b_ex), _ptr(dbr), len(plan.b_recs), plan.b_rows, slices, st)
+    N.call('yb_ozaki_gemm', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
+           len(plan.tiles), slices, st)
 
 
 def ozaki_device_error(reset=True):
@@ -453,10 +448,12 @@ def qr(data, meta, sizes):
 
 
 def qr_backward(Q, R, gQ, gR, data, meta):
-    """Adjoint of ``qr`` for float64 blocks (the reduced-QR rule that torch's autograd
-    applies to the reference's torch.linalg.qr + sign fix, backend_torch.py:475-484):
-    dA = (gQ' + Q copyltu(M)) U^{-T}, M = U gU^T - gQ'^T Q, with U = R[:, :k], gU = gR[:, :k],
-    gQ' = gQ + A[:, m:] gR[:, m:]^T and dA[:, m:] = Q gR[:, m:] for wide blocks."""
+    """Adjoint of ``qr`` for float64 and complex128 blocks (the reduced-QR rule that torch's
+    autograd applies to the reference's torch.linalg.qr + sign fix, backend_torch.py:475-484):
+    dA = (gQ' + Q copyltu(M)) U^{-H}, M = U gU^H - gQ'^H Q, with U = R[:, :k], gU = gR[:, :k],
+    gQ' = gQ + A[:, m:] gR[:, m:]^H and dA[:, m:] = Q gR[:, m:] for wide blocks;
+    copyltu(M) = tril(M, -1) + tril(M, -1)^H + Re diag(M) (gradients in torch's convention
+    for complex tensors)."""
     plan = P.qr_plan(meta, Q.is_complex())
     dev = Q.device
     dA = torch.zeros(data.numel(), dtype=data.dtype, device=dev)
@@ -564,25 +561,20 @@ def fix_svd_signs(U, V, meta):
     return Uo, Vo, phases
 
 
-def fix_svd_signs_backward(gU, gV, phases, meta):
-    """Adjoint of the real gauge fix: cotangents multiplied by the same +-1 phases."""
+def fix_svd_signs_backward(U, V, gU, gV, meta):
+    """Adjoint of the gauge fix (real and complex; yb_fix_signs_adjoint) given the forward's
+    inputs U, V and the cotangents of its outputs."""
     plan = P.svd_plan(meta, ROWS_PER_SUPER[0])
     nb = len(plan.blocks)
-    gU = torch.zeros(0) if gU is None else gU
-    gV = torch.zeros(0) if gV is None else gV
-    outs = []
-    for g, is_u in ((gU, True), (gV, False)):
-        outs.append(None if g.numel() == 0 else g.contiguous().clone())
-    if nb == 0:
-        return outs[0], outs[1]
-    (dblocks,) = _dev(plan, 'svd_blocks', (plan.blocks,), phases.device)
-    Ui = outs[0] if outs[0] is not None else torch.zeros(int(max((r[3] + r[1] * r[9]) for r in plan.blocks)),
-                                                           dtype=phases.dtype, device=phases.device)
-    Vi = outs[1] if outs[1] is not None else torch.zeros(int(max((r[5] + r[9] * r[2]) for r in plan.blocks)),
-                                                           dtype=phases.dtype, device=phases.device)
-    N.call('yb_fix_signs', _ptr(Ui), _ptr(Vi), _ptr(Ui), _ptr(Vi), _ptr(phases), _ptr(dblocks), nb, plan.max_k,
-           _dtype_code(Ui.dtype), 1, _stream())
-    return (Ui if outs[0] is not None else None), (Vi if outs[1] is not None else None)
+    need_u, need_v = gU is not None, gV is not None
+    gU = torch.zeros_like(U) if gU is None else gU.contiguous().to(U.dtype)
+    gV = torch.zeros_like(V) if gV is None else gV.contiguous().to(V.dtype)
+    dU, dV = torch.zeros_like(U), torch.zeros_like(V)  # the kernel writes every position of the records
+    if nb:
+        (dblocks,) = _dev(plan, 'svd_blocks', (plan.blocks,), U.device)
+        N.call('yb_fix_signs_adjoint', _ptr(U), _ptr(V), _ptr(gU), _ptr(gV), _ptr(dU), _ptr(dV), _ptr(dblocks), nb,
+               plan.max_k, _dtype_code(U.dtype), _stream())
+    return (dU if need_u else None), (dV if need_v else None)
 
 
 # ----------------------------------------------------------------------------- masks / truncation

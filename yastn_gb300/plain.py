@@ -5,8 +5,8 @@ This is the comparison path of the measurements: the same backend interface as
 yastn/backend/backend_torch.py), but every hot function loops over the blocks on the host
 and issues one torch launch per block — a permute-copy per merged piece
 (backend_torch.py:518-531), one ``matmul`` per sector GEMM (backend_torch.py:466-473),
-one ``torch.linalg.svd`` per block (cuSOLVER on the GPU, LAPACK on the host;
-backend_torch.py:318-319), one ``torch.linalg.qr`` per block with the sign fix
+one ``torch.linalg.svd`` per block (cuSOLVER's gesvd on the GPU, as the reference forces
+in yastn/backend/linalg/torch_svd_gesdd.py:16-17; LAPACK on the host; backend_torch.py:318-319), one ``torch.linalg.qr`` per block with the sign fix
 (backend_torch.py:475-484) — and autograd differentiates the torch operations themselves
 (the SVD through the reference's broadened adjoint, evaluated per block).
 Everything that is not on the hot path is taken from ``yastn_gb300.backend`` unchanged.
@@ -63,7 +63,10 @@ class _PlainSvd(torch.autograd.Function):
         S = torch.empty(sizes[1], dtype=real, device=data.device)
         V = torch.empty(sizes[2], dtype=data.dtype, device=data.device)
         for sl, D, slU, DU, slS, slV, DV in meta:
-            u, s, vh = torch.linalg.svd(data[_sl(sl)].view(D), full_matrices=False)
+            blk = data[_sl(sl)].view(D)
+            # the reference forces cuSOLVER's gesvd on CUDA (yastn/backend/linalg/torch_svd_gesdd.py:16-17)
+            u, s, vh = (torch.linalg.svd(blk, full_matrices=False, driver='gesvd') if blk.is_cuda
+                        else torch.linalg.svd(blk, full_matrices=False))
             U[_sl(slU)].view(DU)[...] = u
             S[_sl(slS)] = s
             V[_sl(slV)].view(DV)[...] = vh
