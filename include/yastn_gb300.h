@@ -115,6 +115,13 @@ int yb_block_copy(const void* src, void* dst, int unit_bytes,
 int yb_grouped_gemm(const void* a, const void* b, void* c, int dtype,
                     const int64_t* outs, const int64_t* terms, const int32_t* tiles, int n_tiles,
                     double alpha, double beta, void* stream);
+/* yb_grouped_gemm_skinny: the same products for skinny tiles only (tile kind 1; other tiles
+ * are skipped), in a kernel of its own so that the 64 x 64 tiles keep their register budget;
+ * single-term outputs with at most 4 rows and K <= 8 (the contractions with a small MPO
+ * block) load their whole column strip before the FMAs. */
+int yb_grouped_gemm_skinny(const void* a, const void* b, void* c, int dtype,
+                           const int64_t* outs, const int64_t* terms, const int32_t* tiles, int n_tiles,
+                           double alpha, double beta, void* stream);
 /* yb_gemm_reduce: the second pass of a split-K product. The host splits the K range of
  * outputs whose few tiles would leave most SMs idle into chunks, computes each chunk's
  * product into its own slot of a workspace P (yb_grouped_gemm with alpha 1, beta 0), then
@@ -212,6 +219,26 @@ int yb_ozaki_dot_static(const double* A, const double* B, double* C, int dtype,
                         int n_nat_tiles, int slices_count,
                         int64_t a_slice_elems, int64_t b_slice_elems, int64_t a_exp_count,
                         int64_t b_exp_count, int64_t bT_elems, void* stream);
+
+/* ==== device-resident Lanczos (yastn/tensor/_krylov.py:17-46, yastn/krylov/_krylov.py:177-238;
+ * the backend's vdot / add / norm, backend_np.py:553-577) ======================================
+ * Vector operations of a Krylov expansion whose coefficients stay on the device (no host
+ * synchronisation per step; capturable in a CUDA graph). YB_F64 or YB_C128 vectors of n
+ * elements; parts: a workspace of yb_krylov_parts() values of the vector type (FP64 for the
+ * norms); reductions are deterministic (fixed grid, partial sums added in order).
+ *   yb_krylov_dot:     *out = sum_i conj(x_i) y_i
+ *   yb_krylov_update:  w <- w - (*alpha) v1 - (*beta) v0 (v0 may be NULL), *norm_out = |w|
+ *   yb_krylov_norm:    *out = |x|
+ *   yb_krylov_scale:   out <- w / (*beta)
+ *   yb_krylov_combine: y <- sum_{r < m} coeffs_r V[r] (V row-major, row stride ldv) */
+int yb_krylov_parts(void);
+int yb_krylov_dot(const void* x, const void* y, int64_t n, int dtype, void* parts, void* out, void* stream);
+int yb_krylov_update(void* w, const void* v1, const void* v0, const void* alpha, const double* beta, int64_t n,
+                     int dtype, double* parts, double* norm_out, void* stream);
+int yb_krylov_norm(const void* x, int64_t n, int dtype, double* parts, double* out, void* stream);
+int yb_krylov_scale(const void* w, const double* beta, int64_t n, int dtype, void* out, void* stream);
+int yb_krylov_combine(const void* V, int64_t ldv, const void* coeffs, int m, int64_t n, int dtype, void* y,
+                      void* stream);
 
 /* ==== family (c): batched one-sided Jacobi SVD / symmetric eigendecomposition ==========
  * blocks: n_blocks records of YB_SVD_REC int64:

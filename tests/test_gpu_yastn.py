@@ -211,11 +211,53 @@ def test_dmrg_heff2_inside_yastn_eigs(cuda_device):
             gb.set_gemm_mode(mode)
             out = heff2(AAg)
             assert out.struct == AAg.struct
-            val, _ = yastn.eigs(heff2, AAg, k=1, ncv=30, which='SR', hermitian=True)
-            got = float(val[0].real) if hasattr(val[0], 'real') else float(val[0])
-            assert abs(got - rec['lanczos_lowest']) <= 1e-10 * abs(rec['lanczos_lowest']), (mode, got)
+            Ys = []
+            for solver in (yastn.eigs, yastn_gb300.eigs):  # YASTN's loop, then the device-resident one
+                val, Y = solver(heff2, AAg, k=1, ncv=30, which='SR', hermitian=True)
+                got = float(val[0].real)
+                assert abs(got - rec['lanczos_lowest']) <= 1e-10 * abs(rec['lanczos_lowest']), (mode, solver, got)
+                assert Y[0].struct == AAg.struct
+                Ys.append(Y[0])
+            # the same Ritz vector (Lanczos without reorthogonalisation: neither has unit norm)
+            ov = abs(float(yastn.vdot(Ys[0], Ys[1]).real)) / float(Ys[0].norm() * Ys[1].norm())
+            assert ov >= 1 - 1e-8, ov
     finally:
         gb.set_gemm_mode(saved)
+
+
+def test_dmrg_with_device_eigs(cuda_device):
+    """yastn.tn.mps.dmrg_ (two-site, XXZ chain of 8 sites, D=16) on this backend with its
+    eigensolver rebound to the device-resident Lanczos: the energy agrees with the NumPy
+    backend's run from the same initial state within 1e-10."""
+    import yastn.tn.mps as mps
+    import yastn.tn.mps._dmrg as dmrg_mod
+    N = 8
+    H_latex = r"\sum_{i,j \in NN} (Jz sz_{i} sz_{j} + 0.5 Jxy (sp_{i} sm_{j} + sm_{i} sp_{j}))"
+    params = {"Jz": 1.0, "Jxy": 1.0, "NN": [(i, i + 1) for i in range(N - 1)]}
+    energies = {}
+    for name in ('np', 'gb'):
+        ops_ = yastn.operators.Spin12(sym='U1', backend='np')
+        gen = mps.Generator(N=N, operators=ops_)
+        gen.random_seed(seed=1)
+        H = gen.mpo_from_latex(H_latex, params)
+        psi = gen.random_mps(D_total=16, n=0)
+        if name == 'gb':
+            cg = _cfg('U1')
+            H = H.shallow_copy()
+            psi = psi.shallow_copy()
+            for k in range(N):
+                H[k] = _to_gpu(H[k], cg)
+                psi[k] = _to_gpu(psi[k], cg)
+        saved = dmrg_mod.eigs
+        if name == 'gb':
+            dmrg_mod.eigs = yastn_gb300.eigs
+        try:
+            out = mps.dmrg_(psi, H, method='2site', max_sweeps=4, opts_svd={'D_total': 16},
+                            opts_eigs={'hermitian': True, 'ncv': 5, 'which': 'SR'})
+        finally:
+            dmrg_mod.eigs = saved
+        energies[name] = float(mps.measure_mpo(psi, H, psi).real)
+    assert abs(energies['gb'] - energies['np']) <= 1e-10 * abs(energies['np'])
 
 
 @pytest.mark.parametrize('name', ['ctmrg_z2_d6', 'ctmrg_z2_d6_qr'])

@@ -7,9 +7,11 @@
 (merge/unmerge, sector GEMMs, block SVD/eigh, masks, their adjoints) runs on
 hand-written CUDA kernels in ``libyastn_gb300.so``; build it with
 ``python yastn_gb300/build.py``. ``truncation_mask`` is a one-launch replacement for
-``yastn.linalg.truncation_mask`` usable as ``mask_f``.
+``yastn.linalg.truncation_mask`` usable as ``mask_f``; ``eigs`` is ``yastn.eigs`` with the
+hermitian Krylov expansion kept on the device (``yastn_gb300.krylov``).
 """
 from . import backend_gb300 as backend
+from .krylov import eigs
 from .truncation import truncation_mask
 
-__all__ = ['backend', 'truncation_mask']
+__all__ = ['backend', 'eigs', 'truncation_mask']

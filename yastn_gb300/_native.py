@@ -22,6 +22,7 @@ SIGNATURES = {
     'yb_block_copy': ([_vp, _vp, _i, _vp, _i, _vp, _i, _vp], _i),
     'yb_gemm_reduce': ([_vp, _vp, _i, _vp, _vp, _i, _d, _d, _vp], _i),
     'yb_grouped_gemm': ([_vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _d, _d, _vp], _i),
+    'yb_grouped_gemm_skinny': ([_vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _d, _d, _vp], _i),
     'yb_svd_init': ([_vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp], _i),
     'yb_svd_qr': ([_vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _i, _vp], _i),
     'yb_qr': ([_vp, _vp, _vp, _vp, _vp, _i, _i, _vp, _i, _vp], _i),
@@ -45,6 +46,12 @@ SIGNATURES = {
     'yb_ozaki_device_error': ([_vp, _i, _vp], _i),
     'yb_ozaki_dot_static': ([_vp, _vp, _vp, _i, _vp, _i, _i, _vp, _i, _i, _vp, _i, _vp, _i, _vp, _vp, _i,
                              _vp, _vp, _vp, _i, _i, _i64, _i64, _i64, _i64, _i64, _vp], _i),
+    'yb_krylov_parts': ([], _i),
+    'yb_krylov_dot': ([_vp, _vp, _i64, _i, _vp, _vp, _vp], _i),
+    'yb_krylov_update': ([_vp, _vp, _vp, _vp, _vp, _i64, _i, _vp, _vp, _vp], _i),
+    'yb_krylov_norm': ([_vp, _i64, _i, _vp, _vp, _vp], _i),
+    'yb_krylov_scale': ([_vp, _vp, _i64, _i, _vp, _vp], _i),
+    'yb_krylov_combine': ([_vp, _i64, _vp, _i, _i64, _i, _vp, _vp], _i),
     'yb_truncation_mask': ([_vp, _i64, _vp, _vp, _i, _d, _i64, _i, _vp, _vp, _vp], _i),
 }
 

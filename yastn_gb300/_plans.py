@@ -299,7 +299,12 @@ class GemmPlan:
     def __init__(self, outs, terms, tiles, flops, split=None):
         self.outs = outs
         self.terms = terms
-        self.tiles = tiles
+        self.tiles = tiles  # all tiles (yb_grouped_gemm takes both kinds)
+        # the launches of the backend: 64 x 64 tiles (yb_grouped_gemm) and skinny tiles
+        # (yb_grouped_gemm_skinny) apart
+        sk = tiles[:, 3] == 1 if len(tiles) else np.zeros(0, dtype=bool)
+        self.tiles_main = np.ascontiguousarray(tiles[~sk]) if len(tiles) else tiles
+        self.tiles_skinny = np.ascontiguousarray(tiles[sk]) if len(tiles) else tiles
         self.flops = flops  # real multiply-adds x 2 (complex counted by the caller)
         self.split = split
         self._dev = {}

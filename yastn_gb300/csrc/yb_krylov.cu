@@ -9,8 +9,9 @@
 // a fixed shared-memory tree), and one warp adds the partials in order.
 //
 //   yb_krylov_dot:    s = sum_i conj(x_i) y_i                      (alpha_j = <V_j, w>)
-//   yb_krylov_update: w <- w - alpha V_j - beta V_{j-1}, s = |w|^2  (one pass over w)
-//   yb_krylov_scale:  v <- w / sqrt(s)                             (V_{j+1} = w / beta_j)
+//   yb_krylov_update: w <- w - alpha V_j - beta V_{j-1}, s = |w|    (one pass over w)
+//   yb_krylov_norm:   s = |x|                                       (|v0|)
+//   yb_krylov_scale:  v <- w / beta                                (V_{j+1} = w / beta_j)
 //   yb_krylov_combine: y = sum_i c_i V_i                           (Ritz vectors)
 #include "yb_common.cuh"
 
@@ -111,6 +112,15 @@ __global__ void finish_norm_kernel(const double* __restrict__ parts, double* __r
 }
 
 template <class F>
+__global__ void __launch_bounds__(kThr) norm_parts_kernel(const typename F::T* __restrict__ x, int64_t n,
+                                                          double* __restrict__ parts) {
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * kThr + threadIdx.x; i < n; i += (int64_t)kParts * kThr) acc += F::norm2(x[i]);
+  const double s = block_sum<R64>(acc);
+  if (threadIdx.x == 0) parts[blockIdx.x] = s;
+}
+
+template <class F>
 __global__ void __launch_bounds__(kThr) scale_kernel(const typename F::T* __restrict__ w, const double* __restrict__ beta,
                                                      int64_t n, typename F::T* __restrict__ out) {
   const double inv = 1.0 / *beta;
@@ -172,6 +182,19 @@ int yb_krylov_update(void* w, const void* v1, const void* v0, const void* alpha,
   else
     return YB_ERR_INVALID;
   yb::finish_norm_kernel<<<1, 32, 0, s>>>(parts, norm_out, yb::kParts);
+  return yb::check_launch();
+}
+
+int yb_krylov_norm(const void* x, int64_t n, int dtype, double* parts, double* out, void* stream) {
+  if (!x || !parts || !out || n < 0) return YB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == YB_F64)
+    yb::norm_parts_kernel<yb::R64><<<yb::kParts, yb::kThr, 0, s>>>((const double*)x, n, parts);
+  else if (dtype == YB_C128)
+    yb::norm_parts_kernel<yb::C128><<<yb::kParts, yb::kThr, 0, s>>>((const double2*)x, n, parts);
+  else
+    return YB_ERR_INVALID;
+  yb::finish_norm_kernel<<<1, 32, 0, s>>>(parts, out, yb::kParts);
   return yb::check_launch();
 }
 

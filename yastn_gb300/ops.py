@@ -122,9 +122,13 @@ def transpose_backward(data_b, axes, meta_transpose):
 def run_gemm(plan, a, b, c, alpha=1.0, beta=0.0):
     code = _dtype_code(c.dtype)
     if len(plan.tiles):
-        do, dtm, dti = _dev(plan, 'gemm', (plan.outs, plan.terms, plan.tiles), a.device)
-        N.call('yb_grouped_gemm', _ptr(a), _ptr(b), _ptr(c), code, _ptr(do), _ptr(dtm), _ptr(dti),
-               len(plan.tiles), float(alpha), float(beta), _stream())
+        do, dtm, dti, dsk = _dev(plan, 'gemm', (plan.outs, plan.terms, plan.tiles_main, plan.tiles_skinny), a.device)
+        if len(plan.tiles_main):
+            N.call('yb_grouped_gemm', _ptr(a), _ptr(b), _ptr(c), code, _ptr(do), _ptr(dtm), _ptr(dti),
+                   len(plan.tiles_main), float(alpha), float(beta), _stream())
+        if len(plan.tiles_skinny):
+            N.call('yb_grouped_gemm_skinny', _ptr(a), _ptr(b), _ptr(c), code, _ptr(do), _ptr(dtm), _ptr(dsk),
+                   len(plan.tiles_skinny), float(alpha), float(beta), _stream())
     sp = plan.split
     if sp is not None:
         # split-K: chunk products into a workspace, then the ordered sum into C
