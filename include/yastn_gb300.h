@@ -155,6 +155,14 @@ int yb_gemm_reduce(void* c, const void* p, int dtype, const int64_t* recs, const
  */
 int yb_ozaki_split(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs,
                    int max_rows, int slices_count, void* stream);
+/* yb_ozaki_split_cols: the split of B's columns read in place from row-major K x n blocks
+ * (no transposed copy): recs (8 int64) [0] B block offset (elements) [1] K [2] n [3] ldb
+ * [4] mode (0 real; 2, 3: the complex modes of yb_ozaki_split applied to column j, i.e. the
+ * rows [re | -im] and [im | re] of B^T) [5] destination offset (BF16 elements) [6] exponent
+ * offset [7] Kp. Writes the same digits and exponents as yb_ozaki_split on B^T's rows, in
+ * [slice][column][Kp]; max_cols: largest n. */
+int yb_ozaki_split_cols(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs,
+                        int max_cols, int slices_count, void* stream);
 int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps,
                   double* c, const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
                   void* stream);

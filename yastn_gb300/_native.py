@@ -40,6 +40,7 @@ SIGNATURES = {
     'yb_fix_signs': ([_vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp], _i),
     'yb_fix_signs_adjoint': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp], _i),
     'yb_ozaki_split': ([_vp, _vp, _vp, _vp, _i, _i, _i, _vp], _i),
+    'yb_ozaki_split_cols': ([_vp, _vp, _vp, _vp, _i, _i, _i, _vp], _i),
     'yb_ozaki_exponents': ([_vp, _vp, _vp, _i, _i, _i, _vp], _i),
     'yb_ozaki_gemm': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
     'yb_ozaki_gemm_fused': ([_vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),

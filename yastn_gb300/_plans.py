@@ -558,7 +558,7 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
     parts of the complex result (column stride 2 in FP64 units).
     """
     def build():
-        a_map, b_map, a_recs, b_recs, bT_tasks = {}, {}, [], [], []
+        a_map, b_map, a_recs, b_recs, bT_tasks, b_cols = {}, {}, [], [], [], []
         a_size = b_size = a_ex = b_ex = bT_size = 0
         outs, flops, small = [], 0, []
         f = 2 if cplx else 1  # FP64 words per element
@@ -581,6 +581,7 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
                 parts = []
                 for mode in ((2, 3) if cplx else (0,)):
                     b_recs.append((bT_size, n, Kr, K, mode, b_size, b_ex, Kp))
+                    b_cols.append((slb[0], K, n, n, mode, b_size, b_ex, Kp))  # B read in place
                     parts.append((b_size, b_ex))
                     b_size += s * n * Kp
                     b_ex += n
@@ -611,6 +612,9 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
         plan.bT_size = bT_size
         plan.native = _pack_gemm(small)
         plan.native_direct = _pack_gemm(small, allow_split=False)  # no chunk workspace
+        # column split of B in place (yb_ozaki_split_cols): the same digit planes, no B^T copy
+        plan.b_cols = np.array(b_cols, dtype=np.int64).reshape(-1, 8)
+        plan.b_cols_max = int(plan.b_cols[:, 2].max()) if len(b_cols) else 0
         _fused_records(plan, meta_dot, cplx)
         # padded MMA work of the two tilings: the tcgen05 kernel (128 x 64 tiles) when its
         # padding costs little more than the 64 x 64 tiles of the mma.sync kernel

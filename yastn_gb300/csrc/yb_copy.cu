@@ -23,10 +23,22 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kIlp = 4;
 
-template <typename Unit>
+// Kind-0 tasks with ND <= 4 dims: the task's extents, strides and division constants are read
+// into registers once per item; every unit then costs ND - 1 fast divisions (the outermost
+// coordinate is what remains) and two index updates per dim.
+template <typename Unit, int ND>
 __device__ __forceinline__ void copy_units(const Unit* __restrict__ src, Unit* __restrict__ dst, const int64_t* rec,
                                            int64_t first) {
-  const int ndim = (int)rec[YB_CP_NDIM];
+  uint32_t size[ND], magic[ND], shift[ND];
+  int64_t sstr[ND], dstr[ND];
+#pragma unroll
+  for (int d = 0; d < ND; ++d) {
+    size[d] = (uint32_t)rec[YB_CP_SIZE + d];
+    magic[d] = (uint32_t)rec[YB_CP_MAGIC + d];
+    shift[d] = (uint32_t)rec[YB_CP_SHIFT + d];
+    sstr[d] = rec[YB_CP_SSTR + d];
+    dstr[d] = rec[YB_CP_DSTR + d];
+  }
   const int64_t count = rec[YB_CP_COUNT];
   const int64_t n = min((int64_t)YB_COPY_ITEM_UNITS, count - first);
   const int64_t sbase = rec[YB_CP_SRC];
@@ -42,16 +54,15 @@ __device__ __forceinline__ void copy_units(const Unit* __restrict__ src, Unit* _
         uint32_t idx = (uint32_t)(first + e);
         int64_t so = sbase, dof = dbase;
 #pragma unroll
-        for (int d = YB_CP_MAXD - 1; d >= 0; --d) {
-          if (d < ndim) {
-            const uint32_t size = (uint32_t)rec[YB_CP_SIZE + d];
-            const uint32_t q = fast_div(idx, (uint32_t)rec[YB_CP_MAGIC + d], (uint32_t)rec[YB_CP_SHIFT + d]);
-            const int64_t r = (int64_t)(idx - q * size);
-            so += r * rec[YB_CP_SSTR + d];
-            dof += r * rec[YB_CP_DSTR + d];
-            idx = q;
-          }
+        for (int d = ND - 1; d >= 1; --d) {
+          const uint32_t q = fast_div(idx, magic[d], shift[d]);
+          const int64_t r = (int64_t)(idx - q * size[d]);
+          so += r * sstr[d];
+          dof += r * dstr[d];
+          idx = q;
         }
+        so += (int64_t)idx * sstr[0];
+        dof += (int64_t)idx * dstr[0];
         v[j] = __ldg(src + so);
         doff[j] = dof;
       }
@@ -59,6 +70,39 @@ __device__ __forceinline__ void copy_units(const Unit* __restrict__ src, Unit* _
 #pragma unroll
     for (int j = 0; j < kIlp; ++j)
       if (doff[j] >= 0) dst[doff[j]] = v[j];
+  }
+}
+
+// Tasks with more than 4 dims (rare: the host collapses every dim contiguous on both sides).
+template <typename Unit>
+__device__ __forceinline__ void copy_units_generic(const Unit* __restrict__ src, Unit* __restrict__ dst,
+                                                   const int64_t* rec, int64_t first) {
+  const int ndim = (int)rec[YB_CP_NDIM];
+  const int64_t n = min((int64_t)YB_COPY_ITEM_UNITS, rec[YB_CP_COUNT] - first);
+  for (int64_t e = threadIdx.x; e < n; e += kThreads) {
+    uint32_t idx = (uint32_t)(first + e);
+    int64_t so = rec[YB_CP_SRC], dof = rec[YB_CP_DST];
+    for (int d = ndim - 1; d >= 0; --d) {
+      const uint32_t size = (uint32_t)rec[YB_CP_SIZE + d];
+      const uint32_t q = fast_div(idx, (uint32_t)rec[YB_CP_MAGIC + d], (uint32_t)rec[YB_CP_SHIFT + d]);
+      const int64_t r = (int64_t)(idx - q * size);
+      so += r * rec[YB_CP_SSTR + d];
+      dof += r * rec[YB_CP_DSTR + d];
+      idx = q;
+    }
+    dst[dof] = __ldg(src + so);
+  }
+}
+
+template <typename Unit>
+__device__ __forceinline__ void copy_units_any(const Unit* __restrict__ src, Unit* __restrict__ dst, const int64_t* rec,
+                                               int64_t first) {
+  switch ((int)rec[YB_CP_NDIM]) {
+    case 1: copy_units<Unit, 1>(src, dst, rec, first); break;
+    case 2: copy_units<Unit, 2>(src, dst, rec, first); break;
+    case 3: copy_units<Unit, 3>(src, dst, rec, first); break;
+    case 4: copy_units<Unit, 4>(src, dst, rec, first); break;
+    default: copy_units_generic<Unit>(src, dst, rec, first); break;
   }
 }
 
@@ -119,9 +163,9 @@ __global__ void __launch_bounds__(kThreads) block_copy_kernel(const Elem* __rest
   if (rec[YB_CP_KIND] == 1)
     copy_tiles<Elem>(src, dst, rec, first, tile);
   else if (sizeof(Elem) == 8 && rec[YB_CP_VEC] != 0)
-    copy_units<double2>(reinterpret_cast<const double2*>(src), reinterpret_cast<double2*>(dst), rec, first);
+    copy_units_any<double2>(reinterpret_cast<const double2*>(src), reinterpret_cast<double2*>(dst), rec, first);
   else
-    copy_units<Elem>(src, dst, rec, first);
+    copy_units_any<Elem>(src, dst, rec, first);
 }
 
 }  // namespace

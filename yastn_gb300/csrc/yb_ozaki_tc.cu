@@ -289,8 +289,8 @@ int launch_fused(const double* A, const double* B, const int* exps, double* C, c
 
 // Per-row (axis 0) or per-column (axis 1) exponents: rec (8 int64): [0] offset (elements)
 // [1] rows [2] cols [3] ld (elements) [4] 1 for complex data (a complex row counts its real
-// and imaginary parts) [5] exponents offset. Axis 0: one warp per row; axis 1: one thread per
-// column, walking down the rows (coalesced across the warp).
+// and imaginary parts) [5] exponents offset. Axis 0: one warp per row; axis 1: 32 columns
+// per CTA, its 8 warps walking down the rows (coalesced along the columns).
 __global__ void ozaki_exps_kernel(const double* __restrict__ X, int* __restrict__ exps,
                                   const int64_t* __restrict__ recs, int axis) {
   const int64_t* r = recs + (int64_t)blockIdx.y * 8;
@@ -310,15 +310,24 @@ __global__ void ozaki_exps_kernel(const double* __restrict__ X, int* __restrict_
     for (int w = 16; w > 0; w >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, w));
     if (lane == 0) exps[eoff + row] = exponent_of(mx);
   } else {
-    const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (col >= cols) return;
+    // 32 columns per CTA, the 8 warps walk down the rows (coalesced along the columns)
+    __shared__ long long red[8][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t col = (int64_t)blockIdx.x * 32 + lane;
+    if ((int64_t)blockIdx.x * 32 >= cols) return;
     long long mx = 0;
-    for (int64_t k = 0; k < rows; ++k) {
-      const int64_t e = off + k * ld + col;
-      if (cplx) mx = max(mx, max(__ldg(Xb + 2 * e) & kMag, __ldg(Xb + 2 * e + 1) & kMag));
-      else mx = max(mx, __ldg(Xb + e) & kMag);
+    if (col < cols)
+      for (int64_t k = warp; k < rows; k += 8) {
+        const int64_t e = off + k * ld + col;
+        if (cplx) mx = max(mx, max(__ldg(Xb + 2 * e) & kMag, __ldg(Xb + 2 * e + 1) & kMag));
+        else mx = max(mx, __ldg(Xb + e) & kMag);
+      }
+    red[warp][lane] = mx;
+    __syncthreads();
+    if (warp == 0 && col < cols) {
+      for (int w = 1; w < 8; ++w) mx = max(mx, red[w][lane]);
+      exps[eoff + col] = exponent_of(mx);
     }
-    exps[eoff + col] = exponent_of(mx);
   }
 }
 
@@ -334,7 +343,7 @@ int yb_ozaki_exponents(const void* x, int* exps, const int64_t* recs, int n_recs
                        void* stream) {
   if (n_recs == 0 || max_len == 0) return YB_OK;
   if (!x || !exps || !recs || n_recs < 0 || max_len < 0 || (axis != 0 && axis != 1)) return YB_ERR_INVALID;
-  const unsigned gx = axis == 0 ? (unsigned)((max_len + 7) / 8) : (unsigned)((max_len + 255) / 256);
+  const unsigned gx = axis == 0 ? (unsigned)((max_len + 7) / 8) : (unsigned)((max_len + 31) / 32);
   yb::ozaki_exps_kernel<<<dim3(gx, (unsigned)n_recs), 256, 0, (cudaStream_t)stream>>>((const double*)x, exps, recs,
                                                                                        axis);
   return yb::check_launch();

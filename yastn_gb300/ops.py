@@ -216,14 +216,15 @@ def _ozaki_run(plan, A, B, out, slices, tc):
         N.call('yb_ozaki_gemm_fused', _ptr(A), _ptr(B), _ptr(ex), _ptr(out), _ptr(dout), _ptr(dtl),
                len(plan.tiles_f), slices, st)
         return
-    dar, dbr, dout, dtl = _dev(plan, 'ozaki', (plan.a_recs, plan.b_recs, plan.outs, plan.tiles), dev)
+    dar, dbc, dout, dtl = _dev(plan, 'ozaki', (plan.a_recs, plan.b_cols, plan.outs, plan.tiles), dev)
     a_sl = torch.empty(plan.a_size, dtype=torch.bfloat16, device=dev)
     b_sl = torch.empty(plan.b_size, dtype=torch.bfloat16, device=dev)
     a_ex = torch.empty(max(plan.a_exps, 1), dtype=torch.int32, device=dev)
     b_ex = torch.empty(max(plan.b_exps, 1), dtype=torch.int32, device=dev)
-    bT = run_copy(plan.bT, B, torch.empty(max(plan.bT_size, 1), dtype=B.dtype, device=dev))
     N.call('yb_ozaki_split', _ptr(A), _ptr(a_sl), _ptr(a_ex), _ptr(dar), len(plan.a_recs), plan.a_rows, slices, st)
-    N.call('yb_ozaki_split', _ptr(bT), _ptr(b_sl), _ptr(b_ex), _ptr(dbr), len(plan.b_recs), plan.b_rows, slices, st)
+    # B's columns split in place (the digits of B^T's rows without a transposed copy)
+    N.call('yb_ozaki_split_cols', _ptr(B), _ptr(b_sl), _ptr(b_ex), _ptr(dbc), len(plan.b_cols), plan.b_cols_max,
+           slices, st)
     N.call('yb_ozaki_gemm', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
            len(plan.tiles), slices, st)
 
