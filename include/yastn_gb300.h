@@ -115,13 +115,6 @@ int yb_block_copy(const void* src, void* dst, int unit_bytes,
 int yb_grouped_gemm(const void* a, const void* b, void* c, int dtype,
                     const int64_t* outs, const int64_t* terms, const int32_t* tiles, int n_tiles,
                     double alpha, double beta, void* stream);
-/* yb_grouped_gemm_skinny: the same products for skinny tiles only (tile kind 1; other tiles
- * are skipped), in a kernel of its own so that the 64 x 64 tiles keep their register budget;
- * single-term outputs with at most 4 rows and K <= 8 (the contractions with a small MPO
- * block) load their whole column strip before the FMAs. */
-int yb_grouped_gemm_skinny(const void* a, const void* b, void* c, int dtype,
-                           const int64_t* outs, const int64_t* terms, const int32_t* tiles, int n_tiles,
-                           double alpha, double beta, void* stream);
 /* yb_gemm_reduce: the second pass of a split-K product. The host splits the K range of
  * outputs whose few tiles would leave most SMs idle into chunks, computes each chunk's
  * product into its own slot of a workspace P (yb_grouped_gemm with alpha 1, beta 0), then
@@ -155,39 +148,28 @@ int yb_gemm_reduce(void* c, const void* p, int dtype, const int64_t* recs, const
  */
 int yb_ozaki_split(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs,
                    int max_rows, int slices_count, void* stream);
-/* yb_ozaki_split_cols: the split of B's columns read in place from row-major K x n blocks
- * (no transposed copy): recs (8 int64) [0] B block offset (elements) [1] K [2] n [3] ldb
- * [4] mode (0 real; 2, 3: the complex modes of yb_ozaki_split applied to column j, i.e. the
- * rows [re | -im] and [im | re] of B^T) [5] destination offset (BF16 elements) [6] exponent
- * offset [7] Kp. Writes the same digits and exponents as yb_ozaki_split on B^T's rows, in
- * [slice][column][Kp]; max_cols: largest n. */
-int yb_ozaki_split_cols(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs,
-                        int max_cols, int slices_count, void* stream);
 int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps,
                   double* c, const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
                   void* stream);
-/* yb_ozaki_exponents: the per-row (axis 0, the A operands) or per-column (axis 1, the B
- * operands) exponents e of the split, max |x| = f 2^e with f in [0.5, 1) (0 for a zero
- * row/column). recs: n_recs records of 8 int64: [0] block offset (elements) [1] rows
- * [2] cols [3] row stride (elements) [4] 1 for complex128 data (a row or column counts both
- * parts) [5] exponents offset; max_len: largest rows (axis 0) or cols (axis 1). */
-int yb_ozaki_exponents(const void* x, int* exps, const int64_t* recs, int n_recs, int max_len, int axis,
-                       void* stream);
-/* yb_ozaki_gemm_fused: the emulated sector GEMMs on the tcgen05 tensor cores with the digit
- * split fused in: each 128 x 64 output tile reads its FP64 (or complex128) operand tiles
- * from A (row-major m x K blocks) and B (row-major K x n blocks) directly, writes their
- * slices_count (6, 7 or 8) BF16 digits into shared memory, accumulates the digit-diagonal
- * products in tensor memory (exact FP32 sums per 400-long K chunk) and rounds each chunk's
- * exact integer combination once to FP64 -- the same bits as yb_ozaki_gemm. outs: 16 int64
- * per output: [0] c offset (FP64 words) [1] m [2] n [3] ldc (FP64 words) [4] A block offset
- * (elements) [5] A exponents offset [6] B block offset (elements) [7] B exponents offset
- * [8] K [9] lda [10] output column stride (FP64 words) [11] complex part (0: C_r, 1: C_i)
- * [12] 1 for complex128 operands [13] ldb; exps: from yb_ozaki_exponents (A rows, B
- * columns); tiles: int32 (output, tile row, tile col, 0), one CTA each. A CTA that gives up
- * on a bounded wait writes nothing for its tile and sets the status word read by
- * yb_ozaki_device_error. Replaces dot (backend_torch.py:549-550) in the emulated mode. */
-int yb_ozaki_gemm_fused(const void* a, const void* b, const int* exps, double* c, const int64_t* outs,
-                        const int32_t* tiles, int n_tiles, int slices_count, void* stream);
+/* yb_ozaki_split_tiled: yb_ozaki_split writing the digit planes in the tile layout of
+ * yb_ozaki_gemm_tc: per slice, tile_rows (128 for A, 64 for B) x 16 blocks, each in the
+ * canonical K-major core-matrix order (byte offset of (row r, k) in a block:
+ * (r/8)*256 + (k/8)*128 + (r%8)*16 + (k%8)*2), blocks ordered (row tile, K step); the
+ * rows are padded with zeros to a multiple of tile_rows (record [5] = slice-0 offset, slice
+ * stride = padded rows x Kp). */
+int yb_ozaki_split_tiled(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs,
+                         int max_rows, int slices_count, int tile_rows, void* stream);
+/* yb_ozaki_gemm_tc: yb_ozaki_gemm on the tcgen05 tensor cores, operands from
+ * yb_ozaki_split_tiled (output records [4], [6] = the A / B slice-0 offsets in the tile
+ * layout); tiles are (output, tile row, tile col, 0) of 128 rows x 64 columns, one CTA each,
+ * whose warps split the work: one streams the digit tiles (cp.async.bulk into a 4-stage
+ * ring), one issues the tcgen05.mma into the digit-diagonal accumulators in tensor memory,
+ * four fold the accumulators exactly and write the tile (the same bits as yb_ozaki_gemm).
+ * A CTA that gives up on a bounded wait writes nothing for its tile and sets the status word
+ * read by yb_ozaki_device_error. */
+int yb_ozaki_gemm_tc(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps,
+                     double* c, const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
+                     void* stream);
 /* yb_ozaki_device_error: copies the tcgen05 kernel's status word to *out (0: no failure),
  * synchronising the stream, and clears it when reset != 0. */
 int yb_ozaki_device_error(int* out, int reset, void* stream);

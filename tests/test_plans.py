@@ -744,11 +744,11 @@ def test_ozaki_plan_records():
                                    A[sla[0]:sla[1]].reshape(Da) @ B[slb[0]:slb[1]].reshape(Db), rtol=1e-13)
 
 
-def test_ozaki_fused_records_reproduce_products():
-    """Records of the fused tcgen05 kernel: per output, A's block (rows of [re | im] for
-    complex data) times B's block read by segments ([B_r; -B_i] for the real part, [B_i; B_r]
-    for the imaginary part), written at c offset + i ldc + j column stride; the exponent
-    records cover every A row and B column once; tiles cover every output, longest K first."""
+def test_ozaki_tiled_records_and_tiles():
+    """Records of the tcgen05 kernel: every operand block gets s * ceil(rows / tile) * tile * Kp
+    digits in the tile layout (128 rows for A, 64 for B^T rows), without overlap and in block
+    order; the output records point at the remapped blocks; tiles cover every output once by
+    decreasing K."""
     rng = np.random.default_rng(23)
     shapes = [(40, 30, 20), (16, 16, 17), (130, 20, 70), (5, 40, 9), (3, 8, 100), (6, 300, 200)]
     meta, oa, ob, oc = [], 0, 0, 0
@@ -757,43 +757,21 @@ def test_ozaki_fused_records_reproduce_products():
         oa += m * k; ob += k * n; oc += m * n
     meta = tuple(meta)
     for cplx in (False, True):
-        A = rng.normal(size=oa) + (1j * rng.normal(size=oa) if cplx else 0)
-        B = rng.normal(size=ob) + (1j * rng.normal(size=ob) if cplx else 0)
         plan = P.ozaki_dot_plan(meta, 8, cplx)
-        f = 2 if cplx else 1
-        assert len(plan.outs_f) == f * 4  # (3, 8, 100) is short, (6, 300, 200) skinny: native
-        Cd = np.zeros(f * oc)
-        for o in plan.outs_f:
-            c_off, m, n, ldc, ao, aex, bo, bex, K, lda, cs, part, cp, ldb = (int(x) for x in o[:14])
-            assert cp == int(cplx) and lda == K and ldb == n
-            Ab = A[ao:ao + m * K].reshape(m, K)
-            Bb = B[bo:bo + K * n].reshape(K, n)
-            if cplx:
-                Ar = np.concatenate([Ab.real, Ab.imag], axis=1)
-                Br = np.concatenate([Bb.real, -Bb.imag] if part == 0 else [Bb.imag, Bb.real], axis=0)
-            else:
-                Ar, Br = Ab, Bb
-            prod = Ar @ Br
-            for i in range(m):
-                Cd[c_off + i * ldc + cs * np.arange(n)] = prod[i]
-        C = Cd[0::2] + 1j * Cd[1::2] if cplx else Cd
-        for (slc, Dc, sla, Da, slb, Db) in meta:
-            m, K = Da
-            n = Db[1]
-            if K < 16 or (m <= 8 and n > 64):
-                continue
-            ref = A[sla[0]:sla[1]].reshape(Da) @ B[slb[0]:slb[1]].reshape(Db)
-            np.testing.assert_allclose(C[slc[0]:slc[1]].reshape(Dc), ref, rtol=1e-12, atol=1e-12)
-        # exponent records: A rows (axis 0) and B columns (axis 1) in one array, no overlap
-        spans = [(int(r[5]), int(r[5]) + int(r[1])) for r in plan.exp_a] + \
-                [(int(r[5]), int(r[5]) + int(r[2])) for r in plan.exp_b]
-        spans.sort()
-        assert spans[0][0] == 0 and spans[-1][1] == plan.n_exps
-        assert all(a[1] == b[0] for a, b in zip(spans, spans[1:]))
-        # tiles: every (output, 128-row tile, 64-column tile) once, by decreasing K steps
-        want = {(oi, tr, tc) for oi, o in enumerate(plan.outs_f)
+        for recs, th, size in ((plan.a_recs_tc, 128, plan.a_size_tc), (plan.b_recs_tc, 64, plan.b_size_tc)):
+            end = 0
+            for r in recs:
+                assert int(r[5]) == end
+                end += 8 * (-(-int(r[1]) // th) * th) * int(r[7])
+            assert end == size
+        a_new = {int(o): int(t) for o, t in zip(plan.a_recs[:, 5], plan.a_recs_tc[:, 5])}
+        b_new = {int(o): int(t) for o, t in zip(plan.b_recs[:, 5], plan.b_recs_tc[:, 5])}
+        for o, t in zip(plan.outs, plan.outs_tc):
+            assert int(t[4]) == a_new[int(o[4])] and int(t[6]) == b_new[int(o[6])]
+            assert np.array_equal(np.delete(o, [4, 6]), np.delete(t, [4, 6]))
+        want = {(oi, tr, tc) for oi, o in enumerate(plan.outs_tc)
                 for tr in range(-(-int(o[1]) // 128)) for tc in range(-(-int(o[2]) // 64))}
-        got = [tuple(int(x) for x in t[:3]) for t in plan.tiles_f]
+        got = [tuple(int(x) for x in t[:3]) for t in plan.tiles_tc]
         assert len(got) == len(want) and set(got) == want
-        ks = [int(plan.outs_f[t[0]][8]) for t in plan.tiles_f]
+        ks = [int(plan.outs_tc[t[0]][8]) for t in plan.tiles_tc]
         assert ks == sorted(ks, reverse=True)

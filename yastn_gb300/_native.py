@@ -22,7 +22,6 @@ SIGNATURES = {
     'yb_block_copy': ([_vp, _vp, _i, _vp, _i, _vp, _i, _vp], _i),
     'yb_gemm_reduce': ([_vp, _vp, _i, _vp, _vp, _i, _d, _d, _vp], _i),
     'yb_grouped_gemm': ([_vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _d, _d, _vp], _i),
-    'yb_grouped_gemm_skinny': ([_vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _d, _d, _vp], _i),
     'yb_svd_init': ([_vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp], _i),
     'yb_svd_qr': ([_vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _i, _vp], _i),
     'yb_qr': ([_vp, _vp, _vp, _vp, _vp, _i, _i, _vp, _i, _vp], _i),
@@ -40,10 +39,9 @@ SIGNATURES = {
     'yb_fix_signs': ([_vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp], _i),
     'yb_fix_signs_adjoint': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp], _i),
     'yb_ozaki_split': ([_vp, _vp, _vp, _vp, _i, _i, _i, _vp], _i),
-    'yb_ozaki_split_cols': ([_vp, _vp, _vp, _vp, _i, _i, _i, _vp], _i),
-    'yb_ozaki_exponents': ([_vp, _vp, _vp, _i, _i, _i, _vp], _i),
+    'yb_ozaki_split_tiled': ([_vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp], _i),
     'yb_ozaki_gemm': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
-    'yb_ozaki_gemm_fused': ([_vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
+    'yb_ozaki_gemm_tc': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
     'yb_ozaki_device_error': ([_vp, _i, _vp], _i),
     'yb_ozaki_dot_static': ([_vp, _vp, _vp, _i, _vp, _i, _i, _vp, _i, _i, _vp, _i, _vp, _i, _vp, _vp, _i,
                              _vp, _vp, _vp, _i, _i, _i64, _i64, _i64, _i64, _i64, _vp], _i),

@@ -299,12 +299,7 @@ class GemmPlan:
     def __init__(self, outs, terms, tiles, flops, split=None):
         self.outs = outs
         self.terms = terms
-        self.tiles = tiles  # all tiles (yb_grouped_gemm takes both kinds)
-        # the launches of the backend: 64 x 64 tiles (yb_grouped_gemm) and skinny tiles
-        # (yb_grouped_gemm_skinny) apart
-        sk = tiles[:, 3] == 1 if len(tiles) else np.zeros(0, dtype=bool)
-        self.tiles_main = np.ascontiguousarray(tiles[~sk]) if len(tiles) else tiles
-        self.tiles_skinny = np.ascontiguousarray(tiles[sk]) if len(tiles) else tiles
+        self.tiles = tiles
         self.flops = flops  # real multiply-adds x 2 (complex counted by the caller)
         self.split = split
         self._dev = {}
@@ -447,13 +442,27 @@ def _pack_gemm(out_list, allow_split=True):
     return GemmPlan(outs, terms, _tiles_for(outs, terms), flops, split)
 
 
+def dot_coverage(meta_dot):
+    """Number of output elements that the sectors of ``meta_dot`` write, when their output
+    slices are disjoint (0 otherwise): equal to Dsize, the output needs no zero fill."""
+    spans = sorted((slc[0], slc[1]) for slc, *_ in meta_dot)
+    end = 0
+    for a, b in spans:
+        if a < end:
+            return 0
+        end = b
+    return sum(b - a for a, b in spans)
+
+
 def dot_plan(meta_dot):
     """C[slc] = A[sla] @ B[slb] (yastn/backend/backend_np.py:580-587)."""
     def build():
         out_list = []
         for slc, Dc, sla, Da, slb, Db in meta_dot:
             out_list.append((slc[0], Dc[0], Dc[1], Dc[1], [(sla[0], slb[0], Da[1], Da[1], 1, Db[1], 1, 0)]))
-        return _pack_gemm(out_list)
+        plan = _pack_gemm(out_list)
+        plan.covered = dot_coverage(meta_dot)
+        return plan
     return CACHE.get((meta_dot,), ('dot',), build)
 
 
@@ -506,45 +515,17 @@ OZAKI_MIN_DIM = 16  # sector GEMMs contracting fewer indices than this stay on t
 OZAKI_SKINNY_ROWS = 8  # sector GEMMs with at most this many rows (and more than 64 columns) too
 
 
-def _fused_records(plan, meta_dot, cplx):
-    """Records of the fused tcgen05 kernel (yb_ozaki_exponents + yb_ozaki_gemm_fused) for the
-    sectors ``plan`` emulates: exponent records per A block (rows) and per B block (columns),
-    one output record per sector (two for complex data: the real and the imaginary part,
-    C_r = [A_r, A_i][B_r; -B_i] and C_i = [A_r, A_i][B_i; B_r]) and 128 x 64 tiles, the
-    longest K first."""
-    a_map, b_map, ea, eb, outs = {}, {}, [], [], []
-    n_exp = 0
-    f = 2 if cplx else 1
-    for slc, Dc, sla, Da, slb, Db in meta_dot:
-        m, K = Da
-        n = Db[1]
-        if K < OZAKI_MIN_DIM or (m <= OZAKI_SKINNY_ROWS and n > GEMM_TILE):
-            continue
-        if sla[0] not in a_map:
-            a_map[sla[0]] = n_exp
-            ea.append((sla[0], m, K, K, int(cplx), n_exp, 0, 0))
-            n_exp += m
-        if slb[0] not in b_map:
-            b_map[slb[0]] = n_exp
-            eb.append((slb[0], K, n, n, int(cplx), n_exp, 0, 0))
-            n_exp += n
-        for part in range(f):
-            outs.append((f * slc[0] + part, m, n, f * n, sla[0], a_map[sla[0]], slb[0], b_map[slb[0]], K, K, f, part,
-                         int(cplx), n, 0, 0))
-    tiles = []
-    for oi, o in enumerate(outs):
-        m, n, K = int(o[1]), int(o[2]), int(o[8])
-        for tr in range(-(-m // OZAKI_TC_M)):
-            for tc in range(-(-n // OZAKI_TC_N)):
-                tiles.append((f * K, oi, tr, tc))
-    tiles.sort(key=lambda x: -x[0])
-    plan.exp_a = np.array(ea, dtype=np.int64).reshape(-1, 8)
-    plan.exp_b = np.array(eb, dtype=np.int64).reshape(-1, 8)
-    plan.exp_a_max = int(plan.exp_a[:, 1].max()) if len(ea) else 0
-    plan.exp_b_max = int(plan.exp_b[:, 2].max()) if len(eb) else 0
-    plan.n_exps = n_exp
-    plan.outs_f = np.array(outs, dtype=np.int64).reshape(-1, 16)
-    plan.tiles_f = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles], dtype=np.int32).reshape(-1, 4)
+def _tiled_recs(recs, s, th):
+    """Split records with destinations in the tcgen05 tile layout: each operand block takes
+    s * ceil(rows / th) * th * Kp digits. Returns (records, total size, old offset -> new)."""
+    out = recs.copy()
+    size, remap = 0, {}
+    for i, r in enumerate(recs):
+        rows, Kp = int(r[1]), int(r[7])
+        remap[int(r[5])] = size
+        out[i, 5] = size
+        size += s * (-(-rows // th) * th) * Kp
+    return out, size, remap
 
 
 def ozaki_dot_plan(meta_dot, s, cplx=False):
@@ -558,7 +539,7 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
     parts of the complex result (column stride 2 in FP64 units).
     """
     def build():
-        a_map, b_map, a_recs, b_recs, bT_tasks, b_cols = {}, {}, [], [], [], []
+        a_map, b_map, a_recs, b_recs, bT_tasks = {}, {}, [], [], []
         a_size = b_size = a_ex = b_ex = bT_size = 0
         outs, flops, small = [], 0, []
         f = 2 if cplx else 1  # FP64 words per element
@@ -581,7 +562,6 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
                 parts = []
                 for mode in ((2, 3) if cplx else (0,)):
                     b_recs.append((bT_size, n, Kr, K, mode, b_size, b_ex, Kp))
-                    b_cols.append((slb[0], K, n, n, mode, b_size, b_ex, Kp))  # B read in place
                     parts.append((b_size, b_ex))
                     b_size += s * n * Kp
                     b_ex += n
@@ -612,10 +592,24 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
         plan.bT_size = bT_size
         plan.native = _pack_gemm(small)
         plan.native_direct = _pack_gemm(small, allow_split=False)  # no chunk workspace
-        # column split of B in place (yb_ozaki_split_cols): the same digit planes, no B^T copy
-        plan.b_cols = np.array(b_cols, dtype=np.int64).reshape(-1, 8)
-        plan.b_cols_max = int(plan.b_cols[:, 2].max()) if len(b_cols) else 0
-        _fused_records(plan, meta_dot, cplx)
+        plan.covered = dot_coverage(meta_dot)
+        # 128 x 64 tiles of the tcgen05 kernel (longest K first) and the digit planes in its
+        # tile layout (rows padded to 128 for A, 64 for B)
+        tiles_tc = []
+        for oi, o in enumerate(outs):
+            m, n, K = int(o[1]), int(o[2]), int(o[8])
+            for tr in range(-(-m // OZAKI_TC_M)):
+                for tc in range(-(-n // OZAKI_TC_N)):
+                    tiles_tc.append((K, oi, tr, tc))
+        tiles_tc.sort(key=lambda x: -x[0])
+        plan.tiles_tc = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles_tc], dtype=np.int32).reshape(-1, 4)
+        plan.a_recs_tc, plan.a_size_tc, a_off_tc = _tiled_recs(a_recs, s, OZAKI_TC_M)
+        plan.b_recs_tc, plan.b_size_tc, b_off_tc = _tiled_recs(b_recs, s, OZAKI_TC_N)
+        outs_tc = outs.copy()
+        if len(outs_tc):
+            outs_tc[:, 4] = [a_off_tc[int(x)] for x in outs[:, 4]]
+            outs_tc[:, 6] = [b_off_tc[int(x)] for x in outs[:, 6]]
+        plan.outs_tc = outs_tc
         # padded MMA work of the two tilings: the tcgen05 kernel (128 x 64 tiles) when its
         # padding costs little more than the 64 x 64 tiles of the mma.sync kernel
         w64 = sum(-(-int(o[1]) // 64) * 64 * -(-int(o[2]) // 64) * 64 * int(o[9]) for o in outs)

@@ -117,76 +117,6 @@ __device__ __forceinline__ void skinny_tile(const typename F::T* __restrict__ A,
   }
 }
 
-// Skinny tile with one term and K <= kShortK (the contractions with a small MPO block): op(A)
-// goes to shared memory once, and every thread issues all K x CPT loads of its columns of
-// op(B) before the FMAs, so the whole column strip is in flight at once.
-constexpr int kShortK = 8;
-template <class F, int M, int CPT>
-__device__ __forceinline__ void skinny_tile_short(const typename F::T* __restrict__ A,
-                                                  const typename F::T* __restrict__ B, typename F::T* __restrict__ C,
-                                                  const int64_t* __restrict__ orec, const int64_t* __restrict__ trec,
-                                                  int tcol, double alpha, double beta, typename F::T* Ak) {
-  using T = typename F::T;
-  const int64_t c_off = orec[0], ldc = orec[3];
-  const int64_t mr = orec[1], nc = orec[2];
-  const int K = (int)trec[2];
-  const T* La = A + trec[0];
-  const int64_t l_is = trec[3], l_ls = trec[4], r_ls = trec[5], r_js = trec[6];
-  const int flags = (int)trec[7];
-  const bool conjL = flags & 1, conjR = flags & 2;
-  if (threadIdx.x < kShortK * M) {
-    const int i = threadIdx.x % M, l = threadIdx.x / M;
-    T v = F::zero();
-    if (l < K && i < mr) {
-      v = La[i * l_is + l * l_ls];
-      if (conjL) v = F::conj(v);
-    }
-    Ak[l * M + i] = v;
-  }
-  __syncthreads();
-  const int64_t j0 = (int64_t)tcol * (kThreads * CPT) + threadIdx.x;
-  T b[kShortK][CPT];
-#pragma unroll
-  for (int u = 0; u < CPT; ++u) {
-    const int64_t j = j0 + u * kThreads;
-    const bool live = j < nc;
-    const T* col = B + trec[1] + (live ? j * r_js : 0);
-#pragma unroll
-    for (int l = 0; l < kShortK; ++l) {
-      b[l][u] = (live && l < K) ? __ldg(col + l * r_ls) : F::zero();
-      if (conjR) b[l][u] = F::conj(b[l][u]);
-    }
-  }
-  T acc[CPT][M];
-#pragma unroll
-  for (int u = 0; u < CPT; ++u)
-#pragma unroll
-    for (int i = 0; i < M; ++i) acc[u][i] = F::zero();
-#pragma unroll
-  for (int l = 0; l < kShortK; ++l) {
-    if (l >= K) break;
-#pragma unroll
-    for (int i = 0; i < M; ++i) {
-      const T a = Ak[l * M + i];
-#pragma unroll
-      for (int u = 0; u < CPT; ++u) F::fma(acc[u][i], a, b[l][u]);
-    }
-  }
-#pragma unroll
-  for (int u = 0; u < CPT; ++u) {
-    const int64_t j = j0 + u * kThreads;
-    if (j >= nc) continue;
-#pragma unroll
-    for (int i = 0; i < M; ++i) {
-      if (i >= mr) break;
-      T* p = C + c_off + i * ldc + j;
-      T v = alpha == 1.0 ? acc[u][i] : F::scale(acc[u][i], alpha);
-      if (beta != 0.0) v = F::add(v, F::scale(*p, beta));
-      *p = v;
-    }
-  }
-}
-
 template <class F>
 __device__ __forceinline__ void skinny_dispatch(int64_t mr, const typename F::T* __restrict__ A,
                                                 const typename F::T* __restrict__ B, typename F::T* __restrict__ C,
@@ -315,38 +245,6 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_kernel(const typename F
   }
 }
 
-// Skinny tiles only (tile record w = 1; other tiles are skipped): the outputs with at most
-// 16 rows, launched apart from the 64 x 64 tiles so that their register budget does not
-// lower the occupancy of the register-tiled kernel. Single-term outputs with K <= kShortK
-// and at most 4 rows take skinny_tile_short.
-template <class F>
-__global__ void __launch_bounds__(kThreads, 1) skinny_gemm_kernel(const typename F::T* __restrict__ A,
-                                                                const typename F::T* __restrict__ B,
-                                                                typename F::T* __restrict__ C,
-                                                                const int64_t* __restrict__ outs,
-                                                                const int64_t* __restrict__ terms,
-                                                                const int32_t* __restrict__ tiles, double alpha,
-                                                                double beta) {
-  using T = typename F::T;
-  __shared__ T Ak[kK * (kTile + kPad)];
-  const int4 tl = reinterpret_cast<const int4*>(tiles)[blockIdx.x];
-  if (tl.w != 1) return;
-  const int64_t* orec = outs + (int64_t)tl.x * YB_GEMM_OUT_REC;
-  const int64_t mr = orec[1];
-  if (orec[5] - orec[4] == 1 && mr <= 4) {
-    const int64_t* trec = terms + orec[4] * YB_GEMM_TERM_REC;
-    if (trec[2] <= kShortK) {
-      switch (mr) {
-        case 1: skinny_tile_short<F, 1, 4>(A, B, C, orec, trec, tl.z, alpha, beta, Ak); return;
-        case 2: skinny_tile_short<F, 2, 4>(A, B, C, orec, trec, tl.z, alpha, beta, Ak); return;
-        case 3: skinny_tile_short<F, 3, 4>(A, B, C, orec, trec, tl.z, alpha, beta, Ak); return;
-        default: skinny_tile_short<F, 4, 4>(A, B, C, orec, trec, tl.z, alpha, beta, Ak); return;
-      }
-    }
-  }
-  skinny_dispatch<F>(mr, A, B, C, orec, terms, tl.z, alpha, beta, Ak);
-}
-
 // Split-K reduction: C_o = alpha * sum_{c < chunks} P[p_off + c m n + i n + j] + beta * C_o,
 // the partial products summed in chunk order (deterministic). One CTA per task of
 // YB_GEMM_RED_ITEM consecutive elements of one output.
@@ -388,24 +286,6 @@ extern "C" int yb_gemm_reduce(void* c, const void* p, int dtype, const int64_t* 
   } else if (dtype == YB_C128) {
     yb::gemm_reduce_kernel<yb::Cplx><<<n_tasks, yb::kThreads, 0, s>>>((double2*)c, (const double2*)p, recs,
                                                                       tasks, alpha, beta);
-  } else {
-    return YB_ERR_INVALID;
-  }
-  return yb::check_launch();
-}
-
-extern "C" int yb_grouped_gemm_skinny(const void* a, const void* b, void* c, int dtype, const int64_t* outs,
-                                      const int64_t* terms, const int32_t* tiles, int n_tiles, double alpha,
-                                      double beta, void* stream) {
-  if (n_tiles == 0) return YB_OK;
-  if (!a || !b || !c || !outs || !tiles || n_tiles < 0) return YB_ERR_INVALID;
-  cudaStream_t s = (cudaStream_t)stream;
-  if (dtype == YB_F64) {
-    yb::skinny_gemm_kernel<yb::Real><<<n_tiles, yb::kThreads, 0, s>>>(
-        (const double*)a, (const double*)b, (double*)c, outs, terms, tiles, alpha, beta);
-  } else if (dtype == YB_C128) {
-    yb::skinny_gemm_kernel<yb::Cplx><<<n_tiles, yb::kThreads, 0, s>>>(
-        (const double2*)a, (const double2*)b, (double2*)c, outs, terms, tiles, alpha, beta);
   } else {
     return YB_ERR_INVALID;
   }

@@ -6,7 +6,7 @@
 // device scalars, so a whole expansion runs without a host synchronisation and can be
 // captured in a CUDA graph. Reductions are deterministic: a fixed grid of kParts CTAs writes
 // per-CTA partial sums (each CTA sums a fixed strided set of elements in a fixed order, then
-// a fixed shared-memory tree), and one warp adds the partials in order.
+// a fixed shared-memory tree), and one warp adds the partials in a fixed order.
 //
 //   yb_krylov_dot:    s = sum_i conj(x_i) y_i                      (alpha_j = <V_j, w>)
 //   yb_krylov_update: w <- w - alpha V_j - beta V_{j-1}, s = |w|    (one pass over w)
@@ -94,21 +94,24 @@ __global__ void __launch_bounds__(kThr) update_kernel(typename F::T* __restrict_
   if (threadIdx.x == 0) parts[blockIdx.x] = s;
 }
 
-// out = sum of the parts in order; sqrt_out: out = sqrt(sum) (real parts only)
+// out = the sum of the parts (one warp: lane l adds parts l, l + 32, ... in order, then a fixed
+// shuffle tree, so the result does not depend on timing); finish_norm_kernel: out = sqrt(sum)
 template <class F>
 __global__ void finish_kernel(const typename F::T* __restrict__ parts, typename F::T* __restrict__ out, int n_parts) {
   using T = typename F::T;
-  if (threadIdx.x != 0) return;
   T s = F::zero();
-  for (int i = 0; i < n_parts; ++i) s = F::add(s, parts[i]);
-  *out = s;
+  for (int i = threadIdx.x; i < n_parts; i += 32) s = F::add(s, parts[i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s = F::add(s, F::shfl(s, o));
+  if (threadIdx.x == 0) *out = s;
 }
 
 __global__ void finish_norm_kernel(const double* __restrict__ parts, double* __restrict__ out, int n_parts) {
-  if (threadIdx.x != 0) return;
   double s = 0.0;
-  for (int i = 0; i < n_parts; ++i) s += parts[i];
-  *out = sqrt(s);
+  for (int i = threadIdx.x; i < n_parts; i += 32) s += parts[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (threadIdx.x == 0) *out = sqrt(s);
 }
 
 template <class F>

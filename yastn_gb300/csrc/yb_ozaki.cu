@@ -123,80 +123,46 @@ __global__ void split_rows_kernel(const double* __restrict__ src, __nv_bfloat16*
 }
 
 
-// The column split of B blocks read in place (no transposed copy): record (8 int64) [0] B
-// block offset (elements) [1] K (rows) [2] n (columns) [3] ldb [4] mode [5] dst offset (bf16)
-// [6] exponent offset [7] Kp. Column j is split as the row of length Kr (K, or 2K for the
-// complex modes 2 and 3: [re | -im] and [im | re] of B[:, j]) that yb_ozaki_split would
-// read from B^T, with the same digits and exponent, into [slice][column][Kp]. A CTA takes 32
-// columns: pass 1 finds their exponents (8 warps down the rows, coalesced along the
-// columns); pass 2 stages 64 x 32 tiles in shared memory and each warp writes 64-long digit
-// rows of 4 columns (128 contiguous bytes per slice).
-__device__ __forceinline__ long long col_elem(const long long* Bb, const int64_t* r, int64_t l, int64_t col) {
-  const int64_t K = r[1], ldb = r[3];
-  const int mode = (int)r[4];
-  if (mode == 0) return __ldg(Bb + r[0] + l * ldb + col);
-  const bool first = l < K;
-  const int64_t e = r[0] + (first ? l : l - K) * ldb + col;
-  const long long re = __ldg(Bb + 2 * e), im = __ldg(Bb + 2 * e + 1);
-  if (mode == 2) return first ? re : (long long)((unsigned long long)im ^ 0x8000000000000000ull);
-  return first ? im : re;  // mode 3
-}
-
-template <int S, int T>
-struct StorePair {
-  __device__ __forceinline__ static void run(uint32_t* d, int64_t ss, long long u0, long long u1) {
-    d[T * ss] = oz::pack_bf16(oz::digit_bits<S, T>(u0), oz::digit_bits<S, T>(u1));
-    StorePair<S, T + 1>::run(d, ss, u0, u1);
-  }
-};
-template <int S>
-struct StorePair<S, S> {
-  __device__ __forceinline__ static void run(uint32_t*, int64_t, long long, long long) {}
-};
-
-template <int S>
-__global__ void __launch_bounds__(256) split_cols_kernel(const double* __restrict__ src,
-                                                         __nv_bfloat16* __restrict__ slices, int* __restrict__ exps,
-                                                         const int64_t* __restrict__ recs) {
-  __shared__ long long tile[64][33];
-  __shared__ long long red[8][32];
-  __shared__ int ecol[32];
+// The same split written in the tensor-core tile layout of the tcgen05 GEMM: per slice, the
+// rows are grouped in tiles of TH (128 for A, 64 for B) and K in steps of 16; every
+// (row tile, K step) is one contiguous TH x 16 block in the canonical K-major layout of the
+// tcgen05 matrix descriptors (8-row x 16-byte core matrices: byte offset of (row r, k) is
+// (r/8)*256 + (k/8)*128 + (r%8)*16 + (k%8)*2), so a GEMM stage is a few bulk copies. Rows
+// from the operand's row count up to the next multiple of TH are written as zeros.
+__global__ void split_rows_tiled_kernel(const double* __restrict__ src, __nv_bfloat16* __restrict__ slices,
+                                        int* __restrict__ exps, const int64_t* __restrict__ recs, int s, int TH) {
   const int64_t* r = recs + (int64_t)blockIdx.y * 8;
-  const int64_t K = r[1], n = r[2], Kp = r[7];
-  const int64_t Kr = r[4] == 0 ? K : 2 * K;
-  const int64_t c0 = (int64_t)blockIdx.x * 32;
-  if (c0 >= n) return;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const long long* Bb = reinterpret_cast<const long long*>(src);
-  const int64_t col = c0 + lane;
+  const int64_t rows = r[1], K = r[2], Kp = r[7];
+  const int64_t rows_p = (rows + TH - 1) / TH * TH;
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= rows_p) return;
+  const bool live = row < rows;
+  const RowSrc a = row_src(src, r, live ? row : 0);
   long long mx = 0;
-  if (col < n)
-    for (int64_t l = warp; l < Kr; l += 8) mx = max(mx, col_elem(Bb, r, l, col) & 0x7fffffffffffffffll);
-  red[warp][lane] = mx;
-  __syncthreads();
-  if (warp == 0) {
-    for (int w = 1; w < 8; ++w) mx = max(mx, red[w][lane]);
-    const int e = oz::exponent_of(mx);
-    ecol[lane] = e;
-    if (col < n) exps[r[6] + col] = e;
-  }
-  const int64_t half_stride = n * Kp / 2;  // one slice, in BF16 pairs
-  for (int64_t k0 = 0; k0 < Kp; k0 += 64) {
-    __syncthreads();  // ecol is set; the previous tile has been consumed
-    for (int i = warp; i < 64; i += 8) {
-      const int64_t l = k0 + i;
-      tile[i][lane] = (col < n && l < Kr) ? col_elem(Bb, r, l, col) : 0ll;
-    }
-    __syncthreads();
+  if (live)
+    for (int64_t l = lane; l < K; l += 32) mx = max(mx, a(l) & 0x7fffffffffffffffll);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int cj = warp * 4 + q;  // tile column
-      const int64_t gc = c0 + cj;
-      if (gc >= n || k0 + 2 * lane >= Kp) continue;
-      const int e = ecol[cj];
-      const long long u0 = oz::digit_word<S>(tile[2 * lane][cj], e);
-      const long long u1 = oz::digit_word<S>(tile[2 * lane + 1][cj], e);
-      StorePair<S, 0>::run(reinterpret_cast<uint32_t*>(slices + r[5] + gc * Kp + k0 + 2 * lane), half_stride, u0, u1);
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  int e = 0;
+  if (mx >= (1ll << 52)) e = (int)(mx >> 52) - 1022;
+  else if (mx > 0) frexp(__longlong_as_double(mx), &e);
+  if (live && lane == 0) exps[r[6] + row] = e;
+  const int64_t slice_stride = rows_p * Kp;
+  const int64_t ksteps = Kp / 16;
+  __nv_bfloat16* base = slices + r[5] + (row / TH) * ksteps * (int64_t)TH * 16;
+  const int rr = (int)(row % TH);
+  const int64_t in_tile = (int64_t)(rr >> 3) * 128 + (rr & 7) * 8;  // elements
+  for (int64_t l = 2 * lane; l < Kp; l += 64) {
+    int d0[8], d1[8];
+    if (live && l < K) digits_of(a(l), e, s, d0); else for (int t = 0; t < 8; ++t) d0[t] = 0;
+    if (live && l + 1 < K) digits_of(a(l + 1), e, s, d1); else for (int t = 0; t < 8; ++t) d1[t] = 0;
+    const int64_t off = (l >> 4) * (int64_t)TH * 16 + in_tile + ((l & 15) >> 3) * 64 + (l & 7);
+    for (int t = 0; t < s; ++t) {
+      __nv_bfloat162 v;
+      v.x = __int2bfloat16_rn(d0[t]);
+      v.y = __int2bfloat16_rn(d1[t]);
+      *reinterpret_cast<__nv_bfloat162*>(base + t * slice_stride + off) = v;
     }
   }
 }
@@ -391,19 +357,15 @@ int yb_ozaki_split(const double* src, void* slices, int* exps, const int64_t* re
   return yb::check_launch();
 }
 
-int yb_ozaki_split_cols(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs, int max_cols,
-                        int slices_count, void* stream) {
-  if (n_recs == 0 || max_cols == 0) return YB_OK;
-  if (!src || !slices || !exps || !recs || n_recs < 0 || max_cols < 0) return YB_ERR_INVALID;
-  dim3 grid((unsigned)((max_cols + 31) / 32), (unsigned)n_recs);
-  cudaStream_t st = (cudaStream_t)stream;
-  __nv_bfloat16* sl = (__nv_bfloat16*)slices;
-  switch (slices_count) {
-    case 8: yb::split_cols_kernel<8><<<grid, 256, 0, st>>>(src, sl, exps, recs); break;
-    case 7: yb::split_cols_kernel<7><<<grid, 256, 0, st>>>(src, sl, exps, recs); break;
-    case 6: yb::split_cols_kernel<6><<<grid, 256, 0, st>>>(src, sl, exps, recs); break;
-    default: return YB_ERR_INVALID;
-  }
+int yb_ozaki_split_tiled(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs, int max_rows,
+                         int slices_count, int tile_rows, void* stream) {
+  if (n_recs == 0 || max_rows == 0) return YB_OK;
+  if (!src || !slices || !exps || !recs || slices_count < 1 || slices_count > 8) return YB_ERR_INVALID;
+  if (tile_rows != 64 && tile_rows != 128) return YB_ERR_INVALID;
+  const int rows_p = (max_rows + tile_rows - 1) / tile_rows * tile_rows;
+  dim3 grid((unsigned)((rows_p + 7) / 8), (unsigned)n_recs);
+  yb::split_rows_tiled_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(src, (__nv_bfloat16*)slices, exps, recs,
+                                                                       slices_count, tile_rows);
   return yb::check_launch();
 }
 

@@ -1,5 +1,5 @@
-// Helpers shared by the split-operand (Ozaki) emulated GEMM kernels: the integer digit
-// split of an FP64 value, exact integer-built conversions, and the tcgen05 / mbarrier
+// Helpers shared by the split-operand (Ozaki) emulated GEMM kernels: the scaled rounding of
+// the integer digit split, exact integer-built conversions, and the tcgen05 / mbarrier
 // primitives of the tensor-core kernel.
 #pragma once
 #include <cuda_bf16.h>
@@ -32,44 +32,6 @@ __device__ __forceinline__ long long scaled_rint(long long bits, int e, int s) {
     if (rem > half || (rem == half && (q & 1))) ++q;
   }
   return bits < 0 ? -q : q;
-}
-
-// U = Q + 64 (1 + 128 + ... + 128^{s-2}): the balanced base-128 digits of Q are
-// d_t = ((U >> 7(s-1-t)) & 127) - 64 for t >= 1 and d_0 = U >> 7(s-1) (arithmetic shift).
-template <int S>
-__device__ __forceinline__ long long digit_word(long long bits, int e) {
-  long long bias = 0;
-#pragma unroll
-  for (int t = 0; t < S - 1; ++t) bias = (bias << 7) | 64;
-  return scaled_rint(bits, e, S) + bias;
-}
-
-// Digit t of a digit word as an FP32 bit pattern whose upper 16 bits are the digit in BF16:
-// 2^23 + field is assembled in the mantissa and the offset is removed by one exact FP32
-// subtraction (|d| <= 128 has at most 8 significant bits, so the low 16 bits are zero).
-template <int S, int T>
-__device__ __forceinline__ uint32_t digit_bits(long long u) {
-  if (T == 0) {
-    const int d0 = (int)(u >> (7 * (S - 1)));  // in [-128, 128]
-    return __float_as_uint(__int_as_float(0x4B000000 + d0 + 128) - 8388736.0f);
-  } else {
-    const int f = (int)((u >> (7 * (S - 1 - T))) & 127);
-    return __float_as_uint(__int_as_float(0x4B000000 | f) - 8388672.0f);
-  }
-}
-
-// Two BF16 digits packed into one 32-bit word (a in the low half, at the lower address).
-__device__ __forceinline__ uint32_t pack_bf16(uint32_t a_bits, uint32_t b_bits) {
-  return __byte_perm(a_bits, b_bits, 0x7632);
-}
-
-// Row/column exponent e with max |a| = f 2^e, f in [0.5, 1), from the largest magnitude's
-// bit pattern (0 for an all-zero row).
-__device__ __forceinline__ int exponent_of(long long mx) {
-  int e = 0;
-  if (mx >= (1ll << 52)) e = (int)(mx >> 52) - 1022;
-  else if (mx > 0) frexp(__longlong_as_double(mx), &e);
-  return e;
 }
 
 // x 2^E by an exponent-field add when x and the result are normal doubles.

@@ -122,13 +122,9 @@ def transpose_backward(data_b, axes, meta_transpose):
 def run_gemm(plan, a, b, c, alpha=1.0, beta=0.0):
     code = _dtype_code(c.dtype)
     if len(plan.tiles):
-        do, dtm, dti, dsk = _dev(plan, 'gemm', (plan.outs, plan.terms, plan.tiles_main, plan.tiles_skinny), a.device)
-        if len(plan.tiles_main):
-            N.call('yb_grouped_gemm', _ptr(a), _ptr(b), _ptr(c), code, _ptr(do), _ptr(dtm), _ptr(dti),
-                   len(plan.tiles_main), float(alpha), float(beta), _stream())
-        if len(plan.tiles_skinny):
-            N.call('yb_grouped_gemm_skinny', _ptr(a), _ptr(b), _ptr(c), code, _ptr(do), _ptr(dtm), _ptr(dsk),
-                   len(plan.tiles_skinny), float(alpha), float(beta), _stream())
+        do, dtm, dti = _dev(plan, 'gemm', (plan.outs, plan.terms, plan.tiles), a.device)
+        N.call('yb_grouped_gemm', _ptr(a), _ptr(b), _ptr(c), code, _ptr(do), _ptr(dtm), _ptr(dti),
+               len(plan.tiles), float(alpha), float(beta), _stream())
     sp = plan.split
     if sp is not None:
         # split-K: chunk products into a workspace, then the ordered sum into C
@@ -150,14 +146,15 @@ def promote(A, B):
 def dot(A, B, meta_dot, Dsize):
     A, B = promote(_check(A, 'A'), _check(B, 'B'))
     plan = P.dot_plan(meta_dot)
-    out = torch.zeros(Dsize, dtype=A.dtype, device=A.device)
+    # every element is written by one sector when the sectors tile the output
+    out = (torch.empty if plan.covered == Dsize else torch.zeros)(Dsize, dtype=A.dtype, device=A.device)
     return run_gemm(plan, A, B, out)
 
 
 OZAKI_SLICES = 8  # 57 bits per operand: FP64-grade products
 
 
-OZAKI_TC = [None]  # emulated GEMM kernel: None = autotuned per dot, True = tcgen05 (split fused in), False = mma.sync
+OZAKI_TC = [None]  # emulated GEMM kernel: None = autotuned per dot, True = tcgen05/TMEM, False = mma.sync
 OZAKI_AUTOTUNE = [True]  # False: choose by the tile-padding estimate without timing
 
 
@@ -172,7 +169,7 @@ def dot_ozaki(A, B, meta_dot, Dsize, slices=OZAKI_SLICES):
     """
     A, B = promote(_check(A, 'A'), _check(B, 'B'))
     plan = P.ozaki_dot_plan(meta_dot, slices, A.is_complex())
-    out = torch.zeros(Dsize, dtype=A.dtype, device=A.device)
+    out = (torch.empty if plan.covered == Dsize else torch.zeros)(Dsize, dtype=A.dtype, device=A.device)
     run_gemm(plan.native, A, B, out)  # short (K < 16) and skinny sectors: native FP64
     if len(plan.tiles) == 0:
         return out
@@ -207,24 +204,27 @@ def _autotune_ozaki(plan, A, B, out, slices):
 def _ozaki_run(plan, A, B, out, slices, tc):
     dev = A.device
     st = _stream()
-    if tc:
-        # tcgen05 kernel with the split fused in: exponents, then one GEMM launch reading A and B
-        dea, deb, dout, dtl = _dev(plan, 'ozaki_fused', (plan.exp_a, plan.exp_b, plan.outs_f, plan.tiles_f), dev)
-        ex = torch.empty(max(plan.n_exps, 1), dtype=torch.int32, device=dev)
-        N.call('yb_ozaki_exponents', _ptr(A), _ptr(ex), _ptr(dea), len(plan.exp_a), plan.exp_a_max, 0, st)
-        N.call('yb_ozaki_exponents', _ptr(B), _ptr(ex), _ptr(deb), len(plan.exp_b), plan.exp_b_max, 1, st)
-        N.call('yb_ozaki_gemm_fused', _ptr(A), _ptr(B), _ptr(ex), _ptr(out), _ptr(dout), _ptr(dtl),
-               len(plan.tiles_f), slices, st)
-        return
-    dar, dbc, dout, dtl = _dev(plan, 'ozaki', (plan.a_recs, plan.b_cols, plan.outs, plan.tiles), dev)
-    a_sl = torch.empty(plan.a_size, dtype=torch.bfloat16, device=dev)
-    b_sl = torch.empty(plan.b_size, dtype=torch.bfloat16, device=dev)
+    bT = run_copy(plan.bT, B, torch.empty(max(plan.bT_size, 1), dtype=B.dtype, device=dev))
     a_ex = torch.empty(max(plan.a_exps, 1), dtype=torch.int32, device=dev)
     b_ex = torch.empty(max(plan.b_exps, 1), dtype=torch.int32, device=dev)
+    if tc:
+        # digit planes in the tile layout of the tcgen05 kernel, then the tensor-core GEMM
+        dar, dbr, dout, dtl = _dev(plan, 'ozaki_tc', (plan.a_recs_tc, plan.b_recs_tc, plan.outs_tc, plan.tiles_tc),
+                                   dev)
+        a_sl = torch.empty(plan.a_size_tc, dtype=torch.bfloat16, device=dev)
+        b_sl = torch.empty(plan.b_size_tc, dtype=torch.bfloat16, device=dev)
+        N.call('yb_ozaki_split_tiled', _ptr(A), _ptr(a_sl), _ptr(a_ex), _ptr(dar), len(plan.a_recs), plan.a_rows,
+               slices, P.OZAKI_TC_M, st)
+        N.call('yb_ozaki_split_tiled', _ptr(bT), _ptr(b_sl), _ptr(b_ex), _ptr(dbr), len(plan.b_recs), plan.b_rows,
+               slices, P.OZAKI_TC_N, st)
+        N.call('yb_ozaki_gemm_tc', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
+               len(plan.tiles_tc), slices, st)
+        return
+    dar, dbr, dout, dtl = _dev(plan, 'ozaki', (plan.a_recs, plan.b_recs, plan.outs, plan.tiles), dev)
+    a_sl = torch.empty(plan.a_size, dtype=torch.bfloat16, device=dev)
+    b_sl = torch.empty(plan.b_size, dtype=torch.bfloat16, device=dev)
     N.call('yb_ozaki_split', _ptr(A), _ptr(a_sl), _ptr(a_ex), _ptr(dar), len(plan.a_recs), plan.a_rows, slices, st)
-    # B's columns split in place (the digits of B^T's rows without a transposed copy)
-    N.call('yb_ozaki_split_cols', _ptr(B), _ptr(b_sl), _ptr(b_ex), _ptr(dbc), len(plan.b_cols), plan.b_cols_max,
-           slices, st)
+    N.call('yb_ozaki_split', _ptr(bT), _ptr(b_sl), _ptr(b_ex), _ptr(dbr), len(plan.b_recs), plan.b_rows, slices, st)
     N.call('yb_ozaki_gemm', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
            len(plan.tiles), slices, st)
 
