@@ -1,7 +1,8 @@
 """The benchmark's reference arm on the host cores (no GPU): one JSON line with the keys of
-the benchmark contract, for the default workload (DMRG Heff2 Lanczos), the tensordot
-workload and the CTMRG workload (its per-move checkpointed replay on the plain per-block
-torch path)."""
+the benchmark contract, for the default workload (DMRG Heff2 Lanczos: the reference package
+itself when it is installed under baseline/_ref, else the oracle's restatement), the
+tensordot workload and the CTMRG workload (its per-move checkpointed replay on the plain
+per-block torch path)."""
 import json
 import os
 import subprocess
@@ -36,6 +37,8 @@ def test_reference_arm_line(args):
     assert line["value"] > 0 and line["e2e"]["value"] == line["value"]
     assert line["cpu_baseline"]["value"] == line["value"] and line["cpu_baseline"]["cores"] >= 1
     assert isinstance(line["config"]["workload"], str)
+    if '--workload' not in args:  # the DMRG workload: YASTN's eigs (or its restatement) reproduces the recording
+        assert line["config"]["lowest_ritz_rel_err_vs_recorded"] <= 1e-10
     if '--workload' in args and args[args.index('--workload') + 1] == 'cfg4':
         assert line["unit"] == "ms" and line["higher_is_better"] is False
         assert line["config"]["energy_rel_err_vs_reference"] <= 1e-12
