@@ -75,6 +75,8 @@ def parse():
                    help='cfg2: run only the headline GEMM mode (for kernel launch lists); the emulated kernel of '
                         'each dot is chosen by its padded tile work rather than by timing, so that a profiler '
                         'slowing the kernels unequally does not change the choice')
+    p.add_argument('--ozaki-kernel', default='auto', choices=['auto', 'tcgen05', 'mma'],
+                   help='emulated sector GEMM kernel: chosen per dot (auto), or forced (for kernel profiles)')
     return p.parse_args()
 
 
@@ -804,6 +806,9 @@ def run_gpu_cfg2(args, wl):
         modes = [args.gemm]
         from yastn_gb300 import ops
         ops.OZAKI_AUTOTUNE[0] = False
+    if args.ozaki_kernel != 'auto':
+        from yastn_gb300 import ops
+        ops.OZAKI_TC[0] = args.ozaki_kernel == 'tcgen05'
     for mode in modes:
         BK.set_gemm_mode(mode)
         v0 = h_v0.to(dev)

@@ -103,7 +103,9 @@ int yb_block_copy(const void* src, void* dst, int unit_bytes,
  * tiles: n_tiles records of 4 int32: (output, tile row, tile col, kind), ordered by the
  *   host (largest work first). kind 0: a 64x64 tile; kind 1: a skinny tile covering all
  *   m <= 16 rows and columns [w*col, w*col + w) with w = 1024 for m <= 8, 256 above (tile
- *   row 0; the host's plans use skinny tiles for m <= 8).
+ *   row 0; the host's plans use skinny tiles for m <= 8); kind 2: a short skinny tile, for an
+ *   output of one term with m <= 8 rows and K <= 8 (any n), covering all rows and the 512
+ *   columns [512*col, 512*col + 512).
  * dtype: YB_F64 or YB_C128 (alpha, beta are real).
  * Replaces dot (one term per output), transpose_dot_sum after the merge of its operands,
  * and the adjoint products A_b += C_b B^H, B_b += A^H C_b (terms grouped by operand block).
@@ -112,9 +114,16 @@ int yb_block_copy(const void* src, void* dst, int unit_bytes,
 #define YB_GEMM_TERM_REC 8
 #define YB_GEMM_TILE 64
 #define YB_GEMM_SKINNY_COLS 1024
+#define YB_GEMM_SHORT_COLS 512
 int yb_grouped_gemm(const void* a, const void* b, void* c, int dtype,
                     const int64_t* outs, const int64_t* terms, const int32_t* tiles, int n_tiles,
                     double alpha, double beta, void* stream);
+/* yb_grouped_gemm_short: yb_grouped_gemm for plans whose tiles are all of kind 2 (the
+ * contractions of a tensor with a small MPO block): a kernel of its own with few registers,
+ * several CTAs per SM, all loads of a thread's columns issued before its FMAs. */
+int yb_grouped_gemm_short(const void* a, const void* b, void* c, int dtype,
+                          const int64_t* outs, const int64_t* terms, const int32_t* tiles, int n_tiles,
+                          double alpha, double beta, void* stream);
 /* yb_gemm_reduce: the second pass of a split-K product. The host splits the K range of
  * outputs whose few tiles would leave most SMs idle into chunks, computes each chunk's
  * product into its own slot of a workspace P (yb_grouped_gemm with alpha 1, beta 0), then
@@ -128,15 +137,24 @@ int yb_gemm_reduce(void* c, const void* p, int dtype, const int64_t* recs, const
                    int n_tasks, double alpha, double beta, void* stream);
 
 /* ==== family (b'): FP64 sector GEMMs emulated on BF16 tensor cores (split operands) ====
- * yb_ozaki_split: every row of each record (K contiguous entries) is scaled by 2^-e
- * (|entries| < 1, e stored as int32) and written as slices_count balanced base-128
- * digits (|d_0| <= 128, d_t in [-64, 63]) with weights 2^{-7(t+1)}, stored exactly as
- * BF16 in planes [slice][row][Kp]. The host splits A blocks directly (their rows) and B
- * blocks after transposing them with yb_block_copy (their columns).
- * recs: n_recs records of 8 int64: [0] source offset [1] rows [2] K [3] row stride
- *   [4] 1 (column stride) [5] destination offset (BF16 elements, multiple of 16)
- *   [6] exponent offset [7] Kp = K rounded up to 16 (padding zeroed).
- *   max_rows: largest rows over records.
+ * yb_ozaki_split: every row of each record is scaled by 2^-e (|entries| < 1, e stored as
+ * int32) and written as slices_count (6, 7 or 8) balanced base-128 digits (|d_0| <= 128,
+ * d_t in [-64, 63]) with weights 2^{-7(t+1)}, stored exactly as BF16. A rows are A's block
+ * rows; B rows are B's block columns, read in place (no transposed copy). One launch splits
+ * both operands of a dot.
+ * recs: YB_OZ_SPLIT_REC int64 per record: [0] source offset [1] rows [2] K (real row length;
+ *   2x the complex length for modes 1-3) [3] row stride [4] mode (0 real; 1, 2, 3: complex
+ *   rows read as [re | im], [re | -im], [im | re]) [5] destination offset (BF16 elements,
+ *   multiple of 16) [6] exponent offset [7] Kp = K rounded up to 16 (padding zeroed)
+ *   [8] stride between consecutive k [9] operand (bit 0: 0 reads a_src and writes
+ *   a_slices / a_exps, 1 the b_ ones) | tile rows << 8 (0: planes [slice][row][Kp] for
+ *   yb_ozaki_gemm; 64 or 128: the tile layout of yb_ozaki_gemm_tc, rows padded with zeros
+ *   to a multiple of the tile rows, per slice blocks of tile rows x 16 ordered (row tile,
+ *   K step), each in the canonical K-major core-matrix order: byte offset of (row r, k) in a
+ *   block (r/8)*256 + (k/8)*128 + (r%8)*16 + (k%8)*2).
+ *   Element k of row i is at source offset [0] + i*[3] + k*[8] (FP64 or complex elements).
+ * groups: int32 pairs (record, first row) of 8-row groups covering each record's rows
+ *   (padded rows included for the tile layout), one CTA each.
  * yb_ozaki_gemm: C = A B for every output record (16 int64): [0] c offset [1] m [2] n
  *   [3] ldc [4] A slices offset [5] A exponents offset [6] B slices offset
  *   [7] B exponents offset [8] K [9] Kp; tiles as for yb_grouped_gemm (64 x 64).
@@ -146,27 +164,22 @@ int yb_gemm_reduce(void* c, const void* p, int dtype, const int64_t* recs, const
  * Replaces dot (backend_torch.py:549-550) for real FP64 operands when the emulated path
  * is selected; the native yb_grouped_gemm stays the default.
  */
-int yb_ozaki_split(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs,
-                   int max_rows, int slices_count, void* stream);
+#define YB_OZ_SPLIT_REC 10
+int yb_ozaki_split(const double* a_src, const double* b_src, void* a_slices, void* b_slices,
+                   int* a_exps, int* b_exps, const int64_t* recs, const int32_t* groups, int n_groups,
+                   int slices_count, void* stream);
 int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps,
                   double* c, const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
                   void* stream);
-/* yb_ozaki_split_tiled: yb_ozaki_split writing the digit planes in the tile layout of
- * yb_ozaki_gemm_tc: per slice, tile_rows (128 for A, 64 for B) x 16 blocks, each in the
- * canonical K-major core-matrix order (byte offset of (row r, k) in a block:
- * (r/8)*256 + (k/8)*128 + (r%8)*16 + (k%8)*2), blocks ordered (row tile, K step); the
- * rows are padded with zeros to a multiple of tile_rows (record [5] = slice-0 offset, slice
- * stride = padded rows x Kp). */
-int yb_ozaki_split_tiled(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs,
-                         int max_rows, int slices_count, int tile_rows, void* stream);
 /* yb_ozaki_gemm_tc: yb_ozaki_gemm on the tcgen05 tensor cores, operands from
- * yb_ozaki_split_tiled (output records [4], [6] = the A / B slice-0 offsets in the tile
- * layout); tiles are (output, tile row, tile col, 0) of 128 rows x 64 columns, one CTA each,
- * whose warps split the work: one streams the digit tiles (cp.async.bulk into a 4-stage
- * ring), one issues the tcgen05.mma into the digit-diagonal accumulators in tensor memory,
- * four fold the accumulators exactly and write the tile (the same bits as yb_ozaki_gemm).
- * A CTA that gives up on a bounded wait writes nothing for its tile and sets the status word
- * read by yb_ozaki_device_error. */
+ * yb_ozaki_split in the tile layout (128 rows for A, 64 for B; output records [4], [6] = the
+ * A / B slice-0 offsets in that layout); tiles are (output, tile row, tile col, 0) of 128 rows
+ * x 64 columns. A persistent kernel, one CTA per SM, each walking its share of the tiles:
+ * one warp streams the digit tiles (cp.async.bulk into a 4-stage ring), one issues the
+ * tcgen05.mma into the digit-diagonal accumulators in tensor memory, sixteen fold the
+ * accumulators exactly and write the tile (the same bits as yb_ozaki_gemm) while the next
+ * tile's MMAs run. A CTA that gives up on a bounded wait stops writing and sets the status
+ * word read by yb_ozaki_device_error. */
 int yb_ozaki_gemm_tc(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps,
                      double* c, const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
                      void* stream);
@@ -175,24 +188,23 @@ int yb_ozaki_gemm_tc(const void* a_slices, const int* a_exps, const void* b_slic
 int yb_ozaki_device_error(int* out, int reset, void* stream);
 
 /* yb_ozaki_dot_static: a whole emulated dot in one call -- the native FP64 sectors
- * (yb_grouped_gemm), yb_ozaki_split (A), yb_block_copy + yb_ozaki_split (B) and
- * yb_ozaki_gemm -- with all scratch (digit planes, exponents, transposed B) placed in a
- * device array built into the library instead of caller-provided memory.
+ * (yb_grouped_gemm), yb_ozaki_split (A and B) and yb_ozaki_gemm -- with all scratch
+ * (digit planes and exponents) placed in a device array built into the library instead of
+ * caller-provided memory.
  * No counterpart in the reference: it exists for callers that cannot allocate device
  * memory at call time (a host framework that owns the whole device memory budget and
  * forbids allocations after start-up, or a caller for which an allocation would
  * synchronise the device in the middle of its stream work). The caller still provides
- * A, B, C and the plan records, laid out as for the separate calls: b_recs refer to the
- * transposed copy of B (offsets from 0), bT_tasks/bT_items are the yb_block_copy plan of
- * B's blocks into those transposes in 8-byte units (no YB_CP_VEC tasks). The sectors the
- * emulation does not take (K < 16, or at most 8 rows and more than 64 columns) come as
- * yb_grouped_gemm records (nat_outs, nat_terms, nat_tiles; alpha 1, beta 0) and must be a
- * direct plan without split-K, whose chunk workspace this call does not hold.
+ * A, B, C and the plan records, laid out as for the separate calls (split records in the
+ * planes layout, tile rows 0). The sectors the emulation does not take (K < 16, or at most
+ * 8 rows and more than 64 columns) come as yb_grouped_gemm records (nat_outs, nat_terms,
+ * nat_tiles; alpha 1, beta 0) and must be a direct plan without split-K, whose chunk
+ * workspace this call does not hold.
  * Limits and behaviour:
  *   - real FP64 only: dtype must be YB_F64 (YB_C128 returns YB_ERR_INVALID);
  *   - the scratch holds YB_STATIC_SCRATCH_BYTES; the call returns YB_ERR_TOO_LARGE when
- *     2*(a_slice_elems + b_slice_elems) + 8*bT_elems + 4*(a_exp_count + b_exp_count)
- *     bytes (each region rounded up to 256 bytes) exceed it;
+ *     2*(a_slice_elems + b_slice_elems) + 4*(a_exp_count + b_exp_count) bytes (each
+ *     region rounded up to 256 bytes) exceed it;
  *   - it allocates nothing; the first call on a device resolves the array's device
  *     address (cudaGetSymbolAddress, with that device current) and caches it, so that
  *     first call should come before any stream capture;
@@ -201,14 +213,12 @@ int yb_ozaki_device_error(int* out, int reset, void* stream);
  *   - C positions not covered by an output record are left untouched (zero them first). */
 #define YB_STATIC_SCRATCH_BYTES (16u << 20)
 int yb_ozaki_dot_static(const double* A, const double* B, double* C, int dtype,
-                        const int64_t* a_recs, int n_a, int a_rows,
-                        const int64_t* b_recs, int n_b, int b_rows,
-                        const int64_t* bT_tasks, int n_bT_tasks, const int64_t* bT_items, int n_bT_items,
+                        const int64_t* split_recs, const int32_t* split_groups, int n_groups,
                         const int64_t* outs, const int32_t* tiles, int n_tiles,
                         const int64_t* nat_outs, const int64_t* nat_terms, const int32_t* nat_tiles,
                         int n_nat_tiles, int slices_count,
                         int64_t a_slice_elems, int64_t b_slice_elems, int64_t a_exp_count,
-                        int64_t b_exp_count, int64_t bT_elems, void* stream);
+                        int64_t b_exp_count, void* stream);
 
 /* ==== device-resident Lanczos (yastn/tensor/_krylov.py:17-46, yastn/krylov/_krylov.py:177-238;
  * the backend's vdot / add / norm, backend_np.py:553-577) ======================================

@@ -104,6 +104,9 @@ def _run_outs(outs, terms, tiles, a, b, c, alpha, beta):
             assert m <= 16, "skinny tiles take at most 16 rows"
             w = P.skinny_cols(m)
             want = {(0, j, 1) for j in range((n + w - 1) // w)}
+        elif any(kd == 2 for _, _, kd in seen.get(oi, ())):  # short skinny: m <= 8, one term, K <= 8
+            assert m <= 8 and t1 - t0 == 1 and int(plan.terms[t0][2]) <= 8, "short tiles: m <= 8, one term, K <= 8"
+            want = {(0, j, 2) for j in range((n + 511) // 512)}
         else:
             want = {(i, j, 0) for i in range((m + 63) // 64) for j in range((n + 63) // 64)}
         assert seen.get(oi, set()) == want, "tiles do not cover the output"
@@ -402,3 +405,73 @@ def qr_plain(work, blocks, data, Q, R):
         Q[int(r[3]):int(r[3]) + m * k] = (Qt.T * sg[None, :]).ravel()
         Rb = R[int(r[5]):int(r[5]) + k * n].reshape(k, n)
         Rb[:, :k] = sg[:, None] * RR
+
+
+def split_rows(src, rec):
+    """The real rows yb_ozaki_split reads for one record: element k of row i at source
+    offset rec[0] + i*rec[3] + k*rec[8] (FP64 or complex elements by the mode rec[4])."""
+    s0, rows, K, rs, mode = (int(x) for x in rec[:5])
+    ks = int(rec[8])
+    if mode == 0:
+        return np.stack([src[s0 + r * rs + ks * np.arange(K)] for r in range(rows)]).reshape(rows, K)
+    half = K // 2
+    out = []
+    for r in range(rows):
+        z = src[s0 + r * rs + ks * np.arange(half)]
+        out.append({1: np.concatenate([z.real, z.imag]), 2: np.concatenate([z.real, -z.imag]),
+                    3: np.concatenate([z.imag, z.real])}[mode])
+    return np.stack(out).reshape(rows, K)
+
+
+def ozaki_digits(x, s):
+    """Row exponents e (max |x| = f 2^e, f in [0.5, 1); 0 for a zero row) and the s balanced
+    base-128 digits of rint(x 2^{7s-e}) (round half to even): d_0 in [-128, 128], d_t in
+    [-64, 63], x 2^-e = sum_t d_t 2^{-7(t+1)} + rounding. Returns (e, digits[s, rows, K])."""
+    x = np.asarray(x, dtype=np.float64)
+    mx = np.abs(x).max(axis=1) if x.shape[1] else np.zeros(x.shape[0])
+    e = np.where(mx > 0, np.frexp(mx)[1], 0).astype(np.int64)
+    q = np.rint(np.ldexp(x, (7 * s - e)[:, None])).astype(np.int64)
+    bias = 0
+    for _ in range(s - 1):
+        bias = (bias << 7) | 64
+    u = q + bias
+    d = np.empty((s,) + x.shape, dtype=np.int64)
+    d[0] = u >> (7 * (s - 1))
+    for t in range(1, s):
+        d[t] = ((u >> (7 * (s - 1 - t))) & 127) - 64
+    return e, d
+
+
+def ozaki_split(recs, groups, a_src, b_src, s, sizes, n_exps):
+    """yb_ozaki_split: digit planes (as integers) and row exponents of both operands in the
+    records' layouts. sizes / n_exps: (A, B) lengths of the digit and exponent arrays."""
+    dig = [np.zeros(sizes[0], dtype=np.int64), np.zeros(sizes[1], dtype=np.int64)]
+    exps = [np.zeros(n_exps[0], dtype=np.int64), np.zeros(n_exps[1], dtype=np.int64)]
+    touched = [np.zeros(sizes[0], dtype=bool), np.zeros(sizes[1], dtype=bool)]
+    grouped = {}
+    for ri, first in groups:
+        grouped.setdefault(int(ri), []).append(int(first))
+    for ri, rec in enumerate(recs):
+        op, th = int(rec[9]) & 1, int(rec[9]) >> 8
+        rows, K, Kp, dst, eo = int(rec[1]), int(rec[2]), int(rec[7]), int(rec[5]), int(rec[6])
+        rows_p = -(-rows // th) * th if th else rows
+        assert sorted(grouped.get(ri, [])) == list(range(0, rows_p, P.OZ_SPLIT_ROWS)), "groups do not cover the rows"
+        x = split_rows(b_src if op else a_src, rec)
+        e, d = ozaki_digits(x, s)
+        exps[op][eo:eo + rows] = e
+        full = np.zeros((s, rows_p, Kp), dtype=np.int64)
+        full[:, :rows, :K] = d[:, :, :]
+        full[:, :rows, K:] = 0
+        r = np.arange(rows_p)[:, None]
+        k = np.arange(Kp)[None, :]
+        if th == 0:
+            off = r * Kp + k
+        else:
+            off = (r // th) * (Kp // 16) * th * 16 + (k // 16) * th * 16 + ((r % th) // 8) * 128 + \
+                ((k % 16) // 8) * 64 + (r % 8) * 8 + k % 8
+        for t in range(s):
+            idx = dst + t * rows_p * Kp + off
+            assert not touched[op][idx].any(), "records overlap"
+            touched[op][idx] = True
+            dig[op][idx] = full[t]
+    return dig, exps

@@ -273,3 +273,52 @@ def test_ozaki_tcgen05_matches_mma_sync(name, cuda_device):
     np.testing.assert_array_equal(got_tc, got_mma)
     ref = oracle.dot(A, B, meta, Dsize)
     assert rel(got_tc, ref) <= TOL
+
+
+@pytest.mark.parametrize('cplx', [False, True])
+@pytest.mark.parametrize('slices', [6, 7, 8])
+def test_ozaki_split_matches_digit_model(cplx, slices, cuda_device):
+    """yb_ozaki_split in both layouts (digit planes and the tcgen05 tile layout), A by rows
+    and B by columns in place, against the NumPy digit model bit for bit: every BF16 digit
+    (padding zeros included) and every row exponent. The data spans many binades, with a
+    zero row, a subnormal row and exact ties of the last digit."""
+    import ctypes
+    from yastn_gb300 import _native as N
+    from yastn_gb300 import _plans as P
+    import plan_interp as PI
+    rng = np.random.default_rng(31 + slices + 10 * cplx)
+    shapes = [(40, 30, 20), (16, 16, 17), (130, 20, 70), (6, 300, 200), (33, 17, 65), (20, 130, 129)]
+    meta, oa, ob, oc = [], 0, 0, 0
+    for m, k, n in shapes:
+        meta.append(((oc, oc + m * n), (m, n), (oa, oa + m * k), (m, k), (ob, ob + k * n), (k, n)))
+        oa += m * k; ob += k * n; oc += m * n
+    meta = tuple(meta)
+    A = rng.normal(size=oa) * np.exp(rng.normal(size=oa) * 4)
+    B = rng.normal(size=ob) * np.exp(rng.normal(size=ob) * 4)
+    A[:30] = 0.0                                   # the first row of the first block
+    A[30:60] = rng.normal(size=30) * 1e-310        # a subnormal row
+    # exact ties of the last digit: row maximum 1 (e = 1), the rest (2j + 1) 2^{-7s}
+    A[60] = 1.0
+    A[61:90] = (2.0 * rng.integers(0, 2 ** 30, size=29) + 1.0) * 2.0 ** (-7 * slices) * rng.choice([-1, 1], 29)
+    if cplx:
+        A = A + 1j * rng.normal(size=oa)
+        B = B + 1j * rng.normal(size=ob)
+    plan = P.ozaki_dot_plan(meta, slices, cplx)
+    dA, dB = dev(A), dev(B)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for recs, groups, sizes in ((plan.split_recs, plan.split_groups, (plan.a_size, plan.b_size)),
+                                (plan.split_recs_tc, plan.split_groups_tc, (plan.a_size_tc, plan.b_size_tc))):
+        want, want_e = PI.ozaki_split(recs, groups, A, B, slices, sizes, (plan.a_exps, plan.b_exps))
+        a_sl = torch.full((sizes[0],), 7.0, dtype=torch.bfloat16, device='cuda')  # nonzero: padding must be written
+        b_sl = torch.full((sizes[1],), 7.0, dtype=torch.bfloat16, device='cuda')
+        a_ex = torch.zeros(plan.a_exps, dtype=torch.int32, device='cuda')
+        b_ex = torch.zeros(plan.b_exps, dtype=torch.int32, device='cuda')
+        drec, dgrp = dev(recs), dev(groups)
+        N.call('yb_ozaki_split', ctypes.c_void_p(dA.data_ptr()), ctypes.c_void_p(dB.data_ptr()),
+               ctypes.c_void_p(a_sl.data_ptr()), ctypes.c_void_p(b_sl.data_ptr()), ctypes.c_void_p(a_ex.data_ptr()),
+               ctypes.c_void_p(b_ex.data_ptr()), ctypes.c_void_p(drec.data_ptr()), ctypes.c_void_p(dgrp.data_ptr()),
+               len(groups), slices, st)
+        torch.cuda.synchronize()
+        for got, got_e, w, we in ((a_sl, a_ex, want[0], want_e[0]), (b_sl, b_ex, want[1], want_e[1])):
+            np.testing.assert_array_equal(host(got.float()).astype(np.int64), w)
+            np.testing.assert_array_equal(host(got_e).astype(np.int64), we)

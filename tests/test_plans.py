@@ -165,6 +165,29 @@ def test_skinny_tile_kinds_cover_and_reproduce():
     P.CACHE.by_id.clear(); P.CACHE.by_val.clear()
 
 
+def test_short_skinny_tiles_cover_and_reproduce():
+    """Outputs of one term with at most 8 rows and K <= 8 (the contractions with a small MPO
+    block) take short skinny tiles of 512 columns; a plan made
+    of them alone runs on the short kernel (all_short). Coverage and values, real and
+    complex; the Heff2 workload's two MPO contractions are such plans."""
+    shapes = [(3, 4, 1500), (1, 1, 65), (8, 8, 513), (2, 3, 4000), (2, 4, 7)]
+    meta, oa, ob, oc = _meta_dot(shapes)
+    plan = P.dot_plan(meta)
+    assert set(int(t[3]) for t in plan.tiles) == {2} and plan.all_short
+    mixed = P.dot_plan(_meta_dot(shapes + [(3, 9, 300), (64, 64, 64)])[0])
+    assert set(int(t[3]) for t in mixed.tiles) == {0, 1, 2} and not mixed.all_short
+    rng = np.random.default_rng(9)
+    for cplx in (False, True):
+        f = lambda n: rng.normal(size=n) + (1j * rng.normal(size=n) if cplx else 0)
+        A, B = f(oa), f(ob)
+        out = PI.run_gemm(plan, A, B, np.zeros(oc, dtype=A.dtype))
+        ref = oracle.dot(A, B, meta, oc)
+        assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
+    from yastn_gb300.workloads import Heff2Workload
+    dots = [c['args'][2] for c in Heff2Workload().calls if c['fn'] == 'dot']
+    assert [P.dot_plan(m).all_short for m in dots] == [False, True, True, False]
+
+
 def test_split_k_not_used_when_tiles_fill_the_gpu():
     meta, *_ = _meta_dot([(64, 4096, 64)] * 400)
     assert P.dot_plan(meta).split is None
@@ -549,17 +572,24 @@ def test_mixed_precision_jacobi_schedule_complex():
 
 
 def _split_rows_view(src, rec):
-    """The real rows the split kernels read for one record (modes of csrc/yb_ozaki.cu)."""
+    """The real rows yb_ozaki_split reads for one record: element k of row i at source
+    offset rec[0] + i*rec[3] + k*rec[8] (FP64 or complex elements by mode)."""
     s0, rows, K, rs, mode = (int(x) for x in rec[:5])
+    ks = int(rec[8])
     if mode == 0:
-        return np.stack([src[s0 + r * rs: s0 + r * rs + K] for r in range(rows)])
+        return np.stack([src[s0 + r * rs + ks * np.arange(K)] for r in range(rows)])
     half = K // 2
     out = []
     for r in range(rows):
-        z = src[s0 + r * rs: s0 + r * rs + half]
+        z = src[s0 + r * rs + ks * np.arange(half)]
         out.append({1: np.concatenate([z.real, z.imag]), 2: np.concatenate([z.real, -z.imag]),
                     3: np.concatenate([z.imag, z.real])}[mode])
     return np.stack(out)
+
+
+def _recs_of(plan, op, tc=False):
+    recs = plan.split_recs_tc if tc else plan.split_recs
+    return recs[(recs[:, 9] & 1) == op]
 
 
 def test_ozaki_complex_plan_reproduces_complex_products():
@@ -576,12 +606,10 @@ def test_ozaki_complex_plan_reproduces_complex_products():
     B = rng.normal(size=ob) + 1j * rng.normal(size=ob)
     plan = P.ozaki_dot_plan(meta, 8, True)
     assert len(plan.outs) == 2 * 3 and len(plan.native.outs) == 1       # (3, 8, 100) is short: native
-    assert sorted(set(int(r[4]) for r in plan.a_recs)) == [1]
-    assert sorted(int(r[4]) for r in plan.b_recs) == [2, 2, 2, 3, 3, 3]
-    tasks, items = plan.bT.packed(False)
-    bT = PI.run_copy(tasks, items, B, np.zeros(plan.bT_size, dtype=complex))
-    a_rows = {int(r[5]): _split_rows_view(A, r) for r in plan.a_recs}
-    b_rows = {int(r[5]): _split_rows_view(bT, r) for r in plan.b_recs}
+    assert sorted(set(int(r[4]) for r in _recs_of(plan, 0))) == [1]
+    assert sorted(int(r[4]) for r in _recs_of(plan, 1)) == [2, 2, 2, 3, 3, 3]
+    a_rows = {int(r[5]): _split_rows_view(A, r) for r in _recs_of(plan, 0)}
+    b_rows = {int(r[5]): _split_rows_view(B, r) for r in _recs_of(plan, 1)}  # B's columns, in place
     Cd = np.zeros(2 * oc)
     for o in plan.outs:
         c_off, m, n, ldc, ao, _, bo, _, Kr, Kp, cs = (int(x) for x in o[:11])
@@ -727,16 +755,20 @@ def test_ozaki_plan_records():
     # short contractions (K < 16) and skinny outputs (m <= 8 < 64 < n) go to the native
     # kernel, the rest (small m or n included) are split
     assert len(plan.outs) == 4 and len(plan.native.outs) == 2
-    assert len({tuple(r[:1]) for r in plan.a_recs}) == len(plan.a_recs)  # each A block split once
-    assert all(r[7] % 16 == 0 and r[7] >= r[2] for r in plan.a_recs)
-    assert all(int(r[5]) % 16 == 0 for r in plan.a_recs) and all(int(r[5]) % 16 == 0 for r in plan.b_recs)
-    # B blocks are split from their transposes: the copy plan reproduces B^T block by block
-    tasks, items = plan.bT.packed(False)
-    bT = PI.run_copy(tasks, items, B, np.zeros(plan.bT_size))
+    a_recs, b_recs = _recs_of(plan, 0), _recs_of(plan, 1)
+    assert len({tuple(r[:1]) for r in a_recs}) == len(a_recs)  # each A block split once
+    assert all(r[7] % 16 == 0 and r[7] >= r[2] for r in plan.split_recs)
+    assert all(int(r[5]) % 16 == 0 for r in plan.split_recs)
     big = [mt for mt in meta if mt[3][1] >= 16 and not (mt[3][0] <= 8 and mt[5][1] > 64)]
-    for rec, (slc, Dc, sla, Da, slb, Db) in zip(plan.b_recs, big):
-        n, K = int(rec[1]), int(rec[2])
-        np.testing.assert_array_equal(bT[rec[0]:rec[0] + n * K].reshape(n, K), B[slb[0]:slb[1]].reshape(Db).T)
+    for rec, (slc, Dc, sla, Da, slb, Db) in zip(a_recs, big):
+        np.testing.assert_array_equal(_split_rows_view(A, rec), A[sla[0]:sla[1]].reshape(Da))
+    # B blocks are split by columns read in place: the rows of B^T
+    for rec, (slc, Dc, sla, Da, slb, Db) in zip(b_recs, big):
+        np.testing.assert_array_equal(_split_rows_view(B, rec), B[slb[0]:slb[1]].reshape(Db).T)
+    # 8-row groups cover every record's rows once
+    cover = sorted((int(g[0]), int(g[1]) + i) for g in plan.split_groups for i in range(P.OZ_SPLIT_ROWS)
+                   if int(g[1]) + i < int(plan.split_recs[int(g[0])][1]))
+    assert cover == [(ri, i) for ri, r in enumerate(plan.split_recs) for i in range(int(r[1]))]
     # the native part reproduces its sector
     out = PI.run_gemm(plan.native, A, B, np.zeros(oc))
     for slc, Dc, sla, Da, slb, Db in meta[4:]:
@@ -746,9 +778,9 @@ def test_ozaki_plan_records():
 
 def test_ozaki_tiled_records_and_tiles():
     """Records of the tcgen05 kernel: every operand block gets s * ceil(rows / tile) * tile * Kp
-    digits in the tile layout (128 rows for A, 64 for B^T rows), without overlap and in block
-    order; the output records point at the remapped blocks; tiles cover every output once by
-    decreasing K."""
+    digits in the tile layout (128 rows for A, 64 for B's columns), without overlap and in
+    block order; the 8-row groups cover the padded rows; the output records point at the
+    remapped blocks; tiles cover every output once by decreasing K."""
     rng = np.random.default_rng(23)
     shapes = [(40, 30, 20), (16, 16, 17), (130, 20, 70), (5, 40, 9), (3, 8, 100), (6, 300, 200)]
     meta, oa, ob, oc = [], 0, 0, 0
@@ -758,16 +790,22 @@ def test_ozaki_tiled_records_and_tiles():
     meta = tuple(meta)
     for cplx in (False, True):
         plan = P.ozaki_dot_plan(meta, 8, cplx)
-        for recs, th, size in ((plan.a_recs_tc, 128, plan.a_size_tc), (plan.b_recs_tc, 64, plan.b_size_tc)):
+        for op, th, size in ((0, 128, plan.a_size_tc), (1, 64, plan.b_size_tc)):
             end = 0
-            for r in recs:
-                assert int(r[5]) == end
+            for r in _recs_of(plan, op, tc=True):
+                assert int(r[5]) == end and int(r[9]) == op | (th << 8)
                 end += 8 * (-(-int(r[1]) // th) * th) * int(r[7])
             assert end == size
-        a_new = {int(o): int(t) for o, t in zip(plan.a_recs[:, 5], plan.a_recs_tc[:, 5])}
-        b_new = {int(o): int(t) for o, t in zip(plan.b_recs[:, 5], plan.b_recs_tc[:, 5])}
+        groups = [(int(g[0]), int(g[1])) for g in plan.split_groups_tc]
+        want = {(ri, g) for ri, r in enumerate(plan.split_recs_tc)
+                for g in range(0, -(-int(r[1]) // (int(r[9]) >> 8)) * (int(r[9]) >> 8), P.OZ_SPLIT_ROWS)}
+        assert set(groups) == want and len(groups) == len(want)
+        # the same blocks in both layouts
+        assert np.array_equal(np.delete(plan.split_recs, [5, 9], axis=1),
+                              np.delete(plan.split_recs_tc, [5, 9], axis=1))
+        new = {(int(r[9]) & 1, int(r[5])): int(t[5]) for r, t in zip(plan.split_recs, plan.split_recs_tc)}
         for o, t in zip(plan.outs, plan.outs_tc):
-            assert int(t[4]) == a_new[int(o[4])] and int(t[6]) == b_new[int(o[6])]
+            assert int(t[4]) == new[(0, int(o[4]))] and int(t[6]) == new[(1, int(o[6]))]
             assert np.array_equal(np.delete(o, [4, 6]), np.delete(t, [4, 6]))
         want = {(oi, tr, tc) for oi, o in enumerate(plan.outs_tc)
                 for tr in range(-(-int(o[1]) // 128)) for tc in range(-(-int(o[2]) // 64))}
@@ -775,3 +813,50 @@ def test_ozaki_tiled_records_and_tiles():
         assert len(got) == len(want) and set(got) == want
         ks = [int(plan.outs_tc[t[0]][8]) for t in plan.tiles_tc]
         assert ks == sorted(ks, reverse=True)
+
+
+def test_ozaki_split_model_reconstructs_the_operands():
+    """The digit model of yb_ozaki_split (both layouts, real and complex records): every
+    record's digits and exponents rebuild its rows to within half a unit of the last digit,
+    the records tile the digit arrays without overlap, and the leading digit stays within
+    [-128, 128], the others within [-64, 63]."""
+    rng = np.random.default_rng(29)
+    shapes = [(40, 30, 20), (16, 16, 17), (130, 20, 70), (6, 300, 200), (33, 17, 65)]
+    meta, oa, ob, oc = [], 0, 0, 0
+    for m, k, n in shapes:
+        meta.append(((oc, oc + m * n), (m, n), (oa, oa + m * k), (m, k), (ob, ob + k * n), (k, n)))
+        oa += m * k; ob += k * n; oc += m * n
+    meta = tuple(meta)
+    for cplx in (False, True):
+        A = rng.normal(size=oa) * np.exp(rng.normal(size=oa) * 3)
+        B = rng.normal(size=ob) * np.exp(rng.normal(size=ob) * 3)
+        if cplx:
+            A = A + 1j * rng.normal(size=oa)
+            B = B + 1j * rng.normal(size=ob)
+        for s in (6, 8):
+            plan = P.ozaki_dot_plan(meta, s, cplx)
+            for recs, groups, sizes in ((plan.split_recs, plan.split_groups, (plan.a_size, plan.b_size)),
+                                        (plan.split_recs_tc, plan.split_groups_tc, (plan.a_size_tc, plan.b_size_tc))):
+                dig, exps = PI.ozaki_split(recs, groups, A, B, s, sizes, (plan.a_exps, plan.b_exps))
+                for op in (0, 1):
+                    d = dig[op]
+                    assert d.min() >= -128 and d.max() <= 128
+                for rec in recs:
+                    op, th = int(rec[9]) & 1, int(rec[9]) >> 8
+                    rows, K, Kp, dst, eo = int(rec[1]), int(rec[2]), int(rec[7]), int(rec[5]), int(rec[6])
+                    rows_p = -(-rows // th) * th if th else rows
+                    x = PI.split_rows(B if op else A, rec)
+                    e = exps[op][eo:eo + rows]
+                    r = np.arange(rows)[:, None]
+                    k = np.arange(K)[None, :]
+                    if th == 0:
+                        off = r * Kp + k
+                    else:
+                        off = (r // th) * (Kp // 16) * th * 16 + (k // 16) * th * 16 + ((r % th) // 8) * 128 + \
+                            ((k % 16) // 8) * 64 + (r % 8) * 8 + k % 8
+                    val = sum(dig[op][dst + t * rows_p * Kp + off].astype(float) * 2.0 ** (-7 * (t + 1))
+                              for t in range(s))
+                    rebuilt = np.ldexp(val, e[:, None])
+                    assert np.all(np.abs(rebuilt - x) <= np.ldexp(0.5 + 1e-9, (e - 7 * s)[:, None]))
+                    lead = dig[op][dst + off]
+                    assert np.all(np.abs(lead) <= 128)

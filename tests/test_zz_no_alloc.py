@@ -50,16 +50,14 @@ def _p(t):
 def _call_static(A, B, meta, Dsize, s=8, dtype=N.YB_F64):
     plan = P.ozaki_dot_plan(meta, s)
     nat = plan.native_direct
-    bt_tasks, bt_items = plan.bT.packed(False)
-    arrs = [_dev(x) for x in (plan.a_recs, plan.b_recs, bt_tasks, bt_items, plan.outs, plan.tiles,
+    arrs = [_dev(x) for x in (plan.split_recs, plan.split_groups, plan.outs, plan.tiles,
                               nat.outs, nat.terms, nat.tiles)]
     C = torch.zeros(Dsize, dtype=torch.float64, device='cuda')
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     st = N.lib().yb_ozaki_dot_static(
-        _p(A), _p(B), _p(C), dtype, _p(arrs[0]), len(plan.a_recs), plan.a_rows, _p(arrs[1]), len(plan.b_recs),
-        plan.b_rows, _p(arrs[2]), len(bt_tasks), _p(arrs[3]), len(bt_items), _p(arrs[4]), _p(arrs[5]),
-        len(plan.tiles), _p(arrs[6]), _p(arrs[7]), _p(arrs[8]), len(nat.tiles), s, plan.a_size, plan.b_size,
-        plan.a_exps, plan.b_exps, plan.bT_size, stream)
+        _p(A), _p(B), _p(C), dtype, _p(arrs[0]), _p(arrs[1]), len(plan.split_groups), _p(arrs[2]), _p(arrs[3]),
+        len(plan.tiles), _p(arrs[4]), _p(arrs[5]), _p(arrs[6]), len(nat.tiles), s, plan.a_size, plan.b_size,
+        plan.a_exps, plan.b_exps, stream)
     torch.cuda.synchronize()
     return st, C
 
@@ -89,7 +87,7 @@ def test_static_scratch_dot_matches_allocating_entry_point_and_oracle(cuda_devic
 
 def test_static_scratch_rejects_problems_beyond_its_size_and_complex_data(cuda_device):
     rng = np.random.default_rng(18)
-    meta, A, B, Dsize = _problem([(900, 900, 900)], rng)  # 2 x 8 x 900 x 912 bf16 + B^T > 16 MiB
+    meta, A, B, Dsize = _problem([(900, 900, 900)], rng)  # 2 x (2 x 8 x 900 x 912) bytes of digits > 16 MiB
     st, _ = _call_static(_dev(A), _dev(B), meta, Dsize)
     assert st == N.YB_ERR_TOO_LARGE
     meta, A, B, Dsize = _problem([(32, 32, 32)], rng)

@@ -22,6 +22,7 @@ SIGNATURES = {
     'yb_block_copy': ([_vp, _vp, _i, _vp, _i, _vp, _i, _vp], _i),
     'yb_gemm_reduce': ([_vp, _vp, _i, _vp, _vp, _i, _d, _d, _vp], _i),
     'yb_grouped_gemm': ([_vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _d, _d, _vp], _i),
+    'yb_grouped_gemm_short': ([_vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _d, _d, _vp], _i),
     'yb_svd_init': ([_vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp], _i),
     'yb_svd_qr': ([_vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _i, _vp], _i),
     'yb_qr': ([_vp, _vp, _vp, _vp, _vp, _i, _i, _vp, _i, _vp], _i),
@@ -38,13 +39,12 @@ SIGNATURES = {
     'yb_mask_gather': ([_vp, _vp, _i, _vp, _vp, _i, _vp, _i, _vp], _i),
     'yb_fix_signs': ([_vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp], _i),
     'yb_fix_signs_adjoint': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp], _i),
-    'yb_ozaki_split': ([_vp, _vp, _vp, _vp, _i, _i, _i, _vp], _i),
-    'yb_ozaki_split_tiled': ([_vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp], _i),
+    'yb_ozaki_split': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
     'yb_ozaki_gemm': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
     'yb_ozaki_gemm_tc': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
     'yb_ozaki_device_error': ([_vp, _i, _vp], _i),
-    'yb_ozaki_dot_static': ([_vp, _vp, _vp, _i, _vp, _i, _i, _vp, _i, _i, _vp, _i, _vp, _i, _vp, _vp, _i,
-                             _vp, _vp, _vp, _i, _i, _i64, _i64, _i64, _i64, _i64, _vp], _i),
+    'yb_ozaki_dot_static': ([_vp, _vp, _vp, _i, _vp, _vp, _i, _vp, _vp, _i, _vp, _vp, _vp, _i, _i,
+                             _i64, _i64, _i64, _i64, _vp], _i),
     'yb_krylov_parts': ([], _i),
     'yb_krylov_dot': ([_vp, _vp, _i64, _i, _vp, _vp, _vp], _i),
     'yb_krylov_update': ([_vp, _vp, _vp, _vp, _vp, _i64, _i, _vp, _vp, _vp], _i),

@@ -302,6 +302,8 @@ class GemmPlan:
         self.tiles = tiles
         self.flops = flops  # real multiply-adds x 2 (complex counted by the caller)
         self.split = split
+        # every tile a short skinny one: the plan runs on the kernel of those alone
+        self.all_short = bool(len(tiles)) and bool((tiles[:, 3] == 2).all())
         self._dev = {}
 
 
@@ -316,17 +318,25 @@ class SplitK:
 
 SKINNY_ROWS, SKINNY_COLS = 8, 1024  # skinny tiles: up to 8 rows (the kernel takes 16), 1024 columns
                                     # (256 above 8 rows)
+SHORT_K, SHORT_COLS = 8, 512  # short skinny tiles (kind 2): one term with K <= 8, 512 columns
 
 
 def skinny_cols(rows):
     return SKINNY_COLS if rows <= 8 else SKINNY_COLS // 4
 
 
-def tile_kind(m, n):
-    """0: 64x64 tiles; 1: skinny tiles over the m <= 16 rows."""
+def tile_kind(m, n, ks=None):
+    """0: 64x64 tiles; 1: skinny tiles over the m <= 16 rows; 2: short skinny tiles (m <= 8
+    rows and a single term whose K <= SHORT_K, any n; ``ks`` = the output's term lengths)."""
+    if m <= SKINNY_ROWS and ks is not None and len(ks) == 1 and ks[0] <= SHORT_K:
+        return 2
     if m <= SKINNY_ROWS and n > GEMM_TILE:
         return 1
     return 0
+
+
+def _tile_cols(kind, m):
+    return SHORT_COLS if kind == 2 else skinny_cols(m)
 GEMM_RED_REC, GEMM_RED_ITEM = 8, 1024
 SPLITK_MAX_TILES = 304   # plans with this many tiles (2 per SM) are not split
 SPLITK_UNITS = 608       # tiles x chunks aimed at after splitting (4 per SM)
@@ -342,11 +352,13 @@ def _tiles_for(outs, terms):
         m, n = int(o[1]), int(o[2])
         if m == 0 or n == 0:
             continue
-        kk = int(sum(terms[t][2] for t in range(o[4], o[5])))
-        if tile_kind(m, n):
-            w = skinny_cols(m)
+        ks = [int(terms[t][2]) for t in range(o[4], o[5])]
+        kk = sum(ks)
+        kind = tile_kind(m, n, ks)
+        if kind:
+            w = _tile_cols(kind, m)
             for tc in range((n + w - 1) // w):
-                tiles.append((kk * m * 16, oi, 0, tc, 1))
+                tiles.append((kk * m * 16, oi, 0, tc, kind))
             continue
         for tr in range((m + GEMM_TILE - 1) // GEMM_TILE):
             for tc in range((n + GEMM_TILE - 1) // GEMM_TILE):
@@ -356,21 +368,22 @@ def _tiles_for(outs, terms):
     return arr
 
 
-def _n_tiles(m, n):
+def _n_tiles(m, n, ks=None):
     if m == 0 or n == 0:
         return 0
-    if tile_kind(m, n):
-        return (n + skinny_cols(m) - 1) // skinny_cols(m)
+    kind = tile_kind(m, n, ks)
+    if kind:
+        return (n + _tile_cols(kind, m) - 1) // _tile_cols(kind, m)
     return ((m + GEMM_TILE - 1) // GEMM_TILE) * ((n + GEMM_TILE - 1) // GEMM_TILE)
 
 
 def _split_chunk_k(out_list):
     """K per chunk when the plan has too few tiles to fill the GPU and some output's K is
     long (None: no split). Work is counted as tiles x K."""
-    tiles = sum(_n_tiles(m, n) for _, m, n, _, _ in out_list)
+    tiles = sum(_n_tiles(m, n, [t[2] for t in tl]) for _, m, n, _, tl in out_list)
     if tiles == 0 or tiles >= SPLITK_MAX_TILES:
         return None
-    work = sum(_n_tiles(m, n) * sum(t[2] for t in tl) for _, m, n, _, tl in out_list)
+    work = sum(_n_tiles(m, n, [t[2] for t in tl]) * sum(t[2] for t in tl) for _, m, n, _, tl in out_list)
     ck = max(SPLITK_MIN_K, -(-work // SPLITK_UNITS))
     ck = -(-ck // 16) * 16
     if not any(sum(t[2] for t in tl) >= 2 * ck for _, m, n, _, tl in out_list if m and n):
@@ -501,10 +514,8 @@ def tds_plan(meta_dot, Areshape, Breshape, Aoffs, Boffs):
 class OzakiPlan:
     """Split records and GEMM tiles of the split-operand (Ozaki) emulated FP64 dot."""
 
-    def __init__(self, a_recs, b_recs, outs, tiles, a_size, b_size, a_exps, b_exps, a_rows, b_rows, flops, s):
-        self.a_recs, self.b_recs, self.outs, self.tiles = a_recs, b_recs, outs, tiles
-        self.a_size, self.b_size, self.a_exps, self.b_exps = a_size, b_size, a_exps, b_exps
-        self.a_rows, self.b_rows = a_rows, b_rows
+    def __init__(self, outs, tiles, flops, s):
+        self.outs, self.tiles = outs, tiles
         self.flops = flops
         self.slices = s
         self._dev = {}
@@ -513,35 +524,46 @@ class OzakiPlan:
 OZAKI_TC_M, OZAKI_TC_N = 128, 64  # output tile of the tcgen05 emulated GEMM
 OZAKI_MIN_DIM = 16  # sector GEMMs contracting fewer indices than this stay on the native FP64 kernel
 OZAKI_SKINNY_ROWS = 8  # sector GEMMs with at most this many rows (and more than 64 columns) too
+OZ_SPLIT_REC = 10  # YB_OZ_SPLIT_REC
+OZ_SPLIT_ROWS = 8  # rows per split CTA
 
 
-def _tiled_recs(recs, s, th):
-    """Split records with destinations in the tcgen05 tile layout: each operand block takes
-    s * ceil(rows / th) * th * Kp digits. Returns (records, total size, old offset -> new)."""
-    out = recs.copy()
-    size, remap = 0, {}
-    for i, r in enumerate(recs):
-        rows, Kp = int(r[1]), int(r[7])
-        remap[int(r[5])] = size
-        out[i, 5] = size
-        size += s * (-(-rows // th) * th) * Kp
-    return out, size, remap
+def _split_layout(blocks, s, th_a, th_b):
+    """Split records (YB_OZ_SPLIT_REC int64) and 8-row groups for the operand blocks
+    ``blocks`` = [(operand, src offset, rows, Kr, row stride, k stride, mode, Kp)], with the
+    digit planes of operand A in tile rows ``th_a`` and of B in ``th_b`` (0: planes
+    [slice][row][Kp]). Returns (records, groups, A size, B size, A exps, B exps) and the
+    slice-0 offset and exponent offset of every block."""
+    recs, groups, where = [], [], []
+    size, nex = [0, 0], [0, 0]
+    for op, src, rows, Kr, rs, ks, mode, Kp in blocks:
+        th = th_b if op else th_a
+        rows_p = -(-rows // th) * th if th else rows
+        where.append((size[op], nex[op]))
+        ri = len(recs)
+        recs.append((src, rows, Kr, rs, mode, size[op], nex[op], Kp, ks, op | (th << 8)))
+        groups.extend((ri, g) for g in range(0, rows_p, OZ_SPLIT_ROWS))
+        size[op] += s * rows_p * Kp
+        nex[op] += rows
+    recs = np.array(recs, dtype=np.int64).reshape(-1, OZ_SPLIT_REC)
+    groups = np.array(groups, dtype=np.int32).reshape(-1, 2)
+    return recs, groups, size[0], size[1], nex[0], nex[1], where
 
 
 def ozaki_dot_plan(meta_dot, s, cplx=False):
     """C[slc] = A[sla] @ B[slb] with A rows / B columns split into ``s`` BF16 digit slices.
 
-    B blocks are first transposed (copy plan ``bT``) into K-contiguous rows, so both
-    operands are split row-wise with coalesced accesses. Complex blocks (``cplx``) become
-    two real products with doubled K, C_r = [A_r, A_i][B_r; -B_i] and
-    C_i = [A_r, A_i][B_i; B_r]: A is split once in mode 1 ([re | im] rows), each B^T block
-    twice (modes 2 and 3), and the two outputs of a sector write the real and imaginary
-    parts of the complex result (column stride 2 in FP64 units).
+    Both operands are split by one launch of yb_ozaki_split: A blocks by rows, B blocks by
+    columns read in place (k stride n). Complex blocks (``cplx``) become two real products
+    with doubled K, C_r = [A_r, A_i][B_r; -B_i] and C_i = [A_r, A_i][B_i; B_r]: A is split
+    once in mode 1 ([re | im] rows), each B block twice (modes 2 and 3), and the two outputs
+    of a sector write the real and imaginary parts of the complex result (column stride 2 in
+    FP64 units). The records exist twice: digit planes for the mma.sync kernel (64 x 64
+    tiles) and the tile layout of the tcgen05 kernel (128 x 64 tiles).
     """
     def build():
-        a_map, b_map, a_recs, b_recs, bT_tasks = {}, {}, [], [], []
-        a_size = b_size = a_ex = b_ex = bT_size = 0
-        outs, flops, small = [], 0, []
+        a_map, b_map, blocks = {}, {}, []
+        outs_ref, flops, small = [], 0, []
         f = 2 if cplx else 1  # FP64 words per element
         for slc, Dc, sla, Da, slb, Db in meta_dot:
             m, K = Da
@@ -553,26 +575,25 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
             Kr = f * K  # length of the real rows that are split
             Kp = (Kr + 15) // 16 * 16
             if sla[0] not in a_map:
-                a_map[sla[0]] = (a_size, a_ex)
-                a_recs.append((sla[0], m, Kr, K, int(cplx), a_size, a_ex, Kp))
-                a_size += s * m * Kp
-                a_ex += m
+                a_map[sla[0]] = len(blocks)
+                blocks.append((0, sla[0], m, Kr, K, 1, int(cplx), Kp))
             if slb[0] not in b_map:
-                bT_tasks.append((slb[0], bT_size, [n, K], [1, n], [K, 1]))
-                parts = []
+                b_map[slb[0]] = []
                 for mode in ((2, 3) if cplx else (0,)):
-                    b_recs.append((bT_size, n, Kr, K, mode, b_size, b_ex, Kp))
-                    parts.append((b_size, b_ex))
-                    b_size += s * n * Kp
-                    b_ex += n
-                b_map[slb[0]] = parts
-                bT_size += n * K
-            ao, ae = a_map[sla[0]]
-            for part, (bo, be) in enumerate(b_map[slb[0]]):
+                    b_map[slb[0]].append(len(blocks))
+                    blocks.append((1, slb[0], n, Kr, 1, n, mode, Kp))
+            for part, bi in enumerate(b_map[slb[0]]):
                 # complex: part 0 = real part (even FP64 words), part 1 = imaginary part
-                outs.append((f * slc[0] + part, m, n, f * n, ao, ae, bo, be, Kr, Kp, f, 0, 0, 0, 0, 0))
+                outs_ref.append((f * slc[0] + part, m, n, f * n, a_map[sla[0]], bi, Kr, Kp, f))
             flops += (8 if cplx else 2) * m * n * K
-        outs = np.array(outs, dtype=np.int64).reshape(-1, 16)
+
+        def outs_for(where):
+            return np.array([(c, m, n, ld, where[ai][0], where[ai][1], where[bi][0], where[bi][1], Kr, Kp, cs,
+                              0, 0, 0, 0, 0) for c, m, n, ld, ai, bi, Kr, Kp, cs in outs_ref],
+                            dtype=np.int64).reshape(-1, 16)
+
+        sr, sg, asz, bsz, aex, bex, where = _split_layout(blocks, s, 0, 0)
+        outs = outs_for(where)
         tiles = []
         for oi, o in enumerate(outs):
             m, n, K = int(o[1]), int(o[2]), int(o[8])
@@ -583,33 +604,25 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
                     tiles.append((K, oi, tr, tc))
         tiles.sort(key=lambda x: -x[0])
         tiles = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles], dtype=np.int32).reshape(-1, 4)
-        a_recs = np.array(a_recs, dtype=np.int64).reshape(-1, 8)
-        b_recs = np.array(b_recs, dtype=np.int64).reshape(-1, 8)
-        a_rows = int(a_recs[:, 1].max()) if len(a_recs) else 0
-        b_rows = int(b_recs[:, 1].max()) if len(b_recs) else 0
-        plan = OzakiPlan(a_recs, b_recs, outs, tiles, a_size, b_size, a_ex, b_ex, a_rows, b_rows, flops, s)
-        plan.bT = CopyPlan([t for t in bT_tasks if t[2][0] * t[2][1] > 0], bT_size, bT_size)
-        plan.bT_size = bT_size
+        plan = OzakiPlan(outs, tiles, flops, s)
+        plan.split_recs, plan.split_groups = sr, sg
+        plan.a_size, plan.b_size, plan.a_exps, plan.b_exps = asz, bsz, aex, bex
         plan.native = _pack_gemm(small)
         plan.native_direct = _pack_gemm(small, allow_split=False)  # no chunk workspace
         plan.covered = dot_coverage(meta_dot)
         # 128 x 64 tiles of the tcgen05 kernel (longest K first) and the digit planes in its
         # tile layout (rows padded to 128 for A, 64 for B)
+        sr, sg, asz, bsz, _, _, where = _split_layout(blocks, s, OZAKI_TC_M, OZAKI_TC_N)
+        plan.split_recs_tc, plan.split_groups_tc, plan.a_size_tc, plan.b_size_tc = sr, sg, asz, bsz
+        plan.outs_tc = outs_for(where)
         tiles_tc = []
-        for oi, o in enumerate(outs):
+        for oi, o in enumerate(plan.outs_tc):
             m, n, K = int(o[1]), int(o[2]), int(o[8])
             for tr in range(-(-m // OZAKI_TC_M)):
                 for tc in range(-(-n // OZAKI_TC_N)):
                     tiles_tc.append((K, oi, tr, tc))
         tiles_tc.sort(key=lambda x: -x[0])
         plan.tiles_tc = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles_tc], dtype=np.int32).reshape(-1, 4)
-        plan.a_recs_tc, plan.a_size_tc, a_off_tc = _tiled_recs(a_recs, s, OZAKI_TC_M)
-        plan.b_recs_tc, plan.b_size_tc, b_off_tc = _tiled_recs(b_recs, s, OZAKI_TC_N)
-        outs_tc = outs.copy()
-        if len(outs_tc):
-            outs_tc[:, 4] = [a_off_tc[int(x)] for x in outs[:, 4]]
-            outs_tc[:, 6] = [b_off_tc[int(x)] for x in outs[:, 6]]
-        plan.outs_tc = outs_tc
         # padded MMA work of the two tilings: the tcgen05 kernel (128 x 64 tiles) when its
         # padding costs little more than the 64 x 64 tiles of the mma.sync kernel
         w64 = sum(-(-int(o[1]) // 64) * 64 * -(-int(o[2]) // 64) * 64 * int(o[9]) for o in outs)

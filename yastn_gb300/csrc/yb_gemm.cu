@@ -138,6 +138,116 @@ __device__ __forceinline__ void skinny_dispatch(int64_t mr, const typename F::T*
   }
 }
 
+// Short skinny outputs (one term, at most 8 rows, K <= 8; the contractions with a small
+// MPO block): op(A) goes to shared memory once, every thread issues all K x kShortCols loads of
+// its columns of op(B) before the FMAs, so the strip's loads are in flight together; the
+// work is FP64-bound (m K FMAs per column), and the kernel of its own (few registers, several
+// CTAs per SM) keeps the DFMA pipe fed.
+constexpr int kShortK = 8;
+constexpr int kShortCols = 2;  // columns per thread: a tile is kThreads * kShortCols columns
+template <class F, int M, int KB>
+__device__ __forceinline__ void short_tile(const typename F::T* __restrict__ A, const typename F::T* __restrict__ B,
+                                           typename F::T* __restrict__ C, const int64_t* __restrict__ orec,
+                                           const int64_t* __restrict__ trec, int tcol, double alpha, double beta,
+                                           bool unit_alpha, bool zero_beta, typename F::T* Ak) {
+  using T = typename F::T;
+  const int64_t c_off = orec[0], ldc = orec[3], nc = orec[2];
+  const int mr = (int)orec[1], K = (int)trec[2];
+  const T* La = A + trec[0];
+  const int64_t l_is = trec[3], l_ls = trec[4], r_ls = trec[5], r_js = trec[6];
+  const int flags = (int)trec[7];
+  const bool conjL = flags & 1, conjR = flags & 2;
+  if (threadIdx.x < KB * M) {
+    const int i = threadIdx.x % M, l = threadIdx.x / M;
+    T v = F::zero();
+    if (l < K && i < mr) {
+      v = La[i * l_is + l * l_ls];
+      if (conjL) v = F::conj(v);
+    }
+    Ak[l * M + i] = v;
+  }
+  __syncthreads();
+  const int64_t j0 = (int64_t)tcol * (kThreads * kShortCols) + threadIdx.x;
+  const T* Rb = B + trec[1];
+  T b[KB][kShortCols];
+#pragma unroll
+  for (int u = 0; u < kShortCols; ++u) {
+    const int64_t j = j0 + u * kThreads;
+    const bool live = j < nc;
+    const T* col = Rb + (live ? j * r_js : 0);
+#pragma unroll
+    for (int l = 0; l < KB; ++l) {
+      b[l][u] = (live && l < K) ? col[l * r_ls] : F::zero();
+      if (conjR) b[l][u] = F::conj(b[l][u]);
+    }
+  }
+  T acc[kShortCols][M];
+#pragma unroll
+  for (int u = 0; u < kShortCols; ++u)
+#pragma unroll
+    for (int i = 0; i < M; ++i) acc[u][i] = F::zero();
+#pragma unroll
+  for (int l = 0; l < KB; ++l) {
+    if (l >= K) break;
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      const T a = Ak[l * M + i];
+#pragma unroll
+      for (int u = 0; u < kShortCols; ++u) F::fma(acc[u][i], a, b[l][u]);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < kShortCols; ++u) {
+    const int64_t j = j0 + u * kThreads;
+    if (j >= nc) continue;
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      if (i >= mr) break;
+      T* p = C + c_off + i * ldc + j;
+      T v = unit_alpha ? acc[u][i] : F::scale(acc[u][i], alpha);
+      if (!zero_beta) v = F::add(v, F::scale(*p, beta));
+      *p = v;
+    }
+  }
+}
+
+template <class F>
+__device__ __forceinline__ void short_dispatch(const typename F::T* __restrict__ A, const typename F::T* __restrict__ B,
+                                               typename F::T* __restrict__ C, const int64_t* __restrict__ orec,
+                                               const int64_t* __restrict__ terms, int tcol, double alpha, double beta,
+                                               typename F::T* Ak) {
+  const int64_t* trec = terms + orec[4] * YB_GEMM_TERM_REC;
+  const bool ua = alpha == 1.0, zb = beta == 0.0;  // once per tile, not per element (FP64 compares)
+  const bool k4 = trec[2] <= 4;
+  switch ((int)orec[1]) {
+    case 1: k4 ? short_tile<F, 1, 4>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak)
+               : short_tile<F, 1, 8>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak); break;
+    case 2: k4 ? short_tile<F, 2, 4>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak)
+               : short_tile<F, 2, 8>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak); break;
+    case 3: k4 ? short_tile<F, 3, 4>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak)
+               : short_tile<F, 3, 8>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak); break;
+    case 4: k4 ? short_tile<F, 4, 4>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak)
+               : short_tile<F, 4, 8>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak); break;
+    default: short_tile<F, 8, 8>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak); break;
+  }
+}
+
+// Kernel of the short skinny tiles only (tile kind 2).
+template <class F>
+__global__ void __launch_bounds__(kThreads, 3) short_gemm_kernel(const typename F::T* __restrict__ A,
+                                                                 const typename F::T* __restrict__ B,
+                                                                 typename F::T* __restrict__ C,
+                                                                 const int64_t* __restrict__ outs,
+                                                                 const int64_t* __restrict__ terms,
+                                                                 const int32_t* __restrict__ tiles, double alpha,
+                                                                 double beta) {
+  using T = typename F::T;
+  __shared__ T Ak[kShortK * 8];
+  const int4 tl = reinterpret_cast<const int4*>(tiles)[blockIdx.x];
+  const int64_t* orec = outs + (int64_t)tl.x * YB_GEMM_OUT_REC;
+  short_dispatch<F>(A, B, C, orec, terms, tl.z, alpha, beta, Ak);
+}
+
 template <class F>
 __global__ void __launch_bounds__(kThreads) grouped_gemm_kernel(const typename F::T* __restrict__ A,
                                                                  const typename F::T* __restrict__ B,
@@ -156,6 +266,10 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_kernel(const typename F
   const int64_t t0 = orec[4], t1 = orec[5];
   if (tl.w == 1) {  // skinny: the m <= 16 rows x 1024 (256) columns
     skinny_dispatch<F>(m, A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]);
+    return;
+  }
+  if (tl.w == 2) {  // short skinny: m <= 8 rows, one term with K <= 8, 512 columns
+    short_dispatch<F>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]);
     return;
   }
 
@@ -303,6 +417,24 @@ extern "C" int yb_grouped_gemm(const void* a, const void* b, void* c, int dtype,
         (const double*)a, (const double*)b, (double*)c, outs, terms, tiles, alpha, beta);
   } else if (dtype == YB_C128) {
     yb::grouped_gemm_kernel<yb::Cplx><<<n_tiles, yb::kThreads, 0, s>>>(
+        (const double2*)a, (const double2*)b, (double2*)c, outs, terms, tiles, alpha, beta);
+  } else {
+    return YB_ERR_INVALID;
+  }
+  return yb::check_launch();
+}
+
+extern "C" int yb_grouped_gemm_short(const void* a, const void* b, void* c, int dtype, const int64_t* outs,
+                                     const int64_t* terms, const int32_t* tiles, int n_tiles, double alpha,
+                                     double beta, void* stream) {
+  if (n_tiles == 0) return YB_OK;
+  if (!a || !b || !c || !outs || !terms || !tiles || n_tiles < 0) return YB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == YB_F64) {
+    yb::short_gemm_kernel<yb::Real><<<n_tiles, yb::kThreads, 0, s>>>(
+        (const double*)a, (const double*)b, (double*)c, outs, terms, tiles, alpha, beta);
+  } else if (dtype == YB_C128) {
+    yb::short_gemm_kernel<yb::Cplx><<<n_tiles, yb::kThreads, 0, s>>>(
         (const double2*)a, (const double2*)b, (double2*)c, outs, terms, tiles, alpha, beta);
   } else {
     return YB_ERR_INVALID;

@@ -28,6 +28,7 @@ namespace yb {
 namespace {
 using oz::scaled_rint;
 using oz::scale_pow2;
+using oz::fold_round;
 
 constexpr int kTile = 64;
 constexpr int kK = 16;
@@ -39,13 +40,22 @@ constexpr int kChunkSteps = 25;
 constexpr int kThreads = 256;
 
 // ------------------------------------------------------------------ splitting
-// rec: [0] src offset [1] rows [2] K [3] row stride [4] mode
-//      [5] dst offset (bf16) [6] exponent offset [7] Kp (K rounded up to 16)
-// mode 0: a real row of K contiguous FP64 values (offsets and stride in elements);
-// modes 1-3: a complex128 row of K/2 values (offsets and stride in complex elements) read
-// as the real row [re | im] (1), [re | -im] (2) or [im | re] (3), the operands of the two
-// real products C_r = [A_r, A_i][B_r; -B_i] and C_i = [A_r, A_i][B_i; B_r] of a complex GEMM.
-// dst layout: [slice][row][Kp] bf16, padding zero-filled.
+// Split record (YB_OZ_SPLIT_REC = 10 int64):
+//   [0] source offset [1] rows [2] K (length of the real rows) [3] row stride [4] mode
+//   [5] destination offset (BF16 elements) [6] exponent offset [7] Kp (K rounded up to 16)
+//   [8] stride between consecutive k [9] operand (bit 0: 0 = A, 1 = B) | tile rows << 8
+// Element k of row i is read at source offset [0] + i*[3] + k*[8] (FP64 elements for mode 0,
+// complex elements for modes 1-3), so an A block (rows contiguous, [8] = 1) and a B block
+// read by columns ([3] = 1, [8] = n: the rows of B^T, no transposed copy) are split alike.
+// mode 0: a real row; modes 1-3: a complex128 row of K/2 values read as the real row
+// [re | im] (1), [re | -im] (2) or [im | re] (3), the operands of the two real products
+// C_r = [A_r, A_i][B_r; -B_i] and C_i = [A_r, A_i][B_i; B_r] of a complex GEMM.
+// Destination layouts (padding zero-filled):
+//   tile rows 0: planes [slice][row][Kp] (the mma.sync kernel);
+//   tile rows TH (64 or 128): per slice, the rows padded to a multiple of TH, in blocks of
+//   TH rows x 16 k ordered (row tile, K step), each block in the canonical K-major
+//   core-matrix order of the tcgen05 descriptors (element offset of (row r, k) in a block:
+//   (r/8)*128 + (k/8)*64 + (r%8)*8 + k%8).
 //
 // The digits are extracted with integer arithmetic only (GB300's FP64 pipe is narrow):
 // Q = rint(a 2^{7s-e}) (|Q| < 2^{7s}) is formed from a's mantissa and exponent bits by a
@@ -53,26 +63,48 @@ constexpr int kThreads = 256;
 // U = Q + 64 (1 + 128 + ... + 128^{s-2}): d_t = ((U >> 7(s-1-t)) & 127) - 64 for t >= 1 and
 // the leading digit d_0 = U >> 7(s-1) in [-128, 128] (arithmetic shift). This represents
 // a 2^-e = sum_t d_t 2^{-7(t+1)} up to the rounding of Q (half a unit of the last digit).
-__device__ __forceinline__ void digits_of(long long bits, int e, int s, int* d) {
-  long long bias = 0;
-  for (int t = 0; t < s - 1; ++t) bias = (bias << 7) | 64;
-  const long long u = scaled_rint(bits, e, s) + bias;
-#pragma unroll
-  for (int t = 1; t < 8; ++t)
-    if (t < s) d[t] = (int)((u >> (7 * (s - 1 - t))) & 127) - 64;
-  d[0] = (int)(u >> (7 * (s - 1)));
+// A digit d (|d| <= 128, at most 8 significant bits) becomes its BF16 pattern without a
+// conversion instruction: the FP32 value 1.5*2^23 + d has the bit pattern 0x4B400000 + d,
+// subtracting 1.5*2^23 leaves d exactly, and the upper half of d's FP32 pattern is its BF16.
+constexpr int kSplitRec = 10;
+constexpr int kSplitRows = 8;       // rows per CTA
+constexpr int kSplitThreads = 256;  // thread t: row t % 8, chunk lane t / 8
+constexpr int kSplitLanes = kSplitThreads / kSplitRows;  // 32 chunk lanes: chunks c = lane, lane + 32, ...
+
+__host__ __device__ constexpr long long digit_bias(int s) {
+  return s <= 1 ? 0 : (digit_bias(s - 1) << 7) | 64;
 }
 
-// Bit pattern of element l of the split row (see the record modes above).
-struct RowSrc {
-  const double* base;
-  int64_t half;  // K/2 for the complex modes
+__device__ __forceinline__ uint32_t digit_f32(int field_plus_magic) {
+  return __float_as_uint(__int_as_float(field_plus_magic) - 12582912.0f);
+}
+
+// The S digits of one element as FP32 bit patterns (BF16 in the upper halves).
+template <int S>
+__device__ __forceinline__ void digit_words(long long bits, int e, uint32_t* w) {
+  constexpr long long kBias = digit_bias(S);
+  const long long u = scaled_rint(bits, e, S) + kBias;
+  const uint32_t lo = (uint32_t)u, hi = (uint32_t)((unsigned long long)u >> 32);
+  w[0] = digit_f32(0x4B400000 + ((int)hi >> (7 * (S - 1) - 32)));
+#pragma unroll
+  for (int t = 1; t < S; ++t) {
+    const int o = 7 * (S - 1 - t);
+    uint32_t f;
+    if (o >= 32) f = hi >> (o - 32);
+    else if (o + 7 <= 32) f = lo >> o;
+    else f = __funnelshift_r(lo, hi, o);
+    w[t] = digit_f32(0x4B400000 - 64 + (int)(f & 127u));
+  }
+}
+
+struct SplitSrc {
+  const long long* base;  // element (row, 0)
+  int64_t ks, half;
   int mode;
-  __device__ __forceinline__ long long operator()(int64_t l) const {
-    if (mode == 0) return __ldg(reinterpret_cast<const long long*>(base) + l);
-    const bool first = l < half;
-    const int64_t j = first ? l : l - half;
-    const long long* c = reinterpret_cast<const long long*>(base) + 2 * j;
+  __device__ __forceinline__ long long operator()(int64_t k) const {
+    if (mode == 0) return __ldg(base + k * ks);
+    const bool first = k < half;
+    const long long* c = base + 2 * (first ? k : k - half) * ks;
     const long long re = __ldg(c), im = __ldg(c + 1);
     if (mode == 1) return first ? re : im;
     if (mode == 2) return first ? re : (long long)((unsigned long long)im ^ 0x8000000000000000ull);
@@ -80,109 +112,100 @@ struct RowSrc {
   }
 };
 
-__device__ __forceinline__ RowSrc row_src(const double* src, const int64_t* r, int64_t row) {
-  const int mode = (int)r[4];
-  RowSrc rs;
-  rs.mode = mode;
-  rs.half = r[2] / 2;
-  rs.base = src + (mode == 0 ? r[0] + row * r[3] : 2 * (r[0] + row * r[3]));
-  return rs;
-}
-
-__global__ void split_rows_kernel(const double* __restrict__ src, __nv_bfloat16* __restrict__ slices,
-                                  int* __restrict__ exps, const int64_t* __restrict__ recs, int s) {
-  // one warp per row (K contiguous), each lane two consecutive elements per step
-  const int64_t* r = recs + (int64_t)blockIdx.y * 8;
+// One CTA per 8 rows of a record (groups: int32 pairs (record, first row)); the 256 threads
+// are 8 rows x 32 chunk lanes, each lane taking the row's 8-long K chunks lane, lane + 32, ...:
+// the row maxima first (exponents), then the digits, each chunk stored as one 16-byte word
+// per slice (8 consecutive rows of a tile-layout block are 128 contiguous bytes).
+template <int S>
+__global__ void __launch_bounds__(kSplitThreads) split_kernel(
+    const double* __restrict__ a_src, const double* __restrict__ b_src, __nv_bfloat16* __restrict__ a_dst,
+    __nv_bfloat16* __restrict__ b_dst, int* __restrict__ a_exps, int* __restrict__ b_exps,
+    const int64_t* __restrict__ recs, const int32_t* __restrict__ groups) {
+  __shared__ long long smax[kSplitLanes][kSplitRows];
+  __shared__ int sexp[kSplitRows];
+  const int2 g = reinterpret_cast<const int2*>(groups)[blockIdx.x];
+  const int64_t* r = recs + (int64_t)g.x * kSplitRec;
   const int64_t rows = r[1], K = r[2], Kp = r[7];
-  const int lane = threadIdx.x & 31;
-  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (row >= rows) return;
-  const RowSrc a = row_src(src, r, row);
-  // row maximum of |a| on the bit patterns (non-negative doubles order as integers)
-  long long mx = 0;
-  for (int64_t l = lane; l < K; l += 32) mx = max(mx, a(l) & 0x7fffffffffffffffll);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  int e = 0;  // max |a| = f 2^e, f in [0.5, 1): |a| < 2^e
-  if (mx >= (1ll << 52)) e = (int)(mx >> 52) - 1022;
-  else if (mx > 0) frexp(__longlong_as_double(mx), &e);
-  if (lane == 0) exps[r[6] + row] = e;
-  const int64_t slice_stride = rows * Kp;
-  __nv_bfloat16* dst = slices + r[5] + row * Kp;
-  for (int64_t l = 2 * lane; l < Kp; l += 64) {
-    int d0[8], d1[8];
-    if (l < K) digits_of(a(l), e, s, d0); else for (int t = 0; t < 8; ++t) d0[t] = 0;
-    if (l + 1 < K) digits_of(a(l + 1), e, s, d1); else for (int t = 0; t < 8; ++t) d1[t] = 0;
-    for (int t = 0; t < s; ++t) {
-      __nv_bfloat162 v;
-      v.x = __int2bfloat16_rn(d0[t]);
-      v.y = __int2bfloat16_rn(d1[t]);
-      *reinterpret_cast<__nv_bfloat162*>(dst + t * slice_stride + l) = v;
-    }
-  }
-}
-
-
-// The same split written in the tensor-core tile layout of the tcgen05 GEMM: per slice, the
-// rows are grouped in tiles of TH (128 for A, 64 for B) and K in steps of 16; every
-// (row tile, K step) is one contiguous TH x 16 block in the canonical K-major layout of the
-// tcgen05 matrix descriptors (8-row x 16-byte core matrices: byte offset of (row r, k) is
-// (r/8)*256 + (k/8)*128 + (r%8)*16 + (k%8)*2), so a GEMM stage is a few bulk copies. Rows
-// from the operand's row count up to the next multiple of TH are written as zeros.
-__global__ void split_rows_tiled_kernel(const double* __restrict__ src, __nv_bfloat16* __restrict__ slices,
-                                        int* __restrict__ exps, const int64_t* __restrict__ recs, int s, int TH) {
-  const int64_t* r = recs + (int64_t)blockIdx.y * 8;
-  const int64_t rows = r[1], K = r[2], Kp = r[7];
-  const int64_t rows_p = (rows + TH - 1) / TH * TH;
-  const int lane = threadIdx.x & 31;
-  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (row >= rows_p) return;
+  const int flags = (int)r[9];
+  const bool opb = flags & 1;
+  const int TH = flags >> 8;
+  const int ri = threadIdx.x % kSplitRows, cl = threadIdx.x / kSplitRows;
+  const int64_t row = (int64_t)g.y + ri;
   const bool live = row < rows;
-  const RowSrc a = row_src(src, r, live ? row : 0);
+  SplitSrc a;
+  a.mode = (int)r[4];
+  a.ks = r[8];
+  a.half = K / 2;
+  a.base = reinterpret_cast<const long long*>(opb ? b_src : a_src) +
+           (a.mode == 0 ? 1 : 2) * (r[0] + (live ? row : 0) * r[3]);
+  const int64_t kc = (K + 7) / 8;  // chunks holding data
   long long mx = 0;
   if (live)
-    for (int64_t l = lane; l < K; l += 32) mx = max(mx, a(l) & 0x7fffffffffffffffll);
+    for (int64_t c = cl; c < kc; c += kSplitLanes) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  int e = 0;
-  if (mx >= (1ll << 52)) e = (int)(mx >> 52) - 1022;
-  else if (mx > 0) frexp(__longlong_as_double(mx), &e);
-  if (live && lane == 0) exps[r[6] + row] = e;
-  const int64_t slice_stride = rows_p * Kp;
-  const int64_t ksteps = Kp / 16;
-  __nv_bfloat16* base = slices + r[5] + (row / TH) * ksteps * (int64_t)TH * 16;
-  const int rr = (int)(row % TH);
-  const int64_t in_tile = (int64_t)(rr >> 3) * 128 + (rr & 7) * 8;  // elements
-  for (int64_t l = 2 * lane; l < Kp; l += 64) {
-    int d0[8], d1[8];
-    if (live && l < K) digits_of(a(l), e, s, d0); else for (int t = 0; t < 8; ++t) d0[t] = 0;
-    if (live && l + 1 < K) digits_of(a(l + 1), e, s, d1); else for (int t = 0; t < 8; ++t) d1[t] = 0;
-    const int64_t off = (l >> 4) * (int64_t)TH * 16 + in_tile + ((l & 15) >> 3) * 64 + (l & 7);
-    for (int t = 0; t < s; ++t) {
-      __nv_bfloat162 v;
-      v.x = __int2bfloat16_rn(d0[t]);
-      v.y = __int2bfloat16_rn(d1[t]);
-      *reinterpret_cast<__nv_bfloat162*>(base + t * slice_stride + off) = v;
+      for (int u = 0; u < 8; ++u) {
+        const int64_t k = 8 * c + u;
+        if (k < K) mx = max(mx, a(k) & 0x7fffffffffffffffll);
+      }
     }
+  smax[cl][ri] = mx;
+  __syncthreads();
+  if (threadIdx.x < kSplitRows) {
+#pragma unroll 8
+    for (int w = 1; w < kSplitLanes; ++w) mx = max(mx, smax[w][ri]);
+    int e = 0;  // max |a| = f 2^e, f in [0.5, 1): |a| < 2^e
+    if (mx >= (1ll << 52)) e = (int)(mx >> 52) - 1022;
+    else if (mx > 0) frexp(__longlong_as_double(mx), &e);
+    sexp[ri] = e;
+    if (live) (opb ? b_exps : a_exps)[r[6] + row] = e;
   }
+  __syncthreads();
+  const int e = sexp[ri];
+  int64_t slice_stride, row_base;
+  int in_tile = 0;
+  if (TH == 0) {
+    if (!live) return;
+    slice_stride = rows * Kp;
+    row_base = row * Kp;
+  } else {
+    const int64_t rows_p = (rows + TH - 1) / TH * TH;
+    if (row >= rows_p) return;
+    slice_stride = rows_p * Kp;
+    const int rr = (int)(row % TH);
+    row_base = (row / TH) * (Kp / 16) * (int64_t)TH * 16;
+    in_tile = (rr >> 3) * 128 + (rr & 7) * 8;
+  }
+  __nv_bfloat16* dst = (opb ? b_dst : a_dst) + r[5];
+  for (int64_t c = cl; c < Kp / 8; c += kSplitLanes) {
+    uint32_t pk[S][4];
+#pragma unroll
+    for (int u = 0; u < 8; u += 2) {
+      const int64_t k = 8 * c + u;
+      const long long b0 = (live && k < K) ? a(k) : 0ll;
+      const long long b1 = (live && k + 1 < K) ? a(k + 1) : 0ll;
+      uint32_t w0[S], w1[S];
+      digit_words<S>(b0, e, w0);
+      digit_words<S>(b1, e, w1);
+#pragma unroll
+      for (int t = 0; t < S; ++t) pk[t][u >> 1] = __byte_perm(w0[t], w1[t], 0x7632);
+    }
+    const int64_t off =
+        TH == 0 ? row_base + 8 * c : row_base + (c >> 1) * (int64_t)TH * 16 + in_tile + (c & 1) * 64;
+#pragma unroll
+    for (int t = 0; t < S; ++t)
+      *reinterpret_cast<uint4*>(dst + t * slice_stride + off) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
+  }
+}
+
+template <int S>
+int launch_split(const double* a_src, const double* b_src, void* a_dst, void* b_dst, int* a_exps, int* b_exps,
+                 const int64_t* recs, const int32_t* groups, int n_groups, cudaStream_t s) {
+  split_kernel<S><<<n_groups, kSplitThreads, 0, s>>>(a_src, b_src, (__nv_bfloat16*)a_dst,
+                                                                  (__nv_bfloat16*)b_dst, a_exps, b_exps, recs, groups);
+  return check_launch();
 }
 
 // ------------------------------------------------------------------ GEMM
-// Exact conversions built on the integer pipe (GB300 issues FP64 arithmetic at a small
-// fraction of its integer rate): v 2^E for an integer |v| < 2^53 is assembled from the
-// leading-bit position, the mantissa bits and the biased exponent; results outside the
-// normal range go through scalbn.
-__device__ __forceinline__ double int_to_double_scaled(long long v, int E) {
-  if (v == 0) return 0.0;
-  const unsigned long long sgn = v < 0 ? 0x8000000000000000ull : 0ull;
-  const unsigned long long mag = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
-  const int p = 63 - __clzll((long long)mag);  // leading bit; p <= 52 keeps every bit
-  const int be = 1023 + p + E;
-  const unsigned long long frac = (mag << (52 - p)) & 0xfffffffffffffull;
-  if (be >= 1 && be <= 2046) return __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) | frac));
-  return scalbn(__longlong_as_double((long long)(sgn | (1023ull + (unsigned long long)p) << 52 | frac)) , E);
-}
-
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
   const unsigned saddr = (unsigned)__cvta_generic_to_shared(smem);
   const int n = valid ? 16 : 0;
@@ -297,8 +320,8 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm_kernel(const __nv_bflo
     if (((st + 1) % kChunkSteps) == 0 || st + 1 == nsteps) {
       // fold the diagonal sums (exact integers below 2^24 in FP32) into FP64: the weighted
       // sum sum_d acc_d 2^(-7d) is formed exactly in two int64 halves (diagonals 0..3 and
-      // 4..7, each below 2^46) on the integer pipe, and only the two halves are converted,
-      // which keeps the fold off GB300's narrow FP64 pipe
+      // 4..7, each below 2^46) and rounded once (fold_round), on the integer pipe, which
+      // keeps the fold off GB300's narrow FP64 pipe
 #pragma unroll
       for (int i = 0; i < 2; ++i)
 #pragma unroll
@@ -313,7 +336,8 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm_kernel(const __nv_bflo
               else lo += q << (7 * (S - 1 - d));
               acc[d][i][j][v] = 0.f;
             }
-            acc64[i][j][v] += int_to_double_scaled(hi, -21) + int_to_double_scaled(lo, -7 * (S - 1));
+            const double x = fold_round(hi, lo, 7 * (S - 4), -7 * (S - 1));
+            acc64[i][j][v] = st < kChunkSteps ? x : acc64[i][j][v] + x;  // FP64 add only past the first chunk
           }
     }
   }
@@ -347,26 +371,18 @@ int launch_gemm(const void* As, const int* Ae, const void* Bs, const int* Be, do
 
 extern "C" {
 
-int yb_ozaki_split(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs, int max_rows,
-                   int slices_count, void* stream) {
-  if (n_recs == 0 || max_rows == 0) return YB_OK;
-  if (!src || !slices || !exps || !recs || slices_count < 1 || slices_count > 8) return YB_ERR_INVALID;
-  dim3 grid((unsigned)((max_rows + 7) / 8), (unsigned)n_recs);
-  yb::split_rows_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(src, (__nv_bfloat16*)slices, exps, recs,
-                                                                 slices_count);
-  return yb::check_launch();
-}
-
-int yb_ozaki_split_tiled(const double* src, void* slices, int* exps, const int64_t* recs, int n_recs, int max_rows,
-                         int slices_count, int tile_rows, void* stream) {
-  if (n_recs == 0 || max_rows == 0) return YB_OK;
-  if (!src || !slices || !exps || !recs || slices_count < 1 || slices_count > 8) return YB_ERR_INVALID;
-  if (tile_rows != 64 && tile_rows != 128) return YB_ERR_INVALID;
-  const int rows_p = (max_rows + tile_rows - 1) / tile_rows * tile_rows;
-  dim3 grid((unsigned)((rows_p + 7) / 8), (unsigned)n_recs);
-  yb::split_rows_tiled_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(src, (__nv_bfloat16*)slices, exps, recs,
-                                                                       slices_count, tile_rows);
-  return yb::check_launch();
+int yb_ozaki_split(const double* a_src, const double* b_src, void* a_slices, void* b_slices, int* a_exps,
+                   int* b_exps, const int64_t* recs, const int32_t* groups, int n_groups, int slices_count,
+                   void* stream) {
+  if (n_groups == 0) return YB_OK;
+  if (!recs || !groups || n_groups < 0) return YB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (slices_count) {
+    case 6: return yb::launch_split<6>(a_src, b_src, a_slices, b_slices, a_exps, b_exps, recs, groups, n_groups, s);
+    case 7: return yb::launch_split<7>(a_src, b_src, a_slices, b_slices, a_exps, b_exps, recs, groups, n_groups, s);
+    case 8: return yb::launch_split<8>(a_src, b_src, a_slices, b_slices, a_exps, b_exps, recs, groups, n_groups, s);
+    default: return YB_ERR_INVALID;
+  }
 }
 
 int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps, double* c,
@@ -426,24 +442,21 @@ inline int64_t align256(int64_t x) { return (x + 255) & ~(int64_t)255; }
 }  // namespace
 }  // namespace yb
 
-extern "C" int yb_ozaki_dot_static(const double* A, const double* B, double* C, int dtype, const int64_t* a_recs,
-                                   int n_a, int a_rows, const int64_t* b_recs, int n_b, int b_rows,
-                                   const int64_t* bT_tasks, int n_bT_tasks, const int64_t* bT_items, int n_bT_items,
+extern "C" int yb_ozaki_dot_static(const double* A, const double* B, double* C, int dtype,
+                                   const int64_t* split_recs, const int32_t* split_groups, int n_groups,
                                    const int64_t* outs, const int32_t* tiles, int n_tiles, const int64_t* nat_outs,
                                    const int64_t* nat_terms, const int32_t* nat_tiles, int n_nat_tiles,
                                    int slices_count, int64_t a_slice_elems, int64_t b_slice_elems, int64_t a_exp_count,
-                                   int64_t b_exp_count, int64_t bT_elems, void* stream) {
-  if (dtype != YB_F64) return YB_ERR_INVALID;  // the B transposes are sized for 8-byte elements
+                                   int64_t b_exp_count, void* stream) {
+  if (dtype != YB_F64) return YB_ERR_INVALID;  // complex split records are not accepted here
   if (n_tiles == 0 && n_nat_tiles == 0) return YB_OK;
-  if (!A || !B || !C || n_a < 0 || n_b < 0 || n_tiles < 0 || n_nat_tiles < 0) return YB_ERR_INVALID;
-  if (n_tiles > 0 && (!a_recs || !b_recs || !outs || !tiles)) return YB_ERR_INVALID;
+  if (!A || !B || !C || n_groups < 0 || n_tiles < 0 || n_nat_tiles < 0) return YB_ERR_INVALID;
+  if (n_tiles > 0 && (!split_recs || !split_groups || !outs || !tiles)) return YB_ERR_INVALID;
   if (n_nat_tiles > 0 && (!nat_outs || !nat_terms || !nat_tiles)) return YB_ERR_INVALID;
-  if (a_slice_elems < 0 || b_slice_elems < 0 || a_exp_count < 0 || b_exp_count < 0 || bT_elems < 0)
-    return YB_ERR_INVALID;
+  if (a_slice_elems < 0 || b_slice_elems < 0 || a_exp_count < 0 || b_exp_count < 0) return YB_ERR_INVALID;
   const int64_t off_a = 0;
   const int64_t off_b = yb::align256(off_a + 2 * a_slice_elems);
-  const int64_t off_t = yb::align256(off_b + 2 * b_slice_elems);
-  const int64_t off_ea = yb::align256(off_t + 8 * bT_elems);
+  const int64_t off_ea = yb::align256(off_b + 2 * b_slice_elems);
   const int64_t off_eb = yb::align256(off_ea + 4 * a_exp_count);
   const int64_t total = yb::align256(off_eb + 4 * b_exp_count);
   if (total > (int64_t)YB_STATIC_SCRATCH_BYTES) return YB_ERR_TOO_LARGE;
@@ -453,16 +466,10 @@ extern "C" int yb_ozaki_dot_static(const double* A, const double* B, double* C, 
   unsigned char* base = nullptr;
   st = yb::static_scratch(&base);
   if (st != YB_OK) return st;
-  double* bT = reinterpret_cast<double*>(base + off_t);
   int* ea = reinterpret_cast<int*>(base + off_ea);
   int* eb = reinterpret_cast<int*>(base + off_eb);
-  if (n_bT_items > 0) {
-    st = yb_block_copy(B, bT, 8, bT_tasks, n_bT_tasks, bT_items, n_bT_items, stream);
-    if (st != YB_OK) return st;
-  }
-  st = yb_ozaki_split(A, base + off_a, ea, a_recs, n_a, a_rows, slices_count, stream);
-  if (st != YB_OK) return st;
-  st = yb_ozaki_split(bT, base + off_b, eb, b_recs, n_b, b_rows, slices_count, stream);
+  st = yb_ozaki_split(A, B, base + off_a, base + off_b, ea, eb, split_recs, split_groups, n_groups, slices_count,
+                      stream);
   if (st != YB_OK) return st;
   return yb_ozaki_gemm(base + off_a, ea, base + off_b, eb, C, outs, tiles, n_tiles, slices_count, stream);
 }

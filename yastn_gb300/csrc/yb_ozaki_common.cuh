@@ -42,32 +42,47 @@ __device__ __forceinline__ double scale_pow2(double x, int E) {
   return __longlong_as_double(b + ((long long)E << 52));
 }
 
-// Correctly rounded (to nearest, ties to even) double of the integer v times 2^E, on the
-// integer pipe; results outside the normal range go through scalbn.
-__device__ __forceinline__ double i128_to_double_scaled(__int128 v, int E) {
-  if (v == 0) return 0.0;
-  const unsigned long long sgn = v < 0 ? 0x8000000000000000ull : 0ull;
-  unsigned __int128 m = v < 0 ? (unsigned __int128)(-v) : (unsigned __int128)v;
-  const unsigned long long mh = (unsigned long long)(m >> 64), ml = (unsigned long long)m;
-  int p = mh ? 127 - __clzll((long long)mh) : 63 - __clzll((long long)ml);  // leading bit
-  unsigned long long mant;
-  if (p <= 52) {
-    mant = ml << (52 - p);
-  } else {
-    const int sh = p - 52;
-    mant = (unsigned long long)(m >> sh);
-    const unsigned __int128 rem = m & (((unsigned __int128)1 << sh) - 1);
-    const unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
-    if (rem > half || (rem == half && (mant & 1ull))) ++mant;
-    if (mant >> 53) {
-      mant >>= 1;
-      ++p;
-    }
-  }
-  const unsigned long long frac = mant & 0xfffffffffffffull;
-  const int be = 1023 + p + E;
-  if (be >= 1 && be <= 2046) return __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) | frac));
-  return scalbn(__longlong_as_double((long long)(sgn | ((1023ull + (unsigned long long)p) << 52) | frac)), E);
+// Correctly rounded (to nearest, ties to even) double of W 2^E for W = hi 2^L + lo, the exact
+// value of a folded tile element (|hi|, |lo| < 2^46, 6 <= L <= 40), without branches so that
+// the compiler can interleave the conversions of several elements; the integer pipe only.
+// W = H 2^L + r with 0 <= r < 2^L is brought to sign and magnitude Hm 2^L + rm, whose leading
+// bit p gives the shift to 53 bits; every result lies in the normal range for the exponents
+// of the fold (1023 + p + E in [1, 2046]).
+__host__ __device__ __forceinline__ int clz64(unsigned long long x) {
+#ifdef __CUDA_ARCH__
+  return __clzll((long long)x);
+#else
+  return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+__host__ __device__ __forceinline__ double fold_round(long long hi, long long lo, int L, int E) {
+  const unsigned long long mask = (1ull << L) - 1ull;
+  const long long H = hi + (lo >> L);                  // arithmetic shift: floor(lo / 2^L)
+  const unsigned long long r = (unsigned long long)lo & mask;
+  const bool neg = H < 0;
+  const unsigned long long Hm = neg ? (unsigned long long)(-H) - (r != 0 ? 1ull : 0ull) : (unsigned long long)H;
+  const unsigned long long rm = neg ? (0ull - r) & mask : r;
+  const int pH = 63 - clz64(Hm), pr = 63 - clz64(rm);  // -1 for zero
+  const int p = Hm ? pH + L : pr;                       // leading bit of Hm 2^L + rm (-1: zero)
+  const int sh = p > 52 ? p - 52 : 0;                   // bits below the 53 kept (sh < L)
+  unsigned long long V = (Hm << (L - sh)) | (rm >> sh);
+  const unsigned long long rem = rm & ((1ull << sh) - 1ull);
+  const unsigned long long half = sh ? (1ull << (sh - 1)) : 0ull;
+  const unsigned long long up = (rem > half) | ((rem == half) & (V & 1ull) & (sh != 0 ? 1ull : 0ull));
+  V += up;
+  const int carry = (int)(V >> 53);                     // rounded up to 2^53
+  V >>= carry;
+  const int lead = p > 52 ? 52 : p;                     // leading bit of V before the rounding
+  const unsigned long long frac = (lead >= 0 ? (V << (52 - lead)) : 0ull) & 0xfffffffffffffull;
+  const unsigned long long bits = (neg ? 0x8000000000000000ull : 0ull) |
+                                  ((unsigned long long)(1023 + p + carry + E) << 52) | frac;
+  union {
+    unsigned long long u;
+    double d;
+  } cv;
+  cv.u = bits;
+  return p < 0 ? 0.0 : cv.d;
 }
 
 // ------------------------------------------------------------------ tcgen05 / mbarrier
@@ -113,6 +128,12 @@ __device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, ui
 
 __device__ __forceinline__ void tc_commit(uint32_t mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
+}
+
+__device__ __forceinline__ void tc_ld4(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
 }
 
 __device__ __forceinline__ void tc_ld8(uint32_t taddr, uint32_t* r) {

@@ -2,21 +2,24 @@
 // the digit planes that yb_ozaki_split_tiled writes in the tile layout of the UMMA
 // shared-memory descriptors.
 //
-// Each CTA computes a 128 x 64 output tile with three warp roles:
+// A persistent kernel (one CTA per SM) walks its share of the 128 x 64 output tiles (tiles
+// sorted by decreasing K, CTA b taking tiles b, b + G, b + 2G, ...) with three warp roles:
 //  - warp 0 (one thread) streams the S digit tiles of A (128 x 16) and of B (64 x 16) of each
 //    16-long K step into a 4-stage shared-memory ring with cp.async.bulk copies completing on
-//    the stage's mbarrier, refilling a stage as soon as the MMAs that read it have completed;
+//    the stage's mbarrier, refilling a stage as soon as the MMAs that read it have completed,
+//    straight on into the next tile's steps;
 //  - warp 1 (one thread) issues the S(S+1)/2 tcgen05.mma (M=128, N=64, K=16, BF16 -> FP32) of a
 //    step into the S digit-diagonal accumulators in tensor memory (S x 64 of the 512 TMEM
 //    columns) and frees the stage with tcgen05.commit;
-//  - warps 2-5 (TMEM lane quarters 2, 3, 0, 1) read the accumulators back at the end of every
-//    400-long K chunk (exact FP32 integer sums), combine the diagonals exactly into a 128-bit
-//    integer on the integer pipe, round it once to FP64 into the tile's FP64 accumulators
-//    (bit-identical to the mma.sync kernel's fold), and write the tile.
-// Loads and MMAs are issued by different warps, so the copies of later steps proceed while a
-// step's MMAs run. Every wait is bounded; a CTA that gives up records the status word of
-// yb_ozaki_device_error, waits (bounded) for its copies and MMAs, frees its tensor memory and
-// writes nothing.
+//  - 16 fold warps (4 per TMEM lane quarter, 16 columns each) read the accumulators back at
+//    the end of every 400-long K chunk (exact FP32 integer sums), combine the diagonals exactly
+//    into a 128-bit integer on the integer pipe, round it once to FP64 into the tile's FP64
+//    accumulators (bit-identical to the mma.sync kernel's fold), release the tensor memory to
+//    the next chunk's MMAs and, after a tile's last chunk, write the tile from registers while
+//    the next tile's MMAs run. Warps whose rows or columns lie wholly outside the sector (the
+//    padding of small sectors) skip their reads and folds.
+// Every wait is bounded; a CTA that gives up records the status word of yb_ozaki_device_error,
+// waits (bounded) for its copies and MMAs, frees its tensor memory and stops writing.
 #include "yb_ozaki_common.cuh"
 
 namespace yb {
@@ -24,9 +27,11 @@ namespace {
 using namespace oz;
 
 constexpr int kM = 128, kN = 64, kK = 16, kStages = 4;
-constexpr int kFold = 128;              // fold / epilogue threads (warps 2-5)
-constexpr int kThreadsT = 64 + kFold;   // producer warp, MMA warp, fold warps
-constexpr int kChunkSteps = 25;         // 400-long K chunks: exact FP32 diagonal sums
+constexpr int kFoldWarps = 16;              // 4 per TMEM lane quarter
+constexpr int kFoldCols = kN / (kFoldWarps / 4);  // 16 columns per fold warp
+constexpr int kFold = 32 * kFoldWarps;      // fold / epilogue threads (warps 2-17)
+constexpr int kThreadsT = 64 + kFold;       // producer warp, MMA warp, fold warps
+constexpr int kChunkSteps = 25;             // 400-long K chunks: exact FP32 diagonal sums
 constexpr long long kSpin = 1ll << 24;
 constexpr uint32_t kATile = kM * kK * 2;  // one slice's 128 x 16 digit tile, bytes
 constexpr uint32_t kBTile = kN * kK * 2;  // 64 x 16
@@ -36,7 +41,6 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_
                "l"(src), "r"(bytes), "r"(mbar)
                : "memory");
 }
-__device__ __forceinline__ void fold_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
 
 // out record (16 int64): [0] c offset [1] m [2] n [3] ldc [4] A slices offset (tile layout)
 // [5] A exponents offset [6] B slices offset (tile layout) [7] B exponents offset [8] K [9] Kp
@@ -45,7 +49,8 @@ template <int S>
 __global__ void __launch_bounds__(kThreadsT, 1)
     ozaki_gemm_tc_kernel(const __nv_bfloat16* __restrict__ As, const int* __restrict__ Ae,
                          const __nv_bfloat16* __restrict__ Bs, const int* __restrict__ Be, double* __restrict__ C,
-                         const int64_t* __restrict__ outs, const int32_t* __restrict__ tiles, int* __restrict__ err) {
+                         const int64_t* __restrict__ outs, const int32_t* __restrict__ tiles, int n_tiles,
+                         int* __restrict__ err) {
   constexpr uint32_t kStage = S * (kATile + kBTile);
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint32_t tmem_slot;
@@ -53,16 +58,8 @@ __global__ void __launch_bounds__(kThreadsT, 1)
   __shared__ int failed_s;
   volatile int* failed = &failed_s;
 
-  const int4 tl = reinterpret_cast<const int4*>(tiles)[blockIdx.x];
-  const int64_t* o = outs + (int64_t)tl.x * 16;
-  const int64_t c_off = o[0], m = o[1], n = o[2], ldc = o[3];
-  const int64_t a_sl = o[4], a_ex = o[5], b_sl = o[6], b_ex = o[7], Kp = o[9];
-  const int64_t ccs = o[10] > 0 ? o[10] : 1;
-  const int64_t row0 = (int64_t)tl.y * kM, col0 = (int64_t)tl.z * kN;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t sbase = smem_u32(smem);
-  const int64_t ksteps = Kp / kK;
-  const int64_t nchunks = (ksteps + kChunkSteps - 1) / kChunkSteps;
 
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -88,32 +85,39 @@ __global__ void __launch_bounds__(kThreadsT, 1)
   if (warp == 0) {
     // ---------------------------------------------------------------- producer
     if (lane == 0) {
-      // digit planes in tile layout: per slice, (row tile, K step) blocks of 128 x 16 (A) / 64 x 16 (B)
-      const int64_t a_slice = (m + kM - 1) / kM * kM * Kp, b_slice = (n + kN - 1) / kN * kN * Kp;
-      const __nv_bfloat16* a_tiles = As + a_sl + (int64_t)tl.y * ksteps * (kM * kK);
-      const __nv_bfloat16* b_tiles = Bs + b_sl + (int64_t)tl.z * ksteps * (kN * kK);
-      int64_t issued = 0;
-      for (int64_t st = 0; st < ksteps; ++st) {
-        const int stage = (int)(st % kStages);
-        if (st >= kStages) {  // the MMAs that read this stage's previous contents have completed
-          if (*failed || !mbar_wait(smem_u32(&empty[stage]), (uint32_t)(((st / kStages) - 1) & 1), kSpin)) {
-            *failed = 1;
-            atomicExch(err, 1);
-            break;
+      int64_t gs = 0;  // K steps issued by this CTA (all its tiles): the ring position
+      bool ok = true;
+      for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+        const int4 tl = reinterpret_cast<const int4*>(tiles)[t];
+        const int64_t* o = outs + (int64_t)tl.x * 16;
+        const int64_t m = o[1], n = o[2], a_sl = o[4], b_sl = o[6], Kp = o[9];
+        const int64_t ksteps = Kp / kK;
+        // digit planes in tile layout: per slice, (row tile, K step) blocks of 128 x 16 (A) / 64 x 16 (B)
+        const int64_t a_slice = (m + kM - 1) / kM * kM * Kp, b_slice = (n + kN - 1) / kN * kN * Kp;
+        const __nv_bfloat16* a_tiles = As + a_sl + (int64_t)tl.y * ksteps * (kM * kK);
+        const __nv_bfloat16* b_tiles = Bs + b_sl + (int64_t)tl.z * ksteps * (kN * kK);
+        for (int64_t st = 0; st < ksteps; ++st, ++gs) {
+          const int stage = (int)(gs % kStages);
+          if (gs >= kStages) {  // the MMAs that read this stage's previous contents have completed
+            if (*failed || !mbar_wait(smem_u32(&empty[stage]), (uint32_t)(((gs / kStages) - 1) & 1), kSpin)) {
+              *failed = 1;
+              atomicExch(err, 1);
+              ok = false;
+              break;
+            }
+          }
+          const uint32_t fb = smem_u32(&full[stage]);
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(kStage) : "memory");
+          const uint32_t d0 = sbase + (uint32_t)stage * kStage;
+          for (int s = 0; s < S; ++s) {
+            bulk_load(d0 + s * kATile, a_tiles + s * a_slice + st * (kM * kK), kATile, fb);
+            bulk_load(d0 + S * kATile + s * kBTile, b_tiles + s * b_slice + st * (kN * kK), kBTile, fb);
           }
         }
-        const uint32_t fb = smem_u32(&full[stage]);
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(kStage) : "memory");
-        const uint32_t d0 = sbase + (uint32_t)stage * kStage;
-        for (int t = 0; t < S; ++t) {
-          bulk_load(d0 + t * kATile, a_tiles + t * a_slice + st * (kM * kK), kATile, fb);
-          bulk_load(d0 + S * kATile + t * kBTile, b_tiles + t * b_slice + st * (kN * kK), kBTile, fb);
-        }
-        issued = st + 1;
       }
       // no copy may still be landing in shared memory when the CTA exits: the last issued
       // step of each stage is that stage's latest phase
-      for (int64_t j = max((int64_t)0, issued - kStages); j < issued; ++j)
+      for (int64_t j = max((int64_t)0, gs - kStages); j < gs; ++j)
         if (!mbar_wait(smem_u32(&full[j % kStages]), (uint32_t)((j / kStages) & 1), kSpin)) atomicExch(err, 1);
     }
     __syncwarp();
@@ -123,30 +127,37 @@ __global__ void __launch_bounds__(kThreadsT, 1)
       const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN >> 3) << 17) |
                              ((uint32_t)(kM >> 4) << 24);  // F32 accumulate, BF16 A/B, K-major, N=64, M=128
       bool ok = true;
-      for (int64_t ch = 0; ch < nchunks && ok; ++ch) {
-        if (ch > 0) {  // the previous chunk's fold has read the accumulators this chunk overwrites
-          if (!mbar_wait(smem_u32(&tfree), (uint32_t)((ch - 1) & 1), kSpin)) { ok = false; break; }
-          asm volatile("tcgen05.fence::after_thread_sync;");
-        }
-        const int64_t s0 = ch * kChunkSteps, s1 = min(ksteps, s0 + kChunkSteps);
-        for (int64_t st = s0; st < s1; ++st) {
-          const int stage = (int)(st % kStages);
-          if (*failed || !mbar_wait(smem_u32(&full[stage]), (uint32_t)((st / kStages) & 1), kSpin)) {
-            ok = false;
-            break;
+      int64_t gs = 0, gch = 0;  // steps and chunks of this CTA
+      for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+        const int4 tl = reinterpret_cast<const int4*>(tiles)[t];
+        const int64_t ksteps = outs[(int64_t)tl.x * 16 + 9] / kK;
+        const int64_t nchunks = (ksteps + kChunkSteps - 1) / kChunkSteps;
+        for (int64_t ch = 0; ch < nchunks && ok; ++ch, ++gch) {
+          if (gch > 0) {  // the previous chunk's fold has read the accumulators this chunk overwrites
+            if (*failed || !mbar_wait(smem_u32(&tfree), (uint32_t)((gch - 1) & 1), kSpin)) { ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;");
           }
-          asm volatile("tcgen05.fence::after_thread_sync;");
-          const uint32_t a0 = sbase + (uint32_t)stage * kStage, b0 = a0 + S * kATile;
+          const int64_t s1 = min(ksteps, (ch + 1) * kChunkSteps);
+          for (int64_t st = ch * kChunkSteps; st < s1; ++st, ++gs) {
+            const int stage = (int)(gs % kStages);
+            if (*failed || !mbar_wait(smem_u32(&full[stage]), (uint32_t)((gs / kStages) & 1), kSpin)) {
+              ok = false;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t a0 = sbase + (uint32_t)stage * kStage, b0 = a0 + S * kATile;
+            const bool first = st == ch * kChunkSteps;
 #pragma unroll
-          for (int ta = 0; ta < S; ++ta)
+            for (int ta = 0; ta < S; ++ta)
 #pragma unroll
-            for (int tb = 0; tb < S - ta; ++tb)
-              tc_mma(tmem + (uint32_t)((ta + tb) * kN), umma_desc(a0 + ta * kATile), umma_desc(b0 + tb * kBTile), idesc,
-                     (st == s0 && ta == 0) ? 0u : 1u);
-          tc_commit(smem_u32(&empty[stage]));
+              for (int tb = 0; tb < S - ta; ++tb)
+                tc_mma(tmem + (uint32_t)((ta + tb) * kN), umma_desc(a0 + ta * kATile), umma_desc(b0 + tb * kBTile),
+                       idesc, (first && ta == 0) ? 0u : 1u);
+            tc_commit(smem_u32(&empty[stage]));
+          }
+          if (!ok) break;
+          tc_commit(smem_u32(&accb));  // this chunk's accumulators are complete once its MMAs are
         }
-        if (!ok) break;
-        tc_commit(smem_u32(&accb));  // this chunk's accumulators are complete once its MMAs are
       }
       if (!ok) {
         *failed = 1;
@@ -159,65 +170,72 @@ __global__ void __launch_bounds__(kThreadsT, 1)
     __syncwarp();
   } else {
     // ---------------------------------------------------------------- fold and store
-    const int f = tid - 64;      // 0..127
-    const int q = warp & 3;      // TMEM lane quarter of this warp
-    double acc[kN];
-#pragma unroll
-    for (int j = 0; j < kN; ++j) acc[j] = 0.0;
+    const int q = warp & 3;             // TMEM lane quarter of this warp
+    const int cg = (warp - 2) >> 2;     // its 16-column group
+    const int r = 32 * q + lane;        // tile row of this thread
+    int64_t gch = 0;
     bool ok = true;
-    for (int64_t ch = 0; ch < nchunks; ++ch) {
-      if (*failed || !mbar_wait(smem_u32(&accb), (uint32_t)(ch & 1), kSpin)) {
-        ok = false;
-        break;
-      }
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      // exact fold: the diagonal sums are integers below 2^24 in FP32; their weighted sum
-      // sum_d q_d 2^{7(S-1-d)} is formed in two int64 halves and one 128-bit integer, then
-      // rounded once to FP64 (the same rounding as the mma.sync kernel's fold)
+    for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+      const int4 tl = reinterpret_cast<const int4*>(tiles)[t];
+      const int64_t* o = outs + (int64_t)tl.x * 16;
+      const int64_t c_off = o[0], m = o[1], n = o[2], ldc = o[3], a_ex = o[5], b_ex = o[7], Kp = o[9];
+      const int64_t ccs = o[10] > 0 ? o[10] : 1;
+      const int64_t row0 = (int64_t)tl.y * kM, col0 = (int64_t)tl.z * kN + kFoldCols * cg;
+      const int64_t nchunks = (Kp / kK + kChunkSteps - 1) / kChunkSteps;
+      // warps wholly in the padding of a small sector skip the reads and the fold
+      const bool busy = (row0 + 32 * q < m) && (col0 < n);
+      double acc[kFoldCols];
+      for (int64_t ch = 0; ch < nchunks; ++ch, ++gch) {
+        if (*failed || !mbar_wait(smem_u32(&accb), (uint32_t)(gch & 1), kSpin)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        if (busy) {
+          // exact fold: the diagonal sums are integers below 2^24 in FP32; their weighted sum
+          // sum_d q_d 2^{7(S-1-d)} = hi 2^{7(S-4)} + lo is formed in two int64 halves and
+          // rounded once to FP64 (the same rounding as the mma.sync kernel's fold). The S
+          // diagonals of 4 columns are read with one wait.
 #pragma unroll
-      for (int cb = 0; cb < kN / 8; ++cb) {
-        long long hi[8], lo[8];
+          for (int cb = 0; cb < kFoldCols / 4; ++cb) {
+            uint32_t v[S][4];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) hi[j] = lo[j] = 0;
+            for (int d = 0; d < S; ++d)
+              tc_ld4(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(d * kN + kFoldCols * cg + cb * 4), v[d]);
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-        for (int d = 0; d < S; ++d) {
-          uint32_t v[8];
-          tc_ld8(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(d * kN + cb * 8), v);
-          asm volatile("tcgen05.wait::ld.sync.aligned;");
+            for (int j = 0; j < 4; ++j) {
+              long long hi = 0, lo = 0;
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const long long qv = (long long)__float2int_rn(__uint_as_float(v[j]));
-            if (d < 4) hi[j] += qv << (7 * (3 - d));
-            else lo[j] += qv << (7 * (S - 1 - d));
+              for (int d = 0; d < S; ++d) {
+                const long long qv = (long long)__float2int_rn(__uint_as_float(v[d][j]));
+                if (d < 4) hi += qv << (7 * (3 - d));
+                else lo += qv << (7 * (S - 1 - d));
+              }
+              const double x = fold_round(hi, lo, 7 * (S - 4), -7 * (S - 1));
+              acc[cb * 4 + j] = ch == 0 ? x : acc[cb * 4 + j] + x;
+            }
           }
         }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        mbar_arrive(smem_u32(&tfree));
+      }
+      if (!ok) break;
+      // the tile, straight from registers (the next tile's MMAs proceed meanwhile)
+      const int64_t gi = row0 + r;
+      if (busy && gi < m) {
+        const int ea = Ae[a_ex + gi] - 14;
+        double* crow = C + c_off + gi * ldc;
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const __int128 tot = (__int128)hi[j] * ((__int128)1 << (7 * (S - 4))) + (__int128)lo[j];
-          const double t = i128_to_double_scaled(tot, -7 * (S - 1));
-          acc[cb * 8 + j] = ch == 0 ? t : acc[cb * 8 + j] + t;
+        for (int j = 0; j < kFoldCols; ++j) {
+          const int64_t gj = col0 + j;
+          if (gj < n) crow[gj * ccs] = scale_pow2(acc[j], ea + Be[b_ex + gj]);
         }
       }
-      asm volatile("tcgen05.fence::before_thread_sync;");
-      mbar_arrive(smem_u32(&tfree));
     }
     if (!ok) {
       *failed = 1;
       atomicExch(err, 1);
-    }
-    fold_bar();  // every fold thread is past its last read: the stages are free
-    if (!*failed) {
-      double* tileC = reinterpret_cast<double*>(smem);
-      const int r = 32 * q + lane;
-#pragma unroll
-      for (int j = 0; j < kN; ++j) tileC[r * (kN + 1) + j] = acc[j];
-      fold_bar();
-      for (int e = f; e < kM * kN; e += kFold) {
-        const int rr = e / kN, cc = e % kN;
-        const int64_t gi = row0 + rr, gj = col0 + cc;
-        if (gi < m && gj < n)
-          C[c_off + gi * ldc + gj * ccs] = scale_pow2(tileC[rr * (kN + 1) + cc], Ae[a_ex + gi] + Be[b_ex + gj] - 14);
-      }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -225,17 +243,26 @@ __global__ void __launch_bounds__(kThreadsT, 1)
   if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
 }
 
+int sm_count() {
+  static int sms[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  if (sms[dev] == 0) cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+  return sms[dev];
+}
+
 template <int S>
 int launch_gemm_tc(const void* As, const int* Ae, const void* Bs, const int* Be, double* C, const int64_t* outs,
                    const int32_t* tiles, int n_tiles, int* err, cudaStream_t s) {
   const size_t smem = (size_t)kStages * S * (kATile + kBTile);
-  static_assert((size_t)kM * (kN + 1) * 8 <= (size_t)kStages * 6 * (kATile + kBTile),
-                "epilogue tile must fit in the stage buffers");
   auto kern = ozaki_gemm_tc_kernel<S>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
-  kern<<<n_tiles, kThreadsT, smem, s>>>((const __nv_bfloat16*)As, Ae, (const __nv_bfloat16*)Bs, Be, C, outs, tiles,
-                                        err);
+  const int sms = sm_count();
+  if (sms <= 0) return YB_ERR_CUDA;
+  const int grid = n_tiles < sms ? n_tiles : sms;  // one CTA per SM (its shared memory and all 512 TMEM columns)
+  kern<<<grid, kThreadsT, smem, s>>>((const __nv_bfloat16*)As, Ae, (const __nv_bfloat16*)Bs, Be, C, outs, tiles,
+                                     n_tiles, err);
   return check_launch();
 }
 

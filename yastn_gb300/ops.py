@@ -123,8 +123,8 @@ def run_gemm(plan, a, b, c, alpha=1.0, beta=0.0):
     code = _dtype_code(c.dtype)
     if len(plan.tiles):
         do, dtm, dti = _dev(plan, 'gemm', (plan.outs, plan.terms, plan.tiles), a.device)
-        N.call('yb_grouped_gemm', _ptr(a), _ptr(b), _ptr(c), code, _ptr(do), _ptr(dtm), _ptr(dti),
-               len(plan.tiles), float(alpha), float(beta), _stream())
+        N.call('yb_grouped_gemm_short' if plan.all_short else 'yb_grouped_gemm', _ptr(a), _ptr(b), _ptr(c), code,
+               _ptr(do), _ptr(dtm), _ptr(dti), len(plan.tiles), float(alpha), float(beta), _stream())
     sp = plan.split
     if sp is not None:
         # split-K: chunk products into a workspace, then the ordered sum into C
@@ -170,17 +170,37 @@ def dot_ozaki(A, B, meta_dot, Dsize, slices=OZAKI_SLICES):
     A, B = promote(_check(A, 'A'), _check(B, 'B'))
     plan = P.ozaki_dot_plan(meta_dot, slices, A.is_complex())
     out = (torch.empty if plan.covered == Dsize else torch.zeros)(Dsize, dtype=A.dtype, device=A.device)
-    run_gemm(plan.native, A, B, out)  # short (K < 16) and skinny sectors: native FP64
     if len(plan.tiles) == 0:
-        return out
+        return run_gemm(plan.native, A, B, out)  # short (K < 16) and skinny sectors: native FP64
     if OZAKI_TC[0] is not None:
         tc = OZAKI_TC[0]
     else:
         if getattr(plan, 'tuned_tc', None) is None:
             plan.tuned_tc = _autotune_ozaki(plan, A, B, out, slices)
         tc = plan.tuned_tc
+    # the native sectors (disjoint outputs) run on a second stream beside the split and the
+    # emulated GEMM, and the current stream waits for them (a fork and join inside a CUDA graph)
+    fork = len(plan.native.tiles) > 0 or plan.native.split is not None
+    if fork:
+        main, side = torch.cuda.current_stream(A.device), _side_stream(A.device)
+        side.wait_stream(main)
+        with torch.cuda.stream(side):
+            run_gemm(plan.native, A, B, out)
     _ozaki_run(plan, A, B, out, slices, tc)
+    if fork:
+        main.wait_stream(side)
     return out
+
+
+_SIDE = {}
+
+
+def _side_stream(device):
+    """The second stream of a device (created once; independent work of one call runs on it)."""
+    s = _SIDE.get(device.index)
+    if s is None:
+        s = _SIDE[device.index] = torch.cuda.Stream(device=device)
+    return s
 
 
 def _autotune_ozaki(plan, A, B, out, slices):
@@ -202,31 +222,25 @@ def _autotune_ozaki(plan, A, B, out, slices):
 
 
 def _ozaki_run(plan, A, B, out, slices, tc):
+    """Both operands split by one yb_ozaki_split launch (B's blocks read by columns in
+    place), then the emulated GEMM: tcgen05 (tile layout) or mma.sync (digit planes)."""
     dev = A.device
     st = _stream()
-    bT = run_copy(plan.bT, B, torch.empty(max(plan.bT_size, 1), dtype=B.dtype, device=dev))
     a_ex = torch.empty(max(plan.a_exps, 1), dtype=torch.int32, device=dev)
     b_ex = torch.empty(max(plan.b_exps, 1), dtype=torch.int32, device=dev)
     if tc:
-        # digit planes in the tile layout of the tcgen05 kernel, then the tensor-core GEMM
-        dar, dbr, dout, dtl = _dev(plan, 'ozaki_tc', (plan.a_recs_tc, plan.b_recs_tc, plan.outs_tc, plan.tiles_tc),
-                                   dev)
-        a_sl = torch.empty(plan.a_size_tc, dtype=torch.bfloat16, device=dev)
-        b_sl = torch.empty(plan.b_size_tc, dtype=torch.bfloat16, device=dev)
-        N.call('yb_ozaki_split_tiled', _ptr(A), _ptr(a_sl), _ptr(a_ex), _ptr(dar), len(plan.a_recs), plan.a_rows,
-               slices, P.OZAKI_TC_M, st)
-        N.call('yb_ozaki_split_tiled', _ptr(bT), _ptr(b_sl), _ptr(b_ex), _ptr(dbr), len(plan.b_recs), plan.b_rows,
-               slices, P.OZAKI_TC_N, st)
-        N.call('yb_ozaki_gemm_tc', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
-               len(plan.tiles_tc), slices, st)
-        return
-    dar, dbr, dout, dtl = _dev(plan, 'ozaki', (plan.a_recs, plan.b_recs, plan.outs, plan.tiles), dev)
-    a_sl = torch.empty(plan.a_size, dtype=torch.bfloat16, device=dev)
-    b_sl = torch.empty(plan.b_size, dtype=torch.bfloat16, device=dev)
-    N.call('yb_ozaki_split', _ptr(A), _ptr(a_sl), _ptr(a_ex), _ptr(dar), len(plan.a_recs), plan.a_rows, slices, st)
-    N.call('yb_ozaki_split', _ptr(bT), _ptr(b_sl), _ptr(b_ex), _ptr(dbr), len(plan.b_recs), plan.b_rows, slices, st)
-    N.call('yb_ozaki_gemm', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
-           len(plan.tiles), slices, st)
+        key, arrs = 'ozaki_tc', (plan.split_recs_tc, plan.split_groups_tc, plan.outs_tc, plan.tiles_tc)
+        asz, bsz, n_tiles, gemm = plan.a_size_tc, plan.b_size_tc, len(plan.tiles_tc), 'yb_ozaki_gemm_tc'
+    else:
+        key, arrs = 'ozaki', (plan.split_recs, plan.split_groups, plan.outs, plan.tiles)
+        asz, bsz, n_tiles, gemm = plan.a_size, plan.b_size, len(plan.tiles), 'yb_ozaki_gemm'
+    drec, dgrp, dout, dtl = _dev(plan, key, arrs, dev)
+    a_sl = torch.empty(max(asz, 1), dtype=torch.bfloat16, device=dev)
+    b_sl = torch.empty(max(bsz, 1), dtype=torch.bfloat16, device=dev)
+    N.call('yb_ozaki_split', _ptr(A), _ptr(B), _ptr(a_sl), _ptr(b_sl), _ptr(a_ex), _ptr(b_ex), _ptr(drec),
+           _ptr(dgrp), len(arrs[1]), slices, st)
+    N.call(gemm, _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl), n_tiles, slices,
+           st)
 
 
 def ozaki_device_error(reset=True):
