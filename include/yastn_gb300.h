@@ -175,14 +175,17 @@ int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices,
  * yb_ozaki_split in the tile layout (128 rows for A, 64 for B; output records [4], [6] = the
  * A / B slice-0 offsets in that layout); tiles are (output, tile row, tile col, 0) of 128 rows
  * x 64 columns. A persistent kernel, one CTA per SM, each walking its share of the tiles:
+ * with cta_tiles = NULL CTA b takes tiles b, b + G, ... (G = min(n_tiles, SMs)); otherwise
+ * the tiles are grouped by CTA and CTA b takes [cta_tiles[b], cta_tiles[b+1]) of n_ctas CTAs
+ * (n_ctas <= the SM count, else YB_ERR_INVALID).
  * one warp streams the digit tiles (cp.async.bulk into a 4-stage ring), one issues the
  * tcgen05.mma into the digit-diagonal accumulators in tensor memory, sixteen fold the
  * accumulators exactly and write the tile (the same bits as yb_ozaki_gemm) while the next
  * tile's MMAs run. A CTA that gives up on a bounded wait stops writing and sets the status
  * word read by yb_ozaki_device_error. */
 int yb_ozaki_gemm_tc(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps,
-                     double* c, const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
-                     void* stream);
+                     double* c, const int64_t* outs, const int32_t* tiles, int n_tiles,
+                     const int32_t* cta_tiles, int n_ctas, int slices_count, void* stream);
 /* yb_ozaki_device_error: copies the tcgen05 kernel's status word to *out (0: no failure),
  * synchronising the stream, and clears it when reset != 0. */
 int yb_ozaki_device_error(int* out, int reset, void* stream);

@@ -860,3 +860,23 @@ def test_ozaki_split_model_reconstructs_the_operands():
                     assert np.all(np.abs(rebuilt - x) <= np.ldexp(0.5 + 1e-9, (e - 7 * s)[:, None]))
                     lead = dig[op][dst + off]
                     assert np.all(np.abs(lead) <= 128)
+
+
+def test_ozaki_tc_schedule_covers_tiles_once_and_balances():
+    """The tcgen05 kernel's per-CTA schedule: every tile exactly once, CTA ranges contiguous,
+    no CTA above the SM count, and the largest CTA load within one tile of the balanced mean
+    (longest-processing-time assignment) on the DMRG workload's two emulated dots."""
+    from yastn_gb300.workloads import Heff2Workload
+    dots = [c['args'][2] for c in Heff2Workload().calls if c['fn'] == 'dot']
+    for meta in (dots[0], dots[3]):
+        plan = P.ozaki_dot_plan(meta, 8)
+        for sms in (152, 37):
+            tiles, offs = P.ozaki_tc_schedule(plan, sms)
+            assert offs[0] == 0 and offs[-1] == len(plan.tiles_tc) and len(offs) == min(sms, len(plan.tiles_tc)) + 1
+            assert np.all(np.diff(offs) >= 0)
+            key = lambda a: sorted(map(tuple, a.tolist()))
+            assert key(tiles) == key(plan.tiles_tc)
+            steps = lambda t: int(plan.outs_tc[t[0]][9]) // 16 + P.OZ_TC_FOLD_STEPS
+            loads = [sum(steps(t) for t in tiles[offs[b]:offs[b + 1]]) for b in range(len(offs) - 1)]
+            biggest = max(steps(t) for t in tiles)
+            assert max(loads) <= sum(loads) / len(loads) + biggest

@@ -550,6 +550,42 @@ def _split_layout(blocks, s, th_a, th_b):
     return recs, groups, size[0], size[1], nex[0], nex[1], where
 
 
+OZ_TC_FOLD_STEPS = 6  # fold + write of a full 128 x 64 tile, in K-step units of the tcgen05 kernel
+
+
+def ozaki_tc_schedule(plan, n_ctas):
+    """Tiles of the tcgen05 kernel grouped by CTA (longest processing time first: each tile,
+    by decreasing cost, to the least loaded CTA; cost = K steps + the fold of its valid
+    elements). Returns (tiles reordered, int32 offsets of the n_ctas + 1 CTA ranges)."""
+    key = ('tc_sched', n_ctas)
+    got = plan._dev.get(key)
+    if got is not None:
+        return got
+    import heapq
+    tiles = plan.tiles_tc
+    n_ctas = max(1, min(n_ctas, len(tiles)))
+    cost = []
+    for i, (oi, tr, tc, _) in enumerate(tiles):
+        o = plan.outs_tc[oi]
+        m, n, Kp = int(o[1]), int(o[2]), int(o[9])
+        steps = Kp // 16
+        chunks = -(-steps // 25)
+        valid = min(OZAKI_TC_M, m - OZAKI_TC_M * int(tr)) * min(OZAKI_TC_N, n - OZAKI_TC_N * int(tc))
+        cost.append((steps + OZ_TC_FOLD_STEPS * chunks * valid / (OZAKI_TC_M * OZAKI_TC_N), i))
+    cost.sort(reverse=True)
+    heap = [(0.0, b) for b in range(n_ctas)]
+    lists = [[] for _ in range(n_ctas)]
+    for c, i in cost:
+        load, b = heapq.heappop(heap)
+        lists[b].append(i)
+        heapq.heappush(heap, (load + c, b))
+    order = [i for lst in lists for i in lst]
+    offs = np.cumsum([0] + [len(lst) for lst in lists]).astype(np.int32)
+    got = (np.ascontiguousarray(tiles[order]), offs)
+    plan._dev[key] = got
+    return got
+
+
 def ozaki_dot_plan(meta_dot, s, cplx=False):
     """C[slc] = A[sla] @ B[slb] with A rows / B columns split into ``s`` BF16 digit slices.
 

@@ -21,6 +21,7 @@
 // mma.sync.m16n8k16 tiles), K-step 16 staged in shared memory with cp.async (double
 // buffered, rows padded to 48 bytes so ldmatrix is bank-conflict free).
 #include <atomic>
+#include <type_traits>
 #include <mutex>
 #include "yb_ozaki_common.cuh"
 
@@ -97,27 +98,32 @@ __device__ __forceinline__ void digit_words(long long bits, int e, uint32_t* w) 
   }
 }
 
-struct SplitSrc {
-  const long long* base;  // element (row, 0)
-  int64_t ks, half;
-  int mode;
-  __device__ __forceinline__ long long operator()(int64_t k) const {
-    if (mode == 0) return __ldg(base + k * ks);
-    const bool first = k < half;
-    const long long* c = base + 2 * (first ? k : k - half) * ks;
-    const long long re = __ldg(c), im = __ldg(c + 1);
-    if (mode == 1) return first ? re : im;
-    if (mode == 2) return first ? re : (long long)((unsigned long long)im ^ 0x8000000000000000ull);
-    return first ? im : re;
-  }
-};
 
 // One CTA per 8 rows of a record (groups: int32 pairs (record, first row)); the 256 threads
 // are 8 rows x 32 chunk lanes, each lane taking the row's 8-long K chunks lane, lane + 32, ...:
 // the row maxima first (exponents), then the digits, each chunk stored as one 16-byte word
-// per slice (8 consecutive rows of a tile-layout block are 128 contiguous bytes).
+// per slice (8 consecutive rows of a tile-layout block are 128 contiguous bytes). Real rows
+// with at most two chunks per lane (K <= 512) keep their values in registers between the two
+// passes; a group wholly in the row padding of the tile layout only writes zeros.
 template <int S>
-__global__ void __launch_bounds__(kSplitThreads) split_kernel(
+__device__ __forceinline__ void store_chunk(__nv_bfloat16* dst, int64_t slice_stride, int64_t off, const long long* x,
+                                           int e) {
+  uint32_t pk[S][4];
+#pragma unroll
+  for (int u = 0; u < 8; u += 2) {
+    uint32_t w0[S], w1[S];
+    digit_words<S>(x[u], e, w0);
+    digit_words<S>(x[u + 1], e, w1);
+#pragma unroll
+    for (int t = 0; t < S; ++t) pk[t][u >> 1] = __byte_perm(w0[t], w1[t], 0x7632);
+  }
+#pragma unroll
+  for (int t = 0; t < S; ++t)
+    *reinterpret_cast<uint4*>(dst + t * slice_stride + off) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
+}
+
+template <int S>
+__global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(
     const double* __restrict__ a_src, const double* __restrict__ b_src, __nv_bfloat16* __restrict__ a_dst,
     __nv_bfloat16* __restrict__ b_dst, int* __restrict__ a_exps, int* __restrict__ b_exps,
     const int64_t* __restrict__ recs, const int32_t* __restrict__ groups) {
@@ -132,68 +138,104 @@ __global__ void __launch_bounds__(kSplitThreads) split_kernel(
   const int ri = threadIdx.x % kSplitRows, cl = threadIdx.x / kSplitRows;
   const int64_t row = (int64_t)g.y + ri;
   const bool live = row < rows;
-  SplitSrc a;
-  a.mode = (int)r[4];
-  a.ks = r[8];
-  a.half = K / 2;
-  a.base = reinterpret_cast<const long long*>(opb ? b_src : a_src) +
-           (a.mode == 0 ? 1 : 2) * (r[0] + (live ? row : 0) * r[3]);
-  const int64_t kc = (K + 7) / 8;  // chunks holding data
-  long long mx = 0;
-  if (live)
-    for (int64_t c = cl; c < kc; c += kSplitLanes) {
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int64_t k = 8 * c + u;
-        if (k < K) mx = max(mx, a(k) & 0x7fffffffffffffffll);
-      }
-    }
-  smax[cl][ri] = mx;
-  __syncthreads();
-  if (threadIdx.x < kSplitRows) {
-#pragma unroll 8
-    for (int w = 1; w < kSplitLanes; ++w) mx = max(mx, smax[w][ri]);
-    int e = 0;  // max |a| = f 2^e, f in [0.5, 1): |a| < 2^e
-    if (mx >= (1ll << 52)) e = (int)(mx >> 52) - 1022;
-    else if (mx > 0) frexp(__longlong_as_double(mx), &e);
-    sexp[ri] = e;
-    if (live) (opb ? b_exps : a_exps)[r[6] + row] = e;
-  }
-  __syncthreads();
-  const int e = sexp[ri];
+  const int64_t nck = Kp / 8;  // chunks of the padded row
+  // destination of chunk c of this row
   int64_t slice_stride, row_base;
   int in_tile = 0;
   if (TH == 0) {
-    if (!live) return;
     slice_stride = rows * Kp;
     row_base = row * Kp;
   } else {
-    const int64_t rows_p = (rows + TH - 1) / TH * TH;
-    if (row >= rows_p) return;
-    slice_stride = rows_p * Kp;
+    slice_stride = (rows + TH - 1) / TH * TH * Kp;
     const int rr = (int)(row % TH);
     row_base = (row / TH) * (Kp / 16) * (int64_t)TH * 16;
     in_tile = (rr >> 3) * 128 + (rr & 7) * 8;
   }
+  auto offset = [&](int64_t c) -> int64_t {
+    return TH == 0 ? row_base + 8 * c : row_base + (c >> 1) * (int64_t)TH * 16 + in_tile + (c & 1) * 64;
+  };
   __nv_bfloat16* dst = (opb ? b_dst : a_dst) + r[5];
-  for (int64_t c = cl; c < Kp / 8; c += kSplitLanes) {
-    uint32_t pk[S][4];
+  if (g.y >= rows) {  // all 8 rows are padding rows of the tile layout: zeros
+    const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+    for (int64_t c = cl; c < nck; c += kSplitLanes)
 #pragma unroll
-    for (int u = 0; u < 8; u += 2) {
-      const int64_t k = 8 * c + u;
-      const long long b0 = (live && k < K) ? a(k) : 0ll;
-      const long long b1 = (live && k + 1 < K) ? a(k + 1) : 0ll;
-      uint32_t w0[S], w1[S];
-      digit_words<S>(b0, e, w0);
-      digit_words<S>(b1, e, w1);
+      for (int t = 0; t < S; ++t) *reinterpret_cast<uint4*>(dst + t * slice_stride + offset(c)) = z;
+    return;
+  }
+  const int mode = (int)r[4];
+  const int64_t ks = r[8];
+  const long long* base =
+      reinterpret_cast<const long long*>(opb ? b_src : a_src) + (mode == 0 ? 1 : 2) * (r[0] + (live ? row : 0) * r[3]);
+  // bit pattern of element k (k < K) of this row
+  auto elem = [&](int64_t k) -> long long {
+    if (mode == 0) return __ldg(base + k * ks);
+    const int64_t half = K / 2;
+    const bool first = k < half;
+    const long long* c = base + 2 * (first ? k : k - half) * ks;
+    const long long re = __ldg(c), im = __ldg(c + 1);
+    if (mode == 1) return first ? re : im;
+    if (mode == 2) return first ? re : (long long)((unsigned long long)im ^ 0x8000000000000000ull);
+    return first ? im : re;
+  };
+  auto load_chunk = [&](int64_t c, long long* x) {
+    const int64_t k0 = 8 * c;
+    if (mode == 0 && live && k0 + 8 <= K) {
+      const long long* p = base + k0 * ks;
 #pragma unroll
-      for (int t = 0; t < S; ++t) pk[t][u >> 1] = __byte_perm(w0[t], w1[t], 0x7632);
+      for (int u = 0; u < 8; ++u) x[u] = __ldg(p + u * ks);
+    } else {
+#pragma unroll
+      for (int u = 0; u < 8; ++u) x[u] = (live && k0 + u < K) ? elem(k0 + u) : 0ll;
     }
-    const int64_t off =
-        TH == 0 ? row_base + 8 * c : row_base + (c >> 1) * (int64_t)TH * 16 + in_tile + (c & 1) * 64;
+  };
+  auto rowmax = [&](const long long* x, long long mx) {
 #pragma unroll
-    for (int t = 0; t < S; ++t)
-      *reinterpret_cast<uint4*>(dst + t * slice_stride + off) = make_uint4(pk[t][0], pk[t][1], pk[t][2], pk[t][3]);
+    for (int u = 0; u < 8; ++u) mx = max(mx, x[u] & 0x7fffffffffffffffll);
+    return mx;
+  };
+  auto exponent = [&](long long mx) {
+    smax[cl][ri] = mx;
+    __syncthreads();
+    if (threadIdx.x < kSplitRows) {
+#pragma unroll 8
+      for (int w = 1; w < kSplitLanes; ++w) mx = max(mx, smax[w][ri]);
+      int e = 0;  // max |a| = f 2^e, f in [0.5, 1): |a| < 2^e
+      if (mx >= (1ll << 52)) e = (int)(mx >> 52) - 1022;
+      else if (mx > 0) frexp(__longlong_as_double(mx), &e);
+      sexp[ri] = e;
+      if (live) (opb ? b_exps : a_exps)[r[6] + row] = e;
+    }
+    __syncthreads();
+    return sexp[ri];
+  };
+  const bool pad_row = TH == 0 && !live;  // planes layout: rows past the record are not stored
+  if (nck <= 2 * kSplitLanes) {
+    // at most two chunks per lane: values held in registers between the passes
+    long long x0[8], x1[8];
+    const int64_t c0 = cl, c1 = cl + kSplitLanes;
+    load_chunk(c0 < nck ? c0 : 0, x0);
+    load_chunk(c1 < nck ? c1 : 0, x1);
+    long long mx = 0;
+    if (c0 < nck) mx = rowmax(x0, mx);
+    if (c1 < nck) mx = rowmax(x1, mx);
+    const int e = exponent(mx);
+    if (pad_row) return;
+    if (c0 < nck) store_chunk<S>(dst, slice_stride, offset(c0), x0, e);
+    if (c1 < nck) store_chunk<S>(dst, slice_stride, offset(c1), x1, e);
+    return;
+  }
+  long long mx = 0;
+  for (int64_t c = cl; c < nck; c += kSplitLanes) {
+    long long x[8];
+    load_chunk(c, x);
+    mx = rowmax(x, mx);
+  }
+  const int e = exponent(mx);
+  if (pad_row) return;
+  for (int64_t c = cl; c < nck; c += kSplitLanes) {
+    long long x[8];
+    load_chunk(c, x);
+    store_chunk<S>(dst, slice_stride, offset(c), x, e);
   }
 }
 
@@ -321,24 +363,31 @@ __global__ void __launch_bounds__(kThreads, 1) ozaki_gemm_kernel(const __nv_bflo
       // fold the diagonal sums (exact integers below 2^24 in FP32) into FP64: the weighted
       // sum sum_d acc_d 2^(-7d) is formed exactly in two int64 halves (diagonals 0..3 and
       // 4..7, each below 2^46) and rounded once (fold_round), on the integer pipe, which
-      // keeps the fold off GB300's narrow FP64 pipe
+      // keeps the fold off GB300's narrow FP64 pipe; the first chunk is assigned, later ones
+      // added (two copies of the loop, so that the first issues no FP64 add)
+      auto fold = [&](auto first_tag) {
+        constexpr bool kFirst = decltype(first_tag)::value;
 #pragma unroll
-      for (int i = 0; i < 2; ++i)
+        for (int i = 0; i < 2; ++i)
 #pragma unroll
-        for (int j = 0; j < 2; ++j)
+          for (int j = 0; j < 2; ++j)
 #pragma unroll
-          for (int v = 0; v < 4; ++v) {
-            long long hi = 0, lo = 0;
+            for (int v = 0; v < 4; ++v) {
+              int qi[S];
 #pragma unroll
-            for (int d = 0; d < S; ++d) {
-              const long long q = (long long)__float2int_rn(acc[d][i][j][v]);
-              if (d < 4) hi += q << (7 * (3 - d));
-              else lo += q << (7 * (S - 1 - d));
-              acc[d][i][j][v] = 0.f;
+              for (int d = 0; d < S; ++d) {
+                qi[d] = __float2int_rn(acc[d][i][j][v]);
+                acc[d][i][j][v] = 0.f;
+              }
+              long long hi, lo;
+              oz::fold_halves<S>(qi, hi, lo);
+              const double x = fold_round(hi, lo, 7 * (S - 4), -7 * (S - 1));
+              if (kFirst) acc64[i][j][v] = x;
+              else acc64[i][j][v] += x;
             }
-            const double x = fold_round(hi, lo, 7 * (S - 4), -7 * (S - 1));
-            acc64[i][j][v] = st < kChunkSteps ? x : acc64[i][j][v] + x;  // FP64 add only past the first chunk
-          }
+      };
+      if (st < kChunkSteps) fold(std::true_type{});
+      else fold(std::false_type{});
     }
   }
   // epilogue: C = acc64 * 2^(e_i + f_j - 14)

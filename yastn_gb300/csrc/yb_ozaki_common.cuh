@@ -9,29 +9,21 @@ namespace yb {
 namespace oz {
 
 // Q = rint(a 2^{7s-e}) (|Q| < 2^{7s}) from a's mantissa and exponent bits, by a shift with
-// round-half-to-even (a = the double with bit pattern ``bits``; |a| < 2^e).
-__device__ __forceinline__ long long scaled_rint(long long bits, int e, int s) {
-  const long long mag = bits & 0x7fffffffffffffffll;
-  if (mag == 0) return 0;
+// round-half-to-even (a = the double with bit pattern ``bits``; |a| < 2^e), without branches:
+// elements near the row maximum (left shift, up to 3 bits for s = 8) and smaller ones (right
+// shift with rounding) take the same instructions.
+__host__ __device__ __forceinline__ long long scaled_rint(long long bits, int e, int s) {
+  const unsigned long long mag = (unsigned long long)bits & 0x7fffffffffffffffull;
   const int E = (int)(mag >> 52);
-  long long M = mag & 0xfffffffffffffll;
-  int ex = -1074;  // a = M 2^ex
-  if (E != 0) {
-    M |= 1ll << 52;
-    ex = E - 1075;
-  }
-  const int up = ex + 7 * s - e;  // Q = rint(M 2^up)
-  long long q;
-  if (up >= 0) {
-    q = M << up;  // |Q| < 2^{7s}: up <= 7s - 53
-  } else {
-    const int sh = min(-up, 63);
-    q = M >> sh;
-    const unsigned long long rem = (unsigned long long)M & ((1ull << sh) - 1ull);
-    const unsigned long long half = 1ull << (sh - 1);
-    if (rem > half || (rem == half && (q & 1))) ++q;
-  }
-  return bits < 0 ? -q : q;
+  const unsigned long long M = (mag & 0xfffffffffffffull) | (E ? (1ull << 52) : 0ull);
+  const int up = (E ? E - 1075 : -1074) + 7 * s - e;  // Q = rint(M 2^up)
+  const int shl = up > 0 ? up : 0;
+  const int shr = up < 0 ? (-up < 63 ? -up : 63) : 0;
+  unsigned long long q = (M << shl) >> shr;
+  const unsigned long long rem = M & ((1ull << shr) - 1ull);
+  const unsigned long long half = (1ull << shr) >> 1;
+  q += (unsigned long long)((rem > half) | ((rem == half) & (shr != 0) & ((q & 1ull) != 0)));
+  return bits < 0 ? -(long long)q : (long long)q;
 }
 
 // x 2^E by an exponent-field add when x and the result are normal doubles.
@@ -83,6 +75,19 @@ __host__ __device__ __forceinline__ double fold_round(long long hi, long long lo
   } cv;
   cv.u = bits;
   return p < 0 ? 0.0 : cv.d;
+}
+
+// The two int64 halves of a fold from the S exact diagonal sums q_d (|q_d| <= 400 * 10 * 2^12,
+// chunks of at most 400): hi = sum_{d<4} q_d 2^{7(3-d)}, lo = sum_{d>=4} q_d 2^{7(S-1-d)}.
+// The last two terms of each half are combined in 32 bits (|128 q + q'| < 2^31 by that bound)
+// and the rest with 32 x 32 -> 64-bit multiply-adds.
+template <int S>
+__device__ __forceinline__ void fold_halves(const int* q, long long& hi, long long& lo) {
+  hi = (long long)q[0] * (1ll << 21) + (long long)q[1] * (1ll << 14) + (long long)(q[2] * 128 + q[3]);
+  long long l = (long long)(q[S - 2] * 128 + q[S - 1]);
+#pragma unroll
+  for (int d = 4; d < S - 2; ++d) l += (long long)q[d] * (1ll << (7 * (S - 1 - d)));
+  lo = l;
 }
 
 // ------------------------------------------------------------------ tcgen05 / mbarrier

@@ -8,9 +8,11 @@
 //    16-long K step into a 4-stage shared-memory ring with cp.async.bulk copies completing on
 //    the stage's mbarrier, refilling a stage as soon as the MMAs that read it have completed,
 //    straight on into the next tile's steps;
-//  - warp 1 (one thread) issues the S(S+1)/2 tcgen05.mma (M=128, N=64, K=16, BF16 -> FP32) of a
-//    step into the S digit-diagonal accumulators in tensor memory (S x 64 of the 512 TMEM
-//    columns) and frees the stage with tcgen05.commit;
+//  - warp 1 (one thread) issues the S(S+1)/2 slice products of a step (BF16 -> FP32, M=128,
+//    K=16) into the S digit-diagonal accumulators in tensor memory (S x 64 of the 512 TMEM
+//    columns), up to four products per tcgen05.mma (N = 64 per B slice: slices tb..tb+3 are
+//    one operand, diagonals ta+tb..ta+tb+3 adjacent accumulators; 13 MMAs per step for S = 8),
+//    and frees the stage with tcgen05.commit;
 //  - 16 fold warps (4 per TMEM lane quarter, 16 columns each) read the accumulators back at
 //    the end of every 400-long K chunk (exact FP32 integer sums), combine the diagonals exactly
 //    into a 128-bit integer on the integer pipe, round it once to FP64 into the tile's FP64
@@ -20,6 +22,7 @@
 //    padding of small sectors) skip their reads and folds.
 // Every wait is bounded; a CTA that gives up records the status word of yb_ozaki_device_error,
 // waits (bounded) for its copies and MMAs, frees its tensor memory and stops writing.
+#include <type_traits>
 #include "yb_ozaki_common.cuh"
 
 namespace yb {
@@ -50,7 +53,7 @@ __global__ void __launch_bounds__(kThreadsT, 1)
     ozaki_gemm_tc_kernel(const __nv_bfloat16* __restrict__ As, const int* __restrict__ Ae,
                          const __nv_bfloat16* __restrict__ Bs, const int* __restrict__ Be, double* __restrict__ C,
                          const int64_t* __restrict__ outs, const int32_t* __restrict__ tiles, int n_tiles,
-                         int* __restrict__ err) {
+                         const int32_t* __restrict__ cta_tiles, int* __restrict__ err) {
   constexpr uint32_t kStage = S * (kATile + kBTile);
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint32_t tmem_slot;
@@ -60,6 +63,11 @@ __global__ void __launch_bounds__(kThreadsT, 1)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t sbase = smem_u32(smem);
+  // this CTA's tiles: [t0, t1) of a schedule grouped by CTA, or every gridDim.x-th tile
+  const bool sched = cta_tiles != nullptr;
+  const int t0 = sched ? cta_tiles[blockIdx.x] : (int)blockIdx.x;
+  const int t1 = sched ? cta_tiles[blockIdx.x + 1] : n_tiles;
+  const int dt = sched ? 1 : (int)gridDim.x;
 
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -87,7 +95,7 @@ __global__ void __launch_bounds__(kThreadsT, 1)
     if (lane == 0) {
       int64_t gs = 0;  // K steps issued by this CTA (all its tiles): the ring position
       bool ok = true;
-      for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+      for (int t = t0; t < t1 && ok; t += dt) {
         const int4 tl = reinterpret_cast<const int4*>(tiles)[t];
         const int64_t* o = outs + (int64_t)tl.x * 16;
         const int64_t m = o[1], n = o[2], a_sl = o[4], b_sl = o[6], Kp = o[9];
@@ -124,11 +132,11 @@ __global__ void __launch_bounds__(kThreadsT, 1)
   } else if (warp == 1) {
     // ---------------------------------------------------------------- MMA issue
     if (lane == 0) {
-      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN >> 3) << 17) |
-                             ((uint32_t)(kM >> 4) << 24);  // F32 accumulate, BF16 A/B, K-major, N=64, M=128
+      // F32 accumulate, BF16 A/B, K-major, M=128; N = 64 x (slices in one MMA) is set per MMA
+      const uint32_t idesc0 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kM >> 4) << 24);
       bool ok = true;
       int64_t gs = 0, gch = 0;  // steps and chunks of this CTA
-      for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+      for (int t = t0; t < t1 && ok; t += dt) {
         const int4 tl = reinterpret_cast<const int4*>(tiles)[t];
         const int64_t ksteps = outs[(int64_t)tl.x * 16 + 9] / kK;
         const int64_t nchunks = (ksteps + kChunkSteps - 1) / kChunkSteps;
@@ -147,12 +155,18 @@ __global__ void __launch_bounds__(kThreadsT, 1)
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t a0 = sbase + (uint32_t)stage * kStage, b0 = a0 + S * kATile;
             const bool first = st == ch * kChunkSteps;
+            // A_ta times up to four B slices at once: the B slices lie one after the other in
+            // the stage (64 rows each, the same core-matrix strides), so B_tb..B_tb+k-1 is one
+            // operand of N = 64k rows, and the diagonals ta+tb..ta+tb+k-1 are adjacent 64-column
+            // accumulators: one MMA of N = 64k does the k slice products
 #pragma unroll
             for (int ta = 0; ta < S; ++ta)
 #pragma unroll
-              for (int tb = 0; tb < S - ta; ++tb)
+              for (int tb = 0; tb < S - ta; tb += 4) {
+                const int k = (S - ta - tb) < 4 ? (S - ta - tb) : 4;
                 tc_mma(tmem + (uint32_t)((ta + tb) * kN), umma_desc(a0 + ta * kATile), umma_desc(b0 + tb * kBTile),
-                       idesc, (first && ta == 0) ? 0u : 1u);
+                       idesc0 | ((uint32_t)((kN * k) >> 3) << 17), (first && ta == 0) ? 0u : 1u);
+              }
             tc_commit(smem_u32(&empty[stage]));
           }
           if (!ok) break;
@@ -175,7 +189,7 @@ __global__ void __launch_bounds__(kThreadsT, 1)
     const int r = 32 * q + lane;        // tile row of this thread
     int64_t gch = 0;
     bool ok = true;
-    for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+    for (int t = t0; t < t1 && ok; t += dt) {
       const int4 tl = reinterpret_cast<const int4*>(tiles)[t];
       const int64_t* o = outs + (int64_t)tl.x * 16;
       const int64_t c_off = o[0], m = o[1], n = o[2], ldc = o[3], a_ex = o[5], b_ex = o[7], Kp = o[9];
@@ -191,11 +205,13 @@ __global__ void __launch_bounds__(kThreadsT, 1)
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        if (busy) {
-          // exact fold: the diagonal sums are integers below 2^24 in FP32; their weighted sum
-          // sum_d q_d 2^{7(S-1-d)} = hi 2^{7(S-4)} + lo is formed in two int64 halves and
-          // rounded once to FP64 (the same rounding as the mma.sync kernel's fold). The S
-          // diagonals of 4 columns are read with one wait.
+        // exact fold: the diagonal sums are integers below 2^24 in FP32; their weighted sum
+        // sum_d q_d 2^{7(S-1-d)} = hi 2^{7(S-4)} + lo is formed in two int64 halves and
+        // rounded once to FP64 (the same rounding as the mma.sync kernel's fold). The S
+        // diagonals of 4 columns are read with one wait. The first chunk is assigned, later
+        // ones added (two copies of the loop, so that the first issues no FP64 add).
+        auto fold = [&](auto first_tag) {
+          constexpr bool kFirst = decltype(first_tag)::value;
 #pragma unroll
           for (int cb = 0; cb < kFoldCols / 4; ++cb) {
             uint32_t v[S][4];
@@ -205,17 +221,20 @@ __global__ void __launch_bounds__(kThreadsT, 1)
             asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-              long long hi = 0, lo = 0;
+              int qi[S];
 #pragma unroll
-              for (int d = 0; d < S; ++d) {
-                const long long qv = (long long)__float2int_rn(__uint_as_float(v[d][j]));
-                if (d < 4) hi += qv << (7 * (3 - d));
-                else lo += qv << (7 * (S - 1 - d));
-              }
+              for (int d = 0; d < S; ++d) qi[d] = __float2int_rn(__uint_as_float(v[d][j]));
+              long long hi, lo;
+              fold_halves<S>(qi, hi, lo);
               const double x = fold_round(hi, lo, 7 * (S - 4), -7 * (S - 1));
-              acc[cb * 4 + j] = ch == 0 ? x : acc[cb * 4 + j] + x;
+              if (kFirst) acc[cb * 4 + j] = x;
+              else acc[cb * 4 + j] += x;
             }
           }
+        };
+        if (busy) {
+          if (ch == 0) fold(std::true_type{});
+          else fold(std::false_type{});
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
         mbar_arrive(smem_u32(&tfree));
@@ -253,16 +272,19 @@ int sm_count() {
 
 template <int S>
 int launch_gemm_tc(const void* As, const int* Ae, const void* Bs, const int* Be, double* C, const int64_t* outs,
-                   const int32_t* tiles, int n_tiles, int* err, cudaStream_t s) {
+                   const int32_t* tiles, int n_tiles, const int32_t* cta_tiles, int n_ctas, int* err,
+                   cudaStream_t s) {
   const size_t smem = (size_t)kStages * S * (kATile + kBTile);
   auto kern = ozaki_gemm_tc_kernel<S>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
   const int sms = sm_count();
   if (sms <= 0) return YB_ERR_CUDA;
-  const int grid = n_tiles < sms ? n_tiles : sms;  // one CTA per SM (its shared memory and all 512 TMEM columns)
+  // one CTA per SM (its shared memory and all 512 TMEM columns): a schedule may not ask for more
+  if (cta_tiles && (n_ctas < 1 || n_ctas > sms)) return YB_ERR_INVALID;
+  const int grid = cta_tiles ? n_ctas : (n_tiles < sms ? n_tiles : sms);
   kern<<<grid, kThreadsT, smem, s>>>((const __nv_bfloat16*)As, Ae, (const __nv_bfloat16*)Bs, Be, C, outs, tiles,
-                                     n_tiles, err);
+                                     n_tiles, cta_tiles, err);
   return check_launch();
 }
 
@@ -275,7 +297,8 @@ static __device__ int g_ozaki_tc_error;
 extern "C" {
 
 int yb_ozaki_gemm_tc(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps, double* c,
-                     const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count, void* stream) {
+                     const int64_t* outs, const int32_t* tiles, int n_tiles, const int32_t* cta_tiles, int n_ctas,
+                     int slices_count, void* stream) {
   if (n_tiles == 0) return YB_OK;
   if (!a_slices || !a_exps || !b_slices || !b_exps || !c || !outs || !tiles || n_tiles < 0) return YB_ERR_INVALID;
   int* err = nullptr;
@@ -283,9 +306,12 @@ int yb_ozaki_gemm_tc(const void* a_slices, const int* a_exps, const void* b_slic
   if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
   cudaStream_t s = (cudaStream_t)stream;
   switch (slices_count) {
-    case 8: return yb::launch_gemm_tc<8>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
-    case 7: return yb::launch_gemm_tc<7>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
-    case 6: return yb::launch_gemm_tc<6>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, err, s);
+    case 8:
+      return yb::launch_gemm_tc<8>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, cta_tiles, n_ctas, err, s);
+    case 7:
+      return yb::launch_gemm_tc<7>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, cta_tiles, n_ctas, err, s);
+    case 6:
+      return yb::launch_gemm_tc<6>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, cta_tiles, n_ctas, err, s);
     default: return YB_ERR_INVALID;
   }
 }

@@ -229,18 +229,35 @@ def _ozaki_run(plan, A, B, out, slices, tc):
     a_ex = torch.empty(max(plan.a_exps, 1), dtype=torch.int32, device=dev)
     b_ex = torch.empty(max(plan.b_exps, 1), dtype=torch.int32, device=dev)
     if tc:
-        key, arrs = 'ozaki_tc', (plan.split_recs_tc, plan.split_groups_tc, plan.outs_tc, plan.tiles_tc)
-        asz, bsz, n_tiles, gemm = plan.a_size_tc, plan.b_size_tc, len(plan.tiles_tc), 'yb_ozaki_gemm_tc'
+        # tiles grouped by CTA (one CTA per SM) with balanced work
+        tiles, offs = P.ozaki_tc_schedule(plan, _sm_count(dev))
+        key, arrs = 'ozaki_tc', (plan.split_recs_tc, plan.split_groups_tc, plan.outs_tc, tiles, offs)
+        asz, bsz = plan.a_size_tc, plan.b_size_tc
     else:
         key, arrs = 'ozaki', (plan.split_recs, plan.split_groups, plan.outs, plan.tiles)
-        asz, bsz, n_tiles, gemm = plan.a_size, plan.b_size, len(plan.tiles), 'yb_ozaki_gemm'
-    drec, dgrp, dout, dtl = _dev(plan, key, arrs, dev)
+        asz, bsz = plan.a_size, plan.b_size
+    darr = _dev(plan, key, arrs, dev)
+    drec, dgrp, dout, dtl = darr[:4]
     a_sl = torch.empty(max(asz, 1), dtype=torch.bfloat16, device=dev)
     b_sl = torch.empty(max(bsz, 1), dtype=torch.bfloat16, device=dev)
     N.call('yb_ozaki_split', _ptr(A), _ptr(B), _ptr(a_sl), _ptr(b_sl), _ptr(a_ex), _ptr(b_ex), _ptr(drec),
            _ptr(dgrp), len(arrs[1]), slices, st)
-    N.call(gemm, _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl), n_tiles, slices,
-           st)
+    if tc:
+        N.call('yb_ozaki_gemm_tc', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
+               len(arrs[3]), _ptr(darr[4]), len(arrs[4]) - 1, slices, st)
+    else:
+        N.call('yb_ozaki_gemm', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
+               len(arrs[3]), slices, st)
+
+
+_SMS = {}
+
+
+def _sm_count(device):
+    n = _SMS.get(device.index)
+    if n is None:
+        n = _SMS[device.index] = torch.cuda.get_device_properties(device).multi_processor_count
+    return n
 
 
 def ozaki_device_error(reset=True):
