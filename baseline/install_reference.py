@@ -13,6 +13,10 @@ unchanged into ``baseline/_ref``, installs ``tqdm`` there from the offline wheel
 copies the pure-Python ``opt_einsum`` package of this interpreter (both are imported by
 ``import yastn``; the GPU machine has neither). Nothing of the reference is modified.
 
+The reference's own tensor test suite (tests/tensor, with its input files) is copied
+unchanged to ``baseline/_ref/yastn_tests/tensor``, where tests/test_gpu_reference_suite.py
+runs it against this backend.
+
 Usage: python baseline/install_reference.py <reference tree> [wheelhouse]
 """
 import os
@@ -39,7 +43,7 @@ def main(ref, wheelhouse='/opt/wheelhouse'):
         res = _pip(['--find-links', wheelhouse, '--target', TARGET, src])
     if res.returncode == 0:
         print('pip install of the reference: ok')
-        return 0
+        return copy_tests(ref)
     print('pip install of the reference failed (metadata generation: setuptools-scm is a build requirement '
           'absent from the offline wheelhouse); installing the pure-Python package by copy')
     os.makedirs(TARGET, exist_ok=True)
@@ -53,6 +57,16 @@ def main(ref, wheelhouse='/opt/wheelhouse'):
     shutil.copytree(os.path.dirname(opt_einsum.__file__), os.path.join(TARGET, 'opt_einsum'),
                     ignore=shutil.ignore_patterns('__pycache__'))
     print(f'installed yastn, tqdm, opt_einsum into {TARGET}')
+    return copy_tests(ref)
+
+
+def copy_tests(ref):
+    """The reference's tests/tensor suite, unchanged, beside the installed package."""
+    dst = os.path.join(TARGET, 'yastn_tests', 'tensor')
+    if os.path.exists(dst):
+        shutil.rmtree(dst)
+    shutil.copytree(os.path.join(ref, 'tests', 'tensor'), dst, ignore=shutil.ignore_patterns('__pycache__'))
+    print(f'copied the reference tensor tests into {dst}')
     return 0
 
 

@@ -322,3 +322,33 @@ def test_ozaki_split_matches_digit_model(cplx, slices, cuda_device):
         for got, got_e, w, we in ((a_sl, a_ex, want[0], want_e[0]), (b_sl, b_ex, want[1], want_e[1])):
             np.testing.assert_array_equal(host(got.float()).astype(np.int64), w)
             np.testing.assert_array_equal(host(got_e).astype(np.int64), we)
+
+
+def test_short_skinny_gemm_values_and_nan(cuda_device):
+    """The short skinny kernel (one term, m <= 8, K <= 8): values match the oracle, and an
+    infinity or NaN in B meeting a zero of A gives NaN, as in the reference's NumPy product."""
+    from yastn_gb300 import _plans as P
+    rng = np.random.default_rng(41)
+    shapes = [(3, 4, 1500), (2, 3, 700), (1, 4, 65)]
+    meta, oa, ob, oc = [], 0, 0, 0
+    for m, k, n in shapes:
+        meta.append(((oc, oc + m * n), (m, n), (oa, oa + m * k), (m, k), (ob, ob + k * n), (k, n)))
+        oa += m * k; ob += k * n; oc += m * n
+    meta = tuple(meta)
+    assert P.dot_plan(meta).all_short
+    A = rng.normal(size=oa)
+    A[::3] = 0.0
+    B = rng.normal(size=ob)
+    got = host(ops.dot(dev(A), dev(B), meta, oc))
+    ref = oracle.dot(A, B, meta, oc)
+    assert rel(got, ref) <= TOL
+    B2 = B.copy()
+    B2[5] = np.inf
+    B2[ob - 3] = np.nan
+    with np.errstate(invalid='ignore', over='ignore'):
+        ref2 = oracle.dot(A, B2, meta, oc)
+    got2 = host(ops.dot(dev(A), dev(B2), meta, oc))
+    np.testing.assert_array_equal(np.isnan(got2), np.isnan(ref2))
+    np.testing.assert_array_equal(np.isinf(got2), np.isinf(ref2))
+    ok = np.isfinite(ref2)
+    assert np.abs(got2[ok] - ref2[ok]).max() <= TOL * np.abs(ref2[ok]).max()

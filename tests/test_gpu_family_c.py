@@ -256,6 +256,31 @@ def test_eigh_on_reference_calls(cuda_device):
     assert n > 0
 
 
+@pytest.mark.parametrize('cplx', [False, True])
+def test_eigh_rank_deficient_psd_blocks_reconstruct(cplx, cuda_device):
+    """Gram matrices F F^H of wide-rowed F (rank-deficient, positive semidefinite, the
+    eigenvalues of the shifted block clustered near the shift): U diag(S) U^H reproduces
+    every block to the rounding level (relative 1e-13) and U is unitary, over many draws
+    (YASTN's test_fuse_hard.py::test_hard_split meets such blocks)."""
+    rng = np.random.default_rng(5)
+    for trial in range(12):
+        shapes = [(86, 19), (91, 120), (30, 40), (7, 3)]
+        blocks, meta, off_a, off_u, off_s = [], [], 0, 0, 0
+        for n, r in shapes:
+            F = rng.normal(size=(n, r)) + (1j * rng.normal(size=(n, r)) if cplx else 0)
+            G = F @ F.conj().T
+            blocks.append(G)
+            meta.append(((off_a, off_a + n * n), (n, n), (off_u, off_u + n * n), (n, n), (off_s, off_s + n)))
+            off_a += n * n; off_u += n * n; off_s += n
+        data = np.concatenate([b.ravel() for b in blocks])
+        S, U = (host(x) for x in ops.eigh(dev(data), tuple(meta), (off_s, off_u)))
+        for G, (sl, D, slU, DU, slS) in zip(blocks, meta):
+            u = U[slU[0]:slU[1]].reshape(DU)
+            s = S[slS[0]:slS[1]]
+            assert np.linalg.norm((u * s) @ u.conj().T - G) <= 1e-13 * np.linalg.norm(G), (trial, D)
+            assert np.abs(u.conj().T @ u - np.eye(DU[1])).max() <= 1e-13 * DU[1]
+
+
 def test_eigh_order_by_magnitude(cuda_device):
     rng = np.random.default_rng(9)
     a = rng.normal(size=(9, 9)); a = a + a.T

@@ -659,12 +659,13 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
                     tiles_tc.append((K, oi, tr, tc))
         tiles_tc.sort(key=lambda x: -x[0])
         plan.tiles_tc = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles_tc], dtype=np.int32).reshape(-1, 4)
-        # padded MMA work of the two tilings: the tcgen05 kernel (128 x 64 tiles) when its
-        # padding costs little more than the 64 x 64 tiles of the mma.sync kernel
+        # padded MMA work of the two tilings: the tcgen05 kernel (128 x 64 tiles) unless its
+        # padding costs over 1.6 times the 64 x 64 tiles of the mma.sync kernel (the tcgen05
+        # kernel measured faster on the DMRG workload's sectors at 1.3 times the padded work)
         w64 = sum(-(-int(o[1]) // 64) * 64 * -(-int(o[2]) // 64) * 64 * int(o[9]) for o in outs)
         w128 = sum(-(-int(o[1]) // OZAKI_TC_M) * OZAKI_TC_M * -(-int(o[2]) // OZAKI_TC_N) * OZAKI_TC_N * int(o[9])
                    for o in outs)
-        plan.prefer_tc = bool(len(outs)) and w128 <= 1.1 * w64
+        plan.prefer_tc = bool(len(outs)) and w128 <= 1.6 * w64
         return plan
     return CACHE.get((meta_dot,), ('ozaki_dot', s, bool(cplx)), build)
 

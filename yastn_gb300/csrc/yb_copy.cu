@@ -11,6 +11,7 @@
 // handles one item. Within an item consecutive threads take consecutive units of the
 // innermost dim (destination-contiguous after collapsing), so stores are coalesced.
 // Tasks that transpose (source contiguous along another dim) are tiled instead.
+#include <type_traits>
 #include "yb_common.cuh"
 
 namespace yb {
@@ -162,7 +163,7 @@ __global__ void __launch_bounds__(kThreads) block_copy_kernel(const Elem* __rest
   __syncthreads();
   if (rec[YB_CP_KIND] == 1)
     copy_tiles<Elem>(src, dst, rec, first, tile);
-  else if (sizeof(Elem) == 8 && rec[YB_CP_VEC] != 0)
+  else if (std::is_same<Elem, double>::value && rec[YB_CP_VEC] != 0)
     copy_units_any<double2>(reinterpret_cast<const double2*>(src), reinterpret_cast<double2*>(dst), rec, first);
   else
     copy_units_any<Elem>(src, dst, rec, first);
@@ -182,12 +183,23 @@ int yb_block_copy(const void* src, void* dst, int unit_bytes, const int64_t* tas
   if (!src || !dst || !tasks || !items || n_tasks <= 0 || n_items < 0) return YB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
   dim3 grid((unsigned)n_items);
-  if (unit_bytes == 8) {
-    yb::block_copy_kernel<double><<<grid, yb::kThreads, 0, s>>>((const double*)src, (double*)dst, tasks, items);
-  } else if (unit_bytes == 16) {
-    yb::block_copy_kernel<double2><<<grid, yb::kThreads, 0, s>>>((const double2*)src, (double2*)dst, tasks, items);
-  } else {
-    return YB_ERR_INVALID;
+  // the copy moves elements as raw units: 8 bytes (float64, complex64), 16 (complex128), and
+  // 1, 2, 4 for the other dtypes a tensor may hold (bool masks, float32, ...)
+  switch (unit_bytes) {
+    case 8: yb::block_copy_kernel<double><<<grid, yb::kThreads, 0, s>>>((const double*)src, (double*)dst, tasks, items); break;
+    case 16:
+      yb::block_copy_kernel<double2><<<grid, yb::kThreads, 0, s>>>((const double2*)src, (double2*)dst, tasks, items);
+      break;
+    case 4:
+      yb::block_copy_kernel<uint32_t><<<grid, yb::kThreads, 0, s>>>((const uint32_t*)src, (uint32_t*)dst, tasks, items);
+      break;
+    case 2:
+      yb::block_copy_kernel<uint16_t><<<grid, yb::kThreads, 0, s>>>((const uint16_t*)src, (uint16_t*)dst, tasks, items);
+      break;
+    case 1:
+      yb::block_copy_kernel<uint8_t><<<grid, yb::kThreads, 0, s>>>((const uint8_t*)src, (uint8_t*)dst, tasks, items);
+      break;
+    default: return YB_ERR_INVALID;
   }
   return yb::check_launch();
 }

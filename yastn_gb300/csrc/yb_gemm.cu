@@ -234,7 +234,7 @@ __device__ __forceinline__ void short_dispatch(const typename F::T* __restrict__
 
 // Kernel of the short skinny tiles only (tile kind 2).
 template <class F>
-__global__ void __launch_bounds__(kThreads, 3) short_gemm_kernel(const typename F::T* __restrict__ A,
+__global__ void __launch_bounds__(kThreads, sizeof(typename F::T) == 8 ? 3 : 1) short_gemm_kernel(const typename F::T* __restrict__ A,
                                                                  const typename F::T* __restrict__ B,
                                                                  typename F::T* __restrict__ C,
                                                                  const int64_t* __restrict__ outs,

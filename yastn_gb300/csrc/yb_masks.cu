@@ -339,14 +339,29 @@ int yb_mask_gather(const void* A, void* out, int unit_bytes, const int64_t* recs
   if (n_items == 0) return YB_OK;
   if (!A || !out || !recs || !items || !idx || n_items < 0) return YB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
-  if (unit_bytes == 8)
-    yb::mask_gather_kernel<double><<<(unsigned)n_items, 256, 0, s>>>((const double*)A, (double*)out, recs, items, idx,
-                                                                     scatter);
-  else if (unit_bytes == 16)
-    yb::mask_gather_kernel<double2><<<(unsigned)n_items, 256, 0, s>>>((const double2*)A, (double2*)out, recs, items,
-                                                                      idx, scatter);
-  else
-    return YB_ERR_INVALID;
+  switch (unit_bytes) {  // raw units of the element size
+    case 8:
+      yb::mask_gather_kernel<double><<<(unsigned)n_items, 256, 0, s>>>((const double*)A, (double*)out, recs, items, idx,
+                                                                       scatter);
+      break;
+    case 16:
+      yb::mask_gather_kernel<double2><<<(unsigned)n_items, 256, 0, s>>>((const double2*)A, (double2*)out, recs, items,
+                                                                        idx, scatter);
+      break;
+    case 4:
+      yb::mask_gather_kernel<uint32_t><<<(unsigned)n_items, 256, 0, s>>>((const uint32_t*)A, (uint32_t*)out, recs,
+                                                                         items, idx, scatter);
+      break;
+    case 2:
+      yb::mask_gather_kernel<uint16_t><<<(unsigned)n_items, 256, 0, s>>>((const uint16_t*)A, (uint16_t*)out, recs,
+                                                                         items, idx, scatter);
+      break;
+    case 1:
+      yb::mask_gather_kernel<uint8_t><<<(unsigned)n_items, 256, 0, s>>>((const uint8_t*)A, (uint8_t*)out, recs, items,
+                                                                        idx, scatter);
+      break;
+    default: return YB_ERR_INVALID;
+  }
   return yb::check_launch();
 }
 

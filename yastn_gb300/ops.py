@@ -22,7 +22,18 @@ def _vp(x):
 
 
 def _ptr(t):
+    if t.is_conj() or t.is_neg():  # a lazy view: its memory is not what the kernels would read
+        raise ValueError("yastn_gb300: a conjugate/negative view reached a kernel unresolved")
     return ctypes.c_void_p(t.data_ptr())
+
+
+def _plain(t):
+    """t with torch's lazy conjugate / negative flags resolved, contiguous."""
+    if t.is_conj():
+        t = t.resolve_conj()
+    if t.is_neg():
+        t = t.resolve_neg()
+    return t.contiguous()
 
 
 def _stream():
@@ -37,11 +48,27 @@ def _dtype_code(dtype):
     raise NotImplementedError(f"yastn_gb300 kernels support float64 and complex128, got {dtype}")
 
 
-def _check(t, name='data'):
+_COPY_UNITS = (1, 2, 4, 8, 16)  # element sizes the block copy and mask kernels move as raw units
+_NARROW = {torch.float32: torch.float64, torch.complex64: torch.complex128}
+
+
+def _check(t, name='data', any_dtype=False):
+    """A CUDA tensor, flat, contiguous, with lazy conjugate / negative views resolved. The
+    arithmetic kernels take float64 and complex128; the copies (``any_dtype``) any element of
+    1, 2, 4, 8 or 16 bytes (bool masks, float32, complex64, ...)."""
     if not isinstance(t, torch.Tensor) or not t.is_cuda:
         raise TypeError(f"{name} must be a CUDA tensor (yastn_gb300 has no CPU path)")
-    if t.dtype not in _SUPPORTED:
+    if any_dtype:
+        if t.element_size() not in _COPY_UNITS:
+            raise NotImplementedError(f"yastn_gb300 copies move 1-16 byte elements, got {t.dtype}")
+    elif t.dtype not in _SUPPORTED:
         raise NotImplementedError(f"yastn_gb300 kernels support float64 and complex128, got {t.dtype}")
+    # torch's lazy conjugate / negative views (conj(), neg() of a conjugate) keep the memory
+    # unchanged and only set a flag that the kernels, reading raw memory, would not see
+    if t.is_conj():
+        t = t.resolve_conj()
+    if t.is_neg():
+        t = t.resolve_neg()
     if t.dim() != 1 or not t.is_contiguous():
         t = t.reshape(-1).contiguous()
     return t
@@ -73,14 +100,14 @@ def run_copy(plan, src, dst):
 
 def merge(data, order, meta_new, meta_mrg, Dsize):
     """transpose_and_merge: fused blocks, zero where no source block lands."""
-    data = _check(data)
+    data = _check(data, any_dtype=True)
     plan = P.merge_plan(order, meta_new, meta_mrg, Dsize)
     out = (torch.empty if plan.full else torch.zeros)(Dsize, dtype=data.dtype, device=data.device)
     return run_copy(plan, data, out)
 
 
 def merge_backward(data_b, order, meta_new, meta_mrg, Dsize, D_source):
-    data_b = _check(data_b)
+    data_b = _check(data_b, any_dtype=True)
     plan = P.merge_plan(order, meta_new, meta_mrg, Dsize)
     inv = P.CACHE.get((order, meta_new, meta_mrg), ('merge_bwd', Dsize, D_source), lambda: plan.swapped(D_source))
     out = (torch.empty if inv.full else torch.zeros)(D_source, dtype=data_b.dtype, device=data_b.device)
@@ -88,14 +115,14 @@ def merge_backward(data_b, order, meta_new, meta_mrg, Dsize, D_source):
 
 
 def unmerge(data, meta):
-    data = _check(data)
+    data = _check(data, any_dtype=True)
     plan = P.unmerge_plan(meta, data.numel())
     out = (torch.empty if plan.full else torch.zeros)(data.numel(), dtype=data.dtype, device=data.device)
     return run_copy(plan, data, out)
 
 
 def unmerge_backward(data_b, meta, fwd_size):
-    data_b = _check(data_b)
+    data_b = _check(data_b, any_dtype=True)
     plan = P.unmerge_plan(meta, fwd_size)
     inv = P.CACHE.get((meta,), ('unmerge_bwd', fwd_size), lambda: plan.swapped(fwd_size))
     out = (torch.empty if inv.full else torch.zeros)(fwd_size, dtype=data_b.dtype, device=data_b.device)
@@ -103,14 +130,14 @@ def unmerge_backward(data_b, meta, fwd_size):
 
 
 def transpose(data, axes, meta_transpose):
-    data = _check(data)
+    data = _check(data, any_dtype=True)
     plan = P.transpose_plan(axes, meta_transpose, data.numel())
     out = (torch.empty if plan.full else torch.zeros)(data.numel(), dtype=data.dtype, device=data.device)
     return run_copy(plan, data, out)
 
 
 def transpose_backward(data_b, axes, meta_transpose):
-    data_b = _check(data_b)
+    data_b = _check(data_b, any_dtype=True)
     plan = P.transpose_plan(axes, meta_transpose, data_b.numel())
     inv = P.CACHE.get((axes, meta_transpose), ('transpose_bwd', data_b.numel()), lambda: plan.swapped(data_b.numel()))
     out = (torch.empty if inv.full else torch.zeros)(data_b.numel(), dtype=data_b.dtype, device=data_b.device)
@@ -143,7 +170,20 @@ def promote(A, B):
     return (A if A.dtype == dtype else A.to(dtype)), (B if B.dtype == dtype else B.to(dtype))
 
 
+def _narrow_inputs(*ts):
+    """True when a float32 / complex64 operand is present: the product then runs in float64 /
+    complex128 on the same kernels and the result is rounded to the promoted input dtype (at
+    least the accuracy of a single-precision product)."""
+    return any(isinstance(t, torch.Tensor) and t.dtype in _NARROW for t in ts)
+
+
+def _wide(t):
+    return t.to(_NARROW[t.dtype]) if t.dtype in _NARROW else t
+
+
 def dot(A, B, meta_dot, Dsize):
+    if _narrow_inputs(A, B):
+        return dot(_wide(A), _wide(B), meta_dot, Dsize).to(torch.promote_types(A.dtype, B.dtype))
     A, B = promote(_check(A, 'A'), _check(B, 'B'))
     plan = P.dot_plan(meta_dot)
     # every element is written by one sector when the sectors tile the output
@@ -167,6 +207,8 @@ def dot_ozaki(A, B, meta_dot, Dsize, slices=OZAKI_SLICES):
     with digit-weight sum below ``slices`` are accumulated exactly in FP32 per K-chunk and
     combined in FP64. ``slices=8`` reproduces the FP64 product to its rounding level.
     """
+    if _narrow_inputs(A, B):
+        return dot_ozaki(_wide(A), _wide(B), meta_dot, Dsize, slices).to(torch.promote_types(A.dtype, B.dtype))
     A, B = promote(_check(A, 'A'), _check(B, 'B'))
     plan = P.ozaki_dot_plan(meta_dot, slices, A.is_complex())
     out = (torch.empty if plan.covered == Dsize else torch.zeros)(Dsize, dtype=A.dtype, device=A.device)
@@ -269,6 +311,9 @@ def ozaki_device_error(reset=True):
 
 
 def dot_backward(C_b, A, B, meta_dot, need_a=True, need_b=True):
+    if _narrow_inputs(C_b, A, B):
+        A_b, B_b = dot_backward(_wide(C_b), _wide(A), _wide(B), meta_dot, need_a, need_b)
+        return (None if A_b is None else A_b.to(A.dtype)), (None if B_b is None else B_b.to(B.dtype))
     A, B = promote(_check(A, 'A'), _check(B, 'B'))
     C_b = _check(C_b, 'C_b')
     if C_b.dtype != A.dtype:
@@ -300,6 +345,9 @@ def permute_blocks(data, reshape, order):
 
 
 def transpose_dot_sum(A, B, meta_dot, Areshape, Breshape, Aorder, Border, Dsize):
+    if _narrow_inputs(A, B):
+        return transpose_dot_sum(_wide(A), _wide(B), meta_dot, Areshape, Breshape, Aorder, Border,
+                                 Dsize).to(torch.promote_types(A.dtype, B.dtype))
     A, B = promote(_check(A, 'A'), _check(B, 'B'))
     Ap, Aoffs, _ = permute_blocks(A, Areshape, Aorder)
     Bp, Boffs, _ = permute_blocks(B, Breshape, Border)
@@ -309,6 +357,10 @@ def transpose_dot_sum(A, B, meta_dot, Areshape, Breshape, Aorder, Border, Dsize)
 
 
 def transpose_dot_sum_backward(C_b, A, B, meta_dot, Areshape, Breshape, Aorder, Border):
+    if _narrow_inputs(C_b, A, B):
+        A_b, B_b = transpose_dot_sum_backward(_wide(C_b), _wide(A), _wide(B), meta_dot, Areshape, Breshape, Aorder,
+                                              Border)
+        return A_b.to(A.dtype), B_b.to(B.dtype)
     A, B = promote(_check(A, 'A'), _check(B, 'B'))
     C_b = _check(C_b, 'C_b').to(A.dtype)
     Ap, Aoffs, pa_perm = permute_blocks(A, Areshape, Aorder)
@@ -330,6 +382,10 @@ TOL_STOP32 = 1.0e-4   # FP32 phase ends after a sweep whose largest rotation |co
 TOL_STOP64 = 1.0e-8   # FP64 phase: idem; Jacobi converges quadratically (a sweep that starts at
                       # max |cos| c leaves ~c^2), so the residual after such a sweep is ~1e-16
 TOL_STOP64_QR = 1.0e-7  # the same for the QR-preconditioned SVD (separated, graded rows: ~1e-14 left)
+TOL_STOP64_EIGH = 1.0e-11  # eigh: the shifted block A + shift I (shift = ||A||_F + 1) has its singular
+                           # values clustered around the shift, so a sweep that starts at |cos| c leaves
+                           # ~c^2 shift / gap rather than c^2: 1e-8 left 1e-9 relative reconstruction
+                           # errors on rank-deficient blocks, 1e-11 reaches the rounding level
 INNER_SWEEPS32 = 1    # blocked FP32 phase: Jacobi sweeps among the rows of a super pair per visit
 BLOCKED_FP32 = [True]  # FP32 phase on super-vectors in shared memory (False: one pair per warp)
 BLOCKED_FP64 = [True]  # FP64 phase likewise, on 4-row super-vectors (False: one pair per warp)
@@ -400,7 +456,7 @@ def _jacobi(data, plan, U, S, V, mode, max_sweeps=MAX_SWEEPS):
         run_gemm(plan.xform, w64, data, w64, beta=1.0)
     else:
         run_gemm(plan.xform, w64, data, w64)
-    tol64 = TOL_STOP64_QR if plan.qr else TOL_STOP64
+    tol64 = TOL_STOP64_QR if plan.qr else (TOL_STOP64 if mode == 0 else TOL_STOP64_EIGH)
     if plan.rows_per_super64 and BLOCKED_FP64[0]:
         (dsup64,) = _dev(plan, 'svd_super64', (plan.super_items64,), dev)
         N.call('yb_svd_block_sweeps', _ptr(w64), _ptr(dblocks), nb, _ptr(dsup64), len(plan.super_items64),
@@ -495,8 +551,8 @@ def qr_backward(Q, R, gQ, gR, data, meta):
     dA = torch.zeros(data.numel(), dtype=data.dtype, device=dev)
     if len(plan.blocks) == 0:
         return dA
-    Bw = torch.zeros_like(Q) if gQ is None else gQ.contiguous().to(Q.dtype).clone()
-    gR = torch.zeros_like(R) if gR is None else gR.contiguous().to(R.dtype)
+    Bw = torch.zeros_like(Q) if gQ is None else _plain(gQ).to(Q.dtype).clone()
+    gR = torch.zeros_like(R) if gR is None else _plain(gR).to(R.dtype)
     M = torch.empty(plan.m_size, dtype=Q.dtype, device=dev)
     run_gemm(plan.w1, data, gR, Bw, beta=1.0)
     run_gemm(plan.m1, R, gR, M)
@@ -521,9 +577,9 @@ def svd_backward(U, S, V, gU, gS, gV, meta, data_size, dtype):
     if len(plan.recs) == 0:
         return dA
     code = _dtype_code(U.dtype)
-    gU = torch.zeros_like(U) if gU is None else gU.contiguous().to(U.dtype)
-    gV = torch.zeros_like(V) if gV is None else gV.contiguous().to(V.dtype)
-    gS = None if gS is None else gS.contiguous().to(torch.float64)
+    gU = torch.zeros_like(U) if gU is None else _plain(gU).to(U.dtype)
+    gV = torch.zeros_like(V) if gV is None else _plain(gV).to(V.dtype)
+    gS = None if gS is None else _plain(gS).to(torch.float64)
     Pm = torch.empty(plan.kk, dtype=U.dtype, device=dev)
     Qm = torch.empty(plan.kk, dtype=U.dtype, device=dev)
     Km = torch.empty(plan.kk, dtype=U.dtype, device=dev)
@@ -568,8 +624,8 @@ def eigh_backward(U, S, gU, gS, meta, data_size, dtype, order_by_magnitude=False
     dA = torch.zeros(data_size, dtype=dtype, device=dev)
     if len(plan.recs) == 0:
         return dA
-    gU = torch.zeros_like(U) if gU is None else gU.contiguous().to(U.dtype)
-    gS = None if gS is None else gS.contiguous().to(torch.float64)
+    gU = torch.zeros_like(U) if gU is None else _plain(gU).to(U.dtype)
+    gS = None if gS is None else _plain(gS).to(torch.float64)
     X = torch.empty(plan.kk, dtype=U.dtype, device=dev)
     K = torch.empty(plan.kk, dtype=U.dtype, device=dev)
     run_gemm(plan.gX, U, gU, X)
@@ -603,8 +659,8 @@ def fix_svd_signs_backward(U, V, gU, gV, meta):
     plan = P.svd_plan(meta, ROWS_PER_SUPER[0])
     nb = len(plan.blocks)
     need_u, need_v = gU is not None, gV is not None
-    gU = torch.zeros_like(U) if gU is None else gU.contiguous().to(U.dtype)
-    gV = torch.zeros_like(V) if gV is None else gV.contiguous().to(V.dtype)
+    gU = torch.zeros_like(U) if gU is None else _plain(gU).to(U.dtype)
+    gV = torch.zeros_like(V) if gV is None else _plain(gV).to(V.dtype)
     dU, dV = torch.zeros_like(U), torch.zeros_like(V)  # the kernel writes every position of the records
     if nb:
         (dblocks,) = _dev(plan, 'svd_blocks', (plan.blocks,), U.device)
@@ -631,7 +687,7 @@ def _idx_buffer(mask, meta, device):
 
 def apply_mask(A, mask, meta, Dsize, axis, ndim, scatter_size=None):
     """Gather kept indices along ``axis`` (scatter_size given: the adjoint scatter)."""
-    A = _check(A)
+    A = _check(A, any_dtype=True)
     idx, lengths = _idx_buffer(mask, meta, A.device)
     recs, items, _ = P.mask_plan(meta, axis, lengths)
     if scatter_size is None:
