@@ -1264,9 +1264,23 @@ def kernel_roofline(torch, dev, run_once, w, gemm_mode, reps=5):
         work = sum(16 * st[2][4] for st in merges)
         peak, unit, bound, src = peaks.get('hbm_gbs', 6800.0), "GB/s", "hbm", "hbm copy"
         achieved = work / tot[top] / 1e9
-    return {"bound": bound, "kernel": top, "achieved": achieved, "peak": peak, "unit": unit,
-            "frac": achieved / peak, "peak_source": "measured: " + src, "traffic": None,
-            "device_ms_per_matvec": {k: v * 1e3 for k, v in tot.items()}}
+    out = {"bound": bound, "kernel": top, "achieved": achieved, "peak": peak, "unit": unit,
+           "frac": achieved / peak, "peak_source": "measured: " + src, "traffic": None,
+           "device_ms_per_matvec": {k: v * 1e3 for k, v in tot.items()}}
+    if top == 'yb_ozaki_gemm_tc':
+        # DRAM bytes (read + write) of the two tcgen05 GEMM launches of one matvec, from the ncu
+        # capture in profiles/ozaki_gemm_tcgen05_dmrg_heff2.md; the digit planes they read
+        # (algorithmic bytes, tile layout) are computed here
+        digits = sum(2 * (P.ozaki_dot_plan(st[2][2], ops.OZAKI_SLICES).a_size_tc +
+                          P.ozaki_dot_plan(st[2][2], ops.OZAKI_SLICES).b_size_tc) for st in dots)
+        out.update(traffic=TC_GEMM_DRAM_BYTES_PER_MATVEC, traffic_unit="bytes per matvec (2 launches)",
+                   traffic_source="ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                  "profiles/ozaki_gemm_tcgen05_dmrg_heff2.md",
+                   algorithmic_bytes_per_matvec=digits)
+    return out
+
+
+TC_GEMM_DRAM_BYTES_PER_MATVEC = 21.497344e6 + 45.472512e6 + 256 + 25856  # ncu capture, DMRG Heff2 matvec
 
 
 def svd144_blocks(torch, dev):
