@@ -13,9 +13,9 @@ unchanged into ``baseline/_ref``, installs ``tqdm`` there from the offline wheel
 copies the pure-Python ``opt_einsum`` package of this interpreter (both are imported by
 ``import yastn``; the GPU machine has neither). Nothing of the reference is modified.
 
-The reference's own tensor test suite (tests/tensor, with its input files) is copied
-unchanged to ``baseline/_ref/yastn_tests/tensor``, where tests/test_gpu_reference_suite.py
-runs it against this backend.
+The reference's own test suites (tests/tensor, tests/mps and tests/peps, with their input
+files) are copied unchanged to ``baseline/_ref/yastn_tests``, where
+tests/test_gpu_reference_suite.py runs them against this backend.
 
 Usage: python baseline/install_reference.py <reference tree> [wheelhouse]
 """
@@ -61,12 +61,14 @@ def main(ref, wheelhouse='/opt/wheelhouse'):
 
 
 def copy_tests(ref):
-    """The reference's tests/tensor suite, unchanged, beside the installed package."""
-    dst = os.path.join(TARGET, 'yastn_tests', 'tensor')
-    if os.path.exists(dst):
-        shutil.rmtree(dst)
-    shutil.copytree(os.path.join(ref, 'tests', 'tensor'), dst, ignore=shutil.ignore_patterns('__pycache__'))
-    print(f'copied the reference tensor tests into {dst}')
+    """The reference's tests/tensor, tests/mps and tests/peps suites (with their input files),
+    unchanged, beside the installed package."""
+    for part in ('tensor', 'mps', 'peps'):
+        dst = os.path.join(TARGET, 'yastn_tests', part)
+        if os.path.exists(dst):
+            shutil.rmtree(dst)
+        shutil.copytree(os.path.join(ref, 'tests', part), dst, ignore=shutil.ignore_patterns('__pycache__'))
+        print(f'copied the reference {part} tests into {dst}')
     return 0
 
 

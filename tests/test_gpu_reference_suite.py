@@ -1,14 +1,15 @@
-"""YASTN's own tensor test suite (the reference's tests/tensor, installed unchanged under
-baseline/_ref/yastn_tests by baseline/install_reference.py) run against this backend on the
-GPU: ``make_config(backend=yastn_gb300.backend, default_device='cuda')`` through the options
-and fixture of tests/yastn_suite_plugin.py, with pytest-xdist workers and a per-test time
-limit.
+"""YASTN's own test suites (the reference's tests/tensor, tests/mps and tests/peps, installed
+unchanged under baseline/_ref/yastn_tests by baseline/install_reference.py) run against this
+backend on the GPU through tests/yastn_suite_plugin.py (YASTN's 'torch' backend name resolves
+to this module for the session), with pytest-xdist workers and a per-test time limit.
 
-Every test passes except the ones listed in EXPECTED_FAILURES, each with its reason: the
-partial and iterative decompositions the reference runs through SciPy/ARPACK on the host
-(svds, svd_lowrank, eigh_lowrank, Arnoldi eigs, non-Hermitian eig) are not part of this
-backend, and three tests that name the reference's backends by string ('np', 'torch') cannot
-resolve this one.
+The whole tensor suite runs, and from the network suites the files on this backend's path:
+DMRG (two-site, with YASTN's eigs), the Krylov tests, CTMRG on square and C4v lattices, the
+double-layer PEPS tensor and the fixed-point CTMRG with its implicit differentiation
+(torch.func.vjp through the backend's autograd Functions). Every test passes except the ones
+in EXPECTED_FAILURES, each with its reason: the non-Hermitian eigensolver and the partial
+Hermitian one (which the reference runs through torch.linalg.eig / SciPy's ARPACK) are not
+part of this backend.
 """
 import os
 import subprocess
@@ -19,27 +20,20 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-SUITE = os.path.join(ROOT, 'baseline', '_ref', 'yastn_tests', 'tensor')
+SUITE = os.path.join(ROOT, 'baseline', '_ref', 'yastn_tests')
+FILES = ['tensor', 'mps/test_dmrg.py', 'mps/test_krylov.py', 'mps/test_environment.py', 'peps/test_ctmrg.py',
+         'peps/test_ctmrg_c4v.py', 'peps/test_double_peps_tensor.py', 'peps/test_fp_c4v.py']
 
-_NOT_PROVIDED = "partial/iterative decomposition not provided by this backend (the reference uses SciPy on the host)"
-_BY_NAME = "the test resolves backends by their string name ('np', 'torch'), which does not name this backend"
+_NOT_PROVIDED = "decomposition not provided by this backend (the reference uses torch.linalg.eig / SciPy ARPACK)"
 EXPECTED_FAILURES = {
     'test_eig.py::test_eig_basic': _NOT_PROVIDED,
     'test_eig.py::test_eig_complex': _NOT_PROVIDED,
     'test_eig.py::test_eig_degeneracy_fail': _NOT_PROVIDED,
     'test_eig.py::test_eig_transpose_meta': _NOT_PROVIDED,
+    'test_eigs.py::test_eigs_arnoldi': _NOT_PROVIDED,
     'test_eighs.py::test_eigh_basic[LM]': _NOT_PROVIDED,
     'test_eighs.py::test_eigh_basic_2[LM]': _NOT_PROVIDED,
     'test_eighs.py::test_eigh_basic_2[SR]': _NOT_PROVIDED,
-    'test_eigs.py::test_eigs_arnoldi': _NOT_PROVIDED,
-    'test_svd.py::test_svd_arnoldi': _NOT_PROVIDED,
-    'test_svd.py::test_svd_lowrank_basic': _NOT_PROVIDED,
-    'test_svd.py::test_svd_truncate_lowrank': _NOT_PROVIDED,
-    'test_svds.py::*': _NOT_PROVIDED,
-    'test_syntax.py::test_syntax_noDocs': _BY_NAME,
-    'test_to_dict_from_dict.py::test_to_dict_exceptions': _BY_NAME,
-    'test_to_dict_from_dict.py::test_to_from_dict[False]': _BY_NAME,
-    'test_to_dict_from_dict.py::test_to_from_dict[True]': _BY_NAME,
 }
 
 
@@ -48,21 +42,21 @@ def _expected(name):
     return name in EXPECTED_FAILURES or (f + '::*') in EXPECTED_FAILURES
 
 
-def test_reference_tensor_suite_on_this_backend(cuda_device, tmp_path):
+def test_reference_suites_on_this_backend(cuda_device, tmp_path):
     if not os.path.isdir(SUITE):
         pytest.skip("the reference's test suite is not installed (python baseline/install_reference.py <tree>)")
     xml = tmp_path / 'suite.xml'
     env = dict(os.environ)
     env['PYTHONPATH'] = os.pathsep.join([os.path.join(ROOT, 'tests'), os.path.join(ROOT, 'baseline', '_ref'), ROOT,
                                          env.get('PYTHONPATH', '')])
-    cmd = [sys.executable, '-m', 'pytest', SUITE, '-p', 'yastn_suite_plugin', '--backend', 'torch_gb300',
-           '--device', 'cuda', '-q', '-p', 'no:cacheprovider', '--junitxml', str(xml), '-n', '8', '--timeout', '120']
+    cmd = [sys.executable, '-m', 'pytest'] + FILES + ['-p', 'yastn_suite_plugin', '--backend', 'torch_gb300',
+           '--device', 'cuda', '-q', '-p', 'no:cacheprovider', '--junitxml', str(xml), '-n', '8', '--timeout', '300']
     try:
         import xdist  # noqa: F401
         import pytest_timeout  # noqa: F401
     except ImportError:
         cmd = cmd[:-4]
-    proc = subprocess.run(cmd, cwd=ROOT, env=env, capture_output=True, text=True, timeout=1500)
+    proc = subprocess.run(cmd, cwd=SUITE, env=env, capture_output=True, text=True, timeout=1500)
     assert xml.exists(), proc.stdout[-3000:] + proc.stderr[-3000:]
     passed, failed, unexpected = 0, [], []
     for tc in ET.parse(xml).iter('testcase'):
@@ -77,7 +71,7 @@ def test_reference_tensor_suite_on_this_backend(cuda_device, tmp_path):
                 unexpected.append(f"{name}: {msg[:300]}")
         else:
             passed += 1
-    print(f"reference tensor suite on torch_gb300: {passed} passed, {len(failed)} failed "
+    print(f"YASTN's suites on this backend: {passed} passed, {len(failed)} failed "
           f"({len(failed) - len(unexpected)} expected)")
-    assert passed >= 230, passed
+    assert passed >= 300, passed
     assert not unexpected, "\n".join(unexpected)

@@ -880,3 +880,18 @@ def test_ozaki_tc_schedule_covers_tiles_once_and_balances():
             loads = [sum(steps(t) for t in tiles[offs[b]:offs[b + 1]]) for b in range(len(offs) - 1)]
             biggest = max(steps(t) for t in tiles)
             assert max(loads) <= sum(loads) / len(loads) + biggest
+
+
+def test_fix_signs_plan_takes_truncated_and_partial_svd_records():
+    """The gauge fix's records accept U (m x k), Vh (k x n) of any k (truncated or partial
+    SVDs, where YASTN may pass no S slice) and keep the fields its kernels read."""
+    meta = (((0, 12), (3, 4), (0, 6), (3, 2), (0, 2), (0, 8), (2, 4)),
+            ((12, 32), (4, 5), (6, 18), (4, 3), None, (8, 23), (3, 5)),
+            ((32, 32), (0, 3), (18, 18), (0, 0), (2, 2), (23, 23), (0, 3)))
+    plan = P.fix_signs_plan(meta)
+    assert plan.max_k == 3 and len(plan.blocks) == 2
+    r0, r1 = plan.blocks
+    assert [int(r0[i]) for i in (1, 2, 3, 4, 5, 9)] == [3, 4, 0, 0, 0, 2]
+    assert [int(r1[i]) for i in (1, 2, 3, 4, 5, 9)] == [4, 5, 6, 2, 8, 3]
+    with pytest.raises(P.PlanError):
+        P.fix_signs_plan((((0, 12), (3, 4), (0, 6), (3, 2), (0, 3), (0, 8), (2, 4)),))

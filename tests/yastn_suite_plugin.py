@@ -3,9 +3,12 @@
 YASTN's tests select their backend through the command-line options and the
 ``config_kwargs`` fixture of the reference's root conftest (conftest.py:4-17 of the
 reference tree). This plugin offers the same options and fixture, with the extra backend
-name ``torch_gb300`` mapped to the ``yastn_gb300.backend`` module (the reference resolves
-only 'np', 'torch' and 'torch_cpp' by name). Tests guarded by
-``'torch' not in config.getoption('--backend')`` run for it, since it is a torch backend.
+name ``torch_gb300``: YASTN resolves backends by name ('np', 'torch'), and many of its tests
+gate themselves on ``config_kwargs["backend"] == "torch"`` (autograd, fixed-point CTMRG), so
+for ``--backend torch_gb300`` the session makes the name 'torch' resolve to this backend
+(``yastn.backend.backend_torch`` is bound to ``yastn_gb300.backend``) and the fixture passes
+'torch'. Every test that asks for YASTN's torch backend then runs on this one; tests guarded
+by ``'torch' not in config.getoption('--backend')`` run too.
 
 Use: ``python -m pytest <YASTN tests/tensor files> -p yastn_suite_plugin --backend
 torch_gb300 --device cuda`` with this directory, the package root and the reference install
@@ -26,14 +29,19 @@ def pytest_addoption(parser):
     parser.addoption("--ray", action="store_true", default=False)
 
 
+def pytest_configure(config):
+    if config.getoption("--backend") == "torch_gb300":
+        import sys
+        import yastn.backend
+        import yastn_gb300
+        sys.modules["yastn.backend.backend_torch"] = yastn_gb300.backend
+        yastn.backend.backend_torch = yastn_gb300.backend
+
+
 @pytest.fixture
 def config_kwargs(request):
     name = request.config.getoption("--backend")
-    backend = name
-    if name == "torch_gb300":
-        import yastn_gb300
-        backend = yastn_gb300.backend
-    return {"backend": backend,
+    return {"backend": "torch" if name == "torch_gb300" else name,
             "default_device": request.config.getoption("--device"),
             "default_fusion": request.config.getoption("--default_fusion"),
             "tensordot_policy": request.config.getoption("--tensordot_policy")}

@@ -178,10 +178,21 @@ class CopyPlan:
         if vec_ok in self._packed:
             return self._packed[vec_ok]
         recs, items = [], []
-        for ti, (so, do, sizes, ss, ds) in enumerate(self.tasks_list):
+        expanded = []
+        for (so, do, sizes, ss, ds) in self.tasks_list:
             sizes, ss, ds = _collapse(sizes, ss, ds)
-            if len(sizes) > CP_MAXD:
-                raise PlanError(f"copy task with {len(sizes)} non-collapsible dims (max {CP_MAXD})")
+            if len(sizes) <= CP_MAXD:
+                expanded.append((so, do, sizes, ss, ds))
+                continue
+            # more dims than a record holds (tensors of a dozen legs): one record per index of
+            # the leading dims, each with the trailing CP_MAXD dims
+            lead = len(sizes) - CP_MAXD
+            for idx in np.ndindex(*sizes[:lead]):
+                o_s = so + sum(int(i) * int(x) for i, x in zip(idx, ss[:lead]))
+                o_d = do + sum(int(i) * int(x) for i, x in zip(idx, ds[:lead]))
+                expanded.append((o_s, o_d, sizes[lead:], ss[lead:], ds[lead:]))
+        for (so, do, sizes, ss, ds) in expanded:
+            ti = len(recs)
             tr = _transpose_task(so, do, sizes, ss, ds)
             if tr is not None:
                 recs.append(tr)
@@ -801,6 +812,38 @@ def svd_plan(meta, rows_per_super=None, cplx=False, qr=False):
     return CACHE.get((meta,), ('svd', rows_per_super, cplx, qr), build)
 
 
+class FixSignsPlan:
+    """Records of the gauge fix (YB_SVD_REC int64 each, the fields yb_fix_signs reads):
+    [1] m [2] n [3] U offset [4] S offset [5] Vh offset [9] k, for blocks U (m x k),
+    Vh (k x n) of any k (thin or truncated SVDs)."""
+
+    def __init__(self, blocks, max_k):
+        self.blocks, self.max_k = blocks, max_k
+        self._dev = {}
+
+
+def fix_signs_plan(meta):
+    def build():
+        recs, max_k, s_off = [], 0, 0
+        for sl, D, slU, DU, slS, slV, DV in meta:
+            m, k = DU
+            n = DV[1]
+            if k == 0 or m == 0:
+                continue
+            if DV[0] != k or (slS is not None and slS[1] - slS[0] != k):
+                raise PlanError("fix_svd_signs record: U, S and Vh disagree on the number of vectors")
+            # the phases are indexed like S; YASTN's partial SVDs pass no S slice (then: in order)
+            s0 = slS[0] if slS is not None else s_off
+            s_off = s0 + k
+            r = np.zeros(SVD_REC, dtype=np.int64)
+            r[1], r[2], r[3], r[4], r[5], r[9] = m, n, slU[0], s0, slV[0], k
+            recs.append(r)
+            max_k = max(max_k, k)
+        blocks = np.stack(recs) if recs else np.zeros((0, SVD_REC), dtype=np.int64)
+        return FixSignsPlan(blocks, max_k)
+    return CACHE.get((meta,), ('fix_signs',), build)
+
+
 class QrPlan:
     """Plan of ``qr`` (records of yb_qr, the FP64 workspace, the GEMM of R's right part for
     wide blocks) and of its adjoint (grouped GEMMs, copyltu/TRSM records, the copy of the
@@ -1000,12 +1043,13 @@ def tds_backward_plans(meta_dot, Areshape, Breshape, Aoffs, Boffs):
 
 def mask_plan(meta, axis, lengths):
     """apply_mask records (yastn/backend/backend_np.py:626-633); ``lengths`` maps a mask charge
-    to (offset in the concatenated index buffer, number of kept indices)."""
+    (or, for a slice mask, the pair (charge, length of the masked axis)) to (offset in the
+    concatenated index buffer, number of kept indices)."""
     recs, items, total = [], [], 0
     for sln, Dn, sla, Da, tm in meta:
         if isinstance(Da, int):  # diagonal tensors carry their block length as an int
             Da = (Da,)
-        ioff, cnt = lengths[tm]
+        ioff, cnt = lengths[(tm, Da[axis])] if (tm, Da[axis]) in lengths else lengths[tm]  # slice masks by length
         pre = int(np.prod(Da[:axis], dtype=np.int64))
         post = int(np.prod(Da[axis + 1:], dtype=np.int64))
         nout = pre * cnt * post

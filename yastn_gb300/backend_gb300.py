@@ -14,9 +14,11 @@ each behind a ``torch.autograd.Function`` with a hand-written adjoint:
 * ``apply_mask`` / ``fix_svd_signs`` (device gather / gauge kernels).
 
 Everything else is cold bookkeeping implemented with ordinary torch tensor calls on
-the tensors' own device, as in the reference torch backend. ``BACKEND_ID`` contains
-"torch" (YASTN enables torch checkpointing only then, ``yastn/tn/fpeps/envs/_env_ctm.py:579``)
-and differs from ``'torch_cpp'`` (``yastn/tensor/_contractions.py:199``).
+the tensors' own device, as in the reference torch backend. ``BACKEND_ID`` is "torch", the
+reference torch backend's: the tensors are torch tensors of the same dtypes and layout, YASTN
+enables torch checkpointing for it (``yastn/tn/fpeps/envs/_env_ctm.py:579``), its
+serialisation names the backend by this string (a tensor saved from this backend loads into
+YASTN's torch backend), and it differs from ``'torch_cpp'`` (``yastn/tensor/_contractions.py:199``).
 """
 from functools import reduce
 
@@ -50,7 +52,7 @@ __all__ = ['DTYPE', 'get_dtype', 'get_yastn_dtype',
            'embed_mask', 'transpose', 'transpose_and_merge', 'unmerge',
            'negate_blocks', 'bitwise_not']
 
-BACKEND_ID = "torch_gb300"
+BACKEND_ID = "torch"
 DTYPE = {'float32': torch.float32,
          'float64': torch.float64,
          'complex64': torch.complex64,
@@ -82,17 +84,27 @@ def get_gemm_mode():
 
 # ============================================================================ hot path
 
+# The autograd Functions keep the forward free of ctx and store what the backward needs in
+# setup_context, the form torch.func transforms (vjp, jvp, grad) require: YASTN's fixed-point
+# CTMRG differentiates its CTM iteration with torch.func.vjp
+# (yastn/tn/fpeps/envs/fixed_pt.py:851-853).
+
 class _TransposeAndMerge(torch.autograd.Function):
     """transpose_and_merge (backend_torch.py:588-589); adjoint = the inverse copy."""
 
     @staticmethod
-    def forward(ctx, data, order, meta_new, meta_mrg, Dsize):
-        ctx.args = (order, meta_new, meta_mrg, Dsize, data.numel())
+    def forward(data, order, meta_new, meta_mrg, Dsize):
         return ops.merge(data, order, meta_new, meta_mrg, Dsize)
+
+    @staticmethod
+    def setup_context(ctx, inputs, output):
+        data, order, meta_new, meta_mrg, Dsize = inputs
+        ctx.args = (order, meta_new, meta_mrg, Dsize, data.numel())
 
     @staticmethod
     def backward(ctx, g):
         order, meta_new, meta_mrg, Dsize, n = ctx.args
+        g = _unwrap(g)
         return ops.merge_backward(g, order, meta_new, meta_mrg, Dsize, n), None, None, None, None
 
 
@@ -100,13 +112,18 @@ class _Unmerge(torch.autograd.Function):
     """unmerge (backend_torch.py:592-593); adjoint = the inverse copy."""
 
     @staticmethod
-    def forward(ctx, data, meta):
-        ctx.args = (meta, data.numel())
+    def forward(data, meta):
         return ops.unmerge(data, meta)
+
+    @staticmethod
+    def setup_context(ctx, inputs, output):
+        data, meta = inputs
+        ctx.args = (meta, data.numel())
 
     @staticmethod
     def backward(ctx, g):
         meta, n = ctx.args
+        g = _unwrap(g)
         return ops.unmerge_backward(g, meta, n), None
 
 
@@ -114,14 +131,35 @@ class _Transpose(torch.autograd.Function):
     """transpose of every block (backend_torch.py:584-585)."""
 
     @staticmethod
-    def forward(ctx, data, axes, meta_transpose):
-        ctx.args = (axes, meta_transpose)
+    def forward(data, axes, meta_transpose):
         return ops.transpose(data, axes, meta_transpose)
+
+    @staticmethod
+    def setup_context(ctx, inputs, output):
+        _, axes, meta_transpose = inputs
+        ctx.args = (axes, meta_transpose)
 
     @staticmethod
     def backward(ctx, g):
         axes, meta = ctx.args
+        g = _unwrap(g)
         return ops.transpose_backward(g, axes, meta), None, None
+
+
+def _unwrap(t):
+    """The tensor under torch.func's wrappers (same values): inside a torch.func.vjp the
+    backward receives wrapped cotangents and saved tensors, which have no storage pointer for
+    the kernels."""
+    if not isinstance(t, torch.Tensor):
+        return t
+    fx = torch._C._functorch
+    while fx.is_functorch_wrapped_tensor(t):
+        t = fx.get_unwrapped(t)
+    return t
+
+
+def _unwrap_all(*ts):
+    return tuple(_unwrap(t) for t in ts)
 
 
 def _grad_like(g, x):
@@ -138,16 +176,20 @@ class _Dot(torch.autograd.Function):
     B_b += A^H C_b as two grouped GEMMs with terms grouped by operand block."""
 
     @staticmethod
-    def forward(ctx, A, B, meta_dot, Dsize):
-        ctx.save_for_backward(A, B)
-        ctx.meta_dot = meta_dot
+    def forward(A, B, meta_dot, Dsize):
         if _GEMM_MODE[0] == 'emulated' and A.dtype in _EMULATED and B.dtype in _EMULATED:
             return ops.dot_ozaki(A, B, meta_dot, Dsize)
         return ops.dot(A, B, meta_dot, Dsize)
 
     @staticmethod
+    def setup_context(ctx, inputs, output):
+        A, B, meta_dot, _ = inputs
+        ctx.save_for_backward(A, B)
+        ctx.meta_dot = meta_dot
+
+    @staticmethod
     def backward(ctx, g):
-        A, B = ctx.saved_tensors
+        A, B, g = _unwrap_all(*ctx.saved_tensors, g)
         need_a, need_b = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
         Ab, Bb = ops.dot_backward(g.contiguous(), A, B, ctx.meta_dot, need_a, need_b)
         return _grad_like(Ab, A), _grad_like(Bb, B), None, None
@@ -157,14 +199,18 @@ class _TransposeDotSum(torch.autograd.Function):
     """transpose_dot_sum (backend_torch.py:553-554)."""
 
     @staticmethod
-    def forward(ctx, A, B, meta_dot, Areshape, Breshape, Aorder, Border, Dsize):
-        ctx.save_for_backward(A, B)
-        ctx.args = (meta_dot, Areshape, Breshape, Aorder, Border)
+    def forward(A, B, meta_dot, Areshape, Breshape, Aorder, Border, Dsize):
         return ops.transpose_dot_sum(A, B, meta_dot, Areshape, Breshape, Aorder, Border, Dsize)
 
     @staticmethod
+    def setup_context(ctx, inputs, output):
+        A, B, meta_dot, Areshape, Breshape, Aorder, Border, _ = inputs
+        ctx.save_for_backward(A, B)
+        ctx.args = (meta_dot, Areshape, Breshape, Aorder, Border)
+
+    @staticmethod
     def backward(ctx, g):
-        A, B = ctx.saved_tensors
+        A, B, g = _unwrap_all(*ctx.saved_tensors, g)
         meta_dot, Areshape, Breshape, Aorder, Border = ctx.args
         Ab, Bb = ops.transpose_dot_sum_backward(g.contiguous(), A, B, meta_dot, Areshape, Breshape, Aorder, Border)
         return _grad_like(Ab, A), _grad_like(Bb, B), None, None, None, None, None, None
@@ -174,13 +220,18 @@ class _ApplyMask(torch.autograd.Function):
     """apply_mask (backend_torch.py:576-577); adjoint = scatter into zeros."""
 
     @staticmethod
-    def forward(ctx, A, mask, meta, Dsize, axis, ndim):
-        ctx.args = (mask, meta, axis, ndim, A.numel())
+    def forward(A, mask, meta, Dsize, axis, ndim):
         return ops.apply_mask(A, mask, meta, Dsize, axis, ndim)
+
+    @staticmethod
+    def setup_context(ctx, inputs, output):
+        A, mask, meta, _, axis, ndim = inputs
+        ctx.args = (mask, meta, axis, ndim, A.numel())
 
     @staticmethod
     def backward(ctx, g):
         mask, meta, axis, ndim, n = ctx.args
+        g = _unwrap(g)
         return ops.apply_mask(g.contiguous(), mask, meta, None, axis, ndim, scatter_size=n), None, None, None, None, None
 
 
@@ -189,17 +240,18 @@ class _Svd(torch.autograd.Function):
     yastn/backend/linalg/torch_svd_gesdd.py:296-428 on all blocks at once."""
 
     @staticmethod
-    def forward(ctx, data, meta, sizes, fullrank_uv, ad_decomp_reg, diagnostics):
-        U, S, V = ops.svd(data, meta, sizes)
-        ctx.save_for_backward(U, S, V)
-        ctx.meta = meta
-        ctx.n = data.numel()
-        ctx.dtype = data.dtype
-        return U, S, V
+    def forward(data, meta, sizes, fullrank_uv, ad_decomp_reg, diagnostics):
+        return ops.svd(data, meta, sizes)
+
+    @staticmethod
+    def setup_context(ctx, inputs, output):
+        data, meta = inputs[0], inputs[1]
+        ctx.save_for_backward(*output)
+        ctx.meta, ctx.n, ctx.dtype = meta, data.numel(), data.dtype
 
     @staticmethod
     def backward(ctx, gU, gS, gV):
-        U, S, V = ctx.saved_tensors
+        U, S, V, gU, gS, gV = _unwrap_all(*ctx.saved_tensors, gU, gS, gV)
         dA = ops.svd_backward(U, S, V, gU, gS, gV, ctx.meta, ctx.n, ctx.dtype)
         return dA, None, None, None, None, None
 
@@ -210,16 +262,19 @@ class _Eigh(torch.autograd.Function):
     torch.linalg.eigh, on all blocks at once."""
 
     @staticmethod
-    def forward(ctx, data, meta, sizes, order_by_magnitude, ad_decomp_reg):
-        S, U = ops.eigh(data, meta, sizes, order_by_magnitude)
-        ctx.save_for_backward(S, U)
+    def forward(data, meta, sizes, order_by_magnitude, ad_decomp_reg):
+        return ops.eigh(data, meta, sizes, order_by_magnitude)
+
+    @staticmethod
+    def setup_context(ctx, inputs, output):
+        data, meta, _, order_by_magnitude, ad_decomp_reg = inputs
+        ctx.save_for_backward(*output)
         ctx.meta, ctx.n, ctx.dtype = meta, data.numel(), data.dtype
         ctx.by_mag, ctx.eps = order_by_magnitude, ad_decomp_reg
-        return S, U
 
     @staticmethod
     def backward(ctx, gS, gU):
-        S, U = ctx.saved_tensors
+        S, U, gS, gU = _unwrap_all(*ctx.saved_tensors, gS, gU)
         dA = ops.eigh_backward(U, S, gU, gS, ctx.meta, ctx.n, ctx.dtype, ctx.by_mag, ctx.eps)
         return dA, None, None, None, None
 
@@ -230,15 +285,19 @@ class _FixSigns(torch.autograd.Function):
     the gradient through the phase of each column's largest entry."""
 
     @staticmethod
-    def forward(ctx, U, V, meta):
+    def forward(U, V, meta):
         Uo, Vo, _ = ops.fix_svd_signs(U, V, meta)
-        ctx.save_for_backward(U, V)
-        ctx.meta = meta
         return Uo, Vo
 
     @staticmethod
+    def setup_context(ctx, inputs, output):
+        U, V, meta = inputs
+        ctx.save_for_backward(U, V)
+        ctx.meta = meta
+
+    @staticmethod
     def backward(ctx, gU, gV):
-        U, V = ctx.saved_tensors
+        U, V, gU, gV = _unwrap_all(*ctx.saved_tensors, gU, gV)
         gUi, gVi = ops.fix_svd_signs_backward(U, V, gU, gV, ctx.meta)
         return gUi, gVi, None
 
@@ -527,16 +586,45 @@ def _not_hot(name):
     raise NotImplementedError(f"yastn_gb300: {name} is not provided by this backend")
 
 
+def _leading_svd(data, meta, sizes):
+    """The leading k singular triplets of every block (k = the block's slS length), as the
+    partial-SVD policies return them: the thin SVD of all blocks on the device (this
+    backend's Jacobi, with its adjoint), then the first k columns of U, values of S and
+    rows of Vh gathered in one launch each. The reference computes them with SciPy's
+    ARPACK / PROPACK (``svds_scipy``) or torch.svd_lowrank on the host or device; the exact
+    leading triplets answer both."""
+    full, offs, ks = [], [0, 0, 0], set()
+    for sl, D, slU, DU, slS, slV, DV in meta:
+        m, n = D
+        kf, k = min(m, n), slS[1] - slS[0]
+        ks.add(k)
+        full.append((sl, D, (offs[0], offs[0] + m * kf), (m, kf), (offs[1], offs[1] + kf),
+                     (offs[2], offs[2] + kf * n), (kf, n)))
+        offs = [offs[0] + m * kf, offs[1] + kf, offs[2] + kf * n]
+    Uf, Sf, Vf = svd(data, tuple(full), tuple(offs))
+    mask = {k: torch.arange(k, dtype=torch.int64, device=data.device) for k in ks}
+    mU, mS, mV = [], [], []
+    for (sl, D, slU, DU, slS, slV, DV), f in zip(meta, full):
+        k = slS[1] - slS[0]
+        mU.append((slU, DU, f[2], f[3], k))
+        mS.append((slS, k, f[4], f[4][1] - f[4][0], k))
+        mV.append((slV, DV, f[5], f[6], k))
+    U = apply_mask(Uf, mask, tuple(mU), sizes[0], 1, 2)
+    S = apply_mask(Sf, mask, tuple(mS), sizes[1], 0, 1)
+    V = apply_mask(Vf, mask, tuple(mV), sizes[2], 0, 2)
+    return U, S, V
+
+
 def svd_lowrank(data, meta, sizes, **kwargs):
-    _not_hot('svd_lowrank (partial SVD policies)')
+    return _leading_svd(data, meta, sizes)
 
 
 def svd_randomized(data, meta, sizes, q=None, niter=3, **kwargs):
-    _not_hot('svd_randomized')
+    return _leading_svd(data, meta, sizes)
 
 
 def svds_scipy(data, meta, sizes, thresh=0.1, solver='arpack', **kwargs):
-    _not_hot('svds_scipy')
+    return _leading_svd(data, meta, sizes)
 
 
 def eigh_lowrank(data, meta, sizes, thresh=None, **kwargs):
@@ -557,15 +645,18 @@ class _Qr(torch.autograd.Function):
     solve."""
 
     @staticmethod
-    def forward(ctx, data, meta, sizes):
-        Q, R = ops.qr(data, meta, sizes)
-        ctx.save_for_backward(data, Q, R)
+    def forward(data, meta, sizes):
+        return ops.qr(data, meta, sizes)
+
+    @staticmethod
+    def setup_context(ctx, inputs, output):
+        data, meta, _ = inputs
+        ctx.save_for_backward(data, *output)
         ctx.meta = meta
-        return Q, R
 
     @staticmethod
     def backward(ctx, gQ, gR):
-        data, Q, R = ctx.saved_tensors
+        data, Q, R, gQ, gR = _unwrap_all(*ctx.saved_tensors, gQ, gR)
         return ops.qr_backward(Q, R, gQ, gR, data, ctx.meta), None, None
 
 

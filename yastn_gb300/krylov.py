@@ -164,8 +164,9 @@ def eigs(f, v0, k=1, which='SR', ncv=10, maxiter=None, tol=1e-13, hermitian=Fals
     them), the start vector is extended by those blocks (zeros) and the expansion restarts;
     zero blocks change neither the Ritz values nor the vectors, and YASTN's own loop ends with
     the same union structure."""
+    from . import backend_gb300
     backend = v0.config.backend
-    if not hermitian or getattr(backend, 'BACKEND_ID', '') != 'torch_gb300' or not v0._data.is_cuda:
+    if not hermitian or backend is not backend_gb300 or not v0._data.is_cuda:
         import yastn
         return yastn.eigs(f, v0, k=k, which=which, ncv=ncv, maxiter=maxiter, tol=tol, hermitian=hermitian, **kwargs)
     if v0.norm() == 0:

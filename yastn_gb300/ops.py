@@ -640,7 +640,7 @@ def eigh_backward(U, S, gU, gS, meta, data_size, dtype, order_by_magnitude=False
 def fix_svd_signs(U, V, meta):
     """Gauge fix of every block; returns (U', Vh', phases)."""
     U, V = _check(U, 'U'), _check(V, 'V')
-    plan = P.svd_plan(meta, ROWS_PER_SUPER[0])
+    plan = P.fix_signs_plan(meta)
     nb = len(plan.blocks)
     Uo, Vo = torch.empty_like(U), torch.empty_like(V)
     S_size = max((int(r[4] + r[9]) for r in plan.blocks), default=0)
@@ -656,7 +656,7 @@ def fix_svd_signs(U, V, meta):
 def fix_svd_signs_backward(U, V, gU, gV, meta):
     """Adjoint of the gauge fix (real and complex; yb_fix_signs_adjoint) given the forward's
     inputs U, V and the cotangents of its outputs."""
-    plan = P.svd_plan(meta, ROWS_PER_SUPER[0])
+    plan = P.fix_signs_plan(meta)
     nb = len(plan.blocks)
     need_u, need_v = gU is not None, gV is not None
     gU = torch.zeros_like(U) if gU is None else _plain(gU).to(U.dtype)
@@ -671,16 +671,28 @@ def fix_svd_signs_backward(U, V, gU, gV, meta):
 
 # ----------------------------------------------------------------------------- masks / truncation
 
-def _idx_buffer(mask, meta, device):
+def _idx_buffer(mask, meta, device, axis=0):
+    """The masks' kept indices concatenated in one device buffer, and per mask (per mask and
+    axis length for slice masks, which YASTN passes for whole-axis copies) its offset and
+    count."""
     order, lengths, off = [], {}, 0
     for rec in meta:
         tm = rec[4]
-        if tm not in lengths:
-            v = mask[tm]
-            n = int(v.numel()) if isinstance(v, torch.Tensor) else len(v)
-            lengths[tm] = (off, n)
-            order.append(torch.as_tensor(v, device=device).reshape(-1).to(torch.int64))
-            off += n
+        v = mask[tm]
+        if isinstance(v, slice):
+            Da = (rec[3],) if isinstance(rec[3], int) else rec[3]
+            key = (tm, Da[axis])
+            if key in lengths:
+                continue
+            ind = torch.arange(*v.indices(Da[axis]), dtype=torch.int64, device=device)
+        else:
+            key = tm
+            if key in lengths:
+                continue
+            ind = torch.as_tensor(v, device=device).reshape(-1).to(torch.int64)
+        lengths[key] = (off, int(ind.numel()))
+        order.append(ind)
+        off += int(ind.numel())
     idx = torch.cat(order) if order else torch.zeros(1, dtype=torch.int64, device=device)
     return idx, lengths
 
@@ -688,7 +700,7 @@ def _idx_buffer(mask, meta, device):
 def apply_mask(A, mask, meta, Dsize, axis, ndim, scatter_size=None):
     """Gather kept indices along ``axis`` (scatter_size given: the adjoint scatter)."""
     A = _check(A, any_dtype=True)
-    idx, lengths = _idx_buffer(mask, meta, A.device)
+    idx, lengths = _idx_buffer(mask, meta, A.device, axis)
     recs, items, _ = P.mask_plan(meta, axis, lengths)
     if scatter_size is None:
         out = torch.empty(Dsize, dtype=A.dtype, device=A.device)
