@@ -105,7 +105,8 @@ int yb_block_copy(const void* src, void* dst, int unit_bytes,
  *   m <= 16 rows and columns [w*col, w*col + w) with w = 1024 for m <= 8, 256 above (tile
  *   row 0; the host's plans use skinny tiles for m <= 8); kind 2: a short skinny tile, for an
  *   output of one term with m <= 8 rows and K <= 8 (any n), covering all rows and the 512
- *   columns [512*col, 512*col + 512).
+ *   columns [512*col, 512*col + 512); its "tile row" field holds the index of that term (the
+ *   output's first term), so that the output and term records are read at once.
  * dtype: YB_F64 or YB_C128 (alpha, beta are real).
  * Replaces dot (one term per output), transpose_dot_sum after the merge of its operands,
  * and the adjoint products A_b += C_b B^H, B_b += A^H C_b (terms grouped by operand block).
@@ -120,7 +121,7 @@ int yb_grouped_gemm(const void* a, const void* b, void* c, int dtype,
                     double alpha, double beta, void* stream);
 /* yb_grouped_gemm_short: yb_grouped_gemm for plans whose tiles are all of kind 2 (the
  * contractions of a tensor with a small MPO block): a kernel of its own with few registers,
- * several CTAs per SM, all loads of a thread's columns issued before its FMAs. */
+ * eight warps per SM scheduler, all loads of a thread's columns issued before its FMAs. */
 int yb_grouped_gemm_short(const void* a, const void* b, void* c, int dtype,
                           const int64_t* outs, const int64_t* terms, const int32_t* tiles, int n_tiles,
                           double alpha, double beta, void* stream);

@@ -106,7 +106,7 @@ def _run_outs(outs, terms, tiles, a, b, c, alpha, beta):
             want = {(0, j, 1) for j in range((n + w - 1) // w)}
         elif any(kd == 2 for _, _, kd in seen.get(oi, ())):  # short skinny: m <= 8, one term, K <= 8
             assert m <= 8 and t1 - t0 == 1 and int(plan.terms[t0][2]) <= 8, "short tiles: m <= 8, one term, K <= 8"
-            want = {(0, j, 2) for j in range((n + 511) // 512)}
+            want = {(t0, j, 2) for j in range((n + 511) // 512)}  # tile row: the term index
         else:
             want = {(i, j, 0) for i in range((m + 63) // 64) for j in range((n + 63) // 64)}
         assert seen.get(oi, set()) == want, "tiles do not cover the output"

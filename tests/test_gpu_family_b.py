@@ -352,3 +352,34 @@ def test_short_skinny_gemm_values_and_nan(cuda_device):
     np.testing.assert_array_equal(np.isinf(got2), np.isinf(ref2))
     ok = np.isfinite(ref2)
     assert np.abs(got2[ok] - ref2[ok]).max() <= TOL * np.abs(ref2[ok]).max()
+
+
+def test_short_skinny_gemm_alpha_beta_complex_and_eight_rows(cuda_device):
+    """The short skinny kernel's other compiled forms: alpha/beta (C = alpha A B + beta C, the
+    form the decompositions call), complex128 strips, and sectors of 5..8 rows or K of 5..8
+    (A read per use, columns in passes), all against the oracle."""
+    from yastn_gb300 import _plans as P
+    rng = np.random.default_rng(43)
+    shapes = [(3, 4, 1500), (8, 7, 900), (5, 2, 513), (2, 8, 1030), (1, 1, 40)]
+    meta, oa, ob, oc = [], 0, 0, 0
+    for m, k, n in shapes:
+        meta.append(((oc, oc + m * n), (m, n), (oa, oa + m * k), (m, k), (ob, ob + k * n), (k, n)))
+        oa += m * k; ob += k * n; oc += m * n
+    meta = tuple(meta)
+    plan = P.dot_plan(meta)
+    assert plan.all_short
+    for cplx in (False, True):
+        A, B, C0 = rng.normal(size=oa), rng.normal(size=ob), rng.normal(size=oc)
+        if cplx:
+            A = A + 1j * rng.normal(size=oa)
+            B = B + 1j * rng.normal(size=ob)
+            C0 = C0 + 1j * rng.normal(size=oc)
+        ref = oracle.dot(A, B, meta, oc)
+        got = host(ops.dot(dev(A), dev(B), meta, oc))
+        assert rel(got, ref) <= TOL
+        got_ab = host(ops.run_gemm(plan, dev(A), dev(B), dev(C0), alpha=-0.5, beta=1.5))
+        assert rel(got_ab, -0.5 * ref + 1.5 * C0) <= TOL
+        # beta = 0 with alpha != 1 never reads C: a NaN there does not reach the result
+        Cn = np.full(oc, np.nan, dtype=C0.dtype)
+        got_a = host(ops.run_gemm(plan, dev(A), dev(B), dev(Cn), alpha=2.0, beta=0.0))
+        assert rel(got_a, 2.0 * ref) <= TOL

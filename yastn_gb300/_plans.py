@@ -356,8 +356,9 @@ SPLITK_MIN_K = 128       # shortest K chunk
 
 def _tiles_for(outs, terms):
     """Tiles (output, tile row, tile col, kind): kind 0 = 64x64, kind 1 = skinny (all m <= 16
-    rows x 1024 columns, 256 above 8 rows), ordered by descending work so long tiles start
-    first."""
+    rows x 1024 columns, 256 above 8 rows), kind 2 = short skinny (all m <= 8 rows x 512
+    columns; its tile row holds the output's single term index, so the kernel loads the output
+    and term records at once), ordered by descending work so long tiles start first."""
     tiles = []
     for oi, o in enumerate(outs):
         m, n = int(o[1]), int(o[2])
@@ -368,8 +369,9 @@ def _tiles_for(outs, terms):
         kind = tile_kind(m, n, ks)
         if kind:
             w = _tile_cols(kind, m)
+            tr = int(o[4]) if kind == 2 else 0
             for tc in range((n + w - 1) // w):
-                tiles.append((kk * m * 16, oi, 0, tc, kind))
+                tiles.append((kk * m * 16, oi, tr, tc, kind))
             continue
         for tr in range((m + GEMM_TILE - 1) // GEMM_TILE):
             for tc in range((n + GEMM_TILE - 1) // GEMM_TILE):

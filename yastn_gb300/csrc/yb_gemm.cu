@@ -139,21 +139,32 @@ __device__ __forceinline__ void skinny_dispatch(int64_t mr, const typename F::T*
 }
 
 // Short skinny outputs (one term, at most 8 rows, K <= 8; the contractions with a small
-// MPO block): op(A) goes to shared memory once, every thread issues all K x kShortCols loads of
-// its columns of op(B) before the FMAs, so the strip's loads are in flight together; the
-// work is FP64-bound (m K FMAs per column), and the kernel of its own (few registers, several
-// CTAs per SM) keeps the DFMA pipe fed.
-constexpr int kShortK = 8;
-constexpr int kShortCols = 2;  // columns per thread: a tile is kThreads * kShortCols columns
-template <class F, int M, int KB>
+// MPO block): C (mr rows x a strip of YB_GEMM_SHORT_COLS columns) = alpha op(A) op(B) + beta C.
+// GB300 issues 2 DFMA per SM per cycle, so the m K FMAs per column bound these strips rather
+// than their bytes, and the pipe stays fed only while enough warps have their loads back: a
+// strip's record reads are one round trip (the tile names both the output and its term), a
+// thread keeps few registers (eight warps per SM scheduler) and issues its loads of op(B)
+// before the barrier that publishes op(A) in shared memory. NT threads own
+// YB_GEMM_SHORT_COLS / NT columns each, NT apart (every load and store instruction of a warp
+// is coalesced), in passes of G columns. The epilogue of alpha = 1, beta = 0 is compiled
+// apart: an if-converted alpha multiply would cost one DMUL per output on the FP64 pipe.
+__host__ __device__ constexpr int short_pass(int elem_bytes, int M, int KB, int cpt) {
+  int g = cpt;  // columns per pass: op(B) and accumulators within 32 registers
+  while (g > 1 && (KB + M) * g * elem_bytes / 4 > 32) g >>= 1;
+  return g;
+}
+
+template <class F, int M, int KB, bool PLAIN, int NT>
 __device__ __forceinline__ void short_tile(const typename F::T* __restrict__ A, const typename F::T* __restrict__ B,
                                            typename F::T* __restrict__ C, const int64_t* __restrict__ orec,
                                            const int64_t* __restrict__ trec, int tcol, double alpha, double beta,
-                                           bool unit_alpha, bool zero_beta, typename F::T* Ak) {
+                                           typename F::T* Ak) {
   using T = typename F::T;
+  constexpr int CPT = YB_GEMM_SHORT_COLS / NT;  // columns per thread
+  constexpr int G = short_pass((int)sizeof(T), M, KB, CPT);
   const int64_t c_off = orec[0], ldc = orec[3], nc = orec[2];
-  const int mr = (int)orec[1], K = (int)trec[2];
-  const T* La = A + trec[0];
+  const int mr = M <= 4 ? M : (int)orec[1];  // M is exact below 5 rows
+  const int K = (int)trec[2];
   const int64_t l_is = trec[3], l_ls = trec[4], r_ls = trec[5], r_js = trec[6];
   const int flags = (int)trec[7];
   const bool conjL = flags & 1, conjR = flags & 2;
@@ -161,91 +172,113 @@ __device__ __forceinline__ void short_tile(const typename F::T* __restrict__ A, 
     const int i = threadIdx.x % M, l = threadIdx.x / M;
     T v = F::zero();
     if (l < K && i < mr) {
-      v = La[i * l_is + l * l_ls];
+      v = __ldg(A + trec[0] + i * l_is + l * l_ls);
       if (conjL) v = F::conj(v);
     }
     Ak[l * M + i] = v;
   }
-  __syncthreads();
-  const int64_t j0 = (int64_t)tcol * (kThreads * kShortCols) + threadIdx.x;
-  const T* Rb = B + trec[1];
-  T b[KB][kShortCols];
+  const int64_t j0 = (int64_t)tcol * YB_GEMM_SHORT_COLS + threadIdx.x;
+  const T* __restrict__ Rb = B + trec[1];
+  T b[KB][G];
+  auto load_b = [&](int u0) {
 #pragma unroll
-  for (int u = 0; u < kShortCols; ++u) {
-    const int64_t j = j0 + u * kThreads;
-    const bool live = j < nc;
-    const T* col = Rb + (live ? j * r_js : 0);
+    for (int u = 0; u < G; ++u) {
+      const int64_t j = j0 + (u0 + u) * NT;
+      const bool live = j < nc;
+      const T* col = Rb + (live ? j * r_js : 0);
+#pragma unroll
+      for (int l = 0; l < KB; ++l) {
+        b[l][u] = (live && l < K) ? __ldg(col + l * r_ls) : F::zero();
+        if (conjR) b[l][u] = F::conj(b[l][u]);
+      }
+    }
+  };
+  load_b(0);
+  __syncthreads();  // op(A) staged
+#pragma unroll
+  for (int u0 = 0; u0 < CPT; u0 += G) {
+    if (u0) load_b(u0);
+    T acc[G][M];
+#pragma unroll
+    for (int u = 0; u < G; ++u)
+#pragma unroll
+      for (int i = 0; i < M; ++i) acc[u][i] = F::zero();
 #pragma unroll
     for (int l = 0; l < KB; ++l) {
-      b[l][u] = (live && l < K) ? col[l * r_ls] : F::zero();
-      if (conjR) b[l][u] = F::conj(b[l][u]);
+      if (l < K) {
+#pragma unroll
+        for (int i = 0; i < M; ++i) {
+          const T ai = Ak[l * M + i];
+#pragma unroll
+          for (int u = 0; u < G; ++u) F::fma(acc[u][i], ai, b[l][u]);
+        }
+      }
     }
-  }
-  T acc[kShortCols][M];
 #pragma unroll
-  for (int u = 0; u < kShortCols; ++u)
+    for (int u = 0; u < G; ++u) {
+      const int64_t j = j0 + (u0 + u) * NT;
+      if (j >= nc) continue;
 #pragma unroll
-    for (int i = 0; i < M; ++i) acc[u][i] = F::zero();
-#pragma unroll
-  for (int l = 0; l < KB; ++l) {
-    if (l >= K) break;
-#pragma unroll
-    for (int i = 0; i < M; ++i) {
-      const T a = Ak[l * M + i];
-#pragma unroll
-      for (int u = 0; u < kShortCols; ++u) F::fma(acc[u][i], a, b[l][u]);
-    }
-  }
-#pragma unroll
-  for (int u = 0; u < kShortCols; ++u) {
-    const int64_t j = j0 + u * kThreads;
-    if (j >= nc) continue;
-#pragma unroll
-    for (int i = 0; i < M; ++i) {
-      if (i >= mr) break;
-      T* p = C + c_off + i * ldc + j;
-      T v = unit_alpha ? acc[u][i] : F::scale(acc[u][i], alpha);
-      if (!zero_beta) v = F::add(v, F::scale(*p, beta));
-      *p = v;
+      for (int i = 0; i < M; ++i) {
+        if (i >= mr) break;
+        T* p = C + c_off + i * ldc + j;
+        if (PLAIN) {
+          *p = acc[u][i];
+        } else {
+          T v = F::scale(acc[u][i], alpha);
+          if (beta != 0.0) v = F::add(v, F::scale(*p, beta));  // C is not read for beta = 0
+          *p = v;
+        }
+      }
     }
   }
 }
 
-template <class F>
-__device__ __forceinline__ void short_dispatch(const typename F::T* __restrict__ A, const typename F::T* __restrict__ B,
-                                               typename F::T* __restrict__ C, const int64_t* __restrict__ orec,
-                                               const int64_t* __restrict__ terms, int tcol, double alpha, double beta,
-                                               typename F::T* Ak) {
-  const int64_t* trec = terms + orec[4] * YB_GEMM_TERM_REC;
-  const bool ua = alpha == 1.0, zb = beta == 0.0;  // once per tile, not per element (FP64 compares)
+template <class F, bool PLAIN, int NT>
+__device__ __forceinline__ void short_rows(const typename F::T* __restrict__ A, const typename F::T* __restrict__ B,
+                                           typename F::T* __restrict__ C, const int64_t* __restrict__ orec,
+                                           const int64_t* __restrict__ trec, int tcol, double alpha, double beta,
+                                           typename F::T* Ak) {
   const bool k4 = trec[2] <= 4;
   switch ((int)orec[1]) {
-    case 1: k4 ? short_tile<F, 1, 4>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak)
-               : short_tile<F, 1, 8>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak); break;
-    case 2: k4 ? short_tile<F, 2, 4>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak)
-               : short_tile<F, 2, 8>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak); break;
-    case 3: k4 ? short_tile<F, 3, 4>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak)
-               : short_tile<F, 3, 8>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak); break;
-    case 4: k4 ? short_tile<F, 4, 4>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak)
-               : short_tile<F, 4, 8>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak); break;
-    default: short_tile<F, 8, 8>(A, B, C, orec, trec, tcol, alpha, beta, ua, zb, Ak); break;
+    case 1: k4 ? short_tile<F, 1, 4, PLAIN, NT>(A, B, C, orec, trec, tcol, alpha, beta, Ak)
+               : short_tile<F, 1, 8, PLAIN, NT>(A, B, C, orec, trec, tcol, alpha, beta, Ak); break;
+    case 2: k4 ? short_tile<F, 2, 4, PLAIN, NT>(A, B, C, orec, trec, tcol, alpha, beta, Ak)
+               : short_tile<F, 2, 8, PLAIN, NT>(A, B, C, orec, trec, tcol, alpha, beta, Ak); break;
+    case 3: k4 ? short_tile<F, 3, 4, PLAIN, NT>(A, B, C, orec, trec, tcol, alpha, beta, Ak)
+               : short_tile<F, 3, 8, PLAIN, NT>(A, B, C, orec, trec, tcol, alpha, beta, Ak); break;
+    case 4: k4 ? short_tile<F, 4, 4, PLAIN, NT>(A, B, C, orec, trec, tcol, alpha, beta, Ak)
+               : short_tile<F, 4, 8, PLAIN, NT>(A, B, C, orec, trec, tcol, alpha, beta, Ak); break;
+    default: short_tile<F, 8, 8, PLAIN, NT>(A, B, C, orec, trec, tcol, alpha, beta, Ak); break;
   }
 }
 
-// Kernel of the short skinny tiles only (tile kind 2).
-template <class F>
-__global__ void __launch_bounds__(kThreads, sizeof(typename F::T) == 8 ? 3 : 1) short_gemm_kernel(const typename F::T* __restrict__ A,
-                                                                 const typename F::T* __restrict__ B,
-                                                                 typename F::T* __restrict__ C,
-                                                                 const int64_t* __restrict__ outs,
-                                                                 const int64_t* __restrict__ terms,
-                                                                 const int32_t* __restrict__ tiles, double alpha,
-                                                                 double beta) {
-  using T = typename F::T;
-  __shared__ T Ak[kShortK * 8];
-  const int4 tl = reinterpret_cast<const int4*>(tiles)[blockIdx.x];
+// A kind-2 tile (output, term index, strip, 2): both records are read at once.
+template <class F, int NT>
+__device__ __forceinline__ void short_dispatch(const typename F::T* __restrict__ A, const typename F::T* __restrict__ B,
+                                               typename F::T* __restrict__ C, const int64_t* __restrict__ outs,
+                                               const int64_t* __restrict__ terms, int4 tl, double alpha, double beta,
+                                               typename F::T* Ak) {
   const int64_t* orec = outs + (int64_t)tl.x * YB_GEMM_OUT_REC;
-  short_dispatch<F>(A, B, C, orec, terms, tl.z, alpha, beta, Ak);
+  const int64_t* trec = terms + (int64_t)tl.y * YB_GEMM_TERM_REC;
+  if (alpha == 1.0 && beta == 0.0)  // once per strip (FP64 compares)
+    short_rows<F, true, NT>(A, B, C, orec, trec, tl.z, alpha, beta, Ak);
+  else
+    short_rows<F, false, NT>(A, B, C, orec, trec, tl.z, alpha, beta, Ak);
+}
+
+// Kernel of the short skinny strips only (tile kind 2): 256 threads x 2 columns; at most 64
+// registers for FP64 (four CTAs, 32 warps per SM), 128 for complex128.
+constexpr int kShortThreads = YB_GEMM_SHORT_COLS / 2;
+
+template <class F>
+__global__ void __launch_bounds__(kShortThreads, sizeof(typename F::T) == 8 ? 4 : 2) short_gemm_kernel(
+    const typename F::T* __restrict__ A, const typename F::T* __restrict__ B, typename F::T* __restrict__ C,
+    const int64_t* __restrict__ outs, const int64_t* __restrict__ terms, const int32_t* __restrict__ tiles,
+    double alpha, double beta) {
+  __shared__ typename F::T Ak[8 * 8];
+  const int4 tl = reinterpret_cast<const int4*>(tiles)[blockIdx.x];
+  short_dispatch<F, kShortThreads>(A, B, C, outs, terms, tl, alpha, beta, Ak);
 }
 
 template <class F>
@@ -269,7 +302,7 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_kernel(const typename F
     return;
   }
   if (tl.w == 2) {  // short skinny: m <= 8 rows, one term with K <= 8, 512 columns
-    short_dispatch<F>(A, B, C, orec, terms, tl.z, alpha, beta, &As[0][0]);
+    short_dispatch<F, kThreads>(A, B, C, outs, terms, tl, alpha, beta, &As[0][0]);
     return;
   }
 
@@ -431,10 +464,10 @@ extern "C" int yb_grouped_gemm_short(const void* a, const void* b, void* c, int 
   if (!a || !b || !c || !outs || !terms || !tiles || n_tiles < 0) return YB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
   if (dtype == YB_F64) {
-    yb::short_gemm_kernel<yb::Real><<<n_tiles, yb::kThreads, 0, s>>>(
+    yb::short_gemm_kernel<yb::Real><<<n_tiles, yb::kShortThreads, 0, s>>>(
         (const double*)a, (const double*)b, (double*)c, outs, terms, tiles, alpha, beta);
   } else if (dtype == YB_C128) {
-    yb::short_gemm_kernel<yb::Cplx><<<n_tiles, yb::kThreads, 0, s>>>(
+    yb::short_gemm_kernel<yb::Cplx><<<n_tiles, yb::kShortThreads, 0, s>>>(
         (const double2*)a, (const double2*)b, (double2*)c, outs, terms, tiles, alpha, beta);
   } else {
     return YB_ERR_INVALID;
