@@ -22,6 +22,12 @@ per leg over charges -16..16 and every block scaled by 10^U(-4,0) (sector GEMMs 
 946^3), reporting emulated and native FP64 TFLOP/s and the largest relative error per
 sector result of both against the FP64 oracle.
 
+``--workload dlayer``: one double-layer PEPS contraction (append_vec_tl, the CTMRG corner
+step: the boundary vector x [l l'] [t t'] y with the ket and bra site tensors; Z2, D=6, d=2,
+chi=144) as a compiled program (``yastn_gb300.double_layer``: composed copies + grouped GEMMs)
+against YASTN's own composition on this backend and on the reference's torch backend on the
+same GPU; the composed-copy kernel's bandwidth against the measured HBM peak.
+
 ``--workload cfg4``: differentiable iPEPS CTMRG (1x1 cell, Z2, D=6, d=2, 8 CTM iterations with
 truncated block-SVD projectors, transverse-field Ising energy at h=3 and its gradient) at
 environment dimension chi=24: the reference's own call sequence, recorded from YASTN, replayed
@@ -58,7 +64,7 @@ def parse():
     p.add_argument('--steps', type=int, default=20)
     p.add_argument('--warmup', type=int, default=5)
     p.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
-    p.add_argument('--workload', default='cfg2', choices=['cfg1', 'cfg2', 'cfg3', 'cfg4', 'cfg5', 'svd144'])
+    p.add_argument('--workload', default='cfg2', choices=['cfg1', 'cfg2', 'cfg3', 'cfg4', 'cfg5', 'svd144', 'dlayer'])
     p.add_argument('--gemm', default='emulated', choices=['emulated', 'fp64'],
                    help='sector-GEMM mode of the headline (cfg2)')
     p.add_argument('--no-svd', action='store_true', help='skip the extra svd_with_truncation timing')
@@ -1360,8 +1366,129 @@ def run_svd144(args):
     print(json.dumps(line))
 
 
+def run_dlayer(args):
+    """Double-layer contraction (append_vec_tl, mode 'b-self' as the CTM corners call it) at the
+    chi=144 CTMRG shape: the compiled program against YASTN's composition on this backend and
+    on the reference's torch backend (default_device='cuda'); FP64 GEMM FLOP of the program's
+    sector GEMMs per call; every output compared with the reference torch backend's."""
+    import torch
+    ref = os.path.join(ROOT, 'baseline', '_ref')
+    if ref not in sys.path:
+        sys.path.insert(0, ref)
+    import yastn
+    import yastn.tn.fpeps as fpeps
+    import yastn.tn.fpeps.envs._env_contractions as ec
+    from yastn_gb300 import backend as BK
+    from yastn_gb300 import double_layer as dl
+    from yastn_gb300 import ops
+    dev = torch.device('cuda', 0)
+    torch.cuda.set_device(dev)
+    chi = 144
+    cfn = yastn.make_config(sym='Z2', backend='np', default_dtype='float64')
+    cfn.backend.random_seed(0)
+    vl = yastn.Leg(cfn, s=1, t=(0, 1), D=(3, 3))
+    pl = yastn.Leg(cfn, s=1, t=(0, 1), D=(1, 1))
+    el = yastn.Leg(cfn, s=1, t=(0, 1), D=(chi // 2, chi // 2))
+    ket = yastn.rand(cfn, legs=[vl.conj(), vl, vl, vl.conj(), pl])
+    bra = ket
+    la, lb = fpeps.DoublePepsTensor(bra=bra, ket=ket).get_legs((1, 0))
+    vec = yastn.rand(cfn, legs=[el, la.conj(), lb.conj(), el.conj()])
+    kw = dict(mode='b-self', in_b=(2, 1), out_a=(3, 2))
+    arms = {}
+    for name, backend in (('gb300', BK), ('reference_torch_cuda', 'torch')):
+        cfg = yastn.make_config(sym='Z2', backend=backend, default_dtype='float64', default_device='cuda')
+        arms[name] = [t._replace(config=cfg, data=torch.from_numpy(np.ascontiguousarray(t._data)).to(dev))
+                      for t in (bra, ket, vec)]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def timed(fn, ts, reps):
+        out = fn(*ts, **kw)
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(reps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            out = fn(*ts, **kw)
+            e1.record()
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.median(ms)), out
+    reps = max(3, args.steps)
+    dl.clear_cache()
+    t_fused, out_f = timed(dl.append_vec_tl, arms['gb300'], reps)
+    t_comp, out_c = timed(ec.append_vec_tl, arms['gb300'], reps)
+    t_ref, out_r = timed(ec.append_vec_tl, arms['reference_torch_cuda'], reps)
+    rel = float((out_f._data - out_r._data).abs().max() / out_r._data.abs().max())
+    assert torch.equal(out_f._data, out_c._data) and rel <= 1e-12, rel
+    key = next(iter(dl._PROGRAMS))
+    prog = dl._PROGRAMS[key]
+    flops = 0
+    for st in prog.steps:
+        if st[0] == 'gemm':
+            flops += sum(2 * Da[0] * Da[1] * Db[1] for _, _, _, Da, _, Db in st[4][0])
+    # the composed-copy kernel alone: the largest gather of the program, timed in a loop
+    maps = prog.maps(BK, dev)
+    env = {('in', i): t._data for i, t in enumerate(arms['gb300'])}
+    biggest = None
+    for st in prog.steps:
+        if st[0] == 'gather':
+            m = maps[st[1]]
+            src = env[st[2]]
+            if m is not None and (biggest is None or m[0].numel() > biggest[1].numel()):
+                biggest = (src, m[0], m[2])
+            env[st[1]] = src if m is None else ops.map_gather(src, m[0], m[2])
+        else:
+            env[st[2]] = getattr(BK, st[1])(env[st[3][0]], env[st[3][1]], *st[4])
+    src, gmap, conj = biggest
+    ops.map_gather(src, gmap, conj)
+    gms = []
+    for _ in range(reps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        ops.map_gather(src, gmap, conj)
+        e1.record()
+        e1.synchronize()
+        gms.append(e0.elapsed_time(e1))
+    t_g = float(np.median(gms))
+    n_nz = int(torch.count_nonzero(gmap))
+    gbytes = gmap.numel() * (4 + 8) + n_nz * 8
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            peaks = json.load(f)
+    except (OSError, ValueError):
+        pass
+    hbm = peaks.get('hbm_gbs', 6800.0)
+    line = {"metric": "double-layer contraction TFLOP/s (append_vec_tl, Z2 D=6 chi=144, FP64)",
+            "value": flops / t_fused / 1e9, "unit": "TFLOP/s", "n_gpus": 1, "steps": reps, "warmup": 1,
+            "ms_per_step": t_fused, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded normal draws as yastn.rand)",
+            "config": {"workload": "append_vec_tl mode b-self, vector x [l l'] [t t'] y, chi=144, D=6, d=2, Z2",
+                       "gemm_flop_per_call": flops, "vector_elements": int(vec.size),
+                       "l2": "flushed between timed calls (256 MB write)",
+                       "program": [st[0] for st in prog.steps]},
+            "roofline": {"bound": "hbm", "kernel": "yb_map_gather", "achieved": gbytes / t_g / 1e6, "peak": hbm,
+                         "unit": "GB/s", "frac": gbytes / t_g / 1e6 / hbm, "peak_source": "measured: hbm copy",
+                         "traffic": None, "algorithmic_bytes": gbytes,
+                         "note": "largest composed copy of the program: int32 map + 8 B store per entry, "
+                                 "8 B load per mapped entry"},
+            "extra": {"yastn_composition_gb300_ms": t_comp, "reference_torch_cuda_ms": t_ref,
+                      "composition_over_fused": t_comp / t_fused, "reference_over_fused": t_ref / t_fused,
+                      "rel_err_vs_reference_torch": rel, "fused_bitwise_equal_to_composition": True}}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
+    if args.workload == 'dlayer':
+        if args.impl == 'reference':
+            print(json.dumps({"impl": "reference", "unavailable": "dlayer times the reference's torch backend "
+                                                                  "on the GPU inside the GPU arm"}))
+        else:
+            run_dlayer(args)
+        return
     if args.workload == 'svd144':
         if args.impl == 'reference':
             print(json.dumps({"impl": "reference", "unavailable": "svd144 compares against cuSOLVER in the GPU arm"}))

@@ -92,6 +92,23 @@ int yb_block_copy(const void* src, void* dst, int unit_bytes,
                   const int64_t* tasks, int n_tasks,
                   const int64_t* items, int n_items, void* stream);
 
+/* Composed copy: one pass for a chain of block copies (merges, unmerges, transposes, block
+ * negations, conjugation) between two GEMMs of a double-layer PEPS contraction.
+ *   dst[i] = conj?(sign * src[|map[i]| - 1]) for map[i] != 0, sign = -1 where map[i] < 0;
+ *   dst[i] = 0 for map[i] == 0.
+ * map: n int32 entries (source indices + 1, so sources hold fewer than 2^31 - 1 elements);
+ * dtype YB_F64 or YB_C128 (conj conjugates complex elements; ignored for YB_F64). Negation
+ * and conjugation flip IEEE sign bits (as -x and conj(x) do), so the result is bit-exact.
+ * src and dst must not overlap. The adjoint of an injective map is the same call with the
+ * inverse map (inv[|map[i]| - 1] = sign * (i + 1)).
+ * Replaces the chain fuse_legs / unfuse_legs / swap_gate / conj / the merges of tensordot in
+ * append_vec_tl, append_vec_br, append_vec_tr, append_vec_bl
+ * (yastn/tn/fpeps/envs/_env_contractions.py:211-365), each of whose steps is one
+ * transpose_and_merge / unmerge / negate_blocks / conj call of the backend
+ * (backend_torch.py:588-593). */
+int yb_map_gather(const void* src, void* dst, int dtype, const int32_t* map, int64_t n, int conj,
+                  void* stream);
+
 /* ==== family (b): grouped sum-of-products GEMM ========================================
  * For every output block o:  C_o = alpha * sum_{t in terms(o)} op(A_t) op(B_t) + beta * C_o
  * outs: n_out records of YB_GEMM_OUT_REC int64:

@@ -20,6 +20,7 @@ SIGNATURES = {
     'yb_abi_version': ([], _i),
     'yb_last_cuda_error': ([], _i),
     'yb_block_copy': ([_vp, _vp, _i, _vp, _i, _vp, _i, _vp], _i),
+    'yb_map_gather': ([_vp, _vp, _i, _vp, _i64, _i, _vp], _i),
     'yb_gemm_reduce': ([_vp, _vp, _i, _vp, _vp, _i, _d, _d, _vp], _i),
     'yb_grouped_gemm': ([_vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _d, _d, _vp], _i),
     'yb_grouped_gemm_short': ([_vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _d, _d, _vp], _i),

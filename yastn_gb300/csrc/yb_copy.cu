@@ -169,6 +169,53 @@ __global__ void __launch_bounds__(kThreads) block_copy_kernel(const Elem* __rest
     copy_units_any<Elem>(src, dst, rec, first);
 }
 
+
+// Composed copies: dst[i] = src[|map[i]| - 1], negated where map[i] < 0 and conjugated when
+// `conj` is set, zero where map[i] == 0. The map (int32, one entry per destination element) is
+// the composition of a chain of merges, unmerges, transposes and block negations, so one pass
+// replaces the chain. Map reads and stores are coalesced; the loads follow the map (runs of the
+// source's innermost dims; a transposed run reuses its sectors from L2). Negation and
+// conjugation flip IEEE sign bits, as -x and conj(x) do. Words = 8-byte words per element
+// (1: float64, 2: complex128).
+template <int Words>
+__global__ void __launch_bounds__(kThreads) map_gather_kernel(const uint64_t* __restrict__ src,
+                                                               uint64_t* __restrict__ dst,
+                                                               const int32_t* __restrict__ map, int64_t n,
+                                                               uint64_t conj_hi) {
+  constexpr uint64_t kSign = 0x8000000000000000ull;
+  const int64_t base = (int64_t)blockIdx.x * (kThreads * kIlp) + threadIdx.x;
+  int32_t m[kIlp];
+#pragma unroll
+  for (int j = 0; j < kIlp; ++j) {
+    const int64_t e = base + (int64_t)j * kThreads;
+    m[j] = e < n ? __ldg(map + e) : 0;
+  }
+  uint64_t v[kIlp][Words];
+#pragma unroll
+  for (int j = 0; j < kIlp; ++j) {
+    const int32_t a = m[j] < 0 ? -m[j] : m[j];
+    const uint64_t neg = m[j] < 0 ? kSign : 0ull;
+    if (Words == 2) {
+      ulonglong2 w = make_ulonglong2(0ull, 0ull);
+      if (a != 0) w = __ldg(reinterpret_cast<const ulonglong2*>(src) + (a - 1));
+      v[j][0] = a != 0 ? (w.x ^ neg) : 0ull;
+      v[j][Words - 1] = a != 0 ? (w.y ^ neg ^ conj_hi) : 0ull;
+    } else {
+      v[j][0] = a != 0 ? (__ldg(src + (a - 1)) ^ neg) : 0ull;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < kIlp; ++j) {
+    const int64_t e = base + (int64_t)j * kThreads;
+    if (e < n) {
+      if (Words == 2)
+        reinterpret_cast<ulonglong2*>(dst)[e] = make_ulonglong2(v[j][0], v[j][Words - 1]);
+      else
+        dst[e] = v[j][0];
+    }
+  }
+}
+
 }  // namespace
 }  // namespace yb
 
@@ -201,6 +248,23 @@ int yb_block_copy(const void* src, void* dst, int unit_bytes, const int64_t* tas
       break;
     default: return YB_ERR_INVALID;
   }
+  return yb::check_launch();
+}
+
+
+int yb_map_gather(const void* src, void* dst, int dtype, const int32_t* map, int64_t n, int conj, void* stream) {
+  if (n == 0) return YB_OK;
+  if (!src || !dst || !map || n < 0 || n >= ((int64_t)1 << 40)) return YB_ERR_INVALID;
+  if (dtype != YB_F64 && dtype != YB_C128) return YB_ERR_INVALID;
+  if (dtype == YB_C128 && ((((uintptr_t)src) | ((uintptr_t)dst)) & 15u)) return YB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t per_cta = (int64_t)yb::kThreads * yb::kIlp;
+  const dim3 grid((unsigned)((n + per_cta - 1) / per_cta));
+  if (dtype == YB_C128)
+    yb::map_gather_kernel<2><<<grid, yb::kThreads, 0, s>>>((const uint64_t*)src, (uint64_t*)dst, map, n,
+                                                           conj ? 0x8000000000000000ull : 0ull);
+  else
+    yb::map_gather_kernel<1><<<grid, yb::kThreads, 0, s>>>((const uint64_t*)src, (uint64_t*)dst, map, n, 0ull);
   return yb::check_launch();
 }
 

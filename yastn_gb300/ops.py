@@ -98,6 +98,20 @@ def run_copy(plan, src, dst):
     return dst
 
 
+def map_gather(src, gmap, conj=False):
+    """One composed copy: ``out[i] = conj?(sign * src[|gmap[i]| - 1])`` (0 where gmap[i] == 0),
+    ``gmap`` an int32 CUDA tensor of source indices + 1 with the sign of a block negation
+    (``yb_map_gather``)."""
+    src = _check(src, 'src')
+    if gmap.dtype != torch.int32 or not gmap.is_cuda or gmap.dim() != 1 or not gmap.is_contiguous():
+        raise TypeError("gmap must be a contiguous 1-D int32 CUDA tensor")
+    out = torch.empty(gmap.numel(), dtype=src.dtype, device=src.device)
+    if out.numel():
+        N.call('yb_map_gather', _ptr(src), _ptr(out), _dtype_code(src.dtype), _ptr(gmap), gmap.numel(),
+               int(bool(conj) and src.is_complex()), _stream())
+    return out
+
+
 def merge(data, order, meta_new, meta_mrg, Dsize):
     """transpose_and_merge: fused blocks, zero where no source block lands."""
     data = _check(data, any_dtype=True)
