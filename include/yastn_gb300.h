@@ -19,6 +19,8 @@
  *   fix_svd_signs        yastn/backend/backend_torch.py:353-366
  *   apply_mask           yastn/backend/backend_torch.py:576-577 (-> _backend_torch_backwards.py:251-279)
  *   truncation_mask      yastn/tensor/linalg.py:637-735 (caller-side rule, fused here into one launch)
+ *   append_vec_tl/br/tr/bl  yastn/tn/fpeps/envs/_env_contractions.py:211-365 (their copy chains, composed
+ *                        into one yb_map_gather each)
  */
 #ifndef YASTN_GB300_H
 #define YASTN_GB300_H
