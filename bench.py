@@ -1418,8 +1418,15 @@ def run_dlayer(args):
     dl.clear_cache()
     t_fused, out_f = timed(dl.append_vec_tl, arms['gb300'], reps)
     t_comp, out_c = timed(ec.append_vec_tl, arms['gb300'], reps)
+    saved_mode = BK.get_gemm_mode()
+    BK.set_gemm_mode('emulated')
+    try:
+        t_emu, out_e = timed(dl.append_vec_tl, arms['gb300'], reps)
+    finally:
+        BK.set_gemm_mode(saved_mode)
     t_ref, out_r = timed(ec.append_vec_tl, arms['reference_torch_cuda'], reps)
     rel = float((out_f._data - out_r._data).abs().max() / out_r._data.abs().max())
+    rel_emu = float((out_e._data - out_r._data).abs().max() / out_r._data.abs().max())
     assert torch.equal(out_f._data, out_c._data) and rel <= 1e-12, rel
     key = next(iter(dl._PROGRAMS))
     prog = dl._PROGRAMS[key]
@@ -1474,7 +1481,9 @@ def run_dlayer(args):
                          "traffic": None, "algorithmic_bytes": gbytes,
                          "note": "largest composed copy of the program: int32 map + 8 B store per entry, "
                                  "8 B load per mapped entry"},
-            "extra": {"yastn_composition_gb300_ms": t_comp, "reference_torch_cuda_ms": t_ref,
+            "extra": {"emulated_gemm_ms": t_emu, "emulated_tflops": flops / t_emu / 1e9,
+                      "emulated_rel_err_vs_reference_torch": rel_emu,
+                      "yastn_composition_gb300_ms": t_comp, "reference_torch_cuda_ms": t_ref,
                       "composition_over_fused": t_comp / t_fused, "reference_over_fused": t_ref / t_fused,
                       "rel_err_vs_reference_torch": rel, "fused_bitwise_equal_to_composition": True}}
     print(json.dumps(line))

@@ -104,6 +104,9 @@ def _run_outs(outs, terms, tiles, a, b, c, alpha, beta):
             assert m <= 16, "skinny tiles take at most 16 rows"
             w = P.skinny_cols(m)
             want = {(0, j, 1) for j in range((n + w - 1) // w)}
+        elif any(kd == 3 for _, _, kd in seen.get(oi, ())):  # tall skinny: 256 rows x all n <= 16 columns
+            assert n <= 16, "tall tiles take at most 16 columns"
+            want = {(i, 0, 3) for i in range((m + 255) // 256)}
         elif any(kd == 2 for _, _, kd in seen.get(oi, ())):  # short skinny: m <= 8, one term, K <= 8
             assert m <= 8 and t1 - t0 == 1 and int(plan.terms[t0][2]) <= 8, "short tiles: m <= 8, one term, K <= 8"
             want = {(t0, j, 2) for j in range((n + 511) // 512)}  # tile row: the term index

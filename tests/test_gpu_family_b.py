@@ -144,6 +144,36 @@ def test_skinny_tile_kinds(cplx, cuda_device):
     assert rel(host(Ab), Ar) <= TOL and rel(host(Bb), Br) <= TOL
 
 
+@pytest.mark.parametrize('cplx', [False, True])
+def test_tall_and_wide_skinny_tiles(cplx, cuda_device):
+    """Default plans: outputs of at most 16 columns and many rows (tall tiles: 256 rows x all
+    columns, one row per thread) and of 9..16 rows at least 4096 wide (skinny tiles), as the
+    double-layer contraction's sector GEMMs are, against the oracle: forward, adjoint, and
+    alpha/beta."""
+    from yastn_gb300 import _plans as P
+    rng = np.random.default_rng(14)
+    shapes = [(3000, 18, 9), (700, 5, 16), (65, 40, 1), (9, 36, 5000), (16, 7, 4096), (12, 3, 4500),
+              (2600, 70, 3), (64, 9, 9)]
+    meta, oa, ob, oc = [], 0, 0, 0
+    for m, k, n in shapes:
+        meta.append(((oc, oc + m * n), (m, n), (oa, oa + m * k), (m, k), (ob, ob + k * n), (k, n)))
+        oa += m * k; ob += k * n; oc += m * n
+    meta = tuple(meta)
+    plan = P.dot_plan(meta)
+    assert {1, 3} <= set(int(t[3]) for t in plan.tiles)
+    f = lambda n: rng.normal(size=n) + (1j * rng.normal(size=n) if cplx else 0)
+    A, B, Cb, C0 = f(oa), f(ob), f(oc), f(oc)
+    got = host(ops.dot(dev(A), dev(B), meta, oc))
+    ref = oracle.dot(A, B, meta, oc)
+    assert rel(got, ref) <= TOL
+    Ab, Bb = ops.dot_backward(dev(Cb), dev(A), dev(B), meta)
+    Ar, Br = oracle.dot_backward(Cb, A, B, meta)
+    assert rel(host(Ab), Ar) <= TOL and rel(host(Bb), Br) <= TOL
+    c = dev(C0)
+    ops.run_gemm(plan, dev(A), dev(B), c, alpha=0.5, beta=2.0)
+    assert rel(host(c), 0.5 * ref + 2.0 * C0) <= TOL
+
+
 def test_cfg1_full_size_dot(cuda_device):
     """The benchmark's 13 sector GEMMs (n up to 822, 3.25 GFLOP) vs numpy BLAS."""
     tr = load_trace('cfg1')

@@ -148,8 +148,40 @@ def test_skinny_tile_kinds_cover_and_reproduce():
         P.SKINNY_ROWS = saved
     P.CACHE.by_id.clear(); P.CACHE.by_val.clear()
     kinds = set(int(t[3]) for t in plan.tiles)
-    assert kinds == {0, 1}
+    assert kinds == {0, 1, 3}  # (500, 30, 5) and (2592, 18, 9) take tall tiles
     rng = np.random.default_rng(8)
+    for cplx in (False, True):
+        f = lambda n: rng.normal(size=n) + (1j * rng.normal(size=n) if cplx else 0)
+        A, B, Cb = f(oa), f(ob), f(oc)
+        out = PI.run_gemm(plan, A, B, np.zeros(oc, dtype=A.dtype))
+        ref = oracle.dot(A, B, meta, oc)
+        assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
+        pa, pb = P.dot_backward_plans(meta)
+        Ab = PI.run_gemm(pa, Cb, B, np.zeros(oa, dtype=A.dtype))
+        Bb = PI.run_gemm(pb, A, Cb, np.zeros(ob, dtype=A.dtype))
+        Ab_r, Bb_r = oracle.dot_backward(Cb, A, B, meta)
+        assert np.abs(Ab - Ab_r).max() <= 1e-12 * np.abs(Ab_r).max()
+        assert np.abs(Bb - Bb_r).max() <= 1e-12 * np.abs(Bb_r).max()
+    P.CACHE.by_id.clear(); P.CACHE.by_val.clear()
+
+
+def test_tall_and_wide_skinny_tiles_cover_and_reproduce():
+    """Default plans: outputs of at most 16 columns and more than 64 rows take tall tiles
+    (256 rows x all columns, kind 3), outputs of 9..16 rows at least 4096 wide take skinny
+    tiles (kind 1); the double-layer contraction's sector GEMMs (93312 x 18 by 18 x 9 and
+    9 x 36 by 36 x 93312 at chi=144) are such outputs. Coverage and values, forward and
+    adjoint, real and complex, on smaller instances."""
+    shapes = [(3000, 18, 9), (700, 5, 16), (65, 40, 1), (9, 36, 5000), (16, 7, 4096), (12, 3, 4500),
+              (64, 9, 9), (15, 20, 300)]
+    meta, oa, ob, oc = _meta_dot(shapes)
+    plan = P.dot_plan(meta)
+    kinds = [int(t[3]) for t in plan.tiles]
+    by_out = {}
+    for oi, tr, tc, kd in plan.tiles:
+        by_out.setdefault(int(oi), set()).add(int(kd))
+    assert [by_out[i] for i in range(len(shapes))] == [{3}, {3}, {3}, {1}, {1}, {1}, {0}, {0}]
+    assert kinds.count(3) == 12 + 3 + 1
+    rng = np.random.default_rng(9)
     for cplx in (False, True):
         f = lambda n: rng.normal(size=n) + (1j * rng.normal(size=n) if cplx else 0)
         A, B, Cb = f(oa), f(ob), f(oc)

@@ -329,7 +329,9 @@ class SplitK:
 
 SKINNY_ROWS, SKINNY_COLS = 8, 1024  # skinny tiles: up to 8 rows (the kernel takes 16), 1024 columns
                                     # (256 above 8 rows)
+SKINNY_WIDE_ROWS, SKINNY_WIDE_N = 16, 4096  # outputs of 9..16 rows take skinny tiles when this wide
 SHORT_K, SHORT_COLS = 8, 512  # short skinny tiles (kind 2): one term with K <= 8, 512 columns
+TALL_COLS, TALL_ROWS = 16, 256  # tall skinny tiles (kind 3): all n <= 16 columns x 256 rows
 
 
 def skinny_cols(rows):
@@ -337,12 +339,18 @@ def skinny_cols(rows):
 
 
 def tile_kind(m, n, ks=None):
-    """0: 64x64 tiles; 1: skinny tiles over the m <= 16 rows; 2: short skinny tiles (m <= 8
-    rows and a single term whose K <= SHORT_K, any n; ``ks`` = the output's term lengths)."""
+    """0: 64x64 tiles; 1: skinny tiles over the m <= 16 rows (m <= 8 and n > 64, or
+    m <= 16 and n >= SKINNY_WIDE_N); 2: short skinny tiles (m <= 8 rows and a single term whose
+    K <= SHORT_K, any n; ``ks`` = the output's term lengths); 3: tall skinny tiles over the
+    n <= 16 columns (m > 64)."""
     if m <= SKINNY_ROWS and ks is not None and len(ks) == 1 and ks[0] <= SHORT_K:
         return 2
     if m <= SKINNY_ROWS and n > GEMM_TILE:
         return 1
+    if m <= SKINNY_WIDE_ROWS and n >= SKINNY_WIDE_N:
+        return 1
+    if n <= TALL_COLS and m > GEMM_TILE:
+        return 3
     return 0
 
 
@@ -356,7 +364,8 @@ SPLITK_MIN_K = 128       # shortest K chunk
 
 def _tiles_for(outs, terms):
     """Tiles (output, tile row, tile col, kind): kind 0 = 64x64, kind 1 = skinny (all m <= 16
-    rows x 1024 columns, 256 above 8 rows), kind 2 = short skinny (all m <= 8 rows x 512
+    rows x 1024 columns, 256 above 8 rows), kind 3 = tall skinny (256 rows x all n <= 16
+    columns; tile row = the 256-row block), kind 2 = short skinny (all m <= 8 rows x 512
     columns; its tile row holds the output's single term index, so the kernel loads the output
     and term records at once), ordered by descending work so long tiles start first."""
     tiles = []
@@ -367,6 +376,10 @@ def _tiles_for(outs, terms):
         ks = [int(terms[t][2]) for t in range(o[4], o[5])]
         kk = sum(ks)
         kind = tile_kind(m, n, ks)
+        if kind == 3:
+            for tr in range((m + TALL_ROWS - 1) // TALL_ROWS):
+                tiles.append((kk * n * TALL_ROWS // GEMM_TILE, oi, tr, 0, 3))
+            continue
         if kind:
             w = _tile_cols(kind, m)
             tr = int(o[4]) if kind == 2 else 0
@@ -385,6 +398,8 @@ def _n_tiles(m, n, ks=None):
     if m == 0 or n == 0:
         return 0
     kind = tile_kind(m, n, ks)
+    if kind == 3:
+        return (m + TALL_ROWS - 1) // TALL_ROWS
     if kind:
         return (n + _tile_cols(kind, m) - 1) // _tile_cols(kind, m)
     return ((m + GEMM_TILE - 1) // GEMM_TILE) * ((n + GEMM_TILE - 1) // GEMM_TILE)

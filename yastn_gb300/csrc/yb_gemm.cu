@@ -5,9 +5,10 @@
 // One launch covers every 64x64 output tile of every sector; the host orders tiles
 // largest-K first so that the long tiles start early. Outputs with few rows (the
 // contractions with a small MPO block, for instance) use "skinny" tiles instead: all rows x
-// 1024 columns, four columns per thread, op(A) staged in shared memory (the kernel takes up
-// to 16 rows, above 8 with 256 columns, one per thread; the host sends outputs of up to 8
-// rows, which measured faster than 64x64 tiles, while 9..16 rows did not). On GB300 FP64 arithmetic runs at
+// 1024 columns, four columns per thread, op(A) staged in shared memory (up to 16 rows, above 8
+// with 256 columns, one per thread; the host sends outputs of up to 8 rows, and of 9..16 rows
+// only when they are wide). Outputs of at most 16 columns and many rows take "tall" tiles
+// (256 rows, one per thread, all columns). On GB300 FP64 arithmetic runs at
 // about 1.2 TFLOP/s on the DFMA pipe (the DMMA m8n8k4 tensor path measured slower),
 // so a register-tiled DFMA kernel with shared-memory staging is FP64-bound: each thread
 // owns a 4x4 sub-tile and issues 16 independent FMAs per staged k.
@@ -132,9 +133,97 @@ __device__ __forceinline__ void skinny_dispatch(int64_t mr, const typename F::T*
     case 6: skinny_tile<F, 6, 4>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
     case 7: skinny_tile<F, 7, 4>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
     case 8: skinny_tile<F, 8, 4>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
-    case 9: case 10: case 11: case 12:
-      skinny_tile<F, 12, 1>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
+    case 9: skinny_tile<F, 9, 1>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
+    case 10: skinny_tile<F, 10, 1>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
+    case 11: skinny_tile<F, 11, 1>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
+    case 12: skinny_tile<F, 12, 1>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
+    case 13: case 14: skinny_tile<F, 14, 1>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
     default: skinny_tile<F, 16, 1>(A, B, C, orec, terms, tcol, alpha, beta, Ak); break;
+  }
+}
+
+// Tall skinny tile (kind 3): 256 rows x all n <= 16 columns of an output, one row per thread.
+// op(B) is staged in shared memory K-chunk by K-chunk ([kTallK][N], broadcast reads); each
+// thread reads its own op(A) row (a row's K-contiguous entries come from L1 after the first
+// touch) and keeps its N accumulators in registers, so no FMA is spent on padding columns (a
+// 64x64 tile of an n = 9 output runs 9 of each warp's 32 columns). N is the exact column count.
+constexpr int kTallK = 64;
+constexpr int kTallRows = kThreads;
+
+template <class F, int N>
+__device__ __forceinline__ void tall_tile(const typename F::T* __restrict__ A, const typename F::T* __restrict__ B,
+                                          typename F::T* __restrict__ C, const int64_t* __restrict__ orec,
+                                          const int64_t* __restrict__ terms, int trow, double alpha, double beta,
+                                          typename F::T* Bk) {
+  using T = typename F::T;
+  const int64_t c_off = orec[0], m = orec[1], ldc = orec[3], t0 = orec[4], t1 = orec[5];
+  const int64_t i = (int64_t)trow * kTallRows + threadIdx.x;
+  const bool live = i < m;
+  T acc[N];
+#pragma unroll
+  for (int j = 0; j < N; ++j) acc[j] = F::zero();
+  for (int64_t t = t0; t < t1; ++t) {
+    const int64_t* trec = terms + t * YB_GEMM_TERM_REC;
+    const int64_t K = trec[2];
+    const int64_t l_is = trec[3], l_ls = trec[4], r_ls = trec[5], r_js = trec[6];
+    const int flags = (int)trec[7];
+    const bool conjL = flags & 1, conjR = flags & 2;
+    const T* Arow = A + trec[0] + (live ? i * l_is : 0);
+    const T* Rb = B + trec[1];
+    for (int64_t k0 = 0; k0 < K; k0 += kTallK) {
+      __syncthreads();
+      for (int e = threadIdx.x; e < kTallK * N; e += kThreads) {
+        const int j = e % N, l = e / N;
+        T v = F::zero();
+        if (k0 + l < K) {
+          v = Rb[(k0 + l) * r_ls + j * r_js];
+          if (conjR) v = F::conj(v);
+        }
+        Bk[l * N + j] = v;
+      }
+      __syncthreads();
+      if (!live) continue;
+      const int kn = (int)min((int64_t)kTallK, K - k0);
+      for (int l0 = 0; l0 < kn; l0 += 8) {
+        T a[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          a[u] = (l0 + u < kn) ? Arow[(k0 + l0 + u) * l_ls] : F::zero();
+          if (conjL) a[u] = F::conj(a[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          if (l0 + u < kn) {
+#pragma unroll
+            for (int j = 0; j < N; ++j) F::fma(acc[j], a[u], Bk[(l0 + u) * N + j]);
+          }
+        }
+      }
+    }
+  }
+  if (!live) return;
+  T* crow = C + c_off + i * ldc;
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    T v = alpha == 1.0 ? acc[j] : F::scale(acc[j], alpha);
+    if (beta != 0.0) v = F::add(v, F::scale(crow[j], beta));
+    crow[j] = v;
+  }
+}
+
+template <class F>
+__device__ __forceinline__ void tall_dispatch(int64_t nc, const typename F::T* __restrict__ A,
+                                              const typename F::T* __restrict__ B, typename F::T* __restrict__ C,
+                                              const int64_t* __restrict__ orec, const int64_t* __restrict__ terms,
+                                              int trow, double alpha, double beta, typename F::T* Bk) {
+  switch (nc) {
+#define YB_TALL_CASE(NN) \
+    case NN: tall_tile<F, NN>(A, B, C, orec, terms, trow, alpha, beta, Bk); break;
+    YB_TALL_CASE(1) YB_TALL_CASE(2) YB_TALL_CASE(3) YB_TALL_CASE(4) YB_TALL_CASE(5) YB_TALL_CASE(6)
+    YB_TALL_CASE(7) YB_TALL_CASE(8) YB_TALL_CASE(9) YB_TALL_CASE(10) YB_TALL_CASE(11) YB_TALL_CASE(12)
+    YB_TALL_CASE(13) YB_TALL_CASE(14) YB_TALL_CASE(15) YB_TALL_CASE(16)
+#undef YB_TALL_CASE
+    default: break;
   }
 }
 
@@ -303,6 +392,10 @@ __global__ void __launch_bounds__(kThreads) grouped_gemm_kernel(const typename F
   }
   if (tl.w == 2) {  // short skinny: m <= 8 rows, one term with K <= 8, 512 columns
     short_dispatch<F, kThreads>(A, B, C, outs, terms, tl, alpha, beta, &As[0][0]);
+    return;
+  }
+  if (tl.w == 3) {  // tall skinny: 256 rows x all n <= 16 columns
+    tall_dispatch<F>(n, A, B, C, orec, terms, tl.y, alpha, beta, &As[0][0]);
     return;
   }
 
