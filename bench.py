@@ -1014,6 +1014,17 @@ def plain_and_ctmrg_extras(args, torch, dev, wl, w, env, h_v0, flush, t_fused_cf
     torch.linalg.svd(blk, full_matrices=False, driver='gesvd')
     torch.linalg.qr(blk)
     t_plain4, (ep, gp) = timed_ctm(plain, 1)
+    try:
+        d = dlayer_line(args)
+        out["double_layer_chi144"] = {
+            "ms_per_call": d["ms_per_step"], "tflops": d["value"], "workload": d["config"]["workload"],
+            "yastn_composition_gb300_ms": d["extra"]["yastn_composition_gb300_ms"],
+            "reference_torch_cuda_ms": d["extra"]["reference_torch_cuda_ms"],
+            "reference_over_fused": d["extra"]["reference_over_fused"],
+            "rel_err_vs_reference_torch": d["extra"]["rel_err_vs_reference_torch"],
+            "composed_copy_frac_of_hbm": d["roofline"]["frac"]}
+    except ImportError as e:
+        out["double_layer_chi144"] = {"unavailable": f"the reference package is not installed ({e})"}
     out["ctmrg_chi24_fwd_bwd"] = {
         "ms_per_step": t_fast, "energy_rel_err_vs_reference": ef, "grad_rel_err_vs_reference": gf,
         "plain_per_block_gpu_ms": t_plain4, "plain_energy_rel_err": ep, "plain_grad_rel_err": gp,
@@ -1367,6 +1378,10 @@ def run_svd144(args):
 
 
 def run_dlayer(args):
+    print(json.dumps(dlayer_line(args)))
+
+
+def dlayer_line(args):
     """Double-layer contraction (append_vec_tl, mode 'b-self' as the CTM corners call it) at the
     chi=144 CTMRG shape: the compiled program against YASTN's composition on this backend and
     on the reference's torch backend (default_device='cuda'); FP64 GEMM FLOP of the program's
@@ -1416,11 +1431,12 @@ def run_dlayer(args):
         return float(np.median(ms)), out
     reps = max(3, args.steps)
     dl.clear_cache()
-    t_fused, out_f = timed(dl.append_vec_tl, arms['gb300'], reps)
-    t_comp, out_c = timed(ec.append_vec_tl, arms['gb300'], reps)
     saved_mode = BK.get_gemm_mode()
-    BK.set_gemm_mode('emulated')
     try:
+        BK.set_gemm_mode('fp64')
+        t_fused, out_f = timed(dl.append_vec_tl, arms['gb300'], reps)
+        t_comp, out_c = timed(ec.append_vec_tl, arms['gb300'], reps)
+        BK.set_gemm_mode('emulated')
         t_emu, out_e = timed(dl.append_vec_tl, arms['gb300'], reps)
     finally:
         BK.set_gemm_mode(saved_mode)
@@ -1486,7 +1502,7 @@ def run_dlayer(args):
                       "yastn_composition_gb300_ms": t_comp, "reference_torch_cuda_ms": t_ref,
                       "composition_over_fused": t_comp / t_fused, "reference_over_fused": t_ref / t_fused,
                       "rel_err_vs_reference_torch": rel, "fused_bitwise_equal_to_composition": True}}
-    print(json.dumps(line))
+    return line
 
 
 def main():
