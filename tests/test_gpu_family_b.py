@@ -204,6 +204,46 @@ def test_dot_ozaki_on_reference_calls(name, cuda_device):
     assert n > 0
 
 
+@pytest.mark.parametrize('tc', [True, False])
+def test_hold_constant_operands(tc, cuda_device):
+    """Inside ops.hold_constant_operands an unchanged operand's merge and digit planes are
+    computed once: results stay bit-identical to calls outside the scope, a held operand
+    modified in place (version counter) or a held merge output modified in place is
+    recomputed, and nothing is held across the scope's end."""
+    tr = load_trace('cfg1')
+    A, B = cfg1_inputs(tr)
+    c0, c1, c2 = tr['calls'][:3]
+    _, _, meta, Dsize = c2['args']
+    Am = oracle.transpose_and_merge(A, *c0['args'][1:])
+    Bg = dev(B)
+    saved = ops.OZAKI_TC[0]
+    ops.OZAKI_TC[0] = tc
+    try:
+        rng = np.random.default_rng(21)
+        As = [dev(Am * (1.0 + 0.1 * i) + 1e-3 * rng.normal(size=Am.size)) for i in range(3)]
+        want = [host(ops.dot_ozaki(a, ops.merge(Bg, *c1['args'][1:]), meta, Dsize)) for a in As]
+        with ops.hold_constant_operands():
+            Bm1 = ops.merge(Bg, *c1['args'][1:])
+            Bm2 = ops.merge(Bg, *c1['args'][1:])
+            assert Bm2 is Bm1  # the held merge
+            got = [host(ops.dot_ozaki(a, ops.merge(Bg, *c1['args'][1:]), meta, Dsize)) for a in As]
+            assert all(np.array_equal(g, w) for g, w in zip(got, want))
+            assert len(ops._HOLD['split']) >= 1 and len(ops._HOLD['merge']) == 1
+            # the source changes in place: merge and digits are recomputed
+            Bg.mul_(2.0)
+            Bm3 = ops.merge(Bg, *c1['args'][1:])
+            assert Bm3 is not Bm1
+            g2 = host(ops.dot_ozaki(As[0], Bm3, meta, Dsize))
+            assert np.array_equal(g2, 2.0 * want[0])
+            # the held output changes in place: the merge is recomputed from the source
+            Bm3.zero_()
+            Bm4 = ops.merge(Bg, *c1['args'][1:])
+            assert Bm4 is not Bm3 and float(Bm4.abs().max()) > 0
+        assert not ops._HOLD['split'] and not ops._HOLD['merge']
+    finally:
+        ops.OZAKI_TC[0] = saved
+
+
 def test_cfg1_full_size_dot_ozaki(cuda_device):
     """The benchmark's 13 sector GEMMs emulated: error vs the FP64 oracle per slice count."""
     tr = load_trace('cfg1')

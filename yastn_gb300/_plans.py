@@ -578,6 +578,13 @@ def _split_layout(blocks, s, th_a, th_b):
     return recs, groups, size[0], size[1], nex[0], nex[1], where
 
 
+def _groups_by_operand(recs, groups):
+    """The split groups of operand A and of operand B (a split launch of one operand)."""
+    op = (recs[groups[:, 0], 9] & 0xff) if len(groups) else np.zeros(0, dtype=np.int64)
+    return (np.ascontiguousarray(groups[op == 0]).reshape(-1, 2),
+            np.ascontiguousarray(groups[op == 1]).reshape(-1, 2))
+
+
 OZ_TC_FOLD_STEPS = 6  # fold + write of a full 128 x 64 tile, in K-step units of the tcgen05 kernel
 
 
@@ -670,6 +677,7 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
         tiles = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles], dtype=np.int32).reshape(-1, 4)
         plan = OzakiPlan(outs, tiles, flops, s)
         plan.split_recs, plan.split_groups = sr, sg
+        plan.split_groups_ab = _groups_by_operand(sr, sg)
         plan.a_size, plan.b_size, plan.a_exps, plan.b_exps = asz, bsz, aex, bex
         plan.native = _pack_gemm(small)
         plan.native_direct = _pack_gemm(small, allow_split=False)  # no chunk workspace
@@ -678,6 +686,7 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
         # tile layout (rows padded to 128 for A, 64 for B)
         sr, sg, asz, bsz, _, _, where = _split_layout(blocks, s, OZAKI_TC_M, OZAKI_TC_N)
         plan.split_recs_tc, plan.split_groups_tc, plan.a_size_tc, plan.b_size_tc = sr, sg, asz, bsz
+        plan.split_groups_tc_ab = _groups_by_operand(sr, sg)
         plan.outs_tc = outs_for(where)
         tiles_tc = []
         for oi, o in enumerate(plan.outs_tc):

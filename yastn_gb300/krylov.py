@@ -25,6 +25,7 @@ import numpy as np
 import torch
 
 from . import _native as N
+from . import ops
 from .ops import _check, _ptr, _stream, _dtype_code
 
 _PARTS = [None]
@@ -138,7 +139,9 @@ class LanczosGraph:
         torch.cuda.current_stream().wait_stream(side)
         self.graph = torch.cuda.CUDAGraph()
         l0 = N.LAUNCHES[0]
-        with torch.cuda.graph(self.graph):
+        # the operator's constant operands (environments, their merges and digit planes) are
+        # computed once per replay, by its first matvec
+        with ops.hold_constant_operands(), torch.cuda.graph(self.graph):
             self.state = lanczos(matvec, self.v0, ncv, st)
         self.launches = N.LAUNCHES[0] - l0
 
@@ -185,7 +188,8 @@ def eigs(f, v0, k=1, which='SR', ncv=10, maxiter=None, tol=1e-13, hermitian=Fals
             return w._data
 
         try:
-            st = lanczos(matvec, v._data.detach(), ncv)
+            with ops.hold_constant_operands():  # the environments' merges and splits, once per expansion
+                st = lanczos(matvec, v._data.detach(), ncv)
         except _StructureGrew as e:
             v = v.add(e.w, amplitudes=[1, 0])  # v's data, the union of the block structures
             continue

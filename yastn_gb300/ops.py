@@ -6,6 +6,7 @@ CUDA tensors of dtype float64 or complex128; anything else raises (there is no
 fallback path).
 """
 import ctypes
+import weakref
 
 import numpy as np
 import torch
@@ -112,12 +113,87 @@ def map_gather(src, gmap, conj=False):
     return out
 
 
+# ----------------------------------------------------------------------------- constant operands
+
+_HOLD = {'depth': 0, 'capturing': None, 'merge': {}, 'split': {}}
+
+
+class hold_constant_operands:
+    """Scope in which the merges and digit splits of unchanged operands are computed once.
+
+    An iterative solver applies one operator many times: in YASTN's ``eigs`` the effective
+    Hamiltonian's environment tensors, and their merged sector matrices, are the same tensor
+    objects in every call. Inside this scope a merge of the same source tensor object (its
+    version counter unchanged) by the same plan returns its earlier output while that output
+    is unmodified (its version counter unchanged), and an emulated dot reuses the BF16 digit
+    planes of an operand object it split before; tensors that require grad are never held.
+    Entries refer to their sources weakly (an entry ends with its source, so the temporaries
+    of each operator application are not kept), end with the outermost scope, and are
+    dropped when the stream capture state changes: entries made during a CUDA-graph capture
+    are used within that capture only, whose replays recompute them in order."""
+
+    def __enter__(self):
+        _HOLD['depth'] += 1
+        return self
+
+    def __exit__(self, *exc):
+        _HOLD['depth'] -= 1
+        if _HOLD['depth'] == 0:
+            _HOLD['merge'].clear()
+            _HOLD['split'].clear()
+        return False
+
+
+def _held(kind, key, src):
+    """(cache, key) for ``src`` in the current scope, or None (no scope, or src requires grad)."""
+    if _HOLD['depth'] == 0 or src.requires_grad:
+        return None
+    cap = torch.cuda.is_current_stream_capturing()
+    if _HOLD['capturing'] != cap:
+        _HOLD['merge'].clear()
+        _HOLD['split'].clear()
+        _HOLD['capturing'] = cap
+    return _HOLD[kind], key + (id(src),)
+
+
+def _hit(held, src):
+    """The held payload of src, if its entry is current."""
+    if held is None:
+        return None
+    cache, key = held
+    e = cache.get(key)
+    if e is None or e[0]() is not src or e[1] != src._version:
+        return None
+    payload, out_version = e[2], e[3]
+    if out_version is not None and payload._version != out_version:
+        return None
+    return payload
+
+
+def _store(held, src, payload, track_output=False):
+    cache, key = held
+
+    def drop(ref, cache=cache, key=key):
+        e = cache.get(key)
+        if e is not None and e[0] is ref:
+            del cache[key]
+    cache[key] = (weakref.ref(src, drop), src._version, payload, payload._version if track_output else None)
+
+
 def merge(data, order, meta_new, meta_mrg, Dsize):
-    """transpose_and_merge: fused blocks, zero where no source block lands."""
+    """transpose_and_merge: fused blocks, zero where no source block lands (inside
+    ``hold_constant_operands``, the earlier output for an unchanged source)."""
     data = _check(data, any_dtype=True)
     plan = P.merge_plan(order, meta_new, meta_mrg, Dsize)
+    held = _held('merge', (id(plan),), data)
+    out = _hit(held, data)
+    if out is not None:
+        return out
     out = (torch.empty if plan.full else torch.zeros)(Dsize, dtype=data.dtype, device=data.device)
-    return run_copy(plan, data, out)
+    run_copy(plan, data, out)
+    if held is not None:
+        _store(held, data, out, track_output=True)
+    return out
 
 
 def merge_backward(data_b, order, meta_new, meta_mrg, Dsize, D_source):
@@ -279,25 +355,45 @@ def _autotune_ozaki(plan, A, B, out, slices):
 
 def _ozaki_run(plan, A, B, out, slices, tc):
     """Both operands split by one yb_ozaki_split launch (B's blocks read by columns in
-    place), then the emulated GEMM: tcgen05 (tile layout) or mma.sync (digit planes)."""
+    place), then the emulated GEMM: tcgen05 (tile layout) or mma.sync (digit planes). Inside
+    ``hold_constant_operands`` an operand split before, unchanged, keeps its digit planes and
+    only the other operand is split (or neither)."""
     dev = A.device
     st = _stream()
-    a_ex = torch.empty(max(plan.a_exps, 1), dtype=torch.int32, device=dev)
-    b_ex = torch.empty(max(plan.b_exps, 1), dtype=torch.int32, device=dev)
     if tc:
         # tiles grouped by CTA (one CTA per SM) with balanced work
         tiles, offs = P.ozaki_tc_schedule(plan, _sm_count(dev))
         key, arrs = 'ozaki_tc', (plan.split_recs_tc, plan.split_groups_tc, plan.outs_tc, tiles, offs)
         asz, bsz = plan.a_size_tc, plan.b_size_tc
+        by_op = plan.split_groups_tc_ab
     else:
         key, arrs = 'ozaki', (plan.split_recs, plan.split_groups, plan.outs, plan.tiles)
         asz, bsz = plan.a_size, plan.b_size
+        by_op = plan.split_groups_ab
     darr = _dev(plan, key, arrs, dev)
     drec, dgrp, dout, dtl = darr[:4]
-    a_sl = torch.empty(max(asz, 1), dtype=torch.bfloat16, device=dev)
-    b_sl = torch.empty(max(bsz, 1), dtype=torch.bfloat16, device=dev)
-    N.call('yb_ozaki_split', _ptr(A), _ptr(B), _ptr(a_sl), _ptr(b_sl), _ptr(a_ex), _ptr(b_ex), _ptr(drec),
-           _ptr(dgrp), len(arrs[1]), slices, st)
+    held_a = _held('split', (id(plan), 0, bool(tc), slices), A)
+    held_b = _held('split', (id(plan), 1, bool(tc), slices), B)
+    hit_a, hit_b = _hit(held_a, A), _hit(held_b, B)
+    a_sl, a_ex = hit_a if hit_a else (torch.empty(max(asz, 1), dtype=torch.bfloat16, device=dev),
+                                      torch.empty(max(plan.a_exps, 1), dtype=torch.int32, device=dev))
+    b_sl, b_ex = hit_b if hit_b else (torch.empty(max(bsz, 1), dtype=torch.bfloat16, device=dev),
+                                      torch.empty(max(plan.b_exps, 1), dtype=torch.int32, device=dev))
+    if not hit_a and not hit_b:
+        groups, n_groups = dgrp, len(arrs[1])
+    elif hit_a != hit_b:
+        side = 1 if hit_a else 0  # split only the operand that is not held
+        groups = _dev(plan, (key, 'op', side), (by_op[side],), dev)[0]
+        n_groups = len(by_op[side])
+    else:
+        groups, n_groups = None, 0
+    if n_groups:
+        N.call('yb_ozaki_split', _ptr(A), _ptr(B), _ptr(a_sl), _ptr(b_sl), _ptr(a_ex), _ptr(b_ex), _ptr(drec),
+               _ptr(groups), n_groups, slices, st)
+    if held_a is not None and not hit_a:
+        _store(held_a, A, (a_sl, a_ex))
+    if held_b is not None and not hit_b:
+        _store(held_b, B, (b_sl, b_ex))
     if tc:
         N.call('yb_ozaki_gemm_tc', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
                len(arrs[3]), _ptr(darr[4]), len(arrs[4]) - 1, slices, st)
