@@ -370,7 +370,8 @@ def _ozaki_run(plan, A, B, out, slices, tc):
         key, arrs = 'ozaki', (plan.split_recs, plan.split_groups, plan.outs, plan.tiles)
         asz, bsz = plan.a_size, plan.b_size
         by_op = plan.split_groups_ab
-    darr = _dev(plan, key, arrs, dev)
+    # the per-operand group lists travel with the plan's arrays (no upload during a capture)
+    darr = _dev(plan, key, arrs + tuple(by_op), dev)
     drec, dgrp, dout, dtl = darr[:4]
     held_a = _held('split', (id(plan), 0, bool(tc), slices), A)
     held_b = _held('split', (id(plan), 1, bool(tc), slices), B)
@@ -383,8 +384,7 @@ def _ozaki_run(plan, A, B, out, slices, tc):
         groups, n_groups = dgrp, len(arrs[1])
     elif hit_a != hit_b:
         side = 1 if hit_a else 0  # split only the operand that is not held
-        groups = _dev(plan, (key, 'op', side), (by_op[side],), dev)[0]
-        n_groups = len(by_op[side])
+        groups, n_groups = darr[len(arrs) + side], len(by_op[side])
     else:
         groups, n_groups = None, 0
     if n_groups:
