@@ -81,7 +81,7 @@ def parse():
                    help='cfg2: run only the headline GEMM mode (for kernel launch lists); the emulated kernel of '
                         'each dot is chosen by its padded tile work rather than by timing, so that a profiler '
                         'slowing the kernels unequally does not change the choice')
-    p.add_argument('--ozaki-kernel', default='auto', choices=['auto', 'tcgen05', 'mma'],
+    p.add_argument('--ozaki-kernel', default='auto', choices=['auto', 'tcgen05', 'tcgen05-32', 'mma'],
                    help='emulated sector GEMM kernel: chosen per dot (auto), or forced (for kernel profiles)')
     return p.parse_args()
 
@@ -625,7 +625,7 @@ def run_gpu(args, wl):
     oz = ozaki_dot_plan(wl.mdot[0], ops.OZAKI_SLICES, wl.complex_gemm)
     tensor_flops = oz.flops * ops.OZAKI_SLICES * (ops.OZAKI_SLICES + 1) // 2
     use_tc = getattr(oz, 'tuned_tc', oz.prefer_tc) if ops.OZAKI_TC[0] is None else ops.OZAKI_TC[0]
-    top_name = 'tcgen05 (TMEM accumulators)' if use_tc else 'mma.sync'
+    top_name = (f'tcgen05 (TMEM accumulators, 128x{32 if use_tc == 32 else 64} tiles)' if use_tc else 'mma.sync')
 
     BK.set_gemm_mode('fp64')
 
@@ -814,7 +814,7 @@ def run_gpu_cfg2(args, wl):
         ops.OZAKI_AUTOTUNE[0] = False
     if args.ozaki_kernel != 'auto':
         from yastn_gb300 import ops
-        ops.OZAKI_TC[0] = args.ozaki_kernel == 'tcgen05'
+        ops.OZAKI_TC[0] = {'tcgen05': 64, 'tcgen05-32': 32, 'mma': False}[args.ozaki_kernel]
     for mode in modes:
         BK.set_gemm_mode(mode)
         v0 = h_v0.to(dev)
@@ -1288,8 +1288,11 @@ def kernel_roofline(torch, dev, run_once, w, gemm_mode, reps=5):
         # DRAM bytes (read + write) of the two tcgen05 GEMM launches of one matvec, from the ncu
         # capture in profiles/ozaki_gemm_tcgen05_dmrg_heff2.md; the digit planes they read
         # (algorithmic bytes, tile layout) are computed here
-        digits = sum(2 * (P.ozaki_dot_plan(st[2][2], ops.OZAKI_SLICES).a_size_tc +
-                          P.ozaki_dot_plan(st[2][2], ops.OZAKI_SLICES).b_size_tc) for st in dots)
+        def tc_digits(plan):
+            tn = getattr(plan, 'tuned_tc', plan.prefer_tc)
+            sfx = '_tc32' if tn == 32 else '_tc'
+            return 2 * (getattr(plan, 'a_size' + sfx) + getattr(plan, 'b_size' + sfx))
+        digits = sum(tc_digits(P.ozaki_dot_plan(st[2][2], ops.OZAKI_SLICES)) for st in dots)
         out.update(traffic=TC_GEMM_DRAM_BYTES_PER_MATVEC, traffic_unit="bytes per matvec (2 launches)",
                    traffic_source="ncu dram__bytes_read.sum + dram__bytes_write.sum, "
                                   "profiles/ozaki_gemm_tcgen05_dmrg_heff2.md",

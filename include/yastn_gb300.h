@@ -168,7 +168,7 @@ int yb_gemm_reduce(void* c, const void* p, int dtype, const int64_t* recs, const
  *   multiple of 16) [6] exponent offset [7] Kp = K rounded up to 16 (padding zeroed)
  *   [8] stride between consecutive k [9] operand (bit 0: 0 reads a_src and writes
  *   a_slices / a_exps, 1 the b_ ones) | tile rows << 8 (0: planes [slice][row][Kp] for
- *   yb_ozaki_gemm; 64 or 128: the tile layout of yb_ozaki_gemm_tc, rows padded with zeros
+ *   yb_ozaki_gemm; 32, 64 or 128: the tile layout of yb_ozaki_gemm_tc, rows padded with zeros
  *   to a multiple of the tile rows, per slice blocks of tile rows x 16 ordered (row tile,
  *   K step), each in the canonical K-major core-matrix order: byte offset of (row r, k) in a
  *   block (r/8)*256 + (k/8)*128 + (r%8)*16 + (k%8)*2).
@@ -192,9 +192,12 @@ int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices,
                   double* c, const int64_t* outs, const int32_t* tiles, int n_tiles, int slices_count,
                   void* stream);
 /* yb_ozaki_gemm_tc: yb_ozaki_gemm on the tcgen05 tensor cores, operands from
- * yb_ozaki_split in the tile layout (128 rows for A, 64 for B; output records [4], [6] = the
- * A / B slice-0 offsets in that layout); tiles are (output, tile row, tile col, 0) of 128 rows
- * x 64 columns. A persistent kernel, one CTA per SM, each walking its share of the tiles:
+ * yb_ozaki_split in the tile layout (128 rows for A, tile_n for B; output records [4], [6] =
+ * the A / B slice-0 offsets in that layout); tiles are (output, tile row, tile col, 0) of 128
+ * rows x tile_n columns, tile_n = 64 or 32 (else YB_ERR_INVALID). With tile_n = 32 a chunk's
+ * digit-diagonal accumulators take slices_count x 32 of the 512 tensor-memory columns and
+ * consecutive chunks alternate between two such buffers, so the fold of one tile overlaps the
+ * MMAs of the next. A persistent kernel, one CTA per SM, each walking its share of the tiles:
  * with cta_tiles = NULL CTA b takes tiles b, b + G, ... (G = min(n_tiles, SMs)); otherwise
  * the tiles are grouped by CTA and CTA b takes [cta_tiles[b], cta_tiles[b+1]) of n_ctas CTAs
  * (n_ctas <= the SM count, else YB_ERR_INVALID).
@@ -205,7 +208,7 @@ int yb_ozaki_gemm(const void* a_slices, const int* a_exps, const void* b_slices,
  * word read by yb_ozaki_device_error. */
 int yb_ozaki_gemm_tc(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps,
                      double* c, const int64_t* outs, const int32_t* tiles, int n_tiles,
-                     const int32_t* cta_tiles, int n_ctas, int slices_count, void* stream);
+                     const int32_t* cta_tiles, int n_ctas, int tile_n, int slices_count, void* stream);
 /* yb_ozaki_device_error: copies the tcgen05 kernel's status word to *out (0: no failure),
  * synchronising the stream, and clears it when reset != 0. */
 int yb_ozaki_device_error(int* out, int reset, void* stream);

@@ -204,7 +204,7 @@ def test_dot_ozaki_on_reference_calls(name, cuda_device):
     assert n > 0
 
 
-@pytest.mark.parametrize('tc', [True, False])
+@pytest.mark.parametrize('tc', [64, 32, False])
 def test_hold_constant_operands(tc, cuda_device):
     """Inside ops.hold_constant_operands an unchanged operand's merge and digit planes are
     computed once: results stay bit-identical to calls outside the scope, a held operand
@@ -306,7 +306,7 @@ def test_dot_small_and_ragged_sectors(emulated, cplx, cuda_device):
     ref = oracle.dot(A, B, meta, oc)
     saved = ops.OZAKI_TC[0]
     try:
-        for tc in ((True, False) if emulated else (None,)):
+        for tc in ((64, 32, False) if emulated else (None,)):
             ops.OZAKI_TC[0] = tc
             f = ops.dot_ozaki if emulated else ops.dot
             got = host(f(dev(A), dev(B), meta, oc))
@@ -319,8 +319,9 @@ def test_dot_small_and_ragged_sectors(emulated, cplx, cuda_device):
 
 @pytest.mark.parametrize('name', ['cfg1', 'small'])
 def test_ozaki_tcgen05_matches_mma_sync(name, cuda_device):
-    """The tcgen05/TMEM kernel and the mma.sync kernel form the same exact diagonal sums and
-    the same folds: their products agree bit for bit; no CTA reports a failed wait."""
+    """The tcgen05/TMEM kernel (128 x 64 and 128 x 32 tiles) and the mma.sync kernel form the
+    same exact diagonal sums and the same folds: their products agree bit for bit; no CTA
+    reports a failed wait."""
     if name == 'cfg1':
         tr = load_trace('cfg1')
         A, B = cfg1_inputs(tr)
@@ -332,17 +333,20 @@ def test_ozaki_tcgen05_matches_mma_sync(name, cuda_device):
         meta, A, B, Dsize = _small_sector_problem(22)
     saved = ops.OZAKI_TC[0]
     try:
-        ops.OZAKI_TC[0] = True
-        assert ops.ozaki_device_error(reset=True) == 0
-        got_tc = host(ops.dot_ozaki(dev(A), dev(B), meta, Dsize))
-        assert ops.ozaki_device_error(reset=True) == 0
+        got_tc = {}
+        for tn in (64, 32):  # 128 x 64 tiles; 128 x 32 tiles with two alternating TMEM buffers
+            ops.OZAKI_TC[0] = tn
+            assert ops.ozaki_device_error(reset=True) == 0
+            got_tc[tn] = host(ops.dot_ozaki(dev(A), dev(B), meta, Dsize))
+            assert ops.ozaki_device_error(reset=True) == 0
         ops.OZAKI_TC[0] = False
         got_mma = host(ops.dot_ozaki(dev(A), dev(B), meta, Dsize))
     finally:
         ops.OZAKI_TC[0] = saved
-    np.testing.assert_array_equal(got_tc, got_mma)
+    np.testing.assert_array_equal(got_tc[64], got_mma)
+    np.testing.assert_array_equal(got_tc[32], got_mma)
     ref = oracle.dot(A, B, meta, Dsize)
-    assert rel(got_tc, ref) <= TOL
+    assert rel(got_mma, ref) <= TOL
 
 
 @pytest.mark.parametrize('cplx', [False, True])
@@ -377,7 +381,8 @@ def test_ozaki_split_matches_digit_model(cplx, slices, cuda_device):
     dA, dB = dev(A), dev(B)
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     for recs, groups, sizes in ((plan.split_recs, plan.split_groups, (plan.a_size, plan.b_size)),
-                                (plan.split_recs_tc, plan.split_groups_tc, (plan.a_size_tc, plan.b_size_tc))):
+                                (plan.split_recs_tc, plan.split_groups_tc, (plan.a_size_tc, plan.b_size_tc)),
+                                (plan.split_recs_tc32, plan.split_groups_tc32, (plan.a_size_tc32, plan.b_size_tc32))):
         want, want_e = PI.ozaki_split(recs, groups, A, B, slices, sizes, (plan.a_exps, plan.b_exps))
         a_sl = torch.full((sizes[0],), 7.0, dtype=torch.bfloat16, device='cuda')  # nonzero: padding must be written
         b_sl = torch.full((sizes[1],), 7.0, dtype=torch.bfloat16, device='cuda')

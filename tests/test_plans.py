@@ -808,11 +808,14 @@ def test_ozaki_plan_records():
                                    A[sla[0]:sla[1]].reshape(Da) @ B[slb[0]:slb[1]].reshape(Db), rtol=1e-13)
 
 
-def test_ozaki_tiled_records_and_tiles():
+@pytest.mark.parametrize('tn', [64, 32])
+def test_ozaki_tiled_records_and_tiles(tn):
     """Records of the tcgen05 kernel: every operand block gets s * ceil(rows / tile) * tile * Kp
-    digits in the tile layout (128 rows for A, 64 for B's columns), without overlap and in
-    block order; the 8-row groups cover the padded rows; the output records point at the
-    remapped blocks; tiles cover every output once by decreasing K."""
+    digits in the tile layout (128 rows for A, the tile width 64 or 32 for B's columns),
+    without overlap and in block order; the 8-row groups cover the padded rows; the output
+    records point at the remapped blocks; tiles cover every output once by decreasing K."""
+    sfx = '_tc' if tn == 64 else '_tc32'
+    at = lambda plan, name: getattr(plan, name + sfx)
     rng = np.random.default_rng(23)
     shapes = [(40, 30, 20), (16, 16, 17), (130, 20, 70), (5, 40, 9), (3, 8, 100), (6, 300, 200)]
     meta, oa, ob, oc = [], 0, 0, 0
@@ -822,28 +825,33 @@ def test_ozaki_tiled_records_and_tiles():
     meta = tuple(meta)
     for cplx in (False, True):
         plan = P.ozaki_dot_plan(meta, 8, cplx)
-        for op, th, size in ((0, 128, plan.a_size_tc), (1, 64, plan.b_size_tc)):
+        recs_t = at(plan, 'split_recs')
+        for op, th, size in ((0, 128, at(plan, 'a_size')), (1, tn, at(plan, 'b_size'))):
             end = 0
-            for r in _recs_of(plan, op, tc=True):
+            for r in recs_t:
+                if int(r[9]) & 1 != op:
+                    continue
                 assert int(r[5]) == end and int(r[9]) == op | (th << 8)
                 end += 8 * (-(-int(r[1]) // th) * th) * int(r[7])
             assert end == size
-        groups = [(int(g[0]), int(g[1])) for g in plan.split_groups_tc]
-        want = {(ri, g) for ri, r in enumerate(plan.split_recs_tc)
+        groups = [(int(g[0]), int(g[1])) for g in at(plan, 'split_groups')]
+        want = {(ri, g) for ri, r in enumerate(recs_t)
                 for g in range(0, -(-int(r[1]) // (int(r[9]) >> 8)) * (int(r[9]) >> 8), P.OZ_SPLIT_ROWS)}
         assert set(groups) == want and len(groups) == len(want)
+        ga, gb = getattr(plan, 'split_groups' + sfx + '_ab')
+        assert sorted(map(tuple, np.concatenate([ga, gb]).tolist())) == sorted(groups)
+        assert all(int(recs_t[g[0]][9]) & 1 == 0 for g in ga) and all(int(recs_t[g[0]][9]) & 1 == 1 for g in gb)
         # the same blocks in both layouts
-        assert np.array_equal(np.delete(plan.split_recs, [5, 9], axis=1),
-                              np.delete(plan.split_recs_tc, [5, 9], axis=1))
-        new = {(int(r[9]) & 1, int(r[5])): int(t[5]) for r, t in zip(plan.split_recs, plan.split_recs_tc)}
-        for o, t in zip(plan.outs, plan.outs_tc):
+        assert np.array_equal(np.delete(plan.split_recs, [5, 9], axis=1), np.delete(recs_t, [5, 9], axis=1))
+        new = {(int(r[9]) & 1, int(r[5])): int(t[5]) for r, t in zip(plan.split_recs, recs_t)}
+        for o, t in zip(plan.outs, at(plan, 'outs')):
             assert int(t[4]) == new[(0, int(o[4]))] and int(t[6]) == new[(1, int(o[6]))]
             assert np.array_equal(np.delete(o, [4, 6]), np.delete(t, [4, 6]))
-        want = {(oi, tr, tc) for oi, o in enumerate(plan.outs_tc)
-                for tr in range(-(-int(o[1]) // 128)) for tc in range(-(-int(o[2]) // 64))}
-        got = [tuple(int(x) for x in t[:3]) for t in plan.tiles_tc]
+        want = {(oi, tr, tc) for oi, o in enumerate(at(plan, 'outs'))
+                for tr in range(-(-int(o[1]) // 128)) for tc in range(-(-int(o[2]) // tn))}
+        got = [tuple(int(x) for x in t[:3]) for t in at(plan, 'tiles')]
         assert len(got) == len(want) and set(got) == want
-        ks = [int(plan.outs_tc[t[0]][8]) for t in plan.tiles_tc]
+        ks = [int(at(plan, 'outs')[t[0]][8]) for t in at(plan, 'tiles')]
         assert ks == sorted(ks, reverse=True)
 
 
@@ -868,7 +876,9 @@ def test_ozaki_split_model_reconstructs_the_operands():
         for s in (6, 8):
             plan = P.ozaki_dot_plan(meta, s, cplx)
             for recs, groups, sizes in ((plan.split_recs, plan.split_groups, (plan.a_size, plan.b_size)),
-                                        (plan.split_recs_tc, plan.split_groups_tc, (plan.a_size_tc, plan.b_size_tc))):
+                                        (plan.split_recs_tc, plan.split_groups_tc, (plan.a_size_tc, plan.b_size_tc)),
+                                        (plan.split_recs_tc32, plan.split_groups_tc32,
+                                         (plan.a_size_tc32, plan.b_size_tc32))):
                 dig, exps = PI.ozaki_split(recs, groups, A, B, s, sizes, (plan.a_exps, plan.b_exps))
                 for op in (0, 1):
                     d = dig[op]
@@ -900,15 +910,17 @@ def test_ozaki_tc_schedule_covers_tiles_once_and_balances():
     (longest-processing-time assignment) on the DMRG workload's two emulated dots."""
     from yastn_gb300.workloads import Heff2Workload
     dots = [c['args'][2] for c in Heff2Workload().calls if c['fn'] == 'dot']
-    for meta in (dots[0], dots[3]):
+    for meta, tn in ((dots[0], 64), (dots[3], 64), (dots[0], 32), (dots[3], 32)):
         plan = P.ozaki_dot_plan(meta, 8)
+        tiles_t = plan.tiles_tc if tn == 64 else plan.tiles_tc32
+        outs_t = plan.outs_tc if tn == 64 else plan.outs_tc32
         for sms in (152, 37):
-            tiles, offs = P.ozaki_tc_schedule(plan, sms)
-            assert offs[0] == 0 and offs[-1] == len(plan.tiles_tc) and len(offs) == min(sms, len(plan.tiles_tc)) + 1
+            tiles, offs = P.ozaki_tc_schedule(plan, sms, tn)
+            assert offs[0] == 0 and offs[-1] == len(tiles_t) and len(offs) == min(sms, len(tiles_t)) + 1
             assert np.all(np.diff(offs) >= 0)
             key = lambda a: sorted(map(tuple, a.tolist()))
-            assert key(tiles) == key(plan.tiles_tc)
-            steps = lambda t: int(plan.outs_tc[t[0]][9]) // 16 + P.OZ_TC_FOLD_STEPS
+            assert key(tiles) == key(tiles_t)
+            steps = lambda t: int(outs_t[t[0]][9]) // 16 + P.OZ_TC_FOLD_STEPS
             loads = [sum(steps(t) for t in tiles[offs[b]:offs[b + 1]]) for b in range(len(offs) - 1)]
             biggest = max(steps(t) for t in tiles)
             assert max(loads) <= sum(loads) / len(loads) + biggest

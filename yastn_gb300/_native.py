@@ -42,7 +42,7 @@ SIGNATURES = {
     'yb_fix_signs_adjoint': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp], _i),
     'yb_ozaki_split': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
     'yb_ozaki_gemm': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp], _i),
-    'yb_ozaki_gemm_tc': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp, _i, _i, _vp], _i),
+    'yb_ozaki_gemm_tc': ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp, _i, _i, _i, _vp], _i),
     'yb_ozaki_device_error': ([_vp, _i, _vp], _i),
     'yb_ozaki_dot_static': ([_vp, _vp, _vp, _i, _vp, _vp, _i, _vp, _vp, _i, _vp, _vp, _vp, _i, _i,
                              _i64, _i64, _i64, _i64, _vp], _i),

@@ -549,7 +549,7 @@ class OzakiPlan:
         self._dev = {}
 
 
-OZAKI_TC_M, OZAKI_TC_N = 128, 64  # output tile of the tcgen05 emulated GEMM
+OZAKI_TC_M, OZAKI_TC_N = 128, 64  # output tile of the tcgen05 emulated GEMM (also 128 x 32)
 OZAKI_MIN_DIM = 16  # sector GEMMs contracting fewer indices than this stay on the native FP64 kernel
 OZAKI_SKINNY_ROWS = 8  # sector GEMMs with at most this many rows (and more than 64 columns) too
 OZ_SPLIT_REC = 10  # YB_OZ_SPLIT_REC
@@ -588,25 +588,26 @@ def _groups_by_operand(recs, groups):
 OZ_TC_FOLD_STEPS = 6  # fold + write of a full 128 x 64 tile, in K-step units of the tcgen05 kernel
 
 
-def ozaki_tc_schedule(plan, n_ctas):
-    """Tiles of the tcgen05 kernel grouped by CTA (longest processing time first: each tile,
-    by decreasing cost, to the least loaded CTA; cost = K steps + the fold of its valid
-    elements). Returns (tiles reordered, int32 offsets of the n_ctas + 1 CTA ranges)."""
-    key = ('tc_sched', n_ctas)
+def ozaki_tc_schedule(plan, n_ctas, tile_n=64):
+    """Tiles of the tcgen05 kernel (128 x ``tile_n``) grouped by CTA (longest processing time
+    first: each tile, by decreasing cost, to the least loaded CTA; cost = K steps + the fold of
+    its valid elements). Returns (tiles reordered, int32 offsets of the n_ctas + 1 CTA ranges)."""
+    key = ('tc_sched', n_ctas, tile_n)
     got = plan._dev.get(key)
     if got is not None:
         return got
     import heapq
-    tiles = plan.tiles_tc
+    sfx = '_tc' if tile_n == 64 else '_tc32'
+    tiles, outs = getattr(plan, 'tiles' + sfx), getattr(plan, 'outs' + sfx)
     n_ctas = max(1, min(n_ctas, len(tiles)))
     cost = []
     for i, (oi, tr, tc, _) in enumerate(tiles):
-        o = plan.outs_tc[oi]
+        o = outs[oi]
         m, n, Kp = int(o[1]), int(o[2]), int(o[9])
         steps = Kp // 16
         chunks = -(-steps // 25)
-        valid = min(OZAKI_TC_M, m - OZAKI_TC_M * int(tr)) * min(OZAKI_TC_N, n - OZAKI_TC_N * int(tc))
-        cost.append((steps + OZ_TC_FOLD_STEPS * chunks * valid / (OZAKI_TC_M * OZAKI_TC_N), i))
+        valid = min(OZAKI_TC_M, m - OZAKI_TC_M * int(tr)) * min(tile_n, n - tile_n * int(tc))
+        cost.append((steps + OZ_TC_FOLD_STEPS * chunks * valid / (OZAKI_TC_M * 64), i))
     cost.sort(reverse=True)
     heap = [(0.0, b) for b in range(n_ctas)]
     lists = [[] for _ in range(n_ctas)]
@@ -682,27 +683,34 @@ def ozaki_dot_plan(meta_dot, s, cplx=False):
         plan.native = _pack_gemm(small)
         plan.native_direct = _pack_gemm(small, allow_split=False)  # no chunk workspace
         plan.covered = dot_coverage(meta_dot)
-        # 128 x 64 tiles of the tcgen05 kernel (longest K first) and the digit planes in its
-        # tile layout (rows padded to 128 for A, 64 for B)
-        sr, sg, asz, bsz, _, _, where = _split_layout(blocks, s, OZAKI_TC_M, OZAKI_TC_N)
-        plan.split_recs_tc, plan.split_groups_tc, plan.a_size_tc, plan.b_size_tc = sr, sg, asz, bsz
-        plan.split_groups_tc_ab = _groups_by_operand(sr, sg)
-        plan.outs_tc = outs_for(where)
-        tiles_tc = []
-        for oi, o in enumerate(plan.outs_tc):
-            m, n, K = int(o[1]), int(o[2]), int(o[8])
-            for tr in range(-(-m // OZAKI_TC_M)):
-                for tc in range(-(-n // OZAKI_TC_N)):
-                    tiles_tc.append((K, oi, tr, tc))
-        tiles_tc.sort(key=lambda x: -x[0])
-        plan.tiles_tc = np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles_tc], dtype=np.int32).reshape(-1, 4)
-        # padded MMA work of the two tilings: the tcgen05 kernel (128 x 64 tiles) unless its
-        # padding costs over 1.6 times the 64 x 64 tiles of the mma.sync kernel (the tcgen05
-        # kernel measured faster on the DMRG workload's sectors at 1.3 times the padded work)
-        w64 = sum(-(-int(o[1]) // 64) * 64 * -(-int(o[2]) // 64) * 64 * int(o[9]) for o in outs)
-        w128 = sum(-(-int(o[1]) // OZAKI_TC_M) * OZAKI_TC_M * -(-int(o[2]) // OZAKI_TC_N) * OZAKI_TC_N * int(o[9])
-                   for o in outs)
-        plan.prefer_tc = bool(len(outs)) and w128 <= 1.6 * w64
+        # tiles of the tcgen05 kernel, 128 x 64 and 128 x 32 (longest K first), and the digit
+        # planes in its tile layout (rows padded to 128 for A, to the tile width for B)
+        for tn, sfx in ((64, '_tc'), (32, '_tc32')):
+            sr, sg, asz, bsz, _, _, where = _split_layout(blocks, s, OZAKI_TC_M, tn)
+            outs_t = outs_for(where)
+            tiles_t = []
+            for oi, o in enumerate(outs_t):
+                m, n, K = int(o[1]), int(o[2]), int(o[8])
+                for tr in range(-(-m // OZAKI_TC_M)):
+                    for tc in range(-(-n // tn)):
+                        tiles_t.append((K, oi, tr, tc))
+            tiles_t.sort(key=lambda x: -x[0])
+            setattr(plan, 'split_recs' + sfx, sr)
+            setattr(plan, 'split_groups' + sfx, sg)
+            setattr(plan, 'split_groups' + sfx + '_ab', _groups_by_operand(sr, sg))
+            setattr(plan, 'a_size' + sfx, asz)
+            setattr(plan, 'b_size' + sfx, bsz)
+            setattr(plan, 'outs' + sfx, outs_t)
+            setattr(plan, 'tiles' + sfx, np.array([(oi, tr, tc, 0) for _, oi, tr, tc in tiles_t],
+                                                  dtype=np.int32).reshape(-1, 4))
+        # padded MMA work of the tilings: a tcgen05 tiling (the narrower one unless it pads more)
+        # unless its padding costs over 1.6 times the 64 x 64 tiles of the mma.sync kernel (the
+        # tcgen05 kernel measured faster on the DMRG workload's sectors at 1.3 times the padded work)
+        def padded(tm, tn):
+            return sum(-(-int(o[1]) // tm) * tm * -(-int(o[2]) // tn) * tn * int(o[9]) for o in outs)
+        w64, w128, w32 = padded(64, 64), padded(OZAKI_TC_M, 64), padded(OZAKI_TC_M, 32)
+        best_tc = 32 if w32 <= w128 else 64
+        plan.prefer_tc = (best_tc if min(w32, w128) <= 1.6 * w64 else False) if len(outs) else False
         return plan
     return CACHE.get((meta_dot,), ('ozaki_dot', s, bool(cplx)), build)
 

@@ -2,8 +2,8 @@
 // the digit planes that yb_ozaki_split_tiled writes in the tile layout of the UMMA
 // shared-memory descriptors.
 //
-// A persistent kernel (one CTA per SM) walks its share of the 128 x 64 output tiles (tiles
-// sorted by decreasing K, CTA b taking tiles b, b + G, b + 2G, ...) with three warp roles:
+// A persistent kernel (one CTA per SM) walks its share of the 128 x NT output tiles (NT = 64
+// or 32; tiles sorted by decreasing K, or grouped by CTA by the host) with three warp roles:
 //  - warp 0 (one thread) streams the S digit tiles of A (128 x 16) and of B (64 x 16) of each
 //    16-long K step into a 4-stage shared-memory ring with cp.async.bulk copies completing on
 //    the stage's mbarrier, refilling a stage as soon as the MMAs that read it have completed,
@@ -12,8 +12,10 @@
 //    K=16) into the S digit-diagonal accumulators in tensor memory (S x 64 of the 512 TMEM
 //    columns), up to four products per tcgen05.mma (N = 64 per B slice: slices tb..tb+3 are
 //    one operand, diagonals ta+tb..ta+tb+3 adjacent accumulators; 13 MMAs per step for S = 8),
-//    and frees the stage with tcgen05.commit;
-//  - 16 fold warps (4 per TMEM lane quarter, 16 columns each) read the accumulators back at
+//    and frees the stage with tcgen05.commit; with NT = 32 the S x 32 accumulator columns of
+//    a chunk fit twice in the 512 columns, and consecutive chunks alternate between the two
+//    buffers, so the MMAs of the next chunk (and tile) need not wait for this chunk's fold;
+//  - 16 fold warps (4 per TMEM lane quarter, NT/4 columns each) read the accumulators back at
 //    the end of every 400-long K chunk (exact FP32 integer sums), combine the diagonals exactly
 //    into a 128-bit integer on the integer pipe, round it once to FP64 into the tile's FP64
 //    accumulators (bit-identical to the mma.sync kernel's fold), release the tensor memory to
@@ -29,15 +31,13 @@ namespace yb {
 namespace {
 using namespace oz;
 
-constexpr int kM = 128, kN = 64, kK = 16, kStages = 4;
+constexpr int kM = 128, kK = 16, kStages = 4;
 constexpr int kFoldWarps = 16;              // 4 per TMEM lane quarter
-constexpr int kFoldCols = kN / (kFoldWarps / 4);  // 16 columns per fold warp
 constexpr int kFold = 32 * kFoldWarps;      // fold / epilogue threads (warps 2-17)
 constexpr int kThreadsT = 64 + kFold;       // producer warp, MMA warp, fold warps
 constexpr int kChunkSteps = 25;             // 400-long K chunks: exact FP32 diagonal sums
 constexpr long long kSpin = 1ll << 24;
 constexpr uint32_t kATile = kM * kK * 2;  // one slice's 128 x 16 digit tile, bytes
-constexpr uint32_t kBTile = kN * kK * 2;  // 64 x 16
 
 __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
@@ -48,16 +48,24 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_
 // out record (16 int64): [0] c offset [1] m [2] n [3] ldc [4] A slices offset (tile layout)
 // [5] A exponents offset [6] B slices offset (tile layout) [7] B exponents offset [8] K [9] Kp
 // [10] output column stride (2: one part of complex data)
-template <int S>
+// NT: output tile width (64, or 32: then the S diagonal accumulators of a chunk take S x 32 of
+// the 512 TMEM columns and two chunks alternate between two buffers, so that the fold of one
+// tile overlaps the MMAs of the next).
+template <int S, int NT>
 __global__ void __launch_bounds__(kThreadsT, 1)
     ozaki_gemm_tc_kernel(const __nv_bfloat16* __restrict__ As, const int* __restrict__ Ae,
                          const __nv_bfloat16* __restrict__ Bs, const int* __restrict__ Be, double* __restrict__ C,
                          const int64_t* __restrict__ outs, const int32_t* __restrict__ tiles, int n_tiles,
                          const int32_t* __restrict__ cta_tiles, int* __restrict__ err) {
+  constexpr int kN = NT;
+  constexpr uint32_t kBTile = kN * kK * 2;          // one slice's NT x 16 digit tile, bytes
+  constexpr int kFoldCols = kN / (kFoldWarps / 4);  // columns per fold warp (16 or 8)
+  constexpr int kBufCols = S * kN;                  // TMEM columns of one chunk's accumulators
+  constexpr int kBufs = 2 * kBufCols <= 512 ? 2 : 1;
   constexpr uint32_t kStage = S * (kATile + kBTile);
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ uint32_t tmem_slot;
-  __shared__ __align__(8) uint64_t full[kStages], empty[kStages], accb, tfree, drain;
+  __shared__ __align__(8) uint64_t full[kStages], empty[kStages], accb[2], tfree[2], drain;
   __shared__ int failed_s;
   volatile int* failed = &failed_s;
 
@@ -79,8 +87,10 @@ __global__ void __launch_bounds__(kThreadsT, 1)
       mbar_init(smem_u32(&full[i]), 1);
       mbar_init(smem_u32(&empty[i]), 1);
     }
-    mbar_init(smem_u32(&accb), 1);
-    mbar_init(smem_u32(&tfree), kFold);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(smem_u32(&accb[i]), 1);
+      mbar_init(smem_u32(&tfree[i]), kFold);
+    }
     mbar_init(smem_u32(&drain), 1);
     asm volatile("fence.mbarrier_init.release.cluster;");
     *failed = 0;
@@ -141,8 +151,11 @@ __global__ void __launch_bounds__(kThreadsT, 1)
         const int64_t ksteps = outs[(int64_t)tl.x * 16 + 9] / kK;
         const int64_t nchunks = (ksteps + kChunkSteps - 1) / kChunkSteps;
         for (int64_t ch = 0; ch < nchunks && ok; ++ch, ++gch) {
-          if (gch > 0) {  // the previous chunk's fold has read the accumulators this chunk overwrites
-            if (*failed || !mbar_wait(smem_u32(&tfree), (uint32_t)((gch - 1) & 1), kSpin)) { ok = false; break; }
+          const int buf = (int)(gch % kBufs);
+          const int64_t use = gch / kBufs;  // earlier chunks in this buffer
+          const uint32_t acc_base = tmem + (uint32_t)(buf * kBufCols);
+          if (use > 0) {  // the fold of this buffer's previous chunk has read the accumulators
+            if (*failed || !mbar_wait(smem_u32(&tfree[buf]), (uint32_t)((use - 1) & 1), kSpin)) { ok = false; break; }
             asm volatile("tcgen05.fence::after_thread_sync;");
           }
           const int64_t s1 = min(ksteps, (ch + 1) * kChunkSteps);
@@ -164,13 +177,13 @@ __global__ void __launch_bounds__(kThreadsT, 1)
 #pragma unroll
               for (int tb = 0; tb < S - ta; tb += 4) {
                 const int k = (S - ta - tb) < 4 ? (S - ta - tb) : 4;
-                tc_mma(tmem + (uint32_t)((ta + tb) * kN), umma_desc(a0 + ta * kATile), umma_desc(b0 + tb * kBTile),
+                tc_mma(acc_base + (uint32_t)((ta + tb) * kN), umma_desc(a0 + ta * kATile), umma_desc(b0 + tb * kBTile),
                        idesc0 | ((uint32_t)((kN * k) >> 3) << 17), (first && ta == 0) ? 0u : 1u);
               }
             tc_commit(smem_u32(&empty[stage]));
           }
           if (!ok) break;
-          tc_commit(smem_u32(&accb));  // this chunk's accumulators are complete once its MMAs are
+          tc_commit(smem_u32(&accb[buf]));  // this chunk's accumulators are complete once its MMAs are
         }
       }
       if (!ok) {
@@ -200,7 +213,9 @@ __global__ void __launch_bounds__(kThreadsT, 1)
       const bool busy = (row0 + 32 * q < m) && (col0 < n);
       double acc[kFoldCols];
       for (int64_t ch = 0; ch < nchunks; ++ch, ++gch) {
-        if (*failed || !mbar_wait(smem_u32(&accb), (uint32_t)(gch & 1), kSpin)) {
+        const int buf = (int)(gch % kBufs);
+        const uint32_t acc_base = tmem + (uint32_t)(buf * kBufCols);
+        if (*failed || !mbar_wait(smem_u32(&accb[buf]), (uint32_t)((gch / kBufs) & 1), kSpin)) {
           ok = false;
           break;
         }
@@ -217,7 +232,7 @@ __global__ void __launch_bounds__(kThreadsT, 1)
             uint32_t v[S][4];
 #pragma unroll
             for (int d = 0; d < S; ++d)
-              tc_ld4(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(d * kN + kFoldCols * cg + cb * 4), v[d]);
+              tc_ld4(acc_base + ((uint32_t)(32 * q) << 16) + (uint32_t)(d * kN + kFoldCols * cg + cb * 4), v[d]);
             asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
@@ -237,7 +252,7 @@ __global__ void __launch_bounds__(kThreadsT, 1)
           else fold(std::false_type{});
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
-        mbar_arrive(smem_u32(&tfree));
+        mbar_arrive(smem_u32(&tfree[buf]));
       }
       if (!ok) break;
       // the tile, straight from registers (the next tile's MMAs proceed meanwhile)
@@ -270,12 +285,12 @@ int sm_count() {
   return sms[dev];
 }
 
-template <int S>
+template <int S, int NT>
 int launch_gemm_tc(const void* As, const int* Ae, const void* Bs, const int* Be, double* C, const int64_t* outs,
                    const int32_t* tiles, int n_tiles, const int32_t* cta_tiles, int n_ctas, int* err,
                    cudaStream_t s) {
-  const size_t smem = (size_t)kStages * S * (kATile + kBTile);
-  auto kern = ozaki_gemm_tc_kernel<S>;
+  const size_t smem = (size_t)kStages * S * (kATile + (uint32_t)(NT * kK * 2));
+  auto kern = ozaki_gemm_tc_kernel<S, NT>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) { set_cuda_error((int)e); return YB_ERR_CUDA; }
   const int sms = sm_count();
@@ -298,22 +313,26 @@ extern "C" {
 
 int yb_ozaki_gemm_tc(const void* a_slices, const int* a_exps, const void* b_slices, const int* b_exps, double* c,
                      const int64_t* outs, const int32_t* tiles, int n_tiles, const int32_t* cta_tiles, int n_ctas,
-                     int slices_count, void* stream) {
+                     int tile_n, int slices_count, void* stream) {
   if (n_tiles == 0) return YB_OK;
   if (!a_slices || !a_exps || !b_slices || !b_exps || !c || !outs || !tiles || n_tiles < 0) return YB_ERR_INVALID;
+  if (tile_n != 64 && tile_n != 32) return YB_ERR_INVALID;
   int* err = nullptr;
   cudaError_t e = cudaGetSymbolAddress((void**)&err, g_ozaki_tc_error);
   if (e != cudaSuccess) { yb::set_cuda_error((int)e); return YB_ERR_CUDA; }
   cudaStream_t s = (cudaStream_t)stream;
-  switch (slices_count) {
-    case 8:
-      return yb::launch_gemm_tc<8>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, cta_tiles, n_ctas, err, s);
-    case 7:
-      return yb::launch_gemm_tc<7>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, cta_tiles, n_ctas, err, s);
-    case 6:
-      return yb::launch_gemm_tc<6>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, cta_tiles, n_ctas, err, s);
+#define YB_TC_LAUNCH(SS, NN) \
+  return yb::launch_gemm_tc<SS, NN>(a_slices, a_exps, b_slices, b_exps, c, outs, tiles, n_tiles, cta_tiles, n_ctas, err, s)
+  switch (slices_count * 100 + tile_n) {
+    case 864: YB_TC_LAUNCH(8, 64);
+    case 832: YB_TC_LAUNCH(8, 32);
+    case 764: YB_TC_LAUNCH(7, 64);
+    case 732: YB_TC_LAUNCH(7, 32);
+    case 664: YB_TC_LAUNCH(6, 64);
+    case 632: YB_TC_LAUNCH(6, 32);
     default: return YB_ERR_INVALID;
   }
+#undef YB_TC_LAUNCH
 }
 
 int yb_ozaki_device_error(int* out, int reset, void* stream) {

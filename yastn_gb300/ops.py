@@ -284,7 +284,8 @@ def dot(A, B, meta_dot, Dsize):
 OZAKI_SLICES = 8  # 57 bits per operand: FP64-grade products
 
 
-OZAKI_TC = [None]  # emulated GEMM kernel: None = autotuned per dot, True = tcgen05/TMEM, False = mma.sync
+OZAKI_TC = [None]  # emulated GEMM kernel: None = autotuned per dot; False = mma.sync; 64 (or True) / 32 =
+                  # tcgen05/TMEM with 128 x 64 / 128 x 32 output tiles
 OZAKI_AUTOTUNE = [True]  # False: choose by the tile-padding estimate without timing
 
 
@@ -336,13 +337,14 @@ def _side_stream(device):
 
 
 def _autotune_ozaki(plan, A, B, out, slices):
-    """Kernel choice for one dot metadata: the tcgen05 and the mma.sync kernels produce the
-    same bits, so the first call times both (CUDA events; skipped during stream capture,
-    where the tile-padding estimate decides) and the plan keeps the faster."""
+    """Kernel choice for one dot metadata: the mma.sync kernel and the tcgen05 kernel with
+    128 x 64 or 128 x 32 tiles produce the same bits, so the first call times the three (CUDA
+    events; skipped during stream capture, where the tile-padding estimate decides) and the
+    plan keeps the fastest."""
     if not OZAKI_AUTOTUNE[0] or torch.cuda.is_current_stream_capturing():
         return plan.prefer_tc
     times = {}
-    for tc in (False, True, False, True):
+    for tc in (False, 64, 32, False, 64, 32):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda._sleep(2_000_000)  # hold the stream while the host enqueues: time the GPU, not the host
         e0.record()
@@ -350,7 +352,7 @@ def _autotune_ozaki(plan, A, B, out, slices):
         e1.record()
         e1.synchronize()
         times[tc] = e0.elapsed_time(e1)  # the second (warm) measurement of each kernel is kept
-    return times[True] < times[False]
+    return min(times, key=times.get)
 
 
 def _ozaki_run(plan, A, B, out, slices, tc):
@@ -360,12 +362,15 @@ def _ozaki_run(plan, A, B, out, slices, tc):
     only the other operand is split (or neither)."""
     dev = A.device
     st = _stream()
-    if tc:
+    tile_n = 0 if not tc else (32 if tc == 32 else 64)
+    if tile_n:
         # tiles grouped by CTA (one CTA per SM) with balanced work
-        tiles, offs = P.ozaki_tc_schedule(plan, _sm_count(dev))
-        key, arrs = 'ozaki_tc', (plan.split_recs_tc, plan.split_groups_tc, plan.outs_tc, tiles, offs)
-        asz, bsz = plan.a_size_tc, plan.b_size_tc
-        by_op = plan.split_groups_tc_ab
+        sfx = '_tc' if tile_n == 64 else '_tc32'
+        tiles, offs = P.ozaki_tc_schedule(plan, _sm_count(dev), tile_n)
+        key, arrs = 'ozaki' + sfx, (getattr(plan, 'split_recs' + sfx), getattr(plan, 'split_groups' + sfx),
+                                    getattr(plan, 'outs' + sfx), tiles, offs)
+        asz, bsz = getattr(plan, 'a_size' + sfx), getattr(plan, 'b_size' + sfx)
+        by_op = getattr(plan, 'split_groups' + sfx + '_ab')
     else:
         key, arrs = 'ozaki', (plan.split_recs, plan.split_groups, plan.outs, plan.tiles)
         asz, bsz = plan.a_size, plan.b_size
@@ -373,8 +378,8 @@ def _ozaki_run(plan, A, B, out, slices, tc):
     # the per-operand group lists travel with the plan's arrays (no upload during a capture)
     darr = _dev(plan, key, arrs + tuple(by_op), dev)
     drec, dgrp, dout, dtl = darr[:4]
-    held_a = _held('split', (id(plan), 0, bool(tc), slices), A)
-    held_b = _held('split', (id(plan), 1, bool(tc), slices), B)
+    held_a = _held('split', (id(plan), 0, tile_n, slices), A)
+    held_b = _held('split', (id(plan), 1, tile_n, slices), B)
     hit_a, hit_b = _hit(held_a, A), _hit(held_b, B)
     a_sl, a_ex = hit_a if hit_a else (torch.empty(max(asz, 1), dtype=torch.bfloat16, device=dev),
                                       torch.empty(max(plan.a_exps, 1), dtype=torch.int32, device=dev))
@@ -394,9 +399,9 @@ def _ozaki_run(plan, A, B, out, slices, tc):
         _store(held_a, A, (a_sl, a_ex))
     if held_b is not None and not hit_b:
         _store(held_b, B, (b_sl, b_ex))
-    if tc:
+    if tile_n:
         N.call('yb_ozaki_gemm_tc', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
-               len(arrs[3]), _ptr(darr[4]), len(arrs[4]) - 1, slices, st)
+               len(arrs[3]), _ptr(darr[4]), len(arrs[4]) - 1, tile_n, slices, st)
     else:
         N.call('yb_ozaki_gemm', _ptr(a_sl), _ptr(a_ex), _ptr(b_sl), _ptr(b_ex), _ptr(out), _ptr(dout), _ptr(dtl),
                len(arrs[3]), slices, st)
