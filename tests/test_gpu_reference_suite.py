@@ -42,15 +42,16 @@ def _expected(name):
     return name in EXPECTED_FAILURES or (f + '::*') in EXPECTED_FAILURES
 
 
-def test_reference_suites_on_this_backend(cuda_device, tmp_path):
-    if not os.path.isdir(SUITE):
-        pytest.skip("the reference's test suite is not installed (python baseline/install_reference.py <tree>)")
+def _run_suite(files, tmp_path, extra=(), env_extra=None):
+    """Run YASTN's test files on this backend; returns the junit XML path."""
     xml = tmp_path / 'suite.xml'
     env = dict(os.environ)
     env['PYTHONPATH'] = os.pathsep.join([os.path.join(ROOT, 'tests'), os.path.join(ROOT, 'baseline', '_ref'), ROOT,
                                          env.get('PYTHONPATH', '')])
-    cmd = [sys.executable, '-m', 'pytest'] + FILES + ['-p', 'yastn_suite_plugin', '--backend', 'torch_gb300',
-           '--device', 'cuda', '-q', '-p', 'no:cacheprovider', '--junitxml', str(xml), '-n', '8', '--timeout', '300']
+    env.update(env_extra or {})
+    cmd = [sys.executable, '-m', 'pytest'] + list(files) + ['-p', 'yastn_suite_plugin', '--backend', 'torch_gb300',
+           '--device', 'cuda', '-q', '-p', 'no:cacheprovider', '--junitxml', str(xml)] + list(extra) + \
+          ['-n', '8', '--timeout', '300']
     try:
         import xdist  # noqa: F401
         import pytest_timeout  # noqa: F401
@@ -58,6 +59,54 @@ def test_reference_suites_on_this_backend(cuda_device, tmp_path):
         cmd = cmd[:-4]
     proc = subprocess.run(cmd, cwd=SUITE, env=env, capture_output=True, text=True, timeout=1500)
     assert xml.exists(), proc.stdout[-3000:] + proc.stderr[-3000:]
+    return xml
+
+
+def _outcomes(xml):
+    """{test name: passed?} of a junit XML (skipped tests left out)."""
+    out = {}
+    for tc in ET.parse(xml).iter('testcase'):
+        if tc.find('skipped') is not None:
+            continue
+        name = tc.get('classname').split('.')[-1] + '.py::' + tc.get('name')
+        out[name] = tc.find('failure') is None and tc.find('error') is None
+    return out
+
+
+# the network suites whose environments contract double-layer PEPS tensors (append_vec_*):
+# CTMRG on square and C4v lattices, their measurements (fermionic ones included), the
+# double-layer tensor itself and the fixed-point CTMRG
+PEPS_FILES = ['peps/test_ctmrg.py', 'peps/test_ctmrg_c4v.py', 'peps/test_double_peps_tensor.py', 'peps/test_fp_c4v.py',
+              'peps/test_ctmrg_measure.py', 'peps/test_fermionic_measure.py']
+
+
+def test_reference_peps_suites_with_fused_double_layer(cuda_device, tmp_path):
+    """YASTN's PEPS suites with the double-layer contractions run as this backend's compiled
+    programs (yastn_gb300.double_layer.install()): every test that passes with YASTN's own
+    composition on this backend passes with the compiled programs, and the programs ran
+    (compiled and reused)."""
+    if not os.path.isdir(SUITE):
+        pytest.skip("the reference's test suite is not installed (python baseline/install_reference.py <tree>)")
+    (tmp_path / 'plain').mkdir()
+    (tmp_path / 'fused').mkdir()
+    (tmp_path / 'stats').mkdir()
+    plain = _outcomes(_run_suite(PEPS_FILES, tmp_path / 'plain'))
+    fused = _outcomes(_run_suite(PEPS_FILES, tmp_path / 'fused', ['--gb300-double-layer'],
+                                 {'YB_DOUBLE_LAYER_STATS': str(tmp_path / 'stats')}))
+    assert sum(plain.values()) >= 20, plain
+    lost = sorted(n for n, ok in plain.items() if ok and not fused.get(n, False))
+    assert not lost, lost
+    import json
+    stats = [json.load(open(tmp_path / 'stats' / f)) for f in os.listdir(tmp_path / 'stats')]
+    assert stats and sum(s['compiled'] for s in stats) > 0 and sum(s['hits'] for s in stats) > 0, stats
+    print(f"PEPS suites: {sum(plain.values())} pass with YASTN's composition, {sum(fused.values())} with the "
+          f"compiled double-layer programs; programs {[s for s in stats]}")
+
+
+def test_reference_suites_on_this_backend(cuda_device, tmp_path):
+    if not os.path.isdir(SUITE):
+        pytest.skip("the reference's test suite is not installed (python baseline/install_reference.py <tree>)")
+    xml = _run_suite(FILES, tmp_path)
     passed, failed, unexpected = 0, [], []
     for tc in ET.parse(xml).iter('testcase'):
         name = tc.get('classname').split('.')[-1] + '.py::' + tc.get('name')

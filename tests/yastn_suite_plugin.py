@@ -10,6 +10,9 @@ for ``--backend torch_gb300`` the session makes the name 'torch' resolve to this
 'torch'. Every test that asks for YASTN's torch backend then runs on this one; tests guarded
 by ``'torch' not in config.getoption('--backend')`` run too.
 
+With ``--gb300-double-layer`` the PEPS double-layer contractions (``append_vec_*``) run as
+``yastn_gb300.double_layer``'s compiled programs (``double_layer.install()``).
+
 Use: ``python -m pytest <YASTN tests/tensor files> -p yastn_suite_plugin --backend
 torch_gb300 --device cuda`` with this directory, the package root and the reference install
 (baseline/_ref) on PYTHONPATH.
@@ -27,6 +30,8 @@ def pytest_addoption(parser):
     parser.addoption("--quickstart", action="store_true", dest="quickstart", default=False)
     parser.addoption("--long_tests", action="store_true", default=False)
     parser.addoption("--ray", action="store_true", default=False)
+    parser.addoption("--gb300-double-layer", action="store_true", default=False,
+                     help="run the PEPS double-layer contractions as yastn_gb300's compiled programs")
 
 
 def pytest_configure(config):
@@ -36,6 +41,23 @@ def pytest_configure(config):
         import yastn_gb300
         sys.modules["yastn.backend.backend_torch"] = yastn_gb300.backend
         yastn.backend.backend_torch = yastn_gb300.backend
+    if config.getoption("--gb300-double-layer"):
+        from yastn_gb300 import double_layer
+        double_layer.install()
+
+
+def pytest_unconfigure(config):
+    """With --gb300-double-layer: the compiled programs' counts of this process go to
+    $YB_DOUBLE_LAYER_STATS/<worker>.json (the test that runs the suite sums them)."""
+    import os
+    out = os.environ.get("YB_DOUBLE_LAYER_STATS")
+    if not out or not config.getoption("--gb300-double-layer"):
+        return
+    import json
+    from yastn_gb300 import double_layer
+    worker = os.environ.get("PYTEST_XDIST_WORKER", "main")
+    with open(os.path.join(out, worker + ".json"), "w") as f:
+        json.dump(double_layer.cache_info(), f)
 
 
 @pytest.fixture

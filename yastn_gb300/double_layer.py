@@ -52,7 +52,8 @@ _GEMMS = frozenset(('dot', 'transpose_dot_sum'))
 _INSPECT = frozenset(('get_dtype', 'get_yastn_dtype', 'is_complex', 'get_device', 'get_shape', 'get_size',
                       'requires_grad', 'cuda_is_available'))
 _MAX_SOURCE = 2 ** 31 - 2
-_CACHE_SIZE = 64
+_CACHE_SIZE = 256            # programs kept (least recently used dropped first) ...
+_CACHE_BYTES = 8 << 30       # ... and at most this much device memory in their gather maps
 
 
 class Unfusable(Exception):
@@ -164,6 +165,11 @@ class DoubleLayerProgram:
                     maps[sink] = _compose(backend, device, self.sizes[root], chain)
             self._maps[key] = maps
         return maps
+
+    def map_bytes(self):
+        """Device bytes held by the gather maps (and inverses) of every device."""
+        return sum(m[0].numel() * 4 + m[1].numel() * 4 for maps in self._maps.values()
+                   for m in maps.values() if m is not None)
 
     def run(self, datas, backend, gather=_native_gather):
         """Execute on the inputs' data (in the recorded order); returns the output's data."""
@@ -281,7 +287,7 @@ def compile_program(fn, tensors, kwargs):
 # ----------------------------------------------------------------------------- drop-ins
 
 _PROGRAMS = OrderedDict()
-_STATS = {'hits': 0, 'compiled': 0, 'unfused': 0}
+_STATS = {'hits': 0, 'compiled': 0, 'unfused': 0, 'bytes': 0}
 _ORIGINAL = {}
 _SUPPORTED = (torch.float64, torch.complex128)
 
@@ -335,8 +341,10 @@ def _run(name, Ac, A, vec, op, mode, in_b, out_a):
         except Unfusable:
             prog = None
         _PROGRAMS[key] = prog
-        while len(_PROGRAMS) > _CACHE_SIZE:
-            _PROGRAMS.popitem(last=False)
+        _STATS['bytes'] = _STATS.get('bytes', 0) + (prog.map_bytes() if prog is not None else 0)
+        while len(_PROGRAMS) > 1 and (len(_PROGRAMS) > _CACHE_SIZE or _STATS['bytes'] > _CACHE_BYTES):
+            _, old = _PROGRAMS.popitem(last=False)
+            _STATS['bytes'] -= old.map_bytes() if old is not None else 0
     else:
         _PROGRAMS.move_to_end(key)
         _STATS['hits'] += 1
