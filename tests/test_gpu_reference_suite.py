@@ -90,9 +90,12 @@ def test_reference_peps_suites_with_fused_double_layer(cuda_device, tmp_path):
     (tmp_path / 'plain').mkdir()
     (tmp_path / 'fused').mkdir()
     (tmp_path / 'stats').mkdir()
-    plain = _outcomes(_run_suite(PEPS_FILES, tmp_path / 'plain'))
-    fused = _outcomes(_run_suite(PEPS_FILES, tmp_path / 'fused', ['--gb300-double-layer'],
-                                 {'YB_DOUBLE_LAYER_STATS': str(tmp_path / 'stats')}))
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(2) as pool:  # the two runs side by side
+        jp = pool.submit(_run_suite, PEPS_FILES, tmp_path / 'plain')
+        jf = pool.submit(_run_suite, PEPS_FILES, tmp_path / 'fused', ['--gb300-double-layer'],
+                         {'YB_DOUBLE_LAYER_STATS': str(tmp_path / 'stats')})
+        plain, fused = _outcomes(jp.result()), _outcomes(jf.result())
     assert sum(plain.values()) >= 20, plain
     lost = sorted(n for n, ok in plain.items() if ok and not fused.get(n, False))
     assert not lost, lost

@@ -939,3 +939,50 @@ def test_fix_signs_plan_takes_truncated_and_partial_svd_records():
     assert [int(r1[i]) for i in (1, 2, 3, 4, 5, 9)] == [4, 5, 6, 2, 8, 3]
     with pytest.raises(P.PlanError):
         P.fix_signs_plan((((0, 12), (3, 4), (0, 6), (3, 2), (0, 3), (0, 8), (2, 4)),))
+
+
+def test_plan_cache_save_and_load(tmp_path):
+    """Plans written by save_cache and read back by load_cache (without their device state)
+    are found by value: rebuilding them from the same metadata is a cache hit, no build, and
+    every packed array is equal to the original's."""
+    from yastn_gb300.workloads import Heff2Workload
+    w = Heff2Workload()
+    P.CACHE.by_id.clear(); P.CACHE.by_val.clear()
+    built = []
+    for fn, keys, args, okey in w.steps:
+        if fn == 'dot':
+            built.append(('dot', args[2], P.dot_plan(args[2])))
+            built.append(('ozaki', args[2], P.ozaki_dot_plan(args[2], 8)))
+        else:
+            plan = P.merge_plan(*args[1:])
+            plan.packed(True)
+            plan._dev['x'] = (object(),)  # stands in for device copies, which are not written
+            built.append(('merge', args[1:], plan))
+    P.ozaki_tc_schedule(built[1][2], 152)
+    path = tmp_path / 'plans.pkl'
+    n = P.save_cache(str(path))
+    assert n == len(P.CACHE.by_val) >= len(built) - 3
+    P.CACHE.by_id.clear(); P.CACHE.by_val.clear()
+    assert P.load_cache(str(path)) == n
+    misses = P.CACHE.misses
+    for kind, key, old in built:
+        new = {'dot': lambda: P.dot_plan(key), 'ozaki': lambda: P.ozaki_dot_plan(key, 8),
+               'merge': lambda: P.merge_plan(*key)}[kind]()
+        assert new is not old and new._dev == {}
+        if kind == 'merge':
+            for v in (True, False):
+                for a, b in zip(new.packed(v), old.packed(v)):
+                    assert np.array_equal(a, b)
+        elif kind == 'dot':
+            assert np.array_equal(new.tiles, old.tiles) and np.array_equal(new.outs, old.outs)
+        else:
+            assert np.array_equal(new.split_recs_tc, old.split_recs_tc) and new.prefer_tc == old.prefer_tc
+            assert np.array_equal(new.native.tiles, old.native.tiles)
+            assert not hasattr(new, 'tuned_tc')
+    assert P.CACHE.misses == misses  # every plan came from the file
+    bad = tmp_path / 'bad.pkl'
+    import pickle
+    bad.write_bytes(pickle.dumps({'version': 0, 'entries': []}))
+    with pytest.raises(P.PlanError):
+        P.load_cache(str(bad))
+    P.CACHE.by_id.clear(); P.CACHE.by_val.clear()

@@ -7,6 +7,7 @@ Plans depend only on the metadata, so they are cached by the identity of the tup
 (YASTN memoises its metadata with ``lru_cache``, so the same tuple object comes back)
 and, failing that, by value.
 """
+import pickle
 from collections import OrderedDict
 
 import numpy as np
@@ -69,6 +70,76 @@ CACHE = PlanCache()
 
 def cache_info():
     return {'hits': CACHE.hits, 'misses': CACHE.misses, 'size': len(CACHE.by_id)}
+
+
+# ----------------------------------------------------------------------------- serialization
+
+PLAN_FILE_VERSION = 1
+_DEVICE_ONLY = ('_dev', 'tuned_tc')  # per-process state: device copies, autotuned kernel choices
+
+
+class _PlanPickler(pickle.Pickler):
+    """Pickles plans without their device state (torch tensors are written as None)."""
+
+    def reducer_override(self, obj):
+        import torch
+        if isinstance(obj, torch.Tensor):
+            return type(None), ()
+        return NotImplemented
+
+
+def _reset_device_state(obj, seen):
+    """Drop the per-process state of every plan reachable from obj (after unpickling)."""
+    if id(obj) in seen:
+        return
+    seen.add(id(obj))
+    if isinstance(obj, (list, tuple)):
+        for x in obj:
+            _reset_device_state(x, seen)
+        return
+    if isinstance(obj, dict):
+        for x in obj.values():
+            _reset_device_state(x, seen)
+        return
+    d = getattr(obj, '__dict__', None)
+    if d is None or type(obj).__module__ != __name__:
+        return
+    for k in _DEVICE_ONLY:
+        if k == '_dev':
+            if k in d:
+                d[k] = {}
+        else:
+            d.pop(k, None)
+    for v in list(d.values()):
+        _reset_device_state(v, seen)
+
+
+def save_cache(path):
+    """Write every plan of the cache (keyed by its metadata by value) to ``path``, without
+    device state, so that a later process (``load_cache``) skips building them: a long CTMRG
+    or DMRG run restarts with the plans of its metadata ready. The file is a pickle: load only
+    files this library wrote."""
+    entries = [(k, v) for k, v in CACHE.by_val.items()]
+    with open(path, 'wb') as f:
+        _PlanPickler(f, protocol=pickle.HIGHEST_PROTOCOL).dump({'version': PLAN_FILE_VERSION, 'entries': entries})
+    return len(entries)
+
+
+def load_cache(path):
+    """Add the plans saved by ``save_cache`` to the cache (by value: the first lookup of a
+    metadata tuple finds its plan without building it). Returns the number of plans loaded."""
+    with open(path, 'rb') as f:
+        payload = pickle.load(f)
+    if payload.get('version') != PLAN_FILE_VERSION:
+        raise PlanError(f"plan file version {payload.get('version')} (this library reads {PLAN_FILE_VERSION})")
+    n = 0
+    for key, plan in payload['entries']:
+        _reset_device_state(plan, set())
+        CACHE.by_val[key] = plan
+        n += 1
+    while len(CACHE.by_val) > CACHE.maxsize:
+        CACHE.by_val.popitem(last=False)
+    return n
 
 
 # ----------------------------------------------------------------------------- helpers

@@ -108,11 +108,16 @@ class _Recorder:
 # ----------------------------------------------------------------------------- programs
 
 class _Gather(torch.autograd.Function):
-    """A composed copy (``yb_map_gather``); its adjoint is the gather by the inverse map."""
+    """A composed copy (``yb_map_gather``); its adjoint is the gather by the inverse map.
+
+    Under torch.func transforms (YASTN's fixed-point CTMRG differentiates its CTM step with
+    torch.func.vjp) the maps reach setup_context as wrapped tensors, which have no storage
+    pointer for the kernel: they are unwrapped before use, as the cotangent is."""
 
     @staticmethod
     def forward(src, gmap, inv, conj):
-        return ops.map_gather(src, gmap, conj)
+        unwrap = backend_gb300._unwrap
+        return ops.map_gather(unwrap(src), unwrap(gmap), conj)
 
     @staticmethod
     def setup_context(ctx, inputs, output):
@@ -121,8 +126,8 @@ class _Gather(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, g):
-        g = backend_gb300._unwrap(g)
-        return ops.map_gather(g.contiguous(), ctx.inv, ctx.conj), None, None, None
+        unwrap = backend_gb300._unwrap
+        return ops.map_gather(unwrap(g).contiguous(), unwrap(ctx.inv), ctx.conj), None, None, None
 
 
 def _native_gather(src, gmap, inv, conj):
