@@ -53,7 +53,7 @@ _INSPECT = frozenset(('get_dtype', 'get_yastn_dtype', 'is_complex', 'get_device'
                       'requires_grad', 'cuda_is_available'))
 _MAX_SOURCE = 2 ** 31 - 2
 _CACHE_SIZE = 256            # programs kept (least recently used dropped first) ...
-_CACHE_BYTES = 8 << 30       # ... and at most this much device memory in their gather maps
+_CACHE_BYTES = 32 << 30      # ... and at most this much device memory in their gather maps
 
 
 class Unfusable(Exception):
@@ -343,7 +343,7 @@ def _run(name, Ac, A, vec, op, mode, in_b, out_a):
             prog = compile_program(ref, tensors, kwargs)
             prog.maps(backend_gb300, A._data.device)
             _STATS['compiled'] += 1
-        except Unfusable:
+        except Exception:  # noqa: BLE001 -- Unfusable, or YASTN's own error, which its function raises again
             prog = None
         _PROGRAMS[key] = prog
         _STATS['bytes'] = _STATS.get('bytes', 0) + (prog.map_bytes() if prog is not None else 0)
