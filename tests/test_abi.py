@@ -54,6 +54,15 @@ def test_invalid_arguments_are_rejected_on_host(lib):
     assert lib.yb_truncation_mask(null, 20000, null, null, 1, 0.0, -1, 0, null, null, null) == N.YB_ERR_TOO_LARGE
     assert lib.yb_fix_signs(null, null, null, null, null, null, 1, 4, 0, 0, null) == N.YB_ERR_INVALID
     assert lib.yb_mask_gather(null, null, 8, null, null, 2, null, 0, null) == N.YB_ERR_INVALID
+    # composed copies: null pointers, an unknown dtype, a misaligned complex128 pointer
+    fake = ctypes.c_void_p(0x100000)
+    assert lib.yb_map_gather(null, null, N.YB_F64, null, 5, 0, null) == N.YB_ERR_INVALID
+    assert lib.yb_map_gather(fake, fake, 7, fake, 5, 0, null) == N.YB_ERR_INVALID
+    assert lib.yb_map_gather(ctypes.c_void_p(0x100008), fake, N.YB_C128, fake, 5, 1, null) == N.YB_ERR_INVALID
+    assert lib.yb_map_gather(null, null, N.YB_F64, null, 0, 0, null) == N.YB_OK  # nothing to do
+    # the tcgen05 emulated GEMM takes 128 x 64 or 128 x 32 tiles only
+    assert lib.yb_ozaki_gemm_tc(fake, fake, fake, fake, fake, fake, fake, 1, null, 0, 48, 8, null) == N.YB_ERR_INVALID
+    assert lib.yb_ozaki_gemm_tc(null, null, null, null, null, null, null, 1, null, 0, 32, 8, null) == N.YB_ERR_INVALID
 
 
 def test_backend_module_surface():
