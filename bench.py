@@ -1025,6 +1025,8 @@ def plain_and_ctmrg_extras(args, torch, dev, wl, w, env, h_v0, flush, t_fused_cf
             "composed_copy_frac_of_hbm": d["roofline"]["frac"]}
     except ImportError as e:
         out["double_layer_chi144"] = {"unavailable": f"the reference package is not installed ({e})"}
+    except Exception as e:  # noqa: BLE001 -- a side measurement: the headline line is printed regardless
+        out["double_layer_chi144"] = {"failed": f"{type(e).__name__}: {e}"[:300]}
     out["ctmrg_chi24_fwd_bwd"] = {
         "ms_per_step": t_fast, "energy_rel_err_vs_reference": ef, "grad_rel_err_vs_reference": gf,
         "plain_per_block_gpu_ms": t_plain4, "plain_energy_rel_err": ep, "plain_grad_rel_err": gp,
@@ -1380,8 +1382,121 @@ def run_svd144(args):
     print(json.dumps(line))
 
 
+DLAYER_METRIC = "double-layer contraction TFLOP/s (append_vec_tl, Z2 D=6 chi=144, FP64)"
+DLAYER_WORKLOAD = "append_vec_tl mode b-self, vector x [l l'] [t t'] y, chi=144, D=6, d=2, Z2"
+DLAYER_KW = dict(mode='b-self', in_b=(2, 1), out_a=(3, 2))
+
+
+def _yastn_ref():
+    ref = os.path.join(ROOT, 'baseline', '_ref')
+    if ref not in sys.path:
+        sys.path.insert(0, ref)
+    import yastn
+    return yastn
+
+
+def dlayer_inputs(chi=144):
+    """The site tensor (bra = ket) and the boundary vector x [l l'] [t t'] y of the chi=144
+    CTMRG corner step, as YASTN tensors on its NumPy backend (seeded normal draws)."""
+    yastn = _yastn_ref()
+    import yastn.tn.fpeps as fpeps
+    cfn = yastn.make_config(sym='Z2', backend='np', default_dtype='float64')
+    cfn.backend.random_seed(0)
+    vl = yastn.Leg(cfn, s=1, t=(0, 1), D=(3, 3))
+    pl = yastn.Leg(cfn, s=1, t=(0, 1), D=(1, 1))
+    el = yastn.Leg(cfn, s=1, t=(0, 1), D=(chi // 2, chi // 2))
+    ket = yastn.rand(cfn, legs=[vl.conj(), vl, vl, vl.conj(), pl])
+    la, lb = fpeps.DoublePepsTensor(bra=ket, ket=ket).get_legs((1, 0))
+    vec = yastn.rand(cfn, legs=[el, la.conj(), lb.conj(), el.conj()])
+    return ket, ket, vec
+
+
+def dlayer_flops(bra, ket, vec):
+    """FP64 FLOP of the sector GEMMs of one append_vec_tl call (2 m n k per sector), counted
+    by running YASTN's function once with its NumPy backend's dot observed."""
+    import yastn.backend.backend_np as bnp
+    import yastn.tn.fpeps.envs._env_contractions as ec
+    count = [0]
+    dot = bnp.dot
+
+    def counting_dot(A, B, meta_dot, Dsize):
+        count[0] += sum(2 * Da[0] * Da[1] * Db[1] for _, _, _, Da, _, Db in meta_dot)
+        return dot(A, B, meta_dot, Dsize)
+    bnp.dot = counting_dot
+    try:
+        ec.append_vec_tl(bra, ket, vec, **DLAYER_KW)
+    finally:
+        bnp.dot = dot
+    return count[0]
+
+
+def run_reference_dlayer(args):
+    """Reference arm of the double-layer workload: YASTN's own append_vec_tl on its NumPy
+    backend (the reference's CPU path) on all host cores, each step one call."""
+    _yastn_ref()
+    import yastn.tn.fpeps.envs._env_contractions as ec
+    bra, ket, vec = dlayer_inputs()
+    flops = dlayer_flops(bra, ket, vec)
+    for _ in range(args.warmup):
+        ec.append_vec_tl(bra, ket, vec, **DLAYER_KW)
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        ec.append_vec_tl(bra, ket, vec, **DLAYER_KW)
+        ts.append(time.perf_counter() - t0)
+    t = float(np.mean(ts))
+    value = flops / t / 1e12
+    line = {"impl": "reference", "metric": DLAYER_METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded yastn normal draws)",
+            "config": {"workload": DLAYER_WORKLOAD, "gemm_flop_per_call": flops},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_cores(), "kind": "reference",
+                             "sample": f"{args.steps} calls of YASTN's append_vec_tl on its NumPy backend"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def dlayer_e2e(reps):
+    """One call through the public API with host data: the three tensors' data copied from
+    pinned host memory to the device, the compiled contraction, the result read back; mean
+    seconds per call and the bytes copied each way."""
+    import torch
+    yastn = _yastn_ref()
+    from yastn_gb300 import backend as BK
+    from yastn_gb300 import double_layer as dl
+    bra, ket, vec = dlayer_inputs()
+    cfg = yastn.make_config(sym='Z2', backend=BK, default_dtype='float64', default_device='cuda')
+    host = [torch.from_numpy(np.ascontiguousarray(t._data)).pin_memory() for t in (bra, ket, vec)]
+    saved_mode = BK.get_gemm_mode()
+    BK.set_gemm_mode('fp64')
+    try:
+        def step():
+            ts = [t._replace(config=cfg, data=h.to('cuda', non_blocking=True)) for t, h in zip((bra, ket, vec), host)]
+            return dl.append_vec_tl(*ts, **DLAYER_KW)._data.to('cpu')
+        out = step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            out = step()
+        torch.cuda.synchronize()
+        t = (time.perf_counter() - t0) / reps
+    finally:
+        BK.set_gemm_mode(saved_mode)
+    return t, int(sum(h.numel() * h.element_size() for h in host)), int(out.numel() * out.element_size())
+
+
 def run_dlayer(args):
-    print(json.dumps(dlayer_line(args)))
+    line = dlayer_line(args)
+    flops = line['config']['gemm_flop_per_call']
+    t_e2e, bi, bo = dlayer_e2e(max(3, args.steps))
+    line['e2e'] = {"value": flops / t_e2e / 1e12, "unit": UNIT, "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo}
+    # the reference's CPU path on the host cores: YASTN's own function on its NumPy backend
+    import yastn.tn.fpeps.envs._env_contractions as ec
+    bra, ket, vec = dlayer_inputs()
+    t_cpu, reps = time_cpu(lambda: ec.append_vec_tl(bra, ket, vec, **DLAYER_KW), budget_s=10.0, min_reps=2)
+    line['cpu_baseline'] = {"value": flops / t_cpu / 1e12, "unit": UNIT, "cores": cpu_cores(), "kind": "reference",
+                            "sample": f"{reps} calls of YASTN's append_vec_tl on its NumPy backend (median)"}
+    print(json.dumps(line))
 
 
 def dlayer_line(args):
@@ -1512,8 +1627,8 @@ def main():
     args = parse()
     if args.workload == 'dlayer':
         if args.impl == 'reference':
-            print(json.dumps({"impl": "reference", "unavailable": "dlayer times the reference's torch backend "
-                                                                  "on the GPU inside the GPU arm"}))
+            if int(os.environ.get('RANK', '0')) == 0:
+                run_reference_dlayer(args)
         else:
             run_dlayer(args)
         return

@@ -1,8 +1,9 @@
 """The benchmark's reference arm on the host cores (no GPU): one JSON line with the keys of
 the benchmark contract, for the default workload (DMRG Heff2 Lanczos: the reference package
 itself when it is installed under baseline/_ref, else the oracle's restatement), the
-tensordot workload and the CTMRG workload (its per-move checkpointed replay on the plain
-per-block torch path)."""
+tensordot workload, the CTMRG workload (its per-move checkpointed replay on the plain
+per-block torch path) and the double-layer contraction (YASTN's own append_vec_tl on its
+NumPy backend)."""
 import json
 import os
 import subprocess
@@ -29,6 +30,7 @@ def _run(*args):
     ('--steps', '1', '--warmup', '0'),
     ('--workload', 'cfg1', '--steps', '1', '--warmup', '0'),
     ('--workload', 'cfg4', '--steps', '1', '--warmup', '0'),
+    ('--workload', 'dlayer', '--steps', '1', '--warmup', '0'),
 ])
 def test_reference_arm_line(args):
     line = _run(*args)
@@ -42,3 +44,8 @@ def test_reference_arm_line(args):
     if '--workload' in args and args[args.index('--workload') + 1] == 'cfg4':
         assert line["unit"] == "ms" and line["higher_is_better"] is False
         assert line["config"]["energy_rel_err_vs_reference"] <= 1e-12
+    if '--workload' in args and args[args.index('--workload') + 1] == 'dlayer':
+        # YASTN's own append_vec_tl on its NumPy backend; its sector GEMMs count the FLOP the
+        # GPU arm counts from its compiled program (the chi=144 corner step: 1.935 GFLOP)
+        assert line["cpu_baseline"]["kind"] == "reference"
+        assert line["config"]["gemm_flop_per_call"] == 1934917632
