@@ -185,3 +185,15 @@ def test_install_rebinds_and_delegates_for_other_backends():
     finally:
         dl.uninstall()
     assert ec.append_vec_tl is original and dpt_mod.append_vec_tl is original
+
+
+def test_program_of_a_vector_without_blocks():
+    """A boundary vector whose charges meet none of the site's (no blocks): the program's
+    output has YASTN's structure (no blocks) and no data."""
+    cfg, ket, bra, el, pl = _site('U1', False, 'float64', seed=2)
+    la, lb = fpeps.DoublePepsTensor(bra=bra, ket=ket).get_legs((1, 0))
+    far = yastn.Leg(cfg, s=1, t=(5,), D=(2,))
+    vec = yastn.zeros(cfg, legs=[far, la.conj(), lb.conj(), far.conj()], n=7)
+    assert vec.size == 0
+    ref, out, prog = _run_both('append_vec_tl', bra, ket, vec, None, 'old', (2, 1), (2, 3))
+    assert out.struct == ref.struct and out.size == 0 and torch.equal(out._data, ref._data)

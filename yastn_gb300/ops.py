@@ -106,6 +106,8 @@ def map_gather(src, gmap, conj=False):
     src = _check(src, 'src')
     if gmap.dtype != torch.int32 or not gmap.is_cuda or gmap.dim() != 1 or not gmap.is_contiguous():
         raise TypeError("gmap must be a contiguous 1-D int32 CUDA tensor")
+    if src.numel() == 0:  # nothing to gather: every entry of a valid map is 0 (zero fill)
+        return torch.zeros(gmap.numel(), dtype=src.dtype, device=src.device)
     out = torch.empty(gmap.numel(), dtype=src.dtype, device=src.device)
     if out.numel():
         N.call('yb_map_gather', _ptr(src), _ptr(out), _dtype_code(src.dtype), _ptr(gmap), gmap.numel(),
