@@ -876,6 +876,8 @@ def run_gpu_cfg2(args, wl):
     extras = {}
     if not args.no_extras:
         extras = plain_and_ctmrg_extras(args, torch, dev, wl, w, env, h_v0, flush, results[args.gemm]['t'])
+        if world == 1:
+            extras["other_configs"] = other_config_lines()
     head = results[args.gemm]
     t_max, t_e2e = head['t'], head['te']
     if world > 1:
@@ -920,6 +922,39 @@ def run_gpu_cfg2(args, wl):
     print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
+
+
+_CHILD_ENV_DROP = ('RANK', 'WORLD_SIZE', 'LOCAL_RANK', 'LOCAL_WORLD_SIZE', 'GROUP_RANK', 'ROLE_RANK', 'MASTER_ADDR',
+                   'MASTER_PORT', 'TORCHELASTIC_RUN_ID', 'GROUP_WORLD_SIZE', 'ROLE_WORLD_SIZE')
+
+
+def other_config_lines(workloads=('cfg1', 'cfg3', 'cfg5'), extra_args=(), timeout=300):
+    """The tensordot workloads of the other configurations (U(1) D=64, U(1)xU(1) complex128,
+    the precision study), each run by this script in a child process (5 timed steps after 3
+    warm-up steps, the truncated SVD left out) and summarised for the headline line: value,
+    e2e, the emulated GEMM's roofline fraction, errors, the CPU baseline. A child that fails
+    is recorded as such."""
+    out = {}
+    env = {k: v for k, v in os.environ.items() if k not in _CHILD_ENV_DROP}
+    for name in workloads:
+        cmd = [sys.executable, os.path.join(ROOT, 'bench.py'), '--workload', name, '--steps', '5', '--warmup', '3',
+               '--no-svd'] + list(extra_args)
+        try:
+            res = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout, env=env, cwd=ROOT)
+            lines = [ln for ln in res.stdout.splitlines() if ln.startswith('{')]
+            if res.returncode != 0 or not lines:
+                out[name] = {"failed": f"exit {res.returncode}: {res.stderr[-300:]}"}
+                continue
+            d = json.loads(lines[-1])
+            roof = d.get('roofline') or {}
+            out[name] = {"metric": d.get('metric'), "value": d.get('value'), "unit": d.get('unit'),
+                         "ms_per_step": d.get('ms_per_step'), "dtype": d.get('dtype'),
+                         "e2e": (d.get('e2e') or {}).get('value'), "roofline_kernel": roof.get('kernel'),
+                         "roofline_frac": roof.get('frac'), "cpu_baseline": (d.get('cpu_baseline') or {}).get('value'),
+                         "config": d.get('config'), "extra": d.get('extra')}
+        except Exception as e:  # noqa: BLE001 -- a side measurement
+            out[name] = {"failed": f"{type(e).__name__}: {e}"[:300]}
+    return out
 
 
 def emulated_dot_errors(torch, BK, mv, v0):

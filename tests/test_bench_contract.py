@@ -49,3 +49,18 @@ def test_reference_arm_line(args):
         # GPU arm counts from its compiled program (the chi=144 corner step: 1.935 GFLOP)
         assert line["cpu_baseline"]["kind"] == "reference"
         assert line["config"]["gemm_flop_per_call"] == 1934917632
+
+
+def test_other_configuration_summaries_of_the_headline_line(monkeypatch):
+    """The headline line's summaries of the other configurations come from this script run
+    in child processes (here its reference arm, on the host): parsed into value, unit,
+    workload; a failing child is recorded, not raised."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location('bench_mod', os.path.join(ROOT, 'bench.py'))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    monkeypatch.setenv('CUDA_VISIBLE_DEVICES', '')
+    out = bench.other_config_lines(workloads=('cfg1', 'nope'), extra_args=('--impl', 'reference'))
+    assert out['cfg1']['value'] > 0 and out['cfg1']['unit'] == 'TFLOP/s'
+    assert 'D=64' in out['cfg1']['config']['workload']
+    assert 'failed' in out['nope']
