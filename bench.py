@@ -928,7 +928,7 @@ _CHILD_ENV_DROP = ('RANK', 'WORLD_SIZE', 'LOCAL_RANK', 'LOCAL_WORLD_SIZE', 'GROU
                    'MASTER_PORT', 'TORCHELASTIC_RUN_ID', 'GROUP_WORLD_SIZE', 'ROLE_WORLD_SIZE')
 
 
-def other_config_lines(workloads=('cfg1', 'cfg3', 'cfg5'), extra_args=(), timeout=300):
+def other_config_lines(workloads=('cfg1', 'cfg3', 'cfg5'), extra_args=(), timeout=150, total=360):
     """The tensordot workloads of the other configurations (U(1) D=64, U(1)xU(1) complex128,
     the precision study), each run by this script in a child process (5 timed steps after 3
     warm-up steps, the truncated SVD left out) and summarised for the headline line: value,
@@ -936,11 +936,16 @@ def other_config_lines(workloads=('cfg1', 'cfg3', 'cfg5'), extra_args=(), timeou
     is recorded as such."""
     out = {}
     env = {k: v for k, v in os.environ.items() if k not in _CHILD_ENV_DROP}
+    t_end = time.perf_counter() + total
     for name in workloads:
+        left = t_end - time.perf_counter()
+        if left <= 10:
+            out[name] = {"skipped": f"the summaries' time budget ({total} s) is spent"}
+            continue
         cmd = [sys.executable, os.path.join(ROOT, 'bench.py'), '--workload', name, '--steps', '5', '--warmup', '3',
                '--no-svd'] + list(extra_args)
         try:
-            res = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout, env=env, cwd=ROOT)
+            res = subprocess.run(cmd, capture_output=True, text=True, timeout=min(timeout, left), env=env, cwd=ROOT)
             lines = [ln for ln in res.stdout.splitlines() if ln.startswith('{')]
             if res.returncode != 0 or not lines:
                 out[name] = {"failed": f"exit {res.returncode}: {res.stderr[-300:]}"}
