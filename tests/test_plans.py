@@ -986,3 +986,39 @@ def test_plan_cache_save_and_load(tmp_path):
     with pytest.raises(P.PlanError):
         P.load_cache(str(bad))
     P.CACHE.by_id.clear(); P.CACHE.by_val.clear()
+
+
+@pytest.mark.parametrize('seed', [0, 1, 2])
+def test_random_sector_shapes_every_tile_kind(seed):
+    """Seeded random sector shapes spanning every tile kind (64 x 64, skinny, short skinny,
+    tall skinny) and the split-K path: tile coverage and values of the packed records,
+    forward and both adjoints, real and complex, against the oracle."""
+    rng = np.random.default_rng(100 + seed)
+    shapes = []
+    for _ in range(14):
+        kind = rng.integers(0, 5)
+        if kind == 0:
+            shapes.append((int(rng.integers(1, 200)), int(rng.integers(1, 200)), int(rng.integers(1, 200))))
+        elif kind == 1:  # few rows, wide
+            shapes.append((int(rng.integers(1, 17)), int(rng.integers(1, 60)), int(rng.integers(65, 5000))))
+        elif kind == 2:  # few rows, short K
+            shapes.append((int(rng.integers(1, 9)), int(rng.integers(1, 9)), int(rng.integers(1, 3000))))
+        elif kind == 3:  # few columns, tall
+            shapes.append((int(rng.integers(65, 3000)), int(rng.integers(1, 80)), int(rng.integers(1, 17))))
+        else:  # long K
+            shapes.append((int(rng.integers(1, 40)), int(rng.integers(500, 4000)), int(rng.integers(1, 40))))
+    meta, oa, ob, oc = _meta_dot(shapes)
+    plan = P.dot_plan(meta)
+    for cplx in (False, True):
+        f = lambda n: rng.normal(size=n) + (1j * rng.normal(size=n) if cplx else 0)
+        A, B, Cb = f(oa), f(ob), f(oc)
+        out = PI.run_gemm(plan, A, B, np.zeros(oc, dtype=A.dtype))
+        ref = oracle.dot(A, B, meta, oc)
+        assert np.abs(out - ref).max() <= 1e-12 * max(np.abs(ref).max(), 1.0)
+        pa, pb = P.dot_backward_plans(meta)
+        Ab = PI.run_gemm(pa, Cb, B, np.zeros(oa, dtype=A.dtype))
+        Bb = PI.run_gemm(pb, A, Cb, np.zeros(ob, dtype=A.dtype))
+        Ab_r, Bb_r = oracle.dot_backward(Cb, A, B, meta)
+        assert np.abs(Ab - Ab_r).max() <= 1e-12 * max(np.abs(Ab_r).max(), 1.0)
+        assert np.abs(Bb - Bb_r).max() <= 1e-12 * max(np.abs(Bb_r).max(), 1.0)
+    P.CACHE.by_id.clear(); P.CACHE.by_val.clear()
