@@ -1473,8 +1473,13 @@ def dlayer_flops(bra, ket, vec):
 def run_reference_dlayer(args):
     """Reference arm of the double-layer workload: YASTN's own append_vec_tl on its NumPy
     backend (the reference's CPU path) on all host cores, each step one call."""
-    _yastn_ref()
-    import yastn.tn.fpeps.envs._env_contractions as ec
+    try:
+        _yastn_ref()
+        import yastn.tn.fpeps.envs._env_contractions as ec
+    except ImportError as e:
+        print(json.dumps({"impl": "reference", "unavailable": f"the reference package is not installed under "
+                                                              f"baseline/_ref ({e})"}))
+        return
     bra, ket, vec = dlayer_inputs()
     flops = dlayer_flops(bra, ket, vec)
     for _ in range(args.warmup):

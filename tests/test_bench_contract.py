@@ -33,6 +33,8 @@ def _run(*args):
     ('--workload', 'dlayer', '--steps', '1', '--warmup', '0'),
 ])
 def test_reference_arm_line(args):
+    if 'dlayer' in args and not os.path.isdir(os.path.join(ROOT, 'baseline', '_ref', 'yastn')):
+        pytest.skip("the double-layer reference arm runs the reference package (baseline/_ref)")
     line = _run(*args)
     assert KEYS <= set(line)
     assert line["impl"] == "reference"
